@@ -1,0 +1,234 @@
+/*
+ * louvain_gb300.h — C-ABI of the GB300-native Louvain library.
+ *
+ * This is the drop-in boundary for the Louvain hot path of
+ * puzzlef/louvain-communities-openmp-dynamic (inc/louvain.hxx). The four run
+ * entry points replace the reference's four public templates; the options and
+ * result records mirror LouvainOptions and LouvainResult<K, double> field for
+ * field. Behind the ABI every step runs as hand-written sm_103a CUDA kernels
+ * on one GPU; there is no CPU fallback (a call on a machine without a usable
+ * GPU fails with LVG_ECUDA).
+ *
+ * Conventions (as in the reference):
+ *   - vertex ids are uint32 (K = uint32_t), edge weights float (TYPE float,
+ *     main.cxx:19), result weights double (LOUVAIN_WEIGHT_TYPE, inc/louvain.hxx:67);
+ *   - a graph has `span` vertex slots; a slot may be absent (`exists[u] == 0`),
+ *     as vertex 0 of the reference's SNAP graphs is (inc/snap.hxx:133);
+ *   - a batch lists both directions of each undirected update; the
+ *     delta-screening entry requires insertions sorted by source
+ *     (inc/louvain.hxx:1432-1433), and checks it.
+ *
+ * Threading: calls on distinct graph handles may run concurrently from
+ * different host threads; calls on one handle must be serialised by the
+ * caller. Every call runs on the handle's own CUDA stream.
+ *
+ * Errors: every function returns LVG_OK (0) or a negative status; the message
+ * of the last failure on the calling thread is lvg_last_error().
+ */
+#ifndef LOUVAIN_GB300_H
+#define LOUVAIN_GB300_H
+#include <stddef.h>
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. The reference has none: it returns by value, throws only
+ * std::bad_alloc and compiles its ASSERTs out (inc/_debug.hxx:215-227). */
+#define LVG_OK        0
+#define LVG_EINVAL   (-22)   /* bad argument: id >= span, unsorted DS batch, size mismatch */
+#define LVG_ENOMEM   (-12)   /* device or host allocation failed */
+#define LVG_ETIMEOUT (-62)   /* a bounded device loop hit its cap (hash table overflow guard) */
+#define LVG_ECUDA    (-1000) /* CUDA runtime error (no device, launch failure, ...) */
+
+/* Options. Mirrors LouvainOptions (inc/louvain.hxx:30-63) with the same
+ * defaults, including aggregationTolerance = 1.0 (inc/louvain.hxx:60). */
+typedef struct lvg_options {
+  int    repeat;                /* runs to average the timings over [1] */
+  double resolution;            /* modularity resolution R [1] */
+  double tolerance;             /* local-moving convergence tolerance [1e-2] */
+  double aggregationTolerance;  /* stop when communities/vertices >= this [1.0] */
+  double toleranceDrop;         /* tolerance divisor after each pass [10] */
+  int    maxIterations;         /* local-moving iterations per pass [20] */
+  int    maxPasses;             /* passes [10] */
+  /* Extension (no reference counterpart): 0 = asynchronous moves with the
+   * reference's semantics; 1 = deterministic synchronous moves (every
+   * decision reads the previous iteration's state, ties go to the lowest
+   * community id), reproducible bit for bit. */
+  int    deterministic;
+  /* Extension: colour classes per local-moving sweep (1..32; 0 = default,
+   * 8 asynchronous / 16 deterministic). Vertices are split into classes by a
+   * hash of their id and each iteration visits the classes in turn, so most
+   * neighbours see each other's moves within the iteration, as in the
+   * reference's sequential sweep. */
+  int    colors;
+} lvg_options;
+
+/* Fill *o with the reference's defaults. Replaces LouvainOptions::LouvainOptions
+ * (inc/louvain.hxx:60). */
+void lvg_options_default(lvg_options *o);
+
+/* Result. Mirrors LouvainResult<uint32_t, double> (inc/louvain.hxx:78-145).
+ * Array fields: if the caller leaves a pointer NULL, the library allocates it
+ * (malloc, span entries) and lvg_result_free() releases it; a non-NULL pointer
+ * is taken as a caller-owned buffer of `span` entries and is filled in place
+ * (use lvg_host_alloc() for pinned buffers). */
+typedef struct lvg_result {
+  size_t    span;
+  uint32_t *membership;       /* community of each vertex (last level, renumbered) */
+  double   *vertexWeight;     /* total edge weight of each vertex (first pass) */
+  double   *communityWeight;  /* last pass's community totals; entries past the live ids are stale */
+  int       iterations;       /* local-moving iterations over all passes */
+  int       passes;           /* passes performed */
+  float     time;             /* ms, mean over repeats: init + mark + passes */
+  float     markingTime;      /* ms, marking affected vertices */
+  float     initializationTime; /* ms, initial membership and weights */
+  float     firstPassTime;    /* ms, first pass */
+  float     localMoveTime;    /* ms, all local-moving phases */
+  float     aggregationTime;  /* ms, all aggregation phases */
+  size_t    affectedVertices; /* flags still set after the run (inc/louvain.hxx:1220) */
+  int       owned;            /* bit 0/1/2: membership/vertexWeight/communityWeight allocated by the library */
+} lvg_result;
+
+/* A batch update (host arrays). Replaces the reference's
+ * vector<tuple<K,K,V>> deletions / insertions. */
+typedef struct lvg_batch {
+  size_t          num_deletions;
+  const uint32_t *del_src, *del_dst;
+  const float    *del_w;
+  size_t          num_insertions;
+  const uint32_t *ins_src, *ins_dst;
+  const float    *ins_w;
+} lvg_batch;
+
+/* A graph resident on the GPU (CSR: offsets, neighbour ids, weights). */
+typedef struct lvg_graph lvg_graph;
+
+/* Upload a CSR graph. offsets[span+1], keys/weights[offsets[span]];
+ * exists[span] may be NULL (every slot exists). Replaces the reference's
+ * graph argument `const G& x` (inc/louvain.hxx:1285): the G concept
+ * (span/order/size/hasVertex/forEachEdge, inc/Graph.hxx:59-150) flattened. */
+int lvg_graph_create(size_t span, const uint64_t *offsets, const uint32_t *keys, const float *weights,
+                     const uint8_t *exists, lvg_graph **out);
+int lvg_graph_destroy(lvg_graph *g);
+/* G::span(), G::order(), G::size() (inc/Graph.hxx:59-80). */
+size_t lvg_graph_span(const lvg_graph *g);
+size_t lvg_graph_order(const lvg_graph *g);
+size_t lvg_graph_size(const lvg_graph *g);
+
+/* Static Louvain. Replaces louvainStaticOmp(x, o) (inc/louvain.hxx:1285). */
+int lvg_static(lvg_graph *x, const lvg_options *o, lvg_result *out);
+
+/* Naive-dynamic Louvain on the updated graph y, from the prior membership q
+ * and weights qvtot/qctot (span entries each). Replaces
+ * louvainNaiveDynamicOmp(y, deletions, insertions, q, qvtot, qctot, o)
+ * (inc/louvain.hxx:1349). */
+int lvg_naive_dynamic(lvg_graph *y, const lvg_batch *b, const uint32_t *q, const double *qvtot,
+                      const double *qctot, const lvg_options *o, lvg_result *out);
+
+/* Delta-screening dynamic Louvain. Replaces louvainDynamicDeltaScreeningOmp
+ * (inc/louvain.hxx:1542). Insertions must be sorted by source (LVG_EINVAL otherwise). */
+int lvg_delta_screening(lvg_graph *y, const lvg_batch *b, const uint32_t *q, const double *qvtot,
+                        const double *qctot, const lvg_options *o, lvg_result *out);
+
+/* Dynamic-frontier Louvain. Replaces louvainDynamicFrontierOmp
+ * (inc/louvain.hxx:1674). */
+int lvg_frontier(lvg_graph *y, const lvg_batch *b, const uint32_t *q, const double *qvtot,
+                 const double *qctot, const lvg_options *o, lvg_result *out);
+
+/* Affected-vertex marking alone: applies the batch to the prior weights and
+ * marks the vertices a method would start from, without running the passes.
+ * method LVG_METHOD_FRONTIER replaces louvainAffectedVerticesFrontierOmpW
+ * (inc/louvain.hxx:1606); LVG_METHOD_DELTA replaces
+ * louvainAffectedVerticesDeltaScreeningOmpW (inc/louvain.hxx:1441) and also
+ * returns its neighbour and community flags (either pointer may be NULL);
+ * LVG_METHOD_NAIVE / LVG_METHOD_STATIC mark every slot. flags[span]. */
+int lvg_affected_vertices(lvg_graph *y, int method, const lvg_batch *b, const uint32_t *q, const double *qvtot,
+                          const double *qctot, const lvg_options *o, uint8_t *flags, uint8_t *neighbors,
+                          uint8_t *communities);
+
+/* One aggregation step for a given membership: renumbers the communities in
+ * id order (louvainCommunityExistsOmpW + louvainRenumberCommunitiesOmpW,
+ * inc/louvain.hxx:668, 941) and builds the super-vertex graph
+ * (louvainCommunityVerticesOmpW + louvainAggregateOmpW, :800, :987).
+ * renumbered[span] receives the renumbered membership, *num_communities the
+ * community count, offsets[CN+1] / keys / weights the super-vertex CSR
+ * (compact; keys/weights need room for lvg_graph_size(g) entries). Row order
+ * within a super-vertex is unspecified, as in the reference. */
+int lvg_aggregate(lvg_graph *g, const uint32_t *membership, uint32_t *renumbered, size_t *num_communities,
+                  uint64_t *offsets, uint32_t *keys, double *weights);
+
+/* Release the library-owned arrays of a result (LouvainResult's destructor). */
+void lvg_result_free(lvg_result *r);
+
+/* Modularity of a membership on graph g, reduced in FP64 on the GPU.
+ * Replaces modularityBy (inc/properties.hxx:178) as used by main.cxx:48-51.
+ * M <= 0 means "half the total edge weight of g". */
+int lvg_modularity(lvg_graph *g, const uint32_t *membership, double M, double R, double *out);
+
+/* Total edge weight of g (FP64 on the GPU). Replaces edgeWeightOmp
+ * (inc/properties.hxx:96). */
+int lvg_edge_weight(lvg_graph *g, double *out);
+
+/* Pinned host memory for result buffers and batches (no reference counterpart). */
+void *lvg_host_alloc(size_t bytes);
+void  lvg_host_free(void *p);
+
+/* ---- Device-resident inputs (no reference counterpart). The reference keeps
+ * its graph, batch and prior state in host memory; these keep them in HBM so a
+ * caller that applies many batches (a serving loop) pays no host<->device copy
+ * per call. */
+
+/* Methods of lvg_run_resident. */
+#define LVG_METHOD_STATIC    0
+#define LVG_METHOD_NAIVE     1
+#define LVG_METHOD_DELTA     2
+#define LVG_METHOD_FRONTIER  3
+
+/* Membership, vertex weights and community weights of a graph (span entries
+ * each) in HBM. Weights are held in FP32 on the device. */
+typedef struct lvg_state lvg_state;
+int lvg_state_create(lvg_graph *g, lvg_state **out);
+/* Upload (q, qvtot, qctot) from host arrays of span entries. */
+int lvg_state_set(lvg_state *st, const uint32_t *q, const double *qvtot, const double *qctot);
+/* Download into host arrays of span entries; any pointer may be NULL. */
+int lvg_state_get(const lvg_state *st, uint32_t *membership, double *vtot, double *ctot);
+int lvg_state_destroy(lvg_state *st);
+
+/* A validated batch in HBM. */
+typedef struct lvg_device_batch lvg_device_batch;
+int lvg_device_batch_create(lvg_graph *g, const lvg_batch *b, lvg_device_batch **out);
+int lvg_device_batch_destroy(lvg_device_batch *b);
+
+/* Run a method on device-resident inputs: prior state `prior` (ignored by
+ * LVG_METHOD_STATIC) and batch `b` (NULL for static); the result state is
+ * written to `out` (out may equal prior: updated in place). `info` receives
+ * the scalar fields of the result; its arrays are not touched. */
+int lvg_run_resident(lvg_graph *g, int method, const lvg_device_batch *b, const lvg_state *prior, lvg_state *out,
+                     const lvg_options *o, lvg_result *info);
+
+/* Per-call device statistics of the last run on g (no reference
+ * counterpart; used for the roofline figures): kernel time of the
+ * local-moving launches and the work they did. */
+typedef struct lvg_stats {
+  double   move_kernel_ms;     /* sum of local-moving launch durations (CUDA events) */
+  uint64_t move_launches;      /* local-moving kernel launches */
+  uint64_t move_vertices;      /* vertices processed (active) */
+  uint64_t move_edges;         /* edges scanned by processed vertices */
+  uint64_t moves;              /* vertices that changed community */
+  double   aggregate_kernel_ms;
+  uint64_t aggregate_edges;    /* edges read by aggregation */
+  uint64_t aggregate_launches;
+  uint64_t kernel_launches;    /* all kernels launched by the last call */
+} lvg_stats;
+/* Enable (1) or disable (0) per-launch event timing for calls on g. */
+int lvg_set_profiling(lvg_graph *g, int enable);
+int lvg_get_stats(const lvg_graph *g, lvg_stats *out);
+
+/* Message of the last failure on the calling thread ("" if none). */
+const char *lvg_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,95 @@
+/*
+ * louvain_gb300_graphgen.h — seeded synthetic graphs and batch updates (host only).
+ *
+ * These stand in for the reference's inputs. The reference reads SNAP temporal
+ * edge lists (inc/snap.hxx:41-212), generates random batches
+ * (inc/batch.hxx:100-140), tidies them (inc/batch.hxx:202-209) and applies them
+ * to a copy of the graph (inc/batch.hxx:241-248). The datasets are not shipped,
+ * so these generators produce seeded graphs with the reference's conventions:
+ *   - vertex ids are 1..n and vertex 0 never exists (inc/snap.hxx:133), so the
+ *     span is n+1;
+ *   - rows are sorted ascending by neighbour id, as the reference's LazyBitset
+ *     adjacency is (inc/_bitset.hxx:227-262);
+ *   - graphs are undirected: every edge is stored in both directions, without
+ *     self-loops or duplicates, with unit float weights.
+ *
+ * Every generator draws from counter-based random streams keyed by
+ * (seed, stream, index), so the output does not depend on the thread count.
+ * Memory is allocated by the library; release it with lvgg_csr_free /
+ * lvgg_batch_free. Functions return 0 on success and a negative errno-style
+ * code on failure (see lvgg_last_error()).
+ *
+ * This library has no CUDA dependency: the reference's CPU arm of the
+ * benchmark links it without loading any GPU code.
+ */
+#ifndef LOUVAIN_GB300_GRAPHGEN_H
+#define LOUVAIN_GB300_GRAPHGEN_H
+#include <stddef.h>
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/** A CSR graph on the host: row u is keys[offsets[u] .. offsets[u+1]). */
+typedef struct lvgg_csr {
+  size_t    span;       /* number of vertex slots (max id + 1) */
+  size_t    num_edges;  /* directed edges = offsets[span] */
+  uint64_t *offsets;    /* [span+1] */
+  uint32_t *keys;       /* [num_edges] neighbour ids, sorted within each row */
+  float    *weights;    /* [num_edges] */
+  uint8_t  *exists;     /* [span] 1 if the vertex exists (vertex 0 never does) */
+} lvgg_csr;
+
+/** A tidy batch update: both directions of each undirected edge, sorted by (src, dst), unique. */
+typedef struct lvgg_batch {
+  size_t    num_deletions;
+  size_t    num_insertions;
+  uint32_t *del_src, *del_dst;  /* [num_deletions] */
+  float    *del_w;              /* [num_deletions] weight of the removed edge */
+  uint32_t *ins_src, *ins_dst;  /* [num_insertions] */
+  float    *ins_w;              /* [num_insertions] */
+} lvgg_batch;
+
+/**
+ * Planted-partition graph: n vertices (ids 1..n) in consecutive blocks of
+ * `block` vertices; round(n*avg_degree/2) undirected draws. Each draw picks u
+ * uniformly, then v uniformly inside u's block with probability p_in, else
+ * uniformly over all vertices. Self-loops are dropped, then the edges are
+ * symmetrized and deduplicated.
+ */
+int lvgg_planted_partition(uint32_t n, uint32_t block, double avg_degree, double p_in,
+                           uint64_t seed, lvgg_csr *out);
+
+/**
+ * R-MAT graph: 2^scale vertices (ids 1..2^scale), round(edge_factor*2^scale)
+ * undirected draws with quadrant probabilities (a, b, c, 1-a-b-c). If permute
+ * is non-zero, vertex ids are relabelled by a seeded random permutation (as
+ * Graph500 does), so that id order carries no degree information. Self-loops
+ * dropped, symmetrized, deduplicated.
+ */
+int lvgg_rmat(int scale, double edge_factor, double a, double b, double c, int permute,
+              uint64_t seed, lvgg_csr *out);
+
+/**
+ * Random batch on graph x: num_updates undirected updates, of which
+ * round(num_updates*insertion_fraction) are insertions of uniformly random
+ * vertex pairs (u != v, edge absent) and the rest deletions of uniformly
+ * sampled existing undirected edges (edge-uniform). The batch is returned tidy:
+ * both directions, sorted by (src, dst), unique.
+ */
+int lvgg_random_batch(const lvgg_csr *x, size_t num_updates, double insertion_fraction,
+                      uint64_t seed, lvgg_batch *out);
+
+/** y = x with the batch's deletions removed and insertions added (rows stay sorted). */
+int lvgg_apply_batch(const lvgg_csr *x, const lvgg_batch *b, lvgg_csr *y);
+
+void lvgg_csr_free(lvgg_csr *g);
+void lvgg_batch_free(lvgg_batch *b);
+
+/** Message of the last failure on this thread ("" if none). */
+const char *lvgg_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

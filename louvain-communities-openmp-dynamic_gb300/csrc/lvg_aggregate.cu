@@ -1,0 +1,289 @@
+// lvg_aggregate.cu — aggregation phase (replaces louvainAggregateEdgesOmpW
+// and louvainAggregateOmpW, inc/louvain.hxx:897-912, 987-992).
+//
+// Input: a level, its renumbered membership, the community -> member CSR and
+// the row capacity offsets yoff (exclusive scan of each community's total
+// degree, as louvainCommunityTotalDegreeOmpW + scan do, inc/louvain.hxx:989-990).
+// Each community merges the neighbour communities of all its members'
+// edges, self-loops included (louvainScanCommunitiesW<true>), into a hash
+// table sized by the community's total degree, then writes the distinct
+// (community, summed weight) pairs to its row at yoff[c] and the row's degree
+// to ydeg[c] (the reference's gapped DiGraphCsr). The row sum is the
+// super-vertex's weight (louvainVertexWeightsOmpW on the new level, :1209).
+//
+// Communities are binned by total degree like vertices in the move kernels:
+// sub-warp tiles / warps with shared tables, blocks with large shared tables,
+// and blocks with per-block global tables. Inside a tile, the members' edge
+// lists are flattened with a tile prefix scan over member degrees, so lanes
+// stay busy whatever the member degrees are.
+#include "lvg_internal.cuh"
+
+namespace lvg {
+namespace {
+
+__host__ __device__ constexpr int ilog2c(int x) { return x <= 1 ? 0 : 1 + ilog2c(x >> 1); }
+
+template <int T>
+__device__ __forceinline__ unsigned tile_mask() {
+  if (T == 32) return 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  return ((1u << T) - 1u) << (lane & ~(T - 1));
+}
+
+template <class KP, class VP>
+__device__ __forceinline__ bool table_add(KP keys, VP vals, int log2cap, uint32_t c, float w) {
+  const uint32_t mask = (1u << log2cap) - 1u;
+  uint32_t s = hash_hi(c, log2cap);
+  for (uint32_t probe = 0; probe <= mask; ++probe) {
+    uint32_t k = keys[s];
+    if (k == c) { atomicAdd(&vals[s], w); return true; }
+    if (k == EMPTY) {
+      uint32_t prev = atomicCAS(&keys[s], EMPTY, c);
+      if (prev == EMPTY || prev == c) { atomicAdd(&vals[s], w); return true; }
+    }
+    s = (s + 1u) & mask;
+  }
+  return false;
+}
+
+// Insert all edges of members cmem[m0..m1) into the table, T lanes
+// cooperating (T = tile size, lanes tl = 0..T-1, mask m). Returns edges read.
+template <int T, class KP, class VP>
+__device__ __forceinline__ uint64_t insert_members(const AggArgs &a, uint32_t m0, uint32_t m1, int tl, unsigned m,
+                                                   KP keys, VP vals, int log2cap, bool &ok) {
+  uint64_t nread = 0;
+  for (uint32_t base = m0; base < m1; base += T) {
+    const uint32_t mm = base + tl;
+    uint32_t dg = 0;
+    uint64_t o = 0;
+    if (mm < m1) {
+      const uint32_t u = a.cmem[mm];
+      dg = a.deg[u];
+      o = a.off[u];
+    }
+    uint32_t incl = dg;
+#pragma unroll
+    for (int sh = 1; sh < T; sh <<= 1) {
+      uint32_t t = __shfl_up_sync(m, incl, sh, T);
+      if (tl >= sh) incl += t;
+    }
+    const uint32_t total = __shfl_sync(m, incl, T - 1, T);
+    nread += total;
+    for (uint32_t k0 = 0; k0 < total; k0 += T) {
+      const uint32_t k = k0 + tl;
+      // owner lane: first lane whose inclusive prefix exceeds k
+      int lo = 0, hi = T - 1;
+#pragma unroll
+      for (int step = 0; step < ilog2c(T); ++step) {
+        const int mid = (lo + hi) >> 1;
+        const uint32_t x = __shfl_sync(m, incl, mid, T);
+        if (x <= k) lo = mid + 1; else hi = mid;
+      }
+      const uint32_t oincl = __shfl_sync(m, incl, lo, T);
+      const uint32_t odeg = __shfl_sync(m, dg, lo, T);
+      const uint64_t oo = __shfl_sync(m, o, lo, T);
+      if (k < total) {
+        const uint64_t e = oo + (k - (oincl - odeg));
+        ok &= table_add(keys, vals, log2cap, a.vcom[a.key[e]], a.w[e]);
+      }
+    }
+  }
+  return nread;
+}
+
+constexpr int TILE_BLOCK = 256;
+
+template <int T, int C>
+__global__ void __launch_bounds__(TILE_BLOCK) agg_tile_kernel(AggArgs a) {
+  constexpr int LOGC = ilog2c(C);
+  constexpr int TPB = TILE_BLOCK / T;
+  extern __shared__ __align__(16) uint8_t smem[];
+  const int tib = threadIdx.x / T;
+  const int tl = threadIdx.x & (T - 1);
+  const int lane = threadIdx.x & 31;
+  uint32_t *keys = reinterpret_cast<uint32_t *>(smem) + tib * C;
+  float *vals = reinterpret_cast<float *>(smem + size_t(TPB) * C * sizeof(uint32_t)) + tib * C;
+  const unsigned m = tile_mask<T>();
+  const uint32_t ntiles = gridDim.x * TPB;
+  unsigned long long nread = 0;
+  bool ok = true;
+  for (uint32_t i = blockIdx.x * TPB + tib; i < a.count; i += ntiles) {
+    const uint32_t c = a.list[i];
+    const uint32_t m0 = a.coff[c], m1 = a.coff[c + 1];
+#pragma unroll
+    for (int s = tl; s < C; s += T) { keys[s] = EMPTY; vals[s] = 0.f; }
+    __syncwarp(m);
+    nread += insert_members<T>(a, m0, m1, tl, m, keys, vals, LOGC, ok);
+    __syncwarp(m);
+    const uint64_t y0 = a.yoff[c];
+    uint32_t cnt = 0;
+    float vsum = 0.f;
+#pragma unroll
+    for (int s0 = 0; s0 < C; s0 += T) {
+      const int s = s0 + tl;
+      const uint32_t k = keys[s];
+      const bool has = k != EMPTY;
+      const unsigned bal = (__ballot_sync(m, has) >> (lane & ~(T - 1))) & (T == 32 ? 0xffffffffu : ((1u << T) - 1u));
+      if (has) {
+        const uint32_t r = __popc(bal & ((1u << tl) - 1u));
+        const float v = vals[s];
+        a.ykey[y0 + cnt + r] = k;
+        a.yw[y0 + cnt + r] = v;
+        vsum += v;
+      }
+      cnt += __popc(bal);
+    }
+#pragma unroll
+    for (int sh = T / 2; sh > 0; sh >>= 1) vsum += __shfl_xor_sync(m, vsum, sh, T);
+    if (tl == 0) { a.ydeg[c] = cnt; a.vtot[c] = vsum; }
+    __syncwarp(m);
+  }
+  if (tl != 0) nread = 0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) nread += __shfl_xor_sync(0xffffffffu, nread, o);
+  const bool bad = __any_sync(0xffffffffu, !ok);
+  if (lane == 0) {
+    if (nread) atomicAdd(&a.ctr->agg_edges, nread);
+    if (bad) atomicOr(&a.ctr->err, ERR_TABLE_FULL);
+  }
+}
+
+// One block per community; each warp flattens a 32-member chunk at a time.
+template <int B, bool GLOBAL>
+__global__ void __launch_bounds__(B) agg_block_kernel(AggArgs a, int log2cap) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  __shared__ uint32_t s_cnt;
+  __shared__ float s_sum[B / 32];
+  const uint32_t cap = 1u << log2cap;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t *keys;
+  float *vals;
+  if (GLOBAL) {
+    keys = a.gkeys + size_t(blockIdx.x) * cap;
+    vals = a.gvals + size_t(blockIdx.x) * cap;
+  } else {
+    keys = reinterpret_cast<uint32_t *>(smem);
+    vals = reinterpret_cast<float *>(smem + size_t(cap) * sizeof(uint32_t));
+  }
+  unsigned long long nread = 0;
+  bool ok = true;
+  for (uint32_t i = blockIdx.x; i < a.count; i += gridDim.x) {
+    const uint32_t c = a.list[i];
+    const uint32_t m0 = a.coff[c], m1 = a.coff[c + 1];
+    for (uint32_t s = threadIdx.x; s < cap; s += B) { keys[s] = EMPTY; vals[s] = 0.f; }
+    if (threadIdx.x == 0) s_cnt = 0;
+    __syncthreads();
+    for (uint32_t b0 = m0 + uint32_t(wid) * 32; b0 < m1; b0 += B) {
+      const uint32_t b1 = b0 + 32 < m1 ? b0 + 32 : m1;
+      nread += insert_members<32>(a, b0, b1, lane, 0xffffffffu, keys, vals, log2cap, ok);
+    }
+    __syncthreads();
+    const uint64_t y0 = a.yoff[c];
+    float vsum = 0.f;
+    for (uint32_t s0 = 0; s0 < cap; s0 += B) {
+      const uint32_t s = s0 + threadIdx.x;
+      const uint32_t k = s < cap ? keys[s] : EMPTY;
+      const bool has = k != EMPTY;
+      const unsigned bal = __ballot_sync(0xffffffffu, has);
+      uint32_t base = 0;
+      if (lane == 0 && bal) base = atomicAdd(&s_cnt, uint32_t(__popc(bal)));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (has) {
+        const uint32_t r = __popc(bal & ((1u << lane) - 1u));
+        const float v = vals[s];
+        a.ykey[y0 + base + r] = k;
+        a.yw[y0 + base + r] = v;
+        vsum += v;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) vsum += __shfl_xor_sync(0xffffffffu, vsum, o);
+    if (lane == 0) s_sum[wid] = vsum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float t = 0.f;
+      for (int k = 0; k < B / 32; ++k) t += s_sum[k];
+      a.ydeg[c] = s_cnt;
+      a.vtot[c] = t;
+    }
+    __syncthreads();
+  }
+  if (lane != 0) nread = 0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) nread += __shfl_xor_sync(0xffffffffu, nread, o);
+  const bool bad = __any_sync(0xffffffffu, !ok);
+  if (lane == 0) {
+    if (nread) atomicAdd(&a.ctr->agg_edges, nread);
+    if (bad) atomicOr(&a.ctr->err, ERR_TABLE_FULL);
+  }
+}
+
+int g_sms = 0;
+int sms() {
+  if (!g_sms) {
+    int dev = 0;
+    LVG_CUDA(cudaGetDevice(&dev));
+    LVG_CUDA(cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev));
+  }
+  return g_sms;
+}
+
+template <class K>
+void set_smem(K kernel, size_t bytes) {
+  if (bytes > 48 * 1024) LVG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)));
+}
+
+template <int T, int C>
+void launch_tile(const AggArgs &a, cudaStream_t s) {
+  constexpr int TPB = TILE_BLOCK / T;
+  const size_t smem = size_t(TPB) * C * 8;
+  auto k = agg_tile_kernel<T, C>;
+  static bool configured = false;
+  if (!configured) { set_smem(k, smem); configured = true; }
+  size_t want = (a.count + TPB - 1) / TPB;
+  size_t cap = size_t(sms()) * (smem > 32 * 1024 ? 3 : 8);
+  unsigned grid = unsigned(want < cap ? want : cap);
+  if (!grid) return;
+  k<<<grid, TILE_BLOCK, smem, s>>>(a);
+  LVG_CHECK_LAUNCH();
+}
+
+template <int B, int LOGC>
+void launch_block_smem(const AggArgs &a, cudaStream_t s) {
+  const size_t smem = (size_t(1) << LOGC) * 8;
+  auto k = agg_block_kernel<B, false>;
+  static bool configured = false;
+  if (!configured) { set_smem(k, smem); configured = true; }
+  size_t cap = size_t(sms()) * (smem > 64 * 1024 ? 1 : 2);
+  unsigned grid = unsigned(a.count < cap ? a.count : cap);
+  if (!grid) return;
+  k<<<grid, B, smem, s>>>(a, LOGC);
+  LVG_CHECK_LAUNCH();
+}
+
+}  // namespace
+
+void launch_aggregate_bin(int b, const AggArgs &a, cudaStream_t s) {
+  switch (b) {
+    case 1: launch_tile<4, 8>(a, s); break;
+    case 2: launch_tile<8, 16>(a, s); break;
+    case 3: launch_tile<16, 32>(a, s); break;
+    case 4: launch_tile<32, 64>(a, s); break;
+    case 5: launch_tile<32, 128>(a, s); break;
+    case 6: launch_tile<32, 256>(a, s); break;
+    case 7: launch_tile<32, 512>(a, s); break;
+    case 8: launch_tile<32, 1024>(a, s); break;
+    case 9: launch_block_smem<256, 12>(a, s); break;
+    case 10: launch_block_smem<512, 14>(a, s); break;
+    case 11: {
+      unsigned grid = unsigned(global_table_blocks(a.count));
+      if (!grid) return;
+      agg_block_kernel<512, true><<<grid, 512, 0, s>>>(a, a.glog2);
+      LVG_CHECK_LAUNCH();
+      break;
+    }
+    default: break;
+  }
+}
+
+}  // namespace lvg

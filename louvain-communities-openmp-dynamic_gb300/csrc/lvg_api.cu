@@ -1,0 +1,982 @@
+// lvg_api.cu — C-ABI entry points, device graph handles and the pass driver.
+//
+// The pass driver follows louvainInvokeOmp (inc/louvain.hxx:1120-1221): per
+// repetition it initialises membership and weights (fi), marks affected
+// vertices (fm), then alternates local moving and aggregation until a pass
+// converges in one iteration, maxPasses is reached, or the community count
+// stops shrinking below aggregationTolerance. Everything runs on the graph's
+// own CUDA stream; the host only reads back the per-iteration gain sum and the
+// per-pass community count to take the reference's branch decisions.
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "lvg_internal.cuh"
+
+namespace lvg {
+
+thread_local std::string g_err;
+
+template <class T>
+struct DBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  ~DBuf() { release(); }
+  void ensure(size_t k) {
+    if (p && k <= n) return;
+    release();
+    if (k == 0) k = 1;
+    LVG_CUDA(cudaMalloc(&p, k * sizeof(T)));
+    n = k;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+template <class T>
+struct HBuf {  // pinned host buffer
+  T *p = nullptr;
+  size_t n = 0;
+  HBuf() = default;
+  HBuf(const HBuf &) = delete;
+  HBuf &operator=(const HBuf &) = delete;
+  ~HBuf() { if (p) cudaFreeHost(p); }
+  void ensure(size_t k) {
+    if (p && k <= n) return;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    LVG_CUDA(cudaMallocHost(&p, (k ? k : 1) * sizeof(T)));
+    n = k;
+  }
+};
+
+struct LevelBuffers {
+  DBuf<uint64_t> off;
+  DBuf<uint32_t> deg, key, bins;
+  DBuf<float> w;
+};
+
+struct Workspace {
+  size_t S = 0, X = 0;
+  DBuf<uint8_t> vaff, mark, fv, fn, fc;
+  DBuf<uint32_t> ucom, vcom, com_next, dec, cext, csize, ccur, cmem, cbins;
+  DBuf<float> utot, vtot, ctot;
+  DBuf<uint64_t> scan64;
+  DBuf<uint32_t> scan32, binscratch;
+  LevelBuffers lv[2];
+  DBuf<uint32_t> gkeys, gfirst;
+  DBuf<float> gvals;
+  DBuf<double> ctot64;
+  DBuf<uint32_t> prior_q;
+  DBuf<float> prior_vt, prior_ct;
+  DBuf<double> stage_a, stage_b;
+
+  void allocate(size_t S_, size_t X_, cudaStream_t st) {
+    S = S_;
+    X = X_;
+    vaff.ensure(S); mark.ensure(S); fv.ensure(S); fn.ensure(S); fc.ensure(S);
+    ucom.ensure(S); vcom.ensure(S); com_next.ensure(S); dec.ensure(S);
+    cext.ensure(S + 1); csize.ensure(S + 1); ccur.ensure(S + 1); cmem.ensure(S + 1); cbins.ensure(S + 1);
+    utot.ensure(S); vtot.ensure(S); ctot.ensure(S);
+    scan64.ensure(scan_scratch_elems(S + 1));
+    scan32.ensure(scan_scratch_elems(S + 1));
+    binscratch.ensure(bin_scratch_elems(S + 1, MAX_COLORS));
+    for (auto &l : lv) {
+      l.off.ensure(S + 1);
+      l.deg.ensure(S + 1);
+      l.bins.ensure(S + 1);
+      l.key.ensure(X);
+      l.w.ensure(X);
+    }
+    LVG_CUDA(cudaMemsetAsync(mark.p, 0, S, st));
+    LVG_CUDA(cudaMemsetAsync(dec.p, 0xFF, S * sizeof(uint32_t), st));
+  }
+};
+
+struct EventPool {
+  std::vector<cudaEvent_t> ev;
+  size_t used = 0;
+  ~EventPool() {
+    for (auto e : ev) cudaEventDestroy(e);
+  }
+  cudaEvent_t record(cudaStream_t s) {
+    if (used == ev.size()) {
+      cudaEvent_t e;
+      LVG_CUDA(cudaEventCreate(&e));
+      ev.push_back(e);
+    }
+    cudaEvent_t e = ev[used++];
+    LVG_CUDA(cudaEventRecord(e, s));
+    return e;
+  }
+  void reset() { used = 0; }
+};
+
+float elapsed(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0;
+  LVG_CUDA(cudaEventElapsedTime(&ms, a, b));
+  return ms;
+}
+
+struct DBatch {
+  const uint32_t *ds = nullptr, *dd = nullptr, *is = nullptr, *id = nullptr;
+  const float *dw = nullptr, *iw = nullptr;
+  uint32_t *seg = nullptr;
+  size_t nd = 0, ni = 0;
+  size_t max_group = 0;  // longest run of insertions sharing a source
+};
+
+struct RunInfo {
+  int iterations = 0, passes = 0;
+  float t = 0, tm = 0, ti = 0, tp = 0, tl = 0, ta = 0;
+  uint64_t affected = 0;
+};
+
+}  // namespace lvg
+
+using namespace lvg;
+
+struct lvg_graph {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  Level base;
+  DBuf<uint64_t> off;
+  DBuf<uint32_t> deg, key, bins;
+  DBuf<float> w;
+  DBuf<uint8_t> ex;
+  double total_weight = 0;
+  std::unique_ptr<Workspace> ws;
+  DBuf<Counters> ctr;
+  HBuf<Counters> hctr;
+  HBuf<uint32_t> hbins;
+  EventPool events;
+  bool profiling = false;
+  lvg_stats stats = {};
+  // batch buffers of the host-array entry points
+  DBuf<uint32_t> b_ds, b_dd, b_is, b_id, b_seg;
+  DBuf<float> b_dw, b_iw;
+};
+
+struct lvg_state {
+  lvg_graph *g = nullptr;
+  DBuf<uint32_t> q;
+  DBuf<float> vt, ct;
+};
+
+struct lvg_device_batch {
+  lvg_graph *g = nullptr;
+  DBuf<uint32_t> ds, dd, is, id, seg;
+  DBuf<float> dw, iw;
+  DBatch b;
+};
+
+namespace lvg {
+namespace {
+
+int fail(int code, const std::string &msg) {
+  g_err = msg;
+  return code;
+}
+
+template <class F>
+int guarded(F &&f) {
+  try {
+    g_err.clear();
+    return f();
+  } catch (const Error &e) {
+    return fail(e.code, e.what());
+  } catch (const std::bad_alloc &) {
+    return fail(LVG_ENOMEM, "host allocation failed");
+  } catch (const std::exception &e) {
+    return fail(LVG_ECUDA, e.what());
+  }
+}
+
+void ensure_ws(lvg_graph *g) {
+  if (!g->ws) {
+    g->ws = std::make_unique<Workspace>();
+    g->ws->allocate(g->base.span, g->base.edges, g->stream);
+  }
+}
+
+void read_counters(lvg_graph *g) {
+  LVG_CUDA(cudaMemcpyAsync(g->hctr.p, g->ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, g->stream));
+  LVG_CUDA(cudaStreamSynchronize(g->stream));
+  if (g->hctr.p->err) {
+    unsigned e = g->hctr.p->err;
+    LVG_CUDA(cudaMemsetAsync(&g->ctr.p->err, 0, sizeof(unsigned), g->stream));
+    throw Error(LVG_ETIMEOUT, "device hash table overflow guard tripped (err=" + std::to_string(e) + ")");
+  }
+}
+
+void compute_bins(lvg_graph *g, Level &lv, const uint32_t *deg, uint32_t *list, uint32_t *scratch, int colors) {
+  g->hbins.ensure(bin_host_elems(MAX_COLORS));
+  lv.colors = colors;
+  bin_items_u32(deg, lv.ex, lv.span, colors, list, lv.bin_start, lv.bin_maxdeg, scratch, g->hbins.p, g->stream);
+  lv.bins = list;
+}
+
+int colors_for(const lvg_options &o) {
+  int k = o.colors > 0 ? o.colors : (o.deterministic ? DEFAULT_COLORS_SYNC : DEFAULT_COLORS_ASYNC);
+  return k < 1 ? 1 : (k > MAX_COLORS ? MAX_COLORS : k);
+}
+
+void ensure_global_tables(Workspace &W, size_t blocks, int log2cap, bool first_too) {
+  size_t need = blocks * (size_t(1) << log2cap);
+  W.gkeys.ensure(need);
+  W.gvals.ensure(need);
+  if (first_too) W.gfirst.ensure(need);
+}
+
+// ---------------------------------------------------------------- local moving
+
+// louvainMoveOmpW (inc/louvain.hxx:588-609). Returns the iteration count, 0
+// if the first iteration found nothing to gain. Each iteration sweeps the
+// colour classes in order; within a class the degree bins run one kernel
+// each. In deterministic mode a class first decides (reading the state left
+// by the previous classes), then its decisions and neighbour marks are applied.
+int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const float *tot, const uint8_t *fa,
+               double M, float kr, int L, double E, bool sync) {
+  Workspace &W = *g->ws;
+  cudaStream_t s = g->stream;
+  const size_t n = lv.span;
+  const int K = lv.colors;
+  // Existing degree-0 vertices are processed once and never re-marked.
+  for (int k = 0; k < K; ++k)
+    launch_clear_isolated(lv.bins + lv.bucket_begin(k, 0), lv.bucket_size(k, 0), W.vaff.p, fa, s);
+  int glog2 = 1;
+  size_t hubs = 0;
+  for (int k = 0; k < K; ++k) hubs = std::max(hubs, lv.bucket_size(k, NUM_BINS - 1));
+  if (hubs) {
+    glog2 = global_table_log2(lv.bin_maxdeg[NUM_BINS - 1]);
+    ensure_global_tables(W, size_t(global_table_blocks(hubs)), glog2, false);
+  }
+  int l = 0;
+  double el = 0;
+  while (l < L) {
+    LVG_CUDA(cudaMemsetAsync(&g->ctr.p->el_fix, 0, sizeof(unsigned long long), s));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (g->profiling) e0 = g->events.record(s);
+    for (int k = 0; k < K; ++k) {
+      for (int b = 1; b < NUM_BINS; ++b) {
+        const size_t cnt = lv.bucket_size(k, b);
+        if (!cnt) continue;
+        MoveArgs a;
+        a.off = lv.off; a.deg = lv.deg; a.key = lv.key; a.w = lv.w;
+        a.list = lv.bins + lv.bucket_begin(k, b);
+        a.count = uint32_t(cnt);
+        a.vcom = com; a.ctot = ctot; a.dec = W.dec.p;
+        a.vaff = W.vaff.p; a.mark = W.mark.p; a.fa = fa; a.vtot = tot;
+        a.kr = kr; a.ctr = g->ctr.p;
+        a.gkeys = W.gkeys.p; a.gvals = W.gvals.p; a.glog2 = glog2;
+        launch_move_bin(b, sync, a, s);
+        ++g->stats.move_launches;
+      }
+      if (sync) {
+        launch_apply_moves(lv.bins + lv.color_begin(k), lv.color_end(k) - lv.color_begin(k), W.dec.p, com, ctot, tot,
+                           s);
+        launch_merge_marks(W.vaff.p, W.mark.p, n, s);
+      }
+    }
+    if (g->profiling) e1 = g->events.record(s);
+    read_counters(g);
+    if (g->profiling) g->stats.move_kernel_ms += elapsed(e0, e1);
+    el = double(g->hctr.p->el_fix) / GAIN_FIX / M;
+    ++l;
+    if (el <= E) break;
+  }
+  return (l > 1 || el != 0) ? l : 0;
+}
+
+// ---------------------------------------------------------------- aggregation
+
+// Renumbered membership `com` of level `lv` with CN communities -> next level
+// in buffer set `which` (louvainCommunityVerticesOmpW + louvainAggregateOmpW,
+// inc/louvain.hxx:1197-1203). Also writes the new level's vertex weights.
+Level aggregate(lvg_graph *g, const Level &lv, const uint32_t *com, size_t CN, int which, int colors) {
+  Workspace &W = *g->ws;
+  cudaStream_t s = g->stream;
+  LevelBuffers &nb = W.lv[which];
+  Level nl;
+  nl.span = nl.order = CN;
+  nl.off = nb.off.p; nl.deg = nb.deg.p; nl.key = nb.key.p; nl.w = nb.w.p; nl.ex = nullptr;
+  // Community -> members CSR and row capacities.
+  LVG_CUDA(cudaMemsetAsync(W.csize.p, 0, (CN + 1) * sizeof(uint32_t), s));
+  LVG_CUDA(cudaMemsetAsync(W.ccur.p, 0, (CN + 1) * sizeof(uint32_t), s));
+  LVG_CUDA(cudaMemsetAsync(nl.off, 0, (CN + 1) * sizeof(uint64_t), s));
+  launch_community_sizes(lv, com, W.csize.p, nl.off, s);
+  size_t cb[NUM_BINS + 1];
+  uint64_t cmax[NUM_BINS];
+  g->hbins.ensure(bin_host_elems(MAX_COLORS));
+  bin_items_u64(nl.off, nullptr, CN, 1, W.cbins.p, cb, cmax, W.binscratch.p, g->hbins.p, s);
+  exclusive_scan_u32(W.csize.p, W.csize.p, CN, W.csize.p + CN, W.scan32.p, s);
+  exclusive_scan_u64(nl.off, nl.off, CN, nl.off + CN, W.scan64.p, s);
+  launch_community_scatter(lv, com, W.csize.p, W.ccur.p, W.cmem.p, s);
+  // Empty communities never reach a kernel: zero their rows and weights first.
+  LVG_CUDA(cudaMemsetAsync(nl.deg, 0, CN * sizeof(uint32_t), s));
+  LVG_CUDA(cudaMemsetAsync(W.vtot.p, 0, CN * sizeof(float), s));
+  int glog2 = 1;
+  const size_t big = cb[NUM_BINS] - cb[NUM_BINS - 1];
+  if (big) {
+    glog2 = global_table_log2(std::min<uint64_t>(cmax[NUM_BINS - 1], CN));
+    ensure_global_tables(W, size_t(global_table_blocks(big)), glog2, false);
+  }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (g->profiling) e0 = g->events.record(s);
+  for (int b = 1; b < NUM_BINS; ++b) {
+    const size_t cnt = cb[b + 1] - cb[b];
+    if (!cnt) continue;
+    AggArgs a;
+    a.off = lv.off; a.deg = lv.deg; a.key = lv.key; a.w = lv.w;
+    a.vcom = com; a.coff = W.csize.p; a.cmem = W.cmem.p;
+    a.list = W.cbins.p + cb[b];
+    a.count = uint32_t(cnt);
+    a.yoff = nl.off; a.ydeg = nl.deg; a.ykey = nl.key; a.yw = nl.w;
+    a.vtot = W.vtot.p; a.ctr = g->ctr.p;
+    a.gkeys = W.gkeys.p; a.gvals = W.gvals.p; a.glog2 = glog2;
+    launch_aggregate_bin(b, a, s);
+    ++g->stats.aggregate_launches;
+  }
+  if (g->profiling) {
+    e1 = g->events.record(s);
+  }
+  compute_bins(g, nl, nl.deg, nb.bins.p, W.binscratch.p, colors);  // synchronises
+  if (g->profiling) g->stats.aggregate_kernel_ms += elapsed(e0, e1);
+  return nl;
+}
+
+// ---------------------------------------------------------------- driver
+
+struct StateRef {
+  uint32_t *q;
+  float *vt, *ct;
+};
+
+// One call of a method. prior: device FP32 prior state (dynamic methods);
+// out: where the first level's membership/weights and final totals live.
+void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out, const lvg_options &o,
+         RunInfo &info) {
+  ensure_ws(g);
+  Workspace &W = *g->ws;
+  cudaStream_t s = g->stream;
+  const size_t S = g->base.span;
+  const double M = g->total_weight / 2;
+  const double R = o.resolution;
+  const float kr = M > 0 ? float(R / (2.0 * M)) : 0.f;
+  const int L = o.maxIterations, P = o.maxPasses;
+  const bool sync = o.deterministic != 0;
+  const int rep = std::max(1, o.repeat);
+  const int K = colors_for(o);
+  if (g->base.colors != K) compute_bins(g, g->base, g->deg.p, g->bins.p, W.binscratch.p, K);
+  uint32_t *ucom = out.q;
+  float *utot = out.vt, *ctot = out.ct;
+  g->stats = lvg_stats{};
+  const unsigned long long launches0 = launch_counter();
+  LVG_CUDA(cudaMemsetAsync(g->ctr.p, 0, sizeof(Counters), s));
+  int l = 0, p = 0;
+  for (int r = 0; r < rep; ++r) {
+    g->events.reset();
+    // Reset buffers, as the reference does before each repetition.
+    LVG_CUDA(cudaMemsetAsync(W.vaff.p, 0, S, s));
+    LVG_CUDA(cudaMemsetAsync(W.vcom.p, 0, S * sizeof(uint32_t), s));
+    LVG_CUDA(cudaMemsetAsync(W.vtot.p, 0, S * sizeof(float), s));
+    cudaEvent_t e0 = g->events.record(s);
+    // fi: initial membership and weights.
+    if (method == LVG_METHOD_STATIC) {
+      launch_init_static(g->base, ucom, utot, ctot, s);
+    } else {
+      if (prior.q != ucom) LVG_CUDA(cudaMemcpyAsync(ucom, prior.q, S * 4, cudaMemcpyDeviceToDevice, s));
+      if (prior.vt != utot) LVG_CUDA(cudaMemcpyAsync(utot, prior.vt, S * 4, cudaMemcpyDeviceToDevice, s));
+      if (prior.ct != ctot) LVG_CUDA(cudaMemcpyAsync(ctot, prior.ct, S * 4, cudaMemcpyDeviceToDevice, s));
+      launch_batch_weights(b.ds, b.dw, b.nd, -1.f, ucom, utot, ctot, s);
+      launch_batch_weights(b.is, b.iw, b.ni, +1.f, ucom, utot, ctot, s);
+    }
+    cudaEvent_t e1 = g->events.record(s);
+    // fm: mark affected vertices.
+    const uint8_t *fa = nullptr;
+    if (method == LVG_METHOD_STATIC || method == LVG_METHOD_NAIVE) {
+      LVG_CUDA(cudaMemsetAsync(W.vaff.p, 1, S, s));
+    } else if (method == LVG_METHOD_FRONTIER) {
+      launch_df_mark(b.ds, b.dd, b.nd, b.is, b.id, b.ni, ucom, W.vaff.p, s);
+    } else {
+      LVG_CUDA(cudaMemsetAsync(W.fv.p, 0, S, s));
+      LVG_CUDA(cudaMemsetAsync(W.fn.p, 0, S, s));
+      LVG_CUDA(cudaMemsetAsync(W.fc.p, 0, S, s));
+      int dlog = 1;
+      if (b.max_group * 2 > 2048) {
+        dlog = global_table_log2(b.max_group);
+        ensure_global_tables(W, size_t(global_table_blocks(b.ni)), dlog, true);
+      }
+      launch_ds_mark(g->base, b.ds, b.dd, b.nd, b.is, b.id, b.iw, b.ni, b.seg, b.ni, ucom, utot, ctot, M, R,
+                     W.fv.p, W.fn.p, W.fc.p, W.gkeys.p, W.gvals.p, W.gfirst.p, dlog, g->ctr.p, s);
+      LVG_CUDA(cudaMemcpyAsync(W.vaff.p, W.fv.p, S, cudaMemcpyDeviceToDevice, s));
+      fa = W.fv.p;
+    }
+    cudaEvent_t e2 = g->events.record(s);
+    cudaEvent_t ep1 = nullptr;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> tl_ev, ta_ev;
+    double E = o.tolerance;
+    Level lv = g->base;
+    uint32_t *com = ucom;
+    const float *tot = utot;
+    int which = 0;
+    for (l = 0, p = 0; M > 0 && P > 0;) {
+      if (p == 1) ep1 = g->events.record(s);
+      const bool first = p == 0;
+      cudaEvent_t a0 = g->events.record(s);
+      const int m = move_phase(g, lv, com, ctot, tot, first ? fa : nullptr, M, kr, L, E, sync);
+      tl_ev.push_back({a0, g->events.record(s)});
+      l += std::max(m, 1);
+      ++p;
+      if (m <= 1 || p >= P) break;
+      const size_t GN = first ? g->base.order : lv.span;
+      LVG_CUDA(cudaMemsetAsync(W.cext.p, 0, (lv.span + 1) * sizeof(uint32_t), s));
+      launch_community_flags(lv, com, W.cext.p, s);
+      exclusive_scan_u32(W.cext.p, W.cext.p, lv.span, &g->ctr.p->cn, W.scan32.p, s);
+      read_counters(g);
+      const size_t CN = g->hctr.p->cn;
+      if (double(CN) / double(GN) >= o.aggregationTolerance) break;
+      launch_lookup(com, W.cext.p, S, s);
+      if (!first) launch_lookup(ucom, W.vcom.p, S, s);
+      cudaEvent_t g0 = g->events.record(s);
+      lv = aggregate(g, lv, com, CN, which, K);
+      ta_ev.push_back({g0, g->events.record(s)});
+      which ^= 1;
+      com = W.vcom.p;
+      tot = W.vtot.p;
+      launch_level_init(CN, W.vtot.p, W.vcom.p, ctot, W.vaff.p, s);
+      E /= o.toleranceDrop;
+    }
+    if (p > 1) launch_lookup(ucom, W.vcom.p, S, s);
+    cudaEvent_t eend = g->events.record(s);
+    LVG_CUDA(cudaStreamSynchronize(s));
+    info.ti += elapsed(e0, e1);
+    info.tm += elapsed(e1, e2);
+    info.tp += elapsed(e2, ep1 ? ep1 : eend);
+    for (auto &pr : tl_ev) info.tl += elapsed(pr.first, pr.second);
+    for (auto &pr : ta_ev) info.ta += elapsed(pr.first, pr.second);
+    info.t += elapsed(e0, eend);
+  }
+  launch_count_flags(W.vaff.p, S, g->ctr.p, s);
+  read_counters(g);
+  info.affected = g->hctr.p->affected;
+  info.iterations = l;
+  info.passes = p;
+  info.t /= rep; info.tm /= rep; info.ti /= rep; info.tp /= rep; info.tl /= rep; info.ta /= rep;
+  g->stats.move_vertices = g->hctr.p->vertices;
+  g->stats.move_edges = g->hctr.p->edges;
+  g->stats.moves = g->hctr.p->moves;
+  g->stats.aggregate_edges = g->hctr.p->agg_edges;
+  g->stats.kernel_launches = launch_counter() - launches0;
+}
+
+// ---------------------------------------------------------------- host-side validation
+
+void check_batch(const lvg_graph *g, const lvg_batch *b, bool need_sorted) {
+  const size_t S = g->base.span;
+  if (!b) return;
+  if ((b->num_deletions && (!b->del_src || !b->del_dst || !b->del_w)) ||
+      (b->num_insertions && (!b->ins_src || !b->ins_dst || !b->ins_w)))
+    throw Error(LVG_EINVAL, "batch: null array with a non-zero count");
+  for (size_t i = 0; i < b->num_deletions; ++i)
+    if (b->del_src[i] >= S || b->del_dst[i] >= S) throw Error(LVG_EINVAL, "batch: deletion id >= span");
+  for (size_t i = 0; i < b->num_insertions; ++i) {
+    if (b->ins_src[i] >= S || b->ins_dst[i] >= S) throw Error(LVG_EINVAL, "batch: insertion id >= span");
+    if (need_sorted && i && b->ins_src[i] < b->ins_src[i - 1])
+      throw Error(LVG_EINVAL, "delta-screening needs insertions sorted by source vertex");
+  }
+}
+
+size_t max_group(const lvg_batch *b) {
+  size_t best = 0, run_len = 0;
+  for (size_t i = 0; i < b->num_insertions; ++i) {
+    run_len = (i && b->ins_src[i] == b->ins_src[i - 1]) ? run_len + 1 : 1;
+    best = std::max(best, run_len);
+  }
+  return best;
+}
+
+void upload_batch(lvg_graph *g, const lvg_batch *b, DBuf<uint32_t> &ds, DBuf<uint32_t> &dd, DBuf<float> &dw,
+                  DBuf<uint32_t> &is, DBuf<uint32_t> &id, DBuf<float> &iw, DBuf<uint32_t> &seg, DBatch &out) {
+  cudaStream_t s = g->stream;
+  out = DBatch{};
+  if (!b) return;
+  out.nd = b->num_deletions;
+  out.ni = b->num_insertions;
+  ds.ensure(out.nd); dd.ensure(out.nd); dw.ensure(out.nd);
+  is.ensure(out.ni); id.ensure(out.ni); iw.ensure(out.ni); seg.ensure(out.ni + 1);
+  if (out.nd) {
+    LVG_CUDA(cudaMemcpyAsync(ds.p, b->del_src, out.nd * 4, cudaMemcpyHostToDevice, s));
+    LVG_CUDA(cudaMemcpyAsync(dd.p, b->del_dst, out.nd * 4, cudaMemcpyHostToDevice, s));
+    LVG_CUDA(cudaMemcpyAsync(dw.p, b->del_w, out.nd * 4, cudaMemcpyHostToDevice, s));
+  }
+  if (out.ni) {
+    LVG_CUDA(cudaMemcpyAsync(is.p, b->ins_src, out.ni * 4, cudaMemcpyHostToDevice, s));
+    LVG_CUDA(cudaMemcpyAsync(id.p, b->ins_dst, out.ni * 4, cudaMemcpyHostToDevice, s));
+    LVG_CUDA(cudaMemcpyAsync(iw.p, b->ins_w, out.ni * 4, cudaMemcpyHostToDevice, s));
+  }
+  out.ds = ds.p; out.dd = dd.p; out.dw = dw.p;
+  out.is = is.p; out.id = id.p; out.iw = iw.p; out.seg = seg.p;
+  out.max_group = max_group(b);
+}
+
+void fill_result(lvg_result *out, const RunInfo &info, size_t span) {
+  out->span = span;
+  out->iterations = info.iterations;
+  out->passes = info.passes;
+  out->time = info.t;
+  out->markingTime = info.tm;
+  out->initializationTime = info.ti;
+  out->firstPassTime = info.tp;
+  out->localMoveTime = info.tl;
+  out->aggregationTime = info.ta;
+  out->affectedVertices = info.affected;
+}
+
+// Download the first-level membership/weights and final totals to the
+// result's host arrays (allocating the ones left NULL).
+void download_result(lvg_graph *g, lvg_result *out, StateRef st) {
+  Workspace &W = *g->ws;
+  cudaStream_t s = g->stream;
+  const size_t S = g->base.span;
+  if (!out->membership) { out->membership = (uint32_t *)std::malloc(S * 4 + 1); out->owned |= 1; }
+  if (!out->vertexWeight) { out->vertexWeight = (double *)std::malloc(S * 8 + 1); out->owned |= 2; }
+  if (!out->communityWeight) { out->communityWeight = (double *)std::malloc(S * 8 + 1); out->owned |= 4; }
+  if (!out->membership || !out->vertexWeight || !out->communityWeight) throw std::bad_alloc();
+  W.stage_a.ensure(S);
+  W.stage_b.ensure(S);
+  launch_f32_to_f64(st.vt, W.stage_a.p, S, s);
+  launch_f32_to_f64(st.ct, W.stage_b.p, S, s);
+  LVG_CUDA(cudaMemcpyAsync(out->membership, st.q, S * 4, cudaMemcpyDeviceToHost, s));
+  LVG_CUDA(cudaMemcpyAsync(out->vertexWeight, W.stage_a.p, S * 8, cudaMemcpyDeviceToHost, s));
+  LVG_CUDA(cudaMemcpyAsync(out->communityWeight, W.stage_b.p, S * 8, cudaMemcpyDeviceToHost, s));
+  LVG_CUDA(cudaStreamSynchronize(s));
+}
+
+void upload_prior(lvg_graph *g, const uint32_t *q, const double *qvtot, const double *qctot, uint32_t *dq,
+                  float *dvt, float *dct) {
+  Workspace &W = *g->ws;
+  cudaStream_t s = g->stream;
+  const size_t S = g->base.span;
+  if (!q || !qvtot || !qctot) throw Error(LVG_EINVAL, "prior state: null array");
+  for (size_t u = 0; u < S; ++u)
+    if (q[u] >= S) throw Error(LVG_EINVAL, "prior membership id >= span");
+  W.stage_a.ensure(S);
+  W.stage_b.ensure(S);
+  LVG_CUDA(cudaMemcpyAsync(dq, q, S * 4, cudaMemcpyHostToDevice, s));
+  LVG_CUDA(cudaMemcpyAsync(W.stage_a.p, qvtot, S * 8, cudaMemcpyHostToDevice, s));
+  LVG_CUDA(cudaMemcpyAsync(W.stage_b.p, qctot, S * 8, cudaMemcpyHostToDevice, s));
+  launch_prior_to_f32(W.stage_a.p, dvt, S, s);
+  launch_prior_to_f32(W.stage_b.p, dct, S, s);
+}
+
+int run_host(lvg_graph *g, int method, const lvg_batch *b, const uint32_t *q, const double *qvtot,
+             const double *qctot, const lvg_options *o, lvg_result *out) {
+  if (!g || !out) return fail(LVG_EINVAL, "null graph or result");
+  return guarded([&] {
+    LVG_CUDA(cudaSetDevice(g->device));
+    lvg_options opt;
+    if (o) opt = *o; else lvg_options_default(&opt);
+    check_batch(g, b, method == LVG_METHOD_DELTA);
+    ensure_ws(g);
+    Workspace &W = *g->ws;
+    DBatch db;
+    upload_batch(g, method == LVG_METHOD_STATIC ? nullptr : b, g->b_ds, g->b_dd, g->b_dw, g->b_is, g->b_id,
+                 g->b_iw, g->b_seg, db);
+    StateRef prior{nullptr, nullptr, nullptr};
+    if (method != LVG_METHOD_STATIC) {
+      W.prior_q.ensure(W.S); W.prior_vt.ensure(W.S); W.prior_ct.ensure(W.S);
+      upload_prior(g, q, qvtot, qctot, W.prior_q.p, W.prior_vt.p, W.prior_ct.p);
+      prior = StateRef{W.prior_q.p, W.prior_vt.p, W.prior_ct.p};
+    }
+    StateRef st{W.ucom.p, W.utot.p, W.ctot.p};
+    RunInfo info;
+    run(g, method, db, prior, st, opt, info);
+    fill_result(out, info, g->base.span);
+    download_result(g, out, st);
+    return LVG_OK;
+  });
+}
+
+}  // namespace
+}  // namespace lvg
+
+// ==================================================================== C-ABI
+
+extern "C" {
+
+const char *lvg_last_error(void) { return lvg::g_err.c_str(); }
+
+void lvg_options_default(lvg_options *o) {
+  if (!o) return;
+  o->repeat = 1;
+  o->resolution = 1;
+  o->tolerance = 1e-2;
+  o->aggregationTolerance = 1.0;
+  o->toleranceDrop = 10;
+  o->maxIterations = 20;
+  o->maxPasses = 10;
+  o->deterministic = 0;
+  o->colors = 0;
+}
+
+int lvg_graph_create(size_t span, const uint64_t *offsets, const uint32_t *keys, const float *weights,
+                     const uint8_t *exists, lvg_graph **out) {
+  if (!out || !offsets || span == 0 || span > 0xFFFFFFFFull) return lvg::fail(LVG_EINVAL, "lvg_graph_create: bad argument");
+  *out = nullptr;
+  const size_t X = offsets[span];
+  if (X && (!keys || !weights)) return lvg::fail(LVG_EINVAL, "lvg_graph_create: null keys/weights");
+  if (offsets[0] != 0) return lvg::fail(LVG_EINVAL, "lvg_graph_create: offsets[0] != 0");
+  size_t order = 0;
+  for (size_t u = 0; u < span; ++u) {
+    if (offsets[u + 1] < offsets[u]) return lvg::fail(LVG_EINVAL, "lvg_graph_create: offsets not monotone");
+    if (offsets[u + 1] - offsets[u] > 0xFFFFFFFFull) return lvg::fail(LVG_EINVAL, "lvg_graph_create: row too long");
+    const bool has = !exists || exists[u];
+    order += has;
+    if (!has && offsets[u + 1] != offsets[u])
+      return lvg::fail(LVG_EINVAL, "lvg_graph_create: absent vertex with edges");
+  }
+  for (size_t i = 0; i < X; ++i)
+    if (keys[i] >= span) return lvg::fail(LVG_EINVAL, "lvg_graph_create: neighbour id >= span");
+  std::unique_ptr<lvg_graph> g(new lvg_graph());
+  int rc = lvg::guarded([&] {
+    LVG_CUDA(cudaGetDevice(&g->device));
+    LVG_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+    cudaStream_t s = g->stream;
+    g->off.ensure(span + 1);
+    g->deg.ensure(span + 1);
+    g->key.ensure(X);
+    g->w.ensure(X);
+    g->bins.ensure(span + 1);
+    LVG_CUDA(cudaMemcpyAsync(g->off.p, offsets, (span + 1) * 8, cudaMemcpyHostToDevice, s));
+    if (X) {
+      LVG_CUDA(cudaMemcpyAsync(g->key.p, keys, X * 4, cudaMemcpyHostToDevice, s));
+      LVG_CUDA(cudaMemcpyAsync(g->w.p, weights, X * 4, cudaMemcpyHostToDevice, s));
+    }
+    if (exists) {
+      g->ex.ensure(span);
+      LVG_CUDA(cudaMemcpyAsync(g->ex.p, exists, span, cudaMemcpyHostToDevice, s));
+    }
+    g->ctr.ensure(1);
+    g->hctr.ensure(1);
+    LVG_CUDA(cudaMemsetAsync(g->ctr.p, 0, sizeof(Counters), s));
+    lvg::Level &b = g->base;
+    b.span = span; b.order = order; b.edges = X;
+    b.off = g->off.p; b.deg = g->deg.p; b.key = g->key.p; b.w = g->w.p; b.ex = exists ? g->ex.p : nullptr;
+    lvg::launch_degrees(b.off, g->deg.p, span, s);
+    lvg::launch_total_weight(b, g->ctr.p, s);
+    lvg::DBuf<uint32_t> scratch;
+    scratch.ensure(lvg::bin_scratch_elems(span + 1, lvg::DEFAULT_COLORS_ASYNC));
+    lvg::compute_bins(g.get(), b, g->deg.p, g->bins.p, scratch.p, lvg::DEFAULT_COLORS_ASYNC);  // synchronises
+    lvg::read_counters(g.get());
+    g->total_weight = g->hctr.p->fp64[0];
+    return LVG_OK;
+  });
+  if (rc != LVG_OK) {
+    if (g->stream) cudaStreamDestroy(g->stream);
+    return rc;
+  }
+  *out = g.release();
+  return LVG_OK;
+}
+
+int lvg_graph_destroy(lvg_graph *g) {
+  if (!g) return LVG_OK;
+  cudaSetDevice(g->device);
+  if (g->stream) cudaStreamSynchronize(g->stream);
+  cudaStream_t s = g->stream;
+  delete g;
+  if (s) cudaStreamDestroy(s);
+  return LVG_OK;
+}
+
+size_t lvg_graph_span(const lvg_graph *g) { return g ? g->base.span : 0; }
+size_t lvg_graph_order(const lvg_graph *g) { return g ? g->base.order : 0; }
+size_t lvg_graph_size(const lvg_graph *g) { return g ? g->base.edges : 0; }
+
+int lvg_static(lvg_graph *x, const lvg_options *o, lvg_result *out) {
+  return lvg::run_host(x, LVG_METHOD_STATIC, nullptr, nullptr, nullptr, nullptr, o, out);
+}
+
+int lvg_naive_dynamic(lvg_graph *y, const lvg_batch *b, const uint32_t *q, const double *qvtot, const double *qctot,
+                      const lvg_options *o, lvg_result *out) {
+  return lvg::run_host(y, LVG_METHOD_NAIVE, b, q, qvtot, qctot, o, out);
+}
+
+int lvg_delta_screening(lvg_graph *y, const lvg_batch *b, const uint32_t *q, const double *qvtot,
+                        const double *qctot, const lvg_options *o, lvg_result *out) {
+  return lvg::run_host(y, LVG_METHOD_DELTA, b, q, qvtot, qctot, o, out);
+}
+
+int lvg_frontier(lvg_graph *y, const lvg_batch *b, const uint32_t *q, const double *qvtot, const double *qctot,
+                 const lvg_options *o, lvg_result *out) {
+  return lvg::run_host(y, LVG_METHOD_FRONTIER, b, q, qvtot, qctot, o, out);
+}
+
+void lvg_result_free(lvg_result *r) {
+  if (!r) return;
+  if (r->owned & 1) std::free(r->membership);
+  if (r->owned & 2) std::free(r->vertexWeight);
+  if (r->owned & 4) std::free(r->communityWeight);
+  if (r->owned & 1) r->membership = nullptr;
+  if (r->owned & 2) r->vertexWeight = nullptr;
+  if (r->owned & 4) r->communityWeight = nullptr;
+  r->owned = 0;
+}
+
+int lvg_edge_weight(lvg_graph *g, double *out) {
+  if (!g || !out) return lvg::fail(LVG_EINVAL, "null argument");
+  *out = g->total_weight;
+  return LVG_OK;
+}
+
+int lvg_modularity(lvg_graph *g, const uint32_t *membership, double M, double R, double *out) {
+  if (!g || !membership || !out) return lvg::fail(LVG_EINVAL, "null argument");
+  return lvg::guarded([&] {
+    LVG_CUDA(cudaSetDevice(g->device));
+    const size_t S = g->base.span;
+    for (size_t u = 0; u < S; ++u)
+      if (membership[u] >= S) throw lvg::Error(LVG_EINVAL, "membership id >= span");
+    lvg::ensure_ws(g);
+    lvg::Workspace &W = *g->ws;
+    cudaStream_t s = g->stream;
+    if (M <= 0) M = g->total_weight / 2;
+    W.ctot64.ensure(S);
+    LVG_CUDA(cudaMemcpyAsync(W.com_next.p, membership, S * 4, cudaMemcpyHostToDevice, s));
+    lvg::launch_modularity(g->base, W.com_next.p, W.ctot64.p, g->ctr.p, s);
+    lvg::launch_sq_sum(W.ctot64.p, S, g->ctr.p, s);
+    lvg::read_counters(g);
+    const double intra = g->hctr.p->fp64[1], sq = g->hctr.p->fp64[2];
+    *out = intra / (2 * M) - R * sq / (4 * M * M);
+    return LVG_OK;
+  });
+}
+
+int lvg_affected_vertices(lvg_graph *y, int method, const lvg_batch *b, const uint32_t *q, const double *qvtot,
+                          const double *qctot, const lvg_options *o, uint8_t *flags, uint8_t *neighbors,
+                          uint8_t *communities) {
+  if (!y || !flags || method < 0 || method > 3) return lvg::fail(LVG_EINVAL, "bad argument");
+  return lvg::guarded([&] {
+    LVG_CUDA(cudaSetDevice(y->device));
+    lvg_options opt;
+    if (o) opt = *o; else lvg_options_default(&opt);
+    opt.maxPasses = 0;  // initialise and mark only
+    opt.repeat = 1;
+    lvg::check_batch(y, b, method == LVG_METHOD_DELTA);
+    lvg::ensure_ws(y);
+    lvg::Workspace &W = *y->ws;
+    lvg::DBatch db;
+    lvg::upload_batch(y, method == LVG_METHOD_STATIC ? nullptr : b, y->b_ds, y->b_dd, y->b_dw, y->b_is, y->b_id,
+                      y->b_iw, y->b_seg, db);
+    lvg::StateRef prior{nullptr, nullptr, nullptr};
+    if (method != LVG_METHOD_STATIC) {
+      W.prior_q.ensure(W.S); W.prior_vt.ensure(W.S); W.prior_ct.ensure(W.S);
+      lvg::upload_prior(y, q, qvtot, qctot, W.prior_q.p, W.prior_vt.p, W.prior_ct.p);
+      prior = lvg::StateRef{W.prior_q.p, W.prior_vt.p, W.prior_ct.p};
+    }
+    lvg::StateRef st{W.ucom.p, W.utot.p, W.ctot.p};
+    lvg::RunInfo info;
+    lvg::run(y, method, db, prior, st, opt, info);
+    const size_t S = y->base.span;
+    LVG_CUDA(cudaMemcpyAsync(flags, W.vaff.p, S, cudaMemcpyDeviceToHost, y->stream));
+    if (method == LVG_METHOD_DELTA && neighbors) LVG_CUDA(cudaMemcpyAsync(neighbors, W.fn.p, S, cudaMemcpyDeviceToHost, y->stream));
+    if (method == LVG_METHOD_DELTA && communities) LVG_CUDA(cudaMemcpyAsync(communities, W.fc.p, S, cudaMemcpyDeviceToHost, y->stream));
+    LVG_CUDA(cudaStreamSynchronize(y->stream));
+    return LVG_OK;
+  });
+}
+
+int lvg_aggregate(lvg_graph *g, const uint32_t *membership, uint32_t *renumbered, size_t *num_communities,
+                  uint64_t *offsets, uint32_t *keys, double *weights) {
+  if (!g || !membership || !renumbered || !num_communities || !offsets) return lvg::fail(LVG_EINVAL, "null argument");
+  return lvg::guarded([&] {
+    LVG_CUDA(cudaSetDevice(g->device));
+    const size_t S = g->base.span, X = g->base.edges;
+    for (size_t u = 0; u < S; ++u)
+      if (membership[u] >= S) throw lvg::Error(LVG_EINVAL, "membership id >= span");
+    if (X && (!keys || !weights)) throw lvg::Error(LVG_EINVAL, "null keys/weights");
+    lvg::ensure_ws(g);
+    lvg::Workspace &W = *g->ws;
+    cudaStream_t s = g->stream;
+    LVG_CUDA(cudaMemcpyAsync(W.ucom.p, membership, S * 4, cudaMemcpyHostToDevice, s));
+    LVG_CUDA(cudaMemsetAsync(W.cext.p, 0, (S + 1) * sizeof(uint32_t), s));
+    lvg::launch_community_flags(g->base, W.ucom.p, W.cext.p, s);
+    lvg::exclusive_scan_u32(W.cext.p, W.cext.p, S, &g->ctr.p->cn, W.scan32.p, s);
+    lvg::read_counters(g);
+    const size_t CN = g->hctr.p->cn;
+    lvg::launch_lookup(W.ucom.p, W.cext.p, S, s);
+    lvg::Level nl = lvg::aggregate(g, g->base, W.ucom.p, CN, 0, 1);
+    std::vector<uint64_t> yoff(CN + 1);
+    std::vector<uint32_t> ydeg(CN + 1), yk(X ? X : 1);
+    std::vector<float> yw(X ? X : 1);
+    LVG_CUDA(cudaMemcpyAsync(renumbered, W.ucom.p, S * 4, cudaMemcpyDeviceToHost, s));
+    LVG_CUDA(cudaMemcpyAsync(yoff.data(), nl.off, (CN + 1) * 8, cudaMemcpyDeviceToHost, s));
+    if (CN) LVG_CUDA(cudaMemcpyAsync(ydeg.data(), nl.deg, CN * 4, cudaMemcpyDeviceToHost, s));
+    if (X) {
+      LVG_CUDA(cudaMemcpyAsync(yk.data(), nl.key, X * 4, cudaMemcpyDeviceToHost, s));
+      LVG_CUDA(cudaMemcpyAsync(yw.data(), nl.w, X * 4, cudaMemcpyDeviceToHost, s));
+    }
+    LVG_CUDA(cudaStreamSynchronize(s));
+    *num_communities = CN;
+    uint64_t k = 0;
+    for (size_t c = 0; c < CN; ++c) {
+      offsets[c] = k;
+      for (uint32_t j = 0; j < ydeg[c]; ++j, ++k) {
+        keys[k] = yk[yoff[c] + j];
+        weights[k] = yw[yoff[c] + j];
+      }
+    }
+    offsets[CN] = k;
+    return LVG_OK;
+  });
+}
+
+void *lvg_host_alloc(size_t bytes) {
+  void *p = nullptr;
+  if (cudaMallocHost(&p, bytes ? bytes : 1) != cudaSuccess) return nullptr;
+  return p;
+}
+
+void lvg_host_free(void *p) {
+  if (p) cudaFreeHost(p);
+}
+
+int lvg_set_profiling(lvg_graph *g, int enable) {
+  if (!g) return lvg::fail(LVG_EINVAL, "null graph");
+  g->profiling = enable != 0;
+  return LVG_OK;
+}
+
+int lvg_get_stats(const lvg_graph *g, lvg_stats *out) {
+  if (!g || !out) return lvg::fail(LVG_EINVAL, "null argument");
+  *out = g->stats;
+  return LVG_OK;
+}
+
+int lvg_state_create(lvg_graph *g, lvg_state **out) {
+  if (!g || !out) return lvg::fail(LVG_EINVAL, "null argument");
+  *out = nullptr;
+  std::unique_ptr<lvg_state> st(new lvg_state());
+  int rc = lvg::guarded([&] {
+    LVG_CUDA(cudaSetDevice(g->device));
+    const size_t S = g->base.span;
+    st->g = g;
+    st->q.ensure(S); st->vt.ensure(S); st->ct.ensure(S);
+    LVG_CUDA(cudaMemsetAsync(st->q.p, 0, S * 4, g->stream));
+    LVG_CUDA(cudaMemsetAsync(st->vt.p, 0, S * 4, g->stream));
+    LVG_CUDA(cudaMemsetAsync(st->ct.p, 0, S * 4, g->stream));
+    LVG_CUDA(cudaStreamSynchronize(g->stream));
+    return LVG_OK;
+  });
+  if (rc == LVG_OK) *out = st.release();
+  return rc;
+}
+
+int lvg_state_set(lvg_state *st, const uint32_t *q, const double *qvtot, const double *qctot) {
+  if (!st) return lvg::fail(LVG_EINVAL, "null state");
+  return lvg::guarded([&] {
+    lvg_graph *g = st->g;
+    LVG_CUDA(cudaSetDevice(g->device));
+    lvg::ensure_ws(g);
+    lvg::upload_prior(g, q, qvtot, qctot, st->q.p, st->vt.p, st->ct.p);
+    LVG_CUDA(cudaStreamSynchronize(g->stream));
+    return LVG_OK;
+  });
+}
+
+int lvg_state_get(const lvg_state *st, uint32_t *membership, double *vtot, double *ctot) {
+  if (!st) return lvg::fail(LVG_EINVAL, "null state");
+  return lvg::guarded([&] {
+    lvg_graph *g = st->g;
+    LVG_CUDA(cudaSetDevice(g->device));
+    lvg::ensure_ws(g);
+    lvg::Workspace &W = *g->ws;
+    cudaStream_t s = g->stream;
+    const size_t S = g->base.span;
+    W.stage_a.ensure(S);
+    W.stage_b.ensure(S);
+    if (membership) LVG_CUDA(cudaMemcpyAsync(membership, st->q.p, S * 4, cudaMemcpyDeviceToHost, s));
+    if (vtot) {
+      lvg::launch_f32_to_f64(st->vt.p, W.stage_a.p, S, s);
+      LVG_CUDA(cudaMemcpyAsync(vtot, W.stage_a.p, S * 8, cudaMemcpyDeviceToHost, s));
+    }
+    if (ctot) {
+      lvg::launch_f32_to_f64(st->ct.p, W.stage_b.p, S, s);
+      LVG_CUDA(cudaMemcpyAsync(ctot, W.stage_b.p, S * 8, cudaMemcpyDeviceToHost, s));
+    }
+    LVG_CUDA(cudaStreamSynchronize(s));
+    return LVG_OK;
+  });
+}
+
+int lvg_state_destroy(lvg_state *st) {
+  if (!st) return LVG_OK;
+  cudaSetDevice(st->g->device);
+  cudaStreamSynchronize(st->g->stream);
+  delete st;
+  return LVG_OK;
+}
+
+int lvg_device_batch_create(lvg_graph *g, const lvg_batch *b, lvg_device_batch **out) {
+  if (!g || !b || !out) return lvg::fail(LVG_EINVAL, "null argument");
+  *out = nullptr;
+  std::unique_ptr<lvg_device_batch> db(new lvg_device_batch());
+  int rc = lvg::guarded([&] {
+    LVG_CUDA(cudaSetDevice(g->device));
+    lvg::check_batch(g, b, false);
+    db->g = g;
+    lvg::upload_batch(g, b, db->ds, db->dd, db->dw, db->is, db->id, db->iw, db->seg, db->b);
+    LVG_CUDA(cudaStreamSynchronize(g->stream));
+    // remember whether the insertions are source-sorted (delta-screening needs it)
+    bool sorted = true;
+    for (size_t i = 1; i < b->num_insertions; ++i) sorted &= b->ins_src[i] >= b->ins_src[i - 1];
+    if (!sorted) db->b.max_group = ~size_t(0);
+    return LVG_OK;
+  });
+  if (rc == LVG_OK) *out = db.release();
+  return rc;
+}
+
+int lvg_device_batch_destroy(lvg_device_batch *b) {
+  if (!b) return LVG_OK;
+  cudaSetDevice(b->g->device);
+  cudaStreamSynchronize(b->g->stream);
+  delete b;
+  return LVG_OK;
+}
+
+int lvg_run_resident(lvg_graph *g, int method, const lvg_device_batch *b, const lvg_state *prior, lvg_state *out,
+                     const lvg_options *o, lvg_result *info) {
+  if (!g || !out || method < 0 || method > 3) return lvg::fail(LVG_EINVAL, "bad argument");
+  if (method != LVG_METHOD_STATIC && !prior) return lvg::fail(LVG_EINVAL, "dynamic methods need a prior state");
+  if ((b && b->g != g) || (prior && prior->g != g) || out->g != g)
+    return lvg::fail(LVG_EINVAL, "state/batch belongs to another graph");
+  if (method == LVG_METHOD_DELTA && b && b->b.max_group == ~size_t(0))
+    return lvg::fail(LVG_EINVAL, "delta-screening needs insertions sorted by source vertex");
+  return lvg::guarded([&] {
+    LVG_CUDA(cudaSetDevice(g->device));
+    lvg_options opt;
+    if (o) opt = *o; else lvg_options_default(&opt);
+    lvg::DBatch db;
+    if (b && method != LVG_METHOD_STATIC) db = b->b;
+    lvg::StateRef pr{nullptr, nullptr, nullptr};
+    if (prior) pr = lvg::StateRef{prior->q.p, prior->vt.p, prior->ct.p};
+    lvg::StateRef st{out->q.p, out->vt.p, out->ct.p};
+    lvg::RunInfo ri;
+    lvg::run(g, method, db, pr, st, opt, ri);
+    if (info) lvg::fill_result(info, ri, g->base.span);
+    return LVG_OK;
+  });
+}
+
+}  // extern "C"

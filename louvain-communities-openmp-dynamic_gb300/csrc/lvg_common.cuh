@@ -1,0 +1,133 @@
+// lvg_common.cuh — shared types, error handling and device helpers.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+
+#include "louvain_gb300.h"
+
+namespace lvg {
+
+// ------------------------------------------------------------------ errors
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+#define LVG_CUDA(call)                                                                          \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess) {                                                                    \
+      throw ::lvg::Error(e_ == cudaErrorMemoryAllocation ? LVG_ENOMEM : LVG_ECUDA,              \
+                         std::string(#call) + ": " + cudaGetErrorString(e_) + " (" __FILE__ ":" + \
+                             std::to_string(__LINE__) + ")");                                   \
+    }                                                                                           \
+  } while (0)
+
+// Kernels launched by the calling thread (for the launch count of a call).
+inline unsigned long long &launch_counter() {
+  static thread_local unsigned long long c = 0;
+  return c;
+}
+
+#define LVG_CHECK_LAUNCH()            \
+  do {                                \
+    ++::lvg::launch_counter();        \
+    LVG_CUDA(cudaGetLastError());     \
+  } while (0)
+
+// ------------------------------------------------------------------ constants
+
+constexpr uint32_t EMPTY = 0xFFFFFFFFu;  // empty hash slot
+constexpr int WARP = 32;
+constexpr int NUM_SMS_HINT = 152;
+
+// Fixed-point scale of the per-iteration gain sum (exact, order free).
+constexpr double GAIN_FIX = 65536.0;
+
+// Device error flags (bit set in Engine::d_err).
+constexpr uint32_t ERR_TABLE_FULL = 1u;
+
+// Degree bins of the per-vertex (and per-community) reduce kernels.
+//   bin 0: degree 0 (nothing to scan)
+//   bins 1-4: sub-warp tiles of 4/8/16/32 lanes, degree <= tile
+//   bins 5-8: one warp, shared table of 128..1024 slots, degree <= 64..512
+//   bins 9-10: one block, shared table of 4096 / 16384 slots, degree <= 2048 / 8192
+//   bin 11: one block, global-memory table, degree > 8192
+constexpr int NUM_BINS = 12;
+__host__ __device__ inline int degree_bin(uint64_t d) {
+  if (d == 0) return 0;
+  if (d <= 4) return 1;
+  if (d <= 8) return 2;
+  if (d <= 16) return 3;
+  if (d <= 32) return 4;
+  if (d <= 64) return 5;
+  if (d <= 128) return 6;
+  if (d <= 256) return 7;
+  if (d <= 512) return 8;
+  if (d <= 2048) return 9;
+  if (d <= 8192) return 10;
+  return 11;
+}
+constexpr uint64_t BIN_MAX_DEGREE[NUM_BINS] = {0, 4, 8, 16, 32, 64, 128, 256, 512, 2048, 8192, ~0ull};
+
+// Colour classes of the local-moving sweeps. Each iteration visits the
+// classes one after another, so a vertex sees the moves its neighbours in
+// earlier classes made in the same iteration (as in the reference's
+// sequential sweep). The class of a vertex is a hash of its id.
+constexpr int MAX_COLORS = 32;
+constexpr int DEFAULT_COLORS_ASYNC = 8;
+constexpr int DEFAULT_COLORS_SYNC = 16;
+constexpr int MAX_BUCKETS = MAX_COLORS * NUM_BINS;
+__host__ __device__ inline uint32_t vertex_color(uint32_t u, uint32_t k) {
+  uint32_t h = u * 0x9E3779B1u;
+  h ^= h >> 16;
+  return h % k;
+}
+
+// ------------------------------------------------------------------ device helpers
+
+__device__ __forceinline__ uint32_t hash_slot(uint32_t k, uint32_t mask) {
+  return (k * 0x9E3779B1u) & mask;
+}
+
+// Multiplicative hash using the high bits, for power-of-two capacities >= 2.
+__device__ __forceinline__ uint32_t hash_hi(uint32_t k, int log2cap) {
+  return (k * 0x9E3779B1u) >> (32 - log2cap);
+}
+
+// FP32 gain of moving a vertex (weight wu, links kc to c and kd to its own d)
+// into community c: M times the reference's deltaModularity
+// (inc/properties.hxx:253-256). Written with explicit round-to-nearest
+// intrinsics so no FMA contraction changes the result; the oracle's
+// orc_louvain_sync evaluates the same operations in the same order.
+__device__ __forceinline__ float gain_f32(float kc, float kd, float wu, float tc, float td, float kr) {
+  float a = __fsub_rn(kc, kd);
+  float b = __fadd_rn(wu, tc);
+  float c = __fsub_rn(b, td);
+  float d = __fmul_rn(wu, c);
+  float e = __fmul_rn(d, kr);
+  return __fsub_rn(a, e);
+}
+
+// Candidate order: larger gain first, then lower community id.
+__device__ __forceinline__ bool better(float g, uint32_t c, float bg, uint32_t bc) {
+  return g > bg || (g == bg && c < bc);
+}
+
+// g * 2^16 is exact in FP32, so rounding it to an integer equals the oracle's
+// llrint((double)g * 65536.0).
+__device__ __forceinline__ unsigned long long gain_to_fix(float g) {
+  return (unsigned long long)__float2ll_rn(g * 65536.0f);
+}
+
+template <class T>
+__device__ __forceinline__ T ld_relaxed(const T *p) {
+  return *((const volatile T *)p);
+}
+
+}  // namespace lvg

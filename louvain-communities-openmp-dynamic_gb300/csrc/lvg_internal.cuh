@@ -1,0 +1,156 @@
+// lvg_internal.cuh — device data layout and kernel launchers shared by the
+// translation units of liblouvain_gb300.so.
+#pragma once
+#include "lvg_common.cuh"
+
+namespace lvg {
+
+// A graph level in HBM: gapped CSR (row u = key/w[off[u] .. off[u]+deg[u])),
+// the layout of the reference's DiGraphCsr (inc/Graph.hxx:384-640). Level 0 is
+// the uploaded graph (ex = existence flags); aggregated levels have every
+// vertex present (ex = nullptr), as the reference's DiGraphCsr::hasVertex.
+struct Level {
+  size_t span = 0, order = 0, edges = 0;
+  uint64_t *off = nullptr;
+  uint32_t *deg = nullptr;
+  uint32_t *key = nullptr;
+  float *w = nullptr;
+  const uint8_t *ex = nullptr;
+  // Vertices grouped by (colour class, degree bin), ascending id within a
+  // group: group (k, b) is bins[bin_start[k*NUM_BINS+b] .. bin_start[k*NUM_BINS+b+1]).
+  uint32_t *bins = nullptr;
+  int colors = 1;
+  size_t bin_start[MAX_BUCKETS + 1] = {};
+  uint64_t bin_maxdeg[NUM_BINS] = {};
+  size_t bucket_begin(int k, int b) const { return bin_start[k * NUM_BINS + b]; }
+  size_t bucket_size(int k, int b) const { return bin_start[k * NUM_BINS + b + 1] - bin_start[k * NUM_BINS + b]; }
+  size_t color_begin(int k) const { return bin_start[k * NUM_BINS]; }
+  size_t color_end(int k) const { return bin_start[(k + 1) * NUM_BINS]; }
+};
+
+// Device counters block (one allocation; mirrored in pinned host memory).
+struct Counters {
+  unsigned long long el_fix;     // Σ best gains, 2^-16 fixed point
+  unsigned long long vertices;   // processed vertices
+  unsigned long long edges;      // scanned edges
+  unsigned long long moves;      // moved vertices
+  unsigned long long agg_edges;  // edges read by aggregation
+  unsigned long long affected;   // residual affected flags
+  unsigned int err;              // ERR_* bits
+  unsigned int cn;               // community count
+  double fp64[4];                // FP64 reductions (total weight, modularity terms)
+};
+
+// Arguments of the local-moving kernels (inc/louvain.hxx:588-609).
+struct MoveArgs {
+  const uint64_t *off;
+  const uint32_t *deg;
+  const uint32_t *key;
+  const float *w;
+  const uint32_t *list;  // vertices of one degree bin
+  uint32_t count;
+  uint32_t *vcom;        // membership (async: read/write; sync: snapshot, read only)
+  float *ctot;           // community totals (async: read/write; sync: snapshot)
+  uint32_t *dec;         // sync: decided community per vertex (EMPTY = stay)
+  uint8_t *vaff;         // affected flags
+  uint8_t *mark;         // sync: neighbour marks of this iteration
+  const uint8_t *fa;     // may the vertex move (delta-screening pass 0), or nullptr
+  const float *vtot;     // vertex weights
+  float kr;              // R / (2M)
+  Counters *ctr;
+  uint32_t *gkeys;       // global tables (bin 11): [grid][gcap]
+  float *gvals;
+  int glog2;             // log2 of the global table capacity
+};
+
+// Arguments of the aggregation kernels (inc/louvain.hxx:897-912, 987-992).
+struct AggArgs {
+  const uint64_t *off;   // input level
+  const uint32_t *deg;
+  const uint32_t *key;
+  const float *w;
+  const uint32_t *vcom;  // renumbered membership of the input level
+  const uint32_t *coff;  // community -> members CSR
+  const uint32_t *cmem;
+  const uint32_t *list;  // communities of one total-degree bin
+  uint32_t count;
+  const uint64_t *yoff;  // output row capacity offsets (scan of total degree)
+  uint32_t *ydeg;        // output row degrees
+  uint32_t *ykey;
+  float *yw;
+  float *vtot;           // output level's vertex weights (row sums)
+  Counters *ctr;
+  uint32_t *gkeys;
+  float *gvals;
+  int glog2;
+};
+
+// ---------------------------------------------------------------- scans (lvg_scan.cu)
+size_t scan_scratch_elems(size_t n);
+// Exclusive scan; out may alias in. If total != nullptr the sum is written there.
+void exclusive_scan_u32(const uint32_t *in, uint32_t *out, size_t n, uint32_t *total, uint32_t *scratch,
+                        cudaStream_t s);
+void exclusive_scan_u64(const uint64_t *in, uint64_t *out, size_t n, uint64_t *total, uint64_t *scratch,
+                        cudaStream_t s);
+// Stable multi-split of items [0,n) into `list` by (colour class of the id,
+// degree bin), colour-major, ascending id within a group; items with
+// ex[i] == 0 (ex != nullptr) are left out. Writes the colors*NUM_BINS+1 group
+// starts and the per-bin max degree to the host arrays (synchronises).
+constexpr int BIN_CHUNK = 2048;
+size_t bin_scratch_elems(size_t n, int colors);
+size_t bin_host_elems(int colors);
+void bin_items_u32(const uint32_t *deg, const uint8_t *ex, size_t n, int colors, uint32_t *list, size_t *bin_start,
+                   uint64_t *bin_maxdeg, uint32_t *scratch, uint32_t *host_pinned, cudaStream_t s);
+void bin_items_u64(const uint64_t *deg, const uint8_t *ex, size_t n, int colors, uint32_t *list,
+                   size_t *bin_start, uint64_t *bin_maxdeg, uint32_t *scratch, uint32_t *host_pinned,
+                   cudaStream_t s);
+
+// ---------------------------------------------------------------- element kernels (lvg_kernels.cu)
+int grid_for(size_t n, int block, int max_blocks_per_sm = 8);
+void launch_degrees(const uint64_t *off, uint32_t *deg, size_t span, cudaStream_t s);
+void launch_fill_u8(uint8_t *p, uint8_t v, size_t n, cudaStream_t s);
+void launch_init_static(const Level &g, uint32_t *ucom, float *utot, float *ctot, cudaStream_t s);
+void launch_total_weight(const Level &g, Counters *ctr, cudaStream_t s);  // -> ctr->fp64[0]
+void launch_prior_to_f32(const double *src, float *dst, size_t n, cudaStream_t s);
+void launch_f32_to_f64(const float *src, double *dst, size_t n, cudaStream_t s);
+void launch_batch_weights(const uint32_t *src, const float *w, size_t n, float sign, const uint32_t *vcom,
+                          float *vtot, float *ctot, cudaStream_t s);
+void launch_df_mark(const uint32_t *ds, const uint32_t *dd, size_t nd, const uint32_t *is, const uint32_t *id,
+                    size_t ni, const uint32_t *vcom, uint8_t *vaff, cudaStream_t s);
+void launch_ds_mark(const Level &g, const uint32_t *ds, const uint32_t *dd, size_t nd, const uint32_t *is,
+                    const uint32_t *id, const float *iw, size_t ni, const uint32_t *seg, size_t nseg,
+                    const uint32_t *vcom, const float *vtot, const float *ctot, double M, double R,
+                    uint8_t *vertices, uint8_t *neighbors, uint8_t *communities, uint32_t *gkeys, float *gvals,
+                    uint32_t *gfirst, int glog2, Counters *ctr, cudaStream_t s);
+void launch_clear_isolated(const uint32_t *list, size_t n, uint8_t *vaff, const uint8_t *fa, cudaStream_t s);
+void launch_merge_marks(uint8_t *vaff, uint8_t *mark, size_t n, cudaStream_t s);
+// Deterministic mode: apply the decisions of one colour class (list of its vertices).
+void launch_apply_moves(const uint32_t *list, size_t n, uint32_t *dec, uint32_t *vcom, float *ctot,
+                        const float *vtot, cudaStream_t s);
+void launch_community_flags(const Level &g, const uint32_t *vcom, uint32_t *cext, cudaStream_t s);
+void launch_lookup(uint32_t *a, const uint32_t *map, size_t n, cudaStream_t s);  // a[u] = map[a[u]]
+void launch_community_sizes(const Level &g, const uint32_t *vcom, uint32_t *csize, uint64_t *ctdeg,
+                            cudaStream_t s);
+void launch_community_scatter(const Level &g, const uint32_t *vcom, const uint32_t *coff, uint32_t *ccur,
+                              uint32_t *cmem, cudaStream_t s);
+void launch_level_init(size_t n, const float *vtot, uint32_t *vcom, float *ctot, uint8_t *vaff, cudaStream_t s);
+void launch_count_flags(const uint8_t *f, size_t n, Counters *ctr, cudaStream_t s);
+void launch_modularity(const Level &g, const uint32_t *memb, double *ctot64, Counters *ctr, cudaStream_t s);
+void launch_sq_sum(const double *x, size_t n, Counters *ctr, cudaStream_t s);  // -> ctr->fp64[2]
+
+// ---------------------------------------------------------------- local moving (lvg_move.cu)
+// Launch the move kernel of degree bin b over a.list[0..a.count).
+void launch_move_bin(int b, bool sync, const MoveArgs &a, cudaStream_t s);
+
+// ---------------------------------------------------------------- aggregation (lvg_aggregate.cu)
+void launch_aggregate_bin(int b, const AggArgs &a, cudaStream_t s);
+
+// Global-table capacity (log2) for a maximum degree.
+inline int global_table_log2(uint64_t maxdeg) {
+  int l = 1;
+  while ((uint64_t(1) << l) < 2 * maxdeg) ++l;
+  return l;
+}
+int global_table_blocks(size_t count);
+
+}  // namespace lvg

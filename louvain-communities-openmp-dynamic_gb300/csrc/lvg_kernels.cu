@@ -1,0 +1,550 @@
+// lvg_kernels.cu — initialisation, batch-update, marking, renumbering,
+// community-CSR and modularity kernels.
+#include "lvg_internal.cuh"
+
+namespace lvg {
+namespace {
+
+int g_sms = 0;
+int sms() {
+  if (!g_sms) {
+    int dev = 0;
+    LVG_CUDA(cudaGetDevice(&dev));
+    LVG_CUDA(cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev));
+  }
+  return g_sms;
+}
+
+#define GRID_STRIDE(i, n) for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < (n); i += size_t(gridDim.x) * blockDim.x)
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ void block_add_double(double v, double *dst) {
+  __shared__ double red[32];
+  v = warp_sum_d(v);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    double t = lane < int(blockDim.x >> 5) ? red[lane] : 0.0;
+    t = warp_sum_d(t);
+    if (lane == 0 && t != 0.0) atomicAdd(dst, t);
+  }
+}
+
+__global__ void degrees_kernel(const uint64_t *off, uint32_t *deg, size_t n) {
+  GRID_STRIDE(u, n) deg[u] = uint32_t(off[u + 1] - off[u]);
+}
+
+// louvainVertexWeightsOmpW (inc/louvain.hxx:210) + louvainInitializeOmpW
+// (:285) for level 0: one warp per vertex (lane-strided rows).
+__global__ void init_static_kernel(const uint64_t *off, const uint32_t *deg, const float *w, const uint8_t *ex,
+                                   size_t n, uint32_t *ucom, float *utot, float *ctot) {
+  const size_t warps = size_t(gridDim.x) * blockDim.x / 32;
+  const int lane = threadIdx.x & 31;
+  for (size_t u = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32; u < n; u += warps) {
+    const bool has = !ex || ex[u];
+    float s = 0.f;
+    if (has) {
+      const uint64_t o = off[u];
+      const uint32_t d = deg[u];
+      for (uint32_t j = lane; j < d; j += 32) s += w[o + j];
+#pragma unroll
+      for (int k = 16; k > 0; k >>= 1) s += __shfl_xor_sync(0xffffffffu, s, k);
+    }
+    if (lane == 0) {
+      ucom[u] = has ? uint32_t(u) : 0u;
+      utot[u] = s;
+      ctot[u] = s;
+    }
+  }
+}
+
+__global__ void total_weight_kernel(const float *w, size_t m, double *dst) {
+  double s = 0;
+  GRID_STRIDE(i, m) s += (double)w[i];
+  block_add_double(s, dst);
+}
+
+__global__ void prior_to_f32_kernel(const double *src, float *dst, size_t n) {
+  GRID_STRIDE(i, n) dst[i] = float(src[i]);
+}
+
+__global__ void f32_to_f64_kernel(const float *src, double *dst, size_t n) {
+  GRID_STRIDE(i, n) dst[i] = double(src[i]);
+}
+
+// louvainUpdateWeightsFromOmpU (inc/louvain.hxx:374-388): per directed batch
+// edge, the source's weight and its community's total move by the weight.
+__global__ void batch_weights_kernel(const uint32_t *src, const float *w, size_t n, float sign,
+                                     const uint32_t *vcom, float *vtot, float *ctot) {
+  GRID_STRIDE(i, n) {
+    const uint32_t u = src[i];
+    const float x = sign * w[i];
+    atomicAdd(&vtot[u], x);
+    atomicAdd(&ctot[vcom[u]], x);
+  }
+}
+
+// louvainAffectedVerticesFrontierOmpW (inc/louvain.hxx:1606-1624).
+__global__ void df_mark_kernel(const uint32_t *ds, const uint32_t *dd, size_t nd, const uint32_t *is,
+                               const uint32_t *id, size_t ni, const uint32_t *vcom, uint8_t *vaff) {
+  GRID_STRIDE(i, nd + ni) {
+    if (i < nd) {
+      if (vcom[ds[i]] == vcom[dd[i]]) vaff[ds[i]] = 1;
+    } else {
+      const size_t j = i - nd;
+      if (vcom[is[j]] != vcom[id[j]]) vaff[is[j]] = 1;
+    }
+  }
+}
+
+// Delta-screening, deletions (inc/louvain.hxx:1448-1456).
+__global__ void ds_del_kernel(const uint32_t *ds, const uint32_t *dd, size_t nd, const uint32_t *vcom,
+                              uint8_t *vertices, uint8_t *neighbors, uint8_t *communities) {
+  GRID_STRIDE(i, nd) {
+    const uint32_t u = ds[i], v = dd[i];
+    if (vcom[u] != vcom[v]) continue;
+    vertices[u] = 1;
+    neighbors[u] = 1;
+    communities[vcom[v]] = 1;
+  }
+}
+
+// Segment heads of the source-sorted insertions.
+__global__ void ds_heads_kernel(const uint32_t *is, size_t ni, uint32_t *seg, unsigned int *nseg) {
+  GRID_STRIDE(i, ni) {
+    if (i == 0 || is[i] != is[i - 1]) seg[atomicAdd(nseg, 1u)] = uint32_t(i);
+  }
+}
+
+__device__ __forceinline__ double delta_modularity(double vcout, double vdout, double vtot, double ctot,
+                                                   double dtot, double M, double R) {
+  return (vcout - vdout) / M - R * vtot * (vtot + ctot - dtot) / (2 * M * M);
+}
+
+// Delta-screening, insertions (inc/louvain.hxx:1457-1479): one block per
+// source; the inserted cross-community edges are merged per community, the
+// best community is chosen by the reference's FP64 ΔQ with its tie rule
+// (first community in batch order wins), and if the gain is positive the
+// source, its neighbours and that community are flagged. The FP64 here is
+// batch sized; it makes the flags match the reference bit for bit.
+constexpr int DS_BLOCK = 128;
+constexpr int DS_LOG = 11;  // shared table: 2048 slots, sources with <= 1024 insertions
+__global__ void __launch_bounds__(DS_BLOCK) ds_ins_kernel(const uint32_t *is, const uint32_t *id, const float *iw,
+                                                          size_t ni, const uint32_t *seg, const unsigned int *nseg,
+                                                          const uint32_t *vcom, const float *vtot,
+                                                          const float *ctot, double M, double R, uint8_t *vertices,
+                                                          uint8_t *neighbors, uint8_t *communities,
+                                                          uint32_t *gkeys, float *gvals, uint32_t *gfirst, int glog2,
+                                                          Counters *ctr) {
+  __shared__ uint32_t skeys[1 << DS_LOG];
+  __shared__ float svals[1 << DS_LOG];
+  __shared__ uint32_t sfirst[1 << DS_LOG];
+  __shared__ double rb[DS_BLOCK / 32];
+  __shared__ uint32_t rf[DS_BLOCK / 32], rc[DS_BLOCK / 32];
+  const unsigned ns = *nseg;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (unsigned sidx = blockIdx.x; sidx < ns; sidx += gridDim.x) {
+    const size_t s0 = seg[sidx];
+    const uint32_t u = is[s0];
+    // segment end: first index with a larger source (the batch is sorted)
+    size_t lo = s0, hi = ni;
+    while (lo < hi) {
+      size_t mid = (lo + hi) >> 1;
+      if (is[mid] <= u) lo = mid + 1; else hi = mid;
+    }
+    const size_t s1 = lo, len = s1 - s0;
+    const bool global = len * 2 > (size_t(1) << DS_LOG);
+    const int lg = global ? glog2 : DS_LOG;
+    const uint32_t cap = 1u << lg, mask = cap - 1u;
+    uint32_t *keys = global ? gkeys + size_t(blockIdx.x) * cap : skeys;
+    float *vals = global ? gvals + size_t(blockIdx.x) * cap : svals;
+    uint32_t *first = global ? gfirst + size_t(blockIdx.x) * cap : sfirst;
+    for (uint32_t s = threadIdx.x; s < cap; s += DS_BLOCK) { keys[s] = EMPTY; vals[s] = 0.f; first[s] = 0xffffffffu; }
+    __syncthreads();
+    const uint32_t d = vcom[u];
+    bool ok = true;
+    for (size_t j = s0 + threadIdx.x; j < s1; j += DS_BLOCK) {
+      const uint32_t c = vcom[id[j]];
+      if (c == d) continue;
+      uint32_t sl = hash_hi(c, lg);
+      bool done = false;
+      for (uint32_t probe = 0; probe <= mask && !done; ++probe) {
+        uint32_t k = keys[sl];
+        if (k == EMPTY) {
+          uint32_t prev = atomicCAS(&keys[sl], EMPTY, c);
+          k = prev == EMPTY ? c : prev;
+        }
+        if (k == c) {
+          atomicAdd(&vals[sl], iw[j]);
+          atomicMin(&first[sl], uint32_t(j - s0));
+          done = true;
+        }
+        sl = (sl + 1u) & mask;
+      }
+      ok &= done;
+    }
+    __syncthreads();
+    const double vu = vtot[u], td = ctot[d];
+    double be = 0;
+    uint32_t bf = 0xffffffffu, bc = 0;
+    for (uint32_t s = threadIdx.x; s < cap; s += DS_BLOCK) {
+      const uint32_t c = keys[s];
+      if (c == EMPTY) continue;
+      const double e = delta_modularity((double)vals[s], 0.0, vu, (double)ctot[c], td, M, R);
+      if (e > be || (e == be && e > 0 && first[s] < bf)) { be = e; bf = first[s]; bc = c; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double oe = __shfl_xor_sync(0xffffffffu, be, o);
+      const uint32_t of = __shfl_xor_sync(0xffffffffu, bf, o);
+      const uint32_t oc = __shfl_xor_sync(0xffffffffu, bc, o);
+      if (oe > be || (oe == be && oe > 0 && of < bf)) { be = oe; bf = of; bc = oc; }
+    }
+    if (lane == 0) { rb[wid] = be; rf[wid] = bf; rc[wid] = bc; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double e = 0;
+      uint32_t f = 0xffffffffu, c = 0;
+      for (int k = 0; k < DS_BLOCK / 32; ++k)
+        if (rb[k] > e || (rb[k] == e && rb[k] > 0 && rf[k] < f)) { e = rb[k]; f = rf[k]; c = rc[k]; }
+      if (e > 0) {
+        vertices[u] = 1;
+        neighbors[u] = 1;
+        communities[c] = 1;
+      }
+      if (!ok) atomicOr(&ctr->err, ERR_TABLE_FULL);
+    }
+    __syncthreads();
+  }
+}
+
+// Delta-screening expansion (inc/louvain.hxx:1480-1485): neighbours of flagged
+// sources, and members of flagged communities. One warp per vertex.
+__global__ void ds_expand_kernel(const uint64_t *off, const uint32_t *deg, const uint32_t *key, const uint8_t *ex,
+                                 size_t n, const uint32_t *vcom, const uint8_t *neighbors,
+                                 const uint8_t *communities, uint8_t *vertices) {
+  const size_t warps = size_t(gridDim.x) * blockDim.x / 32;
+  const int lane = threadIdx.x & 31;
+  for (size_t base = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32 * 32; base < n; base += warps * 32) {
+    const size_t u0 = base + lane;
+    const bool has = u0 < n && (!ex || ex[u0]);
+    if (has && communities[vcom[u0]]) vertices[u0] = 1;
+    unsigned todo = __ballot_sync(0xffffffffu, has && neighbors[u0]);
+    while (todo) {
+      const int l = __ffs(todo) - 1;
+      todo &= todo - 1;
+      const size_t u = base + l;
+      const uint64_t o = off[u];
+      const uint32_t d = deg[u];
+      for (uint32_t j = lane; j < d; j += 32) vertices[key[o + j]] = 1;
+    }
+  }
+}
+
+__global__ void clear_isolated_kernel(const uint32_t *list, size_t n, uint8_t *vaff, const uint8_t *fa) {
+  GRID_STRIDE(i, n) {
+    const uint32_t u = list[i];
+    if (vaff[u] && (!fa || fa[u])) vaff[u] = 0;
+  }
+}
+
+__global__ void merge_marks_kernel(uint8_t *vaff, uint8_t *mark, size_t n) {
+  GRID_STRIDE(i, n) {
+    if (mark[i]) { vaff[i] = 1; mark[i] = 0; }
+  }
+}
+
+// Deterministic mode: commit the decisions of one colour class (the moves of
+// louvainChangeCommunityOmpW, inc/louvain.hxx:496-503, applied after every
+// vertex of the class has decided from the same state).
+__global__ void apply_moves_kernel(const uint32_t *list, size_t n, uint32_t *dec, uint32_t *vcom, float *ctot,
+                                   const float *vtot) {
+  GRID_STRIDE(i, n) {
+    const uint32_t u = list[i];
+    const uint32_t c = dec[u];
+    if (c == EMPTY) continue;
+    const uint32_t d = vcom[u];
+    atomicAdd(&ctot[d], -vtot[u]);
+    atomicAdd(&ctot[c], vtot[u]);
+    vcom[u] = c;
+    dec[u] = EMPTY;
+  }
+}
+
+// louvainCommunityExistsOmpW (inc/louvain.hxx:668-682): flags only; the
+// count comes from the scan total.
+__global__ void community_flags_kernel(const uint8_t *ex, size_t n, const uint32_t *vcom, uint32_t *cext) {
+  GRID_STRIDE(u, n) {
+    if (ex && !ex[u]) continue;
+    cext[vcom[u]] = 1;
+  }
+}
+
+// louvainLookupCommunitiesOmpU (inc/louvain.hxx:839-844).
+__global__ void lookup_kernel(uint32_t *a, const uint32_t *map, size_t n) {
+  GRID_STRIDE(u, n) a[u] = map[a[u]];
+}
+
+// Member counts (louvainCountCommunityVerticesOmpW :752) and total degrees
+// (louvainCommunityTotalDegreeOmpW :712), with warp-aggregated atomics.
+__global__ void community_sizes_kernel(const uint32_t *deg, const uint8_t *ex, size_t n, const uint32_t *vcom,
+                                       uint32_t *csize, unsigned long long *ctdeg) {
+  const int lane = threadIdx.x & 31;
+  for (size_t base = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32 * 32; base < n;
+       base += size_t(gridDim.x) * blockDim.x) {
+    const size_t u = base + lane;
+    const bool has = u < n && (!ex || ex[u]);
+    const uint32_t c = has ? vcom[u] : EMPTY;
+    const unsigned long long d = has ? deg[u] : 0;
+    const unsigned grp = __match_any_sync(0xffffffffu, c);
+    // sum of degrees over the lanes that share this community (full-warp shuffles)
+    unsigned long long dsum = 0;
+#pragma unroll 8
+    for (int l = 0; l < 32; ++l) {
+      const uint32_t cl = __shfl_sync(0xffffffffu, c, l);
+      const unsigned long long dl = __shfl_sync(0xffffffffu, d, l);
+      if (cl == c) dsum += dl;
+    }
+    if (has && lane == __ffs(grp) - 1) {
+      atomicAdd(&csize[c], uint32_t(__popc(grp)));
+      atomicAdd(&ctdeg[c], dsum);
+    }
+  }
+}
+
+// Member scatter (louvainCommunityVerticesOmpW :800-812): atomic cursors,
+// warp-aggregated; member order within a community is unspecified, as in
+// the reference.
+__global__ void community_scatter_kernel(const uint8_t *ex, size_t n, const uint32_t *vcom, const uint32_t *coff,
+                                         uint32_t *ccur, uint32_t *cmem) {
+  const int lane = threadIdx.x & 31;
+  for (size_t base = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32 * 32; base < n;
+       base += size_t(gridDim.x) * blockDim.x) {
+    const size_t u = base + lane;
+    const bool has = u < n && (!ex || ex[u]);
+    const uint32_t c = has ? vcom[u] : EMPTY;
+    const unsigned grp = __match_any_sync(0xffffffffu, c);
+    const int leader = __ffs(grp) - 1;
+    uint32_t b = 0;
+    if (has && lane == leader) b = atomicAdd(&ccur[c], uint32_t(__popc(grp)));
+    b = __shfl_sync(0xffffffffu, b, leader);
+    if (has) cmem[coff[c] + b + __popc(grp & ((1u << lane) - 1u))] = uint32_t(u);
+  }
+}
+
+// louvainInitializeOmpW on an aggregated level + the driver's vaff fill
+// (inc/louvain.hxx:1207-1210).
+__global__ void level_init_kernel(size_t n, const float *vtot, uint32_t *vcom, float *ctot, uint8_t *vaff) {
+  GRID_STRIDE(u, n) {
+    vcom[u] = uint32_t(u);
+    ctot[u] = vtot[u];
+    vaff[u] = 1;
+  }
+}
+
+__global__ void count_flags_kernel(const uint8_t *f, size_t n, unsigned long long *dst) {
+  unsigned long long c = 0;
+  GRID_STRIDE(i, n) c += f[i] == 1;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(dst, c);
+}
+
+// modularityBy (inc/properties.hxx:178-191) in FP64: intra-community weight
+// and per-community totals. One warp per vertex.
+__global__ void modularity_kernel(const uint64_t *off, const uint32_t *deg, const uint32_t *key, const float *w,
+                                  const uint8_t *ex, size_t n, const uint32_t *memb, double *ctot64,
+                                  double *intra) {
+  const size_t warps = size_t(gridDim.x) * blockDim.x / 32;
+  const int lane = threadIdx.x & 31;
+  double in = 0;
+  for (size_t u = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32; u < n; u += warps) {
+    if (ex && !ex[u]) continue;
+    const uint32_t c = memb[u];
+    const uint64_t o = off[u];
+    const uint32_t d = deg[u];
+    double tot = 0;
+    for (uint32_t j = lane; j < d; j += 32) {
+      const double x = w[o + j];
+      tot += x;
+      if (memb[key[o + j]] == c) in += x;
+    }
+    tot = warp_sum_d(tot);
+    if (lane == 0 && tot != 0.0) atomicAdd(&ctot64[c], tot);
+  }
+  block_add_double(in, intra);
+}
+
+__global__ void sq_sum_kernel(const double *x, size_t n, double *dst) {
+  double s = 0;
+  GRID_STRIDE(i, n) s += x[i] * x[i];
+  block_add_double(s, dst);
+}
+
+}  // namespace
+
+int grid_for(size_t n, int block, int max_blocks_per_sm) {
+  size_t want = (n + block - 1) / block;
+  size_t cap = size_t(sms()) * max_blocks_per_sm;
+  size_t g = want < cap ? want : cap;
+  return int(g ? g : 1);
+}
+
+void launch_degrees(const uint64_t *off, uint32_t *deg, size_t span, cudaStream_t s) {
+  if (!span) return;
+  degrees_kernel<<<grid_for(span, 256), 256, 0, s>>>(off, deg, span);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_fill_u8(uint8_t *p, uint8_t v, size_t n, cudaStream_t s) {
+  if (n) LVG_CUDA(cudaMemsetAsync(p, v, n, s));
+}
+
+void launch_init_static(const Level &g, uint32_t *ucom, float *utot, float *ctot, cudaStream_t s) {
+  if (!g.span) return;
+  init_static_kernel<<<grid_for(g.span * 32, 256), 256, 0, s>>>(g.off, g.deg, g.w, g.ex, g.span, ucom, utot, ctot);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_total_weight(const Level &g, Counters *ctr, cudaStream_t s) {
+  LVG_CUDA(cudaMemsetAsync(&ctr->fp64[0], 0, sizeof(double), s));
+  if (!g.edges) return;
+  total_weight_kernel<<<grid_for(g.edges, 256), 256, 0, s>>>(g.w, g.edges, &ctr->fp64[0]);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_prior_to_f32(const double *src, float *dst, size_t n, cudaStream_t s) {
+  if (!n) return;
+  prior_to_f32_kernel<<<grid_for(n, 256), 256, 0, s>>>(src, dst, n);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_f32_to_f64(const float *src, double *dst, size_t n, cudaStream_t s) {
+  if (!n) return;
+  f32_to_f64_kernel<<<grid_for(n, 256), 256, 0, s>>>(src, dst, n);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_batch_weights(const uint32_t *src, const float *w, size_t n, float sign, const uint32_t *vcom,
+                          float *vtot, float *ctot, cudaStream_t s) {
+  if (!n) return;
+  batch_weights_kernel<<<grid_for(n, 256), 256, 0, s>>>(src, w, n, sign, vcom, vtot, ctot);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_df_mark(const uint32_t *ds, const uint32_t *dd, size_t nd, const uint32_t *is, const uint32_t *id,
+                    size_t ni, const uint32_t *vcom, uint8_t *vaff, cudaStream_t s) {
+  if (!(nd + ni)) return;
+  df_mark_kernel<<<grid_for(nd + ni, 256), 256, 0, s>>>(ds, dd, nd, is, id, ni, vcom, vaff);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_ds_mark(const Level &g, const uint32_t *ds, const uint32_t *dd, size_t nd, const uint32_t *is,
+                    const uint32_t *id, const float *iw, size_t ni, const uint32_t *seg, size_t nseg_cap,
+                    const uint32_t *vcom, const float *vtot, const float *ctot, double M, double R,
+                    uint8_t *vertices, uint8_t *neighbors, uint8_t *communities, uint32_t *gkeys, float *gvals,
+                    uint32_t *gfirst, int glog2, Counters *ctr, cudaStream_t s) {
+  (void)nseg_cap;
+  if (nd) {
+    ds_del_kernel<<<grid_for(nd, 256), 256, 0, s>>>(ds, dd, nd, vcom, vertices, neighbors, communities);
+    LVG_CHECK_LAUNCH();
+  }
+  if (ni) {
+    unsigned int *nseg = &ctr->cn;  // scratch counter
+    LVG_CUDA(cudaMemsetAsync(nseg, 0, sizeof(unsigned int), s));
+    ds_heads_kernel<<<grid_for(ni, 256), 256, 0, s>>>(is, ni, const_cast<uint32_t *>(seg), nseg);
+    LVG_CHECK_LAUNCH();
+    ds_ins_kernel<<<global_table_blocks(ni), DS_BLOCK, 0, s>>>(is, id, iw, ni, seg, nseg, vcom, vtot, ctot, M, R,
+                                                              vertices, neighbors, communities, gkeys, gvals,
+                                                              gfirst, glog2, ctr);
+    LVG_CHECK_LAUNCH();
+  }
+  if (g.span) {
+    ds_expand_kernel<<<grid_for(g.span, 256), 256, 0, s>>>(g.off, g.deg, g.key, g.ex, g.span, vcom, neighbors,
+                                                            communities, vertices);
+    LVG_CHECK_LAUNCH();
+  }
+}
+
+void launch_clear_isolated(const uint32_t *list, size_t n, uint8_t *vaff, const uint8_t *fa, cudaStream_t s) {
+  if (!n) return;
+  clear_isolated_kernel<<<grid_for(n, 256), 256, 0, s>>>(list, n, vaff, fa);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_merge_marks(uint8_t *vaff, uint8_t *mark, size_t n, cudaStream_t s) {
+  if (!n) return;
+  merge_marks_kernel<<<grid_for(n, 256), 256, 0, s>>>(vaff, mark, n);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_apply_moves(const uint32_t *list, size_t n, uint32_t *dec, uint32_t *vcom, float *ctot,
+                        const float *vtot, cudaStream_t s) {
+  if (!n) return;
+  apply_moves_kernel<<<grid_for(n, 256), 256, 0, s>>>(list, n, dec, vcom, ctot, vtot);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_community_flags(const Level &g, const uint32_t *vcom, uint32_t *cext, cudaStream_t s) {
+  if (!g.span) return;
+  community_flags_kernel<<<grid_for(g.span, 256), 256, 0, s>>>(g.ex, g.span, vcom, cext);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_lookup(uint32_t *a, const uint32_t *map, size_t n, cudaStream_t s) {
+  if (!n) return;
+  lookup_kernel<<<grid_for(n, 256), 256, 0, s>>>(a, map, n);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_community_sizes(const Level &g, const uint32_t *vcom, uint32_t *csize, uint64_t *ctdeg,
+                            cudaStream_t s) {
+  if (!g.span) return;
+  community_sizes_kernel<<<grid_for(g.span, 256), 256, 0, s>>>(g.deg, g.ex, g.span, vcom, csize,
+                                                                reinterpret_cast<unsigned long long *>(ctdeg));
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_community_scatter(const Level &g, const uint32_t *vcom, const uint32_t *coff, uint32_t *ccur,
+                              uint32_t *cmem, cudaStream_t s) {
+  if (!g.span) return;
+  community_scatter_kernel<<<grid_for(g.span, 256), 256, 0, s>>>(g.ex, g.span, vcom, coff, ccur, cmem);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_level_init(size_t n, const float *vtot, uint32_t *vcom, float *ctot, uint8_t *vaff, cudaStream_t s) {
+  if (!n) return;
+  level_init_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, vtot, vcom, ctot, vaff);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_count_flags(const uint8_t *f, size_t n, Counters *ctr, cudaStream_t s) {
+  LVG_CUDA(cudaMemsetAsync(&ctr->affected, 0, sizeof(unsigned long long), s));
+  if (!n) return;
+  count_flags_kernel<<<grid_for(n, 256), 256, 0, s>>>(f, n, &ctr->affected);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_modularity(const Level &g, const uint32_t *memb, double *ctot64, Counters *ctr, cudaStream_t s) {
+  LVG_CUDA(cudaMemsetAsync(&ctr->fp64[1], 0, sizeof(double), s));
+  LVG_CUDA(cudaMemsetAsync(ctot64, 0, g.span * sizeof(double), s));
+  if (!g.span) return;
+  modularity_kernel<<<grid_for(g.span * 32, 256), 256, 0, s>>>(g.off, g.deg, g.key, g.w, g.ex, g.span, memb, ctot64,
+                                                               &ctr->fp64[1]);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_sq_sum(const double *x, size_t n, Counters *ctr, cudaStream_t s) {
+  LVG_CUDA(cudaMemsetAsync(&ctr->fp64[2], 0, sizeof(double), s));
+  if (!n) return;
+  sq_sum_kernel<<<grid_for(n, 256), 256, 0, s>>>(x, n, &ctr->fp64[2]);
+  LVG_CHECK_LAUNCH();
+}
+
+}  // namespace lvg

@@ -1,0 +1,608 @@
+"""Python bindings of louvain-gb300 (ctypes over the C-ABI).
+
+Mirrors the reference's Louvain interface (inc/louvain.hxx):
+
+* :class:`LouvainOptions` — ``LouvainOptions`` (inc/louvain.hxx:30-63), same
+  fields and defaults, plus ``deterministic``;
+* :class:`LouvainResult` — ``LouvainResult<K, double>`` (inc/louvain.hxx:78-145);
+* :func:`louvain_static`, :func:`louvain_naive_dynamic`,
+  :func:`louvain_dynamic_delta_screening`, :func:`louvain_dynamic_frontier` —
+  ``louvainStaticOmp`` / ``louvainNaiveDynamicOmp`` /
+  ``louvainDynamicDeltaScreeningOmp`` / ``louvainDynamicFrontierOmp``
+  (inc/louvain.hxx:1285, 1349, 1542, 1674), on a :class:`Graph` in HBM.
+
+Every call runs on the GPU through ``liblouvain_gb300.so``. There is no CPU
+fallback: if the library or a GPU is missing the call raises.
+Host graphs and batches come from :mod:`graphgen` helpers in this module
+(``liblvg_graphgen.so``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBDIR = os.path.join(HERE, "lib")
+
+LVG_OK = 0
+LVG_EINVAL = -22
+LVG_ENOMEM = -12
+LVG_ETIMEOUT = -62
+LVG_ECUDA = -1000
+
+METHOD_STATIC, METHOD_NAIVE, METHOD_DELTA, METHOD_FRONTIER = 0, 1, 2, 3
+METHOD_NAMES = {METHOD_STATIC: "static", METHOD_NAIVE: "naive-dynamic", METHOD_DELTA: "delta-screening",
+                METHOD_FRONTIER: "dynamic-frontier"}
+
+_u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+_u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+_u64p = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+
+
+class LvgError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+# ----------------------------------------------------------------- C structs
+
+class _Options(C.Structure):
+    _fields_ = [("repeat", C.c_int), ("resolution", C.c_double), ("tolerance", C.c_double),
+                ("aggregationTolerance", C.c_double), ("toleranceDrop", C.c_double),
+                ("maxIterations", C.c_int), ("maxPasses", C.c_int), ("deterministic", C.c_int),
+                ("colors", C.c_int)]
+
+
+class _Result(C.Structure):
+    _fields_ = [("span", C.c_size_t), ("membership", C.POINTER(C.c_uint32)),
+                ("vertexWeight", C.POINTER(C.c_double)), ("communityWeight", C.POINTER(C.c_double)),
+                ("iterations", C.c_int), ("passes", C.c_int), ("time", C.c_float), ("markingTime", C.c_float),
+                ("initializationTime", C.c_float), ("firstPassTime", C.c_float), ("localMoveTime", C.c_float),
+                ("aggregationTime", C.c_float), ("affectedVertices", C.c_size_t), ("owned", C.c_int)]
+
+
+class _Batch(C.Structure):
+    _fields_ = [("num_deletions", C.c_size_t), ("del_src", C.c_void_p), ("del_dst", C.c_void_p),
+                ("del_w", C.c_void_p), ("num_insertions", C.c_size_t), ("ins_src", C.c_void_p),
+                ("ins_dst", C.c_void_p), ("ins_w", C.c_void_p)]
+
+
+class _Stats(C.Structure):
+    _fields_ = [("move_kernel_ms", C.c_double), ("move_launches", C.c_uint64), ("move_vertices", C.c_uint64),
+                ("move_edges", C.c_uint64), ("moves", C.c_uint64), ("aggregate_kernel_ms", C.c_double),
+                ("aggregate_edges", C.c_uint64), ("aggregate_launches", C.c_uint64),
+                ("kernel_launches", C.c_uint64)]
+
+
+class _Csr(C.Structure):
+    _fields_ = [("span", C.c_size_t), ("num_edges", C.c_size_t), ("offsets", C.POINTER(C.c_uint64)),
+                ("keys", C.POINTER(C.c_uint32)), ("weights", C.POINTER(C.c_float)),
+                ("exists", C.POINTER(C.c_uint8))]
+
+
+class _GBatch(C.Structure):
+    _fields_ = [("num_deletions", C.c_size_t), ("num_insertions", C.c_size_t),
+                ("del_src", C.POINTER(C.c_uint32)), ("del_dst", C.POINTER(C.c_uint32)),
+                ("del_w", C.POINTER(C.c_float)), ("ins_src", C.POINTER(C.c_uint32)),
+                ("ins_dst", C.POINTER(C.c_uint32)), ("ins_w", C.POINTER(C.c_float))]
+
+
+# ----------------------------------------------------------------- loading
+
+_lib = None
+_gen = None
+
+
+def lib_path() -> str:
+    return os.path.join(LIBDIR, "liblouvain_gb300.so")
+
+
+def gen_path() -> str:
+    return os.path.join(LIBDIR, "liblvg_graphgen.so")
+
+
+def load_library() -> C.CDLL:
+    """Load liblouvain_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = lib_path()
+    if not os.path.exists(p):
+        raise LvgError(LVG_ECUDA, f"{p} is missing: build it first (lvg_build.py); there is no CPU fallback")
+    L = C.CDLL(p)
+    vp, sz, i32, f64 = C.c_void_p, C.c_size_t, C.c_int, C.c_double
+    L.lvg_last_error.restype = C.c_char_p
+    L.lvg_options_default.argtypes = [C.POINTER(_Options)]
+    L.lvg_graph_create.argtypes = [sz, _u64p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(vp)]
+    L.lvg_graph_destroy.argtypes = [vp]
+    for n in ("lvg_graph_span", "lvg_graph_order", "lvg_graph_size"):
+        getattr(L, n).argtypes = [vp]
+        getattr(L, n).restype = sz
+    L.lvg_static.argtypes = [vp, C.POINTER(_Options), C.POINTER(_Result)]
+    for n in ("lvg_naive_dynamic", "lvg_delta_screening", "lvg_frontier"):
+        getattr(L, n).argtypes = [vp, C.POINTER(_Batch), _u32p, _f64p, _f64p, C.POINTER(_Options),
+                                  C.POINTER(_Result)]
+    L.lvg_result_free.argtypes = [C.POINTER(_Result)]
+    L.lvg_modularity.argtypes = [vp, _u32p, f64, f64, C.POINTER(f64)]
+    L.lvg_edge_weight.argtypes = [vp, C.POINTER(f64)]
+    L.lvg_host_alloc.argtypes = [sz]
+    L.lvg_host_alloc.restype = vp
+    L.lvg_host_free.argtypes = [vp]
+    L.lvg_set_profiling.argtypes = [vp, i32]
+    L.lvg_get_stats.argtypes = [vp, C.POINTER(_Stats)]
+    L.lvg_state_create.argtypes = [vp, C.POINTER(vp)]
+    L.lvg_state_set.argtypes = [vp, _u32p, _f64p, _f64p]
+    L.lvg_state_get.argtypes = [vp, vp, vp, vp]
+    L.lvg_state_destroy.argtypes = [vp]
+    L.lvg_device_batch_create.argtypes = [vp, C.POINTER(_Batch), C.POINTER(vp)]
+    L.lvg_device_batch_destroy.argtypes = [vp]
+    L.lvg_run_resident.argtypes = [vp, i32, vp, vp, vp, C.POINTER(_Options), C.POINTER(_Result)]
+    L.lvg_affected_vertices.argtypes = [vp, i32, C.POINTER(_Batch), _u32p, _f64p, _f64p, C.POINTER(_Options),
+                                        vp, vp, vp]
+    L.lvg_aggregate.argtypes = [vp, _u32p, _u32p, C.POINTER(sz), _u64p, vp, vp]
+    _lib = L
+    return L
+
+
+def load_graphgen() -> C.CDLL:
+    global _gen
+    if _gen is not None:
+        return _gen
+    p = gen_path()
+    if not os.path.exists(p):
+        raise LvgError(LVG_EINVAL, f"{p} is missing: build it first (lvg_build.py)")
+    G = C.CDLL(p)
+    G.lvgg_last_error.restype = C.c_char_p
+    G.lvgg_planted_partition.argtypes = [C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_uint64,
+                                         C.POINTER(_Csr)]
+    G.lvgg_rmat.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, C.c_uint64,
+                            C.POINTER(_Csr)]
+    G.lvgg_random_batch.argtypes = [C.POINTER(_Csr), C.c_size_t, C.c_double, C.c_uint64, C.POINTER(_GBatch)]
+    G.lvgg_apply_batch.argtypes = [C.POINTER(_Csr), C.POINTER(_GBatch), C.POINTER(_Csr)]
+    G.lvgg_csr_free.argtypes = [C.POINTER(_Csr)]
+    G.lvgg_batch_free.argtypes = [C.POINTER(_GBatch)]
+    _gen = G
+    return G
+
+
+def _check(rc: int) -> None:
+    if rc != LVG_OK:
+        raise LvgError(rc, load_library().lvg_last_error().decode(errors="replace"))
+
+
+# ----------------------------------------------------------------- host data
+
+@dataclass
+class HostGraph:
+    """A CSR graph in host memory (numpy). Row u = keys[offsets[u]:offsets[u+1]]."""
+    offsets: np.ndarray  # uint64 [span+1]
+    keys: np.ndarray     # uint32
+    weights: np.ndarray  # float32
+    exists: np.ndarray   # uint8 [span]
+
+    @property
+    def span(self) -> int:
+        return len(self.offsets) - 1
+
+    @property
+    def num_edges(self) -> int:
+        return int(self.offsets[-1])
+
+    @property
+    def order(self) -> int:
+        return int(self.exists.sum())
+
+    def _struct(self) -> _Csr:
+        c = _Csr()
+        c.span = self.span
+        c.num_edges = self.num_edges
+        c.offsets = self.offsets.ctypes.data_as(C.POINTER(C.c_uint64))
+        c.keys = self.keys.ctypes.data_as(C.POINTER(C.c_uint32))
+        c.weights = self.weights.ctypes.data_as(C.POINTER(C.c_float))
+        c.exists = self.exists.ctypes.data_as(C.POINTER(C.c_uint8))
+        return c
+
+    def degrees(self) -> np.ndarray:
+        return np.diff(self.offsets).astype(np.int64)
+
+
+@dataclass
+class HostBatch:
+    """A tidy batch update: both directions, sorted by (src, dst)."""
+    del_src: np.ndarray
+    del_dst: np.ndarray
+    del_w: np.ndarray
+    ins_src: np.ndarray
+    ins_dst: np.ndarray
+    ins_w: np.ndarray
+
+    @property
+    def num_deletions(self) -> int:
+        return len(self.del_src)
+
+    @property
+    def num_insertions(self) -> int:
+        return len(self.ins_src)
+
+    def _struct(self) -> _Batch:
+        b = _Batch()
+        b.num_deletions = self.num_deletions
+        b.del_src = self.del_src.ctypes.data
+        b.del_dst = self.del_dst.ctypes.data
+        b.del_w = self.del_w.ctypes.data
+        b.num_insertions = self.num_insertions
+        b.ins_src = self.ins_src.ctypes.data
+        b.ins_dst = self.ins_dst.ctypes.data
+        b.ins_w = self.ins_w.ctypes.data
+        return b
+
+    def _gstruct(self) -> _GBatch:
+        b = _GBatch()
+        b.num_deletions = self.num_deletions
+        b.num_insertions = self.num_insertions
+        P32, PF = C.POINTER(C.c_uint32), C.POINTER(C.c_float)
+        b.del_src = self.del_src.ctypes.data_as(P32)
+        b.del_dst = self.del_dst.ctypes.data_as(P32)
+        b.del_w = self.del_w.ctypes.data_as(PF)
+        b.ins_src = self.ins_src.ctypes.data_as(P32)
+        b.ins_dst = self.ins_dst.ctypes.data_as(P32)
+        b.ins_w = self.ins_w.ctypes.data_as(PF)
+        return b
+
+    @staticmethod
+    def empty() -> "HostBatch":
+        z32, zf = np.zeros(0, np.uint32), np.zeros(0, np.float32)
+        return HostBatch(z32, z32.copy(), zf, z32.copy(), z32.copy(), zf.copy())
+
+
+def _take_csr(c: _Csr) -> HostGraph:
+    G = load_graphgen()
+    S, X = c.span, c.num_edges
+    g = HostGraph(np.ctypeslib.as_array(c.offsets, (S + 1,)).copy(),
+                  np.ctypeslib.as_array(c.keys, (max(X, 1),))[:X].copy(),
+                  np.ctypeslib.as_array(c.weights, (max(X, 1),))[:X].copy(),
+                  np.ctypeslib.as_array(c.exists, (S,)).copy())
+    G.lvgg_csr_free(C.byref(c))
+    return g
+
+
+def planted_partition(n: int, block: int, avg_degree: float, p_in: float, seed: int) -> HostGraph:
+    """Seeded planted-partition graph, ids 1..n (vertex 0 absent)."""
+    G = load_graphgen()
+    c = _Csr()
+    if G.lvgg_planted_partition(n, block, avg_degree, p_in, seed, C.byref(c)) != 0:
+        raise LvgError(LVG_EINVAL, G.lvgg_last_error().decode())
+    return _take_csr(c)
+
+
+def rmat(scale: int, edge_factor: float = 16, a: float = 0.57, b: float = 0.19, c: float = 0.19,
+         seed: int = 42, permute: bool = True) -> HostGraph:
+    """Seeded R-MAT graph, ids 1..2^scale (vertex 0 absent)."""
+    G = load_graphgen()
+    cs = _Csr()
+    if G.lvgg_rmat(scale, edge_factor, a, b, c, int(permute), seed, C.byref(cs)) != 0:
+        raise LvgError(LVG_EINVAL, G.lvgg_last_error().decode())
+    return _take_csr(cs)
+
+
+def random_batch(x: HostGraph, num_updates: int, insertion_fraction: float = 0.8, seed: int = 7) -> HostBatch:
+    """Tidy random batch: insertions of absent uniform pairs, edge-uniform deletions."""
+    G = load_graphgen()
+    cs = x._struct()
+    gb = _GBatch()
+    if G.lvgg_random_batch(C.byref(cs), num_updates, insertion_fraction, seed, C.byref(gb)) != 0:
+        raise LvgError(LVG_EINVAL, G.lvgg_last_error().decode())
+
+    def arr(p, n, dt):
+        return np.ctypeslib.as_array(p, (max(n, 1),))[:n].copy().astype(dt, copy=False)
+
+    nd, ni = gb.num_deletions, gb.num_insertions
+    b = HostBatch(arr(gb.del_src, nd, np.uint32), arr(gb.del_dst, nd, np.uint32), arr(gb.del_w, nd, np.float32),
+                  arr(gb.ins_src, ni, np.uint32), arr(gb.ins_dst, ni, np.uint32), arr(gb.ins_w, ni, np.float32))
+    G.lvgg_batch_free(C.byref(gb))
+    return b
+
+
+def apply_batch(x: HostGraph, b: HostBatch) -> HostGraph:
+    """x with the batch applied (remove deletions, add insertions)."""
+    G = load_graphgen()
+    cs = x._struct()
+    gb = b._gstruct()
+    y = _Csr()
+    if G.lvgg_apply_batch(C.byref(cs), C.byref(gb), C.byref(y)) != 0:
+        raise LvgError(LVG_EINVAL, G.lvgg_last_error().decode())
+    return _take_csr(y)
+
+
+# ----------------------------------------------------------------- options / results
+
+@dataclass
+class LouvainOptions:
+    """LouvainOptions (inc/louvain.hxx:30-63); defaults as its constructor (:60)."""
+    repeat: int = 1
+    resolution: float = 1.0
+    tolerance: float = 1e-2
+    aggregationTolerance: float = 1.0
+    toleranceDrop: float = 10.0
+    maxIterations: int = 20
+    maxPasses: int = 10
+    deterministic: bool = False
+    colors: int = 0  # 0 = library default (8 asynchronous, 16 deterministic)
+
+    def _struct(self) -> _Options:
+        return _Options(self.repeat, self.resolution, self.tolerance, self.aggregationTolerance,
+                        self.toleranceDrop, self.maxIterations, self.maxPasses, int(self.deterministic),
+                        int(self.colors))
+
+    def effective_colors(self) -> int:
+        k = self.colors if self.colors > 0 else (16 if self.deterministic else 8)
+        return max(1, min(32, k))
+
+
+@dataclass
+class LouvainResult:
+    """LouvainResult<uint32_t, double> (inc/louvain.hxx:78-145)."""
+    membership: np.ndarray
+    vertexWeight: np.ndarray
+    communityWeight: np.ndarray
+    iterations: int = 0
+    passes: int = 0
+    time: float = 0.0
+    markingTime: float = 0.0
+    initializationTime: float = 0.0
+    firstPassTime: float = 0.0
+    localMoveTime: float = 0.0
+    aggregationTime: float = 0.0
+    affectedVertices: int = 0
+    stats: dict = field(default_factory=dict)
+
+
+def _scalars(r: _Result) -> dict:
+    return dict(iterations=r.iterations, passes=r.passes, time=r.time, markingTime=r.markingTime,
+                initializationTime=r.initializationTime, firstPassTime=r.firstPassTime,
+                localMoveTime=r.localMoveTime, aggregationTime=r.aggregationTime,
+                affectedVertices=r.affectedVertices)
+
+
+# ----------------------------------------------------------------- device objects
+
+class Graph:
+    """A graph resident in HBM (``lvg_graph``)."""
+
+    def __init__(self, g: HostGraph):
+        L = load_library()
+        self._L = L
+        self.h = C.c_void_p()
+        self.host = g
+        w = g.weights if g.num_edges else np.zeros(1, np.float32)
+        k = g.keys if g.num_edges else np.zeros(1, np.uint32)
+        _check(L.lvg_graph_create(g.span, g.offsets, k.ctypes.data, w.ctypes.data, g.exists.ctypes.data,
+                                  C.byref(self.h)))
+
+    def close(self) -> None:
+        if self.h:
+            self._L.lvg_graph_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def span(self) -> int:
+        return int(self._L.lvg_graph_span(self.h))
+
+    @property
+    def order(self) -> int:
+        return int(self._L.lvg_graph_order(self.h))
+
+    @property
+    def size(self) -> int:
+        return int(self._L.lvg_graph_size(self.h))
+
+    def edge_weight(self) -> float:
+        out = C.c_double()
+        _check(self._L.lvg_edge_weight(self.h, C.byref(out)))
+        return out.value
+
+    def modularity(self, membership: np.ndarray, M: float = 0.0, R: float = 1.0) -> float:
+        out = C.c_double()
+        _check(self._L.lvg_modularity(self.h, np.ascontiguousarray(membership, np.uint32), M, R, C.byref(out)))
+        return out.value
+
+    def set_profiling(self, on: bool) -> None:
+        _check(self._L.lvg_set_profiling(self.h, int(on)))
+
+    def stats(self) -> dict:
+        s = _Stats()
+        _check(self._L.lvg_get_stats(self.h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in _Stats._fields_}
+
+
+def affected_vertices(y: Graph, method: int, batch: HostBatch, q, qvtot, qctot, o: LouvainOptions | None = None):
+    """Initial affected flags of a method (lvg_affected_vertices). For delta-screening
+    returns (vertices, neighbors, communities), else the flags array."""
+    L = load_library()
+    S = y.span
+    f, nb, cm = np.zeros(S, np.uint8), np.zeros(S, np.uint8), np.zeros(S, np.uint8)
+    b = (batch or HostBatch.empty())._struct()
+    opt = (o or LouvainOptions())._struct()
+    _check(L.lvg_affected_vertices(y.h, method, C.byref(b), np.ascontiguousarray(q, np.uint32),
+                                   np.ascontiguousarray(qvtot, np.float64), np.ascontiguousarray(qctot, np.float64),
+                                   C.byref(opt), f.ctypes.data, nb.ctypes.data, cm.ctypes.data))
+    return (f, nb, cm) if method == METHOD_DELTA else f
+
+
+def aggregate(g: Graph, membership):
+    """One aggregation step (lvg_aggregate): (renumbered membership, CN, offsets, keys, weights)."""
+    L = load_library()
+    S, X = g.span, g.size
+    ren = np.zeros(S, np.uint32)
+    cn = C.c_size_t()
+    off = np.zeros(S + 1, np.uint64)
+    keys = np.zeros(max(X, 1), np.uint32)
+    w = np.zeros(max(X, 1), np.float64)
+    _check(L.lvg_aggregate(g.h, np.ascontiguousarray(membership, np.uint32), ren, C.byref(cn), off,
+                           keys.ctypes.data, w.ctypes.data))
+    CN = cn.value
+    E = int(off[CN])
+    return ren, CN, off[:CN + 1].copy(), keys[:E].copy(), w[:E].copy()
+
+
+def _run(fn_name: str, g: Graph, batch: HostBatch | None, q, qvtot, qctot, o: LouvainOptions | None,
+         out_buffers=None) -> LouvainResult:
+    L = load_library()
+    o = o or LouvainOptions()
+    S = g.span
+    r = _Result()
+    keep = []
+    if out_buffers is not None:
+        m, vw, cw = out_buffers
+        r.membership = m.ctypes.data_as(C.POINTER(C.c_uint32))
+        r.vertexWeight = vw.ctypes.data_as(C.POINTER(C.c_double))
+        r.communityWeight = cw.ctypes.data_as(C.POINTER(C.c_double))
+    opt = o._struct()
+    if fn_name == "lvg_static":
+        _check(L.lvg_static(g.h, C.byref(opt), C.byref(r)))
+    else:
+        b = (batch or HostBatch.empty())._struct()
+        keep.append(b)
+        _check(getattr(L, fn_name)(g.h, C.byref(b), np.ascontiguousarray(q, np.uint32),
+                                   np.ascontiguousarray(qvtot, np.float64), np.ascontiguousarray(qctot, np.float64),
+                                   C.byref(opt), C.byref(r)))
+    if out_buffers is not None:
+        m, vw, cw = out_buffers
+    else:
+        m = np.ctypeslib.as_array(r.membership, (S,)).copy()
+        vw = np.ctypeslib.as_array(r.vertexWeight, (S,)).copy()
+        cw = np.ctypeslib.as_array(r.communityWeight, (S,)).copy()
+        L.lvg_result_free(C.byref(r))
+    return LouvainResult(m, vw, cw, **_scalars(r), stats=g.stats())
+
+
+def louvain_static(x: Graph, o: LouvainOptions | None = None, out_buffers=None) -> LouvainResult:
+    """louvainStaticOmp (inc/louvain.hxx:1285) on the GPU."""
+    return _run("lvg_static", x, None, None, None, None, o, out_buffers)
+
+
+def louvain_naive_dynamic(y: Graph, batch: HostBatch, q, qvtot, qctot, o: LouvainOptions | None = None,
+                          out_buffers=None) -> LouvainResult:
+    """louvainNaiveDynamicOmp (inc/louvain.hxx:1349) on the GPU."""
+    return _run("lvg_naive_dynamic", y, batch, q, qvtot, qctot, o, out_buffers)
+
+
+def louvain_dynamic_delta_screening(y: Graph, batch: HostBatch, q, qvtot, qctot, o: LouvainOptions | None = None,
+                                    out_buffers=None) -> LouvainResult:
+    """louvainDynamicDeltaScreeningOmp (inc/louvain.hxx:1542) on the GPU."""
+    return _run("lvg_delta_screening", y, batch, q, qvtot, qctot, o, out_buffers)
+
+
+def louvain_dynamic_frontier(y: Graph, batch: HostBatch, q, qvtot, qctot, o: LouvainOptions | None = None,
+                             out_buffers=None) -> LouvainResult:
+    """louvainDynamicFrontierOmp (inc/louvain.hxx:1674) on the GPU."""
+    return _run("lvg_frontier", y, batch, q, qvtot, qctot, o, out_buffers)
+
+
+class State:
+    """Membership / vertex weights / community weights resident in HBM (``lvg_state``)."""
+
+    def __init__(self, g: Graph):
+        self._L = load_library()
+        self.g = g
+        self.h = C.c_void_p()
+        _check(self._L.lvg_state_create(g.h, C.byref(self.h)))
+
+    def set(self, q, qvtot, qctot) -> None:
+        _check(self._L.lvg_state_set(self.h, np.ascontiguousarray(q, np.uint32),
+                                     np.ascontiguousarray(qvtot, np.float64), np.ascontiguousarray(qctot, np.float64)))
+
+    def get(self):
+        S = self.g.span
+        m = np.empty(S, np.uint32)
+        vt = np.empty(S, np.float64)
+        ct = np.empty(S, np.float64)
+        _check(self._L.lvg_state_get(self.h, m.ctypes.data, vt.ctypes.data, ct.ctypes.data))
+        return m, vt, ct
+
+    def membership(self, out: np.ndarray | None = None) -> np.ndarray:
+        m = out if out is not None else np.empty(self.g.span, np.uint32)
+        _check(self._L.lvg_state_get(self.h, m.ctypes.data, None, None))
+        return m
+
+    def close(self) -> None:
+        if self.h:
+            self._L.lvg_state_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class DeviceBatch:
+    """A validated batch resident in HBM (``lvg_device_batch``)."""
+
+    def __init__(self, g: Graph, b: HostBatch):
+        self._L = load_library()
+        self.g = g
+        self.batch = b
+        self.h = C.c_void_p()
+        s = b._struct()
+        _check(self._L.lvg_device_batch_create(g.h, C.byref(s), C.byref(self.h)))
+
+    def close(self) -> None:
+        if self.h:
+            self._L.lvg_device_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def run_resident(g: Graph, method: int, batch: DeviceBatch | None, prior: State | None, out: State,
+                 o: LouvainOptions | None = None) -> dict:
+    """lvg_run_resident: a method on HBM-resident inputs; returns the scalar result fields."""
+    L = load_library()
+    opt = (o or LouvainOptions())._struct()
+    r = _Result()
+    _check(L.lvg_run_resident(g.h, method, batch.h if batch else None, prior.h if prior else None, out.h,
+                              C.byref(opt), C.byref(r)))
+    return _scalars(r)
+
+
+class PinnedArray:
+    """A numpy view of pinned host memory from lvg_host_alloc (for fast copies)."""
+
+    def __init__(self, n: int, dtype):
+        self._L = load_library()
+        dt = np.dtype(dtype)
+        self.ptr = self._L.lvg_host_alloc(max(1, n * dt.itemsize))
+        if not self.ptr:
+            raise LvgError(LVG_ENOMEM, "lvg_host_alloc failed")
+        buf = (C.c_char * (n * dt.itemsize)).from_address(self.ptr)
+        self.array = np.frombuffer(buf, dtype=dt, count=n)
+
+    def close(self) -> None:
+        if self.ptr:
+            self.array = None
+            self._L.lvg_host_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

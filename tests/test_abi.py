@@ -1,0 +1,71 @@
+"""The C-ABI libraries load and export every symbol their headers declare.
+
+No compute call is made here: these run on machines without a GPU.
+"""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+from conftest import PKG, ROOT
+
+INCLUDE = os.path.join(ROOT, "include")
+
+
+def declared(header: str) -> list[str]:
+    src = open(os.path.join(INCLUDE, header)).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    names = re.findall(r"\b(lvgg?_[a-z0-9_]+)\s*\(", src)
+    return sorted(set(names))
+
+
+def exported(lib: str) -> set[str]:
+    out = subprocess.run(["nm", "-D", "--defined-only", lib], capture_output=True, text=True, check=True).stdout
+    return {line.split()[-1] for line in out.splitlines() if " T " in line}
+
+
+def test_graphgen_exports_everything(lvg):
+    names = declared("louvain_gb300_graphgen.h")
+    assert len(names) >= 7
+    missing = [n for n in names if n not in exported(lvg.gen_path())]
+    assert not missing, missing
+
+
+def test_cuda_library_builds_loads_and_exports_everything(lvg):
+    import lvg_build
+
+    lvg_build.build_cuda()
+    names = declared("louvain_gb300.h")
+    assert {"lvg_static", "lvg_naive_dynamic", "lvg_delta_screening", "lvg_frontier", "lvg_result_free"} <= set(names)
+    ex = exported(lvg.lib_path())
+    missing = [n for n in names if n not in ex]
+    assert not missing, missing
+    lib = ctypes.CDLL(lvg.lib_path())  # loads without a GPU; no compute call
+    for n in names:
+        assert hasattr(lib, n)
+
+
+def test_cuda_objects_are_sm_103a_only():
+    """Every device object is compiled for sm_103a (checked from the build flags)."""
+    import lvg_build
+
+    assert lvg_build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def test_options_defaults_match_reference(lvg):
+    o = lvg.LouvainOptions()
+    # LouvainOptions(int repeat=1, double resolution=1, double tolerance=1e-2,
+    #   double aggregationTolerance=1.0, double toleranceDrop=10, int maxIterations=20, int maxPasses=10)
+    assert (o.repeat, o.resolution, o.tolerance, o.aggregationTolerance, o.toleranceDrop, o.maxIterations,
+            o.maxPasses) == (1, 1.0, 1e-2, 1.0, 10.0, 20, 10)
+    assert not o.deterministic
+    assert o.effective_colors() == 8 and lvg.LouvainOptions(deterministic=True).effective_colors() == 16
+
+
+def test_missing_library_fails_loudly(lvg, monkeypatch, tmp_path):
+    monkeypatch.setattr(lvg, "LIBDIR", str(tmp_path))
+    monkeypatch.setattr(lvg, "_lib", None)
+    with pytest.raises(lvg.LvgError):
+        lvg.load_library()

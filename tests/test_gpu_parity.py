@@ -1,0 +1,208 @@
+"""CUDA path (liblouvain_gb300.so, through the C-ABI) against the reference's
+golden outputs and the oracle.
+
+Bit-exact: weighted degrees, the batch weight update, DF/DS affected sets, the
+aggregated graph for a given membership (row-sorted), and the deterministic
+mode against the oracle's CPU replay of the same rule. Tolerance: modularity
+of the asynchronous mode within 0.005 (absolute) of the reference's mean over
+5 multi-threaded runs.
+"""
+import numpy as np
+import pytest
+
+from conftest import rows_sorted
+
+pytestmark = pytest.mark.gpu
+
+QTOL = 0.005  # modularity tolerance against the reference's mean
+
+
+@pytest.fixture(scope="module")
+def dev(cuda, golden):
+    return cuda.Graph(golden.x), cuda.Graph(golden.y)
+
+
+def prior(golden):
+    return golden["static_m"], golden["static_vt"], golden["static_ct"]
+
+
+def test_graph_properties(cuda, golden, dev):
+    X, Y = dev
+    assert X.span == golden.x.span and X.order == golden.x.order and X.size == golden.x.num_edges
+    assert X.edge_weight() / 2 == golden["x_M"]
+    assert Y.edge_weight() / 2 == golden["y_M"]
+
+
+def test_vertex_weights_bit_exact(cuda, golden, dev):
+    X, _ = dev
+    r = cuda.louvain_static(X, cuda.LouvainOptions(maxPasses=0))
+    assert np.array_equal(r.vertexWeight, golden["x_vtot"])
+    assert np.array_equal(r.communityWeight, golden["x_vtot"])
+    ex = golden.x.exists.astype(bool)
+    ids = np.arange(golden.x.span, dtype=np.uint32)
+    assert np.array_equal(r.membership[ex], ids[ex]) and np.all(r.membership[~ex] == 0)
+    assert r.passes == 0 and r.iterations == 0
+
+
+def test_batch_weight_update_bit_exact(cuda, golden, dev):
+    _, Y = dev
+    r = cuda.louvain_dynamic_frontier(Y, golden.b, *prior(golden), cuda.LouvainOptions(maxPasses=0))
+    assert np.array_equal(r.vertexWeight, golden["upd_vt"])
+    assert np.array_equal(r.communityWeight, golden["upd_ct"])
+    assert np.array_equal(r.membership, golden["static_m"])
+
+
+def test_frontier_flags_bit_exact(cuda, golden, dev):
+    _, Y = dev
+    f = cuda.affected_vertices(Y, cuda.METHOD_FRONTIER, golden.b, *prior(golden))
+    assert np.array_equal(f, golden["df_flags"])
+
+
+def test_delta_screening_flags_bit_exact(cuda, golden, dev):
+    _, Y = dev
+    v, n, c = cuda.affected_vertices(Y, cuda.METHOD_DELTA, golden.b, *prior(golden))
+    assert np.array_equal(v, golden["ds_vertices"])
+    assert np.array_equal(n, golden["ds_neighbors"])
+    assert np.array_equal(c, golden["ds_communities"])
+
+
+def test_aggregation_bit_exact(cuda, golden, dev):
+    _, Y = dev
+    ren, CN, off, keys, w = cuda.aggregate(Y, golden["static_m"])
+    assert CN == golden["agg_cn"]
+    assert np.array_equal(ren, golden["agg_ren"])
+    r, k, x = rows_sorted(CN, off, keys, w)
+    assert np.array_equal(r, golden["agg_row"])
+    assert np.array_equal(k, golden["agg_key"])
+    assert np.array_equal(x, golden["agg_w"])
+
+
+def test_modularity_fp64(cuda, golden, dev, orc):
+    X, _ = dev
+    m = golden["static_m"]
+    assert X.modularity(m) == pytest.approx(float(golden["static_q"]), abs=1e-12)
+    assert X.modularity(m) == pytest.approx(orc.modularity(golden.x, m), abs=1e-12)
+
+
+def _det(cuda, orc, golden, dev, method, colors):
+    X, Y = dev
+    o = cuda.LouvainOptions(deterministic=True, colors=colors)
+    if method == 0:
+        r = cuda.louvain_static(X, o)
+        m, vt, ct, info = orc.louvain(golden.x, 0, threads=4, sync=True, colors=colors)
+    else:
+        fn = {1: cuda.louvain_naive_dynamic, 2: cuda.louvain_dynamic_delta_screening,
+              3: cuda.louvain_dynamic_frontier}[method]
+        r = fn(Y, golden.b, *prior(golden), o)
+        m, vt, ct, info = orc.louvain(golden.y, method, golden.b, *prior(golden), threads=4, sync=True,
+                                      colors=colors)
+    return r, (m, vt, ct, info)
+
+
+@pytest.mark.parametrize("method", [0, 1, 2, 3])
+@pytest.mark.parametrize("colors", [1, 4, 16])
+def test_deterministic_mode_matches_cpu_replay(cuda, orc, golden, dev, method, colors):
+    r, (m, vt, ct, info) = _det(cuda, orc, golden, dev, method, colors)
+    assert np.array_equal(r.membership, m)
+    assert np.array_equal(r.vertexWeight, vt)
+    assert np.array_equal(r.communityWeight, ct)
+    assert (r.iterations, r.passes, r.affectedVertices) == (info["iterations"], info["passes"],
+                                                            info["affectedVertices"])
+
+
+def test_deterministic_mode_is_reproducible(cuda, golden, dev):
+    X, _ = dev
+    o = cuda.LouvainOptions(deterministic=True, repeat=3)
+    a = cuda.louvain_static(X, o)
+    b = cuda.louvain_static(X, cuda.LouvainOptions(deterministic=True))
+    assert np.array_equal(a.membership, b.membership)
+
+
+@pytest.mark.parametrize("method,tag", [(0, "static"), (1, "nd"), (2, "ds"), (3, "df")])
+def test_async_quality_within_tolerance(cuda, golden, dev, orc, method, tag):
+    X, Y = dev
+    if method == 0:
+        r = cuda.louvain_static(X)
+        q = orc.modularity(golden.x, r.membership)
+    else:
+        fn = {1: cuda.louvain_naive_dynamic, 2: cuda.louvain_dynamic_delta_screening,
+              3: cuda.louvain_dynamic_frontier}[method]
+        r = fn(Y, golden.b, *prior(golden))
+        q = orc.modularity(golden.y, r.membership)
+    assert abs(q - float(golden[f"{tag}_q_mean8"])) <= QTOL, (q, float(golden[f"{tag}_q_mean8"]))
+    assert r.passes >= 1 and r.iterations >= r.passes
+
+
+def test_async_community_totals_consistent(cuda, golden, dev):
+    """Σ vertex weights of each final community == its total (integer weights: exact)."""
+    X, _ = dev
+    r = cuda.louvain_static(X)
+    ex = golden.x.exists.astype(bool)
+    sums = np.zeros(golden.x.span)
+    np.add.at(sums, r.membership[ex], r.vertexWeight[ex])
+    live = np.unique(r.membership[ex])
+    assert np.array_equal(sums[live], r.communityWeight[live])
+
+
+def test_resident_api_matches_host_api(cuda, golden, dev):
+    _, Y = dev
+    o = cuda.LouvainOptions(deterministic=True)
+    ref = cuda.louvain_dynamic_frontier(Y, golden.b, *prior(golden), o)
+    st_prior, st_out = cuda.State(Y), cuda.State(Y)
+    st_prior.set(*prior(golden))
+    db = cuda.DeviceBatch(Y, golden.b)
+    info = cuda.run_resident(Y, cuda.METHOD_FRONTIER, db, st_prior, st_out, o)
+    m, vt, ct = st_out.get()
+    assert np.array_equal(m, ref.membership)
+    assert np.array_equal(vt, ref.vertexWeight) and np.array_equal(ct, ref.communityWeight)
+    assert info["iterations"] == ref.iterations and info["passes"] == ref.passes
+    # in place: prior == out
+    st_prior.set(*prior(golden))
+    cuda.run_resident(Y, cuda.METHOD_FRONTIER, db, st_prior, st_prior, o)
+    assert np.array_equal(st_prior.get()[0], ref.membership)
+
+
+def test_result_into_caller_buffers(cuda, golden, dev):
+    X, _ = dev
+    S = golden.x.span
+    bufs = (cuda.PinnedArray(S, np.uint32), cuda.PinnedArray(S, np.float64), cuda.PinnedArray(S, np.float64))
+    o = cuda.LouvainOptions(deterministic=True)
+    r = cuda.louvain_static(X, o, out_buffers=tuple(b.array for b in bufs))
+    r2 = cuda.louvain_static(X, o)
+    assert np.array_equal(bufs[0].array, r2.membership) and np.array_equal(bufs[2].array, r2.communityWeight)
+    assert r.passes == r2.passes
+
+
+def test_invalid_inputs_rejected(cuda, golden, dev):
+    _, Y = dev
+    S = golden.y.span
+    q, vt, ct = prior(golden)
+    bad = cuda.HostBatch(np.array([S], np.uint32), np.array([1], np.uint32), np.ones(1, np.float32),
+                         *[a.copy() for a in (golden.b.ins_src, golden.b.ins_dst, golden.b.ins_w)])
+    with pytest.raises(cuda.LvgError) as e:
+        cuda.louvain_dynamic_frontier(Y, bad, q, vt, ct)
+    assert e.value.code == cuda.LVG_EINVAL
+    badq = q.copy()
+    badq[1] = S
+    with pytest.raises(cuda.LvgError) as e:
+        cuda.louvain_naive_dynamic(Y, golden.b, badq, vt, ct)
+    assert e.value.code == cuda.LVG_EINVAL
+    if golden.b.num_insertions > 1:
+        rev = cuda.HostBatch(golden.b.del_src, golden.b.del_dst, golden.b.del_w, golden.b.ins_src[::-1].copy(),
+                             golden.b.ins_dst[::-1].copy(), golden.b.ins_w[::-1].copy())
+        with pytest.raises(cuda.LvgError) as e:
+            cuda.louvain_dynamic_delta_screening(Y, rev, q, vt, ct)
+        assert e.value.code == cuda.LVG_EINVAL
+
+
+def test_empty_batch_and_empty_graph(cuda, golden, dev):
+    _, Y = dev
+    r = cuda.louvain_dynamic_frontier(Y, cuda.HostBatch.empty(), *prior(golden))
+    assert r.passes >= 1
+    S = 10
+    e = cuda.HostGraph(np.zeros(S + 1, np.uint64), np.zeros(0, np.uint32), np.zeros(0, np.float32),
+                       np.r_[0, np.ones(S - 1)].astype(np.uint8))
+    G = cuda.Graph(e)
+    r = cuda.louvain_static(G)
+    assert r.passes == 0 and r.iterations == 0
+    assert r.membership.tolist() == [0] + list(range(1, S))

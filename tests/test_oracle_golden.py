@@ -1,0 +1,99 @@
+"""The oracle (oracle/louvain_oracle.c) against the golden fixtures.
+
+The fixtures hold the outputs of the reference's own code (made by
+tests/golden/make_golden.py). Integer and index results must match bit for
+bit; the 1-thread runs of the reference are deterministic (sequential sweep),
+so the oracle's 1-thread runs must reproduce them exactly.
+"""
+import numpy as np
+import pytest
+
+from conftest import rows_sorted
+
+
+def test_edge_weight_and_vertex_weights(golden, orc):
+    assert orc.edge_weight(golden.x) / 2 == golden["x_M"]
+    assert orc.edge_weight(golden.y) / 2 == golden["y_M"]
+    assert np.array_equal(orc.vertex_weights(golden.x), golden["x_vtot"])
+
+
+def test_static_one_thread_matches_reference(golden, orc):
+    m, vt, ct, info = orc.louvain(golden.x, 0, threads=1)
+    assert np.array_equal(m, golden["static_m"])
+    assert np.array_equal(vt, golden["static_vt"])
+    assert np.array_equal(ct, golden["static_ct"])
+    assert info["iterations"] == golden["static_iter"]
+    assert info["passes"] == golden["static_pass"]
+    assert info["affectedVertices"] == golden["static_aff"]
+    assert orc.modularity(golden.x, m) == pytest.approx(float(golden["static_q"]), abs=1e-12)
+
+
+def test_batch_weight_update(golden, orc):
+    vt, ct = orc.update_weights(golden.b, golden["static_m"], golden["static_vt"], golden["static_ct"])
+    assert np.array_equal(vt, golden["upd_vt"])
+    assert np.array_equal(ct, golden["upd_ct"])
+
+
+def test_frontier_marking(golden, orc):
+    f = orc.df_mark(golden.y.span, golden.b, golden["static_m"])
+    assert np.array_equal(f, golden["df_flags"])
+
+
+def test_delta_screening_marking(golden, orc):
+    v, n, c = orc.ds_mark(golden.y, golden.b, golden["static_m"], golden["upd_vt"], golden["upd_ct"],
+                          float(golden["y_M"]))
+    assert np.array_equal(v, golden["ds_vertices"])
+    assert np.array_equal(n, golden["ds_neighbors"])
+    assert np.array_equal(c, golden["ds_communities"])
+
+
+def test_aggregation(golden, orc):
+    ren, CN, rows = orc.aggregate(golden.y, golden["static_m"])
+    assert CN == golden["agg_cn"]
+    assert np.array_equal(ren, golden["agg_ren"])
+    r, k, w = [], [], []
+    for c, row in enumerate(rows):
+        for d in sorted(row):
+            r.append(c); k.append(d); w.append(row[d])
+    assert np.array_equal(np.array(r, np.uint32), golden["agg_row"])
+    assert np.array_equal(np.array(k, np.uint32), golden["agg_key"])
+    assert np.array_equal(np.array(w, np.float64), golden["agg_w"])
+
+
+@pytest.mark.parametrize("method,tag", [(1, "nd"), (2, "ds"), (3, "df")])
+def test_dynamic_one_thread_matches_reference(golden, orc, method, tag):
+    m, vt, ct, info = orc.louvain(golden.y, method, golden.b, golden["static_m"], golden["static_vt"],
+                                  golden["static_ct"], threads=1)
+    assert np.array_equal(m, golden[f"{tag}_m"])
+    assert np.array_equal(vt, golden[f"{tag}_vt"])
+    assert np.array_equal(ct, golden[f"{tag}_ct"])
+    assert info["iterations"] == golden[f"{tag}_iter"]
+    assert info["passes"] == golden[f"{tag}_pass"]
+    assert info["affectedVertices"] == golden[f"{tag}_aff"]
+
+
+def test_multithread_quality_within_tolerance(golden, orc):
+    """Asynchronous multi-threaded runs differ run to run; modularity stays within 0.005."""
+    m, *_ = orc.louvain(golden.x, 0, threads=4)
+    assert abs(orc.modularity(golden.x, m) - float(golden["static_q_mean8"])) <= 0.005
+
+
+@pytest.mark.parametrize("method", [0, 3])
+def test_deterministic_replay_is_thread_independent(golden, orc, method):
+    args = (golden.x, 0) if method == 0 else (golden.y, 3, golden.b, golden["static_m"], golden["static_vt"],
+                                              golden["static_ct"])
+    a = orc.louvain(*args, threads=1, sync=True, colors=16)
+    b = orc.louvain(*args, threads=5, sync=True, colors=16)
+    assert np.array_equal(a[0], b[0])
+    assert np.array_equal(a[2], b[2])
+    assert a[3]["iterations"] == b[3]["iterations"]
+
+
+def test_deterministic_replay_quality(golden, orc):
+    m, *_ = orc.louvain(golden.x, 0, threads=2, sync=True, colors=16)
+    assert abs(orc.modularity(golden.x, m) - float(golden["static_q_mean8"])) <= 0.005
+
+
+def test_rows_sorted_helper():
+    r, k, w = rows_sorted(2, np.array([0, 2, 3]), np.array([5, 1, 4]), np.array([1.0, 2.0, 3.0]))
+    assert r.tolist() == [0, 0, 1] and k.tolist() == [1, 5, 4] and w.tolist() == [2.0, 1.0, 3.0]
