@@ -1,0 +1,386 @@
+#!/usr/bin/env python3
+"""Benchmark: dynamic-frontier Louvain edges/s on an R-MAT scale-24 graph.
+
+Workload (the headline configuration): R-MAT scale 24, edge factor 16,
+(a,b,c,d) = (0.57,0.19,0.19,0.05), symmetrized and deduplicated (~5.4e8
+directed edges), FP32 unit weights, uint32 ids, vertex 0 absent. A step is one
+dynamic-frontier Louvain run over one batch of 1e-4 |E| random updates (80 %
+insertions of absent uniform pairs, 20 % deletions of uniformly sampled edges)
+on the updated graph, from the static Louvain result of the base graph.
+
+Arms:
+  default              the GPU library. `value` = |E| / per-step device time
+                       with graph, batch and prior state resident in HBM
+                       (lvg_run_resident, timed by the library's CUDA events);
+                       `e2e` = the same through the drop-in call lvg_frontier
+                       with host arrays (pinned): batch + prior state uploaded,
+                       result downloaded, inside the timed region.
+  --impl reference     the CPU implementation of the path on this host's
+                       cores (the oracle's port of the reference, OpenMP, all
+                       threads), same graph, batch and metric.
+
+Multi-GPU: the path does not shard (replicas only); under torchrun every rank
+runs an independent replica on its own GPU and rank 0 reports the aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "louvain-communities-openmp-dynamic_gb300")
+for _p in (PKG, ROOT):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "DF-Louvain edges/s, HBM GB/s, p99 update latency vs plain GPU at |ΔQ|≤1e-3"
+MOVE_BYTES_PER_EDGE = 12   # neighbour id + weight + neighbour's community
+MOVE_BYTES_PER_VERTEX = 17  # offset + degree + community + weight + flag
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--scale", type=int, default=24)
+    p.add_argument("--edge-factor", type=float, default=16.0)
+    p.add_argument("--batch-fraction", type=float, default=1e-4)
+    p.add_argument("--seed", type=int, default=42)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-steps", type=int, default=2)
+    return p.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier and max-over-ranks with torch.distributed (gloo); no-op for one rank."""
+
+    def __init__(self, world: int):
+        self.world = world
+        self.dist = None
+        if world > 1:
+            import torch.distributed as dist
+
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.dist:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist:
+            self.dist.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_inputs(lvg, args):
+    t = time.time()
+    x = lvg.rmat(args.scale, args.edge_factor, 0.57, 0.19, 0.19, seed=args.seed, permute=True)
+    nupd = max(1, int(round(args.batch_fraction * x.num_edges / 2)))
+    b = lvg.random_batch(x, nupd, 0.8, seed=args.seed + 1)
+    y = lvg.apply_batch(x, b)
+    return x, b, y, nupd, time.time() - t
+
+
+def workload_name(args):
+    return (f"R-MAT scale {args.scale} (ef {args.edge_factor:g}, a/b/c/d .57/.19/.19/.05), dynamic-frontier "
+            f"Louvain per batch of {args.batch_fraction:g}|E| updates (80% ins / 20% del)")
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_per_launch():
+    """DRAM bytes per move launch from the committed ncu summary, if any."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "move_traffic.json")) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
+def cpu_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def run_reference(args):
+    """The CPU implementation (oracle's port of the reference), all host threads."""
+    rank, world, _ = dist_info()
+    if world > 1 and rank != 0:
+        return 0
+    import lvg
+    import lvg_build
+    from oracle import oracle as O
+
+    lvg_build.build_graphgen()
+    O.build(ref=False)
+    orc = O.Oracle()
+    x, b, y, nupd, tgen = make_inputs(lvg, args)
+    T = cpu_threads()
+    opts = O.options()
+    m, vt, ct, info = orc.louvain(x, 0, threads=T, opts=opts)  # prior (untimed), as main.cxx:89
+    times = []
+    for i in range(args.warmup + args.steps):
+        _, _, _, inf = orc.louvain(y, 3, b, m, vt, ct, threads=T, opts=opts)
+        if i >= args.warmup:
+            times.append(inf["time"])
+    ms = float(np.mean(times))
+    value = y.num_edges / (ms / 1e3)
+    line = {"metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": workload_name(args), "vertices": x.order, "edges": y.num_edges,
+                       "batch_updates": nupd, "l2": "inputs larger than L2"},
+            "cpu_baseline": {"value": value, "unit": "edges/s", "cores": T, "kind": "port",
+                             "sample": f"{args.steps} dynamic-frontier runs on the full graph (the port's "
+                                       f"LouvainResult::time: init + mark + passes)"},
+            "e2e": {"value": value, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    rank, world, local = dist_info()
+    os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("CUDA_VISIBLE_DEVICES", ""))
+    dist = Dist(world)
+    import lvg
+    import lvg_build
+
+    lvg_build.build()
+    lvg.set_device(local)  # one replica per GPU, chosen before any handle is created
+    x, b, y, nupd, tgen = make_inputs(lvg, args)
+    S, E = y.span, y.num_edges
+
+    # prior: static Louvain on the base graph (untimed, as main.cxx:89)
+    X = lvg.Graph(x)
+    prior = lvg.louvain_static(X)
+    q_static_base = X.modularity(prior.membership)
+    X.close()
+    del X
+
+    Y = lvg.Graph(y)
+    st_prior, st_out = lvg.State(Y), lvg.State(Y)
+    st_prior.set(prior.membership, prior.vertexWeight, prior.communityWeight)
+    db = lvg.DeviceBatch(Y, b)
+    o = lvg.LouvainOptions()
+
+    # plain GPU static Louvain on the updated graph (the spec comparator)
+    static_times = []
+    for _ in range(2):
+        info = lvg.run_resident(Y, lvg.METHOD_STATIC, None, None, st_out, o)
+        static_times.append(info["time"])
+    m_static = st_out.membership()
+    q_static = Y.modularity(m_static)
+
+    # warm-up + timed DF steps (inputs resident in HBM; device time by CUDA events)
+    for _ in range(args.warmup):
+        lvg.run_resident(Y, lvg.METHOD_FRONTIER, db, st_prior, st_out, o)
+    step_ms, launches = [], 0
+    dist.barrier()
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            info = lvg.run_resident(Y, lvg.METHOD_FRONTIER, db, st_prior, st_out, o)
+            step_ms.append(info["time"])
+            launches += Y.stats()["kernel_launches"]
+    dist.barrier()
+    # the same steps again with per-launch events around the local-moving kernels (roofline)
+    Y.set_profiling(True)
+    kms, kedges, kverts, klaunch, bin_ms, bin_edges = 0.0, 0, 0, 0, np.zeros(12), np.zeros(12)
+    for _ in range(args.steps):
+        lvg.run_resident(Y, lvg.METHOD_FRONTIER, db, st_prior, st_out, o)
+        s = Y.stats()
+        kms += s["move_kernel_ms"]
+        kedges += s["move_edges"]
+        kverts += s["move_vertices"]
+        klaunch += s["move_launches"]
+        bin_ms += np.array(s["move_bin_ms"])
+        bin_edges += np.array(s["move_bin_edges"])
+    Y.set_profiling(False)
+    m_df = st_out.membership()
+    q_df = Y.modularity(m_df)
+    ms = float(np.mean(step_ms))
+    ms_max = dist.max(ms)
+    value = world * E / (ms_max / 1e3)
+
+    # e2e: the drop-in call with host (pinned) arrays
+    pq = lvg.PinnedArray(S, np.uint32)
+    pvt = lvg.PinnedArray(S, np.float64)
+    pct = lvg.PinnedArray(S, np.float64)
+    pq.array[:] = prior.membership
+    pvt.array[:] = prior.vertexWeight
+    pct.array[:] = prior.communityWeight
+    outs = (lvg.PinnedArray(S, np.uint32), lvg.PinnedArray(S, np.float64), lvg.PinnedArray(S, np.float64))
+    ob = tuple(a.array for a in outs)
+    for _ in range(max(1, args.warmup)):
+        lvg.louvain_dynamic_frontier(Y, b, pq.array, pvt.array, pct.array, o, out_buffers=ob)
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        lvg.louvain_dynamic_frontier(Y, b, pq.array, pvt.array, pct.array, o, out_buffers=ob)
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    e2e_ms_max = dist.max(e2e_ms)
+    h2d = b.num_deletions * 12 + b.num_insertions * 12 + S * (4 + 8 + 8)
+    d2h = S * (4 + 8 + 8)
+
+    peak, peak_kind = peaks()
+    achieved = None
+    if kms > 0:
+        # bytes and time of all local-moving launches of the profiled steps
+        achieved = (MOVE_BYTES_PER_EDGE * kedges + MOVE_BYTES_PER_VERTEX * kverts) / (kms / 1e3) / 1e9
+    tr = traffic_per_launch()
+    line = {
+        "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": workload_name(args), "vertices": y.order, "edges": E, "batch_updates": nupd,
+                   "batch_entries": b.num_deletions + b.num_insertions, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (CSR %.1f GB)" % (E * 8 / 1e9)},
+        "e2e": {"value": world * E / (e2e_ms_max / 1e3), "unit": "edges/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms_max,
+                "call": "lvg_frontier (drop-in for louvainDynamicFrontierOmp), pinned host arrays"},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None,
+                     "traffic": tr.get("bytes_per_launch") if tr else None,
+                     "kernel": "local-moving kernels (move_tile/move_block, all degree bins)",
+                     "launches_per_step": klaunch / args.steps, "ms_per_step": kms / args.steps,
+                     "per_bin_ms_per_step": [round(v / args.steps, 4) for v in bin_ms],
+                     "per_bin_edges_per_step": [int(v / args.steps) for v in bin_edges],
+                     "peak_kind": peak_kind,
+                     "algorithmic_bytes": "12 B/scanned edge + 17 B/processed vertex"},
+        "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
+        "static_gpu": {"ms": float(np.mean(static_times)), "edges_per_s": E / (np.mean(static_times) / 1e3),
+                       "modularity": q_static},
+        "df_speedup_vs_static_gpu": float(np.mean(static_times)) / ms,
+        "modularity": {"df": q_df, "static_updated": q_static, "static_base": q_static_base,
+                       "df_minus_static": q_df - q_static},
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args, y, b, prior)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    dist.close()
+    return 0
+
+
+def cpu_baseline(args, y, b, prior):
+    """The oracle's port of the reference, on the same updated graph, batch and prior."""
+    from oracle import oracle as O
+
+    O.build(ref=False)
+    orc = O.Oracle()
+    T = cpu_threads()
+    times, q = [], None
+    for _ in range(max(1, args.cpu_steps)):
+        m, _, _, inf = orc.louvain(y, 3, b, prior.membership, prior.vertexWeight, prior.communityWeight,
+                                   threads=T)
+        times.append(inf["time"])
+        q = m
+    ms = float(np.mean(times))
+    return {"value": y.num_edges / (ms / 1e3), "unit": "edges/s", "cores": T, "kind": "port",
+            "sample": f"{len(times)} dynamic-frontier runs on the full graph from the GPU's static prior "
+                      f"(LouvainResult::time of the port: init + mark + passes)",
+            "ms_per_step": ms, "modularity": orc.modularity(y, q)}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

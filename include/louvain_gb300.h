@@ -220,10 +220,20 @@ typedef struct lvg_stats {
   uint64_t aggregate_edges;    /* edges read by aggregation */
   uint64_t aggregate_launches;
   uint64_t kernel_launches;    /* all kernels launched by the last call */
+  /* Per degree bin of the local-moving kernels (bin b holds degrees in
+   * (4,8,16,32,64,128,256,512,2048,8192 boundaries), bin 0 = degree 0,
+   * bin 11 = above 8192): launch time, vertices processed, edges scanned. */
+  double   move_bin_ms[12];
+  uint64_t move_bin_vertices[12];
+  uint64_t move_bin_edges[12];
 } lvg_stats;
 /* Enable (1) or disable (0) per-launch event timing for calls on g. */
 int lvg_set_profiling(lvg_graph *g, int enable);
 int lvg_get_stats(const lvg_graph *g, lvg_stats *out);
+
+/* Make `device` the calling thread's current GPU; handles created afterwards
+ * live on it (no reference counterpart: the reference is CPU only). */
+int lvg_set_device(int device);
 
 /* Message of the last failure on the calling thread ("" if none). */
 const char *lvg_last_error(void);

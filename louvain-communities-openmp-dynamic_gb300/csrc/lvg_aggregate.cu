@@ -149,6 +149,8 @@ __global__ void __launch_bounds__(TILE_BLOCK) agg_tile_kernel(AggArgs a) {
 }
 
 // One block per community; each warp flattens a 32-member chunk at a time.
+// The block's table region holds 2^log2cap slots; each community uses the
+// smallest power of two >= 2x min(total degree, community count).
 template <int B, bool GLOBAL>
 __global__ void __launch_bounds__(B) agg_block_kernel(AggArgs a, int log2cap) {
   extern __shared__ __align__(16) uint8_t smem[];
@@ -170,19 +172,21 @@ __global__ void __launch_bounds__(B) agg_block_kernel(AggArgs a, int log2cap) {
   for (uint32_t i = blockIdx.x; i < a.count; i += gridDim.x) {
     const uint32_t c = a.list[i];
     const uint32_t m0 = a.coff[c], m1 = a.coff[c + 1];
-    for (uint32_t s = threadIdx.x; s < cap; s += B) { keys[s] = EMPTY; vals[s] = 0.f; }
+    const uint64_t y0 = a.yoff[c], tdeg = a.yoff[c + 1] - y0;
+    const int lg = min(log2cap, max(1, ceil_log2(2ull * (tdeg < a.cn ? tdeg : a.cn))));
+    const uint32_t ccap = 1u << lg;
+    for (uint32_t s = threadIdx.x; s < ccap; s += B) { keys[s] = EMPTY; vals[s] = 0.f; }
     if (threadIdx.x == 0) s_cnt = 0;
     __syncthreads();
     for (uint32_t b0 = m0 + uint32_t(wid) * 32; b0 < m1; b0 += B) {
       const uint32_t b1 = b0 + 32 < m1 ? b0 + 32 : m1;
-      nread += insert_members<32>(a, b0, b1, lane, 0xffffffffu, keys, vals, log2cap, ok);
+      nread += insert_members<32>(a, b0, b1, lane, 0xffffffffu, keys, vals, lg, ok);
     }
     __syncthreads();
-    const uint64_t y0 = a.yoff[c];
     float vsum = 0.f;
-    for (uint32_t s0 = 0; s0 < cap; s0 += B) {
+    for (uint32_t s0 = 0; s0 < ccap; s0 += B) {
       const uint32_t s = s0 + threadIdx.x;
-      const uint32_t k = s < cap ? keys[s] : EMPTY;
+      const uint32_t k = s < ccap ? keys[s] : EMPTY;
       const bool has = k != EMPTY;
       const unsigned bal = __ballot_sync(0xffffffffu, has);
       uint32_t base = 0;

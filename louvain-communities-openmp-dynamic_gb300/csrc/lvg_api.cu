@@ -263,8 +263,10 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const 
   }
   int l = 0;
   double el = 0;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> bin_ev;
   while (l < L) {
     LVG_CUDA(cudaMemsetAsync(&g->ctr.p->el_fix, 0, sizeof(unsigned long long), s));
+    bin_ev.clear();
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (g->profiling) e0 = g->events.record(s);
     for (int k = 0; k < K; ++k) {
@@ -277,9 +279,11 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const 
         a.count = uint32_t(cnt);
         a.vcom = com; a.ctot = ctot; a.dec = W.dec.p;
         a.vaff = W.vaff.p; a.mark = W.mark.p; a.fa = fa; a.vtot = tot;
-        a.kr = kr; a.ctr = g->ctr.p;
+        a.kr = kr; a.ctr = g->ctr.p; a.bin = b;
         a.gkeys = W.gkeys.p; a.gvals = W.gvals.p; a.glog2 = glog2;
+        cudaEvent_t b0 = g->profiling ? g->events.record(s) : nullptr;
         launch_move_bin(b, sync, a, s);
+        if (g->profiling) bin_ev.push_back({b, {b0, g->events.record(s)}});
         ++g->stats.move_launches;
       }
       if (sync) {
@@ -290,7 +294,10 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const 
     }
     if (g->profiling) e1 = g->events.record(s);
     read_counters(g);
-    if (g->profiling) g->stats.move_kernel_ms += elapsed(e0, e1);
+    if (g->profiling) {
+      g->stats.move_kernel_ms += elapsed(e0, e1);
+      for (auto &be : bin_ev) g->stats.move_bin_ms[be.first] += elapsed(be.second.first, be.second.second);
+    }
     el = double(g->hctr.p->el_fix) / GAIN_FIX / M;
     ++l;
     if (el <= E) break;
@@ -342,7 +349,7 @@ Level aggregate(lvg_graph *g, const Level &lv, const uint32_t *com, size_t CN, i
     a.list = W.cbins.p + cb[b];
     a.count = uint32_t(cnt);
     a.yoff = nl.off; a.ydeg = nl.deg; a.ykey = nl.key; a.yw = nl.w;
-    a.vtot = W.vtot.p; a.ctr = g->ctr.p;
+    a.vtot = W.vtot.p; a.ctr = g->ctr.p; a.cn = uint32_t(CN);
     a.gkeys = W.gkeys.p; a.gvals = W.gvals.p; a.glog2 = glog2;
     launch_aggregate_bin(b, a, s);
     ++g->stats.aggregate_launches;
@@ -477,6 +484,10 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
   g->stats.move_edges = g->hctr.p->edges;
   g->stats.moves = g->hctr.p->moves;
   g->stats.aggregate_edges = g->hctr.p->agg_edges;
+  for (int b = 0; b < NUM_BINS; ++b) {
+    g->stats.move_bin_vertices[b] = g->hctr.p->bin_vertices[b];
+    g->stats.move_bin_edges[b] = g->hctr.p->bin_edges[b];
+  }
   g->stats.kernel_launches = launch_counter() - launches0;
 }
 
@@ -849,6 +860,13 @@ void *lvg_host_alloc(size_t bytes) {
 
 void lvg_host_free(void *p) {
   if (p) cudaFreeHost(p);
+}
+
+int lvg_set_device(int device) {
+  return lvg::guarded([&] {
+    LVG_CUDA(cudaSetDevice(device));
+    return LVG_OK;
+  });
 }
 
 int lvg_set_profiling(lvg_graph *g, int enable) {

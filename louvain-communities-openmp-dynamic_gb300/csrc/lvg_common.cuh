@@ -125,6 +125,9 @@ __device__ __forceinline__ unsigned long long gain_to_fix(float g) {
   return (unsigned long long)__float2ll_rn(g * 65536.0f);
 }
 
+// Smallest l with 2^l >= x (x >= 1).
+__device__ __forceinline__ int ceil_log2(uint64_t x) { return x <= 1 ? 0 : 64 - __clzll(x - 1); }
+
 template <class T>
 __device__ __forceinline__ T ld_relaxed(const T *p) {
   return *((const volatile T *)p);

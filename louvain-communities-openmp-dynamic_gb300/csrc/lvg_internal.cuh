@@ -39,6 +39,8 @@ struct Counters {
   unsigned int err;              // ERR_* bits
   unsigned int cn;               // community count
   double fp64[4];                // FP64 reductions (total weight, modularity terms)
+  unsigned long long bin_vertices[NUM_BINS];  // processed vertices per degree bin
+  unsigned long long bin_edges[NUM_BINS];     // scanned edges per degree bin
 };
 
 // Arguments of the local-moving kernels (inc/louvain.hxx:588-609).
@@ -57,6 +59,7 @@ struct MoveArgs {
   const uint8_t *fa;     // may the vertex move (delta-screening pass 0), or nullptr
   const float *vtot;     // vertex weights
   float kr;              // R / (2M)
+  int bin;               // degree bin of the list (statistics)
   Counters *ctr;
   uint32_t *gkeys;       // global tables (bin 11): [grid][gcap]
   float *gvals;
@@ -79,6 +82,7 @@ struct AggArgs {
   uint32_t *ykey;
   float *yw;
   float *vtot;           // output level's vertex weights (row sums)
+  uint32_t cn;           // number of communities (distinct keys per row <= cn)
   Counters *ctr;
   uint32_t *gkeys;
   float *gvals;

@@ -62,7 +62,7 @@ __device__ __forceinline__ void take_better(float &bg, uint32_t &bc, float og, u
   if (better(og, oc, bg, bc)) { bg = og; bc = oc; }
 }
 
-__device__ __forceinline__ void flush_counters(Counters *ctr, unsigned long long fix, unsigned long long nv,
+__device__ __forceinline__ void flush_counters(Counters *ctr, int bin, unsigned long long fix, unsigned long long nv,
                                                unsigned long long ne, unsigned long long nm, bool bad) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -74,8 +74,8 @@ __device__ __forceinline__ void flush_counters(Counters *ctr, unsigned long long
   bool anybad = __any_sync(0xffffffffu, bad);
   if ((threadIdx.x & 31) == 0) {
     if (fix) atomicAdd(&ctr->el_fix, fix);
-    if (nv) atomicAdd(&ctr->vertices, nv);
-    if (ne) atomicAdd(&ctr->edges, ne);
+    if (nv) { atomicAdd(&ctr->vertices, nv); atomicAdd(&ctr->bin_vertices[bin], nv); }
+    if (ne) { atomicAdd(&ctr->edges, ne); atomicAdd(&ctr->bin_edges[bin], ne); }
     if (nm) atomicAdd(&ctr->moves, nm);
     if (anybad) atomicOr(&ctr->err, ERR_TABLE_FULL);
   }
@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(TILE_BLOCK) move_tile_kernel(MoveArgs a) {
     bad |= !ok;
     __syncwarp(m);
   }
-  flush_counters(a.ctr, fix, nv, ne, nm, bad);
+  flush_counters(a.ctr, a.bin, fix, nv, ne, nm, bad);
 }
 
 // ------------------------------------------------------------ block kernel
@@ -207,7 +207,8 @@ __device__ __forceinline__ void block_argmax(float &bg, uint32_t &bc, float *rg,
 }
 
 // One block per vertex. GLOBAL = table in global memory (bin 11), else in
-// dynamic shared memory of 2^log2cap slots.
+// dynamic shared memory; the block's region holds 2^log2cap slots and each
+// vertex uses the smallest power of two >= 2x its degree.
 template <int B, bool GLOBAL, bool SYNC>
 __global__ void __launch_bounds__(B) move_block_kernel(MoveArgs a, int log2cap) {
   extern __shared__ __align__(16) uint8_t smem[];
@@ -236,7 +237,9 @@ __global__ void __launch_bounds__(B) move_block_kernel(MoveArgs a, int log2cap) 
     const uint64_t o = a.off[u];
     const uint32_t dg = a.deg[u];
     const uint32_t d = a.vcom[u];
-    for (uint32_t s = threadIdx.x; s < cap; s += B) { keys[s] = EMPTY; vals[s] = 0.f; }
+    const int lg = min(log2cap, max(1, ceil_log2(2ull * dg)));
+    const uint32_t vcap = 1u << lg;
+    for (uint32_t s = threadIdx.x; s < vcap; s += B) { keys[s] = EMPTY; vals[s] = 0.f; }
     __syncthreads();
     float kd = 0.f;
     bool ok = true;
@@ -246,14 +249,14 @@ __global__ void __launch_bounds__(B) move_block_kernel(MoveArgs a, int log2cap) 
       const float ww = a.w[o + j];
       const uint32_t c = a.vcom[v];
       if (c == d) kd += ww;
-      else ok &= table_add(keys, vals, log2cap, c, ww);
+      else ok &= table_add(keys, vals, lg, c, ww);
     }
     kd = block_sum<B>(kd, red_g);  // includes a barrier: table complete
     const float wu = a.vtot[u];
     const float td = a.ctot[d];
     float bg = 0.f;
     uint32_t bc = EMPTY;
-    for (uint32_t s = threadIdx.x; s < cap; s += B) {
+    for (uint32_t s = threadIdx.x; s < vcap; s += B) {
       const uint32_t c = keys[s];
       if (c == EMPTY) continue;
       const float g = gain_f32(vals[s], kd, wu, a.ctot[c], td, a.kr);
@@ -289,7 +292,7 @@ __global__ void __launch_bounds__(B) move_block_kernel(MoveArgs a, int log2cap) 
     bad |= !ok;
     __syncthreads();
   }
-  flush_counters(a.ctr, fix, nv, ne, nm, bad);
+  flush_counters(a.ctr, a.bin, fix, nv, ne, nm, bad);
 }
 
 int g_num_sms = 0;

@@ -77,7 +77,8 @@ class _Stats(C.Structure):
     _fields_ = [("move_kernel_ms", C.c_double), ("move_launches", C.c_uint64), ("move_vertices", C.c_uint64),
                 ("move_edges", C.c_uint64), ("moves", C.c_uint64), ("aggregate_kernel_ms", C.c_double),
                 ("aggregate_edges", C.c_uint64), ("aggregate_launches", C.c_uint64),
-                ("kernel_launches", C.c_uint64)]
+                ("kernel_launches", C.c_uint64), ("move_bin_ms", C.c_double * 12),
+                ("move_bin_vertices", C.c_uint64 * 12), ("move_bin_edges", C.c_uint64 * 12)]
 
 
 class _Csr(C.Structure):
@@ -135,6 +136,7 @@ def load_library() -> C.CDLL:
     L.lvg_host_alloc.restype = vp
     L.lvg_host_free.argtypes = [vp]
     L.lvg_set_profiling.argtypes = [vp, i32]
+    L.lvg_set_device.argtypes = [i32]
     L.lvg_get_stats.argtypes = [vp, C.POINTER(_Stats)]
     L.lvg_state_create.argtypes = [vp, C.POINTER(vp)]
     L.lvg_state_set.argtypes = [vp, _u32p, _f64p, _f64p]
@@ -424,7 +426,11 @@ class Graph:
     def stats(self) -> dict:
         s = _Stats()
         _check(self._L.lvg_get_stats(self.h, C.byref(s)))
-        return {k: getattr(s, k) for k, _ in _Stats._fields_}
+        out = {}
+        for k, _ in _Stats._fields_:
+            v = getattr(s, k)
+            out[k] = list(v) if hasattr(v, "__len__") else v
+        return out
 
 
 def affected_vertices(y: Graph, method: int, batch: HostBatch, q, qvtot, qctot, o: LouvainOptions | None = None):
@@ -581,6 +587,11 @@ def run_resident(g: Graph, method: int, batch: DeviceBatch | None, prior: State 
     _check(L.lvg_run_resident(g.h, method, batch.h if batch else None, prior.h if prior else None, out.h,
                               C.byref(opt), C.byref(r)))
     return _scalars(r)
+
+
+def set_device(device: int) -> None:
+    """Make `device` the current GPU of the calling thread (lvg_set_device)."""
+    _check(load_library().lvg_set_device(device))
 
 
 class PinnedArray:
