@@ -231,6 +231,34 @@ typedef struct lvg_stats {
 int lvg_set_profiling(lvg_graph *g, int enable);
 int lvg_get_stats(const lvg_graph *g, lvg_stats *out);
 
+/* ---- Modularity without device allocation. No counterpart in the reference.
+ * For callers that cannot allocate device memory when they call in (a host
+ * framework that has reserved the GPU's memory for its own pool, a
+ * latency-critical loop that must not pay cudaMalloc's cost and implicit
+ * synchronisation, or a deployment that forbids allocation after start-up).
+ * Same result as lvg_modularity, but every pointer is a caller-owned DEVICE
+ * pointer: offsets[span+1], keys/weights[offsets[span]], exists[span] (may be
+ * NULL: every slot exists), membership[span], and out (one double, written on
+ * the device). M <= 0 means half the total edge weight. `stream` is a
+ * cudaStream_t (NULL: the default stream); the call is asynchronous on it.
+ * The function allocates nothing: its scratch is a fixed device array of
+ * LVG_NOALLOC_MAX_SPAN doubles (8 MiB) that every GPU loading the library
+ * holds until the process exits; spans above that return LVG_EINVAL. The
+ * first call on a device looks up that array's device address (make that
+ * first call before any stream capture). All calls share the array: calls
+ * that overlap on the GPU (other streams, other host threads) race and must
+ * be serialised by the caller. An id >= span in membership or keys makes
+ * *out NaN. */
+#define LVG_NOALLOC_MAX_SPAN (1u << 20)
+int lvg_modularity_noalloc(size_t span, const uint64_t *offsets, const uint32_t *keys, const float *weights,
+                           const uint8_t *exists, const uint32_t *membership, double M, double R, double *out,
+                           void *stream);
+
+/* Start / stop the CUDA profiler's collection (cudaProfilerStart/Stop), so a
+ * profiler started with collection off captures only the bracketed calls. */
+int lvg_profiler_start(void);
+int lvg_profiler_stop(void);
+
 /* Make `device` the calling thread's current GPU; handles created afterwards
  * live on it (no reference counterpart: the reference is CPU only). */
 int lvg_set_device(int device);

@@ -15,6 +15,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda_profiler_api.h>
+
 #include "lvg_internal.cuh"
 
 namespace lvg {
@@ -620,6 +622,9 @@ int run_host(lvg_graph *g, int method, const lvg_batch *b, const uint32_t *q, co
 }
 
 }  // namespace
+
+int fail_noalloc(int code, const char *msg) { return fail(code, msg); }
+
 }  // namespace lvg
 
 // ==================================================================== C-ABI
@@ -860,6 +865,20 @@ void *lvg_host_alloc(size_t bytes) {
 
 void lvg_host_free(void *p) {
   if (p) cudaFreeHost(p);
+}
+
+int lvg_profiler_start(void) {
+  return lvg::guarded([&] {
+    LVG_CUDA(cudaProfilerStart());
+    return LVG_OK;
+  });
+}
+
+int lvg_profiler_stop(void) {
+  return lvg::guarded([&] {
+    LVG_CUDA(cudaProfilerStop());
+    return LVG_OK;
+  });
 }
 
 int lvg_set_device(int device) {

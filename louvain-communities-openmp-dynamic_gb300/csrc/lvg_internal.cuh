@@ -149,6 +149,10 @@ void launch_move_bin(int b, bool sync, const MoveArgs &a, cudaStream_t s);
 // ---------------------------------------------------------------- aggregation (lvg_aggregate.cu)
 void launch_aggregate_bin(int b, const AggArgs &a, cudaStream_t s);
 
+// Record a failure message for lvg_last_error() and return `code` (for entry
+// points outside lvg_api.cu).
+int fail_noalloc(int code, const char *msg);
+
 // Global-table capacity (log2) for a maximum degree.
 inline int global_table_log2(uint64_t maxdeg) {
   int l = 1;

@@ -137,6 +137,7 @@ def load_library() -> C.CDLL:
     L.lvg_host_free.argtypes = [vp]
     L.lvg_set_profiling.argtypes = [vp, i32]
     L.lvg_set_device.argtypes = [i32]
+    L.lvg_modularity_noalloc.argtypes = [sz, vp, vp, vp, vp, vp, f64, f64, vp, vp]
     L.lvg_get_stats.argtypes = [vp, C.POINTER(_Stats)]
     L.lvg_state_create.argtypes = [vp, C.POINTER(vp)]
     L.lvg_state_set.argtypes = [vp, _u32p, _f64p, _f64p]
@@ -589,9 +590,28 @@ def run_resident(g: Graph, method: int, batch: DeviceBatch | None, prior: State 
     return _scalars(r)
 
 
+def profiler_start() -> None:
+    _check(load_library().lvg_profiler_start())
+
+
+def profiler_stop() -> None:
+    _check(load_library().lvg_profiler_stop())
+
+
 def set_device(device: int) -> None:
     """Make `device` the current GPU of the calling thread (lvg_set_device)."""
     _check(load_library().lvg_set_device(device))
+
+
+NOALLOC_MAX_SPAN = 1 << 20
+
+
+def modularity_noalloc(span: int, d_offsets: int, d_keys: int, d_weights: int, d_exists: int | None,
+                       d_membership: int, d_out: int, M: float = 0.0, R: float = 1.0, stream: int | None = None) -> None:
+    """lvg_modularity_noalloc: modularity into *d_out from caller-owned device buffers
+    (raw device addresses), without any device allocation; asynchronous on `stream`."""
+    _check(load_library().lvg_modularity_noalloc(span, d_offsets, d_keys, d_weights, d_exists, d_membership,
+                                                 M, R, d_out, stream))
 
 
 class PinnedArray:
