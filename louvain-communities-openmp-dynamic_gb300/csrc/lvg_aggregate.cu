@@ -12,10 +12,13 @@
 // super-vertex's weight (louvainVertexWeightsOmpW on the new level, :1209).
 //
 // Communities are binned by total degree like vertices in the move kernels:
-// sub-warp tiles / warps with shared tables, blocks with large shared tables,
-// and blocks with per-block global tables. Inside a tile, the members' edge
+// sub-warp tiles / warps with shared tables for small communities, blocks
+// with shared tables (and a global-memory fallback when a community has too
+// many distinct neighbours) for large ones. Inside a tile, the members' edge
 // lists are flattened with a tile prefix scan over member degrees, so lanes
-// stay busy whatever the member degrees are.
+// stay busy whatever the member degrees are. Internal edges (into the
+// community itself, the hottest key) are summed privately per lane and added
+// once.
 #include "lvg_internal.cuh"
 
 namespace lvg {
@@ -46,12 +49,15 @@ __device__ __forceinline__ bool table_add(KP keys, VP vals, int log2cap, uint32_
   return false;
 }
 
-// Insert all edges of members cmem[m0..m1) into the table, T lanes
-// cooperating (T = tile size, lanes tl = 0..T-1, mask m). Returns edges read.
-template <int T, class KP, class VP>
-__device__ __forceinline__ uint64_t insert_members(const AggArgs &a, uint32_t m0, uint32_t m1, int tl, unsigned m,
-                                                   KP keys, VP vals, int log2cap, bool &ok) {
+// Visit all edges of members cmem[m0..m1), T lanes cooperating (tile mask
+// m). Edges into the community itself (`self`, the hottest key: every
+// internal edge) are summed in the lane-private `self_w`; the others go to
+// `add(key, weight)`, which returns false to stop early. Returns edges read.
+template <int T, class Add>
+__device__ __forceinline__ uint64_t visit_members(const AggArgs &a, uint32_t m0, uint32_t m1, int tl, unsigned m,
+                                                  uint32_t self, float &self_w, Add add) {
   uint64_t nread = 0;
+  bool go = true;
   for (uint32_t base = m0; base < m1; base += T) {
     const uint32_t mm = base + tl;
     uint32_t dg = 0;
@@ -82,9 +88,12 @@ __device__ __forceinline__ uint64_t insert_members(const AggArgs &a, uint32_t m0
       const uint32_t oincl = __shfl_sync(m, incl, lo, T);
       const uint32_t odeg = __shfl_sync(m, dg, lo, T);
       const uint64_t oo = __shfl_sync(m, o, lo, T);
-      if (k < total) {
+      if (go && k < total) {
         const uint64_t e = oo + (k - (oincl - odeg));
-        ok &= table_add(keys, vals, log2cap, a.vcom[a.key[e]], a.w[e]);
+        const uint32_t c = a.vcom[a.key[e]];
+        const float w = a.w[e];
+        if (c == self) self_w += w;
+        else go = add(c, w);
       }
     }
   }
@@ -113,7 +122,15 @@ __global__ void __launch_bounds__(TILE_BLOCK) agg_tile_kernel(AggArgs a) {
 #pragma unroll
     for (int s = tl; s < C; s += T) { keys[s] = EMPTY; vals[s] = 0.f; }
     __syncwarp(m);
-    nread += insert_members<T>(a, m0, m1, tl, m, keys, vals, LOGC, ok);
+    float self_w = 0.f;
+    nread += visit_members<T>(a, m0, m1, tl, m, c, self_w, [&](uint32_t k, float w) {
+      ok &= table_add(keys, vals, LOGC, k, w);
+      return true;
+    });
+#pragma unroll
+    for (int sh = T / 2; sh > 0; sh >>= 1) self_w += __shfl_xor_sync(m, self_w, sh, T);
+    __syncwarp(m);
+    if (tl == 0 && self_w != 0.f) ok &= table_add(keys, vals, LOGC, c, self_w);
     __syncwarp(m);
     const uint64_t y0 = a.yoff[c];
     uint32_t cnt = 0;
@@ -148,40 +165,91 @@ __global__ void __launch_bounds__(TILE_BLOCK) agg_tile_kernel(AggArgs a) {
   }
 }
 
-// One block per community; each warp flattens a 32-member chunk at a time.
-// The block's table region holds 2^log2cap slots; each community uses the
-// smallest power of two >= 2x min(total degree, community count).
-template <int B, bool GLOBAL>
-__global__ void __launch_bounds__(B) agg_block_kernel(AggArgs a, int log2cap) {
+__device__ __forceinline__ bool smem_add_budget(uint32_t *keys, float *vals, int log2cap, uint32_t c, float w,
+                                                unsigned *used, unsigned limit) {
+  const uint32_t mask = (1u << log2cap) - 1u;
+  uint32_t s = hash_hi(c, log2cap);
+  for (uint32_t probe = 0; probe <= mask; ++probe) {
+    uint32_t k = keys[s];
+    if (k == c) { atomicAdd(&vals[s], w); return true; }
+    if (k == EMPTY) {
+      if (atomicAdd(used, 1u) >= limit) return false;
+      uint32_t prev = atomicCAS(&keys[s], EMPTY, c);
+      if (prev == EMPTY || prev == c) { atomicAdd(&vals[s], w); return true; }
+    }
+    s = (s + 1u) & mask;
+  }
+  return false;
+}
+
+// One block per community (total degree > 512); each warp flattens a
+// 32-member chunk at a time. The community is merged in a shared table of
+// 2^LOGS slots with a claim budget (half the slots); a community with more
+// distinct neighbour communities is redone with a table in its block's
+// region of global memory (2^a.glog2 slots). The table holds
+// min(total degree, community count) * 2 slots rounded up to a power of two.
+template <int B, int LOGS>
+__global__ void __launch_bounds__(B) agg_block_kernel(AggArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
   __shared__ uint32_t s_cnt;
   __shared__ float s_sum[B / 32];
-  const uint32_t cap = 1u << log2cap;
+  __shared__ unsigned s_used;
+  __shared__ int s_over;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  uint32_t *keys;
-  float *vals;
-  if (GLOBAL) {
-    keys = a.gkeys + size_t(blockIdx.x) * cap;
-    vals = a.gvals + size_t(blockIdx.x) * cap;
-  } else {
-    keys = reinterpret_cast<uint32_t *>(smem);
-    vals = reinterpret_cast<float *>(smem + size_t(cap) * sizeof(uint32_t));
-  }
+  uint32_t *skeys = reinterpret_cast<uint32_t *>(smem);
+  float *svals = reinterpret_cast<float *>(smem + (size_t(1) << LOGS) * sizeof(uint32_t));
+  uint32_t *gkeys = a.gkeys ? a.gkeys + (size_t(blockIdx.x) << a.glog2) : nullptr;
+  float *gvals = a.gvals ? a.gvals + (size_t(blockIdx.x) << a.glog2) : nullptr;
   unsigned long long nread = 0;
   bool ok = true;
   for (uint32_t i = blockIdx.x; i < a.count; i += gridDim.x) {
     const uint32_t c = a.list[i];
     const uint32_t m0 = a.coff[c], m1 = a.coff[c + 1];
     const uint64_t y0 = a.yoff[c], tdeg = a.yoff[c + 1] - y0;
-    const int lg = min(log2cap, max(1, ceil_log2(2ull * (tdeg < a.cn ? tdeg : a.cn))));
-    const uint32_t ccap = 1u << lg;
-    for (uint32_t s = threadIdx.x; s < ccap; s += B) { keys[s] = EMPTY; vals[s] = 0.f; }
-    if (threadIdx.x == 0) s_cnt = 0;
+    const uint64_t want = 2ull * (tdeg < a.cn ? tdeg : a.cn);
+    int lg = min(LOGS, max(1, ceil_log2(want)));
+    uint32_t ccap = 1u << lg;
+    for (uint32_t s = threadIdx.x; s < ccap; s += B) { skeys[s] = EMPTY; svals[s] = 0.f; }
+    if (threadIdx.x == 0) { s_cnt = 0; s_used = 0; s_over = 0; }
     __syncthreads();
+    const unsigned limit = ccap >> 1;
+    float self_w = 0.f;
+    uint64_t nr = 0;
     for (uint32_t b0 = m0 + uint32_t(wid) * 32; b0 < m1; b0 += B) {
       const uint32_t b1 = b0 + 32 < m1 ? b0 + 32 : m1;
-      nread += insert_members<32>(a, b0, b1, lane, 0xffffffffu, keys, vals, lg, ok);
+      nr += visit_members<32>(a, b0, b1, lane, 0xffffffffu, c, self_w, [&](uint32_t k, float w) {
+        if (smem_add_budget(skeys, svals, lg, k, w, &s_used, limit)) return true;
+        s_over = 1;
+        return false;
+      });
     }
+    __syncthreads();
+    uint32_t *keys = skeys;
+    float *vals = svals;
+    if (s_over) {
+      lg = min(a.glog2, max(1, ceil_log2(want)));
+      ccap = 1u << lg;
+      keys = gkeys;
+      vals = gvals;
+      if (!keys) { ok = false; ccap = 0; }
+      for (uint32_t s = threadIdx.x; s < ccap; s += B) { keys[s] = EMPTY; vals[s] = 0.f; }
+      __syncthreads();
+      self_w = 0.f;
+      nr = 0;
+      if (keys)
+        for (uint32_t b0 = m0 + uint32_t(wid) * 32; b0 < m1; b0 += B) {
+          const uint32_t b1 = b0 + 32 < m1 ? b0 + 32 : m1;
+          nr += visit_members<32>(a, b0, b1, lane, 0xffffffffu, c, self_w, [&](uint32_t k, float w) {
+            ok &= table_add(keys, vals, lg, k, w);
+            return true;
+          });
+        }
+    }
+    nread += nr;
+    // internal weight: one insertion per warp
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) self_w += __shfl_xor_sync(0xffffffffu, self_w, o);
+    if (lane == 0 && self_w != 0.f && ccap) ok &= table_add(keys, vals, lg, c, self_w);
     __syncthreads();
     float vsum = 0.f;
     for (uint32_t s0 = 0; s0 < ccap; s0 += B) {
@@ -252,16 +320,15 @@ void launch_tile(const AggArgs &a, cudaStream_t s) {
   LVG_CHECK_LAUNCH();
 }
 
-template <int B, int LOGC>
-void launch_block_smem(const AggArgs &a, cudaStream_t s) {
-  const size_t smem = (size_t(1) << LOGC) * 8;
-  auto k = agg_block_kernel<B, false>;
+template <int B, int LOGS>
+void launch_big(const AggArgs &a, cudaStream_t s) {
+  const size_t smem = (size_t(1) << LOGS) * 8;
+  auto k = agg_block_kernel<B, LOGS>;
   static bool configured = false;
   if (!configured) { set_smem(k, smem); configured = true; }
-  size_t cap = size_t(sms()) * (smem > 64 * 1024 ? 1 : 2);
-  unsigned grid = unsigned(a.count < cap ? a.count : cap);
+  unsigned grid = unsigned(global_table_blocks(a.count));
   if (!grid) return;
-  k<<<grid, B, smem, s>>>(a, LOGC);
+  k<<<grid, B, smem, s>>>(a);
   LVG_CHECK_LAUNCH();
 }
 
@@ -277,15 +344,9 @@ void launch_aggregate_bin(int b, const AggArgs &a, cudaStream_t s) {
     case 6: launch_tile<32, 256>(a, s); break;
     case 7: launch_tile<32, 512>(a, s); break;
     case 8: launch_tile<32, 1024>(a, s); break;
-    case 9: launch_block_smem<256, 12>(a, s); break;
-    case 10: launch_block_smem<512, 14>(a, s); break;
-    case 11: {
-      unsigned grid = unsigned(global_table_blocks(a.count));
-      if (!grid) return;
-      agg_block_kernel<512, true><<<grid, 512, 0, s>>>(a, a.glog2);
-      LVG_CHECK_LAUNCH();
-      break;
-    }
+    case 9: launch_big<256, 12>(a, s); break;
+    case 10: launch_big<512, 13>(a, s); break;
+    case 11: launch_big<512, 13>(a, s); break;
     default: break;
   }
 }

@@ -62,10 +62,17 @@ struct HBuf {  // pinned host buffer
   }
 };
 
+struct HubPlanBuffers {
+  DBuf<uint32_t> hub_vertex, hub_first, degs;
+  DBuf<uint4> chunk;
+  DBuf<uint64_t> chunk_part;
+};
+
 struct LevelBuffers {
   DBuf<uint64_t> off;
   DBuf<uint32_t> deg, key, bins;
   DBuf<float> w;
+  HubPlanBuffers hubplan;
 };
 
 struct Workspace {
@@ -82,6 +89,9 @@ struct Workspace {
   DBuf<uint32_t> prior_q;
   DBuf<float> prior_vt, prior_ct;
   DBuf<double> stage_a, stage_b;
+  // chunked hub path
+  DBuf<uint32_t> chunk_cnt, part_key;
+  DBuf<float> part_val, hub_kd;
 
   void allocate(size_t S_, size_t X_, cudaStream_t st) {
     S = S_;
@@ -102,6 +112,8 @@ struct Workspace {
     }
     LVG_CUDA(cudaMemsetAsync(mark.p, 0, S, st));
     LVG_CUDA(cudaMemsetAsync(dec.p, 0xFF, S * sizeof(uint32_t), st));
+    hub_kd.ensure(S);
+    LVG_CUDA(cudaMemsetAsync(hub_kd.p, 0, S * sizeof(float), st));
   }
 };
 
@@ -156,6 +168,7 @@ struct lvg_graph {
   DBuf<uint32_t> deg, key, bins;
   DBuf<float> w;
   DBuf<uint8_t> ex;
+  HubPlanBuffers hubplan;  // chunked hub work of the uploaded level
   double total_weight = 0;
   std::unique_ptr<Workspace> ws;
   DBuf<Counters> ctr;
@@ -217,6 +230,7 @@ void read_counters(lvg_graph *g) {
   if (g->hctr.p->err) {
     unsigned e = g->hctr.p->err;
     LVG_CUDA(cudaMemsetAsync(&g->ctr.p->err, 0, sizeof(unsigned), g->stream));
+    if (e & ERR_BAD_ID) throw Error(LVG_EINVAL, "prior membership id >= span");
     throw Error(LVG_ETIMEOUT, "device hash table overflow guard tripped (err=" + std::to_string(e) + ")");
   }
 }
@@ -226,6 +240,65 @@ void compute_bins(lvg_graph *g, Level &lv, const uint32_t *deg, uint32_t *list, 
   lv.colors = colors;
   bin_items_u32(deg, lv.ex, lv.span, colors, list, lv.bin_start, lv.bin_maxdeg, scratch, g->hbins.p, g->stream);
   lv.bins = list;
+}
+
+// Chunked work of degree bin 11 (see HubPlan): hubs in colour order, each
+// hub's edges cut into HUB_CHUNK-edge chunks with a partial region of the
+// chunk's size. Built on the host from the hubs' degrees (synchronises).
+void build_hub_plan(lvg_graph *g, Level &lv, HubPlanBuffers &hb) {
+  cudaStream_t s = g->stream;
+  HubPlan &P = lv.hub;
+  P = HubPlan{};
+  const int K = lv.colors;
+  size_t H = 0;
+  for (int k = 0; k < K; ++k) {
+    P.hub_begin[k] = H;
+    H += lv.bucket_size(k, NUM_BINS - 1);
+  }
+  P.hub_begin[K] = H;
+  P.hubs = H;
+  if (!H) return;
+  hb.hub_vertex.ensure(H);
+  hb.degs.ensure(H);
+  for (int k = 0; k < K; ++k) {
+    const size_t n = lv.bucket_size(k, NUM_BINS - 1);
+    if (n)
+      LVG_CUDA(cudaMemcpyAsync(hb.hub_vertex.p + P.hub_begin[k], lv.bins + lv.bucket_begin(k, NUM_BINS - 1),
+                               n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+  }
+  launch_gather_u32(hb.hub_vertex.p, H, lv.deg, hb.degs.p, s);
+  std::vector<uint32_t> degs(H), first(H + 1);
+  LVG_CUDA(cudaMemcpyAsync(degs.data(), hb.degs.p, H * 4, cudaMemcpyDeviceToHost, s));
+  LVG_CUDA(cudaStreamSynchronize(s));
+  std::vector<uint4> chunks;
+  std::vector<uint64_t> parts;
+  uint64_t part = 0;
+  for (int k = 0; k < K; ++k) {
+    P.chunk_begin[k] = chunks.size();
+    for (size_t h = P.hub_begin[k]; h < P.hub_begin[k + 1]; ++h) {
+      first[h] = uint32_t(chunks.size());
+      for (uint32_t lo = 0; lo < degs[h]; lo += HUB_CHUNK) {
+        chunks.push_back(make_uint4(uint32_t(h), lo, std::min<uint32_t>(degs[h], lo + HUB_CHUNK), 0));
+        parts.push_back(part + lo);
+      }
+      part += degs[h];
+    }
+  }
+  P.chunk_begin[K] = chunks.size();
+  first[H] = uint32_t(chunks.size());
+  P.chunks = chunks.size();
+  P.part = part;
+  hb.hub_first.ensure(H + 1);
+  hb.chunk.ensure(chunks.size());
+  hb.chunk_part.ensure(chunks.size());
+  LVG_CUDA(cudaMemcpyAsync(hb.hub_first.p, first.data(), (H + 1) * 4, cudaMemcpyHostToDevice, s));
+  LVG_CUDA(cudaMemcpyAsync(hb.chunk.p, chunks.data(), chunks.size() * sizeof(uint4), cudaMemcpyHostToDevice, s));
+  LVG_CUDA(cudaMemcpyAsync(hb.chunk_part.p, parts.data(), parts.size() * 8, cudaMemcpyHostToDevice, s));
+  LVG_CUDA(cudaStreamSynchronize(s));
+  P.hub_vertex = hb.hub_vertex.p;
+  P.hub_first = hb.hub_first.p;
+  P.chunk = hb.chunk.p;
+  P.chunk_part = hb.chunk_part.p;
 }
 
 int colors_for(const lvg_options &o) {
@@ -256,12 +329,25 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const 
   // Existing degree-0 vertices are processed once and never re-marked.
   for (int k = 0; k < K; ++k)
     launch_clear_isolated(lv.bins + lv.bucket_begin(k, 0), lv.bucket_size(k, 0), W.vaff.p, fa, s);
-  int glog2 = 1;
-  size_t hubs = 0;
-  for (int k = 0; k < K; ++k) hubs = std::max(hubs, lv.bucket_size(k, NUM_BINS - 1));
-  if (hubs) {
-    glog2 = global_table_log2(lv.bin_maxdeg[NUM_BINS - 1]);
-    ensure_global_tables(W, size_t(global_table_blocks(hubs)), glog2, false);
+  // Global fallback regions of the large-degree bins (9-11): each launch's
+  // blocks get 2^glog2[b] slots, enough for the bin's largest degree.
+  int glog2[NUM_BINS] = {};
+  size_t need = 0;
+  for (int b = 9; b < NUM_BINS; ++b) {
+    size_t most = 0;
+    for (int k = 0; k < K; ++k) most = std::max(most, lv.bucket_size(k, b));
+    if (!most) continue;
+    glog2[b] = global_table_log2(lv.bin_maxdeg[b]);
+    need = std::max(need, size_t(global_table_blocks(most)) << glog2[b]);
+  }
+  if (need) {
+    W.gkeys.ensure(need);
+    W.gvals.ensure(need);
+  }
+  if (lv.hub.hubs) {
+    W.chunk_cnt.ensure(lv.hub.chunks);
+    W.part_key.ensure(lv.hub.part);
+    W.part_val.ensure(lv.hub.part);
   }
   int l = 0;
   double el = 0;
@@ -282,9 +368,19 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const 
         a.vcom = com; a.ctot = ctot; a.dec = W.dec.p;
         a.vaff = W.vaff.p; a.mark = W.mark.p; a.fa = fa; a.vtot = tot;
         a.kr = kr; a.ctr = g->ctr.p; a.bin = b;
-        a.gkeys = W.gkeys.p; a.gvals = W.gvals.p; a.glog2 = glog2;
+        a.gkeys = need ? W.gkeys.p : nullptr; a.gvals = need ? W.gvals.p : nullptr; a.glog2 = glog2[b];
         cudaEvent_t b0 = g->profiling ? g->events.record(s) : nullptr;
-        launch_move_bin(b, sync, a, s);
+        if (b == NUM_BINS - 1) {
+          a.hub = lv.hub;
+          a.color = k;
+          a.chunk_cnt = W.chunk_cnt.p;
+          a.part_key = W.part_key.p;
+          a.part_val = W.part_val.p;
+          a.hub_kd = W.hub_kd.p;
+          launch_move_hubs(sync, a, s);
+        } else {
+          launch_move_bin(b, sync, a, s);
+        }
         if (g->profiling) bin_ev.push_back({b, {b0, g->events.record(s)}});
         ++g->stats.move_launches;
       }
@@ -334,11 +430,18 @@ Level aggregate(lvg_graph *g, const Level &lv, const uint32_t *com, size_t CN, i
   // Empty communities never reach a kernel: zero their rows and weights first.
   LVG_CUDA(cudaMemsetAsync(nl.deg, 0, CN * sizeof(uint32_t), s));
   LVG_CUDA(cudaMemsetAsync(W.vtot.p, 0, CN * sizeof(float), s));
-  int glog2 = 1;
-  const size_t big = cb[NUM_BINS] - cb[NUM_BINS - 1];
-  if (big) {
-    glog2 = global_table_log2(std::min<uint64_t>(cmax[NUM_BINS - 1], CN));
-    ensure_global_tables(W, size_t(global_table_blocks(big)), glog2, false);
+  // Global fallback regions of the large bins (9-11), as in move_phase.
+  int glog2[NUM_BINS] = {};
+  size_t need = 0;
+  for (int b = 9; b < NUM_BINS; ++b) {
+    const size_t cnt = cb[b + 1] - cb[b];
+    if (!cnt) continue;
+    glog2[b] = global_table_log2(std::min<uint64_t>(cmax[b], CN));
+    need = std::max(need, size_t(global_table_blocks(cnt)) << glog2[b]);
+  }
+  if (need) {
+    W.gkeys.ensure(need);
+    W.gvals.ensure(need);
   }
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (g->profiling) e0 = g->events.record(s);
@@ -352,7 +455,7 @@ Level aggregate(lvg_graph *g, const Level &lv, const uint32_t *com, size_t CN, i
     a.count = uint32_t(cnt);
     a.yoff = nl.off; a.ydeg = nl.deg; a.ykey = nl.key; a.yw = nl.w;
     a.vtot = W.vtot.p; a.ctr = g->ctr.p; a.cn = uint32_t(CN);
-    a.gkeys = W.gkeys.p; a.gvals = W.gvals.p; a.glog2 = glog2;
+    a.gkeys = need ? W.gkeys.p : nullptr; a.gvals = need ? W.gvals.p : nullptr; a.glog2 = glog2[b];
     launch_aggregate_bin(b, a, s);
     ++g->stats.aggregate_launches;
   }
@@ -360,6 +463,7 @@ Level aggregate(lvg_graph *g, const Level &lv, const uint32_t *com, size_t CN, i
     e1 = g->events.record(s);
   }
   compute_bins(g, nl, nl.deg, nb.bins.p, W.binscratch.p, colors);  // synchronises
+  build_hub_plan(g, nl, nb.hubplan);
   if (g->profiling) g->stats.aggregate_kernel_ms += elapsed(e0, e1);
   return nl;
 }
@@ -386,7 +490,10 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
   const bool sync = o.deterministic != 0;
   const int rep = std::max(1, o.repeat);
   const int K = colors_for(o);
-  if (g->base.colors != K) compute_bins(g, g->base, g->deg.p, g->bins.p, W.binscratch.p, K);
+  if (g->base.colors != K) {
+    compute_bins(g, g->base, g->deg.p, g->bins.p, W.binscratch.p, K);
+    build_hub_plan(g, g->base, g->hubplan);
+  }
   uint32_t *ucom = out.q;
   float *utot = out.vt, *ctot = out.ct;
   g->stats = lvg_stats{};
@@ -582,8 +689,6 @@ void upload_prior(lvg_graph *g, const uint32_t *q, const double *qvtot, const do
   cudaStream_t s = g->stream;
   const size_t S = g->base.span;
   if (!q || !qvtot || !qctot) throw Error(LVG_EINVAL, "prior state: null array");
-  for (size_t u = 0; u < S; ++u)
-    if (q[u] >= S) throw Error(LVG_EINVAL, "prior membership id >= span");
   W.stage_a.ensure(S);
   W.stage_b.ensure(S);
   LVG_CUDA(cudaMemcpyAsync(dq, q, S * 4, cudaMemcpyHostToDevice, s));
@@ -591,6 +696,9 @@ void upload_prior(lvg_graph *g, const uint32_t *q, const double *qvtot, const do
   LVG_CUDA(cudaMemcpyAsync(W.stage_b.p, qctot, S * 8, cudaMemcpyHostToDevice, s));
   launch_prior_to_f32(W.stage_a.p, dvt, S, s);
   launch_prior_to_f32(W.stage_b.p, dct, S, s);
+  // every prior id must be < span (checked on the device; read back before any use)
+  launch_check_ids(dq, S, uint32_t(S), g->ctr.p, s);
+  read_counters(g);
 }
 
 int run_host(lvg_graph *g, int method, const lvg_batch *b, const uint32_t *q, const double *qvtot,
@@ -694,6 +802,7 @@ int lvg_graph_create(size_t span, const uint64_t *offsets, const uint32_t *keys,
     lvg::DBuf<uint32_t> scratch;
     scratch.ensure(lvg::bin_scratch_elems(span + 1, lvg::DEFAULT_COLORS_ASYNC));
     lvg::compute_bins(g.get(), b, g->deg.p, g->bins.p, scratch.p, lvg::DEFAULT_COLORS_ASYNC);  // synchronises
+    lvg::build_hub_plan(g.get(), b, g->hubplan);
     lvg::read_counters(g.get());
     g->total_weight = g->hctr.p->fp64[0];
     return LVG_OK;

@@ -5,6 +5,21 @@
 
 namespace lvg {
 
+// Work plan of the chunked path for the largest vertices (degree bin 11) of a
+// level: each hub's edge list is cut into chunks of HUB_CHUNK edges that
+// different blocks aggregate at once; a second kernel merges a hub's chunks.
+// Hubs are ordered by colour class; chunks by hub.
+constexpr uint32_t HUB_CHUNK = 8192;
+struct HubPlan {
+  size_t hubs = 0, chunks = 0, part = 0;        // counts; part = partial-entry capacity
+  size_t hub_begin[MAX_COLORS + 1] = {};        // hubs of colour k: [hub_begin[k], hub_begin[k+1])
+  size_t chunk_begin[MAX_COLORS + 1] = {};      // chunks of colour k
+  const uint32_t *hub_vertex = nullptr;         // [hubs] vertex id
+  const uint32_t *hub_first = nullptr;          // [hubs+1] first chunk of each hub
+  const uint4 *chunk = nullptr;                 // [chunks] (hub, first edge, end edge, -)
+  const uint64_t *chunk_part = nullptr;         // [chunks] offset of the chunk's partial entries
+};
+
 // A graph level in HBM: gapped CSR (row u = key/w[off[u] .. off[u]+deg[u])),
 // the layout of the reference's DiGraphCsr (inc/Graph.hxx:384-640). Level 0 is
 // the uploaded graph (ex = existence flags); aggregated levels have every
@@ -22,6 +37,7 @@ struct Level {
   int colors = 1;
   size_t bin_start[MAX_BUCKETS + 1] = {};
   uint64_t bin_maxdeg[NUM_BINS] = {};
+  HubPlan hub;  // chunked work for degree bin 11
   size_t bucket_begin(int k, int b) const { return bin_start[k * NUM_BINS + b]; }
   size_t bucket_size(int k, int b) const { return bin_start[k * NUM_BINS + b + 1] - bin_start[k * NUM_BINS + b]; }
   size_t color_begin(int k) const { return bin_start[k * NUM_BINS]; }
@@ -61,9 +77,16 @@ struct MoveArgs {
   float kr;              // R / (2M)
   int bin;               // degree bin of the list (statistics)
   Counters *ctr;
-  uint32_t *gkeys;       // global tables (bin 11): [grid][gcap]
+  uint32_t *gkeys;       // global fallback tables: [grid][2^glog2]
   float *gvals;
   int glog2;             // log2 of the global table capacity
+  // chunked hub path (bin 11)
+  HubPlan hub;
+  uint32_t *chunk_cnt;   // [chunks] partial entries written by each chunk
+  uint32_t *part_key;    // [part] partial (community, weight) entries
+  float *part_val;
+  float *hub_kd;         // [span] weight to the own community, summed over chunks
+  int color;             // colour class of the launch
 };
 
 // Arguments of the aggregation kernels (inc/louvain.hxx:897-912, 987-992).
@@ -139,6 +162,8 @@ void launch_community_scatter(const Level &g, const uint32_t *vcom, const uint32
                               uint32_t *cmem, cudaStream_t s);
 void launch_level_init(size_t n, const float *vtot, uint32_t *vcom, float *ctot, uint8_t *vaff, cudaStream_t s);
 void launch_count_flags(const uint8_t *f, size_t n, Counters *ctr, cudaStream_t s);
+// Set ERR_BAD_ID in ctr->err if any a[i] >= limit.
+void launch_check_ids(const uint32_t *a, size_t n, uint32_t limit, Counters *ctr, cudaStream_t s);
 void launch_modularity(const Level &g, const uint32_t *memb, double *ctot64, Counters *ctr, cudaStream_t s);
 void launch_sq_sum(const double *x, size_t n, Counters *ctr, cudaStream_t s);  // -> ctr->fp64[2]
 
@@ -152,6 +177,12 @@ void launch_aggregate_bin(int b, const AggArgs &a, cudaStream_t s);
 // Record a failure message for lvg_last_error() and return `code` (for entry
 // points outside lvg_api.cu).
 int fail_noalloc(int code, const char *msg);
+
+// Chunked path of the largest vertices: per colour, one kernel aggregates
+// the chunks, a second merges each hub's chunks and moves it.
+void launch_move_hubs(bool sync, const MoveArgs &a, cudaStream_t s);
+// dst[i] = src[idx[i]]
+void launch_gather_u32(const uint32_t *idx, size_t n, const uint32_t *src, uint32_t *dst, cudaStream_t s);
 
 // Global-table capacity (log2) for a maximum degree.
 inline int global_table_log2(uint64_t maxdeg) {

@@ -348,6 +348,16 @@ __global__ void level_init_kernel(size_t n, const float *vtot, uint32_t *vcom, f
   }
 }
 
+__global__ void gather_u32_kernel(const uint32_t *idx, size_t n, const uint32_t *src, uint32_t *dst) {
+  GRID_STRIDE(i, n) dst[i] = src[idx[i]];
+}
+
+__global__ void check_ids_kernel(const uint32_t *a, size_t n, uint32_t limit, unsigned int *err) {
+  bool bad = false;
+  GRID_STRIDE(i, n) bad |= a[i] >= limit;
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(err, ERR_BAD_ID);
+}
+
 __global__ void count_flags_kernel(const uint8_t *f, size_t n, unsigned long long *dst) {
   unsigned long long c = 0;
   GRID_STRIDE(i, n) c += f[i] == 1;
@@ -521,6 +531,18 @@ void launch_community_scatter(const Level &g, const uint32_t *vcom, const uint32
 void launch_level_init(size_t n, const float *vtot, uint32_t *vcom, float *ctot, uint8_t *vaff, cudaStream_t s) {
   if (!n) return;
   level_init_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, vtot, vcom, ctot, vaff);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_gather_u32(const uint32_t *idx, size_t n, const uint32_t *src, uint32_t *dst, cudaStream_t s) {
+  if (!n) return;
+  gather_u32_kernel<<<grid_for(n, 256), 256, 0, s>>>(idx, n, src, dst);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_check_ids(const uint32_t *a, size_t n, uint32_t limit, Counters *ctr, cudaStream_t s) {
+  if (!n) return;
+  check_ids_kernel<<<grid_for(n, 256), 256, 0, s>>>(a, n, limit, &ctr->err);
   LVG_CHECK_LAUNCH();
 }
 

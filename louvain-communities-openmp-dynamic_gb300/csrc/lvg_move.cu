@@ -9,10 +9,10 @@
 //             shared-memory open-addressing table of 2x the tile size;
 //   bins 5-8  (degree <= 64..512):   one warp per vertex, shared table of
 //             128..1024 slots;
-//   bins 9-10 (degree <= 2048/8192): one block per vertex, shared table of
-//             4096 / 16384 slots;
-//   bin 11    (larger hubs):         one block per vertex, table in global
-//             memory (a per-block region of HBM, L2 resident when it fits).
+//   bins 9-11 (degree > 512):        one block per vertex, shared table of
+//             4096 / 8192 slots with a claim budget; a vertex with more
+//             distinct neighbour communities than the budget is redone with
+//             a table in its block's region of global memory.
 // Per vertex: clear the table, insert (community of each neighbour, weight)
 // for neighbours outside the vertex's own community (the own community's
 // weight is a lane-private sum), compute the FP32 gain of each candidate,
@@ -112,13 +112,27 @@ __global__ void __launch_bounds__(TILE_BLOCK) move_tile_kernel(MoveArgs a) {
     __syncwarp(m);
     float kd = 0.f;
     bool ok = true;
-    for (uint32_t j = tl; j < dg; j += T) {
-      const uint32_t v = a.key[o + j];
-      if (v == u) continue;
-      const float ww = a.w[o + j];
-      const uint32_t c = a.vcom[v];
-      if (c == d) kd += ww;
-      else ok &= table_add(keys, vals, LOGC, c, ww);
+    // U independent edge loads per lane in flight (degree <= C/2, so a lane
+    // has at most C/(2T) edges).
+    constexpr int U = (C / (2 * T)) < 1 ? 1 : ((C / (2 * T)) > 4 ? 4 : (C / (2 * T)));
+    for (uint32_t j0 = tl; j0 < dg; j0 += U * T) {
+      uint32_t v[U];
+      float w[U];
+#pragma unroll
+      for (int k = 0; k < U; ++k) {
+        const uint32_t j = j0 + k * T;
+        v[k] = j < dg ? a.key[o + j] : u;
+        w[k] = j < dg ? a.w[o + j] : 0.f;
+      }
+      uint32_t c[U];
+#pragma unroll
+      for (int k = 0; k < U; ++k) c[k] = v[k] != u ? a.vcom[v[k]] : EMPTY;
+#pragma unroll
+      for (int k = 0; k < U; ++k) {
+        if (c[k] == EMPTY) continue;
+        if (c[k] == d) kd += w[k];
+        else ok &= table_add(keys, vals, LOGC, c[k], w[k]);
+      }
     }
 #pragma unroll
     for (int sh = T / 2; sh > 0; sh >>= 1) kd += __shfl_xor_sync(m, kd, sh, T);
@@ -206,52 +220,124 @@ __device__ __forceinline__ void block_argmax(float &bg, uint32_t &bc, float *rg,
   __syncthreads();
 }
 
-// One block per vertex. GLOBAL = table in global memory (bin 11), else in
-// dynamic shared memory; the block's region holds 2^log2cap slots and each
-// vertex uses the smallest power of two >= 2x its degree.
-template <int B, bool GLOBAL, bool SYNC>
-__global__ void __launch_bounds__(B) move_block_kernel(MoveArgs a, int log2cap) {
+// Insert into a shared table with a claim budget: a new key may take a slot
+// only while fewer than `limit` slots were claimed (load <= 50 %). Returns
+// false when the budget is exhausted; the caller then redoes the vertex with
+// a table in global memory, so no key is ever split between two tables.
+__device__ __forceinline__ bool smem_add_budget(uint32_t *keys, float *vals, int log2cap, uint32_t c, float w,
+                                                unsigned *used, unsigned limit) {
+  const uint32_t mask = (1u << log2cap) - 1u;
+  uint32_t s = hash_hi(c, log2cap);
+  for (uint32_t probe = 0; probe <= mask; ++probe) {
+    uint32_t k = keys[s];
+    if (k == c) { atomicAdd(&vals[s], w); return true; }
+    if (k == EMPTY) {
+      if (atomicAdd(used, 1u) >= limit) return false;
+      uint32_t prev = atomicCAS(&keys[s], EMPTY, c);
+      if (prev == EMPTY || prev == c) { atomicAdd(&vals[s], w); return true; }
+    }
+    s = (s + 1u) & mask;
+  }
+  return false;
+}
+
+// Scan the edges of u (4 independent loads in flight per thread) into a
+// table; `add` inserts one (community, weight). Returns the lane-private
+// weight to the own community d.
+template <int B, class Add>
+__device__ __forceinline__ float scan_edges(const MoveArgs &a, uint32_t u, uint64_t o, uint32_t dg, uint32_t d,
+                                            Add add) {
+  constexpr int U = 4;
+  float kd = 0.f;
+  for (uint32_t j0 = threadIdx.x; j0 < dg; j0 += U * B) {
+    uint32_t v[U];
+    float w[U];
+#pragma unroll
+    for (int k = 0; k < U; ++k) {
+      const uint32_t j = j0 + k * B;
+      v[k] = j < dg ? a.key[o + j] : u;
+      w[k] = j < dg ? a.w[o + j] : 0.f;
+    }
+    uint32_t c[U];
+#pragma unroll
+    for (int k = 0; k < U; ++k) c[k] = v[k] != u ? a.vcom[v[k]] : EMPTY;
+#pragma unroll
+    for (int k = 0; k < U; ++k) {
+      if (c[k] == EMPTY) continue;
+      if (c[k] == d) kd += w[k];
+      else if (!add(c[k], w[k])) return kd;
+    }
+  }
+  return kd;
+}
+
+// One block per vertex (degree > 512). The vertex is first aggregated in a
+// shared table of 2^LOGS slots; if it has more distinct neighbour
+// communities than the table's budget (half its slots), it is redone with a
+// table in this block's region of global memory (2^a.glog2 slots). After the
+// first local-moving iterations a high-degree vertex's neighbours fall into
+// few communities, so the shared table almost always suffices.
+template <int B, int LOGS, bool SYNC>
+__global__ void __launch_bounds__(B) move_big_kernel(MoveArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
   __shared__ float red_g[B / 32];
   __shared__ uint32_t red_c[B / 32];
   __shared__ int s_act;
-  const uint32_t cap = 1u << log2cap;
-  uint32_t *keys;
-  float *vals;
-  if (GLOBAL) {
-    keys = a.gkeys + size_t(blockIdx.x) * cap;
-    vals = a.gvals + size_t(blockIdx.x) * cap;
-  } else {
-    keys = reinterpret_cast<uint32_t *>(smem);
-    vals = reinterpret_cast<float *>(smem + size_t(cap) * sizeof(uint32_t));
-  }
+  __shared__ unsigned s_used;
+  __shared__ int s_over;
+  constexpr uint32_t CS = 1u << LOGS;
+  uint32_t *skeys = reinterpret_cast<uint32_t *>(smem);
+  float *svals = reinterpret_cast<float *>(smem + size_t(CS) * sizeof(uint32_t));
+  uint32_t *gkeys = a.gkeys ? a.gkeys + (size_t(blockIdx.x) << a.glog2) : nullptr;
+  float *gvals = a.gvals ? a.gvals + (size_t(blockIdx.x) << a.glog2) : nullptr;
   unsigned long long fix = 0, nv = 0, ne = 0, nm = 0;
   bool bad = false;
   for (uint32_t i = blockIdx.x; i < a.count; i += gridDim.x) {
     const uint32_t u = a.list[i];
-    if (threadIdx.x == 0) s_act = a.vaff[u] && (!a.fa || a.fa[u]);
+    if (threadIdx.x == 0) {
+      s_act = a.vaff[u] && (!a.fa || a.fa[u]);
+      s_used = 0;
+      s_over = 0;
+    }
     __syncthreads();
     const int act = s_act;
-    __syncthreads();
-    if (!act) continue;
+    if (!act) {
+      __syncthreads();
+      continue;
+    }
     const uint64_t o = a.off[u];
     const uint32_t dg = a.deg[u];
     const uint32_t d = a.vcom[u];
-    const int lg = min(log2cap, max(1, ceil_log2(2ull * dg)));
-    const uint32_t vcap = 1u << lg;
-    for (uint32_t s = threadIdx.x; s < vcap; s += B) { keys[s] = EMPTY; vals[s] = 0.f; }
+    // attempt 1: shared table sized for the degree (at most 2^LOGS slots)
+    int lg = min(LOGS, max(1, ceil_log2(2ull * dg)));
+    uint32_t vcap = 1u << lg;
+    for (uint32_t s = threadIdx.x; s < vcap; s += B) { skeys[s] = EMPTY; svals[s] = 0.f; }
     __syncthreads();
-    float kd = 0.f;
+    const unsigned limit = vcap >> 1;
+    float kd = scan_edges<B>(a, u, o, dg, d, [&](uint32_t c, float w) {
+      if (smem_add_budget(skeys, svals, lg, c, w, &s_used, limit)) return true;
+      s_over = 1;
+      return false;
+    });
+    __syncthreads();
+    uint32_t *keys = skeys;
+    float *vals = svals;
     bool ok = true;
-    for (uint32_t j = threadIdx.x; j < dg; j += B) {
-      const uint32_t v = a.key[o + j];
-      if (v == u) continue;
-      const float ww = a.w[o + j];
-      const uint32_t c = a.vcom[v];
-      if (c == d) kd += ww;
-      else ok &= table_add(keys, vals, lg, c, ww);
+    if (s_over) {
+      // attempt 2: global table sized for the degree
+      lg = min(a.glog2, max(1, ceil_log2(2ull * dg)));
+      vcap = 1u << lg;
+      keys = gkeys;
+      vals = gvals;
+      if (!keys) { ok = false; vcap = 0; }
+      for (uint32_t s = threadIdx.x; s < vcap; s += B) { keys[s] = EMPTY; vals[s] = 0.f; }
+      __syncthreads();
+      if (keys) kd = scan_edges<B>(a, u, o, dg, d, [&](uint32_t c, float w) {
+        ok &= table_add(keys, vals, lg, c, w);
+        return true;
+      });
     }
-    kd = block_sum<B>(kd, red_g);  // includes a barrier: table complete
+    kd = block_sum<B>(kd, red_g);  // barrier: table complete
     const float wu = a.vtot[u];
     const float td = a.ctot[d];
     float bg = 0.f;
@@ -278,6 +364,230 @@ __global__ void __launch_bounds__(B) move_block_kernel(MoveArgs a, int log2cap) 
     }
     if (moved) {
       uint8_t *mk = SYNC ? a.mark : a.vaff;
+      for (uint32_t j = threadIdx.x; j < dg; j += B) {
+        const uint32_t v = a.key[o + j];
+        if (v != u) mk[v] = 1;
+      }
+    }
+    if (threadIdx.x == 0) {
+      a.vaff[u] = 0;
+      ++nv;
+      ne += dg;
+      nm += moved;
+    }
+    bad |= !ok;
+    __syncthreads();
+  }
+  flush_counters(a.ctr, a.bin, fix, nv, ne, nm, bad);
+}
+
+// ------------------------------------------------------------ chunked hubs
+
+// Hub path, step 1: one block per chunk of HUB_CHUNK edges of one hub of the
+// colour class. The chunk is merged in a shared table with a claim budget
+// and its distinct (community, weight) pairs are written to the chunk's
+// partial region; a chunk with more distinct communities than the budget
+// writes its raw pairs instead. Edges into the hub's own community are summed
+// separately into hub_kd[u].
+template <int B, int LOGS>
+__global__ void __launch_bounds__(B) hub_chunk_kernel(MoveArgs a) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  __shared__ float red_g[B / 32];
+  __shared__ int s_act;
+  __shared__ unsigned s_used, s_cnt;
+  __shared__ int s_over;
+  uint32_t *skeys = reinterpret_cast<uint32_t *>(smem);
+  float *svals = reinterpret_cast<float *>(smem + (size_t(1) << LOGS) * sizeof(uint32_t));
+  const size_t ci = a.hub.chunk_begin[a.color] + blockIdx.x;
+  const uint4 ch = a.hub.chunk[ci];
+  const uint32_t u = a.hub.hub_vertex[ch.x];
+  if (threadIdx.x == 0) {
+    s_act = a.vaff[u] && (!a.fa || a.fa[u]);
+    s_used = 0;
+    s_over = 0;
+    s_cnt = 0;
+  }
+  __syncthreads();
+  if (!s_act) {
+    if (threadIdx.x == 0) a.chunk_cnt[ci] = EMPTY;  // tells step 2 the hub was inactive
+    return;
+  }
+  const uint64_t o = a.off[u] + ch.y;
+  const uint32_t n = ch.z - ch.y;
+  const uint32_t d = a.vcom[u];
+  const int lg = min(LOGS, max(1, ceil_log2(2ull * n)));
+  const uint32_t vcap = 1u << lg;
+  for (uint32_t s = threadIdx.x; s < vcap; s += B) { skeys[s] = EMPTY; svals[s] = 0.f; }
+  __syncthreads();
+  const unsigned limit = vcap >> 1;
+  float kd = 0.f;
+  constexpr int U = 4;
+  for (uint32_t j0 = threadIdx.x; j0 < n; j0 += U * B) {
+    uint32_t v[U];
+    float w[U];
+#pragma unroll
+    for (int k = 0; k < U; ++k) {
+      const uint32_t j = j0 + k * B;
+      v[k] = j < n ? a.key[o + j] : u;
+      w[k] = j < n ? a.w[o + j] : 0.f;
+    }
+    uint32_t c[U];
+#pragma unroll
+    for (int k = 0; k < U; ++k) c[k] = v[k] != u ? a.vcom[v[k]] : EMPTY;
+    bool stop = false;
+#pragma unroll
+    for (int k = 0; k < U; ++k) {
+      if (c[k] == EMPTY || stop) continue;
+      if (c[k] == d) kd += w[k];
+      else if (!smem_add_budget(skeys, svals, lg, c[k], w[k], &s_used, limit)) { s_over = 1; stop = true; }
+    }
+    if (stop) break;
+  }
+  __syncthreads();
+  uint32_t *pk = a.part_key + a.hub.chunk_part[ci];
+  float *pv = a.part_val + a.hub.chunk_part[ci];
+  const int lane = threadIdx.x & 31;
+  if (!s_over) {
+    for (uint32_t s0 = 0; s0 < vcap; s0 += B) {
+      const uint32_t s = s0 + threadIdx.x;
+      const uint32_t k = s < vcap ? skeys[s] : EMPTY;
+      const bool has = k != EMPTY;
+      const unsigned bal = __ballot_sync(0xffffffffu, has);
+      uint32_t base = 0;
+      if (lane == 0 && bal) base = atomicAdd(&s_cnt, uint32_t(__popc(bal)));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (has) {
+        const uint32_t r = __popc(bal & ((1u << lane) - 1u));
+        pk[base + r] = k;
+        pv[base + r] = svals[s];
+      }
+    }
+  } else {
+    // too many distinct communities in this chunk: hand its raw pairs on
+    kd = 0.f;
+    for (uint32_t j = threadIdx.x; j < n; j += B) {
+      const uint32_t v = a.key[o + j];
+      const uint32_t c = v != u ? a.vcom[v] : EMPTY;
+      const float w = a.w[o + j];
+      const bool keep = c != EMPTY && c != d;
+      if (c == d) kd += w;
+      if (keep) {
+        const uint32_t pos = atomicAdd(&s_cnt, 1u);
+        pk[pos] = c;
+        pv[pos] = w;
+      }
+    }
+  }
+  kd = block_sum<B>(kd, red_g);
+  if (threadIdx.x == 0) {
+    if (kd != 0.f) atomicAdd(&a.hub_kd[u], kd);
+    a.chunk_cnt[ci] = s_cnt;
+  }
+}
+
+// Hub path, step 2: one block per hub of the colour class (grid-stride).
+// Merges the partial entries of the hub's chunks (shared table with a claim
+// budget; global fallback region otherwise), then chooses and applies the
+// move like the other local-moving kernels.
+template <int B, int LOGS, bool SYNC>
+__global__ void __launch_bounds__(B) hub_merge_kernel(MoveArgs a) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  __shared__ float red_g[B / 32];
+  __shared__ uint32_t red_c[B / 32];
+  __shared__ int s_act;
+  __shared__ unsigned s_used;
+  __shared__ int s_over;
+  __shared__ float s_kd;
+  constexpr uint32_t CS = 1u << LOGS;
+  uint32_t *skeys = reinterpret_cast<uint32_t *>(smem);
+  float *svals = reinterpret_cast<float *>(smem + size_t(CS) * sizeof(uint32_t));
+  uint32_t *gkeys = a.gkeys ? a.gkeys + (size_t(blockIdx.x) << a.glog2) : nullptr;
+  float *gvals = a.gvals ? a.gvals + (size_t(blockIdx.x) << a.glog2) : nullptr;
+  const size_t h0 = a.hub.hub_begin[a.color], h1 = a.hub.hub_begin[a.color + 1];
+  unsigned long long fix = 0, nv = 0, ne = 0, nm = 0;
+  bool bad = false;
+  for (size_t g = h0 + blockIdx.x; g < h1; g += gridDim.x) {
+    const uint32_t u = a.hub.hub_vertex[g];
+    const uint32_t c0 = a.hub.hub_first[g], c1 = a.hub.hub_first[g + 1];
+    if (threadIdx.x == 0) {
+      // active iff step 1 aggregated it (a hub marked since then waits for
+      // the next iteration, its partials being stale)
+      s_act = a.chunk_cnt[c0] != EMPTY;
+      s_used = 0;
+      s_over = 0;
+      s_kd = a.hub_kd[u];
+    }
+    __syncthreads();
+    if (!s_act) {
+      __syncthreads();
+      continue;
+    }
+    const uint32_t dg = a.deg[u];
+    const uint32_t d = a.vcom[u];
+    // entries to merge: at most the hub's degree
+    int lg = min(LOGS, max(1, ceil_log2(2ull * dg)));
+    uint32_t vcap = 1u << lg;
+    for (uint32_t s = threadIdx.x; s < vcap; s += B) { skeys[s] = EMPTY; svals[s] = 0.f; }
+    __syncthreads();
+    const unsigned limit = vcap >> 1;
+    for (uint32_t c = c0; c < c1 && !s_over; ++c) {
+      const uint64_t p = a.hub.chunk_part[c];
+      const uint32_t cnt = a.chunk_cnt[c];
+      for (uint32_t t = threadIdx.x; t < cnt; t += B)
+        if (!smem_add_budget(skeys, svals, lg, a.part_key[p + t], a.part_val[p + t], &s_used, limit)) {
+          s_over = 1;
+          break;
+        }
+    }
+    __syncthreads();
+    uint32_t *keys = skeys;
+    float *vals = svals;
+    bool ok = true;
+    if (s_over) {
+      lg = min(a.glog2, max(1, ceil_log2(2ull * dg)));
+      vcap = 1u << lg;
+      keys = gkeys;
+      vals = gvals;
+      if (!keys) { ok = false; vcap = 0; }
+      for (uint32_t s = threadIdx.x; s < vcap; s += B) { keys[s] = EMPTY; vals[s] = 0.f; }
+      __syncthreads();
+      if (keys)
+        for (uint32_t c = c0; c < c1; ++c) {
+          const uint64_t p = a.hub.chunk_part[c];
+          const uint32_t cnt = a.chunk_cnt[c];
+          for (uint32_t t = threadIdx.x; t < cnt; t += B) ok &= table_add(keys, vals, lg, a.part_key[p + t], a.part_val[p + t]);
+        }
+    }
+    __syncthreads();
+    const float kd = s_kd;
+    const float wu = a.vtot[u];
+    const float td = a.ctot[d];
+    float bg = 0.f;
+    uint32_t bc = EMPTY;
+    for (uint32_t s = threadIdx.x; s < vcap; s += B) {
+      const uint32_t c = keys[s];
+      if (c == EMPTY) continue;
+      const float g2 = gain_f32(vals[s], kd, wu, a.ctot[c], td, a.kr);
+      if (g2 > 0.f) take_better(bg, bc, g2, c);
+    }
+    block_argmax<B>(bg, bc, red_g, red_c);
+    const bool moved = bc != EMPTY && bc != 0;
+    if (threadIdx.x == 0) {
+      a.hub_kd[u] = 0.f;
+      if (bc != EMPTY) fix += gain_to_fix(bg);
+      if (moved) {
+        if (SYNC) {
+          a.dec[u] = bc;
+        } else {
+          atomicAdd(&a.ctot[d], -wu);
+          atomicAdd(&a.ctot[bc], wu);
+          a.vcom[u] = bc;
+        }
+      }
+    }
+    if (moved) {
+      uint8_t *mk = SYNC ? a.mark : a.vaff;
+      const uint64_t o = a.off[u];
       for (uint32_t j = threadIdx.x; j < dg; j += B) {
         const uint32_t v = a.key[o + j];
         if (v != u) mk[v] = 1;
@@ -325,16 +635,32 @@ void launch_tile(const MoveArgs &a, cudaStream_t s) {
   LVG_CHECK_LAUNCH();
 }
 
-template <int B, int LOGC, bool SYNC>
-void launch_block_smem(const MoveArgs &a, cudaStream_t s) {
-  const size_t smem = (size_t(1) << LOGC) * 8;
-  auto k = move_block_kernel<B, false, SYNC>;
+template <int B, int LOGS, bool SYNC>
+void launch_big(const MoveArgs &a, cudaStream_t s) {
+  const size_t smem = (size_t(1) << LOGS) * 8;
+  auto k = move_big_kernel<B, LOGS, SYNC>;
   static bool configured = false;
   if (!configured) { set_smem(k, smem); configured = true; }
-  size_t cap = size_t(num_sms()) * (smem > 64 * 1024 ? 1 : 2);
-  unsigned grid = unsigned(a.count < cap ? a.count : cap);
+  unsigned grid = unsigned(global_table_blocks(a.count));
   if (!grid) return;
-  k<<<grid, B, smem, s>>>(a, LOGC);
+  k<<<grid, B, smem, s>>>(a);
+  LVG_CHECK_LAUNCH();
+}
+
+template <bool SYNC>
+void launch_hubs(const MoveArgs &a, cudaStream_t s) {
+  constexpr int B = 512, LOGS = 13;
+  const size_t smem = (size_t(1) << LOGS) * 8;
+  const size_t nch = a.hub.chunk_begin[a.color + 1] - a.hub.chunk_begin[a.color];
+  const size_t nh = a.hub.hub_begin[a.color + 1] - a.hub.hub_begin[a.color];
+  if (!nh) return;
+  auto k1 = hub_chunk_kernel<B, LOGS>;
+  auto k2 = hub_merge_kernel<B, LOGS, SYNC>;
+  static bool configured = false;
+  if (!configured) { set_smem(k1, smem); set_smem(k2, smem); configured = true; }
+  k1<<<unsigned(nch), B, smem, s>>>(a);
+  LVG_CHECK_LAUNCH();
+  k2<<<unsigned(global_table_blocks(nh)), B, smem, s>>>(a);
   LVG_CHECK_LAUNCH();
 }
 
@@ -349,15 +675,9 @@ void launch_bin(int b, const MoveArgs &a, cudaStream_t s) {
     case 6: launch_tile<32, 256, SYNC>(a, s); break;
     case 7: launch_tile<32, 512, SYNC>(a, s); break;
     case 8: launch_tile<32, 1024, SYNC>(a, s); break;
-    case 9: launch_block_smem<256, 12, SYNC>(a, s); break;
-    case 10: launch_block_smem<512, 14, SYNC>(a, s); break;
-    case 11: {
-      unsigned grid = unsigned(global_table_blocks(a.count));
-      if (!grid) return;
-      move_block_kernel<512, true, SYNC><<<grid, 512, 0, s>>>(a, a.glog2);
-      LVG_CHECK_LAUNCH();
-      break;
-    }
+    case 9: launch_big<256, 12, SYNC>(a, s); break;
+    case 10: launch_big<512, 13, SYNC>(a, s); break;
+    case 11: launch_big<512, 13, SYNC>(a, s); break;
     default: break;
   }
 }
@@ -365,8 +685,13 @@ void launch_bin(int b, const MoveArgs &a, cudaStream_t s) {
 }  // namespace
 
 int global_table_blocks(size_t count) {
-  size_t cap = size_t(num_sms()) * 2;
+  size_t cap = size_t(num_sms()) * 3;
   return int(count < cap ? count : cap);
+}
+
+void launch_move_hubs(bool sync, const MoveArgs &a, cudaStream_t s) {
+  if (sync) launch_hubs<true>(a, s);
+  else launch_hubs<false>(a, s);
 }
 
 void launch_move_bin(int b, bool sync, const MoveArgs &a, cudaStream_t s) {
