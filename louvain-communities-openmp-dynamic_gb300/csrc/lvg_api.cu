@@ -78,7 +78,7 @@ struct LevelBuffers {
 struct Workspace {
   size_t S = 0, X = 0;
   DBuf<uint8_t> vaff, mark, fv, fn, fc;
-  DBuf<uint32_t> ucom, vcom, com_next, dec, cext, csize, ccur, cmem, cbins;
+  DBuf<uint32_t> ucom, vcom, com_next, dec, cext, csize, ccur, cmem, cbins, wl, wl_count;
   DBuf<float> utot, vtot, ctot;
   DBuf<uint64_t> scan64;
   DBuf<uint32_t> scan32, binscratch;
@@ -97,7 +97,8 @@ struct Workspace {
     S = S_;
     X = X_;
     vaff.ensure(S); mark.ensure(S); fv.ensure(S); fn.ensure(S); fc.ensure(S);
-    ucom.ensure(S); vcom.ensure(S); com_next.ensure(S); dec.ensure(S);
+    ucom.ensure(S); vcom.ensure(S); com_next.ensure(S); dec.ensure(S); wl.ensure(S + 1);
+    wl_count.ensure(size_t(MAX_COLORS) * NUM_BINS);
     cext.ensure(S + 1); csize.ensure(S + 1); ccur.ensure(S + 1); cmem.ensure(S + 1); cbins.ensure(S + 1);
     utot.ensure(S); vtot.ensure(S); ctot.ensure(S);
     scan64.ensure(scan_scratch_elems(S + 1));
@@ -150,6 +151,19 @@ struct DBatch {
   size_t max_group = 0;  // longest run of insertions sharing a source
 };
 
+// Everything an iteration's launches depend on; a captured iteration is
+// replayed only while all of it is unchanged.
+struct IterKey {
+  const void *p[22];
+  size_t n[4];
+  int k[4];
+  float kr;
+  bool operator==(const IterKey &o) const {
+    return !std::memcmp(p, o.p, sizeof(p)) && !std::memcmp(n, o.n, sizeof(n)) && !std::memcmp(k, o.k, sizeof(k)) &&
+           kr == o.kr;
+  }
+};
+
 struct RunInfo {
   int iterations = 0, passes = 0;
   float t = 0, tm = 0, ti = 0, tp = 0, tl = 0, ta = 0;
@@ -175,6 +189,14 @@ struct lvg_graph {
   HBuf<Counters> hctr;
   HBuf<uint32_t> hbins;
   EventPool events;
+  // captured local-moving iteration of the uploaded level
+  cudaGraphExec_t iter_exec = nullptr;
+  IterKey iter_key{};
+  unsigned long long iter_nodes = 0, iter_moves = 0;
+  bool no_graphs = false;
+  ~lvg_graph() {
+    if (iter_exec) cudaGraphExecDestroy(iter_exec);
+  }
   bool profiling = false;
   lvg_stats stats = {};
   // batch buffers of the host-array entry points
@@ -315,16 +337,109 @@ void ensure_global_tables(Workspace &W, size_t blocks, int log2cap, bool first_t
 
 // ---------------------------------------------------------------- local moving
 
+// Launch one local-moving iteration: every colour class in order; within a
+// class the worklist compaction, then one kernel per degree bin (two for the
+// chunked hubs); in deterministic mode the class's decisions are applied and
+// its marks merged before the next class. The device gain sum is reset first.
+// With bin_ev, events bracket each bin launch (profiling).
+void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const float *tot,
+                       const uint8_t *fa, float kr, bool sync, const int *glog2, size_t need,
+                       std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> *bin_ev) {
+  Workspace &W = *g->ws;
+  cudaStream_t s = g->stream;
+  const int K = lv.colors;
+  LVG_CUDA(cudaMemsetAsync(&g->ctr.p->el_fix, 0, sizeof(unsigned long long), s));
+  LVG_CUDA(cudaMemsetAsync(W.wl_count.p, 0, size_t(K) * NUM_BINS * sizeof(uint32_t), s));
+  for (int k = 0; k < K; ++k) {
+    // this class's active vertices of bins 1..NUM_BINS-2 -> worklists
+    BinBounds bb;
+    for (int b = 0; b <= NUM_BINS; ++b) bb.start[b] = lv.bin_start[k * NUM_BINS + b];
+    uint32_t *wlc = W.wl_count.p + size_t(k) * NUM_BINS;
+    if (bb.start[NUM_BINS - 1] > bb.start[1]) launch_compact_active(lv.bins, bb, W.vaff.p, fa, W.wl.p, wlc, s);
+    for (int b = 1; b < NUM_BINS; ++b) {
+      const size_t cnt = lv.bucket_size(k, b);
+      if (!cnt) continue;
+      MoveArgs a;
+      a.off = lv.off; a.deg = lv.deg; a.key = lv.key; a.w = lv.w;
+      a.list = (b == NUM_BINS - 1 ? lv.bins : W.wl.p) + lv.bucket_begin(k, b);
+      a.count = uint32_t(cnt);
+      a.count_ptr = b == NUM_BINS - 1 ? nullptr : wlc + b;
+      a.vcom = com; a.ctot = ctot; a.dec = W.dec.p;
+      a.vaff = W.vaff.p; a.mark = W.mark.p; a.fa = fa; a.vtot = tot;
+      a.kr = kr; a.ctr = g->ctr.p; a.bin = b;
+      a.gkeys = need ? W.gkeys.p : nullptr; a.gvals = need ? W.gvals.p : nullptr; a.glog2 = glog2[b];
+      cudaEvent_t b0 = bin_ev ? g->events.record(s) : nullptr;
+      if (b == NUM_BINS - 1) {
+        a.hub = lv.hub;
+        a.color = k;
+        a.chunk_cnt = W.chunk_cnt.p;
+        a.part_key = W.part_key.p;
+        a.part_val = W.part_val.p;
+        a.hub_kd = W.hub_kd.p;
+        launch_move_hubs(sync, a, s);
+      } else {
+        launch_move_bin(b, sync, a, s);
+      }
+      if (bin_ev) bin_ev->push_back({b, {b0, g->events.record(s)}});
+      ++g->stats.move_launches;
+    }
+    if (sync) {
+      launch_apply_moves(lv.bins + lv.color_begin(k), lv.color_end(k) - lv.color_begin(k), W.dec.p, com, ctot, tot, s);
+      launch_merge_marks(W.vaff.p, W.mark.p, lv.span, s);
+    }
+  }
+  LVG_CUDA(cudaMemcpyAsync(g->hctr.p, g->ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+}
+
+// Capture one iteration of the uploaded level into a CUDA graph (after an
+// eager iteration, so every kernel's attributes are already set). A capture
+// failure disables graphs for this handle; the eager path stays correct.
+void capture_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const float *tot,
+                       const uint8_t *fa, float kr, bool sync, const int *glog2, size_t need, const IterKey &key) {
+  cudaStream_t s = g->stream;
+  if (g->iter_exec) {
+    cudaGraphExecDestroy(g->iter_exec);
+    g->iter_exec = nullptr;
+  }
+  const unsigned long long l0 = launch_counter();
+  const unsigned long long m0 = g->stats.move_launches;
+  cudaGraph_t graph = nullptr;
+  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    g->no_graphs = true;
+    return;
+  }
+  bool fine = true;
+  try {
+    enqueue_iteration(g, lv, com, ctot, tot, fa, kr, sync, glog2, need, nullptr);
+  } catch (const Error &) {
+    fine = false;
+  }
+  const cudaError_t e = cudaStreamEndCapture(s, &graph);
+  g->iter_nodes = launch_counter() - l0;
+  g->iter_moves = g->stats.move_launches - m0;
+  launch_counter() = l0;
+  g->stats.move_launches = m0;
+  if (!fine || e != cudaSuccess || !graph || cudaGraphInstantiate(&g->iter_exec, graph, 0) != cudaSuccess) {
+    cudaGetLastError();
+    if (graph) cudaGraphDestroy(graph);
+    g->iter_exec = nullptr;
+    g->no_graphs = true;
+    return;
+  }
+  cudaGraphDestroy(graph);
+  g->iter_key = key;
+}
+
 // louvainMoveOmpW (inc/louvain.hxx:588-609). Returns the iteration count, 0
 // if the first iteration found nothing to gain. Each iteration sweeps the
-// colour classes in order; within a class the degree bins run one kernel
-// each. In deterministic mode a class first decides (reading the state left
-// by the previous classes), then its decisions and neighbour marks are applied.
+// colour classes in order (enqueue_iteration). For the uploaded level the
+// iteration is captured once into a CUDA graph and replayed, one graph
+// launch per iteration instead of ~12 launches per colour class.
 int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const float *tot, const uint8_t *fa,
                double M, float kr, int L, double E, bool sync) {
   Workspace &W = *g->ws;
   cudaStream_t s = g->stream;
-  const size_t n = lv.span;
   const int K = lv.colors;
   // Existing degree-0 vertices are processed once and never re-marked.
   for (int k = 0; k < K; ++k)
@@ -349,53 +464,41 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const 
     W.part_key.ensure(lv.hub.part);
     W.part_val.ensure(lv.hub.part);
   }
+  const bool base = lv.off == g->base.off;
+  IterKey key{};
+  if (base) {
+    const void *ps[22] = {lv.off, lv.bins, com, ctot, tot, fa, W.vaff.p, W.mark.p, W.dec.p, W.wl.p, W.wl_count.p,
+                          W.gkeys.p, W.gvals.p, W.chunk_cnt.p, W.part_key.p, W.part_val.p, W.hub_kd.p, g->ctr.p,
+                          g->hctr.p, lv.hub.chunk, lv.hub.hub_vertex, nullptr};
+    std::memcpy(key.p, ps, sizeof(ps));
+    key.n[0] = lv.span; key.n[1] = need; key.n[2] = lv.hub.chunks; key.n[3] = lv.bin_start[K * NUM_BINS];
+    key.k[0] = K; key.k[1] = sync; key.k[2] = glog2[9] | glog2[10] << 8 | glog2[11] << 16;
+    key.kr = kr;
+  }
+  const bool graphs = base && !g->profiling && !g->no_graphs;
   int l = 0;
   double el = 0;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> bin_ev;
   while (l < L) {
-    LVG_CUDA(cudaMemsetAsync(&g->ctr.p->el_fix, 0, sizeof(unsigned long long), s));
-    bin_ev.clear();
     cudaEvent_t e0 = nullptr, e1 = nullptr;
-    if (g->profiling) e0 = g->events.record(s);
-    for (int k = 0; k < K; ++k) {
-      for (int b = 1; b < NUM_BINS; ++b) {
-        const size_t cnt = lv.bucket_size(k, b);
-        if (!cnt) continue;
-        MoveArgs a;
-        a.off = lv.off; a.deg = lv.deg; a.key = lv.key; a.w = lv.w;
-        a.list = lv.bins + lv.bucket_begin(k, b);
-        a.count = uint32_t(cnt);
-        a.vcom = com; a.ctot = ctot; a.dec = W.dec.p;
-        a.vaff = W.vaff.p; a.mark = W.mark.p; a.fa = fa; a.vtot = tot;
-        a.kr = kr; a.ctr = g->ctr.p; a.bin = b;
-        a.gkeys = need ? W.gkeys.p : nullptr; a.gvals = need ? W.gvals.p : nullptr; a.glog2 = glog2[b];
-        cudaEvent_t b0 = g->profiling ? g->events.record(s) : nullptr;
-        if (b == NUM_BINS - 1) {
-          a.hub = lv.hub;
-          a.color = k;
-          a.chunk_cnt = W.chunk_cnt.p;
-          a.part_key = W.part_key.p;
-          a.part_val = W.part_val.p;
-          a.hub_kd = W.hub_kd.p;
-          launch_move_hubs(sync, a, s);
-        } else {
-          launch_move_bin(b, sync, a, s);
-        }
-        if (g->profiling) bin_ev.push_back({b, {b0, g->events.record(s)}});
-        ++g->stats.move_launches;
-      }
-      if (sync) {
-        launch_apply_moves(lv.bins + lv.color_begin(k), lv.color_end(k) - lv.color_begin(k), W.dec.p, com, ctot, tot,
-                           s);
-        launch_merge_marks(W.vaff.p, W.mark.p, n, s);
-      }
+    const bool replay = graphs && g->iter_exec && g->iter_key == key;
+    if (replay) {
+      LVG_CUDA(cudaGraphLaunch(g->iter_exec, s));
+      launch_counter() += g->iter_nodes;
+      g->stats.move_launches += g->iter_moves;
+    } else {
+      bin_ev.clear();
+      if (g->profiling) e0 = g->events.record(s);
+      enqueue_iteration(g, lv, com, ctot, tot, fa, kr, sync, glog2, need, g->profiling ? &bin_ev : nullptr);
+      if (g->profiling) e1 = g->events.record(s);
     }
-    if (g->profiling) e1 = g->events.record(s);
-    read_counters(g);
+    LVG_CUDA(cudaStreamSynchronize(s));
+    if (g->hctr.p->err) read_counters(g);  // raises the device error
     if (g->profiling) {
       g->stats.move_kernel_ms += elapsed(e0, e1);
       for (auto &be : bin_ev) g->stats.move_bin_ms[be.first] += elapsed(be.second.first, be.second.second);
     }
+    if (graphs && !replay) capture_iteration(g, lv, com, ctot, tot, fa, kr, sync, glog2, need, key);
     el = double(g->hctr.p->el_fix) / GAIN_FIX / M;
     ++l;
     if (el <= E) break;

@@ -66,7 +66,8 @@ struct MoveArgs {
   const uint32_t *key;
   const float *w;
   const uint32_t *list;  // vertices of one degree bin
-  uint32_t count;
+  uint32_t count;        // list length (an upper bound when count_ptr is set)
+  const uint32_t *count_ptr;  // device-side list length (worklists), or nullptr
   uint32_t *vcom;        // membership (async: read/write; sync: snapshot, read only)
   float *ctot;           // community totals (async: read/write; sync: snapshot)
   uint32_t *dec;         // sync: decided community per vertex (EMPTY = stay)
@@ -151,6 +152,14 @@ void launch_ds_mark(const Level &g, const uint32_t *ds, const uint32_t *dd, size
                     uint32_t *gfirst, int glog2, Counters *ctr, cudaStream_t s);
 void launch_clear_isolated(const uint32_t *list, size_t n, uint8_t *vaff, const uint8_t *fa, cudaStream_t s);
 void launch_merge_marks(uint8_t *vaff, uint8_t *mark, size_t n, cudaStream_t s);
+// Worklists of one colour class: the active vertices of degree bins
+// 1..NUM_BINS-2 (positions bins[start[1] .. start[NUM_BINS-1])) are copied to
+// wl at the same bin offsets; wl_count[b] receives each bin's count.
+struct BinBounds {
+  uint64_t start[NUM_BINS + 1];
+};
+void launch_compact_active(const uint32_t *bins, const BinBounds &bb, const uint8_t *vaff, const uint8_t *fa,
+                           uint32_t *wl, uint32_t *wl_count, cudaStream_t s);
 // Deterministic mode: apply the decisions of one colour class (list of its vertices).
 void launch_apply_moves(const uint32_t *list, size_t n, uint32_t *dec, uint32_t *vcom, float *ctot,
                         const float *vtot, cudaStream_t s);

@@ -348,6 +348,33 @@ __global__ void level_init_kernel(size_t n, const float *vtot, uint32_t *vcom, f
   }
 }
 
+// Active vertices of one colour class into per-bin worklists (warp-aggregated
+// appends; the order within a worklist is unspecified).
+__global__ void compact_active_kernel(const uint32_t *bins, BinBounds bb, const uint8_t *vaff, const uint8_t *fa,
+                                      uint32_t *wl, uint32_t *wl_count) {
+  const uint64_t begin = bb.start[1], end = bb.start[NUM_BINS - 1];
+  const int lane = threadIdx.x & 31;
+  for (uint64_t base = begin + (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32 * 32; base < end;
+       base += uint64_t(gridDim.x) * blockDim.x) {
+    const uint64_t pos = base + lane;
+    int b = -1;
+    uint32_t u = 0;
+    if (pos < end) {
+      u = bins[pos];
+      if (vaff[u] && (!fa || fa[u])) {
+        b = 1;
+        while (pos >= bb.start[b + 1]) ++b;
+      }
+    }
+    const unsigned grp = __match_any_sync(0xffffffffu, b);
+    const int leader = __ffs(grp) - 1;
+    uint32_t at = 0;
+    if (b >= 0 && lane == leader) at = atomicAdd(&wl_count[b], uint32_t(__popc(grp)));
+    at = __shfl_sync(0xffffffffu, at, leader);
+    if (b >= 0) wl[bb.start[b] + at + __popc(grp & ((1u << lane) - 1u))] = u;
+  }
+}
+
 __global__ void gather_u32_kernel(const uint32_t *idx, size_t n, const uint32_t *src, uint32_t *dst) {
   GRID_STRIDE(i, n) dst[i] = src[idx[i]];
 }
@@ -531,6 +558,14 @@ void launch_community_scatter(const Level &g, const uint32_t *vcom, const uint32
 void launch_level_init(size_t n, const float *vtot, uint32_t *vcom, float *ctot, uint8_t *vaff, cudaStream_t s) {
   if (!n) return;
   level_init_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, vtot, vcom, ctot, vaff);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_compact_active(const uint32_t *bins, const BinBounds &bb, const uint8_t *vaff, const uint8_t *fa,
+                           uint32_t *wl, uint32_t *wl_count, cudaStream_t s) {
+  const uint64_t n = bb.start[NUM_BINS - 1] - bb.start[1];
+  if (!n) return;
+  compact_active_kernel<<<grid_for(n, 256), 256, 0, s>>>(bins, bb, vaff, fa, wl, wl_count);
   LVG_CHECK_LAUNCH();
 }
 

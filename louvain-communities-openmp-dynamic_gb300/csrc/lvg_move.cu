@@ -81,6 +81,29 @@ __device__ __forceinline__ void flush_counters(Counters *ctr, int bin, unsigned 
   }
 }
 
+// Warp-aggregated insertion: the 32 lanes of a converged warp each hold a
+// (c, w) pair (c == EMPTY: nothing). Lanes holding the same key are combined
+// (weights summed in lane order) and only the lowest such lane calls
+// ins(c, sum). Hot keys then cost one table atomic per warp instead of one
+// per lane. Returns false on the lanes whose ins() failed.
+template <class Ins>
+__device__ __forceinline__ bool warp_insert(uint32_t c, float w, Ins ins) {
+  const unsigned grp = __match_any_sync(0xffffffffu, c);
+  const int lane = threadIdx.x & 31;
+  const unsigned cnt = c == EMPTY ? 0u : unsigned(__popc(grp));
+  const unsigned most = __reduce_max_sync(0xffffffffu, cnt);
+  float sum = 0.f;
+  unsigned rem = grp;
+  for (unsigned it = 0; it < most; ++it) {
+    const int src = rem ? __ffs(rem) - 1 : lane;
+    rem &= rem - 1u;
+    const float x = __shfl_sync(0xffffffffu, w, src);
+    if (it < cnt) sum += x;
+  }
+  const bool leader = (grp & ((1u << lane) - 1u)) == 0u;
+  return !(leader && c != EMPTY) || ins(c, sum);
+}
+
 // ------------------------------------------------------------ tile / warp kernel
 
 constexpr int TILE_BLOCK = 256;
@@ -98,7 +121,8 @@ __global__ void __launch_bounds__(TILE_BLOCK) move_tile_kernel(MoveArgs a) {
   const uint32_t ntiles = gridDim.x * TPB;
   unsigned long long fix = 0, nv = 0, ne = 0, nm = 0;
   bool bad = false;
-  for (uint32_t i = blockIdx.x * TPB + tib; i < a.count; i += ntiles) {
+  const uint32_t count = a.count_ptr ? *a.count_ptr : a.count;
+  for (uint32_t i = blockIdx.x * TPB + tib; i < count; i += ntiles) {
     const uint32_t u = a.list[i];
     int act = 0;
     if (tl == 0) act = a.vaff[u] && (!a.fa || a.fa[u]);
@@ -115,6 +139,28 @@ __global__ void __launch_bounds__(TILE_BLOCK) move_tile_kernel(MoveArgs a) {
     // U independent edge loads per lane in flight (degree <= C/2, so a lane
     // has at most C/(2T) edges).
     constexpr int U = (C / (2 * T)) < 1 ? 1 : ((C / (2 * T)) > 4 ? 4 : (C / (2 * T)));
+    if (T == 32) {
+      // one warp per vertex: warp-uniform batches, hot keys combined per warp
+      for (uint32_t base = 0; base < dg; base += U * 32) {
+        uint32_t v[U];
+        float w[U];
+#pragma unroll
+        for (int k = 0; k < U; ++k) {
+          const uint32_t j = base + k * 32 + tl;
+          v[k] = j < dg ? a.key[o + j] : u;
+          w[k] = j < dg ? a.w[o + j] : 0.f;
+        }
+        uint32_t c[U];
+#pragma unroll
+        for (int k = 0; k < U; ++k) {
+          c[k] = v[k] != u ? a.vcom[v[k]] : EMPTY;
+          if (c[k] == d) { kd += w[k]; c[k] = EMPTY; }
+        }
+#pragma unroll
+        for (int k = 0; k < U; ++k)
+          ok &= warp_insert(c[k], w[k], [&](uint32_t cc, float ww) { return table_add(keys, vals, LOGC, cc, ww); });
+      }
+    } else
     for (uint32_t j0 = tl; j0 < dg; j0 += U * T) {
       uint32_t v[U];
       float w[U];
@@ -241,42 +287,92 @@ __device__ __forceinline__ bool smem_add_budget(uint32_t *keys, float *vals, int
   return false;
 }
 
-// Scan the edges of u (4 independent loads in flight per thread) into a
-// table; `add` inserts one (community, weight). Returns the lane-private
-// weight to the own community d.
+// A shared-memory table that also lists its claimed slots, so that the
+// argmax and the reset after a vertex touch only those slots. Claims are
+// limited to `limit` (half the table); a reservation whose slot was taken by
+// another key is listed as EMPTY.
+struct ListedTable {
+  uint32_t *keys;
+  float *vals;
+  uint32_t *list;
+  unsigned *used;
+};
+
+__device__ __forceinline__ bool lt_add(const ListedTable &t, int log2cap, uint32_t c, float w, unsigned limit) {
+  const uint32_t mask = (1u << log2cap) - 1u;
+  uint32_t s = hash_hi(c, log2cap);
+  for (uint32_t probe = 0; probe <= mask; ++probe) {
+    const uint32_t k = t.keys[s];
+    if (k == c) { atomicAdd(&t.vals[s], w); return true; }
+    if (k == EMPTY) {
+      const unsigned r = atomicAdd(t.used, 1u);
+      if (r >= limit) return false;
+      const uint32_t prev = atomicCAS(&t.keys[s], EMPTY, c);
+      if (prev == EMPTY) {
+        t.list[r] = s;
+        atomicAdd(&t.vals[s], w);
+        return true;
+      }
+      t.list[r] = EMPTY;
+      if (prev == c) { atomicAdd(&t.vals[s], w); return true; }
+    }
+    s = (s + 1u) & mask;
+  }
+  return false;
+}
+
+// Reset the listed slots (call with the whole block; ends with a barrier).
+template <int B>
+__device__ __forceinline__ void lt_reset(const ListedTable &t, unsigned n) {
+  for (unsigned i = threadIdx.x; i < n; i += B) {
+    const uint32_t s = t.list[i];
+    if (s != EMPTY) { t.keys[s] = EMPTY; t.vals[s] = 0.f; }
+  }
+  __syncthreads();
+}
+
+// Scan edges [o, o+n) of u with the whole block (warp-uniform trip counts, 4
+// independent loads in flight per lane) into a table via add(c, w), called
+// once per distinct key per warp batch. Edges into the own community d are
+// summed in the lane-private return value. Stops (block-uniformly per warp)
+// as soon as an add() fails.
 template <int B, class Add>
-__device__ __forceinline__ float scan_edges(const MoveArgs &a, uint32_t u, uint64_t o, uint32_t dg, uint32_t d,
+__device__ __forceinline__ float scan_edges(const MoveArgs &a, uint32_t u, uint64_t o, uint32_t n, uint32_t d,
                                             Add add) {
   constexpr int U = 4;
+  const uint32_t lane = threadIdx.x & 31u;
   float kd = 0.f;
-  for (uint32_t j0 = threadIdx.x; j0 < dg; j0 += U * B) {
+  for (uint32_t base = threadIdx.x & ~31u; base < n; base += U * B) {
     uint32_t v[U];
     float w[U];
 #pragma unroll
     for (int k = 0; k < U; ++k) {
-      const uint32_t j = j0 + k * B;
-      v[k] = j < dg ? a.key[o + j] : u;
-      w[k] = j < dg ? a.w[o + j] : 0.f;
+      const uint32_t j = base + k * B + lane;
+      v[k] = j < n ? a.key[o + j] : u;
+      w[k] = j < n ? a.w[o + j] : 0.f;
     }
     uint32_t c[U];
 #pragma unroll
-    for (int k = 0; k < U; ++k) c[k] = v[k] != u ? a.vcom[v[k]] : EMPTY;
-#pragma unroll
     for (int k = 0; k < U; ++k) {
-      if (c[k] == EMPTY) continue;
-      if (c[k] == d) kd += w[k];
-      else if (!add(c[k], w[k])) return kd;
+      c[k] = v[k] != u ? a.vcom[v[k]] : EMPTY;
+      if (c[k] == d) { kd += w[k]; c[k] = EMPTY; }
     }
+    bool fail = false;
+#pragma unroll
+    for (int k = 0; k < U; ++k) fail |= !warp_insert(c[k], w[k], add);
+    if (__any_sync(0xffffffffu, fail)) break;
   }
   return kd;
 }
 
-// One block per vertex (degree > 512). The vertex is first aggregated in a
-// shared table of 2^LOGS slots; if it has more distinct neighbour
-// communities than the table's budget (half its slots), it is redone with a
-// table in this block's region of global memory (2^a.glog2 slots). After the
-// first local-moving iterations a high-degree vertex's neighbours fall into
-// few communities, so the shared table almost always suffices.
+// One block per vertex (degree 513..8192). The vertex is first aggregated in
+// a listed shared table of 2^LOGS slots (cleared once per block, then reset
+// slot by slot); if it has more distinct neighbour communities than the
+// budget (half the slots), it is redone with a table in this block's region
+// of global memory (2^a.glog2 slots). After the first local-moving
+// iterations a high-degree vertex's neighbours fall into few communities, so
+// the shared table almost always suffices and the argmax visits only the
+// claimed slots.
 template <int B, int LOGS, bool SYNC>
 __global__ void __launch_bounds__(B) move_big_kernel(MoveArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
@@ -286,13 +382,19 @@ __global__ void __launch_bounds__(B) move_big_kernel(MoveArgs a) {
   __shared__ unsigned s_used;
   __shared__ int s_over;
   constexpr uint32_t CS = 1u << LOGS;
-  uint32_t *skeys = reinterpret_cast<uint32_t *>(smem);
-  float *svals = reinterpret_cast<float *>(smem + size_t(CS) * sizeof(uint32_t));
+  ListedTable t;
+  t.keys = reinterpret_cast<uint32_t *>(smem);
+  t.vals = reinterpret_cast<float *>(smem + size_t(CS) * 4);
+  t.list = reinterpret_cast<uint32_t *>(smem + size_t(CS) * 8);
+  t.used = &s_used;
+  for (uint32_t s2 = threadIdx.x; s2 < CS; s2 += B) { t.keys[s2] = EMPTY; t.vals[s2] = 0.f; }
   uint32_t *gkeys = a.gkeys ? a.gkeys + (size_t(blockIdx.x) << a.glog2) : nullptr;
   float *gvals = a.gvals ? a.gvals + (size_t(blockIdx.x) << a.glog2) : nullptr;
   unsigned long long fix = 0, nv = 0, ne = 0, nm = 0;
   bool bad = false;
-  for (uint32_t i = blockIdx.x; i < a.count; i += gridDim.x) {
+  const uint32_t count = a.count_ptr ? *a.count_ptr : a.count;
+  __syncthreads();
+  for (uint32_t i = blockIdx.x; i < count; i += gridDim.x) {
     const uint32_t u = a.list[i];
     if (threadIdx.x == 0) {
       s_act = a.vaff[u] && (!a.fa || a.fa[u]);
@@ -300,40 +402,35 @@ __global__ void __launch_bounds__(B) move_big_kernel(MoveArgs a) {
       s_over = 0;
     }
     __syncthreads();
-    const int act = s_act;
-    if (!act) {
+    if (!s_act) {
       __syncthreads();
       continue;
     }
     const uint64_t o = a.off[u];
     const uint32_t dg = a.deg[u];
     const uint32_t d = a.vcom[u];
-    // attempt 1: shared table sized for the degree (at most 2^LOGS slots)
     int lg = min(LOGS, max(1, ceil_log2(2ull * dg)));
-    uint32_t vcap = 1u << lg;
-    for (uint32_t s = threadIdx.x; s < vcap; s += B) { skeys[s] = EMPTY; svals[s] = 0.f; }
-    __syncthreads();
-    const unsigned limit = vcap >> 1;
+    const unsigned limit = (1u << lg) >> 1;
     float kd = scan_edges<B>(a, u, o, dg, d, [&](uint32_t c, float w) {
-      if (smem_add_budget(skeys, svals, lg, c, w, &s_used, limit)) return true;
+      if (lt_add(t, lg, c, w, limit)) return true;
       s_over = 1;
       return false;
     });
     __syncthreads();
-    uint32_t *keys = skeys;
-    float *vals = svals;
+    const unsigned nlist = min(s_used, limit);
+    const bool over = s_over;
     bool ok = true;
-    if (s_over) {
+    uint32_t gcap = 0;
+    if (over) {
       // attempt 2: global table sized for the degree
+      lt_reset<B>(t, nlist);
       lg = min(a.glog2, max(1, ceil_log2(2ull * dg)));
-      vcap = 1u << lg;
-      keys = gkeys;
-      vals = gvals;
-      if (!keys) { ok = false; vcap = 0; }
-      for (uint32_t s = threadIdx.x; s < vcap; s += B) { keys[s] = EMPTY; vals[s] = 0.f; }
+      gcap = gkeys ? (1u << lg) : 0;
+      if (!gkeys) ok = false;
+      for (uint32_t s2 = threadIdx.x; s2 < gcap; s2 += B) { gkeys[s2] = EMPTY; gvals[s2] = 0.f; }
       __syncthreads();
-      if (keys) kd = scan_edges<B>(a, u, o, dg, d, [&](uint32_t c, float w) {
-        ok &= table_add(keys, vals, lg, c, w);
+      if (gkeys) kd = scan_edges<B>(a, u, o, dg, d, [&](uint32_t c, float w) {
+        ok &= table_add(gkeys, gvals, lg, c, w);
         return true;
       });
     }
@@ -342,13 +439,24 @@ __global__ void __launch_bounds__(B) move_big_kernel(MoveArgs a) {
     const float td = a.ctot[d];
     float bg = 0.f;
     uint32_t bc = EMPTY;
-    for (uint32_t s = threadIdx.x; s < vcap; s += B) {
-      const uint32_t c = keys[s];
-      if (c == EMPTY) continue;
-      const float g = gain_f32(vals[s], kd, wu, a.ctot[c], td, a.kr);
-      if (g > 0.f) take_better(bg, bc, g, c);
+    if (!over) {
+      for (unsigned j = threadIdx.x; j < nlist; j += B) {
+        const uint32_t s2 = t.list[j];
+        if (s2 == EMPTY) continue;
+        const uint32_t c = t.keys[s2];
+        const float g = gain_f32(t.vals[s2], kd, wu, a.ctot[c], td, a.kr);
+        if (g > 0.f) take_better(bg, bc, g, c);
+      }
+    } else {
+      for (uint32_t s2 = threadIdx.x; s2 < gcap; s2 += B) {
+        const uint32_t c = gkeys[s2];
+        if (c == EMPTY) continue;
+        const float g = gain_f32(gvals[s2], kd, wu, a.ctot[c], td, a.kr);
+        if (g > 0.f) take_better(bg, bc, g, c);
+      }
     }
     block_argmax<B>(bg, bc, red_g, red_c);
+    if (!over) lt_reset<B>(t, nlist);
     const bool moved = bc != EMPTY && bc != 0;
     if (threadIdx.x == 0) {
       if (bc != EMPTY) fix += gain_to_fix(bg);
@@ -384,11 +492,11 @@ __global__ void __launch_bounds__(B) move_big_kernel(MoveArgs a) {
 // ------------------------------------------------------------ chunked hubs
 
 // Hub path, step 1: one block per chunk of HUB_CHUNK edges of one hub of the
-// colour class. The chunk is merged in a shared table with a claim budget
-// and its distinct (community, weight) pairs are written to the chunk's
-// partial region; a chunk with more distinct communities than the budget
-// writes its raw pairs instead. Edges into the hub's own community are summed
-// separately into hub_kd[u].
+// colour class. The chunk is merged in a listed shared table with a claim
+// budget and its distinct (community, weight) pairs are written to the
+// chunk's partial region; a chunk with more distinct communities than the
+// budget writes its raw pairs instead. Edges into the hub's own community are
+// summed separately into hub_kd[u].
 template <int B, int LOGS>
 __global__ void __launch_bounds__(B) hub_chunk_kernel(MoveArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
@@ -396,8 +504,12 @@ __global__ void __launch_bounds__(B) hub_chunk_kernel(MoveArgs a) {
   __shared__ int s_act;
   __shared__ unsigned s_used, s_cnt;
   __shared__ int s_over;
-  uint32_t *skeys = reinterpret_cast<uint32_t *>(smem);
-  float *svals = reinterpret_cast<float *>(smem + (size_t(1) << LOGS) * sizeof(uint32_t));
+  constexpr uint32_t CS = 1u << LOGS;
+  ListedTable t;
+  t.keys = reinterpret_cast<uint32_t *>(smem);
+  t.vals = reinterpret_cast<float *>(smem + size_t(CS) * 4);
+  t.list = reinterpret_cast<uint32_t *>(smem + size_t(CS) * 8);
+  t.used = &s_used;
   const size_t ci = a.hub.chunk_begin[a.color] + blockIdx.x;
   const uint4 ch = a.hub.chunk[ci];
   const uint32_t u = a.hub.hub_vertex[ch.x];
@@ -417,50 +529,25 @@ __global__ void __launch_bounds__(B) hub_chunk_kernel(MoveArgs a) {
   const uint32_t d = a.vcom[u];
   const int lg = min(LOGS, max(1, ceil_log2(2ull * n)));
   const uint32_t vcap = 1u << lg;
-  for (uint32_t s = threadIdx.x; s < vcap; s += B) { skeys[s] = EMPTY; svals[s] = 0.f; }
+  for (uint32_t s2 = threadIdx.x; s2 < vcap; s2 += B) { t.keys[s2] = EMPTY; t.vals[s2] = 0.f; }
   __syncthreads();
   const unsigned limit = vcap >> 1;
-  float kd = 0.f;
-  constexpr int U = 4;
-  for (uint32_t j0 = threadIdx.x; j0 < n; j0 += U * B) {
-    uint32_t v[U];
-    float w[U];
-#pragma unroll
-    for (int k = 0; k < U; ++k) {
-      const uint32_t j = j0 + k * B;
-      v[k] = j < n ? a.key[o + j] : u;
-      w[k] = j < n ? a.w[o + j] : 0.f;
-    }
-    uint32_t c[U];
-#pragma unroll
-    for (int k = 0; k < U; ++k) c[k] = v[k] != u ? a.vcom[v[k]] : EMPTY;
-    bool stop = false;
-#pragma unroll
-    for (int k = 0; k < U; ++k) {
-      if (c[k] == EMPTY || stop) continue;
-      if (c[k] == d) kd += w[k];
-      else if (!smem_add_budget(skeys, svals, lg, c[k], w[k], &s_used, limit)) { s_over = 1; stop = true; }
-    }
-    if (stop) break;
-  }
+  float kd = scan_edges<B>(a, u, o, n, d, [&](uint32_t c, float w) {
+    if (lt_add(t, lg, c, w, limit)) return true;
+    s_over = 1;
+    return false;
+  });
   __syncthreads();
   uint32_t *pk = a.part_key + a.hub.chunk_part[ci];
   float *pv = a.part_val + a.hub.chunk_part[ci];
-  const int lane = threadIdx.x & 31;
   if (!s_over) {
-    for (uint32_t s0 = 0; s0 < vcap; s0 += B) {
-      const uint32_t s = s0 + threadIdx.x;
-      const uint32_t k = s < vcap ? skeys[s] : EMPTY;
-      const bool has = k != EMPTY;
-      const unsigned bal = __ballot_sync(0xffffffffu, has);
-      uint32_t base = 0;
-      if (lane == 0 && bal) base = atomicAdd(&s_cnt, uint32_t(__popc(bal)));
-      base = __shfl_sync(0xffffffffu, base, 0);
-      if (has) {
-        const uint32_t r = __popc(bal & ((1u << lane) - 1u));
-        pk[base + r] = k;
-        pv[base + r] = svals[s];
-      }
+    const unsigned nl = min(s_used, limit);
+    for (unsigned j = threadIdx.x; j < nl; j += B) {
+      const uint32_t s2 = t.list[j];
+      if (s2 == EMPTY) continue;
+      const uint32_t pos = atomicAdd(&s_cnt, 1u);
+      pk[pos] = t.keys[s2];
+      pv[pos] = t.vals[s2];
     }
   } else {
     // too many distinct communities in this chunk: hand its raw pairs on
@@ -469,9 +556,8 @@ __global__ void __launch_bounds__(B) hub_chunk_kernel(MoveArgs a) {
       const uint32_t v = a.key[o + j];
       const uint32_t c = v != u ? a.vcom[v] : EMPTY;
       const float w = a.w[o + j];
-      const bool keep = c != EMPTY && c != d;
       if (c == d) kd += w;
-      if (keep) {
+      if (c != EMPTY && c != d) {
         const uint32_t pos = atomicAdd(&s_cnt, 1u);
         pk[pos] = c;
         pv[pos] = w;
@@ -486,9 +572,9 @@ __global__ void __launch_bounds__(B) hub_chunk_kernel(MoveArgs a) {
 }
 
 // Hub path, step 2: one block per hub of the colour class (grid-stride).
-// Merges the partial entries of the hub's chunks (shared table with a claim
-// budget; global fallback region otherwise), then chooses and applies the
-// move like the other local-moving kernels.
+// Merges the partial entries of the hub's chunks (listed shared table with a
+// claim budget; global fallback region otherwise), then chooses and applies
+// the move like the other local-moving kernels.
 template <int B, int LOGS, bool SYNC>
 __global__ void __launch_bounds__(B) hub_merge_kernel(MoveArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
@@ -499,13 +585,18 @@ __global__ void __launch_bounds__(B) hub_merge_kernel(MoveArgs a) {
   __shared__ int s_over;
   __shared__ float s_kd;
   constexpr uint32_t CS = 1u << LOGS;
-  uint32_t *skeys = reinterpret_cast<uint32_t *>(smem);
-  float *svals = reinterpret_cast<float *>(smem + size_t(CS) * sizeof(uint32_t));
+  ListedTable t;
+  t.keys = reinterpret_cast<uint32_t *>(smem);
+  t.vals = reinterpret_cast<float *>(smem + size_t(CS) * 4);
+  t.list = reinterpret_cast<uint32_t *>(smem + size_t(CS) * 8);
+  t.used = &s_used;
+  for (uint32_t s2 = threadIdx.x; s2 < CS; s2 += B) { t.keys[s2] = EMPTY; t.vals[s2] = 0.f; }
   uint32_t *gkeys = a.gkeys ? a.gkeys + (size_t(blockIdx.x) << a.glog2) : nullptr;
   float *gvals = a.gvals ? a.gvals + (size_t(blockIdx.x) << a.glog2) : nullptr;
   const size_t h0 = a.hub.hub_begin[a.color], h1 = a.hub.hub_begin[a.color + 1];
   unsigned long long fix = 0, nv = 0, ne = 0, nm = 0;
   bool bad = false;
+  __syncthreads();
   for (size_t g = h0 + blockIdx.x; g < h1; g += gridDim.x) {
     const uint32_t u = a.hub.hub_vertex[g];
     const uint32_t c0 = a.hub.hub_first[g], c1 = a.hub.hub_first[g + 1];
@@ -524,53 +615,63 @@ __global__ void __launch_bounds__(B) hub_merge_kernel(MoveArgs a) {
     }
     const uint32_t dg = a.deg[u];
     const uint32_t d = a.vcom[u];
-    // entries to merge: at most the hub's degree
     int lg = min(LOGS, max(1, ceil_log2(2ull * dg)));
-    uint32_t vcap = 1u << lg;
-    for (uint32_t s = threadIdx.x; s < vcap; s += B) { skeys[s] = EMPTY; svals[s] = 0.f; }
-    __syncthreads();
-    const unsigned limit = vcap >> 1;
-    for (uint32_t c = c0; c < c1 && !s_over; ++c) {
+    const unsigned limit = (1u << lg) >> 1;
+    for (uint32_t c = c0; c < c1; ++c) {
       const uint64_t p = a.hub.chunk_part[c];
       const uint32_t cnt = a.chunk_cnt[c];
-      for (uint32_t t = threadIdx.x; t < cnt; t += B)
-        if (!smem_add_budget(skeys, svals, lg, a.part_key[p + t], a.part_val[p + t], &s_used, limit)) {
+      bool stop = false;
+      for (uint32_t q = threadIdx.x; q < cnt; q += B)
+        if (!lt_add(t, lg, a.part_key[p + q], a.part_val[p + q], limit)) {
           s_over = 1;
+          stop = true;
           break;
         }
+      if (stop) break;
     }
     __syncthreads();
-    uint32_t *keys = skeys;
-    float *vals = svals;
+    const unsigned nlist = min(s_used, limit);
+    const bool over = s_over;
     bool ok = true;
-    if (s_over) {
+    uint32_t gcap = 0;
+    if (over) {
+      lt_reset<B>(t, nlist);
       lg = min(a.glog2, max(1, ceil_log2(2ull * dg)));
-      vcap = 1u << lg;
-      keys = gkeys;
-      vals = gvals;
-      if (!keys) { ok = false; vcap = 0; }
-      for (uint32_t s = threadIdx.x; s < vcap; s += B) { keys[s] = EMPTY; vals[s] = 0.f; }
+      gcap = gkeys ? (1u << lg) : 0;
+      if (!gkeys) ok = false;
+      for (uint32_t s2 = threadIdx.x; s2 < gcap; s2 += B) { gkeys[s2] = EMPTY; gvals[s2] = 0.f; }
       __syncthreads();
-      if (keys)
+      if (gkeys)
         for (uint32_t c = c0; c < c1; ++c) {
           const uint64_t p = a.hub.chunk_part[c];
           const uint32_t cnt = a.chunk_cnt[c];
-          for (uint32_t t = threadIdx.x; t < cnt; t += B) ok &= table_add(keys, vals, lg, a.part_key[p + t], a.part_val[p + t]);
+          for (uint32_t q = threadIdx.x; q < cnt; q += B) ok &= table_add(gkeys, gvals, lg, a.part_key[p + q], a.part_val[p + q]);
         }
+      __syncthreads();
     }
-    __syncthreads();
     const float kd = s_kd;
     const float wu = a.vtot[u];
     const float td = a.ctot[d];
     float bg = 0.f;
     uint32_t bc = EMPTY;
-    for (uint32_t s = threadIdx.x; s < vcap; s += B) {
-      const uint32_t c = keys[s];
-      if (c == EMPTY) continue;
-      const float g2 = gain_f32(vals[s], kd, wu, a.ctot[c], td, a.kr);
-      if (g2 > 0.f) take_better(bg, bc, g2, c);
+    if (!over) {
+      for (unsigned j = threadIdx.x; j < nlist; j += B) {
+        const uint32_t s2 = t.list[j];
+        if (s2 == EMPTY) continue;
+        const uint32_t c = t.keys[s2];
+        const float g2 = gain_f32(t.vals[s2], kd, wu, a.ctot[c], td, a.kr);
+        if (g2 > 0.f) take_better(bg, bc, g2, c);
+      }
+    } else {
+      for (uint32_t s2 = threadIdx.x; s2 < gcap; s2 += B) {
+        const uint32_t c = gkeys[s2];
+        if (c == EMPTY) continue;
+        const float g2 = gain_f32(gvals[s2], kd, wu, a.ctot[c], td, a.kr);
+        if (g2 > 0.f) take_better(bg, bc, g2, c);
+      }
     }
     block_argmax<B>(bg, bc, red_g, red_c);
+    if (!over) lt_reset<B>(t, nlist);
     const bool moved = bc != EMPTY && bc != 0;
     if (threadIdx.x == 0) {
       a.hub_kd[u] = 0.f;
@@ -637,7 +738,7 @@ void launch_tile(const MoveArgs &a, cudaStream_t s) {
 
 template <int B, int LOGS, bool SYNC>
 void launch_big(const MoveArgs &a, cudaStream_t s) {
-  const size_t smem = (size_t(1) << LOGS) * 8;
+  const size_t smem = (size_t(1) << LOGS) * 10;  // keys, values, claimed list
   auto k = move_big_kernel<B, LOGS, SYNC>;
   static bool configured = false;
   if (!configured) { set_smem(k, smem); configured = true; }
@@ -650,7 +751,7 @@ void launch_big(const MoveArgs &a, cudaStream_t s) {
 template <bool SYNC>
 void launch_hubs(const MoveArgs &a, cudaStream_t s) {
   constexpr int B = 512, LOGS = 13;
-  const size_t smem = (size_t(1) << LOGS) * 8;
+  const size_t smem = (size_t(1) << LOGS) * 10;  // keys, values, claimed list
   const size_t nch = a.hub.chunk_begin[a.color + 1] - a.hub.chunk_begin[a.color];
   const size_t nh = a.hub.hub_begin[a.color + 1] - a.hub.hub_begin[a.color];
   if (!nh) return;
