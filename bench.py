@@ -58,6 +58,9 @@ def parse():
     p.add_argument("--seed", type=int, default=42)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-steps", type=int, default=2)
+    p.add_argument("--ncu-steps", type=int, default=0,
+                   help="profiling mode: set up as usual, then run this many DF steps between "
+                        "cudaProfilerStart/Stop (for ncu --profile-from-start off) and exit")
     return p.parse_args()
 
 
@@ -255,6 +258,18 @@ def run_gpu(args):
     db = lvg.DeviceBatch(Y, b)
     o = lvg.LouvainOptions()
 
+    if args.ncu_steps:
+        lvg.run_resident(Y, lvg.METHOD_FRONTIER, db, st_prior, st_out, o)  # warm: graph capture
+        lvg.profiler_start()
+        for _ in range(args.ncu_steps):
+            info = lvg.run_resident(Y, lvg.METHOD_FRONTIER, db, st_prior, st_out, o)
+        lvg.profiler_stop()
+        if rank == 0:
+            print(f"profiled {args.ncu_steps} DF steps: last {info['time']:.3f} ms, {Y.stats()['kernel_launches']} "
+                  f"kernel launches per step", flush=True)
+        dist.close()
+        return 0
+
     # plain GPU static Louvain on the updated graph (the spec comparator)
     static_times = []
     for _ in range(2):
@@ -315,10 +330,12 @@ def run_gpu(args):
 
     peak, peak_kind = peaks()
     achieved = None
+    alg_per_step = (MOVE_BYTES_PER_EDGE * kedges + MOVE_BYTES_PER_VERTEX * kverts) / args.steps
     if kms > 0:
         # bytes and time of all local-moving launches of the profiled steps
-        achieved = (MOVE_BYTES_PER_EDGE * kedges + MOVE_BYTES_PER_VERTEX * kverts) / (kms / 1e3) / 1e9
+        achieved = alg_per_step / (kms / args.steps / 1e3) / 1e9
     tr = traffic_per_launch()
+    traffic = int(tr["traffic_ratio"] * alg_per_step) if tr else None
     line = {
         "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
@@ -332,7 +349,11 @@ def run_gpu(args):
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
-                     "traffic": tr.get("bytes_per_launch") if tr else None,
+                     "traffic": traffic,
+                     "traffic_note": ("DRAM bytes of the local-moving kernels per step, ncu capture on R-MAT "
+                                      "scale 22 (profiles/move_traffic.json, ratio to algorithmic bytes) scaled "
+                                      "by this step's algorithmic bytes") if tr else None,
+                     "algorithmic_bytes_per_step": int(alg_per_step),
                      "kernel": "local-moving kernels (move_tile/move_block, all degree bins)",
                      "launches_per_step": klaunch / args.steps, "ms_per_step": kms / args.steps,
                      "per_bin_ms_per_step": [round(v / args.steps, 4) for v in bin_ms],
