@@ -58,6 +58,18 @@ def parse():
     p.add_argument("--seed", type=int, default=42)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-steps", type=int, default=2)
+    p.add_argument("--workload", default="df", choices=["df", "serving"],
+                   help="df: the headline (R-MAT scale 24, one graph); serving: many resident graphs under "
+                        "Poisson batch-update arrivals through lvg_server")
+    p.add_argument("--graphs", type=int, default=64)
+    p.add_argument("--scale-min", type=int, default=18)
+    p.add_argument("--scale-max", type=int, default=22)
+    p.add_argument("--rate", type=float, default=2000.0, help="serving: offered requests/s")
+    p.add_argument("--duration", type=float, default=3.0, help="serving: seconds of arrivals")
+    p.add_argument("--size-min", type=int, default=10)
+    p.add_argument("--size-max", type=int, default=100000)
+    p.add_argument("--workers", type=int, default=16)
+    p.add_argument("--budget-gb", type=float, default=120.0)
     p.add_argument("--ncu-steps", type=int, default=0,
                    help="profiling mode: set up as usual, then run this many DF steps between "
                         "cudaProfilerStart/Stop (for ncu --profile-from-start off) and exit")
@@ -396,10 +408,104 @@ def cpu_baseline(args, y, b, prior):
             "ms_per_step": ms, "modularity": orc.modularity(y, q)}
 
 
+def run_serving(args):
+    """Serving: resident R-MAT graphs (scale uniform in [scale-min, scale-max],
+    edge factor 16, generated in HBM), Poisson arrivals at `rate`, each request
+    a batch of log-uniform [size-min, size-max] undirected updates (20 %
+    deletions of edges of the graph, 80 % uniform-pair insertions, both
+    directions, drawn as the reference's generators draw them), answered by
+    lvg_server (tidy + apply in HBM, then dynamic-frontier Louvain from the
+    graph's current state). value = p99 request latency (submit to completion)."""
+    rank, world, local = dist_info()
+    import lvg
+    import lvg_build
+
+    lvg_build.build()
+    lvg.set_device(local)
+    rng = np.random.default_rng(args.seed)
+    budget = int(args.budget_gb * (1 << 30))
+    sv = lvg.Server(workers=args.workers, hbm_budget=budget, method=lvg.METHOD_FRONTIER)
+    t0 = time.time()
+    graphs, ids, refused = [], [], 0
+    scales = rng.integers(args.scale_min, args.scale_max + 1, args.graphs)
+    for i, sc in enumerate(scales):
+        G = lvg.Graph.rmat(int(sc), 16, seed=args.seed + i)
+        try:
+            ids.append(sv.add_graph(G))
+            graphs.append(G)
+        except lvg.LvgError as e:
+            if e.code != lvg.LVG_ENOMEM:
+                raise
+            refused += 1
+            G.close()
+    t_setup = time.time() - t0
+    # arrivals and payloads (drawn before the timed window)
+    n_req = max(1, int(args.rate * args.duration))
+    gaps = rng.exponential(1.0 / args.rate, n_req)
+    at = np.cumsum(gaps)
+    which = rng.integers(0, len(ids), n_req)
+    sizes = np.exp(rng.uniform(np.log(args.size_min), np.log(args.size_max), n_req)).astype(np.int64)
+    payloads = [None] * n_req
+    for g in range(len(ids)):
+        reqs = np.nonzero(which == g)[0]
+        if not len(reqs):
+            continue
+        nd = (sizes[reqs] * 0.2).round().astype(np.int64)
+        ni = sizes[reqs] - nd
+        db = lvg.DeviceBatch.generate(graphs[g], int(nd.sum()), int(ni.sum()), seed=args.seed * 1000 + g)
+        hb = db.download()
+        db.close()
+        d0 = i0 = 0
+        for r, a, c in zip(reqs, nd, ni):
+            # failed deletion draws are dropped by the generator: take what is left in order
+            a2 = min(2 * int(a), len(hb.del_src) - d0)
+            payloads[r] = lvg.HostBatch(hb.del_src[d0:d0 + a2], hb.del_dst[d0:d0 + a2], hb.del_w[d0:d0 + a2],
+                                        hb.ins_src[i0:i0 + 2 * c], hb.ins_dst[i0:i0 + 2 * c],
+                                        hb.ins_w[i0:i0 + 2 * c])
+            d0 += a2
+            i0 += 2 * int(c)
+    # warm-up: one small request per graph (capture, workspace)
+    for g in ids:
+        sv.submit(g, lvg.HostBatch.empty())
+    sv.drain()
+    sv.stats(reset=True)
+    with Clocks(local) as clk:
+        start = time.perf_counter()
+        for k in range(n_req):
+            while time.perf_counter() - start < at[k]:
+                pass
+            sv.submit(int(ids[which[k]]), payloads[k])
+        offered_s = time.perf_counter() - start
+        sv.drain()
+    st = sv.stats()
+    entries = int(sum(p.num_deletions + p.num_insertions for p in payloads))
+    line = {
+        "metric": "serving p99 update latency (tidy + apply + DF per request)", "value": st["p99_ms"],
+        "unit": "ms", "n_gpus": world, "steps": n_req, "warmup": len(ids), "ms_per_step": st["mean_ms"],
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"serving: {len(ids)} resident R-MAT graphs scale {args.scale_min}-{args.scale_max} "
+                               f"ef16, Poisson {args.rate:g} req/s for {args.duration:g} s, log-uniform "
+                               f"[{args.size_min}, {args.size_max}] updates 80/20, {args.workers} workers",
+                   "graphs": len(ids), "refused_by_admission": refused, "hbm_budget_gb": args.budget_gb,
+                   "hbm_reserved_gb": st["hbm_reserved"] / 2**30, "requests": n_req, "batch_entries": entries,
+                   "setup_s": t_setup},
+        "latency_ms": {"p50": st["p50_ms"], "p99": st["p99_ms"], "mean": st["mean_ms"], "max": st["max_ms"]},
+        "updates_per_s": st["updates_per_s"], "requests_per_s": st["requests_per_s"],
+        "offered_requests_per_s": n_req / offered_s, "completed": st["completed"], "failed": st["failed"],
+        "clocks": clk.summary(),
+    }
+    sv.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "serving":
+        return run_serving(args)
     return run_gpu(args)
 
 

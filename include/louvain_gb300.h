@@ -193,6 +193,8 @@ int lvg_state_create(lvg_graph *g, lvg_state **out);
 int lvg_state_set(lvg_state *st, const uint32_t *q, const double *qvtot, const double *qctot);
 /* Download into host arrays of span entries; any pointer may be NULL. */
 int lvg_state_get(const lvg_state *st, uint32_t *membership, double *vtot, double *ctot);
+/* A state or device batch may be destroyed before or after its graph; every
+ * other call on it needs the graph alive. */
 int lvg_state_destroy(lvg_state *st);
 
 /* A validated batch in HBM. */
@@ -200,12 +202,117 @@ typedef struct lvg_device_batch lvg_device_batch;
 int lvg_device_batch_create(lvg_graph *g, const lvg_batch *b, lvg_device_batch **out);
 int lvg_device_batch_destroy(lvg_device_batch *b);
 
+/* Caller-owned arrays that receive a batch; the counts are written back. */
+typedef struct lvg_batch_buf {
+  size_t    num_deletions;
+  uint32_t *del_src, *del_dst;
+  float    *del_w;
+  size_t    num_insertions;
+  uint32_t *ins_src, *ins_dst;
+  float    *ins_w;
+} lvg_batch_buf;
+
+/* Tidy a batch against the graph and apply it in place, on the GPU.
+ * Replaces the host-side pair main.cxx:108-109 runs before each dynamic call:
+ * tidyBatchUpdateU(deletions, insertions, y) (inc/batch.hxx:202-209) keeps the
+ * deletions whose edge is present and the insertions whose edge is absent,
+ * sorted by (source, target) without duplicates, and
+ * applyBatchUpdateOmpU(y, deletions, insertions) (inc/batch.hxx:241-248)
+ * removes and adds them; an added edge makes both endpoints present. The
+ * batch may be unsorted and hold duplicates (the first in batch order is
+ * kept; the reference keeps an unspecified one). Ids must be < span (the
+ * graph does not grow its span). Only the touched rows are rewritten: the
+ * graph keeps per-row slack and an overflow pool. Needs the rows given to
+ * lvg_graph_create sorted by neighbour id (LVG_EINVAL otherwise).
+ * `tidy` (may be NULL; arrays with room for b's counts) receives the tidied
+ * batch, which is what the dynamic methods take. */
+int lvg_graph_apply_batch(lvg_graph *g, const lvg_batch *b, lvg_batch_buf *tidy);
+/* The same for a batch in HBM (created on this graph); the batch is replaced
+ * by the tidied batch, ready for lvg_run_resident. A batch applies once
+ * (LVG_EINVAL the second time). */
+int lvg_graph_apply_device_batch(lvg_graph *g, lvg_device_batch *b);
+
+/* ---- Generators in HBM (no reference counterpart; the same draws as the
+ * host generators of louvain_gb300_graphgen.h, so the graphs equal
+ * lvgg_planted_partition / lvgg_rmat row for row). */
+int lvg_graph_create_planted_partition(uint32_t n, uint32_t block, double avg_degree, double p_in, uint64_t seed,
+                                       lvg_graph **out);
+int lvg_graph_create_rmat(int scale, double edge_factor, double a, double b, double c, int permute, uint64_t seed,
+                          lvg_graph **out);
+/* A random batch drawn on the device as the reference draws one:
+ * generateEdgeDeletions(rnd, y, deletions, begin, range, true) and
+ * generateEdgeInsertions(rnd, y, insertions, begin, range, true, weight)
+ * (inc/batch.hxx:105-143), each draw from its own counter-based stream
+ * instead of one mt19937 (lvgg_reference_batch draws the same on the host).
+ * The batch is untidy; lvg_graph_apply_device_batch tidies and applies it. */
+int lvg_device_batch_generate(lvg_graph *g, size_t deletions, size_t insertions, uint32_t begin, uint32_t range,
+                              float weight, uint64_t seed, lvg_device_batch **out);
+/* Entry counts of a device batch, and a copy of it into host arrays. */
+int lvg_device_batch_size(const lvg_device_batch *b, size_t *deletions, size_t *insertions);
+int lvg_device_batch_download(const lvg_device_batch *b, lvg_batch_buf *out);
+
+/* Download the graph as a compact CSR: offsets[span+1], keys/weights[size],
+ * exists[span] (any of keys/weights/exists may be NULL). Rows come out in
+ * the order they are held (sorted when the uploaded rows were). */
+int lvg_graph_download(lvg_graph *g, uint64_t *offsets, uint32_t *keys, float *weights, uint8_t *exists);
+
 /* Run a method on device-resident inputs: prior state `prior` (ignored by
  * LVG_METHOD_STATIC) and batch `b` (NULL for static); the result state is
  * written to `out` (out may equal prior: updated in place). `info` receives
  * the scalar fields of the result; its arrays are not touched. */
 int lvg_run_resident(lvg_graph *g, int method, const lvg_device_batch *b, const lvg_state *prior, lvg_state *out,
                      const lvg_options *o, lvg_result *info);
+
+/* ---- Serving loop (no reference counterpart; the reference runs one graph
+ * and one batch at a time, main.cxx:101-135). A server keeps many graphs and
+ * their community state in HBM and answers batch updates: each request is a
+ * host batch for one graph, which a worker uploads, tidies and applies to the
+ * graph in HBM (lvg_graph_apply_device_batch) before running `method` from
+ * the graph's current state (lvg_run_resident), whose result replaces it.
+ * Requests for one graph run in arrival order; different graphs run
+ * concurrently, one worker thread each, on their own streams. */
+typedef struct lvg_server lvg_server;
+typedef struct lvg_server_options {
+  int         workers;     /* host worker threads = requests in flight (default 8) */
+  size_t      hbm_budget;  /* admission budget in bytes for resident graphs (default 120 GiB) */
+  int         method;      /* LVG_METHOD_NAIVE / _DELTA / _FRONTIER (default FRONTIER) */
+  lvg_options louvain;     /* options of every run */
+} lvg_server_options;
+typedef struct lvg_request_info {
+  uint64_t ticket;
+  int      graph, status;
+  double   queue_ms, apply_ms, run_ms, latency_ms;  /* latency = submit to completion */
+  int      iterations, passes;
+  uint64_t affected;
+  size_t   tidy_deletions, tidy_insertions;         /* the batch after the tidy */
+} lvg_request_info;
+typedef struct lvg_server_stats_t {
+  uint64_t completed, failed, updates;  /* updates = batch entries of completed requests */
+  size_t   graphs, hbm_reserved;
+  double   p50_ms, p99_ms, max_ms, mean_ms;  /* request latency */
+  double   wall_s, updates_per_s, requests_per_s;
+} lvg_server_stats_t;
+void lvg_server_options_default(lvg_server_options *o);
+/* Estimated device bytes of a resident graph (the admission rule). */
+size_t lvg_graph_footprint(size_t span, size_t edges);
+int lvg_server_create(const lvg_server_options *o, lvg_server **out);
+/* Add a graph (LVG_ENOMEM when its footprint does not fit the budget). Its
+ * state starts from (q, qvtot, qctot), or from static Louvain when q is NULL.
+ * With take_ownership the server destroys the graph at the end. */
+int lvg_server_add_graph(lvg_server *sv, lvg_graph *g, int take_ownership, const uint32_t *q, const double *qvtot,
+                         const double *qctot, int *graph_id);
+/* Queue a batch for a graph (copied; the caller's arrays may be reused). */
+int lvg_server_submit(lvg_server *sv, int graph_id, const lvg_batch *b, uint64_t *ticket);
+/* Wait for a request; returns its status. Each ticket can be waited once. */
+int lvg_server_wait(lvg_server *sv, uint64_t ticket, lvg_request_info *info);
+/* Wait until every queued request has completed. */
+int lvg_server_drain(lvg_server *sv);
+int lvg_server_stats(lvg_server *sv, int reset, lvg_server_stats_t *out);
+/* A graph's current state (after its queued requests), into host arrays. */
+int lvg_server_membership(lvg_server *sv, int graph_id, uint32_t *membership, double *vtot, double *ctot);
+lvg_graph *lvg_server_graph(lvg_server *sv, int graph_id);
+/* Drains, stops the workers, frees the states and owned graphs. */
+int lvg_server_destroy(lvg_server *sv);
 
 /* Per-call device statistics of the last run on g (no reference
  * counterpart; used for the roofline figures): kernel time of the

@@ -83,6 +83,17 @@ int lvgg_random_batch(const lvgg_csr *x, size_t num_updates, double insertion_fr
 /** y = x with the batch's deletions removed and insertions added (rows stay sorted). */
 int lvgg_apply_batch(const lvgg_csr *x, const lvgg_batch *b, lvgg_csr *y);
 
+/* A random untidy batch as the reference draws one:
+ * generateEdgeDeletions(rnd, x, deletions, begin, range, true) and
+ * generateEdgeInsertions(rnd, x, insertions, begin, range, true, weight)
+ * (inc/batch.hxx:105-143): a deletion picks a source uniform in
+ * [begin, begin+range), retried up to 5 times while it has no edge, then a
+ * uniform neighbour; an insertion picks both endpoints uniform in the range;
+ * both directions are emitted. Each draw has its own counter-based stream,
+ * so the result equals lvg_device_batch_generate's on the same graph. */
+int lvgg_reference_batch(const lvgg_csr *x, size_t deletions, size_t insertions, uint32_t begin, uint32_t range,
+                         float weight, uint64_t seed, lvgg_batch *out);
+
 void lvgg_csr_free(lvgg_csr *g);
 void lvgg_batch_free(lvgg_batch *b);
 

@@ -290,14 +290,14 @@ __global__ void __launch_bounds__(B) agg_block_kernel(AggArgs a) {
   }
 }
 
-int g_sms = 0;
-int sms() {
-  if (!g_sms) {
-    int dev = 0;
+int sms() {  // SM count of the device, queried once (thread-safe static init)
+  static const int n = [] {
+    int dev = 0, c = 0;
     LVG_CUDA(cudaGetDevice(&dev));
-    LVG_CUDA(cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev));
-  }
-  return g_sms;
+    LVG_CUDA(cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev));
+    return c;
+  }();
+  return n;
 }
 
 template <class K>

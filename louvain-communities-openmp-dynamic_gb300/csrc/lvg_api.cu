@@ -23,45 +23,6 @@ namespace lvg {
 
 thread_local std::string g_err;
 
-template <class T>
-struct DBuf {
-  T *p = nullptr;
-  size_t n = 0;
-  DBuf() = default;
-  DBuf(const DBuf &) = delete;
-  DBuf &operator=(const DBuf &) = delete;
-  ~DBuf() { release(); }
-  void ensure(size_t k) {
-    if (p && k <= n) return;
-    release();
-    if (k == 0) k = 1;
-    LVG_CUDA(cudaMalloc(&p, k * sizeof(T)));
-    n = k;
-  }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
-  }
-};
-
-template <class T>
-struct HBuf {  // pinned host buffer
-  T *p = nullptr;
-  size_t n = 0;
-  HBuf() = default;
-  HBuf(const HBuf &) = delete;
-  HBuf &operator=(const HBuf &) = delete;
-  ~HBuf() { if (p) cudaFreeHost(p); }
-  void ensure(size_t k) {
-    if (p && k <= n) return;
-    if (p) cudaFreeHost(p);
-    p = nullptr;
-    LVG_CUDA(cudaMallocHost(&p, (k ? k : 1) * sizeof(T)));
-    n = k;
-  }
-};
-
 struct HubPlanBuffers {
   DBuf<uint32_t> hub_vertex, hub_first, degs;
   DBuf<uint4> chunk;
@@ -178,10 +139,26 @@ struct lvg_graph {
   int device = 0;
   cudaStream_t stream = nullptr;
   Level base;
+  // Gapped CSR: row u holds deg[u] entries at off[u] with room for cap[u];
+  // rows that outgrow their room move to the overflow pool, entries
+  // [pool_begin, slots) of key/w. Unused entries hold (0, 0.0).
   DBuf<uint64_t> off;
-  DBuf<uint32_t> deg, key, bins;
+  DBuf<uint32_t> deg, cap, key, bins;
   DBuf<float> w;
   DBuf<uint8_t> ex;
+  size_t slots = 0, pool_begin = 0;
+  bool rows_sorted = true;  // every row sorted by neighbour id (batch apply needs it)
+  // batch apply: counters (UPD_*) and scratch
+  DBuf<unsigned long long> upd;
+  HBuf<unsigned long long> hupd;
+  HBuf<uint32_t> hcnt;
+  DBuf<UpdRow> u_rows;
+  DBuf<uint64_t> u_bound, u_spos, u_scan, u_k0, u_k1;
+  DBuf<uint32_t> u_skey, u_newdeg, u_pre, u_keep, u_pos, u_pscan, u_v0, u_v1, u_flag, u_touch, u_tpos, u_tscan;
+  DBuf<uint32_t> u_cnt;
+  DBuf<uint32_t> u_ds, u_dd, u_is, u_id;
+  DBuf<float> u_sw, u_dw, u_iw;
+  DBuf<uint8_t> u_tmp;
   HubPlanBuffers hubplan;  // chunked hub work of the uploaded level
   double total_weight = 0;
   std::unique_ptr<Workspace> ws;
@@ -204,17 +181,22 @@ struct lvg_graph {
   DBuf<float> b_dw, b_iw;
 };
 
+// A state or a device batch may outlive its graph (it keeps its own device
+// id for its destruction and never touches the graph there).
 struct lvg_state {
   lvg_graph *g = nullptr;
+  int device = 0;
   DBuf<uint32_t> q;
   DBuf<float> vt, ct;
 };
 
 struct lvg_device_batch {
   lvg_graph *g = nullptr;
+  int device = 0;
   DBuf<uint32_t> ds, dd, is, id, seg;
   DBuf<float> dw, iw;
   DBatch b;
+  bool applied = false;  // replaced by its tidied batch by a batch apply
 };
 
 namespace lvg {
@@ -832,6 +814,239 @@ int run_host(lvg_graph *g, int method, const lvg_batch *b, const uint32_t *q, co
   });
 }
 
+// Lay out a compact CSR already in HBM (coff[span+1], ckey/cw[X]) as the
+// graph's gapped CSR — room for row_capacity(deg) entries per row, then an
+// overflow pool for rows that outgrow their room under batch updates — and
+// compute its degree bins, hub plan and total weight. g->ex holds the present
+// flags when has_exists.
+void init_graph(lvg_graph *g, size_t span, size_t order, size_t X, const uint64_t *coff, const uint32_t *ckey,
+                const float *cw, bool has_exists) {
+  cudaStream_t s = g->stream;
+  g->off.ensure(span + 1);
+  g->deg.ensure(span + 1);
+  g->cap.ensure(span);
+  g->bins.ensure(span + 1);
+  g->upd.ensure(UPD_SLOTS);
+  g->hupd.ensure(UPD_SLOTS + 1);
+  {
+    DBuf<uint64_t> cap64, sc;
+    cap64.ensure(span);
+    sc.ensure(scan_scratch_elems(span));
+    launch_row_caps(coff, span, g->deg.p, g->cap.p, cap64.p, s);
+    exclusive_scan_u64(cap64.p, g->off.p, span, g->off.p + span, sc.p, s);
+    LVG_CUDA(cudaMemcpyAsync(g->hupd.p, g->off.p + span, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    LVG_CUDA(cudaStreamSynchronize(s));
+    const size_t rows_end = g->hupd.p[0];
+    g->pool_begin = rows_end;
+    g->slots = rows_end + rows_end / 8 + 65536;
+    g->key.ensure(g->slots);
+    g->w.ensure(g->slots);
+    LVG_CUDA(cudaMemsetAsync(g->key.p + rows_end, 0, (g->slots - rows_end) * 4, s));
+    LVG_CUDA(cudaMemsetAsync(g->w.p + rows_end, 0, (g->slots - rows_end) * 4, s));
+    launch_spread_rows(coff, ckey, cw, span, g->off.p, g->cap.p, g->key.p, g->w.p, s);
+    g->hupd.p[UPD_POOL] = rows_end;
+    for (int i = 1; i < UPD_SLOTS; ++i) g->hupd.p[i] = 0;
+    LVG_CUDA(cudaMemcpyAsync(g->upd.p, g->hupd.p, UPD_SLOTS * 8, cudaMemcpyHostToDevice, s));
+    LVG_CUDA(cudaStreamSynchronize(s));  // the scratch is freed next
+  }
+  g->ctr.ensure(1);
+  g->hctr.ensure(1);
+  LVG_CUDA(cudaMemsetAsync(g->ctr.p, 0, sizeof(Counters), s));
+  Level &b = g->base;
+  b.span = span; b.order = order; b.edges = X;
+  b.off = g->off.p; b.deg = g->deg.p; b.key = g->key.p; b.w = g->w.p; b.ex = has_exists ? g->ex.p : nullptr;
+  launch_total_weight(g->w.p, g->slots, g->ctr.p, s);
+  DBuf<uint32_t> scratch;
+  scratch.ensure(bin_scratch_elems(span + 1, DEFAULT_COLORS_ASYNC));
+  compute_bins(g, b, g->deg.p, g->bins.p, scratch.p, DEFAULT_COLORS_ASYNC);  // synchronises
+  build_hub_plan(g, b, g->hubplan);
+  read_counters(g);
+  g->total_weight = g->hctr.p->fp64[0];
+}
+
+// ---------------------------------------------------------------- batch apply
+
+// The batch plan, on the device: each list packed as (src << b | dst) keys,
+// stably sorted, the first of each run kept (tidyBatchUpdateU's sort +
+// unique, inc/batch.hxx:169-192, keeping the first in batch order where the
+// reference's unstable sort keeps an unspecified one) into g->u_ds.. /
+// g->u_is.., and one UpdRow per touched source vertex into g->u_rows.
+struct PlanCounts {
+  size_t nd = 0, ni = 0, nrows = 0, max_group = 0;
+};
+
+int id_bits(size_t span) {  // bits to hold ids 0..span-1
+  int b = 1;
+  while (b < 32 && ((span - 1) >> b)) ++b;
+  return b;
+}
+
+PlanCounts plan_device(lvg_graph *g, const uint32_t *ds, const uint32_t *dd, const float *dw, size_t nd,
+                       const uint32_t *is, const uint32_t *id, const float *iw, size_t ni) {
+  cudaStream_t s = g->stream;
+  const size_t S = g->base.span, n = std::max(nd, ni);
+  const int b = id_bits(S);
+  g->u_k0.ensure(n); g->u_k1.ensure(n); g->u_v0.ensure(n); g->u_v1.ensure(n);
+  g->u_flag.ensure(n + 1); g->u_pos.ensure(n + 1); g->u_pscan.ensure(scan_scratch_elems(n + 1));
+  g->u_ds.ensure(nd); g->u_dd.ensure(nd); g->u_dw.ensure(nd);
+  g->u_is.ensure(ni); g->u_id.ensure(ni); g->u_iw.ensure(ni);
+  g->u_cnt.ensure(4);
+  g->hcnt.ensure(4);
+  LVG_CUDA(cudaMemsetAsync(g->u_cnt.p, 0, 4 * sizeof(uint32_t), s));
+  LVG_CUDA(cudaMemsetAsync(g->upd.p + UPD_MAXG, 0, sizeof(uint64_t), s));
+  auto one = [&](const uint32_t *src, const uint32_t *dst, const float *w, size_t m, uint32_t *os, uint32_t *od,
+                 float *ow, uint32_t *count) {
+    if (!m) return;
+    launch_pack_keys(src, dst, m, b, g->u_k0.p, g->u_v0.p, s);
+    const bool alt = sort_pairs_u64(g->u_k0.p, g->u_k1.p, g->u_v0.p, g->u_v1.p, m, 2 * b, g->u_tmp, s);
+    const uint64_t *k = alt ? g->u_k1.p : g->u_k0.p;
+    const uint32_t *v = alt ? g->u_v1.p : g->u_v0.p;
+    launch_first_flags(k, m, g->u_flag.p, s);
+    exclusive_scan_u32(g->u_flag.p, g->u_pos.p, m, count, g->u_pscan.p, s);
+    launch_unpack_keys(k, v, g->u_flag.p, g->u_pos.p, m, b, w, os, od, ow, s);
+  };
+  one(ds, dd, dw, nd, g->u_ds.p, g->u_dd.p, g->u_dw.p, g->u_cnt.p + 0);
+  one(is, id, iw, ni, g->u_is.p, g->u_id.p, g->u_iw.p, g->u_cnt.p + 1);
+  g->u_touch.ensure(S + 1); g->u_tpos.ensure(S + 1); g->u_tscan.ensure(scan_scratch_elems(S + 1));
+  g->u_rows.ensure(std::min(S, nd + ni));
+  launch_plan_rows(g->u_ds.p, g->u_cnt.p + 0, g->u_is.p, g->u_cnt.p + 1, n, g->u_touch.p, g->u_tpos.p,
+                   g->u_tscan.p, S, g->u_rows.p, g->upd.p, g->u_cnt.p + 2, s);
+  LVG_CUDA(cudaMemcpyAsync(g->hcnt.p, g->u_cnt.p, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  LVG_CUDA(cudaMemcpyAsync(g->hupd.p + UPD_MAXG, g->upd.p + UPD_MAXG, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+  LVG_CUDA(cudaStreamSynchronize(s));
+  PlanCounts c;
+  c.nd = g->hcnt.p[0];
+  c.ni = g->hcnt.p[1];
+  c.nrows = g->hcnt.p[2];
+  c.max_group = g->hupd.p[UPD_MAXG];
+  return c;
+}
+
+// Copy every row into a fresh gapped layout whose pool has room for at least
+// `need` entries. Row order and contents are kept.
+void relayout(lvg_graph *g, size_t need) {
+  cudaStream_t s = g->stream;
+  const size_t S = g->base.span;
+  DBuf<uint64_t> cap64, noff, sc;
+  DBuf<uint32_t> ncap, nkey;
+  DBuf<float> nw;
+  cap64.ensure(S);
+  noff.ensure(S + 1);
+  sc.ensure(scan_scratch_elems(S));
+  ncap.ensure(S);
+  launch_fresh_caps(g->deg.p, S, ncap.p, cap64.p, s);
+  exclusive_scan_u64(cap64.p, noff.p, S, noff.p + S, sc.p, s);
+  LVG_CUDA(cudaMemcpyAsync(g->hupd.p, noff.p + S, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+  LVG_CUDA(cudaStreamSynchronize(s));
+  const size_t rows_end = g->hupd.p[0];
+  const size_t slots = rows_end + std::max(need, rows_end / 8) + 65536;
+  nkey.ensure(slots);
+  nw.ensure(slots);
+  LVG_CUDA(cudaMemsetAsync(nkey.p + rows_end, 0, (slots - rows_end) * sizeof(uint32_t), s));
+  LVG_CUDA(cudaMemsetAsync(nw.p + rows_end, 0, (slots - rows_end) * sizeof(float), s));
+  launch_relayout_rows(g->off.p, g->deg.p, g->key.p, g->w.p, S, noff.p, ncap.p, nkey.p, nw.p, s);
+  LVG_CUDA(cudaStreamSynchronize(s));
+  g->off.swap(noff);
+  g->cap.swap(ncap);
+  g->key.swap(nkey);
+  g->w.swap(nw);
+  g->base.off = g->off.p;
+  g->base.key = g->key.p;
+  g->base.w = g->w.p;
+  g->slots = slots;
+  g->pool_begin = rows_end;
+  g->hupd.p[UPD_POOL] = rows_end;
+  LVG_CUDA(cudaMemcpyAsync(g->upd.p + UPD_POOL, g->hupd.p + UPD_POOL, sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+}
+
+// Tidy and apply a planned batch (plan_device's lists and rows). The kept
+// flags of the tidied batch are left in g->u_keep (deletions, then
+// insertions).
+void apply_plan(lvg_graph *g, const PlanCounts &pc) {
+  const UpdRow *rows = g->u_rows.p;
+  const size_t nrows = pc.nrows, nd = pc.nd, ni = pc.ni;
+  const uint32_t *dd = g->u_dd.p, *id = g->u_id.p;
+  const float *iw = g->u_iw.p;
+  if (!nrows) return;
+  cudaStream_t s = g->stream;
+  Level &b = g->base;
+  g->u_bound.ensure(nrows);
+  g->u_spos.ensure(nrows + 1);
+  g->u_scan.ensure(scan_scratch_elems(nrows));
+  launch_row_bounds(g->deg.p, rows, nrows, g->u_bound.p, s);
+  exclusive_scan_u64(g->u_bound.p, g->u_spos.p, nrows, g->u_spos.p + nrows, g->u_scan.p, s);
+  LVG_CUDA(cudaMemcpyAsync(g->hupd.p, g->upd.p, UPD_SLOTS * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+  LVG_CUDA(cudaMemcpyAsync(g->hupd.p + UPD_SLOTS, g->u_spos.p + nrows, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+  LVG_CUDA(cudaStreamSynchronize(s));
+  const size_t T = g->hupd.p[UPD_SLOTS];
+  // worst case of what commit takes from the pool: every touched row moves
+  const size_t need = T + T / 8 + 4 * nrows;
+  if (g->slots - g->hupd.p[UPD_POOL] < need) relayout(g, need);
+  g->u_skey.ensure(T);
+  g->u_sw.ensure(T);
+  g->u_pre.ensure(nd + ni);
+  g->u_keep.ensure(nd + ni);
+  g->u_newdeg.ensure(nrows);
+  uint8_t *ex = b.ex ? g->ex.p : nullptr;
+  LVG_CUDA(cudaMemsetAsync(g->upd.p + UPD_EDGES, 0, (UPD_SLOTS - UPD_EDGES) * sizeof(uint64_t), s));
+  launch_merge_rows(g->off.p, g->deg.p, g->key.p, g->w.p, rows, nrows, dd, id, iw, nd, g->u_pre.p, g->u_keep.p,
+                    g->u_spos.p, g->u_skey.p, g->u_sw.p, g->u_newdeg.p, ex, g->upd.p, s);
+  launch_commit_rows(g->off.p, g->deg.p, g->cap.p, g->key.p, g->w.p, rows, nrows, g->u_spos.p, g->u_skey.p,
+                     g->u_sw.p, g->u_newdeg.p, g->upd.p, g->slots, s);
+  if (ex) launch_count_present(ex, b.span, g->upd.p, s);
+  launch_total_weight(g->w.p, g->slots, g->ctr.p, s);
+  LVG_CUDA(cudaMemcpyAsync(g->hupd.p, g->upd.p, UPD_SLOTS * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+  read_counters(g);  // synchronises
+  if (g->hupd.p[UPD_ERR]) throw Error(LVG_ECUDA, "batch apply: overflow pool exhausted (internal sizing error)");
+  b.edges = size_t((long long)b.edges + (long long)g->hupd.p[UPD_EDGES]);
+  if (ex) b.order = g->hupd.p[UPD_ORDER];
+  g->total_weight = g->hctr.p->fp64[0];
+  // degrees changed: new bins and hub plan; the captured iteration is stale
+  if (g->iter_exec) {
+    cudaGraphExecDestroy(g->iter_exec);
+    g->iter_exec = nullptr;
+  }
+  ensure_ws(g);
+  if (b.edges > g->ws->X) g->ws->allocate(b.span, b.edges, s);
+  compute_bins(g, b, g->deg.p, g->bins.p, g->ws->binscratch.p, b.colors);  // synchronises
+  build_hub_plan(g, b, g->hubplan);
+}
+
+// Plan, apply and compact the tidied batch into (tds.., tis..): what
+// main.cxx:108-109 does on the host, here in HBM. Returns the tidied counts
+// and the plan's longest insertion run.
+PlanCounts tidy_apply(lvg_graph *g, const uint32_t *ds, const uint32_t *dd, const float *dw, size_t nd,
+                      const uint32_t *is, const uint32_t *id, const float *iw, size_t ni, DBuf<uint32_t> &tds,
+                      DBuf<uint32_t> &tdd, DBuf<float> &tdw, DBuf<uint32_t> &tis, DBuf<uint32_t> &tid,
+                      DBuf<float> &tiw) {
+  if (!g->rows_sorted) throw Error(LVG_EINVAL, "batch apply needs rows sorted by neighbour id");
+  if (nd > 0x7FFFFFFFull || ni > 0x7FFFFFFFull) throw Error(LVG_EINVAL, "batch apply: more than 2^31-1 entries");
+  cudaStream_t s = g->stream;
+  PlanCounts pc = plan_device(g, ds, dd, dw, nd, is, id, iw, ni);
+  apply_plan(g, pc);
+  const size_t n = pc.nd + pc.ni;
+  tds.ensure(pc.nd); tdd.ensure(pc.nd); tdw.ensure(pc.nd);
+  tis.ensure(pc.ni); tid.ensure(pc.ni); tiw.ensure(pc.ni);
+  PlanCounts out;
+  out.max_group = pc.max_group;
+  if (n && pc.nrows) {
+    g->u_pos.ensure(n + 1);
+    g->u_pscan.ensure(scan_scratch_elems(n + 1));
+    exclusive_scan_u32(g->u_keep.p, g->u_pos.p, n, g->u_pos.p + n, g->u_pscan.p, s);
+    launch_tidy_compact(g->u_ds.p, g->u_dd.p, g->u_dw.p, pc.nd, g->u_keep.p, g->u_pos.p, nullptr, tds.p, tdd.p,
+                        tdw.p, s);
+    launch_tidy_compact(g->u_is.p, g->u_id.p, g->u_iw.p, pc.ni, g->u_keep.p + pc.nd, g->u_pos.p + pc.nd,
+                        g->u_pos.p + pc.nd, tis.p, tid.p, tiw.p, s);
+    g->hcnt.ensure(4);
+    LVG_CUDA(cudaMemcpyAsync(g->hcnt.p, g->u_pos.p + pc.nd, 4, cudaMemcpyDeviceToHost, s));
+    LVG_CUDA(cudaMemcpyAsync(g->hcnt.p + 1, g->u_pos.p + n, 4, cudaMemcpyDeviceToHost, s));
+    LVG_CUDA(cudaStreamSynchronize(s));
+    out.nd = g->hcnt.p[0];
+    out.ni = g->hcnt.p[1] - g->hcnt.p[0];
+  }
+  return out;
+}
+
 }  // namespace
 
 int fail_noalloc(int code, const char *msg) { return fail(code, msg); }
@@ -867,47 +1082,40 @@ int lvg_graph_create(size_t span, const uint64_t *offsets, const uint32_t *keys,
   size_t order = 0;
   for (size_t u = 0; u < span; ++u) {
     if (offsets[u + 1] < offsets[u]) return lvg::fail(LVG_EINVAL, "lvg_graph_create: offsets not monotone");
-    if (offsets[u + 1] - offsets[u] > 0xFFFFFFFFull) return lvg::fail(LVG_EINVAL, "lvg_graph_create: row too long");
+    if (offsets[u + 1] - offsets[u] > 0xE0000000ull) return lvg::fail(LVG_EINVAL, "lvg_graph_create: row too long");
     const bool has = !exists || exists[u];
     order += has;
     if (!has && offsets[u + 1] != offsets[u])
       return lvg::fail(LVG_EINVAL, "lvg_graph_create: absent vertex with edges");
   }
-  for (size_t i = 0; i < X; ++i)
-    if (keys[i] >= span) return lvg::fail(LVG_EINVAL, "lvg_graph_create: neighbour id >= span");
+  bool rows_sorted = true;
+  for (size_t u = 0; u < span; ++u)
+    for (uint64_t i = offsets[u]; i < offsets[u + 1]; ++i) {
+      if (keys[i] >= span) return lvg::fail(LVG_EINVAL, "lvg_graph_create: neighbour id >= span");
+      if (i > offsets[u] && keys[i] <= keys[i - 1]) rows_sorted = false;
+    }
   std::unique_ptr<lvg_graph> g(new lvg_graph());
   int rc = lvg::guarded([&] {
     LVG_CUDA(cudaGetDevice(&g->device));
     LVG_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
     cudaStream_t s = g->stream;
-    g->off.ensure(span + 1);
-    g->deg.ensure(span + 1);
-    g->key.ensure(X);
-    g->w.ensure(X);
-    g->bins.ensure(span + 1);
-    LVG_CUDA(cudaMemcpyAsync(g->off.p, offsets, (span + 1) * 8, cudaMemcpyHostToDevice, s));
+    g->rows_sorted = rows_sorted;
+    lvg::DBuf<uint64_t> coff;
+    lvg::DBuf<uint32_t> ckey;
+    lvg::DBuf<float> cw;
+    coff.ensure(span + 1);
+    ckey.ensure(X);
+    cw.ensure(X);
+    LVG_CUDA(cudaMemcpyAsync(coff.p, offsets, (span + 1) * 8, cudaMemcpyHostToDevice, s));
     if (X) {
-      LVG_CUDA(cudaMemcpyAsync(g->key.p, keys, X * 4, cudaMemcpyHostToDevice, s));
-      LVG_CUDA(cudaMemcpyAsync(g->w.p, weights, X * 4, cudaMemcpyHostToDevice, s));
+      LVG_CUDA(cudaMemcpyAsync(ckey.p, keys, X * 4, cudaMemcpyHostToDevice, s));
+      LVG_CUDA(cudaMemcpyAsync(cw.p, weights, X * 4, cudaMemcpyHostToDevice, s));
     }
     if (exists) {
       g->ex.ensure(span);
       LVG_CUDA(cudaMemcpyAsync(g->ex.p, exists, span, cudaMemcpyHostToDevice, s));
     }
-    g->ctr.ensure(1);
-    g->hctr.ensure(1);
-    LVG_CUDA(cudaMemsetAsync(g->ctr.p, 0, sizeof(Counters), s));
-    lvg::Level &b = g->base;
-    b.span = span; b.order = order; b.edges = X;
-    b.off = g->off.p; b.deg = g->deg.p; b.key = g->key.p; b.w = g->w.p; b.ex = exists ? g->ex.p : nullptr;
-    lvg::launch_degrees(b.off, g->deg.p, span, s);
-    lvg::launch_total_weight(b, g->ctr.p, s);
-    lvg::DBuf<uint32_t> scratch;
-    scratch.ensure(lvg::bin_scratch_elems(span + 1, lvg::DEFAULT_COLORS_ASYNC));
-    lvg::compute_bins(g.get(), b, g->deg.p, g->bins.p, scratch.p, lvg::DEFAULT_COLORS_ASYNC);  // synchronises
-    lvg::build_hub_plan(g.get(), b, g->hubplan);
-    lvg::read_counters(g.get());
-    g->total_weight = g->hctr.p->fp64[0];
+    lvg::init_graph(g.get(), span, order, X, coff.p, ckey.p, cw.p, exists != nullptr);
     return LVG_OK;
   });
   if (rc != LVG_OK) {
@@ -916,6 +1124,66 @@ int lvg_graph_create(size_t span, const uint64_t *offsets, const uint32_t *keys,
   }
   *out = g.release();
   return LVG_OK;
+}
+
+namespace lvg {
+namespace {
+int create_generated(const GenSpec &spec, lvg_graph **out) {
+  *out = nullptr;
+  std::unique_ptr<lvg_graph> g(new lvg_graph());
+  int rc = guarded([&] {
+    LVG_CUDA(cudaGetDevice(&g->device));
+    LVG_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+    DBuf<uint64_t> coff;
+    DBuf<uint32_t> ckey;
+    DBuf<float> cw;
+    const size_t X = generate_graph(spec, coff, ckey, cw, g->ex, g->stream);
+    g->rows_sorted = true;
+    init_graph(g.get(), spec.span, spec.span - 1, X, coff.p, ckey.p, cw.p, true);
+    return LVG_OK;
+  });
+  if (rc != LVG_OK) {
+    if (g->stream) cudaStreamDestroy(g->stream);
+    return rc;
+  }
+  *out = g.release();
+  return LVG_OK;
+}
+}  // namespace
+}  // namespace lvg
+
+int lvg_graph_create_planted_partition(uint32_t n, uint32_t block, double avg_degree, double p_in, uint64_t seed,
+                                       lvg_graph **out) {
+  if (!out || n == 0 || n >= 0xFFFFFFFFu || block == 0 || !(avg_degree >= 0) || !(p_in >= 0 && p_in <= 1))
+    return lvg::fail(LVG_EINVAL, "lvg_graph_create_planted_partition: bad argument");
+  lvg::GenSpec g;
+  g.kind = lvg::GenSpec::PP;
+  g.span = size_t(n) + 1;
+  g.draws = size_t(std::llround(double(n) * avg_degree / 2));
+  g.n = n;
+  g.block = block;
+  g.p_in = p_in;
+  g.seed = seed;
+  return lvg::create_generated(g, out);
+}
+
+int lvg_graph_create_rmat(int scale, double edge_factor, double a, double b, double c, int permute, uint64_t seed,
+                          lvg_graph **out) {
+  if (!out || scale < 1 || scale > 30 || !(edge_factor >= 0) || a < 0 || b < 0 || c < 0 || a + b + c > 1)
+    return lvg::fail(LVG_EINVAL, "lvg_graph_create_rmat: bad argument");
+  return lvg::guarded([&] {
+    lvg::GenSpec g;
+    g.kind = lvg::GenSpec::RMAT;
+    g.span = (size_t(1) << scale) + 1;
+    g.draws = size_t(std::llround(double(size_t(1) << scale) * edge_factor));
+    g.scale = scale;
+    g.a = a;
+    g.ab = a + b;
+    g.abc = a + b + c;
+    g.seed = seed;
+    if (permute) g.perm = lvg::rmat_permutation(scale, seed);
+    return lvg::create_generated(g, out);
+  });
 }
 
 int lvg_graph_destroy(lvg_graph *g) {
@@ -1120,6 +1388,7 @@ int lvg_state_create(lvg_graph *g, lvg_state **out) {
     LVG_CUDA(cudaSetDevice(g->device));
     const size_t S = g->base.span;
     st->g = g;
+    st->device = g->device;
     st->q.ensure(S); st->vt.ensure(S); st->ct.ensure(S);
     LVG_CUDA(cudaMemsetAsync(st->q.p, 0, S * 4, g->stream));
     LVG_CUDA(cudaMemsetAsync(st->vt.p, 0, S * 4, g->stream));
@@ -1170,9 +1439,8 @@ int lvg_state_get(const lvg_state *st, uint32_t *membership, double *vtot, doubl
 
 int lvg_state_destroy(lvg_state *st) {
   if (!st) return LVG_OK;
-  cudaSetDevice(st->g->device);
-  cudaStreamSynchronize(st->g->stream);
-  delete st;
+  cudaSetDevice(st->device);
+  delete st;  // cudaFree waits for the work that uses the buffers
   return LVG_OK;
 }
 
@@ -1184,6 +1452,7 @@ int lvg_device_batch_create(lvg_graph *g, const lvg_batch *b, lvg_device_batch *
     LVG_CUDA(cudaSetDevice(g->device));
     lvg::check_batch(g, b, false);
     db->g = g;
+    db->device = g->device;
     lvg::upload_batch(g, b, db->ds, db->dd, db->dw, db->is, db->id, db->iw, db->seg, db->b);
     LVG_CUDA(cudaStreamSynchronize(g->stream));
     // remember whether the insertions are source-sorted (delta-screening needs it)
@@ -1196,11 +1465,163 @@ int lvg_device_batch_create(lvg_graph *g, const lvg_batch *b, lvg_device_batch *
   return rc;
 }
 
+int lvg_graph_apply_batch(lvg_graph *g, const lvg_batch *b, lvg_batch_buf *tidy) {
+  if (!g) return lvg::fail(LVG_EINVAL, "null graph");
+  if (tidy && b &&
+      ((b->num_deletions && (!tidy->del_src || !tidy->del_dst || !tidy->del_w)) ||
+       (b->num_insertions && (!tidy->ins_src || !tidy->ins_dst || !tidy->ins_w))))
+    return lvg::fail(LVG_EINVAL, "lvg_graph_apply_batch: null tidy-batch array");
+  return lvg::guarded([&] {
+    LVG_CUDA(cudaSetDevice(g->device));
+    lvg::check_batch(g, b, false);
+    if (tidy) tidy->num_deletions = tidy->num_insertions = 0;
+    if (!b || !(b->num_deletions + b->num_insertions)) return LVG_OK;
+    cudaStream_t s = g->stream;
+    lvg::DBatch raw;
+    lvg::upload_batch(g, b, g->b_ds, g->b_dd, g->b_dw, g->b_is, g->b_id, g->b_iw, g->b_seg, raw);
+    lvg::DBuf<uint32_t> tds, tdd, tis, tid;
+    lvg::DBuf<float> tdw, tiw;
+    const lvg::PlanCounts t = lvg::tidy_apply(g, raw.ds, raw.dd, raw.dw, raw.nd, raw.is, raw.id, raw.iw, raw.ni,
+                                              tds, tdd, tdw, tis, tid, tiw);
+    if (tidy) {
+      if (t.nd) {
+        LVG_CUDA(cudaMemcpyAsync(tidy->del_src, tds.p, t.nd * 4, cudaMemcpyDeviceToHost, s));
+        LVG_CUDA(cudaMemcpyAsync(tidy->del_dst, tdd.p, t.nd * 4, cudaMemcpyDeviceToHost, s));
+        LVG_CUDA(cudaMemcpyAsync(tidy->del_w, tdw.p, t.nd * 4, cudaMemcpyDeviceToHost, s));
+      }
+      if (t.ni) {
+        LVG_CUDA(cudaMemcpyAsync(tidy->ins_src, tis.p, t.ni * 4, cudaMemcpyDeviceToHost, s));
+        LVG_CUDA(cudaMemcpyAsync(tidy->ins_dst, tid.p, t.ni * 4, cudaMemcpyDeviceToHost, s));
+        LVG_CUDA(cudaMemcpyAsync(tidy->ins_w, tiw.p, t.ni * 4, cudaMemcpyDeviceToHost, s));
+      }
+      LVG_CUDA(cudaStreamSynchronize(s));
+      tidy->num_deletions = t.nd;
+      tidy->num_insertions = t.ni;
+    }
+    LVG_CUDA(cudaStreamSynchronize(s));  // the tidied copies are freed next
+    return LVG_OK;
+  });
+}
+
+int lvg_graph_apply_device_batch(lvg_graph *g, lvg_device_batch *b) {
+  if (!g || !b) return lvg::fail(LVG_EINVAL, "null argument");
+  if (b->g != g) return lvg::fail(LVG_EINVAL, "the batch was created on another graph");
+  if (b->applied) return lvg::fail(LVG_EINVAL, "the batch has already been applied");
+  return lvg::guarded([&] {
+    LVG_CUDA(cudaSetDevice(g->device));
+    cudaStream_t s = g->stream;
+    // the batch becomes the tidied batch (tidyBatchUpdateU's result), which
+    // the dynamic methods then take, as main.cxx:108-125 does
+    const lvg::DBatch &r = b->b;
+    if (!(r.nd + r.ni)) {
+      b->applied = true;
+      return LVG_OK;
+    }
+    lvg::DBuf<uint32_t> tds, tdd, tis, tid;
+    lvg::DBuf<float> tdw, tiw;
+    const lvg::PlanCounts t = lvg::tidy_apply(g, r.ds, r.dd, r.dw, r.nd, r.is, r.id, r.iw, r.ni, tds, tdd, tdw,
+                                              tis, tid, tiw);
+    LVG_CUDA(cudaStreamSynchronize(s));
+    b->ds.swap(tds); b->dd.swap(tdd); b->dw.swap(tdw);
+    b->is.swap(tis); b->id.swap(tid); b->iw.swap(tiw);
+    b->seg.ensure(t.ni + 1);
+    b->b.ds = b->ds.p; b->b.dd = b->dd.p; b->b.dw = b->dw.p;
+    b->b.is = b->is.p; b->b.id = b->id.p; b->b.iw = b->iw.p; b->b.seg = b->seg.p;
+    b->b.nd = t.nd;
+    b->b.ni = t.ni;
+    b->b.max_group = t.max_group;  // an upper bound after the filter
+    b->applied = true;
+    return LVG_OK;
+  });
+}
+
+int lvg_graph_download(lvg_graph *g, uint64_t *offsets, uint32_t *keys, float *weights, uint8_t *exists) {
+  if (!g || !offsets) return lvg::fail(LVG_EINVAL, "null argument");
+  return lvg::guarded([&] {
+    LVG_CUDA(cudaSetDevice(g->device));
+    cudaStream_t s = g->stream;
+    const size_t S = g->base.span;
+    std::vector<uint64_t> off(S);
+    std::vector<uint32_t> deg(S), key(g->slots);
+    std::vector<float> w(g->slots);
+    LVG_CUDA(cudaMemcpyAsync(off.data(), g->off.p, S * 8, cudaMemcpyDeviceToHost, s));
+    LVG_CUDA(cudaMemcpyAsync(deg.data(), g->deg.p, S * 4, cudaMemcpyDeviceToHost, s));
+    if (keys) LVG_CUDA(cudaMemcpyAsync(key.data(), g->key.p, g->slots * 4, cudaMemcpyDeviceToHost, s));
+    if (weights) LVG_CUDA(cudaMemcpyAsync(w.data(), g->w.p, g->slots * 4, cudaMemcpyDeviceToHost, s));
+    if (exists) {
+      if (g->base.ex) LVG_CUDA(cudaMemcpyAsync(exists, g->ex.p, S, cudaMemcpyDeviceToHost, s));
+      else std::memset(exists, 1, S);
+    }
+    LVG_CUDA(cudaStreamSynchronize(s));
+    offsets[0] = 0;
+    for (size_t u = 0; u < S; ++u) {
+      const uint64_t o = offsets[u];
+      if (keys) std::memcpy(keys + o, key.data() + off[u], deg[u] * 4);
+      if (weights) std::memcpy(weights + o, w.data() + off[u], deg[u] * 4);
+      offsets[u + 1] = o + deg[u];
+    }
+    return LVG_OK;
+  });
+}
+
+int lvg_device_batch_generate(lvg_graph *g, size_t deletions, size_t insertions, uint32_t begin, uint32_t range,
+                              float weight, uint64_t seed, lvg_device_batch **out) {
+  if (!g || !out) return lvg::fail(LVG_EINVAL, "null argument");
+  *out = nullptr;
+  if (range == 0 || size_t(begin) + range > g->base.span)
+    return lvg::fail(LVG_EINVAL, "lvg_device_batch_generate: [begin, begin+range) outside the span");
+  std::unique_ptr<lvg_device_batch> db(new lvg_device_batch());
+  int rc = lvg::guarded([&] {
+    LVG_CUDA(cudaSetDevice(g->device));
+    db->g = g;
+    db->device = g->device;
+    size_t nd = 0, ni = 0;
+    lvg::generate_batch(g->off.p, g->deg.p, g->key.p, g->w.p, deletions, insertions, begin, range, weight, seed,
+                        db->ds, db->dd, db->dw, db->is, db->id, db->iw, nd, ni, g->stream);
+    db->seg.ensure(ni + 1);
+    lvg::DBatch &d = db->b;
+    d = lvg::DBatch{};
+    d.ds = db->ds.p; d.dd = db->dd.p; d.dw = db->dw.p;
+    d.is = db->is.p; d.id = db->id.p; d.iw = db->iw.p; d.seg = db->seg.p;
+    d.nd = nd;
+    d.ni = ni;
+    d.max_group = ~size_t(0);  // not sorted by source until applied
+    return LVG_OK;
+  });
+  if (rc == LVG_OK) *out = db.release();
+  return rc;
+}
+
+int lvg_device_batch_download(const lvg_device_batch *b, lvg_batch_buf *out) {
+  if (!b || !out) return lvg::fail(LVG_EINVAL, "null argument");
+  return lvg::guarded([&] {
+    LVG_CUDA(cudaSetDevice(b->device));
+    const lvg::DBatch &d = b->b;
+    cudaStream_t s = b->g->stream;
+    auto get = [&](void *dst, const void *src, size_t bytes) {
+      if (bytes && !dst) throw lvg::Error(LVG_EINVAL, "lvg_device_batch_download: null array");
+      if (bytes) LVG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s));
+    };
+    get(out->del_src, d.ds, d.nd * 4); get(out->del_dst, d.dd, d.nd * 4); get(out->del_w, d.dw, d.nd * 4);
+    get(out->ins_src, d.is, d.ni * 4); get(out->ins_dst, d.id, d.ni * 4); get(out->ins_w, d.iw, d.ni * 4);
+    LVG_CUDA(cudaStreamSynchronize(s));
+    out->num_deletions = d.nd;
+    out->num_insertions = d.ni;
+    return LVG_OK;
+  });
+}
+
+int lvg_device_batch_size(const lvg_device_batch *b, size_t *deletions, size_t *insertions) {
+  if (!b) return lvg::fail(LVG_EINVAL, "null argument");
+  if (deletions) *deletions = b->b.nd;
+  if (insertions) *insertions = b->b.ni;
+  return LVG_OK;
+}
+
 int lvg_device_batch_destroy(lvg_device_batch *b) {
   if (!b) return LVG_OK;
-  cudaSetDevice(b->g->device);
-  cudaStreamSynchronize(b->g->stream);
-  delete b;
+  cudaSetDevice(b->device);
+  delete b;  // cudaFree waits for the work that uses the buffers
   return LVG_OK;
 }
 

@@ -287,6 +287,52 @@ int lvgg_random_batch(const lvgg_csr *x, size_t num_updates, double insertion_fr
   return 0;
 }
 
+int lvgg_reference_batch(const lvgg_csr *x, size_t deletions, size_t insertions, uint32_t begin, uint32_t range,
+                         float weight, uint64_t seed, lvgg_batch *out) {
+  if (!x || !out || range == 0 || size_t(begin) + range > x->span)
+    return fail(-EINVAL, "lvgg_reference_batch: bad argument");
+  std::memset(out, 0, sizeof(*out));
+  try {
+    std::vector<uint32_t> ds, dd;
+    std::vector<float> dw;
+    for (size_t l = 0; l < deletions; ++l) {
+      Rng r(seed, 5, l);
+      for (int t = 0; t < 5; ++t) {
+        const uint32_t u = begin + uint32_t(double(range) * r.uniform());
+        const uint64_t d = x->offsets[u + 1] - x->offsets[u];
+        if (d == 0) continue;
+        const uint64_t j = x->offsets[u] + uint64_t(uint32_t(r.uniform() * double(d)));
+        const uint32_t v = x->keys[j];
+        ds.push_back(u); dd.push_back(v); dw.push_back(x->weights[j]);
+        ds.push_back(v); dd.push_back(u); dw.push_back(x->weights[j]);
+        break;
+      }
+    }
+    out->num_deletions = ds.size();
+    out->del_src = xalloc<uint32_t>(ds.size());
+    out->del_dst = xalloc<uint32_t>(ds.size());
+    out->del_w = xalloc<float>(ds.size());
+    std::copy(ds.begin(), ds.end(), out->del_src);
+    std::copy(dd.begin(), dd.end(), out->del_dst);
+    std::copy(dw.begin(), dw.end(), out->del_w);
+    out->num_insertions = 2 * insertions;
+    out->ins_src = xalloc<uint32_t>(2 * insertions);
+    out->ins_dst = xalloc<uint32_t>(2 * insertions);
+    out->ins_w = xalloc<float>(2 * insertions);
+    for (size_t l = 0; l < insertions; ++l) {
+      Rng r(seed, 6, l);
+      const uint32_t u = begin + uint32_t(double(range) * r.uniform());
+      const uint32_t v = begin + uint32_t(double(range) * r.uniform());
+      out->ins_src[2 * l] = u; out->ins_dst[2 * l] = v; out->ins_w[2 * l] = weight;
+      out->ins_src[2 * l + 1] = v; out->ins_dst[2 * l + 1] = u; out->ins_w[2 * l + 1] = weight;
+    }
+  } catch (const std::bad_alloc &) {
+    lvgg_batch_free(out);
+    return fail(-ENOMEM, "lvgg_reference_batch: out of memory");
+  }
+  return 0;
+}
+
 int lvgg_apply_batch(const lvgg_csr *x, const lvgg_batch *b, lvgg_csr *y) {
   if (!x || !b || !y) return fail(-EINVAL, "lvgg_apply_batch: bad argument");
   std::memset(y, 0, sizeof(*y));

@@ -1,9 +1,57 @@
 // lvg_internal.cuh — device data layout and kernel launchers shared by the
 // translation units of liblouvain_gb300.so.
 #pragma once
+#include <utility>
+#include <vector>
+
 #include "lvg_common.cuh"
 
 namespace lvg {
+
+// Device buffer that grows on demand (contents are not kept when it grows).
+template <class T>
+struct DBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  ~DBuf() { release(); }
+  void ensure(size_t k) {
+    if (p && k <= n) return;
+    release();
+    if (k == 0) k = 1;
+    LVG_CUDA(cudaMalloc(&p, k * sizeof(T)));
+    n = k;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void swap(DBuf &o) {
+    std::swap(p, o.p);
+    std::swap(n, o.n);
+  }
+};
+
+template <class T>
+struct HBuf {  // pinned host buffer, grows on demand
+  T *p = nullptr;
+  size_t n = 0;
+  HBuf() = default;
+  HBuf(const HBuf &) = delete;
+  HBuf &operator=(const HBuf &) = delete;
+  ~HBuf() { if (p) cudaFreeHost(p); }
+  void ensure(size_t k) {
+    if (p && k <= n) return;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    LVG_CUDA(cudaMallocHost(&p, (k ? k : 1) * sizeof(T)));
+    n = k;
+  }
+};
+
 
 // Work plan of the chunked path for the largest vertices (degree bin 11) of a
 // level: each hub's edge list is cut into chunks of HUB_CHUNK edges that
@@ -138,7 +186,7 @@ int grid_for(size_t n, int block, int max_blocks_per_sm = 8);
 void launch_degrees(const uint64_t *off, uint32_t *deg, size_t span, cudaStream_t s);
 void launch_fill_u8(uint8_t *p, uint8_t v, size_t n, cudaStream_t s);
 void launch_init_static(const Level &g, uint32_t *ucom, float *utot, float *ctot, cudaStream_t s);
-void launch_total_weight(const Level &g, Counters *ctr, cudaStream_t s);  // -> ctr->fp64[0]
+void launch_total_weight(const float *w, size_t n, Counters *ctr, cudaStream_t s);  // -> ctr->fp64[0]
 void launch_prior_to_f32(const double *src, float *dst, size_t n, cudaStream_t s);
 void launch_f32_to_f64(const float *src, double *dst, size_t n, cudaStream_t s);
 void launch_batch_weights(const uint32_t *src, const float *w, size_t n, float sign, const uint32_t *vcom,
@@ -186,6 +234,75 @@ void launch_aggregate_bin(int b, const AggArgs &a, cudaStream_t s);
 // Record a failure message for lvg_last_error() and return `code` (for entry
 // points outside lvg_api.cu).
 int fail_noalloc(int code, const char *msg);
+
+// ---------------------------------------------------------------- batch apply (lvg_update.cu)
+// A row touched by a batch: its vertex and its ranges in the (source,
+// target)-sorted, duplicate-free deletion and insertion lists.
+struct UpdRow {
+  uint32_t u, d0, d1, i0, i1;
+};
+// Row capacity of the gapped layout for a row of degree d.
+__host__ __device__ inline uint32_t row_capacity(uint32_t d) { return d + (d >> 3) + 4; }
+// Slots of the batch-apply counters.
+constexpr int UPD_POOL = 0;   // overflow-pool cursor (absolute entry index)
+constexpr int UPD_EDGES = 1;  // change of the edge count (two's complement)
+constexpr int UPD_ERR = 2;    // 1: the overflow pool ran out
+constexpr int UPD_ORDER = 3;  // present vertices after the batch
+constexpr int UPD_MAXG = 4;   // longest run of insertions sharing a source
+constexpr int UPD_SLOTS = 5;
+void launch_row_caps(const uint64_t *coff, size_t n, uint32_t *deg, uint32_t *cap, uint64_t *cap64, cudaStream_t s);
+void launch_spread_rows(const uint64_t *coff, const uint32_t *ckey, const float *cw, size_t n, const uint64_t *off,
+                        const uint32_t *cap, uint32_t *key, float *w, cudaStream_t s);
+void launch_row_bounds(const uint32_t *deg, const UpdRow *rows, size_t nrows, uint64_t *bound, cudaStream_t s);
+void launch_merge_rows(const uint64_t *off, const uint32_t *deg, const uint32_t *key, const float *w,
+                       const UpdRow *rows, size_t nrows, const uint32_t *dd, const uint32_t *id, const float *iw,
+                       size_t nd_all, uint32_t *pre, uint32_t *keep, const uint64_t *spos, uint32_t *skey,
+                       float *sw, uint32_t *newdeg, uint8_t *ex, unsigned long long *upd, cudaStream_t s);
+void launch_commit_rows(uint64_t *off, uint32_t *deg, uint32_t *cap, uint32_t *key, float *w, const UpdRow *rows,
+                        size_t nrows, const uint64_t *spos, const uint32_t *skey, const float *sw,
+                        const uint32_t *newdeg, unsigned long long *upd, unsigned long long pool_end, cudaStream_t s);
+void launch_count_present(const uint8_t *ex, size_t span, unsigned long long *upd, cudaStream_t s);
+void launch_tidy_compact(const uint32_t *src, const uint32_t *dst, const float *w, size_t n, const uint32_t *keep,
+                         const uint32_t *pos, const uint32_t *pos_base, uint32_t *osrc, uint32_t *odst, float *ow,
+                         cudaStream_t s);
+void launch_fresh_caps(const uint32_t *deg, size_t n, uint32_t *cap, uint64_t *cap64, cudaStream_t s);
+// The device-side plan of a batch: packed keys, stable sort, first of each
+// run, rows of the touched vertices.
+void launch_pack_keys(const uint32_t *src, const uint32_t *dst, size_t n, int b, uint64_t *key, uint32_t *val,
+                      cudaStream_t s);
+void launch_first_flags(const uint64_t *key, size_t n, uint32_t *flag, cudaStream_t s);
+void launch_unpack_keys(const uint64_t *key, const uint32_t *val, const uint32_t *flag, const uint32_t *pos,
+                        size_t n, int b, const float *w, uint32_t *os, uint32_t *od, float *ow, cudaStream_t s);
+void launch_plan_rows(const uint32_t *ds, const uint32_t *nd, const uint32_t *is, const uint32_t *ni, size_t cap,
+                      uint32_t *touched, uint32_t *tpos, uint32_t *scan, size_t span, UpdRow *rows,
+                      unsigned long long *upd, uint32_t *nrows, cudaStream_t s);
+
+// ---------------------------------------------------------------- generators (lvg_gen.cu)
+// Stable radix sorts of 64-bit keys over bits [0, end_bit) (cub); the result
+// is in the second buffers when they return true.
+bool sort_keys_u64(uint64_t *k0, uint64_t *k1, size_t n, int end_bit, DBuf<uint8_t> &tmp, cudaStream_t s);
+bool sort_pairs_u64(uint64_t *k0, uint64_t *k1, uint32_t *v0, uint32_t *v1, size_t n, int end_bit,
+                    DBuf<uint8_t> &tmp, cudaStream_t s);
+// A synthetic graph: planted partition or R-MAT, as the host generators draw them.
+struct GenSpec {
+  enum Kind { PP, RMAT } kind = PP;
+  size_t span = 0, draws = 0;
+  uint32_t n = 0, block = 1;
+  double p_in = 0;
+  int scale = 0;
+  double a = 0, ab = 0, abc = 0;
+  std::vector<uint32_t> perm;  // R-MAT vertex permutation (empty: none)
+  uint64_t seed = 0;
+};
+std::vector<uint32_t> rmat_permutation(int scale, uint64_t seed);
+size_t generate_graph(const GenSpec &g, DBuf<uint64_t> &coff, DBuf<uint32_t> &ckey, DBuf<float> &cw,
+                      DBuf<uint8_t> &ex, cudaStream_t s);
+void generate_batch(const uint64_t *off, const uint32_t *deg, const uint32_t *key, const float *w, size_t nd,
+                    size_t ni, uint32_t begin, uint32_t range, float weight, uint64_t seed, DBuf<uint32_t> &ds,
+                    DBuf<uint32_t> &dd, DBuf<float> &dw, DBuf<uint32_t> &is, DBuf<uint32_t> &id,
+                    DBuf<float> &iw, size_t &out_nd, size_t &out_ni, cudaStream_t s);
+void launch_relayout_rows(const uint64_t *old_off, const uint32_t *deg, const uint32_t *old_key, const float *old_w,
+                          size_t n, const uint64_t *off, const uint32_t *cap, uint32_t *key, float *w, cudaStream_t s);
 
 // Chunked path of the largest vertices: per colour, one kernel aggregates
 // the chunks, a second merges each hub's chunks and moves it.

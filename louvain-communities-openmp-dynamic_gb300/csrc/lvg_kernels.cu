@@ -5,14 +5,14 @@
 namespace lvg {
 namespace {
 
-int g_sms = 0;
-int sms() {
-  if (!g_sms) {
-    int dev = 0;
+int sms() {  // SM count of the device, queried once (thread-safe static init)
+  static const int n = [] {
+    int dev = 0, c = 0;
     LVG_CUDA(cudaGetDevice(&dev));
-    LVG_CUDA(cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev));
-  }
-  return g_sms;
+    LVG_CUDA(cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev));
+    return c;
+  }();
+  return n;
 }
 
 #define GRID_STRIDE(i, n) for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < (n); i += size_t(gridDim.x) * blockDim.x)
@@ -449,10 +449,10 @@ void launch_init_static(const Level &g, uint32_t *ucom, float *utot, float *ctot
   LVG_CHECK_LAUNCH();
 }
 
-void launch_total_weight(const Level &g, Counters *ctr, cudaStream_t s) {
+void launch_total_weight(const float *w, size_t n, Counters *ctr, cudaStream_t s) {
   LVG_CUDA(cudaMemsetAsync(&ctr->fp64[0], 0, sizeof(double), s));
-  if (!g.edges) return;
-  total_weight_kernel<<<grid_for(g.edges, 256), 256, 0, s>>>(g.w, g.edges, &ctr->fp64[0]);
+  if (!n) return;
+  total_weight_kernel<<<grid_for(n, 256), 256, 0, s>>>(w, n, &ctr->fp64[0]);
   LVG_CHECK_LAUNCH();
 }
 

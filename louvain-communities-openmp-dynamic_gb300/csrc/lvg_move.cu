@@ -706,14 +706,14 @@ __global__ void __launch_bounds__(B) hub_merge_kernel(MoveArgs a) {
   flush_counters(a.ctr, a.bin, fix, nv, ne, nm, bad);
 }
 
-int g_num_sms = 0;
-int num_sms() {
-  if (!g_num_sms) {
-    int dev = 0;
+int num_sms() {  // SM count of the device, queried once (thread-safe static init)
+  static const int n = [] {
+    int dev = 0, c = 0;
     LVG_CUDA(cudaGetDevice(&dev));
-    LVG_CUDA(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
-  }
-  return g_num_sms;
+    LVG_CUDA(cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev));
+    return c;
+  }();
+  return n;
 }
 
 template <class K>

@@ -1,0 +1,332 @@
+// lvg_server.cu — a serving loop over many graphs resident in HBM.
+//
+// The reference processes one graph and one batch at a time on the host
+// (main.cxx:101-135: tidy + apply the batch, then each dynamic method). A
+// server keeps many graphs and their community state in HBM and answers a
+// stream of batch updates: each request is a host batch for one graph; a
+// worker uploads it, tidies and applies it to the graph in HBM, and runs the
+// configured dynamic method from the graph's current state, which the result
+// replaces. Requests for one graph run in arrival order, one at a time;
+// requests for different graphs run concurrently on the graphs' own streams
+// (one host worker thread per request in flight). Admission control keeps
+// the estimated device footprint of the resident graphs under a budget.
+//
+// Host code only: it calls the library's own C-ABI.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "lvg_internal.cuh"
+
+namespace {
+
+double now_ms() {
+  using namespace std::chrono;
+  return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+struct Request {
+  uint64_t ticket = 0;
+  int graph = 0;
+  std::vector<uint32_t> ds, dd, is, id;
+  std::vector<float> dw, iw;
+  double t_submit = 0;
+};
+
+struct Slot {
+  lvg_graph *g = nullptr;
+  lvg_state *st = nullptr;
+  bool owns_graph = false;
+  std::deque<Request> q;
+  bool busy = false;
+  size_t bytes = 0;
+  uint64_t served = 0;
+};
+
+}  // namespace
+
+struct lvg_server {
+  lvg_server_options opt{};
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::vector<std::unique_ptr<Slot>> slots;
+  std::unordered_map<uint64_t, lvg_request_info> done;
+  std::vector<std::thread> workers;
+  bool stop = false;
+  uint64_t next_ticket = 1;
+  size_t bytes_used = 0, rr = 0, pending = 0;
+  int device = 0;
+  // statistics since the last reset
+  std::vector<double> lat;
+  uint64_t completed = 0, updates = 0, failed = 0;
+  double t_first = 0, t_last = 0;
+};
+
+namespace {
+
+// The next graph with work and no request in flight (round robin), or -1.
+int pick(lvg_server *sv) {
+  const size_t n = sv->slots.size();
+  for (size_t k = 0; k < n; ++k) {
+    const size_t i = (sv->rr + k) % n;
+    Slot &s = *sv->slots[i];
+    if (!s.busy && !s.q.empty()) {
+      sv->rr = i + 1;
+      return int(i);
+    }
+  }
+  return -1;
+}
+
+void serve(lvg_server *sv, Slot &s, const Request &r, lvg_request_info &info) {
+  const double t0 = now_ms();
+  info.queue_ms = t0 - r.t_submit;
+  lvg_batch b{r.ds.size(), r.ds.data(), r.dd.data(), r.dw.data(), r.is.size(), r.is.data(), r.id.data(),
+              r.iw.data()};
+  lvg_device_batch *db = nullptr;
+  int rc = lvg_device_batch_create(s.g, &b, &db);
+  if (rc == LVG_OK) rc = lvg_graph_apply_device_batch(s.g, db);
+  const double t1 = now_ms();
+  info.apply_ms = t1 - t0;
+  if (rc == LVG_OK) {
+    size_t nd = 0, ni = 0;
+    lvg_device_batch_size(db, &nd, &ni);
+    info.tidy_deletions = nd;
+    info.tidy_insertions = ni;
+    lvg_result res{};
+    rc = lvg_run_resident(s.g, sv->opt.method, db, s.st, s.st, &sv->opt.louvain, &res);
+    info.iterations = res.iterations;
+    info.passes = res.passes;
+    info.affected = res.affectedVertices;
+  }
+  if (db) lvg_device_batch_destroy(db);
+  info.run_ms = now_ms() - t1;
+  info.status = rc;
+}
+
+void worker(lvg_server *sv) {
+  cudaSetDevice(sv->device);
+  std::unique_lock<std::mutex> lk(sv->mu);
+  for (;;) {
+    int i = -1;
+    sv->cv_work.wait(lk, [&] { return sv->stop || (i = pick(sv)) >= 0; });
+    if (i < 0) return;  // stopping and nothing runnable
+    Slot &s = *sv->slots[size_t(i)];
+    Request r = std::move(s.q.front());
+    s.q.pop_front();
+    s.busy = true;
+    lk.unlock();
+    lvg_request_info info{};
+    info.ticket = r.ticket;
+    info.graph = r.graph;
+    serve(sv, s, r, info);
+    const double t = now_ms();
+    info.latency_ms = t - r.t_submit;
+    lk.lock();
+    s.busy = false;
+    ++s.served;
+    --sv->pending;
+    if (info.status == LVG_OK) {
+      ++sv->completed;
+      sv->updates += r.ds.size() + r.is.size();
+      sv->lat.push_back(info.latency_ms);
+    } else {
+      ++sv->failed;
+    }
+    if (sv->t_first == 0 || r.t_submit < sv->t_first) sv->t_first = r.t_submit;
+    sv->t_last = std::max(sv->t_last, t);
+    sv->done[r.ticket] = info;
+    sv->cv_done.notify_all();
+    sv->cv_work.notify_all();
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+void lvg_server_options_default(lvg_server_options *o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->workers = 8;
+  o->hbm_budget = size_t(120) << 30;
+  o->method = LVG_METHOD_FRONTIER;
+  lvg_options_default(&o->louvain);
+}
+
+size_t lvg_graph_footprint(size_t span, size_t edges) {
+  // gapped rows + pool (~1.3 x 8 B per edge), two aggregation levels (2 x 8 B
+  // per edge), per-vertex arrays of the graph, workspace and one state
+  return edges * 27 + span * 200 + (size_t(4) << 20);
+}
+
+int lvg_server_create(const lvg_server_options *o, lvg_server **out) {
+  if (!out) return lvg::fail_noalloc(LVG_EINVAL, "null argument");
+  *out = nullptr;
+  std::unique_ptr<lvg_server> sv(new lvg_server());
+  if (o) sv->opt = *o; else lvg_server_options_default(&sv->opt);
+  if (sv->opt.workers < 1 || sv->opt.workers > 256 || sv->opt.method < LVG_METHOD_NAIVE ||
+      sv->opt.method > LVG_METHOD_FRONTIER)
+    return lvg::fail_noalloc(LVG_EINVAL, "lvg_server_create: bad options");
+  if (cudaGetDevice(&sv->device) != cudaSuccess) return lvg::fail_noalloc(LVG_ECUDA, "no CUDA device");
+  for (int i = 0; i < sv->opt.workers; ++i) sv->workers.emplace_back(worker, sv.get());
+  *out = sv.release();
+  return LVG_OK;
+}
+
+int lvg_server_add_graph(lvg_server *sv, lvg_graph *g, int take_ownership, const uint32_t *q, const double *qvtot,
+                         const double *qctot, int *graph_id) {
+  if (!sv || !g || !graph_id) return lvg::fail_noalloc(LVG_EINVAL, "null argument");
+  const size_t bytes = lvg_graph_footprint(lvg_graph_span(g), lvg_graph_size(g));
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    if (sv->bytes_used + bytes > sv->opt.hbm_budget)
+      return lvg::fail_noalloc(LVG_ENOMEM, "lvg_server_add_graph: the HBM budget is used up (admission denied)");
+    sv->bytes_used += bytes;  // reserved; released below on failure
+  }
+  auto release = [&](int rc) {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    sv->bytes_used -= bytes;
+    return rc;
+  };
+  lvg_state *st = nullptr;
+  int rc = lvg_state_create(g, &st);
+  if (rc != LVG_OK) return release(rc);
+  if (q) {
+    if (!qvtot || !qctot) {
+      lvg_state_destroy(st);
+      return release(lvg::fail_noalloc(LVG_EINVAL, "lvg_server_add_graph: q without weights"));
+    }
+    rc = lvg_state_set(st, q, qvtot, qctot);
+  } else {  // no prior: the static communities
+    lvg_result res{};
+    rc = lvg_run_resident(g, LVG_METHOD_STATIC, nullptr, nullptr, st, &sv->opt.louvain, &res);
+  }
+  if (rc != LVG_OK) {
+    lvg_state_destroy(st);
+    return release(rc);
+  }
+  std::lock_guard<std::mutex> lk(sv->mu);
+  std::unique_ptr<Slot> s(new Slot());
+  s->g = g;
+  s->st = st;
+  s->owns_graph = take_ownership != 0;
+  s->bytes = bytes;
+  sv->slots.push_back(std::move(s));
+  *graph_id = int(sv->slots.size() - 1);
+  return LVG_OK;
+}
+
+int lvg_server_submit(lvg_server *sv, int graph_id, const lvg_batch *b, uint64_t *ticket) {
+  if (!sv || !b || !ticket) return lvg::fail_noalloc(LVG_EINVAL, "null argument");
+  Request r;
+  r.graph = graph_id;
+  r.ds.assign(b->del_src, b->del_src + b->num_deletions);
+  r.dd.assign(b->del_dst, b->del_dst + b->num_deletions);
+  r.dw.assign(b->del_w, b->del_w + b->num_deletions);
+  r.is.assign(b->ins_src, b->ins_src + b->num_insertions);
+  r.id.assign(b->ins_dst, b->ins_dst + b->num_insertions);
+  r.iw.assign(b->ins_w, b->ins_w + b->num_insertions);
+  std::lock_guard<std::mutex> lk(sv->mu);
+  if (graph_id < 0 || size_t(graph_id) >= sv->slots.size())
+    return lvg::fail_noalloc(LVG_EINVAL, "lvg_server_submit: unknown graph");
+  r.t_submit = now_ms();
+  r.ticket = sv->next_ticket++;
+  *ticket = r.ticket;
+  sv->slots[size_t(graph_id)]->q.push_back(std::move(r));
+  ++sv->pending;
+  sv->cv_work.notify_one();
+  return LVG_OK;
+}
+
+int lvg_server_wait(lvg_server *sv, uint64_t ticket, lvg_request_info *info) {
+  if (!sv) return lvg::fail_noalloc(LVG_EINVAL, "null argument");
+  std::unique_lock<std::mutex> lk(sv->mu);
+  if (ticket == 0 || ticket >= sv->next_ticket) return lvg::fail_noalloc(LVG_EINVAL, "lvg_server_wait: unknown ticket");
+  sv->cv_done.wait(lk, [&] { return sv->done.count(ticket) > 0; });
+  const lvg_request_info r = sv->done[ticket];
+  sv->done.erase(ticket);
+  if (info) *info = r;
+  return r.status;
+}
+
+int lvg_server_drain(lvg_server *sv) {
+  if (!sv) return lvg::fail_noalloc(LVG_EINVAL, "null argument");
+  std::unique_lock<std::mutex> lk(sv->mu);
+  sv->cv_done.wait(lk, [&] { return sv->pending == 0; });
+  return sv->failed ? LVG_ECUDA : LVG_OK;
+}
+
+int lvg_server_stats(lvg_server *sv, int reset, lvg_server_stats_t *out) {
+  if (!sv || !out) return lvg::fail_noalloc(LVG_EINVAL, "null argument");
+  std::lock_guard<std::mutex> lk(sv->mu);
+  std::memset(out, 0, sizeof(*out));
+  out->completed = sv->completed;
+  out->failed = sv->failed;
+  out->updates = sv->updates;
+  out->graphs = sv->slots.size();
+  out->hbm_reserved = sv->bytes_used;
+  std::vector<double> l = sv->lat;
+  if (!l.empty()) {
+    std::sort(l.begin(), l.end());
+    auto pct = [&](double p) { return l[std::min(l.size() - 1, size_t(p * double(l.size() - 1) + 0.5))]; };
+    out->p50_ms = pct(0.50);
+    out->p99_ms = pct(0.99);
+    out->max_ms = l.back();
+    double sum = 0;
+    for (double x : l) sum += x;
+    out->mean_ms = sum / double(l.size());
+  }
+  out->wall_s = sv->t_last > sv->t_first ? (sv->t_last - sv->t_first) / 1e3 : 0;
+  out->updates_per_s = out->wall_s > 0 ? double(sv->updates) / out->wall_s : 0;
+  out->requests_per_s = out->wall_s > 0 ? double(sv->completed) / out->wall_s : 0;
+  if (reset) {
+    sv->lat.clear();
+    sv->completed = sv->updates = sv->failed = 0;
+    sv->t_first = sv->t_last = 0;
+  }
+  return LVG_OK;
+}
+
+int lvg_server_membership(lvg_server *sv, int graph_id, uint32_t *membership, double *vtot, double *ctot) {
+  if (!sv) return lvg::fail_noalloc(LVG_EINVAL, "null argument");
+  std::unique_lock<std::mutex> lk(sv->mu);
+  if (graph_id < 0 || size_t(graph_id) >= sv->slots.size())
+    return lvg::fail_noalloc(LVG_EINVAL, "lvg_server_membership: unknown graph");
+  Slot &s = *sv->slots[size_t(graph_id)];
+  sv->cv_done.wait(lk, [&] { return !s.busy && s.q.empty(); });
+  return lvg_state_get(s.st, membership, vtot, ctot);
+}
+
+lvg_graph *lvg_server_graph(lvg_server *sv, int graph_id) {
+  if (!sv) return nullptr;
+  std::lock_guard<std::mutex> lk(sv->mu);
+  if (graph_id < 0 || size_t(graph_id) >= sv->slots.size()) return nullptr;
+  return sv->slots[size_t(graph_id)]->g;
+}
+
+int lvg_server_destroy(lvg_server *sv) {
+  if (!sv) return LVG_OK;
+  {
+    std::unique_lock<std::mutex> lk(sv->mu);
+    sv->cv_done.wait(lk, [&] { return sv->pending == 0; });
+    sv->stop = true;
+  }
+  sv->cv_work.notify_all();
+  for (auto &t : sv->workers) t.join();
+  for (auto &s : sv->slots) {
+    lvg_state_destroy(s->st);
+    if (s->owns_graph) lvg_graph_destroy(s->g);
+  }
+  delete sv;
+  return LVG_OK;
+}
+
+}  // extern "C"

@@ -73,6 +73,30 @@ class _Batch(C.Structure):
                 ("ins_dst", C.c_void_p), ("ins_w", C.c_void_p)]
 
 
+class _BatchBuf(C.Structure):
+    _fields_ = [("num_deletions", C.c_size_t), ("del_src", C.c_void_p), ("del_dst", C.c_void_p),
+                ("del_w", C.c_void_p), ("num_insertions", C.c_size_t), ("ins_src", C.c_void_p),
+                ("ins_dst", C.c_void_p), ("ins_w", C.c_void_p)]
+
+
+class _ServerOptions(C.Structure):
+    _fields_ = [("workers", C.c_int), ("hbm_budget", C.c_size_t), ("method", C.c_int), ("louvain", _Options)]
+
+
+class _RequestInfo(C.Structure):
+    _fields_ = [("ticket", C.c_uint64), ("graph", C.c_int), ("status", C.c_int), ("queue_ms", C.c_double),
+                ("apply_ms", C.c_double), ("run_ms", C.c_double), ("latency_ms", C.c_double),
+                ("iterations", C.c_int), ("passes", C.c_int), ("affected", C.c_uint64),
+                ("tidy_deletions", C.c_size_t), ("tidy_insertions", C.c_size_t)]
+
+
+class _ServerStats(C.Structure):
+    _fields_ = [("completed", C.c_uint64), ("failed", C.c_uint64), ("updates", C.c_uint64), ("graphs", C.c_size_t),
+                ("hbm_reserved", C.c_size_t), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
+                ("max_ms", C.c_double), ("mean_ms", C.c_double), ("wall_s", C.c_double),
+                ("updates_per_s", C.c_double), ("requests_per_s", C.c_double)]
+
+
 class _Stats(C.Structure):
     _fields_ = [("move_kernel_ms", C.c_double), ("move_launches", C.c_uint64), ("move_vertices", C.c_uint64),
                 ("move_edges", C.c_uint64), ("moves", C.c_uint64), ("aggregate_kernel_ms", C.c_double),
@@ -149,6 +173,26 @@ def load_library() -> C.CDLL:
     L.lvg_affected_vertices.argtypes = [vp, i32, C.POINTER(_Batch), _u32p, _f64p, _f64p, C.POINTER(_Options),
                                         vp, vp, vp]
     L.lvg_aggregate.argtypes = [vp, _u32p, _u32p, C.POINTER(sz), _u64p, vp, vp]
+    L.lvg_graph_apply_batch.argtypes = [vp, C.POINTER(_Batch), vp]
+    L.lvg_graph_apply_device_batch.argtypes = [vp, vp]
+    L.lvg_graph_download.argtypes = [vp, _u64p, vp, vp, vp]
+    L.lvg_graph_create_planted_partition.argtypes = [C.c_uint32, C.c_uint32, f64, f64, C.c_uint64, C.POINTER(vp)]
+    L.lvg_graph_create_rmat.argtypes = [i32, f64, f64, f64, f64, i32, C.c_uint64, C.POINTER(vp)]
+    L.lvg_device_batch_generate.argtypes = [vp, sz, sz, C.c_uint32, C.c_uint32, C.c_float, C.c_uint64,
+                                            C.POINTER(vp)]
+    L.lvg_device_batch_size.argtypes = [vp, C.POINTER(sz), C.POINTER(sz)]
+    L.lvg_device_batch_download.argtypes = [vp, vp]
+    L.lvg_server_options_default.argtypes = [C.POINTER(_ServerOptions)]
+    L.lvg_graph_footprint.argtypes = [sz, sz]
+    L.lvg_graph_footprint.restype = sz
+    L.lvg_server_create.argtypes = [C.POINTER(_ServerOptions), C.POINTER(vp)]
+    L.lvg_server_add_graph.argtypes = [vp, vp, i32, vp, vp, vp, C.POINTER(i32)]
+    L.lvg_server_submit.argtypes = [vp, i32, C.POINTER(_Batch), C.POINTER(C.c_uint64)]
+    L.lvg_server_wait.argtypes = [vp, C.c_uint64, C.POINTER(_RequestInfo)]
+    L.lvg_server_drain.argtypes = [vp]
+    L.lvg_server_stats.argtypes = [vp, i32, C.POINTER(_ServerStats)]
+    L.lvg_server_membership.argtypes = [vp, i32, vp, vp, vp]
+    L.lvg_server_destroy.argtypes = [vp]
     _lib = L
     return L
 
@@ -168,6 +212,8 @@ def load_graphgen() -> C.CDLL:
                             C.POINTER(_Csr)]
     G.lvgg_random_batch.argtypes = [C.POINTER(_Csr), C.c_size_t, C.c_double, C.c_uint64, C.POINTER(_GBatch)]
     G.lvgg_apply_batch.argtypes = [C.POINTER(_Csr), C.POINTER(_GBatch), C.POINTER(_Csr)]
+    G.lvgg_reference_batch.argtypes = [C.POINTER(_Csr), C.c_size_t, C.c_size_t, C.c_uint32, C.c_uint32, C.c_float,
+                                       C.c_uint64, C.POINTER(_GBatch)]
     G.lvgg_csr_free.argtypes = [C.POINTER(_Csr)]
     G.lvgg_batch_free.argtypes = [C.POINTER(_GBatch)]
     _gen = G
@@ -294,14 +340,7 @@ def rmat(scale: int, edge_factor: float = 16, a: float = 0.57, b: float = 0.19, 
     return _take_csr(cs)
 
 
-def random_batch(x: HostGraph, num_updates: int, insertion_fraction: float = 0.8, seed: int = 7) -> HostBatch:
-    """Tidy random batch: insertions of absent uniform pairs, edge-uniform deletions."""
-    G = load_graphgen()
-    cs = x._struct()
-    gb = _GBatch()
-    if G.lvgg_random_batch(C.byref(cs), num_updates, insertion_fraction, seed, C.byref(gb)) != 0:
-        raise LvgError(LVG_EINVAL, G.lvgg_last_error().decode())
-
+def _take_batch(G, gb) -> HostBatch:
     def arr(p, n, dt):
         return np.ctypeslib.as_array(p, (max(n, 1),))[:n].copy().astype(dt, copy=False)
 
@@ -310,6 +349,29 @@ def random_batch(x: HostGraph, num_updates: int, insertion_fraction: float = 0.8
                   arr(gb.ins_src, ni, np.uint32), arr(gb.ins_dst, ni, np.uint32), arr(gb.ins_w, ni, np.float32))
     G.lvgg_batch_free(C.byref(gb))
     return b
+
+
+def random_batch(x: HostGraph, num_updates: int, insertion_fraction: float = 0.8, seed: int = 7) -> HostBatch:
+    """Tidy random batch: insertions of absent uniform pairs, edge-uniform deletions."""
+    G = load_graphgen()
+    cs = x._struct()
+    gb = _GBatch()
+    if G.lvgg_random_batch(C.byref(cs), num_updates, insertion_fraction, seed, C.byref(gb)) != 0:
+        raise LvgError(LVG_EINVAL, G.lvgg_last_error().decode())
+    return _take_batch(G, gb)
+
+
+def reference_batch(x: HostGraph, deletions: int, insertions: int, begin: int = 1, range_: int | None = None,
+                    weight: float = 1.0, seed: int = 7) -> HostBatch:
+    """Untidy batch drawn as the reference's generateEdgeDeletions/Insertions
+    (lvgg_reference_batch); equals DeviceBatch.generate on the same graph."""
+    G = load_graphgen()
+    cs = x._struct()
+    gb = _GBatch()
+    r = x.span - begin if range_ is None else range_
+    if G.lvgg_reference_batch(C.byref(cs), deletions, insertions, begin, r, weight, seed, C.byref(gb)) != 0:
+        raise LvgError(LVG_EINVAL, G.lvgg_last_error().decode())
+    return _take_batch(G, gb)
 
 
 def apply_batch(x: HostGraph, b: HostBatch) -> HostGraph:
@@ -378,15 +440,31 @@ def _scalars(r: _Result) -> dict:
 class Graph:
     """A graph resident in HBM (``lvg_graph``)."""
 
-    def __init__(self, g: HostGraph):
+    def __init__(self, g: HostGraph | None):
         L = load_library()
         self._L = L
         self.h = C.c_void_p()
-        self.host = g
+        if g is None:  # filled by a generator classmethod
+            return
         w = g.weights if g.num_edges else np.zeros(1, np.float32)
         k = g.keys if g.num_edges else np.zeros(1, np.uint32)
         _check(L.lvg_graph_create(g.span, g.offsets, k.ctypes.data, w.ctypes.data, g.exists.ctypes.data,
                                   C.byref(self.h)))
+
+    @classmethod
+    def planted_partition(cls, n: int, block: int, avg_degree: float, p_in: float, seed: int) -> "Graph":
+        """Generated in HBM (lvg_graph_create_planted_partition); equals planted_partition()."""
+        G = cls(None)
+        _check(G._L.lvg_graph_create_planted_partition(n, block, avg_degree, p_in, seed, C.byref(G.h)))
+        return G
+
+    @classmethod
+    def rmat(cls, scale: int, edge_factor: float = 16, a: float = 0.57, b: float = 0.19, c: float = 0.19,
+             permute: bool = True, seed: int = 42) -> "Graph":
+        """Generated in HBM (lvg_graph_create_rmat); equals rmat()."""
+        G = cls(None)
+        _check(G._L.lvg_graph_create_rmat(scale, edge_factor, a, b, c, int(permute), seed, C.byref(G.h)))
+        return G
 
     def close(self) -> None:
         if self.h:
@@ -423,6 +501,35 @@ class Graph:
 
     def set_profiling(self, on: bool) -> None:
         _check(self._L.lvg_set_profiling(self.h, int(on)))
+
+    def apply_batch(self, b: "HostBatch | DeviceBatch") -> "HostBatch | None":
+        """Tidy a batch against the graph and apply it in place on the GPU (the
+        reference's tidyBatchUpdateU + applyBatchUpdateOmpU). For a HostBatch
+        returns the tidied batch (lvg_graph_apply_batch); a DeviceBatch is
+        replaced by its tidied batch on the device (lvg_graph_apply_device_batch)."""
+        if isinstance(b, DeviceBatch):
+            _check(self._L.lvg_graph_apply_device_batch(self.h, b.h))
+            return None
+        s = b._struct()
+        nd, ni = b.num_deletions, b.num_insertions
+        t = HostBatch(np.zeros(max(nd, 1), np.uint32), np.zeros(max(nd, 1), np.uint32), np.zeros(max(nd, 1), np.float32),
+                      np.zeros(max(ni, 1), np.uint32), np.zeros(max(ni, 1), np.uint32), np.zeros(max(ni, 1), np.float32))
+        o = _BatchBuf(0, t.del_src.ctypes.data, t.del_dst.ctypes.data, t.del_w.ctypes.data,
+                      0, t.ins_src.ctypes.data, t.ins_dst.ctypes.data, t.ins_w.ctypes.data)
+        _check(self._L.lvg_graph_apply_batch(self.h, C.byref(s), C.byref(o)))
+        kd, ki = o.num_deletions, o.num_insertions
+        return HostBatch(t.del_src[:kd].copy(), t.del_dst[:kd].copy(), t.del_w[:kd].copy(),
+                         t.ins_src[:ki].copy(), t.ins_dst[:ki].copy(), t.ins_w[:ki].copy())
+
+    def download(self) -> HostGraph:
+        """The graph as a compact host CSR (lvg_graph_download)."""
+        S, X = self.span, self.size
+        off = np.zeros(S + 1, np.uint64)
+        key = np.zeros(max(X, 1), np.uint32)
+        w = np.zeros(max(X, 1), np.float32)
+        ex = np.zeros(S, np.uint8)
+        _check(self._L.lvg_graph_download(self.h, off, key.ctypes.data, w.ctypes.data, ex.ctypes.data))
+        return HostGraph(off, key[:X].copy(), w[:X].copy(), ex)
 
     def stats(self) -> dict:
         s = _Stats()
@@ -559,13 +666,40 @@ class State:
 class DeviceBatch:
     """A validated batch resident in HBM (``lvg_device_batch``)."""
 
-    def __init__(self, g: Graph, b: HostBatch):
+    def __init__(self, g: Graph, b: HostBatch | None):
         self._L = load_library()
         self.g = g
         self.batch = b
         self.h = C.c_void_p()
+        if b is None:  # filled by generate()
+            return
         s = b._struct()
         _check(self._L.lvg_device_batch_create(g.h, C.byref(s), C.byref(self.h)))
+
+    @classmethod
+    def generate(cls, g: Graph, deletions: int, insertions: int, begin: int = 1, range_: int | None = None,
+                 weight: float = 1.0, seed: int = 7) -> "DeviceBatch":
+        """An untidy batch drawn in HBM as the reference's generators draw one
+        (lvg_device_batch_generate); equals reference_batch() on the same graph."""
+        d = cls(g, None)
+        r = g.span - begin if range_ is None else range_
+        _check(d._L.lvg_device_batch_generate(g.h, deletions, insertions, begin, r, weight, seed, C.byref(d.h)))
+        return d
+
+    def size(self) -> tuple[int, int]:
+        nd, ni = C.c_size_t(), C.c_size_t()
+        _check(self._L.lvg_device_batch_size(self.h, C.byref(nd), C.byref(ni)))
+        return nd.value, ni.value
+
+    def download(self) -> HostBatch:
+        nd, ni = self.size()
+        t = HostBatch(np.zeros(max(nd, 1), np.uint32), np.zeros(max(nd, 1), np.uint32), np.zeros(max(nd, 1), np.float32),
+                      np.zeros(max(ni, 1), np.uint32), np.zeros(max(ni, 1), np.uint32), np.zeros(max(ni, 1), np.float32))
+        o = _BatchBuf(0, t.del_src.ctypes.data, t.del_dst.ctypes.data, t.del_w.ctypes.data,
+                      0, t.ins_src.ctypes.data, t.ins_dst.ctypes.data, t.ins_w.ctypes.data)
+        _check(self._L.lvg_device_batch_download(self.h, C.byref(o)))
+        return HostBatch(t.del_src[:nd].copy(), t.del_dst[:nd].copy(), t.del_w[:nd].copy(),
+                         t.ins_src[:ni].copy(), t.ins_dst[:ni].copy(), t.ins_w[:ni].copy())
 
     def close(self) -> None:
         if self.h:
@@ -637,3 +771,75 @@ class PinnedArray:
             self.close()
         except Exception:
             pass
+
+
+class Server:
+    """A serving loop over graphs resident in HBM (``lvg_server``)."""
+
+    def __init__(self, workers: int = 8, hbm_budget: int = 120 << 30, method: int = 3,
+                 o: "LouvainOptions | None" = None):
+        self._L = load_library()
+        opt = _ServerOptions()
+        self._L.lvg_server_options_default(C.byref(opt))
+        opt.workers, opt.hbm_budget, opt.method = workers, hbm_budget, method
+        if o is not None:
+            opt.louvain = o._struct()
+        self.h = C.c_void_p()
+        self.graphs: list[Graph] = []
+        _check(self._L.lvg_server_create(C.byref(opt), C.byref(self.h)))
+
+    def add_graph(self, g: Graph, prior=None) -> int:
+        """Make g resident (the server borrows it; keep g alive). prior = (q, qvtot, qctot) or None (static)."""
+        gid = C.c_int()
+        if prior is None:
+            _check(self._L.lvg_server_add_graph(self.h, g.h, 0, None, None, None, C.byref(gid)))
+        else:
+            q, vt, ct = (np.ascontiguousarray(prior[0], np.uint32), np.ascontiguousarray(prior[1], np.float64),
+                         np.ascontiguousarray(prior[2], np.float64))
+            _check(self._L.lvg_server_add_graph(self.h, g.h, 0, q.ctypes.data, vt.ctypes.data, ct.ctypes.data,
+                                                C.byref(gid)))
+        self.graphs.append(g)
+        return gid.value
+
+    def submit(self, graph_id: int, b: HostBatch) -> int:
+        t = C.c_uint64()
+        s = b._struct()
+        _check(self._L.lvg_server_submit(self.h, graph_id, C.byref(s), C.byref(t)))
+        return t.value
+
+    def wait(self, ticket: int) -> dict:
+        r = _RequestInfo()
+        rc = self._L.lvg_server_wait(self.h, ticket, C.byref(r))
+        out = {k: getattr(r, k) for k, _ in _RequestInfo._fields_}
+        if rc != LVG_OK:
+            raise LvgError(rc, self._L.lvg_last_error().decode(errors="replace"))
+        return out
+
+    def drain(self) -> None:
+        _check(self._L.lvg_server_drain(self.h))
+
+    def stats(self, reset: bool = False) -> dict:
+        st = _ServerStats()
+        _check(self._L.lvg_server_stats(self.h, int(reset), C.byref(st)))
+        return {k: getattr(st, k) for k, _ in _ServerStats._fields_}
+
+    def state(self, graph_id: int):
+        S = self.graphs[graph_id].span
+        m, vt, ct = np.empty(S, np.uint32), np.empty(S, np.float64), np.empty(S, np.float64)
+        _check(self._L.lvg_server_membership(self.h, graph_id, m.ctypes.data, vt.ctypes.data, ct.ctypes.data))
+        return m, vt, ct
+
+    def close(self) -> None:
+        if self.h:
+            self._L.lvg_server_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def graph_footprint(span: int, edges: int) -> int:
+    return int(load_library().lvg_graph_footprint(span, edges))

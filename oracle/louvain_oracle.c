@@ -25,6 +25,9 @@
  *                        inc/louvain.hxx:1120-1221, 1285, 1349, 1542, 1674
  *                        (async moves louvainMoveOmpW :588-609, ΔQ
  *                        deltaModularity inc/properties.hxx:253-256)
+ *   orc_apply_batch      tidyBatchUpdateU + applyBatchUpdateOmpU
+ *                        inc/batch.hxx:154-209, 241-248 (DiGraph::removeEdge /
+ *                        addEdge inc/Graph.hxx:318-357), as main.cxx:108-109
  *   orc_louvain_sync     the project's deterministic colour-class rule
  *                        (no reference counterpart; replays the GPU's
  *                        deterministic mode in FP32 with the same operation
@@ -817,4 +820,110 @@ int orc_louvain_sync(size_t span, const uint64_t *off, const uint32_t *key, cons
   free(cext); free(fv); free(yoff); free(zoff); free(ykey); free(zkey); free(yw); free(zw);
   omp_set_num_threads(saved);
   return 0;
+}
+
+/* ------------------------------------------------------------ batch apply */
+
+typedef struct orc_edge { uint32_t u, v; size_t i; } orc_edge;
+
+static int cmp_edge(const void *a, const void *b) {
+  const orc_edge *x = (const orc_edge *)a, *y = (const orc_edge *)b;
+  if (x->u != y->u) return x->u < y->u ? -1 : 1;
+  if (x->v != y->v) return x->v < y->v ? -1 : 1;
+  return x->i < y->i ? -1 : x->i > y->i;
+}
+
+static int row_has(const uint64_t *off, const uint32_t *key, const uint8_t *ex, uint32_t u, uint32_t v) {
+  if (ex && !ex[u]) return 0;
+  for (uint64_t j = off[u]; j < off[u + 1]; ++j)
+    if (key[j] == v) return 1;
+  return 0;
+}
+
+/* tidyBatchUpdateU for one list: keep the edges whose presence in x equals
+ * `present` (filterEdgesByExistenceU, inc/batch.hxx:154-161), sort by
+ * (source, target) and drop duplicates, keeping the first in batch order
+ * (sortEdgesByIdU + uniqueEdgesU, :169-192; the reference's unstable sort
+ * keeps an unspecified one). Returns the kept count; indices into the input
+ * in *out. */
+static size_t tidy_list(const uint64_t *off, const uint32_t *key, const uint8_t *ex, size_t n, const uint32_t *s,
+                        const uint32_t *d, int present, size_t *out) {
+  orc_edge *e = malloc((n ? n : 1) * sizeof(orc_edge));
+  size_t m = 0, k = 0;
+  for (size_t i = 0; i < n; ++i)
+    if (row_has(off, key, ex, s[i], d[i]) == present) { e[m].u = s[i]; e[m].v = d[i]; e[m].i = i; ++m; }
+  qsort(e, m, sizeof(orc_edge), cmp_edge);
+  for (size_t i = 0; i < m; ++i) {
+    if (i && e[i].u == e[i - 1].u && e[i].v == e[i - 1].v) continue;
+    out[k++] = e[i].i;
+  }
+  free(e);
+  return k;
+}
+
+/* Order (key | weight bits << 32) pairs by key. */
+static int cmp_kw(const void *a, const void *b) {
+  const uint32_t x = (uint32_t)*(const uint64_t *)a, y = (uint32_t)*(const uint64_t *)b;
+  return x < y ? -1 : x > y;
+}
+
+/* tidyBatchUpdateU + applyBatchUpdateOmpU, as main.cxx:108-109 runs them:
+ * the batch is tidied against x, then its deletions are removed and its
+ * insertions added (DiGraph::removeEdge / addEdge, inc/Graph.hxx:318-357),
+ * an added edge making both endpoints present; rows stay sorted by
+ * neighbour id. Ids must be < span. Outputs: the graph (yoff[span+1],
+ * ykey/yw with room for off[span]+ni entries, yex[span]) and the tidied
+ * batch (tds/tdd/tdw with room for nd, tis/tid/tiw for ni; counts in
+ * *tnd, *tni). Returns the edge count of the result. */
+size_t orc_apply_batch(size_t span, const uint64_t *off, const uint32_t *key, const float *w, const uint8_t *ex,
+                       size_t nd, const uint32_t *ds, const uint32_t *dd, const float *dw, size_t ni,
+                       const uint32_t *is, const uint32_t *id, const float *iw, uint64_t *yoff, uint32_t *ykey,
+                       float *yw, uint8_t *yex, uint32_t *tds, uint32_t *tdd, float *tdw, size_t *tnd,
+                       uint32_t *tis, uint32_t *tid, float *tiw, size_t *tni) {
+  size_t *kd = malloc((nd ? nd : 1) * sizeof(size_t)), *ki = malloc((ni ? ni : 1) * sizeof(size_t));
+  const size_t md = tidy_list(off, key, ex, nd, ds, dd, 1, kd);
+  const size_t mi = tidy_list(off, key, ex, ni, is, id, 0, ki);
+  for (size_t t = 0; t < md; ++t) { tds[t] = ds[kd[t]]; tdd[t] = dd[kd[t]]; tdw[t] = dw[kd[t]]; }
+  for (size_t t = 0; t < mi; ++t) { tis[t] = is[ki[t]]; tid[t] = id[ki[t]]; tiw[t] = iw[ki[t]]; }
+  *tnd = md;
+  *tni = mi;
+  for (size_t u = 0; u < span; ++u) yex[u] = ex ? ex[u] : 1;
+  for (size_t t = 0; t < mi; ++t) { yex[tis[t]] = 1; yex[tid[t]] = 1; }
+  /* the tidied lists are sorted by source: walk them row by row */
+  size_t m = 0, a = 0, c = 0;
+  yoff[0] = 0;
+  for (size_t u = 0; u < span; ++u) {
+    const uint64_t o = m;
+    const size_t a0 = a;
+    while (a < md && tds[a] == u) ++a;
+    for (uint64_t j = off[u]; j < off[u + 1]; ++j) {
+      int gone = 0;
+      for (size_t t = a0; t < a && !gone; ++t) gone = tdd[t] == key[j];
+      if (gone) continue;
+      ykey[m] = key[j];
+      yw[m] = w[j];
+      ++m;
+    }
+    for (; c < mi && tis[c] == u; ++c) { ykey[m] = tid[c]; yw[m] = tiw[c]; ++m; }
+    const size_t n = m - o;
+    if (n > 1) {
+      uint64_t *kw = malloc(n * sizeof(uint64_t));
+      for (size_t j = 0; j < n; ++j) {
+        uint32_t wb;
+        memcpy(&wb, &yw[o + j], 4);
+        kw[j] = ((uint64_t)ykey[o + j]) | ((uint64_t)wb << 32);
+      }
+      qsort(kw, n, sizeof(uint64_t), cmp_kw);
+      for (size_t j = 0; j < n; ++j) {
+        const uint32_t wb = (uint32_t)(kw[j] >> 32);
+        ykey[o + j] = (uint32_t)kw[j];
+        memcpy(&yw[o + j], &wb, 4);
+      }
+      free(kw);
+    }
+    yoff[u + 1] = m;
+  }
+  free(kd);
+  free(ki);
+  return m;
 }

@@ -108,6 +108,10 @@ class Oracle:
         L.orc_modularity.restype = C.c_double
         run = G + [C.c_int] + B + [_u32p, _f64p, _f64p, C.POINTER(Options), C.c_int, _u32p, _f64p, _f64p,
                                    C.POINTER(Info)]
+        szp = C.POINTER(C.c_size_t)
+        L.orc_apply_batch.argtypes = G + B + [_u64p, _u32p, _f32p, _u8p, _u32p, _u32p, _f32p, szp, _u32p, _u32p,
+                                              _f32p, szp]
+        L.orc_apply_batch.restype = _sz
         L.orc_louvain.argtypes = run
         L.orc_louvain_sync.argtypes = run[:-4] + [C.c_int] + run[-4:]
         self.L = L
@@ -150,6 +154,24 @@ class Oracle:
         yw = np.zeros(max(X, 1), np.float64)
         CN = self.L.orc_aggregate(*_graph_args(g), vc, yoff, ydeg, yk, yw)
         return vc, CN, _rows(CN, yoff, ydeg, yk, yw)
+
+    def apply_batch(self, g, b):
+        """tidyBatchUpdateU + applyBatchUpdateOmpU restated. Returns the graph as
+        (offsets, keys, weights, exists) and the tidied batch as a tuple
+        (ds, dd, dw, is, id, iw)."""
+        S = g.span
+        a = _batch_args(b)
+        yoff = np.zeros(S + 1, np.uint64)
+        cap = max(g.num_edges + a[4], 1)
+        yk, yw, yex = np.zeros(cap, np.uint32), np.zeros(cap, np.float32), np.zeros(S, np.uint8)
+        nd, ni = max(a[0], 1), max(a[4], 1)
+        t = [np.zeros(nd, np.uint32), np.zeros(nd, np.uint32), np.zeros(nd, np.float32),
+             np.zeros(ni, np.uint32), np.zeros(ni, np.uint32), np.zeros(ni, np.float32)]
+        tnd, tni = C.c_size_t(), C.c_size_t()
+        m = self.L.orc_apply_batch(*_graph_args(g), *a, yoff, yk, yw, yex, t[0], t[1], t[2], C.byref(tnd),
+                                   t[3], t[4], t[5], C.byref(tni))
+        tidy = tuple(x[:tnd.value].copy() for x in t[:3]) + tuple(x[:tni.value].copy() for x in t[3:])
+        return (yoff, yk[:m].copy(), yw[:m].copy(), yex), tidy
 
     def modularity(self, g, membership, M=None, R=1.0) -> float:
         if M is None:
@@ -204,6 +226,12 @@ class Reference:
         L.ref_ds_mark.argtypes = [_vp] + B + [_u32p, _f64p, _f64p, C.c_double, C.c_double, _u8p, _u8p, _u8p]
         L.ref_aggregate.argtypes = [_vp, _u32p, _u64p, _u32p, _u32p, _f64p]
         L.ref_aggregate.restype = _sz
+        szp = C.POINTER(C.c_size_t)
+        L.ref_apply_batch.argtypes = [_vp] + B + [_u32p, _u32p, _f32p, szp, _u32p, _u32p, _f32p, szp]
+        L.ref_graph_size.argtypes = [_vp]
+        L.ref_graph_size.restype = _sz
+        L.ref_graph_csr.argtypes = [_vp, _u64p, _u32p, _f32p, _u8p]
+        L.ref_graph_csr.restype = _sz
         L.ref_modularity.argtypes = [_vp, _u32p, C.c_double, C.c_double]
         L.ref_modularity.restype = C.c_double
         L.ref_louvain.argtypes = [_vp, C.c_int] + B + [_u32p, _f64p, _f64p, C.c_int, C.c_double, C.c_double,
@@ -264,6 +292,27 @@ class _RefGraph:
         yw = np.zeros(max(X, 1), np.float64)
         CN = self.ref.L.ref_aggregate(self.h, vc, yoff, ydeg, yk, yw)
         return vc, CN, _rows(CN, yoff, ydeg, yk, yw)
+
+    def apply_batch(self, b):
+        """tidyBatchUpdateU + applyBatchUpdateOmpU on this graph, in place, as
+        main.cxx runs them. Returns the graph as (offsets, keys, weights,
+        exists) and the tidied batch as (ds, dd, dw, is, id, iw)."""
+        a = _batch_args(b)
+        nd, ni = max(a[0], 1), max(a[4], 1)
+        t = [np.zeros(nd, np.uint32), np.zeros(nd, np.uint32), np.zeros(nd, np.float32),
+             np.zeros(ni, np.uint32), np.zeros(ni, np.uint32), np.zeros(ni, np.float32)]
+        tnd, tni = C.c_size_t(), C.c_size_t()
+        self.ref.L.ref_apply_batch(self.h, *a, t[0], t[1], t[2], C.byref(tnd), t[3], t[4], t[5], C.byref(tni))
+        tidy = tuple(x[:tnd.value].copy() for x in t[:3]) + tuple(x[:tni.value].copy() for x in t[3:])
+        return self.csr(), tidy
+
+    def csr(self):
+        S = self.g.span
+        X = int(self.ref.L.ref_graph_size(self.h))
+        yoff = np.zeros(S + 1, np.uint64)
+        yk, yw, yex = np.zeros(max(X, 1), np.uint32), np.zeros(max(X, 1), np.float32), np.zeros(S, np.uint8)
+        m = self.ref.L.ref_graph_csr(self.h, yoff, yk, yw, yex)
+        return yoff, yk[:m].copy(), yw[:m].copy(), yex
 
     def modularity(self, membership, M=None, R=1.0) -> float:
         if M is None:

@@ -18,6 +18,9 @@
 //                          sequence (inc/louvain.hxx:1190-1202)
 //   ref_modularity      -> modularityBy (inc/properties.hxx:178)
 //   ref_edge_weight     -> edgeWeightOmp (inc/properties.hxx:96)
+//   ref_apply_batch     -> tidyBatchUpdateU + applyBatchUpdateOmpU
+//                          (inc/batch.hxx:202, 241), in place
+//   ref_graph_csr       -> the graph's rows (forEachEdge) as a compact CSR
 #include "inc/main.hxx"
 
 #include <cstdint>
@@ -148,6 +151,34 @@ size_t ref_aggregate(void *gp, uint32_t *vcom, uint64_t *yoff, uint32_t *ydeg, u
   std::memcpy(ykey, z.edgeKeys.data(), X * sizeof(K));
   std::memcpy(yw, z.edgeValues.data(), X * sizeof(W));
   return CN;
+}
+
+// tidyBatchUpdateU + applyBatchUpdateOmpU, in place, as main.cxx:108-109;
+// the tidied batch is written out (room for nd / ni entries).
+void ref_apply_batch(void *gp, size_t nd, const uint32_t *ds, const uint32_t *dd, const float *dw, size_t ni,
+                     const uint32_t *is, const uint32_t *id, const float *iw, uint32_t *tds, uint32_t *tdd,
+                     float *tdw, size_t *tnd, uint32_t *tis, uint32_t *tid, float *tiw, size_t *tni) {
+  G &y = *static_cast<G *>(gp);
+  auto del = make_edges(nd, ds, dd, dw), ins = make_edges(ni, is, id, iw);
+  tidyBatchUpdateU(del, ins, y);
+  applyBatchUpdateOmpU(y, del, ins);
+  for (size_t i = 0; i < del.size(); ++i) std::tie(tds[i], tdd[i], tdw[i]) = del[i];
+  for (size_t i = 0; i < ins.size(); ++i) std::tie(tis[i], tid[i], tiw[i]) = ins[i];
+  *tnd = del.size();
+  *tni = ins.size();
+}
+
+// Compact CSR of the graph: off[span+1], key/w[size], ex[span]. Returns size.
+size_t ref_graph_csr(void *gp, uint64_t *off, uint32_t *key, float *w, uint8_t *ex) {
+  const G &x = *static_cast<G *>(gp);
+  size_t m = 0;
+  off[0] = 0;
+  for (size_t u = 0; u < x.span(); ++u) {
+    ex[u] = x.hasVertex(K(u)) ? 1 : 0;
+    if (ex[u]) x.forEachEdge(K(u), [&](auto v, auto wt) { key[m] = v; w[m] = wt; ++m; });
+    off[u + 1] = m;
+  }
+  return m;
 }
 
 double ref_modularity(void *gp, const uint32_t *membership, double M, double R) {

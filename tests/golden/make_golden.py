@@ -12,6 +12,12 @@ four entry points (deterministic: the reference's sweep is sequential with one
 thread) and the mean modularity of 5 multi-threaded runs. The inputs are
 seeded synthetic graphs from liblvg_graphgen.so plus one hand-made graph with
 self-loops, absent vertices, isolated vertices and integer weights.
+
+apply.npz holds the batch-update fixtures: untidy batches (unsorted, with
+duplicates, deletions of absent edges, insertions of present edges and of
+edges touching absent vertices) run through the reference's
+tidyBatchUpdateU + applyBatchUpdateOmpU, twice in a row; the graphs after
+each batch and the tidied batches. `--only apply` regenerates just that file.
 """
 from __future__ import annotations
 
@@ -87,6 +93,50 @@ def edge_case_batch(x: lvg.HostGraph) -> lvg.HostBatch:
                          a(i, 0, np.uint32), a(i, 1, np.uint32), a(i, 2, np.float32))
 
 
+def messy_batch(x: lvg.HostGraph, n: int, seed: int) -> lvg.HostBatch:
+    """An untidy batch of about 3n entries. Duplicates repeat the weight of
+    their first occurrence, so the reference's unstable sort cannot change
+    the result."""
+    rng = np.random.default_rng(seed)
+    S = x.span
+    src = np.repeat(np.arange(S, dtype=np.uint32), np.diff(x.offsets).astype(np.int64))
+    n = min(n, x.num_edges)
+    e = rng.choice(x.num_edges, n, replace=False)
+    a = rng.integers(0, S, (n // 4, 2)).astype(np.uint32)               # mostly absent edges
+    ds = np.concatenate([src[e], a[:, 0], src[e[: n // 8]]])
+    dd = np.concatenate([x.keys[e], a[:, 1], x.keys[e[: n // 8]]])
+    dw = np.concatenate([x.weights[e], np.ones(n // 4, np.float32), x.weights[e[: n // 8]]])
+    r = rng.integers(0, S, (n, 2)).astype(np.uint32)                    # mostly new edges
+    e2 = rng.choice(x.num_edges, max(n // 4, 1), replace=False)         # present edges
+    rw = rng.integers(1, 5, n).astype(np.float32)
+    is_ = np.concatenate([r[:, 0], src[e2], r[: n // 8, 0]])
+    id_ = np.concatenate([r[:, 1], x.keys[e2], r[: n // 8, 1]])
+    iw = np.concatenate([rw, rng.integers(5, 9, len(e2)).astype(np.float32), rw[: n // 8]])
+    p, q = rng.permutation(len(ds)), rng.permutation(len(is_))
+    return lvg.HostBatch(ds[p].copy(), dd[p].copy(), dw[p].copy(), is_[q].copy(), id_[q].copy(), iw[q].copy())
+
+
+def apply_fixtures(ref) -> None:
+    d = {}
+    for name, x, n in (("pp1k", lvg.planted_partition(1024, 64, 12, 0.8, 21), 300),
+                       ("edge", edge_case_graph(), 40)):
+        rg = ref.graph(x)
+        d.update({f"{name}_x_off": x.offsets, f"{name}_x_key": x.keys, f"{name}_x_w": x.weights,
+                  f"{name}_x_ex": x.exists})
+        for step in (1, 2):
+            b = messy_batch(x, n, seed=100 * step + len(name))
+            (yo, yk, yw, yex), tidy = rg.apply_batch(b)
+            p = f"{name}_{step}_"
+            d.update({p + "b_ds": b.del_src, p + "b_dd": b.del_dst, p + "b_dw": b.del_w,
+                      p + "b_is": b.ins_src, p + "b_id": b.ins_dst, p + "b_iw": b.ins_w,
+                      p + "y_off": yo, p + "y_key": yk, p + "y_w": yw, p + "y_ex": yex})
+            d.update({p + "t_" + k: v for k, v in zip(("ds", "dd", "dw", "is", "id", "iw"), tidy)})
+            x = lvg.HostGraph(yo, yk, yw, yex)
+            print(name, step, "batch", b.num_deletions, b.num_insertions, "tidied", len(tidy[0]), len(tidy[3]),
+                  "edges", len(yk))
+    np.savez_compressed(os.path.join(OUT, "apply.npz"), **d)
+
+
 def cases():
     yield "pp2k", lvg.planted_partition(2048, 128, 16, 0.8, 11), 200
     yield "rmat11", lvg.rmat(11, 16, seed=5), 200
@@ -107,6 +157,9 @@ def main() -> None:
     lvg_build.build_graphgen()
     O.build(ref=True)
     ref = O.Reference()
+    apply_fixtures(ref)
+    if sys.argv[1:] == ["--only", "apply"]:
+        return
     for name, x, nupd in cases():
         b = edge_case_batch(x) if nupd is None else lvg.random_batch(x, nupd, 0.8, seed=7)
         y = lvg.apply_batch(x, b)

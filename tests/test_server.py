@@ -1,0 +1,87 @@
+"""The serving loop (lvg_server): many graphs resident in HBM, batch-update
+requests applied and answered concurrently.
+
+A server runs, per request, what main.cxx:108-125 runs per batch — tidy and
+apply the batch to the graph, then the dynamic method from the previous
+result — so in deterministic mode a graph's final state must not depend on
+what else the server was doing: the test interleaves requests for several
+graphs through 4 workers and compares each graph's state, bit for bit, with
+the same sequence run alone through lvg_graph_apply_device_batch +
+lvg_run_resident. Admission control refuses a graph that would exceed the
+HBM budget.
+"""
+import numpy as np
+import pytest
+
+
+def _graphs(lvg):
+    return [lvg.planted_partition(3000, 100, 12, 0.8, 1), lvg.rmat(11, 8, seed=2), lvg.planted_partition(5000, 64, 8, 0.7, 3),
+            lvg.rmat(12, 4, seed=4), lvg.planted_partition(1500, 150, 20, 0.9, 5)]
+
+
+def _batches(lvg, orc, x, k, seed):
+    """k untidy batches drawn one after another on the evolving graph."""
+    out = []
+    cur = x
+    for j in range(k):
+        b = lvg.reference_batch(cur, 40 + 10 * j, 200 + 50 * j, seed=seed * 100 + j)
+        cur = lvg.HostGraph(*orc.apply_batch(cur, b)[0])
+        out.append(b)
+    return out
+
+
+def test_footprint_grows_with_the_graph(lvg):
+    lvg.load_library()
+    assert lvg.graph_footprint(1000, 10_000) < lvg.graph_footprint(1000, 20_000) < lvg.graph_footprint(2000, 20_000)
+
+
+@pytest.mark.gpu
+def test_server_results_equal_sequential_runs(cuda, orc):
+    o = cuda.LouvainOptions(deterministic=True)
+    xs = _graphs(cuda)
+    seqs = [_batches(cuda, orc, x, 4, i + 1) for i, x in enumerate(xs)]
+    # alone
+    alone = []
+    for x, seq in zip(xs, seqs):
+        G = cuda.Graph(x)
+        st = cuda.State(G)
+        cuda.run_resident(G, cuda.METHOD_STATIC, None, None, st, o)
+        for b in seq:
+            db = cuda.DeviceBatch(G, b)
+            G.apply_batch(db)
+            cuda.run_resident(G, cuda.METHOD_FRONTIER, db, st, st, o)
+        alone.append(st.get())
+    # served: requests interleaved across graphs
+    sv = cuda.Server(workers=4, method=cuda.METHOD_FRONTIER, o=o)
+    Gs = [cuda.Graph(x) for x in xs]
+    ids = [sv.add_graph(G) for G in Gs]
+    tickets = []
+    for j in range(4):
+        for gid, seq in zip(ids, seqs):
+            tickets.append(sv.submit(gid, seq[j]))
+    infos = [sv.wait(t) for t in tickets]
+    assert all(i["status"] == 0 for i in infos)
+    assert all(i["latency_ms"] >= i["run_ms"] for i in infos)
+    for gid, ref in zip(ids, alone):
+        m, vt, ct = sv.state(gid)
+        assert np.array_equal(m, ref[0])
+        assert np.array_equal(vt, ref[1]) and np.array_equal(ct, ref[2])
+    st = sv.stats()
+    assert st["completed"] == len(tickets) and st["failed"] == 0
+    assert st["p99_ms"] >= st["p50_ms"] > 0
+    sv.close()
+
+
+@pytest.mark.gpu
+def test_server_admission_control(cuda):
+    x = cuda.planted_partition(2000, 100, 10, 0.8, 1)
+    G = cuda.Graph(x)
+    need = cuda.graph_footprint(x.span, x.num_edges)
+    sv = cuda.Server(workers=2, hbm_budget=need + need // 2)
+    sv.add_graph(G)
+    H = cuda.Graph(x)
+    with pytest.raises(cuda.LvgError) as e:
+        sv.add_graph(H)
+    assert e.value.code == cuda.LVG_ENOMEM
+    assert sv.stats()["graphs"] == 1
+    sv.close()
