@@ -111,6 +111,12 @@ typedef struct lvg_graph lvg_graph;
 int lvg_graph_create(size_t span, const uint64_t *offsets, const uint32_t *keys, const float *weights,
                      const uint8_t *exists, lvg_graph **out);
 int lvg_graph_destroy(lvg_graph *g);
+/* Device bytes held by a graph: its gapped CSR, workspace and scratch. */
+size_t lvg_graph_device_bytes(const lvg_graph *g);
+/* Release scratch a graph keeps between calls: level 1 the global hash
+ * tables and the batch-apply scratch, level 2 also the workspace. Later calls
+ * allocate again what they need. */
+int lvg_graph_trim(lvg_graph *g, int level);
 /* G::span(), G::order(), G::size() (inc/Graph.hxx:59-80). */
 size_t lvg_graph_span(const lvg_graph *g);
 size_t lvg_graph_order(const lvg_graph *g);
@@ -196,11 +202,16 @@ int lvg_state_get(const lvg_state *st, uint32_t *membership, double *vtot, doubl
 /* A state or device batch may be destroyed before or after its graph; every
  * other call on it needs the graph alive. */
 int lvg_state_destroy(lvg_state *st);
+size_t lvg_state_device_bytes(const lvg_state *st);
 
 /* A validated batch in HBM. */
 typedef struct lvg_device_batch lvg_device_batch;
 int lvg_device_batch_create(lvg_graph *g, const lvg_batch *b, lvg_device_batch **out);
+/* Replace a device batch's contents with a new host batch (its buffers grow
+ * as needed and are reused: no allocation once they are large enough). */
+int lvg_device_batch_set(lvg_device_batch *db, const lvg_batch *b);
 int lvg_device_batch_destroy(lvg_device_batch *b);
+size_t lvg_device_batch_device_bytes(const lvg_device_batch *b);
 
 /* Caller-owned arrays that receive a batch; the counts are written back. */
 typedef struct lvg_batch_buf {

@@ -153,6 +153,28 @@ class DeviceGraph {
   lvg_graph *g_ = nullptr;
 };
 
+// ----------------------------------------------------------------- batch update
+
+/** tidyBatchUpdateU(deletions, insertions, y) followed by
+ * applyBatchUpdateOmpU(y, deletions, insertions) (inc/batch.hxx:202, 241), as
+ * main.cxx:108-109 runs them, on a graph in HBM: the graph is updated in
+ * place and the vectors are replaced by the tidied batch (present deletions,
+ * absent insertions, sorted by (source, target), unique), ready for the
+ * dynamic entry points. */
+template <class K, class V>
+inline void tidyApplyBatchUpdateOmpU(DeviceGraph &y, std::vector<std::tuple<K, K, V>> &deletions,
+                                     std::vector<std::tuple<K, K, V>> &insertions) {
+  detail::Batch b(deletions, insertions);
+  std::vector<uint32_t> ts(b.ds.size()), td(b.ds.size()), us(b.is.size()), ud(b.is.size());
+  std::vector<float> tw(b.ds.size()), uw(b.is.size());
+  lvg_batch_buf t{0, ts.data(), td.data(), tw.data(), 0, us.data(), ud.data(), uw.data()};
+  detail::check(lvg_graph_apply_batch(y.get(), &b.c, &t), "lvg_graph_apply_batch");
+  deletions.clear();
+  insertions.clear();
+  for (size_t i = 0; i < t.num_deletions; ++i) deletions.emplace_back(K(ts[i]), K(td[i]), V(tw[i]));
+  for (size_t i = 0; i < t.num_insertions; ++i) insertions.emplace_back(K(us[i]), K(ud[i]), V(uw[i]));
+}
+
 // ----------------------------------------------------------------- entry points
 
 template <class K = uint32_t>
@@ -250,4 +272,5 @@ using louvain_gb300::louvainDynamicDeltaScreeningOmp;
 using louvain_gb300::louvainDynamicFrontierOmp;
 using louvain_gb300::louvainNaiveDynamicOmp;
 using louvain_gb300::louvainStaticOmp;
+using louvain_gb300::tidyApplyBatchUpdateOmpU;
 #endif

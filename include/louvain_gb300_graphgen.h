@@ -94,6 +94,48 @@ int lvgg_apply_batch(const lvgg_csr *x, const lvgg_batch *b, lvgg_csr *y);
 int lvgg_reference_batch(const lvgg_csr *x, size_t deletions, size_t insertions, uint32_t begin, uint32_t range,
                          float weight, uint64_t seed, lvgg_batch *out);
 
+/* ---- Temporal edge streams (the reference's SNAP temporal input). */
+
+/** An edge list in stream order. */
+typedef struct lvgg_edges {
+  size_t    n;
+  uint32_t *src, *dst;
+  float    *w;
+} lvgg_edges;
+
+typedef struct lvgg_temporal lvgg_temporal;
+/** Open a SNAP temporal file ("u v [w] [t]" per line, as inc/snap.hxx:41-140 reads it). */
+int lvgg_temporal_open(const char *path, int weighted, lvgg_temporal **out);
+/**
+ * The next `lines` lines as edges (both directions when symmetric, as
+ * readTemporalDo emits them, inc/snap.hxx:41-60; weight 1 unless weighted).
+ * Stops early at the end of the file or a line that does not parse.
+ */
+int lvgg_temporal_read(lvgg_temporal *t, size_t lines, int symmetric, lvgg_edges *out);
+void lvgg_temporal_close(lvgg_temporal *t);
+/** Write edges as a SNAP temporal file: "u v t" lines, t = stream index (one line per edge). */
+int lvgg_temporal_write(const char *path, const lvgg_edges *e);
+
+/**
+ * The graph readTemporalOmpW builds from an edge list (inc/snap.hxx:160-212):
+ * vertices 1..rows exist (and any endpoint of an edge), rows sorted by
+ * neighbour id, duplicate edges merged keeping the last weight. Ids must be
+ * <= rows.
+ */
+int lvgg_csr_from_edges(size_t rows, const lvgg_edges *e, lvgg_csr *out);
+
+/**
+ * A synthetic temporal stream with drifting communities (stands in for the
+ * SNAP temporal datasets): n vertices (ids 1..n) in `communities` groups of
+ * log-normal sizes (sigma), `edges` undirected edges in time order, each
+ * intra-community with probability p_in (else uniform); every
+ * `drift_every` edges, a fraction `drift` of the vertices move to a random
+ * community. One line per undirected edge (as the SNAP files are).
+ */
+int lvgg_temporal_drift(uint32_t n, uint32_t communities, double sigma, size_t edges, double p_in,
+                        size_t drift_every, double drift, uint64_t seed, lvgg_edges *out);
+void lvgg_edges_free(lvgg_edges *e);
+
 void lvgg_csr_free(lvgg_csr *g);
 void lvgg_batch_free(lvgg_batch *b);
 

@@ -136,6 +136,7 @@ struct RunInfo {
 using namespace lvg;
 
 struct lvg_graph {
+  size_t bytes = 0;  // device bytes held (graph, workspace, scratch)
   int device = 0;
   cudaStream_t stream = nullptr;
   Level base;
@@ -146,15 +147,17 @@ struct lvg_graph {
   DBuf<uint32_t> deg, cap, key, bins;
   DBuf<float> w;
   DBuf<uint8_t> ex;
-  size_t slots = 0, pool_begin = 0;
+  size_t slots = 0, pool_begin = 0, pool_cursor = 0;
   bool rows_sorted = true;  // every row sorted by neighbour id (batch apply needs it)
   // batch apply: counters (UPD_*) and scratch
   DBuf<unsigned long long> upd;
   HBuf<unsigned long long> hupd;
   HBuf<uint32_t> hcnt;
   DBuf<UpdRow> u_rows;
-  DBuf<uint64_t> u_bound, u_spos, u_scan, u_k0, u_k1;
-  DBuf<uint32_t> u_skey, u_newdeg, u_pre, u_keep, u_pos, u_pscan, u_v0, u_v1, u_flag, u_touch, u_tpos, u_tscan;
+  DBuf<uint64_t> u_len, u_src, u_grow, u_spos, u_srcpos, u_gpos, u_scan, u_k0, u_k1;
+  DBuf<RowPlan> u_plan;
+  DBuf<double> u_wdelta;
+  DBuf<uint32_t> u_skey, u_pre, u_keep, u_pos, u_pscan, u_v0, u_v1, u_flag, u_touch, u_tpos, u_tscan;
   DBuf<uint32_t> u_cnt;
   DBuf<uint32_t> u_ds, u_dd, u_is, u_id;
   DBuf<float> u_sw, u_dw, u_iw;
@@ -184,6 +187,7 @@ struct lvg_graph {
 // A state or a device batch may outlive its graph (it keeps its own device
 // id for its destruction and never touches the graph there).
 struct lvg_state {
+  size_t bytes = 0;
   lvg_graph *g = nullptr;
   int device = 0;
   DBuf<uint32_t> q;
@@ -191,6 +195,7 @@ struct lvg_state {
 };
 
 struct lvg_device_batch {
+  size_t bytes = 0;
   lvg_graph *g = nullptr;
   int device = 0;
   DBuf<uint32_t> ds, dd, is, id, seg;
@@ -435,7 +440,7 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const 
     for (int k = 0; k < K; ++k) most = std::max(most, lv.bucket_size(k, b));
     if (!most) continue;
     glog2[b] = global_table_log2(lv.bin_maxdeg[b]);
-    need = std::max(need, size_t(global_table_blocks(most)) << glog2[b]);
+    need = std::max(need, size_t(move_grid_blocks(b, sync, most)) << glog2[b]);
   }
   if (need) {
     W.gkeys.ensure(need);
@@ -788,6 +793,7 @@ void upload_prior(lvg_graph *g, const uint32_t *q, const double *qvtot, const do
 
 int run_host(lvg_graph *g, int method, const lvg_batch *b, const uint32_t *q, const double *qvtot,
              const double *qctot, const lvg_options *o, lvg_result *out) {
+  AcctScope acct_(g ? &g->bytes : nullptr);
   if (!g || !out) return fail(LVG_EINVAL, "null graph or result");
   return guarded([&] {
     LVG_CUDA(cudaSetDevice(g->device));
@@ -827,7 +833,7 @@ void init_graph(lvg_graph *g, size_t span, size_t order, size_t X, const uint64_
   g->cap.ensure(span);
   g->bins.ensure(span + 1);
   g->upd.ensure(UPD_SLOTS);
-  g->hupd.ensure(UPD_SLOTS + 1);
+  g->hupd.ensure(UPD_SLOTS + 8);
   {
     DBuf<uint64_t> cap64, sc;
     cap64.ensure(span);
@@ -844,9 +850,8 @@ void init_graph(lvg_graph *g, size_t span, size_t order, size_t X, const uint64_
     LVG_CUDA(cudaMemsetAsync(g->key.p + rows_end, 0, (g->slots - rows_end) * 4, s));
     LVG_CUDA(cudaMemsetAsync(g->w.p + rows_end, 0, (g->slots - rows_end) * 4, s));
     launch_spread_rows(coff, ckey, cw, span, g->off.p, g->cap.p, g->key.p, g->w.p, s);
-    g->hupd.p[UPD_POOL] = rows_end;
-    for (int i = 1; i < UPD_SLOTS; ++i) g->hupd.p[i] = 0;
-    LVG_CUDA(cudaMemcpyAsync(g->upd.p, g->hupd.p, UPD_SLOTS * 8, cudaMemcpyHostToDevice, s));
+    g->pool_cursor = rows_end;
+    LVG_CUDA(cudaMemsetAsync(g->upd.p, 0, UPD_SLOTS * 8, s));
     LVG_CUDA(cudaStreamSynchronize(s));  // the scratch is freed next
   }
   g->ctr.ensure(1);
@@ -955,8 +960,7 @@ void relayout(lvg_graph *g, size_t need) {
   g->base.w = g->w.p;
   g->slots = slots;
   g->pool_begin = rows_end;
-  g->hupd.p[UPD_POOL] = rows_end;
-  LVG_CUDA(cudaMemcpyAsync(g->upd.p + UPD_POOL, g->hupd.p + UPD_POOL, sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+  g->pool_cursor = rows_end;
 }
 
 // Tidy and apply a planned batch (plan_device's lists and rows). The kept
@@ -970,37 +974,58 @@ void apply_plan(lvg_graph *g, const PlanCounts &pc) {
   if (!nrows) return;
   cudaStream_t s = g->stream;
   Level &b = g->base;
-  g->u_bound.ensure(nrows);
-  g->u_spos.ensure(nrows + 1);
-  g->u_scan.ensure(scan_scratch_elems(nrows));
-  launch_row_bounds(g->deg.p, rows, nrows, g->u_bound.p, s);
-  exclusive_scan_u64(g->u_bound.p, g->u_spos.p, nrows, g->u_spos.p + nrows, g->u_scan.p, s);
-  LVG_CUDA(cudaMemcpyAsync(g->hupd.p, g->upd.p, UPD_SLOTS * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
-  LVG_CUDA(cudaMemcpyAsync(g->hupd.p + UPD_SLOTS, g->u_spos.p + nrows, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
-  LVG_CUDA(cudaStreamSynchronize(s));
-  const size_t T = g->hupd.p[UPD_SLOTS];
-  // worst case of what commit takes from the pool: every touched row moves
-  const size_t need = T + T / 8 + 4 * nrows;
-  if (g->slots - g->hupd.p[UPD_POOL] < need) relayout(g, need);
-  g->u_skey.ensure(T);
-  g->u_sw.ensure(T);
   g->u_pre.ensure(nd + ni);
   g->u_keep.ensure(nd + ni);
-  g->u_newdeg.ensure(nrows);
+  g->u_plan.ensure(nrows);
+  g->u_len.ensure(nrows); g->u_src.ensure(nrows); g->u_grow.ensure(nrows);
+  g->u_spos.ensure(nrows + 1); g->u_srcpos.ensure(nrows + 1); g->u_gpos.ensure(nrows + 1);
+  g->u_scan.ensure(scan_scratch_elems(nrows + 1));
+  g->u_wdelta.ensure(1);
   uint8_t *ex = b.ex ? g->ex.p : nullptr;
-  LVG_CUDA(cudaMemsetAsync(g->upd.p + UPD_EDGES, 0, (UPD_SLOTS - UPD_EDGES) * sizeof(uint64_t), s));
-  launch_merge_rows(g->off.p, g->deg.p, g->key.p, g->w.p, rows, nrows, dd, id, iw, nd, g->u_pre.p, g->u_keep.p,
-                    g->u_spos.p, g->u_skey.p, g->u_sw.p, g->u_newdeg.p, ex, g->upd.p, s);
-  launch_commit_rows(g->off.p, g->deg.p, g->cap.p, g->key.p, g->w.p, rows, nrows, g->u_spos.p, g->u_skey.p,
-                     g->u_sw.p, g->u_newdeg.p, g->upd.p, g->slots, s);
-  if (ex) launch_count_present(ex, b.span, g->upd.p, s);
-  launch_total_weight(g->w.p, g->slots, g->ctr.p, s);
-  LVG_CUDA(cudaMemcpyAsync(g->hupd.p, g->upd.p, UPD_SLOTS * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
-  read_counters(g);  // synchronises
-  if (g->hupd.p[UPD_ERR]) throw Error(LVG_ECUDA, "batch apply: overflow pool exhausted (internal sizing error)");
-  b.edges = size_t((long long)b.edges + (long long)g->hupd.p[UPD_EDGES]);
+  uint64_t T = 0, SRC = 0, GROW = 0;
+  for (int attempt = 0;; ++attempt) {
+    LVG_CUDA(cudaMemsetAsync(g->upd.p, 0, UPD_SLOTS * sizeof(uint64_t), s));
+    LVG_CUDA(cudaMemsetAsync(g->u_wdelta.p, 0, sizeof(double), s));
+    launch_row_plan(g->off.p, g->deg.p, g->cap.p, g->key.p, g->w.p, rows, nrows, dd, id, iw, nd, g->u_pre.p,
+                    g->u_keep.p, g->u_plan.p, g->u_len.p, g->u_src.p, g->u_grow.p, ex, g->upd.p, g->u_wdelta.p, s);
+    exclusive_scan_u64(g->u_len.p, g->u_spos.p, nrows, g->u_spos.p + nrows, g->u_scan.p, s);
+    exclusive_scan_u64(g->u_src.p, g->u_srcpos.p, nrows, g->u_srcpos.p + nrows, g->u_scan.p, s);
+    exclusive_scan_u64(g->u_grow.p, g->u_gpos.p, nrows, g->u_gpos.p + nrows, g->u_scan.p, s);
+    unsigned long long *h = g->hupd.p;
+    LVG_CUDA(cudaMemcpyAsync(h, g->upd.p, UPD_SLOTS * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    LVG_CUDA(cudaMemcpyAsync(h + 3, g->u_spos.p + nrows, 8, cudaMemcpyDeviceToHost, s));
+    LVG_CUDA(cudaMemcpyAsync(h + 4, g->u_srcpos.p + nrows, 8, cudaMemcpyDeviceToHost, s));
+    LVG_CUDA(cudaMemcpyAsync(h + 5, g->u_gpos.p + nrows, 8, cudaMemcpyDeviceToHost, s));
+    LVG_CUDA(cudaMemcpyAsync(h + 6, g->u_wdelta.p, 8, cudaMemcpyDeviceToHost, s));
+    LVG_CUDA(cudaStreamSynchronize(s));
+    T = h[3];
+    SRC = h[4];
+    GROW = h[5];
+    if (g->slots - g->pool_cursor >= GROW) break;
+    if (attempt) throw Error(LVG_ECUDA, "batch apply: the re-laid-out pool is too small (internal sizing error)");
+    relayout(g, GROW);  // fresh capacities: plan again
+  }
+  const long long edge_delta = (long long)g->hupd.p[UPD_EDGES];
+  double wdelta;
+  std::memcpy(&wdelta, &g->hupd.p[6], sizeof(double));
+  g->u_skey.ensure(T);
+  g->u_sw.ensure(T);
+  const uint64_t pool = g->pool_cursor;
+  launch_merge_items(g->off.p, g->deg.p, g->key.p, g->w.p, rows, nrows, dd, id, iw, nd, g->u_pre.p, g->u_keep.p,
+                     g->u_plan.p, g->u_srcpos.p, SRC, g->u_spos.p, g->u_skey.p, g->u_sw.p, s);
+  launch_copy_items(g->off.p, rows, nrows, g->u_plan.p, g->u_spos.p, T, g->u_grow.p, g->u_gpos.p, pool, g->u_skey.p,
+                    g->u_sw.p, g->key.p, g->w.p, s);
+  launch_finish_rows(g->off.p, g->deg.p, g->cap.p, g->key.p, g->w.p, rows, nrows, g->u_plan.p, g->u_grow.p,
+                     g->u_gpos.p, pool, s);
+  g->pool_cursor += GROW;
+  if (ex) {
+    launch_count_present(ex, b.span, g->upd.p, s);
+    LVG_CUDA(cudaMemcpyAsync(g->hupd.p + UPD_ORDER, g->upd.p + UPD_ORDER, 8, cudaMemcpyDeviceToHost, s));
+  }
+  LVG_CUDA(cudaStreamSynchronize(s));
+  b.edges = size_t((long long)b.edges + edge_delta);
   if (ex) b.order = g->hupd.p[UPD_ORDER];
-  g->total_weight = g->hctr.p->fp64[0];
+  g->total_weight += wdelta;
   // degrees changed: new bins and hub plan; the captured iteration is stale
   if (g->iter_exec) {
     cudaGraphExecDestroy(g->iter_exec);
@@ -1012,31 +1037,29 @@ void apply_plan(lvg_graph *g, const PlanCounts &pc) {
   build_hub_plan(g, b, g->hubplan);
 }
 
-// Plan, apply and compact the tidied batch into (tds.., tis..): what
-// main.cxx:108-109 does on the host, here in HBM. Returns the tidied counts
-// and the plan's longest insertion run.
+// Plan, apply and compact the tidied batch into (tds.., tis..), arrays with
+// room for nd / ni entries that may be the input arrays themselves (the plan
+// has copied them before the compaction writes): what main.cxx:108-109 does
+// on the host, here in HBM. Returns the tidied counts and the plan's longest
+// insertion run.
 PlanCounts tidy_apply(lvg_graph *g, const uint32_t *ds, const uint32_t *dd, const float *dw, size_t nd,
-                      const uint32_t *is, const uint32_t *id, const float *iw, size_t ni, DBuf<uint32_t> &tds,
-                      DBuf<uint32_t> &tdd, DBuf<float> &tdw, DBuf<uint32_t> &tis, DBuf<uint32_t> &tid,
-                      DBuf<float> &tiw) {
+                      const uint32_t *is, const uint32_t *id, const float *iw, size_t ni, uint32_t *tds,
+                      uint32_t *tdd, float *tdw, uint32_t *tis, uint32_t *tid, float *tiw) {
   if (!g->rows_sorted) throw Error(LVG_EINVAL, "batch apply needs rows sorted by neighbour id");
   if (nd > 0x7FFFFFFFull || ni > 0x7FFFFFFFull) throw Error(LVG_EINVAL, "batch apply: more than 2^31-1 entries");
   cudaStream_t s = g->stream;
   PlanCounts pc = plan_device(g, ds, dd, dw, nd, is, id, iw, ni);
   apply_plan(g, pc);
   const size_t n = pc.nd + pc.ni;
-  tds.ensure(pc.nd); tdd.ensure(pc.nd); tdw.ensure(pc.nd);
-  tis.ensure(pc.ni); tid.ensure(pc.ni); tiw.ensure(pc.ni);
   PlanCounts out;
   out.max_group = pc.max_group;
   if (n && pc.nrows) {
     g->u_pos.ensure(n + 1);
     g->u_pscan.ensure(scan_scratch_elems(n + 1));
     exclusive_scan_u32(g->u_keep.p, g->u_pos.p, n, g->u_pos.p + n, g->u_pscan.p, s);
-    launch_tidy_compact(g->u_ds.p, g->u_dd.p, g->u_dw.p, pc.nd, g->u_keep.p, g->u_pos.p, nullptr, tds.p, tdd.p,
-                        tdw.p, s);
+    launch_tidy_compact(g->u_ds.p, g->u_dd.p, g->u_dw.p, pc.nd, g->u_keep.p, g->u_pos.p, nullptr, tds, tdd, tdw, s);
     launch_tidy_compact(g->u_is.p, g->u_id.p, g->u_iw.p, pc.ni, g->u_keep.p + pc.nd, g->u_pos.p + pc.nd,
-                        g->u_pos.p + pc.nd, tis.p, tid.p, tiw.p, s);
+                        g->u_pos.p + pc.nd, tis, tid, tiw, s);
     g->hcnt.ensure(4);
     LVG_CUDA(cudaMemcpyAsync(g->hcnt.p, g->u_pos.p + pc.nd, 4, cudaMemcpyDeviceToHost, s));
     LVG_CUDA(cudaMemcpyAsync(g->hcnt.p + 1, g->u_pos.p + n, 4, cudaMemcpyDeviceToHost, s));
@@ -1095,6 +1118,7 @@ int lvg_graph_create(size_t span, const uint64_t *offsets, const uint32_t *keys,
       if (i > offsets[u] && keys[i] <= keys[i - 1]) rows_sorted = false;
     }
   std::unique_ptr<lvg_graph> g(new lvg_graph());
+  lvg::AcctScope acct_(&g->bytes);
   int rc = lvg::guarded([&] {
     LVG_CUDA(cudaGetDevice(&g->device));
     LVG_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
@@ -1131,6 +1155,7 @@ namespace {
 int create_generated(const GenSpec &spec, lvg_graph **out) {
   *out = nullptr;
   std::unique_ptr<lvg_graph> g(new lvg_graph());
+  AcctScope acct_(&g->bytes);
   int rc = guarded([&] {
     LVG_CUDA(cudaGetDevice(&g->device));
     LVG_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
@@ -1196,6 +1221,41 @@ int lvg_graph_destroy(lvg_graph *g) {
   return LVG_OK;
 }
 
+size_t lvg_graph_device_bytes(const lvg_graph *g) { return g ? g->bytes : 0; }
+size_t lvg_state_device_bytes(const lvg_state *st) { return st ? st->bytes : 0; }
+size_t lvg_device_batch_device_bytes(const lvg_device_batch *b) { return b ? b->bytes : 0; }
+
+int lvg_graph_trim(lvg_graph *g, int level) {
+  if (!g || level < 1 || level > 2) return lvg::fail(LVG_EINVAL, "lvg_graph_trim: bad argument");
+  return lvg::guarded([&] {
+    LVG_CUDA(cudaSetDevice(g->device));
+    LVG_CUDA(cudaStreamSynchronize(g->stream));
+    if (g->iter_exec) {  // the captured iteration refers to the buffers released below
+      cudaGraphExecDestroy(g->iter_exec);
+      g->iter_exec = nullptr;
+    }
+    if (g->ws) {
+      lvg::Workspace &W = *g->ws;
+      W.gkeys.release(); W.gvals.release();
+      W.part_key.release(); W.part_val.release(); W.chunk_cnt.release();
+    }
+    for (auto *d : {&g->u_k0, &g->u_k1, &g->u_len, &g->u_src, &g->u_grow, &g->u_spos, &g->u_srcpos, &g->u_gpos,
+                    &g->u_scan})
+      d->release();
+    for (auto *d : {&g->u_skey, &g->u_pre, &g->u_keep, &g->u_pos, &g->u_pscan, &g->u_v0, &g->u_v1,
+                    &g->u_flag, &g->u_touch, &g->u_tpos, &g->u_tscan, &g->u_cnt, &g->u_ds, &g->u_dd, &g->u_is,
+                    &g->u_id, &g->b_ds, &g->b_dd, &g->b_is, &g->b_id, &g->b_seg})
+      d->release();
+    for (auto *d : {&g->u_sw, &g->u_dw, &g->u_iw, &g->b_dw, &g->b_iw}) d->release();
+    g->u_tmp.release();
+    g->u_rows.release();
+    g->u_plan.release();
+    g->u_wdelta.release();
+    if (level == 2) g->ws.reset();
+    return LVG_OK;
+  });
+}
+
 size_t lvg_graph_span(const lvg_graph *g) { return g ? g->base.span : 0; }
 size_t lvg_graph_order(const lvg_graph *g) { return g ? g->base.order : 0; }
 size_t lvg_graph_size(const lvg_graph *g) { return g ? g->base.edges : 0; }
@@ -1237,6 +1297,7 @@ int lvg_edge_weight(lvg_graph *g, double *out) {
 }
 
 int lvg_modularity(lvg_graph *g, const uint32_t *membership, double M, double R, double *out) {
+  lvg::AcctScope acct_(g ? &g->bytes : nullptr);
   if (!g || !membership || !out) return lvg::fail(LVG_EINVAL, "null argument");
   return lvg::guarded([&] {
     LVG_CUDA(cudaSetDevice(g->device));
@@ -1261,6 +1322,7 @@ int lvg_modularity(lvg_graph *g, const uint32_t *membership, double M, double R,
 int lvg_affected_vertices(lvg_graph *y, int method, const lvg_batch *b, const uint32_t *q, const double *qvtot,
                           const double *qctot, const lvg_options *o, uint8_t *flags, uint8_t *neighbors,
                           uint8_t *communities) {
+  lvg::AcctScope acct_(y ? &y->bytes : nullptr);
   if (!y || !flags || method < 0 || method > 3) return lvg::fail(LVG_EINVAL, "bad argument");
   return lvg::guarded([&] {
     LVG_CUDA(cudaSetDevice(y->device));
@@ -1294,6 +1356,7 @@ int lvg_affected_vertices(lvg_graph *y, int method, const lvg_batch *b, const ui
 
 int lvg_aggregate(lvg_graph *g, const uint32_t *membership, uint32_t *renumbered, size_t *num_communities,
                   uint64_t *offsets, uint32_t *keys, double *weights) {
+  lvg::AcctScope acct_(g ? &g->bytes : nullptr);
   if (!g || !membership || !renumbered || !num_communities || !offsets) return lvg::fail(LVG_EINVAL, "null argument");
   return lvg::guarded([&] {
     LVG_CUDA(cudaSetDevice(g->device));
@@ -1384,6 +1447,7 @@ int lvg_state_create(lvg_graph *g, lvg_state **out) {
   if (!g || !out) return lvg::fail(LVG_EINVAL, "null argument");
   *out = nullptr;
   std::unique_ptr<lvg_state> st(new lvg_state());
+  lvg::AcctScope acct_(&st->bytes);
   int rc = lvg::guarded([&] {
     LVG_CUDA(cudaSetDevice(g->device));
     const size_t S = g->base.span;
@@ -1448,6 +1512,7 @@ int lvg_device_batch_create(lvg_graph *g, const lvg_batch *b, lvg_device_batch *
   if (!g || !b || !out) return lvg::fail(LVG_EINVAL, "null argument");
   *out = nullptr;
   std::unique_ptr<lvg_device_batch> db(new lvg_device_batch());
+  lvg::AcctScope acct_(&db->bytes);
   int rc = lvg::guarded([&] {
     LVG_CUDA(cudaSetDevice(g->device));
     lvg::check_batch(g, b, false);
@@ -1466,6 +1531,7 @@ int lvg_device_batch_create(lvg_graph *g, const lvg_batch *b, lvg_device_batch *
 }
 
 int lvg_graph_apply_batch(lvg_graph *g, const lvg_batch *b, lvg_batch_buf *tidy) {
+  lvg::AcctScope acct_(g ? &g->bytes : nullptr);
   if (!g) return lvg::fail(LVG_EINVAL, "null graph");
   if (tidy && b &&
       ((b->num_deletions && (!tidy->del_src || !tidy->del_dst || !tidy->del_w)) ||
@@ -1479,26 +1545,26 @@ int lvg_graph_apply_batch(lvg_graph *g, const lvg_batch *b, lvg_batch_buf *tidy)
     cudaStream_t s = g->stream;
     lvg::DBatch raw;
     lvg::upload_batch(g, b, g->b_ds, g->b_dd, g->b_dw, g->b_is, g->b_id, g->b_iw, g->b_seg, raw);
-    lvg::DBuf<uint32_t> tds, tdd, tis, tid;
-    lvg::DBuf<float> tdw, tiw;
+    // the tidied batch is compacted over the uploaded one (g->b_*)
+    uint32_t *tds = g->b_ds.p, *tdd = g->b_dd.p, *tis = g->b_is.p, *tid = g->b_id.p;
+    float *tdw = g->b_dw.p, *tiw = g->b_iw.p;
     const lvg::PlanCounts t = lvg::tidy_apply(g, raw.ds, raw.dd, raw.dw, raw.nd, raw.is, raw.id, raw.iw, raw.ni,
                                               tds, tdd, tdw, tis, tid, tiw);
     if (tidy) {
       if (t.nd) {
-        LVG_CUDA(cudaMemcpyAsync(tidy->del_src, tds.p, t.nd * 4, cudaMemcpyDeviceToHost, s));
-        LVG_CUDA(cudaMemcpyAsync(tidy->del_dst, tdd.p, t.nd * 4, cudaMemcpyDeviceToHost, s));
-        LVG_CUDA(cudaMemcpyAsync(tidy->del_w, tdw.p, t.nd * 4, cudaMemcpyDeviceToHost, s));
+        LVG_CUDA(cudaMemcpyAsync(tidy->del_src, tds, t.nd * 4, cudaMemcpyDeviceToHost, s));
+        LVG_CUDA(cudaMemcpyAsync(tidy->del_dst, tdd, t.nd * 4, cudaMemcpyDeviceToHost, s));
+        LVG_CUDA(cudaMemcpyAsync(tidy->del_w, tdw, t.nd * 4, cudaMemcpyDeviceToHost, s));
       }
       if (t.ni) {
-        LVG_CUDA(cudaMemcpyAsync(tidy->ins_src, tis.p, t.ni * 4, cudaMemcpyDeviceToHost, s));
-        LVG_CUDA(cudaMemcpyAsync(tidy->ins_dst, tid.p, t.ni * 4, cudaMemcpyDeviceToHost, s));
-        LVG_CUDA(cudaMemcpyAsync(tidy->ins_w, tiw.p, t.ni * 4, cudaMemcpyDeviceToHost, s));
+        LVG_CUDA(cudaMemcpyAsync(tidy->ins_src, tis, t.ni * 4, cudaMemcpyDeviceToHost, s));
+        LVG_CUDA(cudaMemcpyAsync(tidy->ins_dst, tid, t.ni * 4, cudaMemcpyDeviceToHost, s));
+        LVG_CUDA(cudaMemcpyAsync(tidy->ins_w, tiw, t.ni * 4, cudaMemcpyDeviceToHost, s));
       }
       LVG_CUDA(cudaStreamSynchronize(s));
       tidy->num_deletions = t.nd;
       tidy->num_insertions = t.ni;
     }
-    LVG_CUDA(cudaStreamSynchronize(s));  // the tidied copies are freed next
     return LVG_OK;
   });
 }
@@ -1517,16 +1583,11 @@ int lvg_graph_apply_device_batch(lvg_graph *g, lvg_device_batch *b) {
       b->applied = true;
       return LVG_OK;
     }
-    lvg::DBuf<uint32_t> tds, tdd, tis, tid;
-    lvg::DBuf<float> tdw, tiw;
-    const lvg::PlanCounts t = lvg::tidy_apply(g, r.ds, r.dd, r.dw, r.nd, r.is, r.id, r.iw, r.ni, tds, tdd, tdw,
-                                              tis, tid, tiw);
-    LVG_CUDA(cudaStreamSynchronize(s));
-    b->ds.swap(tds); b->dd.swap(tdd); b->dw.swap(tdw);
-    b->is.swap(tis); b->id.swap(tid); b->iw.swap(tiw);
-    b->seg.ensure(t.ni + 1);
-    b->b.ds = b->ds.p; b->b.dd = b->dd.p; b->b.dw = b->dw.p;
-    b->b.is = b->is.p; b->b.id = b->id.p; b->b.iw = b->iw.p; b->b.seg = b->seg.p;
+    // compacted over the batch's own arrays, which the plan has copied
+    lvg::AcctScope acct_(&g->bytes);
+    const lvg::PlanCounts t = lvg::tidy_apply(g, r.ds, r.dd, r.dw, r.nd, r.is, r.id, r.iw, r.ni, b->ds.p, b->dd.p,
+                                              b->dw.p, b->is.p, b->id.p, b->iw.p);
+    (void)s;
     b->b.nd = t.nd;
     b->b.ni = t.ni;
     b->b.max_group = t.max_group;  // an upper bound after the filter
@@ -1571,6 +1632,7 @@ int lvg_device_batch_generate(lvg_graph *g, size_t deletions, size_t insertions,
   if (range == 0 || size_t(begin) + range > g->base.span)
     return lvg::fail(LVG_EINVAL, "lvg_device_batch_generate: [begin, begin+range) outside the span");
   std::unique_ptr<lvg_device_batch> db(new lvg_device_batch());
+  lvg::AcctScope acct_(&db->bytes);
   int rc = lvg::guarded([&] {
     LVG_CUDA(cudaSetDevice(g->device));
     db->g = g;
@@ -1618,6 +1680,23 @@ int lvg_device_batch_size(const lvg_device_batch *b, size_t *deletions, size_t *
   return LVG_OK;
 }
 
+int lvg_device_batch_set(lvg_device_batch *db, const lvg_batch *b) {
+  if (!db || !b) return lvg::fail(LVG_EINVAL, "null argument");
+  lvg_graph *g = db->g;
+  lvg::AcctScope acct_(&db->bytes);
+  return lvg::guarded([&] {
+    LVG_CUDA(cudaSetDevice(g->device));
+    lvg::check_batch(g, b, false);
+    lvg::upload_batch(g, b, db->ds, db->dd, db->dw, db->is, db->id, db->iw, db->seg, db->b);
+    bool sorted = true;
+    for (size_t i = 1; i < b->num_insertions; ++i) sorted &= b->ins_src[i] >= b->ins_src[i - 1];
+    if (!sorted) db->b.max_group = ~size_t(0);
+    db->applied = false;
+    LVG_CUDA(cudaStreamSynchronize(g->stream));  // the caller may reuse its arrays
+    return LVG_OK;
+  });
+}
+
 int lvg_device_batch_destroy(lvg_device_batch *b) {
   if (!b) return LVG_OK;
   cudaSetDevice(b->device);
@@ -1627,6 +1706,7 @@ int lvg_device_batch_destroy(lvg_device_batch *b) {
 
 int lvg_run_resident(lvg_graph *g, int method, const lvg_device_batch *b, const lvg_state *prior, lvg_state *out,
                      const lvg_options *o, lvg_result *info) {
+  lvg::AcctScope acct_(g ? &g->bytes : nullptr);
   if (!g || !out || method < 0 || method > 3) return lvg::fail(LVG_EINVAL, "bad argument");
   if (method != LVG_METHOD_STATIC && !prior) return lvg::fail(LVG_EINVAL, "dynamic methods need a prior state");
   if ((b && b->g != g) || (prior && prior->g != g) || out->g != g)

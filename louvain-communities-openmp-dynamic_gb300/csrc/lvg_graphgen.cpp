@@ -333,6 +333,228 @@ int lvgg_reference_batch(const lvgg_csr *x, size_t deletions, size_t insertions,
   return 0;
 }
 
+// ------------------------------------------------------------ temporal
+
+}  // extern "C"
+
+struct lvgg_temporal {
+  std::FILE *f = nullptr;
+  int weighted = 0;
+  std::vector<char> buf;
+};
+
+namespace {
+
+// "u v [w] ..." -> true when at least u and v parse (strtoull/strtod as
+// readTemporalDoOmp parses, inc/snap.hxx:85-90).
+bool parse_line(const char *line, int weighted, uint64_t &u, uint64_t &v, double &w) {
+  char *e = nullptr;
+  u = std::strtoull(line, &e, 10);
+  if (e == line) return false;
+  const char *p = e;
+  v = std::strtoull(p, &e, 10);
+  if (e == p) return false;
+  w = 1;
+  if (weighted) {
+    p = e;
+    double x = std::strtod(p, &e);
+    if (e != p && x != 0) w = x;
+  }
+  return true;
+}
+
+void edges_alloc(lvgg_edges *e, size_t n) {
+  e->n = n;
+  e->src = xalloc<uint32_t>(n);
+  e->dst = xalloc<uint32_t>(n);
+  e->w = xalloc<float>(n);
+}
+
+}  // namespace
+
+extern "C" {
+
+void lvgg_edges_free(lvgg_edges *e) {
+  if (!e) return;
+  std::free(e->src);
+  std::free(e->dst);
+  std::free(e->w);
+  std::memset(e, 0, sizeof(*e));
+}
+
+int lvgg_temporal_open(const char *path, int weighted, lvgg_temporal **out) {
+  if (!path || !out) return fail(-EINVAL, "lvgg_temporal_open: bad argument");
+  *out = nullptr;
+  std::FILE *f = std::fopen(path, "r");
+  if (!f) return fail(-ENOENT, "lvgg_temporal_open: cannot open the file");
+  lvgg_temporal *t = new (std::nothrow) lvgg_temporal();
+  if (!t) {
+    std::fclose(f);
+    return fail(-ENOMEM, "lvgg_temporal_open: out of memory");
+  }
+  t->f = f;
+  t->weighted = weighted;
+  t->buf.resize(1 << 16);
+  *out = t;
+  return 0;
+}
+
+int lvgg_temporal_read(lvgg_temporal *t, size_t lines, int symmetric, lvgg_edges *out) {
+  if (!t || !out) return fail(-EINVAL, "lvgg_temporal_read: bad argument");
+  std::memset(out, 0, sizeof(*out));
+  try {
+    std::vector<uint32_t> s, d;
+    std::vector<float> w;
+    for (size_t i = 0; i < lines; ++i) {
+      if (!std::fgets(t->buf.data(), int(t->buf.size()), t->f)) break;
+      uint64_t u, v;
+      double x;
+      if (!parse_line(t->buf.data(), t->weighted, u, v, x)) break;
+      if (u > 0xFFFFFFFEull || v > 0xFFFFFFFEull) return fail(-EINVAL, "lvgg_temporal_read: id does not fit 32 bits");
+      s.push_back(uint32_t(u)); d.push_back(uint32_t(v)); w.push_back(float(x));
+      if (symmetric) { s.push_back(uint32_t(v)); d.push_back(uint32_t(u)); w.push_back(float(x)); }
+    }
+    edges_alloc(out, s.size());
+    std::copy(s.begin(), s.end(), out->src);
+    std::copy(d.begin(), d.end(), out->dst);
+    std::copy(w.begin(), w.end(), out->w);
+  } catch (const std::bad_alloc &) {
+    lvgg_edges_free(out);
+    return fail(-ENOMEM, "lvgg_temporal_read: out of memory");
+  }
+  return 0;
+}
+
+void lvgg_temporal_close(lvgg_temporal *t) {
+  if (!t) return;
+  if (t->f) std::fclose(t->f);
+  delete t;
+}
+
+int lvgg_temporal_write(const char *path, const lvgg_edges *e) {
+  if (!path || !e) return fail(-EINVAL, "lvgg_temporal_write: bad argument");
+  std::FILE *f = std::fopen(path, "w");
+  if (!f) return fail(-ENOENT, "lvgg_temporal_write: cannot create the file");
+  for (size_t i = 0; i < e->n; ++i) std::fprintf(f, "%u %u %zu\n", e->src[i], e->dst[i], i);
+  return std::fclose(f) == 0 ? 0 : fail(-EIO, "lvgg_temporal_write: write failed");
+}
+
+int lvgg_csr_from_edges(size_t rows, const lvgg_edges *e, lvgg_csr *out) {
+  if (!e || !out || rows >= 0xFFFFFFFFull) return fail(-EINVAL, "lvgg_csr_from_edges: bad argument");
+  std::memset(out, 0, sizeof(*out));
+  const size_t S = rows + 1;
+  for (size_t i = 0; i < e->n; ++i)
+    if (e->src[i] >= S || e->dst[i] >= S) return fail(-EINVAL, "lvgg_csr_from_edges: id > rows");
+  try {
+    // per source, in stream order; then sort by target keeping the last of equal targets
+    std::vector<uint64_t> cnt(S + 1, 0);
+    for (size_t i = 0; i < e->n; ++i) ++cnt[e->src[i] + 1];
+    for (size_t u = 0; u < S; ++u) cnt[u + 1] += cnt[u];
+    std::vector<uint64_t> cur(cnt.begin(), cnt.end() - 1);
+    std::vector<uint64_t> idx(e->n);
+    for (size_t i = 0; i < e->n; ++i) idx[cur[e->src[i]]++] = i;
+    std::vector<uint64_t> deg(S, 0);
+    #pragma omp parallel for schedule(dynamic, 1024)
+    for (size_t u = 0; u < S; ++u) {
+      uint64_t *b = idx.data() + cnt[u], *f = idx.data() + cnt[u + 1];
+      std::stable_sort(b, f, [&](uint64_t a, uint64_t c) { return e->dst[a] < e->dst[c]; });
+      size_t m = 0;
+      for (uint64_t *p = b; p < f; ++p) {
+        if (m && e->dst[b[m - 1]] == e->dst[*p]) b[m - 1] = *p;  // the last duplicate wins
+        else b[m++] = *p;
+      }
+      deg[u] = m;
+    }
+    out->span = S;
+    out->offsets = xalloc<uint64_t>(S + 1);
+    out->offsets[0] = 0;
+    for (size_t u = 0; u < S; ++u) out->offsets[u + 1] = out->offsets[u] + deg[u];
+    out->num_edges = out->offsets[S];
+    out->keys = xalloc<uint32_t>(out->num_edges);
+    out->weights = xalloc<float>(out->num_edges);
+    out->exists = xalloc<uint8_t>(S);
+    #pragma omp parallel for schedule(dynamic, 1024)
+    for (size_t u = 0; u < S; ++u) {
+      for (uint64_t j = 0; j < deg[u]; ++j) {
+        const uint64_t i = idx[cnt[u] + j];
+        out->keys[out->offsets[u] + j] = e->dst[i];
+        out->weights[out->offsets[u] + j] = e->w[i];
+      }
+      out->exists[u] = u > 0;  // vertices 1..rows (addVerticesIfU, inc/snap.hxx:167)
+    }
+    for (size_t i = 0; i < e->n; ++i) out->exists[e->src[i]] = out->exists[e->dst[i]] = 1;
+  } catch (const std::bad_alloc &) {
+    lvgg_csr_free(out);
+    return fail(-ENOMEM, "lvgg_csr_from_edges: out of memory");
+  }
+  return 0;
+}
+
+int lvgg_temporal_drift(uint32_t n, uint32_t communities, double sigma, size_t edges, double p_in,
+                        size_t drift_every, double drift, uint64_t seed, lvgg_edges *out) {
+  if (!out || n == 0 || communities == 0 || communities > n || sigma < 0 || p_in < 0 || p_in > 1 || drift < 0 ||
+      drift > 1)
+    return fail(-EINVAL, "lvgg_temporal_drift: bad argument");
+  std::memset(out, 0, sizeof(*out));
+  try {
+    // community sizes ~ log-normal(0, sigma), scaled to n; vertices assigned in id order
+    std::vector<double> wsz(communities);
+    double tot = 0;
+    for (uint32_t c = 0; c < communities; ++c) {
+      Rng r(seed, 8, c);
+      const double u1 = std::max(r.uniform(), 1e-300), u2 = r.uniform();
+      const double z = std::sqrt(-2 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+      wsz[c] = std::exp(sigma * z);
+      tot += wsz[c];
+    }
+    std::vector<uint32_t> com(size_t(n) + 1, 0);
+    std::vector<std::vector<uint32_t>> members(communities);
+    uint32_t v = 1;
+    double acc = 0;
+    for (uint32_t c = 0; c < communities && v <= n; ++c) {
+      acc += wsz[c];
+      const uint32_t end = (c + 1 == communities) ? n : uint32_t(std::min<double>(n, std::llround(acc / tot * n)));
+      for (; v <= end; ++v) { com[v] = c; members[c].push_back(v); }
+      if (members[c].empty() && v <= n) { com[v] = c; members[c].push_back(v); ++v; }
+    }
+    edges_alloc(out, edges);
+    size_t e = 0;
+    for (size_t epoch = 0; e < edges; ++epoch) {
+      const size_t end = std::min(edges, e + (drift_every ? drift_every : edges));
+      #pragma omp parallel for schedule(static)
+      for (size_t i = e; i < end; ++i) {
+        Rng r(seed, 9, i);
+        const uint32_t a = 1 + uint32_t(r.below(n));
+        uint32_t b;
+        const std::vector<uint32_t> &m = members[com[a]];
+        if (r.uniform() < p_in && m.size() > 1) b = m[r.below(m.size())];
+        else b = 1 + uint32_t(r.below(n));
+        out->src[i] = a;
+        out->dst[i] = b;
+        out->w[i] = 1.0f;
+      }
+      e = end;
+      if (drift > 0 && e < edges) {  // a fraction of the vertices changes community
+        Rng r(seed, 10, epoch);
+        const size_t moves = size_t(std::llround(drift * n));
+        for (size_t k = 0; k < moves; ++k) {
+          const uint32_t x = 1 + uint32_t(r.below(n));
+          const uint32_t c = uint32_t(r.below(communities));
+          if (c == com[x]) continue;
+          auto &old = members[com[x]];
+          old.erase(std::find(old.begin(), old.end(), x));
+          members[c].push_back(x);
+          com[x] = c;
+        }
+      }
+    }
+  } catch (const std::bad_alloc &) {
+    lvgg_edges_free(out);
+    return fail(-ENOMEM, "lvgg_temporal_drift: out of memory");
+  }
+  return 0;
+}
+
 int lvgg_apply_batch(const lvgg_csr *x, const lvgg_batch *b, lvgg_csr *y) {
   if (!x || !b || !y) return fail(-EINVAL, "lvgg_apply_batch: bad argument");
   std::memset(y, 0, sizeof(*y));

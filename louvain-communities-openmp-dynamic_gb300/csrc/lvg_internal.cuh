@@ -8,11 +8,29 @@
 
 namespace lvg {
 
+// Device bytes are counted per owner (a graph with its workspace, a state, a
+// device batch): a C-ABI call names the owner for the duration of the call
+// (AcctScope) and every buffer allocated meanwhile adds to, and on release
+// subtracts from, that owner's counter. One owner is used by one thread at a
+// time (calls on one handle are not concurrent).
+inline size_t *&acct_target() {
+  static thread_local size_t *t = nullptr;
+  return t;
+}
+struct AcctScope {
+  size_t *prev;
+  explicit AcctScope(size_t *t) : prev(acct_target()) { acct_target() = t; }
+  ~AcctScope() { acct_target() = prev; }
+  AcctScope(const AcctScope &) = delete;
+  AcctScope &operator=(const AcctScope &) = delete;
+};
+
 // Device buffer that grows on demand (contents are not kept when it grows).
 template <class T>
 struct DBuf {
   T *p = nullptr;
   size_t n = 0;
+  size_t *acct = nullptr;  // owner's byte counter (see AcctScope)
   DBuf() = default;
   DBuf(const DBuf &) = delete;
   DBuf &operator=(const DBuf &) = delete;
@@ -23,15 +41,22 @@ struct DBuf {
     if (k == 0) k = 1;
     LVG_CUDA(cudaMalloc(&p, k * sizeof(T)));
     n = k;
+    acct = acct_target();
+    if (acct) *acct += n * sizeof(T);
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      cudaFree(p);
+      if (acct) *acct -= n * sizeof(T);
+    }
     p = nullptr;
     n = 0;
+    acct = nullptr;
   }
   void swap(DBuf &o) {
     std::swap(p, o.p);
     std::swap(n, o.n);
+    std::swap(acct, o.acct);
   }
 };
 
@@ -57,7 +82,7 @@ struct HBuf {  // pinned host buffer, grows on demand
 // level: each hub's edge list is cut into chunks of HUB_CHUNK edges that
 // different blocks aggregate at once; a second kernel merges a hub's chunks.
 // Hubs are ordered by colour class; chunks by hub.
-constexpr uint32_t HUB_CHUNK = 8192;
+constexpr uint32_t HUB_CHUNK = 16384;
 struct HubPlan {
   size_t hubs = 0, chunks = 0, part = 0;        // counts; part = partial-entry capacity
   size_t hub_begin[MAX_COLORS + 1] = {};        // hubs of colour k: [hub_begin[k], hub_begin[k+1])
@@ -244,23 +269,35 @@ struct UpdRow {
 // Row capacity of the gapped layout for a row of degree d.
 __host__ __device__ inline uint32_t row_capacity(uint32_t d) { return d + (d >> 3) + 4; }
 // Slots of the batch-apply counters.
-constexpr int UPD_POOL = 0;   // overflow-pool cursor (absolute entry index)
-constexpr int UPD_EDGES = 1;  // change of the edge count (two's complement)
-constexpr int UPD_ERR = 2;    // 1: the overflow pool ran out
-constexpr int UPD_ORDER = 3;  // present vertices after the batch
-constexpr int UPD_MAXG = 4;   // longest run of insertions sharing a source
-constexpr int UPD_SLOTS = 5;
+constexpr int UPD_EDGES = 0;  // change of the edge count (two's complement)
+constexpr int UPD_ORDER = 1;  // present vertices after the batch
+constexpr int UPD_MAXG = 2;   // longest run of insertions sharing a source
+constexpr int UPD_SLOTS = 3;
 void launch_row_caps(const uint64_t *coff, size_t n, uint32_t *deg, uint32_t *cap, uint64_t *cap64, cudaStream_t s);
 void launch_spread_rows(const uint64_t *coff, const uint32_t *ckey, const float *cw, size_t n, const uint64_t *off,
                         const uint32_t *cap, uint32_t *key, float *w, cudaStream_t s);
-void launch_row_bounds(const uint32_t *deg, const UpdRow *rows, size_t nrows, uint64_t *bound, cudaStream_t s);
-void launch_merge_rows(const uint64_t *off, const uint32_t *deg, const uint32_t *key, const float *w,
-                       const UpdRow *rows, size_t nrows, const uint32_t *dd, const uint32_t *id, const float *iw,
-                       size_t nd_all, uint32_t *pre, uint32_t *keep, const uint64_t *spos, uint32_t *skey,
-                       float *sw, uint32_t *newdeg, uint8_t *ex, unsigned long long *upd, cudaStream_t s);
-void launch_commit_rows(uint64_t *off, uint32_t *deg, uint32_t *cap, uint32_t *key, float *w, const UpdRow *rows,
-                        size_t nrows, const uint64_t *spos, const uint32_t *skey, const float *sw,
-                        const uint32_t *newdeg, unsigned long long *upd, unsigned long long pool_end, cudaStream_t s);
+// Per touched row: new degree, first changed old index (0 when the row
+// moves to the pool), kept deletions and insertions.
+struct RowPlan {
+  uint32_t n1, f0, dcarry, icarry;
+};
+void launch_row_plan(const uint64_t *off, const uint32_t *deg, const uint32_t *cap, const uint32_t *key,
+                     const float *w, const UpdRow *rows, size_t nrows, const uint32_t *dd, const uint32_t *id,
+                     const float *iw, size_t nd_all, uint32_t *pre, uint32_t *keep, RowPlan *plan, uint64_t *len,
+                     uint64_t *src, uint64_t *grow, uint8_t *ex, unsigned long long *upd, double *wdelta,
+                     cudaStream_t s);
+void launch_merge_items(const uint64_t *off, const uint32_t *deg, const uint32_t *key, const float *w,
+                        const UpdRow *rows, size_t nrows, const uint32_t *dd, const uint32_t *id, const float *iw,
+                        size_t nd_all, const uint32_t *pre, const uint32_t *keep, const RowPlan *plan,
+                        const uint64_t *src, uint64_t total, const uint64_t *spos, uint32_t *skey, float *sw,
+                        cudaStream_t s);
+void launch_copy_items(const uint64_t *off, const UpdRow *rows, size_t nrows, const RowPlan *plan,
+                       const uint64_t *spos, uint64_t total, const uint64_t *grow, const uint64_t *gpos,
+                       uint64_t pool, const uint32_t *skey, const float *sw, uint32_t *key, float *w,
+                       cudaStream_t s);
+void launch_finish_rows(uint64_t *off, uint32_t *deg, uint32_t *cap, uint32_t *key, float *w, const UpdRow *rows,
+                        size_t nrows, const RowPlan *plan, const uint64_t *grow, const uint64_t *gpos,
+                        uint64_t pool, cudaStream_t s);
 void launch_count_present(const uint8_t *ex, size_t span, unsigned long long *upd, cudaStream_t s);
 void launch_tidy_compact(const uint32_t *src, const uint32_t *dst, const float *w, size_t n, const uint32_t *keep,
                          const uint32_t *pos, const uint32_t *pos_base, uint32_t *osrc, uint32_t *odst, float *ow,
@@ -317,5 +354,8 @@ inline int global_table_log2(uint64_t maxdeg) {
   return l;
 }
 int global_table_blocks(size_t count);
+// Grid of the local-moving kernel of a large-degree bin (9, 10; 11 = the hub
+// merge) for `count` vertices: the size of its per-block global fallback.
+int move_grid_blocks(int bin, bool sync, size_t count);
 
 }  // namespace lvg

@@ -24,6 +24,8 @@
 // totals and flags in place. Deterministic mode only records each vertex's
 // decision (dec[u]) and its neighbour marks (mark[]); the caller applies the
 // decisions of a colour class after all of them were taken.
+#include <algorithm>
+
 #include "lvg_internal.cuh"
 
 namespace lvg {
@@ -736,32 +738,55 @@ void launch_tile(const MoveArgs &a, cudaStream_t s) {
   LVG_CHECK_LAUNCH();
 }
 
+// Block size and shared-table size (log2 slots) of the large-degree kernels.
+// Tables of 2^11 slots (a 1024-community claim budget before the global
+// fallback) keep several blocks resident per SM; after the first iterations
+// a high-degree vertex's neighbours fall into few communities.
+constexpr int BIG9_B = 256, BIG9_LOGS = 11;     // degree 513-2048
+constexpr int BIG10_B = 256, BIG10_LOGS = 11;   // degree 2049-8192
+constexpr int HUBC_B = 512, HUBC_LOGS = 11;     // hub chunks (HUB_CHUNK edges each)
+constexpr int HUBM_B = 512, HUBM_LOGS = 13;     // hub merge
+
+// Resident blocks of a large-degree kernel on the whole device, queried once.
+template <class K>
+unsigned resident_blocks(K kernel, int block, size_t smem) {
+  int per_sm = 0;
+  LVG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem));
+  return unsigned(std::max(1, per_sm)) * unsigned(num_sms());
+}
+
+template <int B, int LOGS, bool SYNC>
+unsigned big_grid(size_t count) {
+  const size_t smem = (size_t(1) << LOGS) * 10;  // keys, values, claimed list
+  static const unsigned resident = [&] {
+    set_smem(move_big_kernel<B, LOGS, SYNC>, smem);
+    return resident_blocks(move_big_kernel<B, LOGS, SYNC>, B, smem);
+  }();
+  return unsigned(std::min<size_t>(count, resident));
+}
+
 template <int B, int LOGS, bool SYNC>
 void launch_big(const MoveArgs &a, cudaStream_t s) {
-  const size_t smem = (size_t(1) << LOGS) * 10;  // keys, values, claimed list
-  auto k = move_big_kernel<B, LOGS, SYNC>;
-  static bool configured = false;
-  if (!configured) { set_smem(k, smem); configured = true; }
-  unsigned grid = unsigned(global_table_blocks(a.count));
+  const size_t smem = (size_t(1) << LOGS) * 10;
+  const unsigned grid = big_grid<B, LOGS, SYNC>(a.count);
   if (!grid) return;
-  k<<<grid, B, smem, s>>>(a);
+  move_big_kernel<B, LOGS, SYNC><<<grid, B, smem, s>>>(a);
   LVG_CHECK_LAUNCH();
 }
 
 template <bool SYNC>
 void launch_hubs(const MoveArgs &a, cudaStream_t s) {
-  constexpr int B = 512, LOGS = 13;
-  const size_t smem = (size_t(1) << LOGS) * 10;  // keys, values, claimed list
+  const size_t smem1 = (size_t(1) << HUBC_LOGS) * 10, smem2 = (size_t(1) << HUBM_LOGS) * 10;
   const size_t nch = a.hub.chunk_begin[a.color + 1] - a.hub.chunk_begin[a.color];
   const size_t nh = a.hub.hub_begin[a.color + 1] - a.hub.hub_begin[a.color];
   if (!nh) return;
-  auto k1 = hub_chunk_kernel<B, LOGS>;
-  auto k2 = hub_merge_kernel<B, LOGS, SYNC>;
+  auto k1 = hub_chunk_kernel<HUBC_B, HUBC_LOGS>;
+  auto k2 = hub_merge_kernel<HUBM_B, HUBM_LOGS, SYNC>;
   static bool configured = false;
-  if (!configured) { set_smem(k1, smem); set_smem(k2, smem); configured = true; }
-  k1<<<unsigned(nch), B, smem, s>>>(a);
+  if (!configured) { set_smem(k1, smem1); set_smem(k2, smem2); configured = true; }
+  k1<<<unsigned(nch), HUBC_B, smem1, s>>>(a);
   LVG_CHECK_LAUNCH();
-  k2<<<unsigned(global_table_blocks(nh)), B, smem, s>>>(a);
+  k2<<<unsigned(global_table_blocks(nh)), HUBM_B, smem2, s>>>(a);
   LVG_CHECK_LAUNCH();
 }
 
@@ -776,14 +801,20 @@ void launch_bin(int b, const MoveArgs &a, cudaStream_t s) {
     case 6: launch_tile<32, 256, SYNC>(a, s); break;
     case 7: launch_tile<32, 512, SYNC>(a, s); break;
     case 8: launch_tile<32, 1024, SYNC>(a, s); break;
-    case 9: launch_big<256, 12, SYNC>(a, s); break;
-    case 10: launch_big<512, 13, SYNC>(a, s); break;
-    case 11: launch_big<512, 13, SYNC>(a, s); break;
+    case 9: launch_big<BIG9_B, BIG9_LOGS, SYNC>(a, s); break;
+    case 10: launch_big<BIG10_B, BIG10_LOGS, SYNC>(a, s); break;
     default: break;
   }
 }
 
 }  // namespace
+
+int move_grid_blocks(int bin, bool sync, size_t count) {
+  if (bin == 9) return int(sync ? big_grid<BIG9_B, BIG9_LOGS, true>(count) : big_grid<BIG9_B, BIG9_LOGS, false>(count));
+  if (bin == 10)
+    return int(sync ? big_grid<BIG10_B, BIG10_LOGS, true>(count) : big_grid<BIG10_B, BIG10_LOGS, false>(count));
+  return global_table_blocks(count);  // the hub merge
+}
 
 int global_table_blocks(size_t count) {
   size_t cap = size_t(num_sms()) * 3;

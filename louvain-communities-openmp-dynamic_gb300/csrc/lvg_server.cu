@@ -9,7 +9,9 @@
 // replaces. Requests for one graph run in arrival order, one at a time;
 // requests for different graphs run concurrently on the graphs' own streams
 // (one host worker thread per request in flight). Admission control keeps
-// the estimated device footprint of the resident graphs under a budget.
+// the device bytes of the resident graphs under a budget: a graph is admitted
+// on its measured bytes after its first run (graph, workspace, state) plus
+// the per-request scratch, and only while the device has that much free.
 //
 // Host code only: it calls the library's own C-ABI.
 #include <algorithm>
@@ -43,6 +45,7 @@ struct Request {
 struct Slot {
   lvg_graph *g = nullptr;
   lvg_state *st = nullptr;
+  lvg_device_batch *db = nullptr;  // reused by every request of the graph
   bool owns_graph = false;
   std::deque<Request> q;
   bool busy = false;
@@ -90,8 +93,8 @@ void serve(lvg_server *sv, Slot &s, const Request &r, lvg_request_info &info) {
   info.queue_ms = t0 - r.t_submit;
   lvg_batch b{r.ds.size(), r.ds.data(), r.dd.data(), r.dw.data(), r.is.size(), r.is.data(), r.id.data(),
               r.iw.data()};
-  lvg_device_batch *db = nullptr;
-  int rc = lvg_device_batch_create(s.g, &b, &db);
+  int rc = s.db ? lvg_device_batch_set(s.db, &b) : lvg_device_batch_create(s.g, &b, &s.db);
+  lvg_device_batch *db = s.db;
   if (rc == LVG_OK) rc = lvg_graph_apply_device_batch(s.g, db);
   const double t1 = now_ms();
   info.apply_ms = t1 - t0;
@@ -106,7 +109,6 @@ void serve(lvg_server *sv, Slot &s, const Request &r, lvg_request_info &info) {
     info.passes = res.passes;
     info.affected = res.affectedVertices;
   }
-  if (db) lvg_device_batch_destroy(db);
   info.run_ms = now_ms() - t1;
   info.status = rc;
 }
@@ -184,36 +186,39 @@ int lvg_server_create(const lvg_server_options *o, lvg_server **out) {
 int lvg_server_add_graph(lvg_server *sv, lvg_graph *g, int take_ownership, const uint32_t *q, const double *qvtot,
                          const double *qctot, int *graph_id) {
   if (!sv || !g || !graph_id) return lvg::fail_noalloc(LVG_EINVAL, "null argument");
-  const size_t bytes = lvg_graph_footprint(lvg_graph_span(g), lvg_graph_size(g));
-  {
+  if (q && (!qvtot || !qctot)) return lvg::fail_noalloc(LVG_EINVAL, "lvg_server_add_graph: q without weights");
+  {  // a first check on the a-priori estimate, before any work
     std::lock_guard<std::mutex> lk(sv->mu);
-    if (sv->bytes_used + bytes > sv->opt.hbm_budget)
+    if (sv->bytes_used + lvg_graph_footprint(lvg_graph_span(g), lvg_graph_size(g)) / 2 > sv->opt.hbm_budget)
       return lvg::fail_noalloc(LVG_ENOMEM, "lvg_server_add_graph: the HBM budget is used up (admission denied)");
-    sv->bytes_used += bytes;  // reserved; released below on failure
   }
-  auto release = [&](int rc) {
-    std::lock_guard<std::mutex> lk(sv->mu);
-    sv->bytes_used -= bytes;
-    return rc;
-  };
   lvg_state *st = nullptr;
   int rc = lvg_state_create(g, &st);
-  if (rc != LVG_OK) return release(rc);
+  if (rc != LVG_OK) return rc;
   if (q) {
-    if (!qvtot || !qctot) {
-      lvg_state_destroy(st);
-      return release(lvg::fail_noalloc(LVG_EINVAL, "lvg_server_add_graph: q without weights"));
-    }
     rc = lvg_state_set(st, q, qvtot, qctot);
   } else {  // no prior: the static communities
     lvg_result res{};
     rc = lvg_run_resident(g, LVG_METHOD_STATIC, nullptr, nullptr, st, &sv->opt.louvain, &res);
   }
+  if (rc == LVG_OK) rc = lvg_graph_trim(g, 1);  // the static pass's hash tables are not needed again
   if (rc != LVG_OK) {
     lvg_state_destroy(st);
-    return release(rc);
+    return rc;
   }
+  // measured: graph + workspace + state, plus per-request scratch (span-sized
+  // plan arrays, batch-sized buffers, the dynamic pass's hash tables)
+  const size_t span = lvg_graph_span(g);
+  const size_t bytes = lvg_graph_device_bytes(g) + lvg_state_device_bytes(st) + 24 * span + (size_t(64) << 20);
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) free_b = 0;
   std::lock_guard<std::mutex> lk(sv->mu);
+  const size_t now = lvg_graph_device_bytes(g) + lvg_state_device_bytes(st);
+  if (sv->bytes_used + bytes > sv->opt.hbm_budget || free_b < bytes - now + (size_t(1) << 30)) {
+    lvg_state_destroy(st);
+    return lvg::fail_noalloc(LVG_ENOMEM, "lvg_server_add_graph: the HBM budget is used up (admission denied)");
+  }
+  sv->bytes_used += bytes;
   std::unique_ptr<Slot> s(new Slot());
   s->g = g;
   s->st = st;
@@ -322,6 +327,7 @@ int lvg_server_destroy(lvg_server *sv) {
   sv->cv_work.notify_all();
   for (auto &t : sv->workers) t.join();
   for (auto &s : sv->slots) {
+    lvg_device_batch_destroy(s->db);
     lvg_state_destroy(s->st);
     if (s->owns_graph) lvg_graph_destroy(s->g);
   }

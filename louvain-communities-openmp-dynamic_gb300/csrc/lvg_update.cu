@@ -38,26 +38,31 @@ __device__ __forceinline__ uint32_t count_less(const uint32_t *a, uint32_t n, ui
   return lo;
 }
 
-__device__ __forceinline__ bool contains(const uint32_t *a, uint32_t n, uint32_t x) {
-  const uint32_t p = count_less(a, n, x);
-  return p < n && a[p] == x;
+__device__ __forceinline__ double warp_sum_f64(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
 }
 
-// One warp per touched row: (old \ present deletions) U absent insertions,
-// sorted, into scratch at spos[r]; the new degree into newdeg[r]; the change
-// of the edge count into upd[UPD_EDGES]; kept flags into keep[]; endpoints of
-// kept insertions marked present in ex (when given).
-//   dpre[j]: kept (present) deletions before j in the row;
-//   ipre[j]: kept (absent) insertions before j in the row.
-__global__ void merge_rows_kernel(const uint64_t *off, const uint32_t *deg, const uint32_t *key, const float *w,
-                                  const UpdRow *rows, size_t nrows, const uint32_t *dd, const uint32_t *id,
-                                  const float *iw, size_t nd_all, uint32_t *pre, uint32_t *keep,
-                                  const uint64_t *spos, uint32_t *skey, float *sw, uint32_t *newdeg, uint8_t *ex,
-                                  unsigned long long *upd) {
+// Step 1, one warp per touched row: the tidy filter and the row's plan.
+//   ikeep/dkeep: the insertion is absent / the deletion is present in the row;
+//   ipre[j] / dpre[j]: kept insertions / deletions before j in the row;
+//   P.n1: new degree; P.f0: first old index whose position changes (0 when
+//   the row moves to the pool); P.len: entries to rewrite (n1 - f0);
+//   P.src: source items (old entries from f0, then every insertion);
+//   P.grow: pool entries the row takes (0 unless it outgrows its capacity).
+// Also the change of the edge count and of the total weight (FP64), and the
+// endpoints of kept insertions marked present in ex (when given).
+__global__ void row_plan_kernel(const uint64_t *off, const uint32_t *deg, const uint32_t *cap, const uint32_t *key,
+                                const float *w, const UpdRow *rows, size_t nrows, const uint32_t *dd,
+                                const uint32_t *id, const float *iw, size_t nd_all, uint32_t *pre, uint32_t *keep,
+                                RowPlan *plan, uint64_t *len, uint64_t *src, uint64_t *grow, uint8_t *ex,
+                                unsigned long long *upd, double *wdelta) {
   const size_t warps = size_t(gridDim.x) * blockDim.x / 32;
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t lt = (1u << lane) - 1;
-  long long delta = 0;
+  long long edges = 0;
+  double dw = 0;
   for (size_t r = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32; r < nrows; r += warps) {
     const UpdRow R = rows[r];
     const uint64_t o = off[R.u];
@@ -67,21 +72,37 @@ __global__ void merge_rows_kernel(const uint64_t *off, const uint32_t *deg, cons
     const uint32_t *il = id + R.i0, ni = R.i1 - R.i0;
     uint32_t *dpre = pre + R.d0, *ipre = pre + nd_all + R.i0;
     uint32_t *dkeep = keep + R.d0, *ikeep = keep + nd_all + R.i0;
-    uint32_t icarry = 0, dcarry = 0;
+    uint32_t icarry = 0, dcarry = 0, first = n;
     for (uint32_t b = 0; b < ni; b += 32) {  // warp-uniform bound
       const uint32_t j = b + lane;
-      const bool k = j < ni && !contains(row, n, il[j]);
+      bool k = false;
+      if (j < ni) {
+        const uint32_t p = count_less(row, n, il[j]);
+        k = !(p < n && row[p] == il[j]);
+        if (k) {
+          first = min(first, p);
+          dw += double(iw[R.i0 + j]);
+          if (ex) ex[il[j]] = 1;
+        }
+      }
       const uint32_t m = __ballot_sync(0xffffffffu, k);
       if (j < ni) {
         ipre[j] = icarry + __popc(m & lt);
         ikeep[j] = k;
-        if (k && ex) ex[il[j]] = 1;
       }
       icarry += __popc(m);
     }
     for (uint32_t b = 0; b < nd; b += 32) {
       const uint32_t j = b + lane;
-      const bool k = j < nd && contains(row, n, dl[j]);
+      bool k = false;
+      if (j < nd) {
+        const uint32_t p = count_less(row, n, dl[j]);
+        k = p < n && row[p] == dl[j];
+        if (k) {
+          first = min(first, p);
+          dw -= double(w[o + p]);
+        }
+      }
       const uint32_t m = __ballot_sync(0xffffffffu, k);
       if (j < nd) {
         dpre[j] = dcarry + __popc(m & lt);
@@ -89,76 +110,123 @@ __global__ void merge_rows_kernel(const uint64_t *off, const uint32_t *deg, cons
       }
       dcarry += __popc(m);
     }
-    __syncwarp();
-    const uint64_t base = spos[r];
-    for (uint32_t i = lane; i < n; i += 32) {
-      const uint32_t k = row[i];
-      const uint32_t a = count_less(dl, nd, k);
-      if (a < nd && dl[a] == k) continue;  // deleted
-      const uint32_t b = count_less(il, ni, k);
-      const uint32_t at = i - (a < nd ? dpre[a] : dcarry) + (b < ni ? ipre[b] : icarry);
-      skey[base + at] = k;
-      sw[base + at] = w[o + i];
-    }
-    for (uint32_t j = lane; j < ni; j += 32) {
-      if (!ikeep[j]) continue;  // already present: tidied away
-      const uint32_t k = il[j];
-      const uint32_t a = count_less(dl, nd, k);
-      const uint32_t at = ipre[j] + count_less(row, n, k) - (a < nd ? dpre[a] : dcarry);
-      skey[base + at] = k;
-      sw[base + at] = iw[R.i0 + j];
-    }
+    first = __reduce_min_sync(0xffffffffu, first);
     if (lane == 0) {
       const uint32_t n1 = n - dcarry + icarry;
-      newdeg[r] = n1;
-      delta += (long long)n1 - (long long)n;
+      const bool moved = n1 > cap[R.u];
+      const uint32_t f0 = moved ? 0 : first;
+      RowPlan P;
+      P.n1 = n1;
+      P.f0 = f0;
+      P.dcarry = dcarry;
+      P.icarry = icarry;
+      plan[r] = P;
+      len[r] = n1 - f0;
+      src[r] = uint64_t(n - f0) + ni;
+      grow[r] = moved ? row_capacity(n1) : 0;
+      edges += (long long)n1 - (long long)n;
       if (icarry && ex) ex[R.u] = 1;
     }
-    __syncwarp();
   }
-  if (lane == 0 && delta) atomicAdd(&upd[UPD_EDGES], (unsigned long long)delta);
+  dw = warp_sum_f64(dw);
+  if (lane == 0) {
+    if (edges) atomicAdd(&upd[UPD_EDGES], (unsigned long long)edges);
+    if (dw != 0.0) atomicAdd(wdelta, dw);
+  }
 }
 
-// One warp per touched row: copy the merged row back (in place if it fits,
-// else to a new stretch of the overflow pool) and zero what the row no longer
-// uses. The pool cursor is upd[UPD_POOL]; the pool ends at pool_end.
-__global__ void commit_rows_kernel(uint64_t *off, uint32_t *deg, uint32_t *cap, uint32_t *key, float *w,
-                                   const UpdRow *rows, size_t nrows, const uint64_t *spos, const uint32_t *skey,
-                                   const float *sw, const uint32_t *newdeg, unsigned long long *upd,
-                                   unsigned long long pool_end) {
+// The row an item of a flat range belongs to: the last r with start[r] <= x.
+__device__ __forceinline__ uint32_t row_of(const uint64_t *start, uint32_t nrows, uint64_t x) {
+  uint32_t lo = 0, hi = nrows;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (start[mid] <= x) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+// Step 2, one thread per source item (old entries from f0, then insertions)
+// of all touched rows: the item's place in the rewritten row, into scratch.
+// An old entry at i goes to i - (kept deletions before it) + (kept
+// insertions before it); a kept insertion j to j's kept rank + (old entries
+// before it) - (kept deletions before it).
+__global__ void merge_items_kernel(const uint64_t *off, const uint32_t *deg, const uint32_t *key, const float *w,
+                                   const UpdRow *rows, uint32_t nrows, const uint32_t *dd, const uint32_t *id,
+                                   const float *iw, size_t nd_all, const uint32_t *pre, const uint32_t *keep,
+                                   const RowPlan *plan, const uint64_t *src, uint64_t total, const uint64_t *spos,
+                                   uint32_t *skey, float *sw) {
+  for (uint64_t x = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; x < total;
+       x += uint64_t(gridDim.x) * blockDim.x) {
+    const uint32_t r = row_of(src, nrows, x);
+    const UpdRow R = rows[r];
+    const RowPlan P = plan[r];
+    const uint64_t o = off[R.u];
+    const uint32_t n = deg[R.u];
+    const uint32_t *row = key + o;
+    const uint32_t *dl = dd + R.d0, nd = R.d1 - R.d0;
+    const uint32_t *il = id + R.i0, ni = R.i1 - R.i0;
+    const uint32_t *dpre = pre + R.d0, *ipre = pre + nd_all + R.i0;
+    const uint32_t j = uint32_t(x - src[r]);
+    const uint64_t base = spos[r];
+    if (j < n - P.f0) {
+      const uint32_t i = P.f0 + j;
+      const uint32_t k = row[i];
+      const uint32_t a = count_less(dl, nd, k);
+      if (a < nd && dl[a] == k) continue;  // deleted (present, so kept)
+      const uint32_t b = count_less(il, ni, k);
+      const uint32_t at = i - (a < nd ? dpre[a] : P.dcarry) + (b < ni ? ipre[b] : P.icarry) - P.f0;
+      skey[base + at] = k;
+      sw[base + at] = w[o + i];
+    } else {
+      const uint32_t jj = j - (n - P.f0);
+      if (!keep[nd_all + R.i0 + jj]) continue;  // already present: tidied away
+      const uint32_t k = il[jj];
+      const uint32_t a = count_less(dl, nd, k);
+      const uint32_t at = ipre[jj] + count_less(row, n, k) - (a < nd ? dpre[a] : P.dcarry) - P.f0;
+      skey[base + at] = k;
+      sw[base + at] = iw[R.i0 + jj];
+    }
+  }
+}
+
+// Step 3, one thread per rewritten entry: scratch -> the row's place (in
+// place from f0, or the row's new stretch in the pool at pool + gpos[r]).
+__global__ void copy_items_kernel(const uint64_t *off, const UpdRow *rows, uint32_t nrows, const RowPlan *plan,
+                                  const uint64_t *spos, uint64_t total, const uint64_t *grow, const uint64_t *gpos,
+                                  uint64_t pool, const uint32_t *skey, const float *sw, uint32_t *key, float *w) {
+  for (uint64_t x = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; x < total;
+       x += uint64_t(gridDim.x) * blockDim.x) {
+    const uint32_t r = row_of(spos, nrows, x);
+    const uint64_t dst = (grow[r] ? pool + gpos[r] : off[rows[r].u]) + plan[r].f0 + (x - spos[r]);
+    key[dst] = skey[x];
+    w[dst] = sw[x];
+  }
+}
+
+// Step 4, one warp per touched row: zero what the row no longer uses (the
+// tail in place; the old stretch and the new stretch's slack when it moved)
+// and set its offset, capacity and degree.
+__global__ void finish_rows_kernel(uint64_t *off, uint32_t *deg, uint32_t *cap, uint32_t *key, float *w,
+                                   const UpdRow *rows, size_t nrows, const RowPlan *plan, const uint64_t *grow,
+                                   const uint64_t *gpos, uint64_t pool) {
   const size_t warps = size_t(gridDim.x) * blockDim.x / 32;
   const uint32_t lane = threadIdx.x & 31;
   for (size_t r = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32; r < nrows; r += warps) {
     const uint32_t u = rows[r].u;
-    const uint32_t n0 = deg[u], n1 = newdeg[r], c = cap[u];
-    const uint64_t src = spos[r];
-    uint64_t o = off[u];
-    if (n1 > c) {
-      const uint32_t nc = row_capacity(n1);
-      unsigned long long at = 0;
-      if (lane == 0) at = atomicAdd(&upd[UPD_POOL], (unsigned long long)nc);
-      at = __shfl_sync(0xffffffffu, at, 0);
-      if (at + nc > pool_end) {  // the host sized the pool for the worst case
-        if (lane == 0) atomicOr(&upd[UPD_ERR], 1ull);
-        continue;
-      }
+    const uint32_t n0 = deg[u], n1 = plan[r].n1;
+    const uint64_t o = off[u];
+    if (grow[r]) {
+      const uint64_t no = pool + gpos[r];
+      const uint32_t nc = uint32_t(grow[r]);
       for (uint32_t i = lane; i < n0; i += 32) { key[o + i] = 0; w[o + i] = 0.f; }
-      o = at;
-      for (uint32_t i = lane; i < nc; i += 32) {
-        key[o + i] = i < n1 ? skey[src + i] : 0;
-        w[o + i] = i < n1 ? sw[src + i] : 0.f;
-      }
+      for (uint32_t i = n1 + lane; i < nc; i += 32) { key[no + i] = 0; w[no + i] = 0.f; }
       __syncwarp();  // every lane has read the row's old extent
-      if (lane == 0) { off[u] = o; cap[u] = nc; deg[u] = n1; }
-      continue;
+      if (lane == 0) { off[u] = no; cap[u] = nc; deg[u] = n1; }
+    } else {
+      for (uint32_t i = n1 + lane; i < n0; i += 32) { key[o + i] = 0; w[o + i] = 0.f; }
+      __syncwarp();
+      if (lane == 0) deg[u] = n1;
     }
-    for (uint32_t i = lane; i < n1; i += 32) {
-      key[o + i] = skey[src + i];
-      w[o + i] = sw[src + i];
-    }
-    for (uint32_t i = n1 + lane; i < n0; i += 32) { key[o + i] = 0; w[o + i] = 0.f; }
-    __syncwarp();
-    if (lane == 0) deg[u] = n1;
   }
 }
 
@@ -195,12 +263,6 @@ __global__ void row_caps_kernel(const uint64_t *coff, size_t n, uint32_t *deg, u
     cap[u] = c;
     cap64[u] = c;
   }
-}
-
-// Upper bound of each touched row's new degree (old degree + insertions).
-__global__ void row_bounds_kernel(const uint32_t *deg, const UpdRow *rows, size_t nrows, uint64_t *bound) {
-  for (size_t r = size_t(blockIdx.x) * blockDim.x + threadIdx.x; r < nrows; r += size_t(gridDim.x) * blockDim.x)
-    bound[r] = uint64_t(deg[rows[r].u]) + (rows[r].i1 - rows[r].i0);
 }
 
 // Fresh capacities from the current degrees.
@@ -328,29 +390,44 @@ void launch_spread_rows(const uint64_t *coff, const uint32_t *ckey, const float 
   LVG_CHECK_LAUNCH();
 }
 
-void launch_row_bounds(const uint32_t *deg, const UpdRow *rows, size_t nrows, uint64_t *bound, cudaStream_t s) {
+void launch_row_plan(const uint64_t *off, const uint32_t *deg, const uint32_t *cap, const uint32_t *key,
+                     const float *w, const UpdRow *rows, size_t nrows, const uint32_t *dd, const uint32_t *id,
+                     const float *iw, size_t nd_all, uint32_t *pre, uint32_t *keep, RowPlan *plan, uint64_t *len,
+                     uint64_t *src, uint64_t *grow, uint8_t *ex, unsigned long long *upd, double *wdelta,
+                     cudaStream_t s) {
   if (!nrows) return;
-  row_bounds_kernel<<<grid_for(nrows, 256), 256, 0, s>>>(deg, rows, nrows, bound);
+  row_plan_kernel<<<grid_for(nrows * 32, 256), 256, 0, s>>>(off, deg, cap, key, w, rows, nrows, dd, id, iw, nd_all,
+                                                              pre, keep, plan, len, src, grow, ex, upd, wdelta);
   LVG_CHECK_LAUNCH();
 }
 
-void launch_merge_rows(const uint64_t *off, const uint32_t *deg, const uint32_t *key, const float *w,
-                       const UpdRow *rows, size_t nrows, const uint32_t *dd, const uint32_t *id, const float *iw,
-                       size_t nd_all, uint32_t *pre, uint32_t *keep, const uint64_t *spos, uint32_t *skey,
-                       float *sw, uint32_t *newdeg, uint8_t *ex, unsigned long long *upd, cudaStream_t s) {
-  if (!nrows) return;
-  merge_rows_kernel<<<grid_for(nrows * 32, 256), 256, 0, s>>>(off, deg, key, w, rows, nrows, dd, id, iw, nd_all, pre,
-                                                                keep, spos, skey, sw, newdeg, ex, upd);
-  LVG_CHECK_LAUNCH();
-}
-
-void launch_commit_rows(uint64_t *off, uint32_t *deg, uint32_t *cap, uint32_t *key, float *w, const UpdRow *rows,
-                        size_t nrows, const uint64_t *spos, const uint32_t *skey, const float *sw,
-                        const uint32_t *newdeg, unsigned long long *upd, unsigned long long pool_end,
+void launch_merge_items(const uint64_t *off, const uint32_t *deg, const uint32_t *key, const float *w,
+                        const UpdRow *rows, size_t nrows, const uint32_t *dd, const uint32_t *id, const float *iw,
+                        size_t nd_all, const uint32_t *pre, const uint32_t *keep, const RowPlan *plan,
+                        const uint64_t *src, uint64_t total, const uint64_t *spos, uint32_t *skey, float *sw,
                         cudaStream_t s) {
+  if (!total) return;
+  merge_items_kernel<<<grid_for(total, 256), 256, 0, s>>>(off, deg, key, w, rows, uint32_t(nrows), dd, id, iw, nd_all,
+                                                          pre, keep, plan, src, total, spos, skey, sw);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_copy_items(const uint64_t *off, const UpdRow *rows, size_t nrows, const RowPlan *plan,
+                       const uint64_t *spos, uint64_t total, const uint64_t *grow, const uint64_t *gpos,
+                       uint64_t pool, const uint32_t *skey, const float *sw, uint32_t *key, float *w,
+                       cudaStream_t s) {
+  if (!total) return;
+  copy_items_kernel<<<grid_for(total, 256), 256, 0, s>>>(off, rows, uint32_t(nrows), plan, spos, total, grow, gpos,
+                                                         pool, skey, sw, key, w);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_finish_rows(uint64_t *off, uint32_t *deg, uint32_t *cap, uint32_t *key, float *w, const UpdRow *rows,
+                        size_t nrows, const RowPlan *plan, const uint64_t *grow, const uint64_t *gpos,
+                        uint64_t pool, cudaStream_t s) {
   if (!nrows) return;
-  commit_rows_kernel<<<grid_for(nrows * 32, 256), 256, 0, s>>>(off, deg, cap, key, w, rows, nrows, spos, skey, sw,
-                                                                 newdeg, upd, pool_end);
+  finish_rows_kernel<<<grid_for(nrows * 32, 256), 256, 0, s>>>(off, deg, cap, key, w, rows, nrows, plan, grow, gpos,
+                                                                 pool);
   LVG_CHECK_LAUNCH();
 }
 

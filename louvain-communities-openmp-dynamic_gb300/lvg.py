@@ -182,6 +182,14 @@ def load_library() -> C.CDLL:
                                             C.POINTER(vp)]
     L.lvg_device_batch_size.argtypes = [vp, C.POINTER(sz), C.POINTER(sz)]
     L.lvg_device_batch_download.argtypes = [vp, vp]
+    L.lvg_device_batch_set.argtypes = [vp, C.POINTER(_Batch)]
+    L.lvg_graph_device_bytes.argtypes = [vp]
+    L.lvg_graph_device_bytes.restype = sz
+    L.lvg_state_device_bytes.argtypes = [vp]
+    L.lvg_state_device_bytes.restype = sz
+    L.lvg_device_batch_device_bytes.argtypes = [vp]
+    L.lvg_device_batch_device_bytes.restype = sz
+    L.lvg_graph_trim.argtypes = [vp, i32]
     L.lvg_server_options_default.argtypes = [C.POINTER(_ServerOptions)]
     L.lvg_graph_footprint.argtypes = [sz, sz]
     L.lvg_graph_footprint.restype = sz
@@ -502,6 +510,13 @@ class Graph:
     def set_profiling(self, on: bool) -> None:
         _check(self._L.lvg_set_profiling(self.h, int(on)))
 
+    def device_bytes(self) -> int:
+        """Device bytes held by the graph, its workspace and scratch (lvg_graph_device_bytes)."""
+        return int(self._L.lvg_graph_device_bytes(self.h))
+
+    def trim(self, level: int = 1) -> None:
+        _check(self._L.lvg_graph_trim(self.h, level))
+
     def apply_batch(self, b: "HostBatch | DeviceBatch") -> "HostBatch | None":
         """Tidy a batch against the graph and apply it in place on the GPU (the
         reference's tidyBatchUpdateU + applyBatchUpdateOmpU). For a HostBatch
@@ -685,6 +700,12 @@ class DeviceBatch:
         r = g.span - begin if range_ is None else range_
         _check(d._L.lvg_device_batch_generate(g.h, deletions, insertions, begin, r, weight, seed, C.byref(d.h)))
         return d
+
+    def set(self, b: HostBatch) -> None:
+        """Replace the contents with another host batch, reusing the device buffers (lvg_device_batch_set)."""
+        s = b._struct()
+        _check(self._L.lvg_device_batch_set(self.h, C.byref(s)))
+        self.batch = b
 
     def size(self) -> tuple[int, int]:
         nd, ni = C.c_size_t(), C.c_size_t()

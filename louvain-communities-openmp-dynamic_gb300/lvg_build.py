@@ -4,8 +4,11 @@ Products (written to ``lib/`` beside this file; git-ignored):
 
 * ``liblouvain_gb300.so`` — the GB300 Louvain library: hand-written sm_103a CUDA
   kernels behind the C-ABI declared in ``include/louvain_gb300.h``.
-* ``liblvg_graphgen.so`` — host-only seeded graph and batch generators
-  (``include/louvain_gb300_graphgen.h``); no CUDA dependency.
+* ``liblvg_graphgen.so`` — host-only seeded graph and batch generators and
+  the SNAP temporal reader (``include/louvain_gb300_graphgen.h``); no CUDA
+  dependency.
+* ``louvain_gb300_experiment`` — the reference's experiment driver (main.cxx)
+  over the two libraries: same command line, same log lines.
 
 Every CUDA translation unit is compiled for sm_103a only
 (``-gencode arch=compute_103a,code=sm_103a``), in parallel, then linked with
@@ -33,6 +36,7 @@ CXX_FLAGS = ["-std=c++17", "-O3", "-fPIC", "-fopenmp", "-I", INCLUDE]
 
 CUDA_LIB = os.path.join(LIB, "liblouvain_gb300.so")
 GEN_LIB = os.path.join(LIB, "liblvg_graphgen.so")
+EXPERIMENT = os.path.join(LIB, "louvain_gb300_experiment")
 
 
 def _nvcc() -> str:
@@ -97,9 +101,18 @@ def build_cuda(verbose: bool = False, extra_flags: list[str] | None = None) -> s
     return CUDA_LIB
 
 
+def build_experiment(verbose: bool = False) -> str:
+    src = os.path.join(CSRC, "lvg_experiment.cpp")
+    if _stale(EXPERIMENT, [src, CUDA_LIB, GEN_LIB] + _headers()):
+        _run([_nvcc(), "-std=c++17", "-O2", "-I", INCLUDE, src, "-o", EXPERIMENT, "-L", LIB, "-llouvain_gb300",
+              "-llvg_graphgen", "-lcudart", "-Xlinker", "-rpath,$ORIGIN"], verbose)
+    return EXPERIMENT
+
+
 def build(verbose: bool = False) -> None:
     build_graphgen(verbose)
     build_cuda(verbose)
+    build_experiment(verbose)
 
 
 if __name__ == "__main__":

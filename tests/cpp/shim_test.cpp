@@ -57,6 +57,20 @@ int main() {
   for (uint32_t u = 1; u <= n; ++u) if (a.vertexWeight[u] != double(x.rows[u].size())) ++bad;
   std::printf("static %d passes %d iters %.3f ms | nd %.3f ds %.3f df %.3f ms | bad %d\n", a.passes, a.iterations,
               a.time, b.time, c.time, d.time, bad);
+  // main.cxx:108-109 in HBM: tidy + apply an untidy batch to x on the device
+  louvain_gb300::DeviceGraph dx(x);
+  auto ins2 = ins;
+  ins2.push_back(ins[0]);                                     // a duplicate
+  ins2.push_back({1u, x.rows[1].begin()->first, 1.0f});       // an edge x already has
+  std::reverse(ins2.begin(), ins2.end());                     // unsorted
+  auto del2 = del;
+  tidyApplyBatchUpdateOmpU(dx, del2, ins2);
+  if (ins2 != ins || !del2.empty()) ++bad;                    // the tidied batch
+  if (lvg_graph_size(dx.get()) != lvg_graph_size(dy.get())) ++bad;
+  double wx = 0, wy = 0;
+  lvg_edge_weight(dx.get(), &wx);
+  lvg_edge_weight(dy.get(), &wy);
+  if (wx != wy) ++bad;
   try {
     std::vector<uint32_t> shortq(3);
     louvainDynamicFrontierOmp(dy, del, ins, shortq, a.vertexWeight, a.communityWeight);

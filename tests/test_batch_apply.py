@@ -144,6 +144,27 @@ def test_device_batch_apply_tidies_the_batch_in_place(cuda, name):
 
 
 @pytest.mark.gpu
+def test_device_batch_reused_for_a_sequence(cuda):
+    """One device batch refilled with lvg_device_batch_set for each step gives
+    the same graph as a fresh device batch per step."""
+    d = _fixture()
+    A = cuda.Graph(_graph(cuda, d, "pp1k", 1))
+    B = cuda.Graph(_graph(cuda, d, "pp1k", 1))
+    db = None
+    for step in (1, 2):
+        b = _batch(cuda, d, "pp1k", step)
+        if db is None:
+            db = cuda.DeviceBatch(A, b)
+        else:
+            db.set(b)
+        A.apply_batch(db)
+        B.apply_batch(cuda.DeviceBatch(B, b))
+        ha, hb = A.download(), B.download()
+        assert np.array_equal(ha.offsets, hb.offsets) and np.array_equal(ha.keys, hb.keys)
+        _download_matches(A, _expect(d, "pp1k", step)[0])
+
+
+@pytest.mark.gpu
 def test_device_apply_through_pool_growth_and_relayout(cuda, orc):
     """Rows that outgrow their slack move to the overflow pool; a batch larger
     than the pool forces a re-layout. Each step equals the oracle."""

@@ -1,0 +1,59 @@
+"""The large-degree paths on the GPU: degree bins 9-10 (block per vertex,
+shared tables with a global fallback) and bin 11 (hubs of degree > 8192:
+chunked partial tables + merge), bit-exact against the CPU replay of the
+deterministic rule.
+
+The golden cases have no vertex above degree ~2000; an R-MAT graph of scale
+16 with edge factor 48 (a = 0.57) has 17 hubs above degree 8192 (one above
+16384, so several chunks) and ~120 vertices of degree 2049-8192, so every
+local-moving path runs — including, in the first iteration of static
+Louvain (every vertex its own community), chunks and vertices whose distinct
+neighbour communities overflow the shared tables.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def hubgraph(lvg):
+    x = lvg.rmat(16, 48, seed=77)
+    deg = np.diff(x.offsets).astype(np.int64)
+    assert (deg > 16384).sum() >= 1 and (deg > 8192).sum() >= 10 and ((deg > 2048) & (deg <= 8192)).sum() >= 50
+    b = lvg.random_batch(x, 3000, 0.8, seed=78)
+    y = lvg.apply_batch(x, b)
+    return x, b, y
+
+
+@pytest.mark.parametrize("colors", [4, 16])
+def test_static_and_frontier_on_hubs_match_cpu_replay(cuda, orc, hubgraph, colors):
+    x, b, y = hubgraph
+    o = cuda.LouvainOptions(deterministic=True, colors=colors)
+    X = cuda.Graph(x)
+    r0 = cuda.louvain_static(X, o)
+    m, vt, ct, info = orc.louvain(x, 0, threads=8, sync=True, colors=colors)
+    assert np.array_equal(r0.membership, m)
+    assert np.array_equal(r0.communityWeight, ct)
+    assert (r0.iterations, r0.passes) == (info["iterations"], info["passes"])
+    Y = cuda.Graph(y)
+    r = cuda.louvain_dynamic_frontier(Y, b, r0.membership, r0.vertexWeight, r0.communityWeight, o)
+    m, vt, ct, info = orc.louvain(y, 3, b, r0.membership, r0.vertexWeight, r0.communityWeight, threads=8, sync=True,
+                                  colors=colors)
+    assert np.array_equal(r.membership, m)
+    assert np.array_equal(r.communityWeight, ct)
+    assert (r.iterations, r.passes, r.affectedVertices) == (info["iterations"], info["passes"],
+                                                            info["affectedVertices"])
+
+
+def test_async_on_hubs_quality_and_totals(cuda, orc, hubgraph):
+    x, b, y = hubgraph
+    X = cuda.Graph(x)
+    r0 = cuda.louvain_static(X)
+    q_gpu = orc.modularity(x, r0.membership)
+    m, _, _, _ = orc.louvain(x, 0, threads=8)
+    q_cpu = orc.modularity(x, m)
+    assert abs(q_gpu - q_cpu) <= 0.01, (q_gpu, q_cpu)
+    # the vertex weights are the weighted degrees (louvainVertexWeightsOmpW)
+    deg_w = np.add.reduceat(x.weights.astype(np.float64), x.offsets[:-1].astype(np.int64)) * (np.diff(x.offsets) > 0)
+    assert np.array_equal(r0.vertexWeight, deg_w)

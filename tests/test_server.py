@@ -74,14 +74,20 @@ def test_server_results_equal_sequential_runs(cuda, orc):
 
 @pytest.mark.gpu
 def test_server_admission_control(cuda):
+    """A graph is admitted on its measured device bytes; the next one that
+    would pass the budget is refused with LVG_ENOMEM."""
     x = cuda.planted_partition(2000, 100, 10, 0.8, 1)
     G = cuda.Graph(x)
-    need = cuda.graph_footprint(x.span, x.num_edges)
-    sv = cuda.Server(workers=2, hbm_budget=need + need // 2)
-    sv.add_graph(G)
-    H = cuda.Graph(x)
+    probe = cuda.Server(workers=1)
+    probe.add_graph(G)
+    one = probe.stats()["hbm_reserved"]
+    probe.close()
+    assert one >= G.device_bytes() > 8 * x.num_edges
+    H, K = cuda.Graph(x), cuda.Graph(x)
+    sv = cuda.Server(workers=2, hbm_budget=one + one // 2)
+    sv.add_graph(H)
     with pytest.raises(cuda.LvgError) as e:
-        sv.add_graph(H)
+        sv.add_graph(K)
     assert e.value.code == cuda.LVG_ENOMEM
     assert sv.stats()["graphs"] == 1
     sv.close()
