@@ -58,9 +58,13 @@ def parse():
     p.add_argument("--seed", type=int, default=42)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-steps", type=int, default=2)
-    p.add_argument("--workload", default="df", choices=["df", "serving"],
+    p.add_argument("--workload", default="df", choices=["df", "serving", "temporal"],
                    help="df: the headline (R-MAT scale 24, one graph); serving: many resident graphs under "
-                        "Poisson batch-update arrivals through lvg_server")
+                        "Poisson batch-update arrivals through lvg_server; temporal: a drifting-community "
+                        "temporal stream, insertion-only batches, all four methods")
+    p.add_argument("--drift-vertices", type=int, default=4_000_000)
+    p.add_argument("--drift-communities", type=int, default=4000)
+    p.add_argument("--drift-edges", type=int, default=200_000_000)
     p.add_argument("--graphs", type=int, default=64)
     p.add_argument("--scale-min", type=int, default=18)
     p.add_argument("--scale-max", type=int, default=22)
@@ -454,46 +458,67 @@ def run_serving(args):
             if G is not None:
                 G.close()
     t_setup = time.time() - t0
-    # arrivals and payloads (drawn before the timed window)
-    n_req = max(1, int(args.rate * args.duration))
-    gaps = rng.exponential(1.0 / args.rate, n_req)
-    at = np.cumsum(gaps)
-    which = rng.integers(0, len(ids), n_req)
-    sizes = np.exp(rng.uniform(np.log(args.size_min), np.log(args.size_max), n_req)).astype(np.int64)
-    payloads = [None] * n_req
-    for g in range(len(ids)):
-        reqs = np.nonzero(which == g)[0]
-        if not len(reqs):
-            continue
-        nd = (sizes[reqs] * 0.2).round().astype(np.int64)
-        ni = sizes[reqs] - nd
-        db = lvg.DeviceBatch.generate(graphs[g], int(nd.sum()), int(ni.sum()), seed=args.seed * 1000 + g)
-        hb = db.download()
-        db.close()
-        d0 = i0 = 0
-        for r, a, c in zip(reqs, nd, ni):
-            # failed deletion draws are dropped by the generator: take what is left in order
-            a2 = min(2 * int(a), len(hb.del_src) - d0)
-            payloads[r] = lvg.HostBatch(hb.del_src[d0:d0 + a2], hb.del_dst[d0:d0 + a2], hb.del_w[d0:d0 + a2],
+    def payloads_for(n_req, rate, seed):
+        """Arrival times, target graphs and host payloads of n_req requests."""
+        r = np.random.default_rng(seed)
+        at = np.cumsum(r.exponential(1.0 / rate, n_req))
+        which = r.integers(0, len(ids), n_req)
+        sizes = np.exp(r.uniform(np.log(args.size_min), np.log(args.size_max), n_req)).astype(np.int64)
+        pays = [None] * n_req
+        for g in range(len(ids)):
+            reqs = np.nonzero(which == g)[0]
+            if not len(reqs):
+                continue
+            nd = (sizes[reqs] * 0.2).round().astype(np.int64)
+            ni = sizes[reqs] - nd
+            db = lvg.DeviceBatch.generate(graphs[g], int(nd.sum()), int(ni.sum()), seed=seed * 1000 + g)
+            hb = db.download()
+            db.close()
+            d0 = i0 = 0
+            for q, a, c in zip(reqs, nd, ni):
+                # failed deletion draws are dropped by the generator: take what is left in order
+                a2 = min(2 * int(a), len(hb.del_src) - d0)
+                pays[q] = lvg.HostBatch(hb.del_src[d0:d0 + a2], hb.del_dst[d0:d0 + a2], hb.del_w[d0:d0 + a2],
                                         hb.ins_src[i0:i0 + 2 * c], hb.ins_dst[i0:i0 + 2 * c],
                                         hb.ins_w[i0:i0 + 2 * c])
-            d0 += a2
-            i0 += 2 * int(c)
-    # warm-up: one small request per graph (capture, workspace)
-    for g in ids:
-        sv.submit(g, lvg.HostBatch.empty())
-    sv.drain()
-    sv.stats(reset=True)
-    with Clocks(local) as clk:
+                d0 += a2
+                i0 += 2 * int(c)
+        return at, which, pays
+
+    def offered(rate, seed):
+        n_req = max(1, int(rate * args.duration))
+        at, which, pays = payloads_for(n_req, rate, seed)
+        sv.drain()
+        sv.stats(reset=True)
         start = time.perf_counter()
         for k in range(n_req):
             while time.perf_counter() - start < at[k]:
                 pass
-            sv.submit(int(ids[which[k]]), payloads[k])
-        offered_s = time.perf_counter() - start
+            sv.submit(int(ids[which[k]]), pays[k])
+        off_s = time.perf_counter() - start
         sv.drain()
-    st = sv.stats()
-    entries = int(sum(p.num_deletions + p.num_insertions for p in payloads))
+        st = sv.stats()
+        st["offered_requests_per_s"] = n_req / off_s
+        st["requests"] = n_req
+        st["batch_entries"] = int(sum(p.num_deletions + p.num_insertions for p in pays))
+        return st
+
+    # warm-up: one small request per graph (capture, workspace)
+    for g in ids:
+        sv.submit(g, lvg.HostBatch.empty())
+    sv.drain()
+    sweep = []
+    for i, rate in enumerate(sorted({args.rate / 8, args.rate / 4, args.rate / 2})):
+        st = offered(rate, args.seed + 100 + i)
+        sweep.append({"offered_rps": st["offered_requests_per_s"], "achieved_rps": st["requests_per_s"],
+                      "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "updates_per_s": st["updates_per_s"],
+                      "service_ms": {"queue": st["mean_queue_ms"], "apply": st["mean_apply_ms"],
+                                     "run": st["mean_run_ms"]}})
+    with Clocks(local) as clk:
+        st = offered(args.rate, args.seed + 7)
+    n_req = st["requests"]
+    entries = st["batch_entries"]
+    offered_s = n_req / st["offered_requests_per_s"]
     line = {
         "metric": "serving p99 update latency (tidy + apply + DF per request)", "value": st["p99_ms"],
         "unit": "ms", "n_gpus": world, "steps": n_req, "warmup": len(ids), "ms_per_step": st["mean_ms"],
@@ -505,11 +530,75 @@ def run_serving(args):
                    "hbm_reserved_gb": st["hbm_reserved"] / 2**30, "requests": n_req, "batch_entries": entries,
                    "setup_s": t_setup},
         "latency_ms": {"p50": st["p50_ms"], "p99": st["p99_ms"], "mean": st["mean_ms"], "max": st["max_ms"]},
+        "service_ms": {"queue": st["mean_queue_ms"], "apply": st["mean_apply_ms"], "run": st["mean_run_ms"]},
         "updates_per_s": st["updates_per_s"], "requests_per_s": st["requests_per_s"],
         "offered_requests_per_s": n_req / offered_s, "completed": st["completed"], "failed": st["failed"],
+        "sweep": sweep,
         "clocks": clk.summary(),
     }
     sv.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_temporal(args):
+    """Temporal drift: a stream of drift-edges undirected edges over
+    drift-vertices vertices in drift-communities log-normal communities
+    (sigma 1, 85 % intra), 1 % of the vertices moving every 10M edges; the
+    first 90 % form the base graph (main.cxx:159-161), then insertion-only
+    batches of 1e-5, 1e-4 and 1e-3 of the stream's lines are tidied and
+    applied to a copy of the base (main.cxx:102-109) and static, ND, DS and DF
+    Louvain run from the base's static result. value = DF ms at 1e-4."""
+    rank, world, local = dist_info()
+    import lvg
+    import lvg_build
+
+    lvg_build.build()
+    lvg.set_device(local)
+    n, E = args.drift_vertices, args.drift_edges
+    t0 = time.time()
+    src, dst, _ = lvg.temporal_drift(n, args.drift_communities, E, sigma=1.0, p_in=0.85,
+                                     drift_every=10_000_000, drift=0.01, seed=args.seed)
+    tgen = time.time() - t0
+    base = int(0.9 * E)
+    t0 = time.time()
+    X = lvg.Graph.from_edges(n + 1, np.concatenate([src[:base], dst[:base]]),
+                             np.concatenate([dst[:base], src[:base]]))
+    tbuild = time.time() - t0
+    o = lvg.LouvainOptions()
+    prior = lvg.louvain_static(X, o)
+    rows = []
+    for f in (1e-5, 1e-4, 1e-3):
+        k = int(f * E)
+        a, b = src[base:base + k], dst[base:base + k]
+        ins = lvg.HostBatch(np.zeros(0, np.uint32), np.zeros(0, np.uint32), np.zeros(0, np.float32),
+                            np.concatenate([a, b]), np.concatenate([b, a]), np.ones(2 * k, np.float32))
+        Y = X.clone()
+        t0 = time.perf_counter()
+        tb = Y.apply_batch(ins)
+        apply_ms = (time.perf_counter() - t0) * 1e3
+        row = {"batch_fraction": f, "lines": k, "tidied_insertions": tb.num_insertions, "apply_ms": apply_ms}
+        for name, fn in (("static", None), ("nd", lvg.louvain_naive_dynamic),
+                         ("ds", lvg.louvain_dynamic_delta_screening), ("df", lvg.louvain_dynamic_frontier)):
+            ms = []
+            for _ in range(3):
+                r = lvg.louvain_static(Y, o) if fn is None else fn(Y, tb, prior.membership, prior.vertexWeight,
+                                                                    prior.communityWeight, o)
+                ms.append(r.time)
+            row[name + "_ms"] = float(np.median(ms))
+            row[name + "_q"] = Y.modularity(r.membership)
+        row["df_speedup_vs_static"] = row["static_ms"] / row["df_ms"]
+        rows.append(row)
+        Y.close()
+    mid = rows[1]
+    line = {"metric": "temporal drift: DF-Louvain ms per insertion batch", "value": mid["df_ms"], "unit": "ms",
+            "n_gpus": world, "steps": 3, "warmup": 0, "ms_per_step": mid["df_ms"], "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"temporal drift: {n} vertices, {args.drift_communities} log-normal communities, "
+                                   f"{E} stream edges (90 % base), insertion-only batches 1e-5/1e-4/1e-3",
+                       "base_edges": X.size, "generate_s": tgen, "build_graph_s": tbuild},
+            "batches": rows}
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
@@ -521,6 +610,8 @@ def main():
         return run_reference(args)
     if args.workload == "serving":
         return run_serving(args)
+    if args.workload == "temporal":
+        return run_temporal(args)
     return run_gpu(args)
 
 

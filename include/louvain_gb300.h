@@ -250,6 +250,14 @@ int lvg_graph_create_planted_partition(uint32_t n, uint32_t block, double avg_de
                                        lvg_graph **out);
 int lvg_graph_create_rmat(int scale, double edge_factor, double a, double b, double c, int permute, uint64_t seed,
                           lvg_graph **out);
+/* The graph readTemporalOmpW + symmetrizeOmp build from an edge list
+ * (inc/snap.hxx:160-216, main.cxx:159-161), built in HBM: n directed edges
+ * (src, dst, w; w NULL = weight 1), ids < span; vertices 1..span-1 and every
+ * endpoint present; rows sorted; duplicates merged keeping the last weight. */
+int lvg_graph_create_from_edges(size_t span, size_t n, const uint32_t *src, const uint32_t *dst, const float *w,
+                                lvg_graph **out);
+/* A copy of a graph in HBM (main.cxx's `auto y = duplicate(x)`). */
+int lvg_graph_clone(lvg_graph *x, lvg_graph **out);
 /* A random batch drawn on the device as the reference draws one:
  * generateEdgeDeletions(rnd, y, deletions, begin, range, true) and
  * generateEdgeInsertions(rnd, y, insertions, begin, range, true, weight)
@@ -302,6 +310,7 @@ typedef struct lvg_server_stats_t {
   size_t   graphs, hbm_reserved;
   double   p50_ms, p99_ms, max_ms, mean_ms;  /* request latency */
   double   wall_s, updates_per_s, requests_per_s;
+  double   mean_queue_ms, mean_apply_ms, mean_run_ms;  /* where a request's time goes */
 } lvg_server_stats_t;
 void lvg_server_options_default(lvg_server_options *o);
 /* Estimated device bytes of a resident graph (the admission rule). */

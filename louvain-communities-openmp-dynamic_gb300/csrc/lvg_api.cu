@@ -1211,6 +1211,103 @@ int lvg_graph_create_rmat(int scale, double edge_factor, double a, double b, dou
   });
 }
 
+int lvg_graph_create_from_edges(size_t span, size_t n, const uint32_t *src, const uint32_t *dst, const float *w,
+                                lvg_graph **out) {
+  if (!out || span == 0 || span > 0xFFFFFFFFull || (n && (!src || !dst)))
+    return lvg::fail(LVG_EINVAL, "lvg_graph_create_from_edges: bad argument");
+  *out = nullptr;
+  for (size_t i = 0; i < n; ++i)
+    if (src[i] >= span || dst[i] >= span) return lvg::fail(LVG_EINVAL, "lvg_graph_create_from_edges: id >= span");
+  std::unique_ptr<lvg_graph> g(new lvg_graph());
+  lvg::AcctScope acct_(&g->bytes);
+  int rc = lvg::guarded([&] {
+    LVG_CUDA(cudaGetDevice(&g->device));
+    LVG_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+    cudaStream_t s = g->stream;
+    lvg::DBuf<uint32_t> ds, dd, ckey;
+    lvg::DBuf<float> dw, cw;
+    lvg::DBuf<uint64_t> coff;
+    ds.ensure(n); dd.ensure(n); dw.ensure(n);
+    if (n) {
+      LVG_CUDA(cudaMemcpyAsync(ds.p, src, n * 4, cudaMemcpyHostToDevice, s));
+      LVG_CUDA(cudaMemcpyAsync(dd.p, dst, n * 4, cudaMemcpyHostToDevice, s));
+      if (w) {
+        LVG_CUDA(cudaMemcpyAsync(dw.p, w, n * 4, cudaMemcpyHostToDevice, s));
+      } else {
+        const float one = 1.0f;
+        lvg::launch_fill_f32(dw.p, n, one, s);
+      }
+    }
+    const size_t X = lvg::graph_from_edges(ds.p, dd.p, dw.p, n, span, coff, ckey, cw, g->ex, s);
+    ds.release(); dd.release(); dw.release();
+    std::vector<uint8_t> ex(span);
+    LVG_CUDA(cudaMemcpyAsync(ex.data(), g->ex.p, span, cudaMemcpyDeviceToHost, s));
+    LVG_CUDA(cudaStreamSynchronize(s));
+    size_t order = 0;
+    for (uint8_t e : ex) order += e;
+    g->rows_sorted = true;
+    lvg::init_graph(g.get(), span, order, X, coff.p, ckey.p, cw.p, true);
+    return LVG_OK;
+  });
+  if (rc != LVG_OK) {
+    if (g->stream) cudaStreamDestroy(g->stream);
+    return rc;
+  }
+  *out = g.release();
+  return LVG_OK;
+}
+
+int lvg_graph_clone(lvg_graph *x, lvg_graph **out) {
+  if (!x || !out) return lvg::fail(LVG_EINVAL, "null argument");
+  *out = nullptr;
+  std::unique_ptr<lvg_graph> g(new lvg_graph());
+  lvg::AcctScope acct_(&g->bytes);
+  int rc = lvg::guarded([&] {
+    LVG_CUDA(cudaSetDevice(x->device));
+    g->device = x->device;
+    LVG_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+    cudaStream_t s = g->stream;
+    LVG_CUDA(cudaStreamSynchronize(x->stream));
+    const size_t S = x->base.span;
+    auto copy = [&](auto &dst, const auto &src, size_t count) {
+      dst.ensure(count);
+      if (count) LVG_CUDA(cudaMemcpyAsync(dst.p, src.p, count * sizeof(*src.p), cudaMemcpyDeviceToDevice, s));
+    };
+    copy(g->off, x->off, S + 1);
+    copy(g->deg, x->deg, S + 1);
+    copy(g->cap, x->cap, S);
+    copy(g->key, x->key, x->slots);
+    copy(g->w, x->w, x->slots);
+    if (x->base.ex) copy(g->ex, x->ex, S);
+    g->bins.ensure(S + 1);
+    g->upd.ensure(lvg::UPD_SLOTS);
+    g->hupd.ensure(lvg::UPD_SLOTS + 8);
+    LVG_CUDA(cudaMemsetAsync(g->upd.p, 0, lvg::UPD_SLOTS * 8, s));
+    g->slots = x->slots;
+    g->pool_begin = x->pool_begin;
+    g->pool_cursor = x->pool_cursor;
+    g->rows_sorted = x->rows_sorted;
+    g->total_weight = x->total_weight;
+    g->ctr.ensure(1);
+    g->hctr.ensure(1);
+    LVG_CUDA(cudaMemsetAsync(g->ctr.p, 0, sizeof(Counters), s));
+    lvg::Level &b = g->base;
+    b.span = S; b.order = x->base.order; b.edges = x->base.edges;
+    b.off = g->off.p; b.deg = g->deg.p; b.key = g->key.p; b.w = g->w.p; b.ex = x->base.ex ? g->ex.p : nullptr;
+    lvg::DBuf<uint32_t> scratch;
+    scratch.ensure(lvg::bin_scratch_elems(S + 1, x->base.colors));
+    lvg::compute_bins(g.get(), b, g->deg.p, g->bins.p, scratch.p, x->base.colors);  // synchronises
+    lvg::build_hub_plan(g.get(), b, g->hubplan);
+    return LVG_OK;
+  });
+  if (rc != LVG_OK) {
+    if (g->stream) cudaStreamDestroy(g->stream);
+    return rc;
+  }
+  *out = g.release();
+  return LVG_OK;
+}
+
 int lvg_graph_destroy(lvg_graph *g) {
   if (!g) return LVG_OK;
   cudaSetDevice(g->device);

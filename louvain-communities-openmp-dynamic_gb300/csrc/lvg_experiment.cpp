@@ -167,11 +167,9 @@ int main(int argc, char **argv) {
   std::vector<uint32_t> s, d;
   std::vector<float> w;
   in.read(size_t(0.90 * double(size)), s, d, w);
-  lvgg_edges base{s.size(), s.data(), d.data(), w.data()};
-  lvgg_csr x{};
-  if (lvgg_csr_from_edges(rows, &base, &x) != 0) die("lvgg_csr_from_edges", lvgg_last_error());
   lvg_graph *gx = nullptr;
-  check(lvg_graph_create(x.span, x.offsets, x.keys, x.weights, x.exists, &gx), "lvg_graph_create");
+  check(lvg_graph_create_from_edges(rows + 1, s.size(), s.data(), d.data(), w.data(), &gx),
+        "lvg_graph_create_from_edges");
   print_graph(gx, " (90%)");
   print_graph(gx, " (symmetrize)");  // the base is read with both directions already
   double M = 0;
@@ -186,7 +184,7 @@ int main(int argc, char **argv) {
   for (int batch = 0; batch < BATCH_LENGTH; ++batch) {
     // y = duplicate(x); tidy + apply the next lines as insertions
     lvg_graph *gy = nullptr;
-    check(lvg_graph_create(x.span, x.offsets, x.keys, x.weights, x.exists, &gy), "lvg_graph_create");
+    check(lvg_graph_clone(gx, &gy), "lvg_graph_clone");
     std::vector<uint32_t> is, id;
     std::vector<float> iw;
     in.read(size_t(batchFraction * double(size)), is, id, iw);
@@ -215,7 +213,6 @@ int main(int argc, char **argv) {
   }
   std::printf("\n");
   lvg_graph_destroy(gx);
-  lvgg_csr_free(&x);
   if (in.file) lvgg_temporal_close(in.file);
   lvgg_edges_free(&in.all);
   return 0;

@@ -179,6 +179,44 @@ __global__ void compact_draws_kernel(const uint32_t *src, const uint32_t *dst, c
   }
 }
 
+// Edge i of a list as a packed key, with its index.
+__global__ void edge_keys_kernel(const uint32_t *src, const uint32_t *dst, size_t n, int b, uint64_t *key,
+                                 uint32_t *val) {
+  GEN_STRIDE(i, n) {
+    key[i] = uint64_t(src[i]) << b | dst[i];
+    val[i] = uint32_t(i);
+  }
+}
+
+// The last of each run of equal keys (the stable sort keeps stream order, so
+// that is the last occurrence: LazyBitset's set_union_last).
+__global__ void last_flags_kernel(const uint64_t *key, size_t n, uint32_t *flag) {
+  GEN_STRIDE(i, n) flag[i] = i + 1 == n || key[i] != key[i + 1];
+}
+
+__global__ void compact_edges_kernel(const uint64_t *key, const uint32_t *val, const uint32_t *flag,
+                                     const uint32_t *pos, size_t n, const float *w, uint64_t *ukey, float *uw) {
+  GEN_STRIDE(i, n) {
+    if (!flag[i]) continue;
+    ukey[pos[i]] = key[i];
+    uw[pos[i]] = w[val[i]];
+  }
+}
+
+__global__ void csr_keys_kernel(const uint64_t *ukeys, size_t m, int b, uint32_t *key) {
+  const uint64_t mask = (uint64_t(1) << b) - 1;
+  GEN_STRIDE(i, m) key[i] = uint32_t(ukeys[i] & mask);
+}
+
+// Vertices 1..span-1 and every endpoint are present (addVerticesIfU over
+// 1..rows, then addEdge's addVertex, inc/snap.hxx:167, inc/Graph.hxx:318).
+__global__ void endpoints_present_kernel(const uint32_t *src, const uint32_t *dst, size_t n, uint8_t *ex) {
+  GEN_STRIDE(i, n) {
+    ex[src[i]] = 1;
+    ex[dst[i]] = 1;
+  }
+}
+
 int bits_for(uint64_t x) {  // bits to hold values 0..x
   int b = 1;
   while (b < 64 && (x >> b)) ++b;
@@ -287,6 +325,60 @@ size_t generate_graph(const GenSpec &g, DBuf<uint64_t> &coff, DBuf<uint32_t> &ck
   }
   present_kernel<<<grid_for(span, 256), 256, 0, s>>>(span, ex.p);
   LVG_CHECK_LAUNCH();
+  LVG_CUDA(cudaStreamSynchronize(s));  // the scratch is freed next
+  return m;
+}
+
+// The graph of an edge list (device arrays src/dst/w of n entries, ids <
+// span): rows sorted by neighbour id, duplicates merged keeping the last
+// weight in list order. Returns X.
+size_t graph_from_edges(const uint32_t *src, const uint32_t *dst, const float *w, size_t n, size_t span,
+                        DBuf<uint64_t> &coff, DBuf<uint32_t> &ckey, DBuf<float> &cw, DBuf<uint8_t> &ex,
+                        cudaStream_t s) {
+  if (n > size_t(0x7FFFFFFF)) throw Error(LVG_EINVAL, "edge list: more than 2^31-1 entries");
+  const int b = bits_for(span);
+  DBuf<uint64_t> k0, k1;
+  DBuf<uint32_t> v0, v1, flag, pos, scan;
+  DBuf<uint8_t> tmp;
+  k0.ensure(n); k1.ensure(n); v0.ensure(n); v1.ensure(n);
+  size_t m = 0;
+  const uint64_t *uniq = k1.p;
+  if (n) {
+    edge_keys_kernel<<<grid_for(n, 256), 256, 0, s>>>(src, dst, n, b, k0.p, v0.p);
+    LVG_CHECK_LAUNCH();
+    const bool alt = sort_pairs_u64(k0.p, k1.p, v0.p, v1.p, n, 2 * b, tmp, s);
+    const uint64_t *sk = alt ? k1.p : k0.p;
+    const uint32_t *sv = alt ? v1.p : v0.p;
+    uint64_t *uk = alt ? k0.p : k1.p;
+    flag.ensure(n + 1); pos.ensure(n + 1); scan.ensure(scan_scratch_elems(n + 1));
+    cw.ensure(n);
+    last_flags_kernel<<<grid_for(n, 256), 256, 0, s>>>(sk, n, flag.p);
+    LVG_CHECK_LAUNCH();
+    exclusive_scan_u32(flag.p, pos.p, n, pos.p + n, scan.p, s);
+    compact_edges_kernel<<<grid_for(n, 256), 256, 0, s>>>(sk, sv, flag.p, pos.p, n, w, uk, cw.p);
+    LVG_CHECK_LAUNCH();
+    uint32_t cnt = 0;
+    LVG_CUDA(cudaMemcpyAsync(&cnt, pos.p + n, 4, cudaMemcpyDeviceToHost, s));
+    LVG_CUDA(cudaStreamSynchronize(s));
+    m = cnt;
+    uniq = uk;
+  }
+  coff.ensure(span + 1);
+  ckey.ensure(m);
+  cw.ensure(m);
+  ex.ensure(span);
+  csr_offsets_kernel<<<grid_for(span + 1, 256), 256, 0, s>>>(uniq, m, span, b, coff.p);
+  LVG_CHECK_LAUNCH();
+  if (m) {
+    csr_keys_kernel<<<grid_for(m, 256), 256, 0, s>>>(uniq, m, b, ckey.p);
+    LVG_CHECK_LAUNCH();
+  }
+  present_kernel<<<grid_for(span, 256), 256, 0, s>>>(span, ex.p);
+  LVG_CHECK_LAUNCH();
+  if (n) {
+    endpoints_present_kernel<<<grid_for(n, 256), 256, 0, s>>>(src, dst, n, ex.p);
+    LVG_CHECK_LAUNCH();
+  }
   LVG_CUDA(cudaStreamSynchronize(s));  // the scratch is freed next
   return m;
 }

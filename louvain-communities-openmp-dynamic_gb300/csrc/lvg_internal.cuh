@@ -210,6 +210,7 @@ void bin_items_u64(const uint64_t *deg, const uint8_t *ex, size_t n, int colors,
 int grid_for(size_t n, int block, int max_blocks_per_sm = 8);
 void launch_degrees(const uint64_t *off, uint32_t *deg, size_t span, cudaStream_t s);
 void launch_fill_u8(uint8_t *p, uint8_t v, size_t n, cudaStream_t s);
+void launch_fill_f32(float *p, size_t n, float v, cudaStream_t s);
 void launch_init_static(const Level &g, uint32_t *ucom, float *utot, float *ctot, cudaStream_t s);
 void launch_total_weight(const float *w, size_t n, Counters *ctr, cudaStream_t s);  // -> ctr->fp64[0]
 void launch_prior_to_f32(const double *src, float *dst, size_t n, cudaStream_t s);
@@ -334,6 +335,9 @@ struct GenSpec {
 std::vector<uint32_t> rmat_permutation(int scale, uint64_t seed);
 size_t generate_graph(const GenSpec &g, DBuf<uint64_t> &coff, DBuf<uint32_t> &ckey, DBuf<float> &cw,
                       DBuf<uint8_t> &ex, cudaStream_t s);
+size_t graph_from_edges(const uint32_t *src, const uint32_t *dst, const float *w, size_t n, size_t span,
+                        DBuf<uint64_t> &coff, DBuf<uint32_t> &ckey, DBuf<float> &cw, DBuf<uint8_t> &ex,
+                        cudaStream_t s);
 void generate_batch(const uint64_t *off, const uint32_t *deg, const uint32_t *key, const float *w, size_t nd,
                     size_t ni, uint32_t begin, uint32_t range, float weight, uint64_t seed, DBuf<uint32_t> &ds,
                     DBuf<uint32_t> &dd, DBuf<float> &dw, DBuf<uint32_t> &is, DBuf<uint32_t> &id,

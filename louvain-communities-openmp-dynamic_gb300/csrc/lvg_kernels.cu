@@ -70,6 +70,10 @@ __global__ void total_weight_kernel(const float *w, size_t m, double *dst) {
   block_add_double(s, dst);
 }
 
+__global__ void fill_f32_kernel(float *p, size_t n, float v) {
+  GRID_STRIDE(i, n) p[i] = v;
+}
+
 __global__ void prior_to_f32_kernel(const double *src, float *dst, size_t n) {
   GRID_STRIDE(i, n) dst[i] = float(src[i]);
 }
@@ -441,6 +445,12 @@ void launch_degrees(const uint64_t *off, uint32_t *deg, size_t span, cudaStream_
 
 void launch_fill_u8(uint8_t *p, uint8_t v, size_t n, cudaStream_t s) {
   if (n) LVG_CUDA(cudaMemsetAsync(p, v, n, s));
+}
+
+void launch_fill_f32(float *p, size_t n, float v, cudaStream_t s) {
+  if (!n) return;
+  fill_f32_kernel<<<grid_for(n, 256), 256, 0, s>>>(p, n, v);
+  LVG_CHECK_LAUNCH();
 }
 
 void launch_init_static(const Level &g, uint32_t *ucom, float *utot, float *ctot, cudaStream_t s) {

@@ -68,6 +68,7 @@ struct lvg_server {
   int device = 0;
   // statistics since the last reset
   std::vector<double> lat;
+  double sum_queue = 0, sum_apply = 0, sum_run = 0;
   uint64_t completed = 0, updates = 0, failed = 0;
   double t_first = 0, t_last = 0;
 };
@@ -139,6 +140,9 @@ void worker(lvg_server *sv) {
       ++sv->completed;
       sv->updates += r.ds.size() + r.is.size();
       sv->lat.push_back(info.latency_ms);
+      sv->sum_queue += info.queue_ms;
+      sv->sum_apply += info.apply_ms;
+      sv->sum_run += info.run_ms;
     } else {
       ++sv->failed;
     }
@@ -288,12 +292,16 @@ int lvg_server_stats(lvg_server *sv, int reset, lvg_server_stats_t *out) {
     double sum = 0;
     for (double x : l) sum += x;
     out->mean_ms = sum / double(l.size());
+    out->mean_queue_ms = sv->sum_queue / double(l.size());
+    out->mean_apply_ms = sv->sum_apply / double(l.size());
+    out->mean_run_ms = sv->sum_run / double(l.size());
   }
   out->wall_s = sv->t_last > sv->t_first ? (sv->t_last - sv->t_first) / 1e3 : 0;
   out->updates_per_s = out->wall_s > 0 ? double(sv->updates) / out->wall_s : 0;
   out->requests_per_s = out->wall_s > 0 ? double(sv->completed) / out->wall_s : 0;
   if (reset) {
     sv->lat.clear();
+    sv->sum_queue = sv->sum_apply = sv->sum_run = 0;
     sv->completed = sv->updates = sv->failed = 0;
     sv->t_first = sv->t_last = 0;
   }

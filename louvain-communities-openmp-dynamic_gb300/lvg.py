@@ -94,7 +94,8 @@ class _ServerStats(C.Structure):
     _fields_ = [("completed", C.c_uint64), ("failed", C.c_uint64), ("updates", C.c_uint64), ("graphs", C.c_size_t),
                 ("hbm_reserved", C.c_size_t), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
                 ("max_ms", C.c_double), ("mean_ms", C.c_double), ("wall_s", C.c_double),
-                ("updates_per_s", C.c_double), ("requests_per_s", C.c_double)]
+                ("updates_per_s", C.c_double), ("requests_per_s", C.c_double), ("mean_queue_ms", C.c_double),
+                ("mean_apply_ms", C.c_double), ("mean_run_ms", C.c_double)]
 
 
 class _Stats(C.Structure):
@@ -116,6 +117,11 @@ class _GBatch(C.Structure):
                 ("del_src", C.POINTER(C.c_uint32)), ("del_dst", C.POINTER(C.c_uint32)),
                 ("del_w", C.POINTER(C.c_float)), ("ins_src", C.POINTER(C.c_uint32)),
                 ("ins_dst", C.POINTER(C.c_uint32)), ("ins_w", C.POINTER(C.c_float))]
+
+
+class _Edges(C.Structure):
+    _fields_ = [("n", C.c_size_t), ("src", C.POINTER(C.c_uint32)), ("dst", C.POINTER(C.c_uint32)),
+                ("w", C.POINTER(C.c_float))]
 
 
 # ----------------------------------------------------------------- loading
@@ -178,6 +184,8 @@ def load_library() -> C.CDLL:
     L.lvg_graph_download.argtypes = [vp, _u64p, vp, vp, vp]
     L.lvg_graph_create_planted_partition.argtypes = [C.c_uint32, C.c_uint32, f64, f64, C.c_uint64, C.POINTER(vp)]
     L.lvg_graph_create_rmat.argtypes = [i32, f64, f64, f64, f64, i32, C.c_uint64, C.POINTER(vp)]
+    L.lvg_graph_create_from_edges.argtypes = [sz, sz, vp, vp, vp, C.POINTER(vp)]
+    L.lvg_graph_clone.argtypes = [vp, C.POINTER(vp)]
     L.lvg_device_batch_generate.argtypes = [vp, sz, sz, C.c_uint32, C.c_uint32, C.c_float, C.c_uint64,
                                             C.POINTER(vp)]
     L.lvg_device_batch_size.argtypes = [vp, C.POINTER(sz), C.POINTER(sz)]
@@ -223,6 +231,14 @@ def load_graphgen() -> C.CDLL:
     G.lvgg_reference_batch.argtypes = [C.POINTER(_Csr), C.c_size_t, C.c_size_t, C.c_uint32, C.c_uint32, C.c_float,
                                        C.c_uint64, C.POINTER(_GBatch)]
     G.lvgg_csr_free.argtypes = [C.POINTER(_Csr)]
+    G.lvgg_temporal_open.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_void_p)]
+    G.lvgg_temporal_read.argtypes = [C.c_void_p, C.c_size_t, C.c_int, C.POINTER(_Edges)]
+    G.lvgg_temporal_close.argtypes = [C.c_void_p]
+    G.lvgg_temporal_write.argtypes = [C.c_char_p, C.POINTER(_Edges)]
+    G.lvgg_csr_from_edges.argtypes = [C.c_size_t, C.POINTER(_Edges), C.POINTER(_Csr)]
+    G.lvgg_temporal_drift.argtypes = [C.c_uint32, C.c_uint32, C.c_double, C.c_size_t, C.c_double, C.c_size_t,
+                                      C.c_double, C.c_uint64, C.POINTER(_Edges)]
+    G.lvgg_edges_free.argtypes = [C.POINTER(_Edges)]
     G.lvgg_batch_free.argtypes = [C.POINTER(_GBatch)]
     _gen = G
     return G
@@ -327,6 +343,86 @@ def _take_csr(c: _Csr) -> HostGraph:
                   np.ctypeslib.as_array(c.exists, (S,)).copy())
     G.lvgg_csr_free(C.byref(c))
     return g
+
+
+def _take_edges(G, e: _Edges):
+    n = e.n
+    out = (np.ctypeslib.as_array(e.src, (max(n, 1),))[:n].copy(),
+           np.ctypeslib.as_array(e.dst, (max(n, 1),))[:n].copy(),
+           np.ctypeslib.as_array(e.w, (max(n, 1),))[:n].copy())
+    G.lvgg_edges_free(C.byref(e))
+    return out
+
+
+def _edges_struct(src, dst, w):
+    src = np.ascontiguousarray(src, np.uint32)
+    dst = np.ascontiguousarray(dst, np.uint32)
+    w = np.ascontiguousarray(w, np.float32)
+    e = _Edges(len(src), src.ctypes.data_as(C.POINTER(C.c_uint32)), dst.ctypes.data_as(C.POINTER(C.c_uint32)),
+               w.ctypes.data_as(C.POINTER(C.c_float)))
+    return e, (src, dst, w)
+
+
+class TemporalReader:
+    """A SNAP temporal file read in order (lvgg_temporal_open/read; inc/snap.hxx:41-140)."""
+
+    def __init__(self, path: str, weighted: bool = False):
+        self._G = load_graphgen()
+        self.h = C.c_void_p()
+        if self._G.lvgg_temporal_open(path.encode(), int(weighted), C.byref(self.h)) != 0:
+            raise LvgError(LVG_EINVAL, self._G.lvgg_last_error().decode())
+
+    def read(self, lines: int, symmetric: bool = True):
+        """The next `lines` lines as (src, dst, w), both directions when symmetric."""
+        e = _Edges()
+        if self._G.lvgg_temporal_read(self.h, lines, int(symmetric), C.byref(e)) != 0:
+            raise LvgError(LVG_EINVAL, self._G.lvgg_last_error().decode())
+        return _take_edges(self._G, e)
+
+    def close(self) -> None:
+        if self.h:
+            self._G.lvgg_temporal_close(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def write_temporal(path: str, src, dst, w=None) -> None:
+    """Edges as a SNAP temporal file ("u v t" lines)."""
+    G = load_graphgen()
+    e, keep = _edges_struct(src, dst, np.ones(len(src), np.float32) if w is None else w)
+    if G.lvgg_temporal_write(path.encode(), C.byref(e)) != 0:
+        raise LvgError(LVG_EINVAL, G.lvgg_last_error().decode())
+
+
+def csr_from_edges(rows: int, src, dst, w=None) -> HostGraph:
+    """The graph readTemporalOmpW builds from an edge list (lvgg_csr_from_edges)."""
+    G = load_graphgen()
+    e, keep = _edges_struct(src, dst, np.ones(len(src), np.float32) if w is None else w)
+    c = _Csr()
+    if G.lvgg_csr_from_edges(rows, C.byref(e), C.byref(c)) != 0:
+        raise LvgError(LVG_EINVAL, G.lvgg_last_error().decode())
+    return _take_csr(c)
+
+
+def temporal_drift(n: int, communities: int, edges: int, sigma: float = 1.0, p_in: float = 0.85,
+                   drift_every: int | None = None, drift: float = 0.01, seed: int = 42):
+    """Synthetic temporal stream with drifting communities (lvgg_temporal_drift): (src, dst, w)."""
+    G = load_graphgen()
+    e = _Edges()
+    every = max(1, edges // 20) if drift_every is None else drift_every
+    if G.lvgg_temporal_drift(n, communities, sigma, edges, p_in, every, drift, seed, C.byref(e)) != 0:
+        raise LvgError(LVG_EINVAL, G.lvgg_last_error().decode())
+    return _take_edges(G, e)
+
+
+def experiment_path() -> str:
+    """The experiment driver (louvain_gb300_experiment), built beside the libraries."""
+    return os.path.join(LIBDIR, "louvain_gb300_experiment")
 
 
 def planted_partition(n: int, block: int, avg_degree: float, p_in: float, seed: int) -> HostGraph:
@@ -472,6 +568,24 @@ class Graph:
         """Generated in HBM (lvg_graph_create_rmat); equals rmat()."""
         G = cls(None)
         _check(G._L.lvg_graph_create_rmat(scale, edge_factor, a, b, c, int(permute), seed, C.byref(G.h)))
+        return G
+
+    @classmethod
+    def from_edges(cls, span: int, src, dst, w=None) -> "Graph":
+        """Built in HBM from an edge list as readTemporalOmpW builds its graph
+        (lvg_graph_create_from_edges); equals csr_from_edges(span - 1, ...)."""
+        G = cls(None)
+        src = np.ascontiguousarray(src, np.uint32)
+        dst = np.ascontiguousarray(dst, np.uint32)
+        wp = None if w is None else np.ascontiguousarray(w, np.float32)
+        _check(G._L.lvg_graph_create_from_edges(span, len(src), src.ctypes.data, dst.ctypes.data,
+                                                None if wp is None else wp.ctypes.data, C.byref(G.h)))
+        return G
+
+    def clone(self) -> "Graph":
+        """A copy in HBM (lvg_graph_clone)."""
+        G = Graph(None)
+        _check(self._L.lvg_graph_clone(self.h, C.byref(G.h)))
         return G
 
     def close(self) -> None:

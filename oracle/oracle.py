@@ -231,6 +231,8 @@ class Reference:
         L.ref_graph_size.argtypes = [_vp]
         L.ref_graph_size.restype = _sz
         L.ref_graph_csr.argtypes = [_vp, _u64p, _u32p, _f32p, _u8p]
+        L.ref_read_temporal.argtypes = [C.c_char_p, _sz, _sz]
+        L.ref_read_temporal.restype = _vp
         L.ref_graph_csr.restype = _sz
         L.ref_modularity.argtypes = [_vp, _u32p, C.c_double, C.c_double]
         L.ref_modularity.restype = C.c_double
@@ -241,6 +243,20 @@ class Reference:
 
     def threads(self, t: int) -> None:
         self.L.ref_set_threads(t)
+
+    def read_temporal(self, path: str, rows: int, lines: int):
+        """main.cxx's base graph: the first `lines` lines of a SNAP temporal file,
+        read both ways and symmetrized; returns (offsets, keys, weights, exists)."""
+        h = self.L.ref_read_temporal(path.encode(), rows, lines)
+        try:
+            S = rows + 1
+            X = int(self.L.ref_graph_size(h))
+            off = np.zeros(S + 1, np.uint64)
+            k, w, ex = np.zeros(max(X, 1), np.uint32), np.zeros(max(X, 1), np.float32), np.zeros(S, np.uint8)
+            m = self.L.ref_graph_csr(h, off, k, w, ex)
+            return off, k[:m].copy(), w[:m].copy(), ex
+        finally:
+            self.L.ref_graph_free(h)
 
     def graph(self, g):
         S, off, k, w, ex = _graph_args(g)

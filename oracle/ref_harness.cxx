@@ -21,10 +21,13 @@
 //   ref_apply_batch     -> tidyBatchUpdateU + applyBatchUpdateOmpU
 //                          (inc/batch.hxx:202, 241), in place
 //   ref_graph_csr       -> the graph's rows (forEachEdge) as a compact CSR
+//   ref_read_temporal   -> readTemporalOmpW + symmetrizeOmp (inc/snap.hxx:212,
+//                          inc/symmetrize.hxx:72), as main.cxx:159-161
 #include "inc/main.hxx"
 
 #include <cstdint>
 #include <cstring>
+#include <fstream>
 #include <omp.h>
 
 using K = uint32_t;
@@ -166,6 +169,15 @@ void ref_apply_batch(void *gp, size_t nd, const uint32_t *ds, const uint32_t *dd
   for (size_t i = 0; i < ins.size(); ++i) std::tie(tis[i], tid[i], tiw[i]) = ins[i];
   *tnd = del.size();
   *tni = ins.size();
+}
+
+// main.cxx:159-161: readTemporalOmpW(x, file, false, true, rows, lines) then
+// x = symmetrizeOmp(x). Returns the graph (free with ref_graph_free).
+void *ref_read_temporal(const char *path, size_t rows, size_t lines) {
+  G x;
+  std::ifstream f(path);
+  readTemporalOmpW(x, f, false, true, rows, lines);
+  return new G(symmetrizeOmp(x));
 }
 
 // Compact CSR of the graph: off[span+1], key/w[size], ex[span]. Returns size.

@@ -17,7 +17,8 @@ apply.npz holds the batch-update fixtures: untidy batches (unsorted, with
 duplicates, deletions of absent edges, insertions of present edges and of
 edges touching absent vertices) run through the reference's
 tidyBatchUpdateU + applyBatchUpdateOmpU, twice in a row; the graphs after
-each batch and the tidied batches. `--only apply` regenerates just that file.
+each batch and the tidied batches. temporal.npz holds a temporal stream and the
+base graph main.cxx builds from it. `--only apply` regenerates just these two.
 """
 from __future__ import annotations
 
@@ -137,6 +138,23 @@ def apply_fixtures(ref) -> None:
     np.savez_compressed(os.path.join(OUT, "apply.npz"), **d)
 
 
+def temporal_fixture(ref) -> None:
+    """temporal.npz: a small drifting-community stream (the lines of a SNAP
+    temporal file) and the base graph the reference's main.cxx builds from its
+    first 90 % (readTemporalOmpW + symmetrizeOmp)."""
+    import tempfile
+
+    rows, lines = 3000, 12000
+    src, dst, _ = lvg.temporal_drift(rows, 60, lines, seed=5)
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "t.txt")
+        lvg.write_temporal(path, src, dst)
+        off, key, w, ex = ref.read_temporal(path, rows, int(0.9 * lines))
+    np.savez_compressed(os.path.join(OUT, "temporal.npz"), src=src, dst=dst, rows=rows, lines=lines,
+                        x_off=off, x_key=key, x_w=w, x_ex=ex)
+    print("temporal", rows, lines, "base edges", len(key))
+
+
 def cases():
     yield "pp2k", lvg.planted_partition(2048, 128, 16, 0.8, 11), 200
     yield "rmat11", lvg.rmat(11, 16, seed=5), 200
@@ -158,6 +176,7 @@ def main() -> None:
     O.build(ref=True)
     ref = O.Reference()
     apply_fixtures(ref)
+    temporal_fixture(ref)
     if sys.argv[1:] == ["--only", "apply"]:
         return
     for name, x, nupd in cases():
