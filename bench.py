@@ -58,10 +58,13 @@ def parse():
     p.add_argument("--seed", type=int, default=42)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-steps", type=int, default=2)
-    p.add_argument("--workload", default="df", choices=["df", "serving", "temporal"],
+    p.add_argument("--workload", default="df", choices=["df", "serving", "temporal", "batched"],
                    help="df: the headline (R-MAT scale 24, one graph); serving: many resident graphs under "
                         "Poisson batch-update arrivals through lvg_server; temporal: a drifting-community "
                         "temporal stream, insertion-only batches, all four methods")
+    p.add_argument("--batched-graphs", type=int, default=4096)
+    p.add_argument("--batched-loop", type=int, default=512,
+                   help="batched: graphs the one-by-one comparator runs (a prefix of the batch)")
     p.add_argument("--drift-vertices", type=int, default=4_000_000)
     p.add_argument("--drift-communities", type=int, default=4000)
     p.add_argument("--drift-edges", type=int, default=200_000_000)
@@ -74,6 +77,8 @@ def parse():
     p.add_argument("--size-max", type=int, default=100000)
     p.add_argument("--workers", type=int, default=16)
     p.add_argument("--budget-gb", type=float, default=120.0)
+    p.add_argument("--coalesce", type=int, default=1 << 18,
+                   help="serving: serve a graph's queued requests as one batch of up to this many entries (0: off)")
     p.add_argument("--ncu-steps", type=int, default=0,
                    help="profiling mode: set up as usual, then run this many DF steps between "
                         "cudaProfilerStart/Stop (for ncu --profile-from-start off) and exit")
@@ -292,8 +297,11 @@ def run_gpu(args):
             info = lvg.run_resident(Y, lvg.METHOD_FRONTIER, db, st_prior, st_out, o)
         lvg.profiler_stop()
         if rank == 0:
-            print(f"profiled {args.ncu_steps} DF steps: last {info['time']:.3f} ms, {Y.stats()['kernel_launches']} "
-                  f"kernel launches per step", flush=True)
+            st = Y.stats()
+            print(json.dumps({"profiled_df_steps": args.ncu_steps, "last_ms": info["time"],
+                              "kernel_launches_per_step": st["kernel_launches"],
+                              "algorithmic_bytes_per_step": MOVE_BYTES_PER_EDGE * st["move_edges"] +
+                              MOVE_BYTES_PER_VERTEX * st["move_vertices"]}), flush=True)
         dist.close()
         return 0
 
@@ -351,6 +359,8 @@ def run_gpu(args):
     for _ in range(args.steps):
         lvg.louvain_dynamic_frontier(Y, b, pq.array, pvt.array, pct.array, o, out_buffers=ob)
     e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    cs = Y.stats()
+    e2e_parts = {"upload_ms": cs["call_upload_ms"], "run_ms": cs["call_run_ms"], "download_ms": cs["call_download_ms"]}
     e2e_ms_max = dist.max(e2e_ms)
     h2d = b.num_deletions * 12 + b.num_insertions * 12 + S * (4 + 8 + 8)
     d2h = S * (4 + 8 + 8)
@@ -372,7 +382,8 @@ def run_gpu(args):
                    "l2": "inputs larger than L2 (CSR %.1f GB)" % (E * 8 / 1e9)},
         "e2e": {"value": world * E / (e2e_ms_max / 1e3), "unit": "edges/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms_max,
-                "call": "lvg_frontier (drop-in for louvainDynamicFrontierOmp), pinned host arrays"},
+                "call": "lvg_frontier (drop-in for louvainDynamicFrontierOmp), pinned host arrays",
+                "last_call_parts": e2e_parts},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
@@ -441,7 +452,7 @@ def run_serving(args):
     lvg.set_device(local)
     rng = np.random.default_rng(args.seed)
     budget = int(args.budget_gb * (1 << 30))
-    sv = lvg.Server(workers=args.workers, hbm_budget=budget, method=lvg.METHOD_FRONTIER)
+    sv = lvg.Server(workers=args.workers, hbm_budget=budget, method=lvg.METHOD_FRONTIER, coalesce=args.coalesce)
     t0 = time.time()
     graphs, ids, refused = [], [], 0
     scales = rng.integers(args.scale_min, args.scale_max + 1, args.graphs)
@@ -525,7 +536,8 @@ def run_serving(args):
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"serving: {len(ids)} resident R-MAT graphs scale {args.scale_min}-{args.scale_max} "
                                f"ef16, Poisson {args.rate:g} req/s for {args.duration:g} s, log-uniform "
-                               f"[{args.size_min}, {args.size_max}] updates 80/20, {args.workers} workers",
+                               f"[{args.size_min}, {args.size_max}] updates 80/20, {args.workers} workers, "
+                               f"coalescing up to {args.coalesce} entries",
                    "graphs": len(ids), "refused_by_admission": refused, "hbm_budget_gb": args.budget_gb,
                    "hbm_reserved_gb": st["hbm_reserved"] / 2**30, "requests": n_req, "batch_entries": entries,
                    "setup_s": t_setup},
@@ -604,6 +616,60 @@ def run_temporal(args):
     return 0
 
 
+def run_batched(args):
+    """Batched: planted-partition graphs with |V| log-uniform in [1k, 256k],
+    average degree uniform in [8, 32], blocks of 128 (C = |V|/128), p_in
+    uniform in [0.6, 0.9], all resident in HBM (generated there). Static
+    Louvain on all of them through lvg_static_many (graphs overlapped on the
+    GPU, one stream each) against lvg_static one graph after another on a
+    prefix. value = edges/s of the batched run."""
+    rank, world, local = dist_info()
+    import lvg
+    import lvg_build
+
+    lvg_build.build()
+    lvg.set_device(local)
+    rng = np.random.default_rng(args.seed)
+    n = args.batched_graphs
+    sizes = np.exp(rng.uniform(np.log(1000), np.log(256_000), n)).astype(np.int64)
+    degs = rng.uniform(8, 32, n)
+    pins = rng.uniform(0.6, 0.9, n)
+    t0 = time.time()
+    graphs = [lvg.Graph.planted_partition(int(v), 128, float(d), float(p), args.seed + i)
+              for i, (v, d, p) in enumerate(zip(sizes, degs, pins))]
+    tgen = time.time() - t0
+    E = sum(g.size for g in graphs)
+    o = lvg.LouvainOptions()
+    k = min(args.batched_loop, n)
+    lvg.louvain_static_many(graphs[:32], o, workers=args.workers, trim=2)  # warm-up
+    t0 = time.perf_counter()
+    for g in graphs[:k]:
+        lvg.louvain_static(g, o)
+        g.trim(2)
+    loop_s = time.perf_counter() - t0
+    Ek = sum(g.size for g in graphs[:k])
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        res = lvg.louvain_static_many(graphs, o, workers=args.workers, trim=2)
+        many_s = time.perf_counter() - t0
+    qs = [graphs[i].modularity(res[i]["membership"]) for i in range(0, n, max(1, n // 16))]
+    line = {"metric": "batched static Louvain edges/s (many graphs)", "value": E / many_s, "unit": "edges/s",
+            "n_gpus": world, "steps": 1, "warmup": 1, "ms_per_step": many_s * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"batched: {n} planted-partition graphs, |V| log-uniform [1k, 256k], degree "
+                                   f"U[8, 32], blocks of 128, p_in U[0.6, 0.9]; lvg_static_many with "
+                                   f"{args.workers} workers vs lvg_static one by one",
+                       "graphs": n, "vertices": int(sizes.sum()), "edges": E, "generate_s": tgen},
+            "graphs_per_s": n / many_s,
+            "one_by_one": {"graphs": k, "edges_per_s": Ek / loop_s, "graphs_per_s": k / loop_s},
+            "speedup_vs_one_by_one": (E / many_s) / (Ek / loop_s),
+            "modularity_sample": {"min": float(np.min(qs)), "mean": float(np.mean(qs))},
+            "clocks": clk.summary()}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -612,6 +678,8 @@ def main():
         return run_serving(args)
     if args.workload == "temporal":
         return run_temporal(args)
+    if args.workload == "batched":
+        return run_batched(args)
     return run_gpu(args)
 
 

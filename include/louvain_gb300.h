@@ -296,6 +296,8 @@ typedef struct lvg_server_options {
   size_t      hbm_budget;  /* admission budget in bytes for resident graphs (default 120 GiB) */
   int         method;      /* LVG_METHOD_NAIVE / _DELTA / _FRONTIER (default FRONTIER) */
   lvg_options louvain;     /* options of every run */
+  size_t      coalesce;    /* 0: one request per run; else serve a graph's queued requests as one batch of
+                              up to this many entries (their union, tidied and applied at once) */
 } lvg_server_options;
 typedef struct lvg_request_info {
   uint64_t ticket;
@@ -331,6 +333,15 @@ int lvg_server_stats(lvg_server *sv, int reset, lvg_server_stats_t *out);
 /* A graph's current state (after its queued requests), into host arrays. */
 int lvg_server_membership(lvg_server *sv, int graph_id, uint32_t *membership, double *vtot, double *ctot);
 lvg_graph *lvg_server_graph(lvg_server *sv, int graph_id);
+/* Static Louvain on many graphs at once (no reference counterpart; the
+ * reference runs one graph per process): `workers` host threads each take the
+ * next graph and run lvg_static on its own stream, so the GPU overlaps the
+ * graphs' kernels; with trim > 0 each graph is trimmed (lvg_graph_trim) after
+ * its run, so only `workers` workspaces are held at a time. results[i] as
+ * lvg_static fills it. Returns the first failure's status (the other graphs
+ * still run). */
+int lvg_static_many(lvg_graph *const *graphs, size_t n, const lvg_options *o, int workers, int trim,
+                    lvg_result *results);
 /* Drains, stops the workers, frees the states and owned graphs. */
 int lvg_server_destroy(lvg_server *sv);
 
@@ -353,6 +364,9 @@ typedef struct lvg_stats {
   double   move_bin_ms[12];
   uint64_t move_bin_vertices[12];
   uint64_t move_bin_edges[12];
+  /* Host-array entry points (lvg_static/.../lvg_frontier): wall-clock time of
+   * the call's three parts — batch + prior upload, the run, result download. */
+  double   call_upload_ms, call_run_ms, call_download_ms;
 } lvg_stats;
 /* Enable (1) or disable (0) per-launch event timing for calls on g. */
 int lvg_set_profiling(lvg_graph *g, int enable);

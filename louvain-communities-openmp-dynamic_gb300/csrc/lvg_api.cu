@@ -8,6 +8,7 @@
 // own CUDA stream; the host only reads back the per-iteration gain sum and the
 // per-pass community count to take the reference's branch decisions.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -330,7 +331,7 @@ void ensure_global_tables(Workspace &W, size_t blocks, int log2cap, bool first_t
 // its marks merged before the next class. The device gain sum is reset first.
 // With bin_ev, events bracket each bin launch (profiling).
 void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const float *tot,
-                       const uint8_t *fa, float kr, bool sync, const int *glog2, size_t need,
+                       const uint8_t *fa, float kr, bool sync, bool fused, const int *glog2, size_t need,
                        std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> *bin_ev) {
   Workspace &W = *g->ws;
   cudaStream_t s = g->stream;
@@ -343,7 +344,36 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot
     for (int b = 0; b <= NUM_BINS; ++b) bb.start[b] = lv.bin_start[k * NUM_BINS + b];
     uint32_t *wlc = W.wl_count.p + size_t(k) * NUM_BINS;
     if (bb.start[NUM_BINS - 1] > bb.start[1]) launch_compact_active(lv.bins, bb, W.vaff.p, fa, W.wl.p, wlc, s);
-    for (int b = 1; b < NUM_BINS; ++b) {
+    if (fused) {
+      // bins 1-6 and 7-8 in one launch each; each bin gets blocks for its
+      // bucket, at most two per SM (its worklist is short)
+      static const int tpb[NUM_BINS] = {0, 64, 32, 16, 8, 8, 8, 8, 8, 0, 0, 0};
+      const size_t cap = size_t(device_sms()) * 2;
+      for (const auto &grp : {std::pair<int, int>{1, 6}, std::pair<int, int>{7, 8}}) {
+        SmallBins sb{};
+        uint32_t nb = 0;
+        for (int b = grp.first; b <= grp.second; ++b) {
+          const int j = b - grp.first;
+          const size_t cnt = lv.bucket_size(k, b);
+          sb.list[j] = W.wl.p + lv.bucket_begin(k, b);
+          sb.count_ptr[j] = wlc + b;
+          sb.block_begin[j] = nb;
+          nb += uint32_t(std::min(cap, (cnt + tpb[b] - 1) / tpb[b]));
+        }
+        sb.block_begin[grp.second - grp.first + 1] = nb;
+        if (!nb) continue;
+        MoveArgs a;
+        a.off = lv.off; a.deg = lv.deg; a.key = lv.key; a.w = lv.w;
+        a.vcom = com; a.ctot = ctot; a.dec = W.dec.p;
+        a.vaff = W.vaff.p; a.mark = W.mark.p; a.fa = fa; a.vtot = tot;
+        a.kr = kr; a.ctr = g->ctr.p; a.bin = grp.first;
+        cudaEvent_t b0 = bin_ev ? g->events.record(s) : nullptr;
+        launch_move_small(grp.first, grp.second, sync, a, sb, s);
+        if (bin_ev) bin_ev->push_back({grp.first, {b0, g->events.record(s)}});
+        ++g->stats.move_launches;
+      }
+    }
+    for (int b = fused ? 9 : 1; b < NUM_BINS; ++b) {
       const size_t cnt = lv.bucket_size(k, b);
       if (!cnt) continue;
       MoveArgs a;
@@ -382,7 +412,8 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot
 // eager iteration, so every kernel's attributes are already set). A capture
 // failure disables graphs for this handle; the eager path stays correct.
 void capture_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const float *tot,
-                       const uint8_t *fa, float kr, bool sync, const int *glog2, size_t need, const IterKey &key) {
+                       const uint8_t *fa, float kr, bool sync, bool fused, const int *glog2, size_t need,
+                       const IterKey &key) {
   cudaStream_t s = g->stream;
   if (g->iter_exec) {
     cudaGraphExecDestroy(g->iter_exec);
@@ -398,7 +429,7 @@ void capture_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot
   }
   bool fine = true;
   try {
-    enqueue_iteration(g, lv, com, ctot, tot, fa, kr, sync, glog2, need, nullptr);
+    enqueue_iteration(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, need, nullptr);
   } catch (const Error &) {
     fine = false;
   }
@@ -424,13 +455,18 @@ void capture_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot
 // iteration is captured once into a CUDA graph and replayed, one graph
 // launch per iteration instead of ~12 launches per colour class.
 int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const float *tot, const uint8_t *fa,
-               double M, float kr, int L, double E, bool sync) {
+               double M, float kr, int L, double E, bool sync, bool fused) {
   Workspace &W = *g->ws;
   cudaStream_t s = g->stream;
   const int K = lv.colors;
   // Existing degree-0 vertices are processed once and never re-marked.
-  for (int k = 0; k < K; ++k)
-    launch_clear_isolated(lv.bins + lv.bucket_begin(k, 0), lv.bucket_size(k, 0), W.vaff.p, fa, s);
+  IsolatedLists iso{};
+  iso.k = K;
+  for (int k = 0; k < K; ++k) {
+    iso.list[k] = lv.bins + lv.bucket_begin(k, 0);
+    iso.n[k] = lv.bucket_size(k, 0);
+  }
+  launch_clear_isolated_multi(iso, W.vaff.p, fa, s);
   // Global fallback regions of the large-degree bins (9-11): each launch's
   // blocks get 2^glog2[b] slots, enough for the bin's largest degree.
   int glog2[NUM_BINS] = {};
@@ -459,7 +495,7 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const 
                           g->hctr.p, lv.hub.chunk, lv.hub.hub_vertex, nullptr};
     std::memcpy(key.p, ps, sizeof(ps));
     key.n[0] = lv.span; key.n[1] = need; key.n[2] = lv.hub.chunks; key.n[3] = lv.bin_start[K * NUM_BINS];
-    key.k[0] = K; key.k[1] = sync; key.k[2] = glog2[9] | glog2[10] << 8 | glog2[11] << 16;
+    key.k[0] = K; key.k[1] = sync; key.k[2] = glog2[9] | glog2[10] << 8 | glog2[11] << 16; key.k[3] = fused;
     key.kr = kr;
   }
   const bool graphs = base && !g->profiling && !g->no_graphs;
@@ -476,7 +512,8 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const 
     } else {
       bin_ev.clear();
       if (g->profiling) e0 = g->events.record(s);
-      enqueue_iteration(g, lv, com, ctot, tot, fa, kr, sync, glog2, need, g->profiling ? &bin_ev : nullptr);
+      enqueue_iteration(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, need,
+                        g->profiling ? &bin_ev : nullptr);
       if (g->profiling) e1 = g->events.record(s);
     }
     LVG_CUDA(cudaStreamSynchronize(s));
@@ -485,7 +522,7 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const 
       g->stats.move_kernel_ms += elapsed(e0, e1);
       for (auto &be : bin_ev) g->stats.move_bin_ms[be.first] += elapsed(be.second.first, be.second.second);
     }
-    if (graphs && !replay) capture_iteration(g, lv, com, ctot, tot, fa, kr, sync, glog2, need, key);
+    if (graphs && !replay) capture_iteration(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, need, key);
     el = double(g->hctr.p->el_fix) / GAIN_FIX / M;
     ++l;
     if (el <= E) break;
@@ -640,7 +677,10 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
       if (p == 1) ep1 = g->events.record(s);
       const bool first = p == 0;
       cudaEvent_t a0 = g->events.record(s);
-      const int m = move_phase(g, lv, com, ctot, tot, first ? fa : nullptr, M, kr, L, E, sync);
+      // the frontier methods' first pass works on short per-class worklists:
+      // the small degree bins go in two fused launches per class
+      const bool fused = first && (method == LVG_METHOD_FRONTIER || method == LVG_METHOD_DELTA);
+      const int m = move_phase(g, lv, com, ctot, tot, first ? fa : nullptr, M, kr, L, E, sync, fused);
       tl_ev.push_back({a0, g->events.record(s)});
       l += std::max(m, 1);
       ++p;
@@ -799,6 +839,7 @@ int run_host(lvg_graph *g, int method, const lvg_batch *b, const uint32_t *q, co
     LVG_CUDA(cudaSetDevice(g->device));
     lvg_options opt;
     if (o) opt = *o; else lvg_options_default(&opt);
+    const auto t0 = std::chrono::steady_clock::now();
     check_batch(g, b, method == LVG_METHOD_DELTA);
     ensure_ws(g);
     Workspace &W = *g->ws;
@@ -811,11 +852,19 @@ int run_host(lvg_graph *g, int method, const lvg_batch *b, const uint32_t *q, co
       upload_prior(g, q, qvtot, qctot, W.prior_q.p, W.prior_vt.p, W.prior_ct.p);
       prior = StateRef{W.prior_q.p, W.prior_vt.p, W.prior_ct.p};
     }
+    LVG_CUDA(cudaStreamSynchronize(g->stream));
+    const auto t1 = std::chrono::steady_clock::now();
     StateRef st{W.ucom.p, W.utot.p, W.ctot.p};
     RunInfo info;
     run(g, method, db, prior, st, opt, info);
     fill_result(out, info, g->base.span);
+    const auto t2 = std::chrono::steady_clock::now();
     download_result(g, out, st);
+    const auto t3 = std::chrono::steady_clock::now();
+    using ms = std::chrono::duration<double, std::milli>;
+    g->stats.call_upload_ms = ms(t1 - t0).count();
+    g->stats.call_run_ms = ms(t2 - t1).count();
+    g->stats.call_download_ms = ms(t3 - t2).count();
     return LVG_OK;
   });
 }

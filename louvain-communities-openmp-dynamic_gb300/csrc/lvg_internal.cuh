@@ -225,6 +225,12 @@ void launch_ds_mark(const Level &g, const uint32_t *ds, const uint32_t *dd, size
                     uint8_t *vertices, uint8_t *neighbors, uint8_t *communities, uint32_t *gkeys, float *gvals,
                     uint32_t *gfirst, int glog2, Counters *ctr, cudaStream_t s);
 void launch_clear_isolated(const uint32_t *list, size_t n, uint8_t *vaff, const uint8_t *fa, cudaStream_t s);
+struct IsolatedLists {
+  const uint32_t *list[MAX_COLORS];
+  size_t n[MAX_COLORS];
+  int k;
+};
+void launch_clear_isolated_multi(const IsolatedLists &L, uint8_t *vaff, const uint8_t *fa, cudaStream_t s);
 void launch_merge_marks(uint8_t *vaff, uint8_t *mark, size_t n, cudaStream_t s);
 // Worklists of one colour class: the active vertices of degree bins
 // 1..NUM_BINS-2 (positions bins[start[1] .. start[NUM_BINS-1])) are copied to
@@ -358,6 +364,16 @@ inline int global_table_log2(uint64_t maxdeg) {
   return l;
 }
 int global_table_blocks(size_t count);
+// Worklists of consecutive degree bins of one colour class for one fused
+// launch (bins lo..hi of 1..8, at most 6): list, device-side length, and the
+// first block of each bin (block_begin[hi-lo+1] = the grid).
+struct SmallBins {
+  const uint32_t *list[6];
+  const uint32_t *count_ptr[6];
+  uint32_t block_begin[7];
+};
+void launch_move_small(int lo, int hi, bool sync, const MoveArgs &a, const SmallBins &sb, cudaStream_t s);
+int device_sms();
 // Grid of the local-moving kernel of a large-degree bin (9, 10; 11 = the hub
 // merge) for `count` vertices: the size of its per-block global fallback.
 int move_grid_blocks(int bin, bool sync, size_t count);

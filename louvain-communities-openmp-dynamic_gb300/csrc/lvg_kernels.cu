@@ -1,5 +1,7 @@
 // lvg_kernels.cu — initialisation, batch-update, marking, renumbering,
 // community-CSR and modularity kernels.
+#include <algorithm>
+
 #include "lvg_internal.cuh"
 
 namespace lvg {
@@ -258,6 +260,18 @@ __global__ void clear_isolated_kernel(const uint32_t *list, size_t n, uint8_t *v
   }
 }
 
+// The same over several lists (the degree-0 buckets of every colour class):
+// block b serves list b % k.
+__global__ void clear_isolated_multi_kernel(IsolatedLists L, uint8_t *vaff, const uint8_t *fa) {
+  const int j = blockIdx.x % L.k;
+  const size_t nb = gridDim.x / L.k + (size_t(j) < gridDim.x % L.k ? 1 : 0);
+  const size_t blk = blockIdx.x / L.k;
+  for (size_t i = blk * blockDim.x + threadIdx.x; i < L.n[j]; i += nb * blockDim.x) {
+    const uint32_t u = L.list[j][i];
+    if (vaff[u] && (!fa || fa[u])) vaff[u] = 0;
+  }
+}
+
 __global__ void merge_marks_kernel(uint8_t *vaff, uint8_t *mark, size_t n) {
   GRID_STRIDE(i, n) {
     if (mark[i]) { vaff[i] = 1; mark[i] = 0; }
@@ -353,29 +367,47 @@ __global__ void level_init_kernel(size_t n, const float *vtot, uint32_t *vcom, f
 }
 
 // Active vertices of one colour class into per-bin worklists (warp-aggregated
-// appends; the order within a worklist is unspecified).
+// appends; the order within a worklist is unspecified). Each warp takes 128
+// consecutive entries, four per lane, so that four flag reads are in flight
+// per lane.
 __global__ void compact_active_kernel(const uint32_t *bins, BinBounds bb, const uint8_t *vaff, const uint8_t *fa,
                                       uint32_t *wl, uint32_t *wl_count) {
+  constexpr int V = 4;
   const uint64_t begin = bb.start[1], end = bb.start[NUM_BINS - 1];
   const int lane = threadIdx.x & 31;
-  for (uint64_t base = begin + (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32 * 32; base < end;
-       base += uint64_t(gridDim.x) * blockDim.x) {
-    const uint64_t pos = base + lane;
-    int b = -1;
-    uint32_t u = 0;
-    if (pos < end) {
-      u = bins[pos];
-      if (vaff[u] && (!fa || fa[u])) {
+  const uint64_t warps = uint64_t(gridDim.x) * blockDim.x / 32;
+  for (uint64_t base = begin + (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32 * (32 * V); base < end;
+       base += warps * 32 * V) {
+    uint32_t u[V];
+    bool act[V];
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+      const uint64_t pos = base + k * 32 + lane;
+      u[k] = pos < end ? bins[pos] : 0;
+    }
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+      const uint64_t pos = base + k * 32 + lane;
+      act[k] = pos < end && vaff[u[k]];
+    }
+#pragma unroll
+    for (int k = 0; k < V; ++k)
+      if (act[k] && fa) act[k] = fa[u[k]];
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+      const uint64_t pos = base + k * 32 + lane;
+      int b = -1;
+      if (act[k]) {
         b = 1;
         while (pos >= bb.start[b + 1]) ++b;
       }
+      const unsigned grp = __match_any_sync(0xffffffffu, b);
+      const int leader = __ffs(grp) - 1;
+      uint32_t at = 0;
+      if (b >= 0 && lane == leader) at = atomicAdd(&wl_count[b], uint32_t(__popc(grp)));
+      at = __shfl_sync(0xffffffffu, at, leader);
+      if (b >= 0) wl[bb.start[b] + at + __popc(grp & ((1u << lane) - 1u))] = u[k];
     }
-    const unsigned grp = __match_any_sync(0xffffffffu, b);
-    const int leader = __ffs(grp) - 1;
-    uint32_t at = 0;
-    if (b >= 0 && lane == leader) at = atomicAdd(&wl_count[b], uint32_t(__popc(grp)));
-    at = __shfl_sync(0xffffffffu, at, leader);
-    if (b >= 0) wl[bb.start[b] + at + __popc(grp & ((1u << lane) - 1u))] = u;
   }
 }
 
@@ -525,6 +557,15 @@ void launch_clear_isolated(const uint32_t *list, size_t n, uint8_t *vaff, const 
   LVG_CHECK_LAUNCH();
 }
 
+void launch_clear_isolated_multi(const IsolatedLists &L, uint8_t *vaff, const uint8_t *fa, cudaStream_t s) {
+  size_t most = 0, total = 0;
+  for (int j = 0; j < L.k; ++j) { most = std::max(most, L.n[j]); total += L.n[j]; }
+  if (!total) return;
+  const unsigned grid = unsigned(std::min<size_t>(size_t(L.k) * ((most + 255) / 256), size_t(sms()) * 8 * L.k));
+  clear_isolated_multi_kernel<<<grid, 256, 0, s>>>(L, vaff, fa);
+  LVG_CHECK_LAUNCH();
+}
+
 void launch_merge_marks(uint8_t *vaff, uint8_t *mark, size_t n, cudaStream_t s) {
   if (!n) return;
   merge_marks_kernel<<<grid_for(n, 256), 256, 0, s>>>(vaff, mark, n);
@@ -575,7 +616,7 @@ void launch_compact_active(const uint32_t *bins, const BinBounds &bb, const uint
                            uint32_t *wl, uint32_t *wl_count, cudaStream_t s) {
   const uint64_t n = bb.start[NUM_BINS - 1] - bb.start[1];
   if (!n) return;
-  compact_active_kernel<<<grid_for(n, 256), 256, 0, s>>>(bins, bb, vaff, fa, wl, wl_count);
+  compact_active_kernel<<<grid_for((n + 3) / 4, 256), 256, 0, s>>>(bins, bb, vaff, fa, wl, wl_count);
   LVG_CHECK_LAUNCH();
 }
 

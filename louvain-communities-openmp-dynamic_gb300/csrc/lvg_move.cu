@@ -110,22 +110,23 @@ __device__ __forceinline__ bool warp_insert(uint32_t c, float w, Ins ins) {
 
 constexpr int TILE_BLOCK = 256;
 
+// The tiles of one block work through list[0..count): tile t of the block
+// takes items first + t, first + t + ntiles, ... (ntiles = tiles of all the
+// blocks sharing the list). Counters are flushed for degree bin `bin`.
 template <int T, int C, bool SYNC>
-__global__ void __launch_bounds__(TILE_BLOCK) move_tile_kernel(MoveArgs a) {
+__device__ __forceinline__ void tile_loop(const MoveArgs &a, const uint32_t *list, uint32_t count, uint32_t first,
+                                          uint32_t ntiles, uint8_t *smem, int bin) {
   constexpr int LOGC = ilog2c(C);
   constexpr int TPB = TILE_BLOCK / T;
-  extern __shared__ __align__(16) uint8_t smem[];
   const int tib = threadIdx.x / T;
   const int tl = threadIdx.x & (T - 1);
   uint32_t *keys = reinterpret_cast<uint32_t *>(smem) + tib * C;
   float *vals = reinterpret_cast<float *>(smem + size_t(TPB) * C * sizeof(uint32_t)) + tib * C;
   const unsigned m = tile_mask<T>();
-  const uint32_t ntiles = gridDim.x * TPB;
   unsigned long long fix = 0, nv = 0, ne = 0, nm = 0;
   bool bad = false;
-  const uint32_t count = a.count_ptr ? *a.count_ptr : a.count;
-  for (uint32_t i = blockIdx.x * TPB + tib; i < count; i += ntiles) {
-    const uint32_t u = a.list[i];
+  for (uint32_t i = first + tib; i < count; i += ntiles) {
+    const uint32_t u = list[i];
     int act = 0;
     if (tl == 0) act = a.vaff[u] && (!a.fa || a.fa[u]);
     act = __shfl_sync(m, act, 0, T);
@@ -142,15 +143,28 @@ __global__ void __launch_bounds__(TILE_BLOCK) move_tile_kernel(MoveArgs a) {
     // has at most C/(2T) edges).
     constexpr int U = (C / (2 * T)) < 1 ? 1 : ((C / (2 * T)) > 4 ? 4 : (C / (2 * T)));
     if (T == 32) {
-      // one warp per vertex: warp-uniform batches, hot keys combined per warp
+      // one warp per vertex: warp-uniform batches, hot keys combined per warp;
+      // the next batch's ids and weights load while this one's communities do
+      uint32_t nv[U];
+      float nw[U];
+#pragma unroll
+      for (int k = 0; k < U; ++k) {
+        const uint32_t j = k * 32 + tl;
+        nv[k] = j < dg ? a.key[o + j] : u;
+        nw[k] = j < dg ? a.w[o + j] : 0.f;
+      }
       for (uint32_t base = 0; base < dg; base += U * 32) {
         uint32_t v[U];
         float w[U];
 #pragma unroll
-        for (int k = 0; k < U; ++k) {
-          const uint32_t j = base + k * 32 + tl;
-          v[k] = j < dg ? a.key[o + j] : u;
-          w[k] = j < dg ? a.w[o + j] : 0.f;
+        for (int k = 0; k < U; ++k) { v[k] = nv[k]; w[k] = nw[k]; }
+        if (base + U * 32 < dg) {
+#pragma unroll
+          for (int k = 0; k < U; ++k) {
+            const uint32_t j = base + U * 32 + k * 32 + tl;
+            nv[k] = j < dg ? a.key[o + j] : u;
+            nw[k] = j < dg ? a.w[o + j] : 0.f;
+          }
         }
         uint32_t c[U];
 #pragma unroll
@@ -233,7 +247,50 @@ __global__ void __launch_bounds__(TILE_BLOCK) move_tile_kernel(MoveArgs a) {
     bad |= !ok;
     __syncwarp(m);
   }
-  flush_counters(a.ctr, a.bin, fix, nv, ne, nm, bad);
+  flush_counters(a.ctr, bin, fix, nv, ne, nm, bad);
+}
+
+template <int T, int C, bool SYNC>
+__global__ void __launch_bounds__(TILE_BLOCK) move_tile_kernel(MoveArgs a) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  constexpr int TPB = TILE_BLOCK / T;
+  const uint32_t count = a.count_ptr ? *a.count_ptr : a.count;
+  tile_loop<T, C, SYNC>(a, a.list, count, blockIdx.x * TPB, gridDim.x * TPB, smem, a.bin);
+}
+
+// Several degree bins of one colour class in one launch (bins lo..hi of
+// 1..8): the blocks [sb.block_begin[b-lo], sb.block_begin[b-lo+1]) serve bin
+// b with its own tile size and table, as move_tile_kernel would. Used when the
+// classes' worklists are short (dynamic-frontier and delta-screening passes
+// over the uploaded graph), where a launch per bin would cost more than its
+// work.
+template <int LO, int HI, bool SYNC>
+__global__ void __launch_bounds__(TILE_BLOCK) move_small_kernel(MoveArgs a, SmallBins sb) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  int k = 0;
+  while (k < HI - LO && blockIdx.x >= sb.block_begin[k + 1]) ++k;
+  // constant indices into sb (a dynamic index would copy it to local memory)
+  switch (LO + k) {
+#define LVG_SMALL_CASE(B, T, C)                                                                          \
+  case B:                                                                                                \
+    if (B >= LO && B <= HI) {                                                                            \
+      constexpr int J = (B >= LO && B <= HI) ? B - LO : 0;                                              \
+      const uint32_t b0 = sb.block_begin[J], nb = sb.block_begin[J + 1] - b0;                           \
+      tile_loop<T, C, SYNC>(a, sb.list[J], *sb.count_ptr[J], (blockIdx.x - b0) * (TILE_BLOCK / T),      \
+                            nb * (TILE_BLOCK / T), smem, B);                                             \
+    }                                                                                                    \
+    break;
+    LVG_SMALL_CASE(1, 4, 8)
+    LVG_SMALL_CASE(2, 8, 16)
+    LVG_SMALL_CASE(3, 16, 32)
+    LVG_SMALL_CASE(4, 32, 64)
+    LVG_SMALL_CASE(5, 32, 128)
+    LVG_SMALL_CASE(6, 32, 256)
+    LVG_SMALL_CASE(7, 32, 512)
+    LVG_SMALL_CASE(8, 32, 1024)
+#undef LVG_SMALL_CASE
+    default: break;
+  }
 }
 
 // ------------------------------------------------------------ block kernel
@@ -344,14 +401,31 @@ __device__ __forceinline__ float scan_edges(const MoveArgs &a, uint32_t u, uint6
   constexpr int U = 4;
   const uint32_t lane = threadIdx.x & 31u;
   float kd = 0.f;
-  for (uint32_t base = threadIdx.x & ~31u; base < n; base += U * B) {
+  // the next batch's ids and weights are loaded while this batch's
+  // communities are gathered (two loads in flight instead of one after the
+  // other)
+  uint32_t nv[U];
+  float nw[U];
+  const uint32_t base0 = threadIdx.x & ~31u;
+#pragma unroll
+  for (int k = 0; k < U; ++k) {
+    const uint32_t j = base0 + k * B + lane;
+    nv[k] = j < n ? a.key[o + j] : u;
+    nw[k] = j < n ? a.w[o + j] : 0.f;
+  }
+  for (uint32_t base = base0; base < n; base += U * B) {
     uint32_t v[U];
     float w[U];
 #pragma unroll
-    for (int k = 0; k < U; ++k) {
-      const uint32_t j = base + k * B + lane;
-      v[k] = j < n ? a.key[o + j] : u;
-      w[k] = j < n ? a.w[o + j] : 0.f;
+    for (int k = 0; k < U; ++k) { v[k] = nv[k]; w[k] = nw[k]; }
+    const uint32_t next = base + U * B;
+    if (next < n) {
+#pragma unroll
+      for (int k = 0; k < U; ++k) {
+        const uint32_t j = next + k * B + lane;
+        nv[k] = j < n ? a.key[o + j] : u;
+        nw[k] = j < n ? a.w[o + j] : 0.f;
+      }
     }
     uint32_t c[U];
 #pragma unroll
@@ -723,6 +797,20 @@ void set_smem(K kernel, size_t bytes) {
   if (bytes > 48 * 1024) LVG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)));
 }
 
+template <int LO, int HI, bool SYNC>
+void launch_small(const MoveArgs &a, SmallBins sb, cudaStream_t s) {
+  // shared memory of the largest table among the bins (tiles x C x 8 bytes)
+  constexpr size_t CMAX = size_t(TILE_BLOCK / (HI <= 1 ? 4 : HI == 2 ? 8 : HI == 3 ? 16 : 32)) *
+                          (size_t(4) << HI) * 8;
+  auto k = move_small_kernel<LO, HI, SYNC>;
+  static bool configured = false;
+  if (!configured) { set_smem(k, CMAX); configured = true; }
+  const unsigned grid = sb.block_begin[HI - LO + 1];
+  if (!grid) return;
+  k<<<grid, TILE_BLOCK, CMAX, s>>>(a, sb);
+  LVG_CHECK_LAUNCH();
+}
+
 template <int T, int C, bool SYNC>
 void launch_tile(const MoveArgs &a, cudaStream_t s) {
   constexpr int TPB = TILE_BLOCK / T;
@@ -824,6 +912,18 @@ int global_table_blocks(size_t count) {
 void launch_move_hubs(bool sync, const MoveArgs &a, cudaStream_t s) {
   if (sync) launch_hubs<true>(a, s);
   else launch_hubs<false>(a, s);
+}
+
+int device_sms() { return num_sms(); }
+
+void launch_move_small(int lo, int hi, bool sync, const MoveArgs &a, const SmallBins &sb, cudaStream_t s) {
+  if (lo == 1 && hi == 6) {
+    if (sync) launch_small<1, 6, true>(a, sb, s); else launch_small<1, 6, false>(a, sb, s);
+  } else if (lo == 7 && hi == 8) {
+    if (sync) launch_small<7, 8, true>(a, sb, s); else launch_small<7, 8, false>(a, sb, s);
+  } else {
+    throw Error(LVG_EINVAL, "launch_move_small: unsupported bin range");
+  }
 }
 
 void launch_move_bin(int b, bool sync, const MoveArgs &a, cudaStream_t s) {

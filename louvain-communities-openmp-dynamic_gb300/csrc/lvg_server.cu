@@ -8,13 +8,19 @@
 // configured dynamic method from the graph's current state, which the result
 // replaces. Requests for one graph run in arrival order, one at a time;
 // requests for different graphs run concurrently on the graphs' own streams
-// (one host worker thread per request in flight). Admission control keeps
+// (one host worker thread per request in flight). With `coalesce` set, a
+// worker that picks a graph takes every request queued for it (up to
+// `coalesce` batch entries) and serves them as one batch — their union, tidied
+// and applied at once — so that fixed per-request costs are paid once under
+// load; every one of them then completes with that run's result. Admission
+// control keeps
 // the device bytes of the resident graphs under a budget: a graph is admitted
 // on its measured bytes after its first run (graph, workspace, state) plus
 // the per-request scratch, and only while the device has that much free.
 //
 // Host code only: it calls the library's own C-ABI.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -89,6 +95,24 @@ int pick(lvg_server *sv) {
   return -1;
 }
 
+// The union of several requests' batches (deletions, then insertions, in
+// arrival order).
+Request merge(std::vector<Request> &rs) {
+  if (rs.size() == 1) return std::move(rs[0]);
+  Request m;
+  m.graph = rs[0].graph;
+  m.t_submit = rs[0].t_submit;
+  for (auto &r : rs) {
+    m.ds.insert(m.ds.end(), r.ds.begin(), r.ds.end());
+    m.dd.insert(m.dd.end(), r.dd.begin(), r.dd.end());
+    m.dw.insert(m.dw.end(), r.dw.begin(), r.dw.end());
+    m.is.insert(m.is.end(), r.is.begin(), r.is.end());
+    m.id.insert(m.id.end(), r.id.begin(), r.id.end());
+    m.iw.insert(m.iw.end(), r.iw.begin(), r.iw.end());
+  }
+  return m;
+}
+
 void serve(lvg_server *sv, Slot &s, const Request &r, lvg_request_info &info) {
   const double t0 = now_ms();
   info.queue_ms = t0 - r.t_submit;
@@ -122,33 +146,47 @@ void worker(lvg_server *sv) {
     sv->cv_work.wait(lk, [&] { return sv->stop || (i = pick(sv)) >= 0; });
     if (i < 0) return;  // stopping and nothing runnable
     Slot &s = *sv->slots[size_t(i)];
-    Request r = std::move(s.q.front());
-    s.q.pop_front();
+    std::vector<Request> rs;
+    size_t entries = 0;
+    do {  // one request, or (coalescing) every queued one up to the entry cap
+      entries += s.q.front().ds.size() + s.q.front().is.size();
+      rs.push_back(std::move(s.q.front()));
+      s.q.pop_front();
+    } while (sv->opt.coalesce && !s.q.empty() &&
+             entries + s.q.front().ds.size() + s.q.front().is.size() <= sv->opt.coalesce);
     s.busy = true;
     lk.unlock();
+    std::vector<uint64_t> tickets;
+    std::vector<double> submitted;
+    for (auto &r : rs) { tickets.push_back(r.ticket); submitted.push_back(r.t_submit); }
+    const Request r = merge(rs);
     lvg_request_info info{};
-    info.ticket = r.ticket;
     info.graph = r.graph;
     serve(sv, s, r, info);
     const double t = now_ms();
-    info.latency_ms = t - r.t_submit;
     lk.lock();
     s.busy = false;
     ++s.served;
-    --sv->pending;
-    if (info.status == LVG_OK) {
-      ++sv->completed;
-      sv->updates += r.ds.size() + r.is.size();
-      sv->lat.push_back(info.latency_ms);
-      sv->sum_queue += info.queue_ms;
-      sv->sum_apply += info.apply_ms;
-      sv->sum_run += info.run_ms;
-    } else {
-      ++sv->failed;
+    for (size_t k = 0; k < tickets.size(); ++k) {
+      lvg_request_info ik = info;
+      ik.ticket = tickets[k];
+      ik.latency_ms = t - submitted[k];
+      ik.queue_ms = info.queue_ms + (submitted[0] - submitted[k]);
+      --sv->pending;
+      if (ik.status == LVG_OK) {
+        ++sv->completed;
+        sv->lat.push_back(ik.latency_ms);
+        sv->sum_queue += ik.queue_ms;
+        sv->sum_apply += ik.apply_ms;
+        sv->sum_run += ik.run_ms;
+      } else {
+        ++sv->failed;
+      }
+      if (sv->t_first == 0 || submitted[k] < sv->t_first) sv->t_first = submitted[k];
+      sv->done[tickets[k]] = ik;
     }
-    if (sv->t_first == 0 || r.t_submit < sv->t_first) sv->t_first = r.t_submit;
+    if (info.status == LVG_OK) sv->updates += entries;
     sv->t_last = std::max(sv->t_last, t);
-    sv->done[r.ticket] = info;
     sv->cv_done.notify_all();
     sv->cv_work.notify_all();
   }
@@ -323,6 +361,30 @@ lvg_graph *lvg_server_graph(lvg_server *sv, int graph_id) {
   std::lock_guard<std::mutex> lk(sv->mu);
   if (graph_id < 0 || size_t(graph_id) >= sv->slots.size()) return nullptr;
   return sv->slots[size_t(graph_id)]->g;
+}
+
+int lvg_static_many(lvg_graph *const *graphs, size_t n, const lvg_options *o, int workers, int trim,
+                    lvg_result *results) {
+  if ((n && (!graphs || !results)) || workers < 1 || workers > 256)
+    return lvg::fail_noalloc(LVG_EINVAL, "lvg_static_many: bad argument");
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return lvg::fail_noalloc(LVG_ECUDA, "no CUDA device");
+  std::atomic<size_t> next{0};
+  std::atomic<int> first_err{LVG_OK};
+  auto work = [&] {
+    cudaSetDevice(dev);
+    for (size_t i; (i = next.fetch_add(1)) < n;) {
+      int rc = lvg_static(graphs[i], o, &results[i]);
+      if (rc == LVG_OK && trim) rc = lvg_graph_trim(graphs[i], trim);
+      int ok = LVG_OK;
+      if (rc != LVG_OK) first_err.compare_exchange_strong(ok, rc);
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < std::min<int>(workers, int(n)); ++t) pool.emplace_back(work);
+  work();
+  for (auto &t : pool) t.join();
+  return first_err.load();
 }
 
 int lvg_server_destroy(lvg_server *sv) {

@@ -80,7 +80,8 @@ class _BatchBuf(C.Structure):
 
 
 class _ServerOptions(C.Structure):
-    _fields_ = [("workers", C.c_int), ("hbm_budget", C.c_size_t), ("method", C.c_int), ("louvain", _Options)]
+    _fields_ = [("workers", C.c_int), ("hbm_budget", C.c_size_t), ("method", C.c_int), ("louvain", _Options),
+                ("coalesce", C.c_size_t)]
 
 
 class _RequestInfo(C.Structure):
@@ -103,7 +104,8 @@ class _Stats(C.Structure):
                 ("move_edges", C.c_uint64), ("moves", C.c_uint64), ("aggregate_kernel_ms", C.c_double),
                 ("aggregate_edges", C.c_uint64), ("aggregate_launches", C.c_uint64),
                 ("kernel_launches", C.c_uint64), ("move_bin_ms", C.c_double * 12),
-                ("move_bin_vertices", C.c_uint64 * 12), ("move_bin_edges", C.c_uint64 * 12)]
+                ("move_bin_vertices", C.c_uint64 * 12), ("move_bin_edges", C.c_uint64 * 12),
+                ("call_upload_ms", C.c_double), ("call_run_ms", C.c_double), ("call_download_ms", C.c_double)]
 
 
 class _Csr(C.Structure):
@@ -209,6 +211,7 @@ def load_library() -> C.CDLL:
     L.lvg_server_stats.argtypes = [vp, i32, C.POINTER(_ServerStats)]
     L.lvg_server_membership.argtypes = [vp, i32, vp, vp, vp]
     L.lvg_server_destroy.argtypes = [vp]
+    L.lvg_static_many.argtypes = [C.POINTER(vp), sz, C.POINTER(_Options), i32, i32, C.POINTER(_Result)]
     _lib = L
     return L
 
@@ -912,11 +915,11 @@ class Server:
     """A serving loop over graphs resident in HBM (``lvg_server``)."""
 
     def __init__(self, workers: int = 8, hbm_budget: int = 120 << 30, method: int = 3,
-                 o: "LouvainOptions | None" = None):
+                 o: "LouvainOptions | None" = None, coalesce: int = 0):
         self._L = load_library()
         opt = _ServerOptions()
         self._L.lvg_server_options_default(C.byref(opt))
-        opt.workers, opt.hbm_budget, opt.method = workers, hbm_budget, method
+        opt.workers, opt.hbm_budget, opt.method, opt.coalesce = workers, hbm_budget, method, coalesce
         if o is not None:
             opt.louvain = o._struct()
         self.h = C.c_void_p()
@@ -978,3 +981,23 @@ class Server:
 
 def graph_footprint(span: int, edges: int) -> int:
     return int(load_library().lvg_graph_footprint(span, edges))
+
+
+def louvain_static_many(graphs: "list[Graph]", o: "LouvainOptions | None" = None, workers: int = 16,
+                        trim: int = 0) -> list[dict]:
+    """Static Louvain on many graphs concurrently (lvg_static_many); per graph
+    the scalar result fields and the membership."""
+    L = load_library()
+    n = len(graphs)
+    hs = (C.c_void_p * max(n, 1))(*[g.h for g in graphs])
+    res = (_Result * max(n, 1))()
+    opt = (o or LouvainOptions())._struct()
+    _check(L.lvg_static_many(hs, n, C.byref(opt), workers, trim, res))
+    out = []
+    for i, g in enumerate(graphs):
+        r = res[i]
+        d = _scalars(r)
+        d["membership"] = np.ctypeslib.as_array(r.membership, (r.span,)).copy()
+        L.lvg_result_free(C.byref(r))
+        out.append(d)
+    return out

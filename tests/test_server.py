@@ -91,3 +91,38 @@ def test_server_admission_control(cuda):
     assert e.value.code == cuda.LVG_ENOMEM
     assert sv.stats()["graphs"] == 1
     sv.close()
+
+
+@pytest.mark.gpu
+def test_server_coalescing_serves_the_union(cuda, orc):
+    """With coalescing, queued requests of one graph run as one batch: every
+    ticket completes, and the graph ends as after the batches one by one."""
+    x = cuda.planted_partition(4000, 100, 12, 0.8, 9)
+    seq = [cuda.reference_batch(x, 0, 300, seed=50 + k) for k in range(12)]  # insertion-only
+    cur = x
+    for b in seq:
+        cur = cuda.HostGraph(*orc.apply_batch(cur, b)[0])
+    G = cuda.Graph(x)
+    sv = cuda.Server(workers=2, coalesce=1 << 20)
+    gid = sv.add_graph(G)
+    tickets = [sv.submit(gid, b) for b in seq]
+    infos = [sv.wait(t) for t in tickets]
+    assert all(i["status"] == 0 for i in infos)
+    st = sv.stats()
+    assert st["completed"] == len(seq)
+    sv.drain()
+    h = G.download()
+    assert np.array_equal(h.offsets, cur.offsets) and np.array_equal(h.keys, cur.keys)
+    sv.close()
+
+
+@pytest.mark.gpu
+def test_static_many_equals_one_by_one(cuda):
+    o = cuda.LouvainOptions(deterministic=True)
+    xs = _graphs(cuda)
+    Gs = [cuda.Graph(x) for x in xs]
+    many = cuda.louvain_static_many(Gs, o, workers=3, trim=2)
+    for G, r in zip(Gs, many):
+        one = cuda.louvain_static(G, o)
+        assert np.array_equal(r["membership"], one.membership)
+        assert (r["iterations"], r["passes"]) == (one.iterations, one.passes)
