@@ -6,7 +6,8 @@ Workload (the headline configuration): R-MAT scale 24, edge factor 16,
 directed edges), FP32 unit weights, uint32 ids, vertex 0 absent. A step is one
 dynamic-frontier Louvain run over one batch of 1e-4 |E| random updates (80 %
 insertions of absent uniform pairs, 20 % deletions of uniformly sampled edges)
-on the updated graph, from the static Louvain result of the base graph.
+on the updated graph, from the static Louvain result of the base graph
+(deterministic mode, so the prior and the step's work are the same every run).
 
 Arms:
   default              the GPU library. `value` = |E| / per-step device time
@@ -266,9 +267,12 @@ def run_gpu(args):
     x, b, y, nupd, tgen = make_inputs(lvg, args)
     S, E = y.span, y.num_edges
 
-    # prior: static Louvain on the base graph (untimed, as main.cxx:89)
+    # prior: static Louvain on the base graph (untimed, as main.cxx:89), in
+    # deterministic mode so that every run's DF step starts from the same
+    # prior (an asynchronous static result varies run to run, and with it the
+    # work a DF step does); the timed DF steps run in the default mode
     X = lvg.Graph(x)
-    prior = lvg.louvain_static(X)
+    prior = lvg.louvain_static(X, lvg.LouvainOptions(deterministic=True))
     q_static_base = X.modularity(prior.membership)
     # the batch update itself, in HBM (tidy + apply, lvg_graph_apply_device_batch):
     # the batch and its inverse applied alternately, each a real update of X

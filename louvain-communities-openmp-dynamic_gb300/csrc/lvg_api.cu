@@ -175,8 +175,17 @@ struct lvg_graph {
   IterKey iter_key{};
   unsigned long long iter_nodes = 0, iter_moves = 0;
   bool no_graphs = false;
+  // side streams for the degree-bin kernels of one colour class, which run
+  // concurrently (fork/join with events)
+  cudaStream_t aux[4] = {};
+  cudaEvent_t fork_ev = nullptr, join_ev[4] = {};
   ~lvg_graph() {
     if (iter_exec) cudaGraphExecDestroy(iter_exec);
+    for (auto &a : aux)
+      if (a) cudaStreamDestroy(a);
+    if (fork_ev) cudaEventDestroy(fork_ev);
+    for (auto &e : join_ev)
+      if (e) cudaEventDestroy(e);
   }
   bool profiling = false;
   lvg_stats stats = {};
@@ -330,12 +339,31 @@ void ensure_global_tables(Workspace &W, size_t blocks, int log2cap, bool first_t
 // chunked hubs); in deterministic mode the class's decisions are applied and
 // its marks merged before the next class. The device gain sum is reset first.
 // With bin_ev, events bracket each bin launch (profiling).
+void ensure_aux(lvg_graph *g) {
+  if (g->aux[0]) return;
+  for (auto &a : g->aux) LVG_CUDA(cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking));
+  LVG_CUDA(cudaEventCreateWithFlags(&g->fork_ev, cudaEventDisableTiming));
+  for (auto &e : g->join_ev) LVG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+}
+
+// The stream of degree bin b within a colour class: the small bins on two
+// side streams, bins 9 and 10 on two more, the hubs on the main stream.
+int bin_stream(int b) { return b <= 4 ? 0 : b <= 8 ? 1 : b == 9 ? 2 : b == 10 ? 3 : -1; }
+
 void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const float *tot,
-                       const uint8_t *fa, float kr, bool sync, bool fused, const int *glog2, size_t need,
-                       std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> *bin_ev) {
+                       const uint8_t *fa, float kr, bool sync, bool fused, const int *glog2, const size_t *goff,
+                       size_t need, std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> *bin_ev) {
   Workspace &W = *g->ws;
   cudaStream_t s = g->stream;
   const int K = lv.colors;
+  // The bins of one class are independent (different vertices; the class's
+  // reads of other vertices' communities race in asynchronous mode exactly as
+  // the reference's threads do, and in deterministic mode nothing they read
+  // changes before the class's moves are applied), so they run concurrently.
+  // Per-bin profiling keeps them on one stream to time each launch.
+  const bool conc = bin_ev == nullptr;
+  if (conc) ensure_aux(g);
+  auto stream_of = [&](int b) { const int i = bin_stream(b); return conc && i >= 0 ? g->aux[i] : s; };
   LVG_CUDA(cudaMemsetAsync(&g->ctr.p->el_fix, 0, sizeof(unsigned long long), s));
   LVG_CUDA(cudaMemsetAsync(W.wl_count.p, 0, size_t(K) * NUM_BINS * sizeof(uint32_t), s));
   for (int k = 0; k < K; ++k) {
@@ -344,6 +372,10 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot
     for (int b = 0; b <= NUM_BINS; ++b) bb.start[b] = lv.bin_start[k * NUM_BINS + b];
     uint32_t *wlc = W.wl_count.p + size_t(k) * NUM_BINS;
     if (bb.start[NUM_BINS - 1] > bb.start[1]) launch_compact_active(lv.bins, bb, W.vaff.p, fa, W.wl.p, wlc, s);
+    if (conc) {  // fork
+      LVG_CUDA(cudaEventRecord(g->fork_ev, s));
+      for (auto a : g->aux) LVG_CUDA(cudaStreamWaitEvent(a, g->fork_ev, 0));
+    }
     if (fused) {
       // bins 1-6 and 7-8 in one launch each; each bin gets blocks for its
       // bucket, at most two per SM (its worklist is short)
@@ -368,7 +400,7 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot
         a.vaff = W.vaff.p; a.mark = W.mark.p; a.fa = fa; a.vtot = tot;
         a.kr = kr; a.ctr = g->ctr.p; a.bin = grp.first;
         cudaEvent_t b0 = bin_ev ? g->events.record(s) : nullptr;
-        launch_move_small(grp.first, grp.second, sync, a, sb, s);
+        launch_move_small(grp.first, grp.second, sync, a, sb, stream_of(grp.first));
         if (bin_ev) bin_ev->push_back({grp.first, {b0, g->events.record(s)}});
         ++g->stats.move_launches;
       }
@@ -384,7 +416,9 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot
       a.vcom = com; a.ctot = ctot; a.dec = W.dec.p;
       a.vaff = W.vaff.p; a.mark = W.mark.p; a.fa = fa; a.vtot = tot;
       a.kr = kr; a.ctr = g->ctr.p; a.bin = b;
-      a.gkeys = need ? W.gkeys.p : nullptr; a.gvals = need ? W.gvals.p : nullptr; a.glog2 = glog2[b];
+      a.gkeys = need ? W.gkeys.p + goff[b] : nullptr;
+      a.gvals = need ? W.gvals.p + goff[b] : nullptr;
+      a.glog2 = glog2[b];
       cudaEvent_t b0 = bin_ev ? g->events.record(s) : nullptr;
       if (b == NUM_BINS - 1) {
         a.hub = lv.hub;
@@ -395,10 +429,16 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot
         a.hub_kd = W.hub_kd.p;
         launch_move_hubs(sync, a, s);
       } else {
-        launch_move_bin(b, sync, a, s);
+        launch_move_bin(b, sync, a, stream_of(b));
       }
       if (bin_ev) bin_ev->push_back({b, {b0, g->events.record(s)}});
       ++g->stats.move_launches;
+    }
+    if (conc) {  // join
+      for (int i = 0; i < 4; ++i) {
+        LVG_CUDA(cudaEventRecord(g->join_ev[i], g->aux[i]));
+        LVG_CUDA(cudaStreamWaitEvent(s, g->join_ev[i], 0));
+      }
     }
     if (sync) {
       launch_apply_moves(lv.bins + lv.color_begin(k), lv.color_end(k) - lv.color_begin(k), W.dec.p, com, ctot, tot, s);
@@ -412,8 +452,8 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot
 // eager iteration, so every kernel's attributes are already set). A capture
 // failure disables graphs for this handle; the eager path stays correct.
 void capture_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const float *tot,
-                       const uint8_t *fa, float kr, bool sync, bool fused, const int *glog2, size_t need,
-                       const IterKey &key) {
+                       const uint8_t *fa, float kr, bool sync, bool fused, const int *glog2, const size_t *goff,
+                       size_t need, const IterKey &key) {
   cudaStream_t s = g->stream;
   if (g->iter_exec) {
     cudaGraphExecDestroy(g->iter_exec);
@@ -429,7 +469,7 @@ void capture_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot
   }
   bool fine = true;
   try {
-    enqueue_iteration(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, need, nullptr);
+    enqueue_iteration(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, goff, need, nullptr);
   } catch (const Error &) {
     fine = false;
   }
@@ -470,13 +510,15 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const 
   // Global fallback regions of the large-degree bins (9-11): each launch's
   // blocks get 2^glog2[b] slots, enough for the bin's largest degree.
   int glog2[NUM_BINS] = {};
+  size_t goff[NUM_BINS] = {};
   size_t need = 0;
   for (int b = 9; b < NUM_BINS; ++b) {
     size_t most = 0;
     for (int k = 0; k < K; ++k) most = std::max(most, lv.bucket_size(k, b));
     if (!most) continue;
     glog2[b] = global_table_log2(lv.bin_maxdeg[b]);
-    need = std::max(need, size_t(move_grid_blocks(b, sync, most)) << glog2[b]);
+    goff[b] = need;  // each bin its own regions: the bins' kernels run concurrently
+    need += size_t(move_grid_blocks(b, sync, most)) << glog2[b];
   }
   if (need) {
     W.gkeys.ensure(need);
@@ -512,7 +554,7 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const 
     } else {
       bin_ev.clear();
       if (g->profiling) e0 = g->events.record(s);
-      enqueue_iteration(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, need,
+      enqueue_iteration(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, goff, need,
                         g->profiling ? &bin_ev : nullptr);
       if (g->profiling) e1 = g->events.record(s);
     }
@@ -522,7 +564,8 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const 
       g->stats.move_kernel_ms += elapsed(e0, e1);
       for (auto &be : bin_ev) g->stats.move_bin_ms[be.first] += elapsed(be.second.first, be.second.second);
     }
-    if (graphs && !replay) capture_iteration(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, need, key);
+    if (graphs && !replay)
+      capture_iteration(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, goff, need, key);
     el = double(g->hctr.p->el_fix) / GAIN_FIX / M;
     ++l;
     if (el <= E) break;

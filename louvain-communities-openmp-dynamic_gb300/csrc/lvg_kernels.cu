@@ -367,47 +367,29 @@ __global__ void level_init_kernel(size_t n, const float *vtot, uint32_t *vcom, f
 }
 
 // Active vertices of one colour class into per-bin worklists (warp-aggregated
-// appends; the order within a worklist is unspecified). Each warp takes 128
-// consecutive entries, four per lane, so that four flag reads are in flight
-// per lane.
+// appends; the order within a worklist is unspecified).
 __global__ void compact_active_kernel(const uint32_t *bins, BinBounds bb, const uint8_t *vaff, const uint8_t *fa,
                                       uint32_t *wl, uint32_t *wl_count) {
-  constexpr int V = 4;
   const uint64_t begin = bb.start[1], end = bb.start[NUM_BINS - 1];
   const int lane = threadIdx.x & 31;
-  const uint64_t warps = uint64_t(gridDim.x) * blockDim.x / 32;
-  for (uint64_t base = begin + (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32 * (32 * V); base < end;
-       base += warps * 32 * V) {
-    uint32_t u[V];
-    bool act[V];
-#pragma unroll
-    for (int k = 0; k < V; ++k) {
-      const uint64_t pos = base + k * 32 + lane;
-      u[k] = pos < end ? bins[pos] : 0;
-    }
-#pragma unroll
-    for (int k = 0; k < V; ++k) {
-      const uint64_t pos = base + k * 32 + lane;
-      act[k] = pos < end && vaff[u[k]];
-    }
-#pragma unroll
-    for (int k = 0; k < V; ++k)
-      if (act[k] && fa) act[k] = fa[u[k]];
-#pragma unroll
-    for (int k = 0; k < V; ++k) {
-      const uint64_t pos = base + k * 32 + lane;
-      int b = -1;
-      if (act[k]) {
+  for (uint64_t base = begin + (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32 * 32; base < end;
+       base += uint64_t(gridDim.x) * blockDim.x) {
+    const uint64_t pos = base + lane;
+    int b = -1;
+    uint32_t u = 0;
+    if (pos < end) {
+      u = bins[pos];
+      if (vaff[u] && (!fa || fa[u])) {
         b = 1;
         while (pos >= bb.start[b + 1]) ++b;
       }
-      const unsigned grp = __match_any_sync(0xffffffffu, b);
-      const int leader = __ffs(grp) - 1;
-      uint32_t at = 0;
-      if (b >= 0 && lane == leader) at = atomicAdd(&wl_count[b], uint32_t(__popc(grp)));
-      at = __shfl_sync(0xffffffffu, at, leader);
-      if (b >= 0) wl[bb.start[b] + at + __popc(grp & ((1u << lane) - 1u))] = u[k];
     }
+    const unsigned grp = __match_any_sync(0xffffffffu, b);
+    const int leader = __ffs(grp) - 1;
+    uint32_t at = 0;
+    if (b >= 0 && lane == leader) at = atomicAdd(&wl_count[b], uint32_t(__popc(grp)));
+    at = __shfl_sync(0xffffffffu, at, leader);
+    if (b >= 0) wl[bb.start[b] + at + __popc(grp & ((1u << lane) - 1u))] = u;
   }
 }
 
@@ -616,7 +598,7 @@ void launch_compact_active(const uint32_t *bins, const BinBounds &bb, const uint
                            uint32_t *wl, uint32_t *wl_count, cudaStream_t s) {
   const uint64_t n = bb.start[NUM_BINS - 1] - bb.start[1];
   if (!n) return;
-  compact_active_kernel<<<grid_for((n + 3) / 4, 256), 256, 0, s>>>(bins, bb, vaff, fa, wl, wl_count);
+  compact_active_kernel<<<grid_for(n, 256), 256, 0, s>>>(bins, bb, vaff, fa, wl, wl_count);
   LVG_CHECK_LAUNCH();
 }
 

@@ -656,7 +656,6 @@ __global__ void __launch_bounds__(B) hub_merge_kernel(MoveArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
   __shared__ float red_g[B / 32];
   __shared__ uint32_t red_c[B / 32];
-  __shared__ int s_act;
   __shared__ unsigned s_used;
   __shared__ int s_over;
   __shared__ float s_kd;
@@ -677,15 +676,20 @@ __global__ void __launch_bounds__(B) hub_merge_kernel(MoveArgs a) {
     const uint32_t u = a.hub.hub_vertex[g];
     const uint32_t c0 = a.hub.hub_first[g], c1 = a.hub.hub_first[g + 1];
     if (threadIdx.x == 0) {
-      // active iff step 1 aggregated it (a hub marked since then waits for
-      // the next iteration, its partials being stale)
-      s_act = a.chunk_cnt[c0] != EMPTY;
       s_used = 0;
       s_over = 0;
       s_kd = a.hub_kd[u];
     }
-    __syncthreads();
-    if (!s_act) {
+    // Merged only if every chunk aggregated it. The chunks read the hub's
+    // flag when they start, and a hub can be marked meanwhile (by a move of
+    // its own class, in a kernel running beside the chunks): then some
+    // chunks skipped it (count EMPTY) and its partials are incomplete, so it
+    // waits for the next iteration and its partial own-community sum is
+    // dropped.
+    bool stale = false;
+    for (uint32_t c = c0 + threadIdx.x; c < c1; c += B) stale |= a.chunk_cnt[c] == EMPTY;
+    if (__syncthreads_or(stale)) {
+      if (threadIdx.x == 0) a.hub_kd[u] = 0.f;
       __syncthreads();
       continue;
     }
@@ -693,17 +697,21 @@ __global__ void __launch_bounds__(B) hub_merge_kernel(MoveArgs a) {
     const uint32_t d = a.vcom[u];
     int lg = min(LOGS, max(1, ceil_log2(2ull * dg)));
     const unsigned limit = (1u << lg) >> 1;
-    for (uint32_t c = c0; c < c1; ++c) {
-      const uint64_t p = a.hub.chunk_part[c];
-      const uint32_t cnt = a.chunk_cnt[c];
+    // a warp per chunk: the chunks' partial lists merge in parallel (a hub of
+    // a million edges has ~60 chunks)
+    {
+      const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
       bool stop = false;
-      for (uint32_t q = threadIdx.x; q < cnt; q += B)
-        if (!lt_add(t, lg, a.part_key[p + q], a.part_val[p + q], limit)) {
-          s_over = 1;
-          stop = true;
-          break;
-        }
-      if (stop) break;
+      for (uint32_t c = c0 + warp; c < c1 && !stop; c += B / 32) {
+        const uint64_t p = a.hub.chunk_part[c];
+        const uint32_t cnt = a.chunk_cnt[c];
+        for (uint32_t q = lane; q < cnt; q += 32)
+          if (!lt_add(t, lg, a.part_key[p + q], a.part_val[p + q], limit)) {
+            s_over = 1;
+            stop = true;
+            break;
+          }
+      }
     }
     __syncthreads();
     const unsigned nlist = min(s_used, limit);
@@ -718,10 +726,11 @@ __global__ void __launch_bounds__(B) hub_merge_kernel(MoveArgs a) {
       for (uint32_t s2 = threadIdx.x; s2 < gcap; s2 += B) { gkeys[s2] = EMPTY; gvals[s2] = 0.f; }
       __syncthreads();
       if (gkeys)
-        for (uint32_t c = c0; c < c1; ++c) {
+        for (uint32_t c = c0 + (threadIdx.x >> 5); c < c1; c += B / 32) {
           const uint64_t p = a.hub.chunk_part[c];
           const uint32_t cnt = a.chunk_cnt[c];
-          for (uint32_t q = threadIdx.x; q < cnt; q += B) ok &= table_add(gkeys, gvals, lg, a.part_key[p + q], a.part_val[p + q]);
+          for (uint32_t q = threadIdx.x & 31u; q < cnt; q += 32)
+            ok &= table_add(gkeys, gvals, lg, a.part_key[p + q], a.part_val[p + q]);
         }
       __syncthreads();
     }
