@@ -342,6 +342,22 @@ lvg_graph *lvg_server_graph(lvg_server *sv, int graph_id);
  * still run). */
 int lvg_static_many(lvg_graph *const *graphs, size_t n, const lvg_options *o, int workers, int trim,
                     lvg_result *results);
+/* Graph unions (no reference counterpart; the batched form of
+ * louvainStaticOmp, inc/louvain.hxx:1180-1215, over many graphs): the graphs'
+ * CSRs copied back to back into one graph in HBM, graph i owning vertices
+ * [vb[i], vb[i+1]) with its ids shifted by vb[i] (the sources are unchanged
+ * and may be destroyed afterwards). */
+int lvg_graph_create_union(lvg_graph *const *graphs, size_t n, lvg_graph **out);
+/* Graphs in a union (0 for a plain graph). */
+int lvg_union_graphs(const lvg_graph *u, size_t *n);
+/* Static Louvain on every graph of a union in one run: each level's local
+ * moving is one set of launches over all graphs still moving, and each graph
+ * keeps its own M, colour classes (by its own ids), iteration and pass tests,
+ * so results[i] equals lvg_static on graph i alone — bit for bit in
+ * deterministic mode with integer weights (membership, weights, iterations,
+ * passes, affectedVertices); the time fields are the whole run's. The other
+ * methods and batch updates reject a union (LVG_EINVAL). */
+int lvg_static_union(lvg_graph *u, const lvg_options *o, lvg_result *results);
 /* Drains, stops the workers, frees the states and owned graphs. */
 int lvg_server_destroy(lvg_server *sv);
 
@@ -367,6 +383,11 @@ typedef struct lvg_stats {
   /* Host-array entry points (lvg_static/.../lvg_frontier): wall-clock time of
    * the call's three parts — batch + prior upload, the run, result download. */
   double   call_upload_ms, call_run_ms, call_download_ms;
+  /* Vertices of each degree bin whose distinct neighbour communities did not
+   * fit the bin's shared-memory table (redone with a table in HBM; bin 11:
+   * hub merges), and hub chunks that handed their raw pairs on. */
+  uint64_t move_bin_overflow[12];
+  uint64_t hub_chunk_overflow;
 } lvg_stats;
 /* Enable (1) or disable (0) per-launch event timing for calls on g. */
 int lvg_set_profiling(lvg_graph *g, int enable);

@@ -120,10 +120,44 @@ struct IterKey {
   size_t n[4];
   int k[4];
   float kr;
+  double E;  // graph unions: the tolerance the per-graph stop test uses
   bool operator==(const IterKey &o) const {
     return !std::memcmp(p, o.p, sizeof(p)) && !std::memcmp(n, o.n, sizeof(n)) && !std::memcmp(k, o.k, sizeof(k)) &&
-           kr == o.kr;
+           kr == o.kr && E == o.E;
   }
+};
+
+// A graph union (lvg_graph_create_union): graph i owns level-0 vertices
+// [vb[i], vb[i+1]) and keeps its own M, order and pass driver.
+struct UnionInfo {
+  size_t n = 0;
+  std::vector<uint64_t> vb;     // host copy of the level-0 bases
+  std::vector<double> M;        // per graph: total edge weight / 2
+  DBuf<uint32_t> gid0, vb0;     // level 0: graph of each vertex; bases [n+1]
+  DBuf<uint64_t> order;         // existing vertices per graph
+  DBuf<double> Md;
+  // per call
+  DBuf<float> kr;               // R / (2M) per graph
+  DBuf<uint32_t> gid[2], gbase[2];  // aggregated levels (alternating)
+  DBuf<unsigned long long> fix; // Σ best gains of the current iteration per graph
+  DBuf<GraphCtl> ctl;
+  HBuf<GraphCtl> hctl;
+  DBuf<uint8_t> gact, aggex;
+  DBuf<uint32_t> q;             // results (level-0 sized)
+  DBuf<float> ct;
+  DBuf<uint8_t> aff;
+};
+
+// What the local-moving launches of a union run need besides the level.
+struct UnionCall {
+  size_t n;
+  const float *kr;
+  unsigned long long *fix;
+  uint8_t *gact;
+  GraphCtl *ctl;
+  const double *M;
+  double E;
+  int L;
 };
 
 struct RunInfo {
@@ -192,6 +226,7 @@ struct lvg_graph {
   // batch buffers of the host-array entry points
   DBuf<uint32_t> b_ds, b_dd, b_is, b_id, b_seg;
   DBuf<float> b_dw, b_iw;
+  std::unique_ptr<UnionInfo> uni;  // set for graph unions
 };
 
 // A state or a device batch may outlive its graph (it keeps its own device
@@ -257,7 +292,8 @@ void read_counters(lvg_graph *g) {
 void compute_bins(lvg_graph *g, Level &lv, const uint32_t *deg, uint32_t *list, uint32_t *scratch, int colors) {
   g->hbins.ensure(bin_host_elems(MAX_COLORS));
   lv.colors = colors;
-  bin_items_u32(deg, lv.ex, lv.span, colors, list, lv.bin_start, lv.bin_maxdeg, scratch, g->hbins.p, g->stream);
+  bin_items_u32(deg, lv.ex, lv.span, colors, list, lv.bin_start, lv.bin_maxdeg, scratch, g->hbins.p, g->stream,
+                lv.gid, lv.gbase);
   lv.bins = list;
 }
 
@@ -286,8 +322,9 @@ void build_hub_plan(lvg_graph *g, Level &lv, HubPlanBuffers &hb) {
                                n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
   }
   launch_gather_u32(hb.hub_vertex.p, H, lv.deg, hb.degs.p, s);
-  std::vector<uint32_t> degs(H), first(H + 1);
+  std::vector<uint32_t> degs(H), verts(H), first(H + 1);
   LVG_CUDA(cudaMemcpyAsync(degs.data(), hb.degs.p, H * 4, cudaMemcpyDeviceToHost, s));
+  LVG_CUDA(cudaMemcpyAsync(verts.data(), hb.hub_vertex.p, H * 4, cudaMemcpyDeviceToHost, s));
   LVG_CUDA(cudaStreamSynchronize(s));
   std::vector<uint4> chunks;
   std::vector<uint64_t> parts;
@@ -297,7 +334,7 @@ void build_hub_plan(lvg_graph *g, Level &lv, HubPlanBuffers &hb) {
     for (size_t h = P.hub_begin[k]; h < P.hub_begin[k + 1]; ++h) {
       first[h] = uint32_t(chunks.size());
       for (uint32_t lo = 0; lo < degs[h]; lo += HUB_CHUNK) {
-        chunks.push_back(make_uint4(uint32_t(h), lo, std::min<uint32_t>(degs[h], lo + HUB_CHUNK), 0));
+        chunks.push_back(make_uint4(uint32_t(h), lo, std::min<uint32_t>(degs[h], lo + HUB_CHUNK), verts[h]));
         parts.push_back(part + lo);
       }
       part += degs[h];
@@ -352,7 +389,12 @@ int bin_stream(int b) { return b <= 4 ? 0 : b <= 8 ? 1 : b == 9 ? 2 : b == 10 ? 
 
 void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const float *tot,
                        const uint8_t *fa, float kr, bool sync, bool fused, const int *glog2, const size_t *goff,
-                       size_t need, std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> *bin_ev) {
+                       size_t need, std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> *bin_ev,
+                       const UnionCall *uc) {
+  auto set_union = [&](MoveArgs &a) {
+    if (!uc) return;
+    a.gid = lv.gid; a.gkr = uc->kr; a.gzero = lv.gbase; a.gfix = uc->fix; a.gact = uc->gact;
+  };
   Workspace &W = *g->ws;
   cudaStream_t s = g->stream;
   const int K = lv.colors;
@@ -371,7 +413,8 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot
     BinBounds bb;
     for (int b = 0; b <= NUM_BINS; ++b) bb.start[b] = lv.bin_start[k * NUM_BINS + b];
     uint32_t *wlc = W.wl_count.p + size_t(k) * NUM_BINS;
-    if (bb.start[NUM_BINS - 1] > bb.start[1]) launch_compact_active(lv.bins, bb, W.vaff.p, fa, W.wl.p, wlc, s);
+    if (bb.start[NUM_BINS - 1] > bb.start[1])
+      launch_compact_active(lv.bins, bb, W.vaff.p, fa, W.wl.p, wlc, s, uc ? lv.gid : nullptr, uc ? uc->gact : nullptr);
     if (conc) {  // fork
       LVG_CUDA(cudaEventRecord(g->fork_ev, s));
       for (auto a : g->aux) LVG_CUDA(cudaStreamWaitEvent(a, g->fork_ev, 0));
@@ -399,6 +442,7 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot
         a.vcom = com; a.ctot = ctot; a.dec = W.dec.p;
         a.vaff = W.vaff.p; a.mark = W.mark.p; a.fa = fa; a.vtot = tot;
         a.kr = kr; a.ctr = g->ctr.p; a.bin = grp.first;
+        set_union(a);
         cudaEvent_t b0 = bin_ev ? g->events.record(s) : nullptr;
         launch_move_small(grp.first, grp.second, sync, a, sb, stream_of(grp.first));
         if (bin_ev) bin_ev->push_back({grp.first, {b0, g->events.record(s)}});
@@ -419,6 +463,7 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot
       a.gkeys = need ? W.gkeys.p + goff[b] : nullptr;
       a.gvals = need ? W.gvals.p + goff[b] : nullptr;
       a.glog2 = glog2[b];
+      set_union(a);
       cudaEvent_t b0 = bin_ev ? g->events.record(s) : nullptr;
       if (b == NUM_BINS - 1) {
         a.hub = lv.hub;
@@ -445,6 +490,7 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot
       launch_merge_marks(W.vaff.p, W.mark.p, lv.span, s);
     }
   }
+  if (uc) launch_iter_control(uc->n, uc->ctl, uc->gact, uc->fix, uc->M, uc->E, uc->L, g->ctr.p, s);
   LVG_CUDA(cudaMemcpyAsync(g->hctr.p, g->ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
 }
 
@@ -453,7 +499,7 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot
 // failure disables graphs for this handle; the eager path stays correct.
 void capture_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const float *tot,
                        const uint8_t *fa, float kr, bool sync, bool fused, const int *glog2, const size_t *goff,
-                       size_t need, const IterKey &key) {
+                       size_t need, const IterKey &key, const UnionCall *uc) {
   cudaStream_t s = g->stream;
   if (g->iter_exec) {
     cudaGraphExecDestroy(g->iter_exec);
@@ -469,7 +515,7 @@ void capture_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot
   }
   bool fine = true;
   try {
-    enqueue_iteration(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, goff, need, nullptr);
+    enqueue_iteration(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, goff, need, nullptr, uc);
   } catch (const Error &) {
     fine = false;
   }
@@ -495,7 +541,7 @@ void capture_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot
 // iteration is captured once into a CUDA graph and replayed, one graph
 // launch per iteration instead of ~12 launches per colour class.
 int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const float *tot, const uint8_t *fa,
-               double M, float kr, int L, double E, bool sync, bool fused) {
+               double M, float kr, int L, double E, bool sync, bool fused, const UnionCall *uc = nullptr) {
   Workspace &W = *g->ws;
   cudaStream_t s = g->stream;
   const int K = lv.colors;
@@ -534,11 +580,12 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const 
   if (base) {
     const void *ps[22] = {lv.off, lv.bins, com, ctot, tot, fa, W.vaff.p, W.mark.p, W.dec.p, W.wl.p, W.wl_count.p,
                           W.gkeys.p, W.gvals.p, W.chunk_cnt.p, W.part_key.p, W.part_val.p, W.hub_kd.p, g->ctr.p,
-                          g->hctr.p, lv.hub.chunk, lv.hub.hub_vertex, nullptr};
+                          g->hctr.p, lv.hub.chunk, lv.hub.hub_vertex, lv.gid};
     std::memcpy(key.p, ps, sizeof(ps));
     key.n[0] = lv.span; key.n[1] = need; key.n[2] = lv.hub.chunks; key.n[3] = lv.bin_start[K * NUM_BINS];
     key.k[0] = K; key.k[1] = sync; key.k[2] = glog2[9] | glog2[10] << 8 | glog2[11] << 16; key.k[3] = fused;
     key.kr = kr;
+    key.E = uc ? E : 0.0;
   }
   const bool graphs = base && !g->profiling && !g->no_graphs;
   int l = 0;
@@ -555,7 +602,7 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const 
       bin_ev.clear();
       if (g->profiling) e0 = g->events.record(s);
       enqueue_iteration(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, goff, need,
-                        g->profiling ? &bin_ev : nullptr);
+                        g->profiling ? &bin_ev : nullptr, uc);
       if (g->profiling) e1 = g->events.record(s);
     }
     LVG_CUDA(cudaStreamSynchronize(s));
@@ -565,9 +612,13 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const 
       for (auto &be : bin_ev) g->stats.move_bin_ms[be.first] += elapsed(be.second.first, be.second.second);
     }
     if (graphs && !replay)
-      capture_iteration(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, goff, need, key);
-    el = double(g->hctr.p->el_fix) / GAIN_FIX / M;
+      capture_iteration(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, goff, need, key, uc);
     ++l;
+    if (uc) {  // each graph ran its own stop test (iter_control_kernel)
+      if (g->hctr.p->gactive == 0) break;
+      continue;
+    }
+    el = double(g->hctr.p->el_fix) / GAIN_FIX / M;
     if (el <= E) break;
   }
   return (l > 1 || el != 0) ? l : 0;
@@ -578,13 +629,15 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const 
 // Renumbered membership `com` of level `lv` with CN communities -> next level
 // in buffer set `which` (louvainCommunityVerticesOmpW + louvainAggregateOmpW,
 // inc/louvain.hxx:1197-1203). Also writes the new level's vertex weights.
-Level aggregate(lvg_graph *g, const Level &lv, const uint32_t *com, size_t CN, int which, int colors) {
+Level aggregate(lvg_graph *g, const Level &lv, const uint32_t *com, size_t CN, int which, int colors,
+                const uint32_t *ngid = nullptr, const uint32_t *ngbase = nullptr) {
   Workspace &W = *g->ws;
   cudaStream_t s = g->stream;
   LevelBuffers &nb = W.lv[which];
   Level nl;
   nl.span = nl.order = CN;
   nl.off = nb.off.p; nl.deg = nb.deg.p; nl.key = nb.key.p; nl.w = nb.w.p; nl.ex = nullptr;
+  nl.gid = ngid; nl.gbase = ngbase;
   // Community -> members CSR and row capacities.
   LVG_CUDA(cudaMemsetAsync(W.csize.p, 0, (CN + 1) * sizeof(uint32_t), s));
   LVG_CUDA(cudaMemsetAsync(W.ccur.p, 0, (CN + 1) * sizeof(uint32_t), s));
@@ -649,6 +702,7 @@ struct StateRef {
 // out: where the first level's membership/weights and final totals live.
 void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out, const lvg_options &o,
          RunInfo &info) {
+  if (g->uni) throw Error(LVG_EINVAL, "graph union: run it with lvg_static_union");
   ensure_ws(g);
   Workspace &W = *g->ws;
   cudaStream_t s = g->stream;
@@ -769,7 +823,138 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
   for (int b = 0; b < NUM_BINS; ++b) {
     g->stats.move_bin_vertices[b] = g->hctr.p->bin_vertices[b];
     g->stats.move_bin_edges[b] = g->hctr.p->bin_edges[b];
+    g->stats.move_bin_overflow[b] = g->hctr.p->bin_over[b];
   }
+  g->stats.hub_chunk_overflow = g->hctr.p->hub_chunk_over;
+  g->stats.kernel_launches = launch_counter() - launches0;
+}
+
+// Static Louvain on a graph union: one run over all graphs, each graph
+// keeping the reference's pass driver for itself (louvainOmp,
+// inc/louvain.hxx:1180-1215) through its GraphCtl entry: its own M and
+// R/(2M), colour classes by its own vertex ids, its own iteration stop test,
+// aggregation test and pass count. A graph that finishes leaves the union:
+// its membership, Σtot and affected flags are final at that point and it
+// takes no ids on the next level. The launches are those of one graph; what
+// differs is that a class's worklists hold the vertices of every graph still
+// moving.
+void run_union(lvg_graph *g, const lvg_options &o, RunInfo &info) {
+  ensure_ws(g);
+  Workspace &W = *g->ws;
+  UnionInfo &U = *g->uni;
+  cudaStream_t s = g->stream;
+  const size_t S = g->base.span, n = U.n;
+  const double R = o.resolution;
+  const int L = o.maxIterations, P = o.maxPasses;
+  const bool sync = o.deterministic != 0;
+  const int rep = std::max(1, o.repeat);
+  const int K = colors_for(o);
+  if (g->base.colors != K) {
+    compute_bins(g, g->base, g->deg.p, g->bins.p, W.binscratch.p, K);
+    build_hub_plan(g, g->base, g->hubplan);
+  }
+  {
+    std::vector<float> kr(n);
+    for (size_t i = 0; i < n; ++i) kr[i] = U.M[i] > 0 ? float(R / (2.0 * U.M[i])) : 0.f;
+    U.kr.ensure(n);
+    LVG_CUDA(cudaMemcpyAsync(U.kr.p, kr.data(), n * sizeof(float), cudaMemcpyHostToDevice, s));
+    LVG_CUDA(cudaStreamSynchronize(s));
+  }
+  U.fix.ensure(n); U.ctl.ensure(n); U.hctl.ensure(n); U.gact.ensure(n);
+  U.gid[0].ensure(S); U.gid[1].ensure(S); U.gbase[0].ensure(n + 1); U.gbase[1].ensure(n + 1);
+  U.aggex.ensure(S); U.q.ensure(S); U.ct.ensure(S); U.aff.ensure(S);
+  uint32_t *ucom = W.ucom.p;
+  float *utot = W.utot.p, *ctot = W.ctot.p;
+  g->stats = lvg_stats{};
+  const unsigned long long launches0 = launch_counter();
+  LVG_CUDA(cudaMemsetAsync(g->ctr.p, 0, sizeof(Counters), s));
+  const UnionCall uc0{n, U.kr.p, U.fix.p, U.gact.p, U.ctl.p, U.Md.p, 0.0, L};
+  for (int r = 0; r < rep; ++r) {
+    g->events.reset();
+    LVG_CUDA(cudaMemsetAsync(W.vaff.p, 0, S, s));
+    LVG_CUDA(cudaMemsetAsync(W.vcom.p, 0, S * sizeof(uint32_t), s));
+    LVG_CUDA(cudaMemsetAsync(W.vtot.p, 0, S * sizeof(float), s));
+    LVG_CUDA(cudaMemsetAsync(U.ctl.p, 0, n * sizeof(GraphCtl), s));
+    LVG_CUDA(cudaMemsetAsync(U.fix.p, 0, n * sizeof(unsigned long long), s));
+    cudaEvent_t e0 = g->events.record(s);
+    launch_init_static(g->base, ucom, utot, ctot, s);
+    cudaEvent_t e1 = g->events.record(s);
+    LVG_CUDA(cudaMemsetAsync(W.vaff.p, 1, S, s));
+    cudaEvent_t e2 = g->events.record(s);
+    // graphs with M = 0 (or no passes) end as initialised
+    launch_pass_skip(n, U.ctl.p, U.Md.p, P, s);
+    launch_union_snapshot(S, U.gid0.p, U.vb0.p, U.vb0.p, U.ctl.p, ctot, W.vaff.p, U.ct.p, U.aff.p, s);
+    launch_union_finalize(S, U.gid0.p, ucom, nullptr, U.vb0.p, U.ctl.p, U.q.p, s);
+    launch_union_mark_done(n, U.ctl.p, s);
+    cudaEvent_t ep1 = nullptr;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> tl_ev, ta_ev;
+    double E = o.tolerance;
+    Level lv = g->base;
+    uint32_t *com = ucom;
+    const float *tot = utot;
+    int which = 0;
+    for (int p = 0;; ++p) {
+      if (p == 1) ep1 = g->events.record(s);
+      const bool first = p == 0;
+      launch_pass_begin(n, U.ctl.p, U.gact.p, s);
+      UnionCall uc = uc0;
+      uc.E = E;
+      cudaEvent_t a0 = g->events.record(s);
+      move_phase(g, lv, com, ctot, tot, nullptr, 0.0, 0.f, L, E, sync, false, &uc);
+      tl_ev.push_back({a0, g->events.record(s)});
+      launch_pass_end(n, U.ctl.p, P, s);
+      launch_union_snapshot(lv.span, lv.gid, lv.gbase, U.vb0.p, U.ctl.p, ctot, W.vaff.p, U.ct.p, U.aff.p, s);
+      // communities of the graphs that go on; the aggregation test per graph
+      LVG_CUDA(cudaMemsetAsync(W.cext.p, 0, (lv.span + 1) * sizeof(uint32_t), s));
+      launch_union_flags(lv.ex, lv.span, com, lv.gid, U.ctl.p, W.cext.p, s);
+      launch_union_tolerance(n, lv.gbase, W.cext.p, U.ctl.p, U.order.p, first, o.aggregationTolerance, s);
+      exclusive_scan_u32(W.cext.p, W.cext.p, lv.span, &g->ctr.p->cn, W.scan32.p, s);
+      launch_union_finalize(S, U.gid0.p, ucom, first ? nullptr : com, lv.gbase, U.ctl.p, U.q.p, s);
+      launch_union_aggex(lv.ex, lv.span, lv.gid, U.ctl.p, U.aggex.p, s);
+      launch_union_mark_done(n, U.ctl.p, s);
+      read_counters(g);
+      const size_t CN = g->hctr.p->cn;
+      if (CN == 0) break;  // every graph is done
+      // next level: the remaining graphs' communities, renumbered in order
+      uint32_t *ngid = U.gid[which].p, *ngbase = U.gbase[which].p;
+      launch_union_bases(n, lv.gbase, lv.span, W.cext.p, &g->ctr.p->cn, ngbase, s);
+      launch_fill_gid(ngbase, n, ngid, s);
+      launch_lookup(com, W.cext.p, lv.span, s);
+      if (!first) launch_union_lookup(ucom, W.vcom.p, S, U.gid0.p, U.ctl.p, s);
+      Level am = lv;
+      am.ex = U.aggex.p;
+      cudaEvent_t g0 = g->events.record(s);
+      lv = aggregate(g, am, com, CN, which, K, ngid, ngbase);
+      ta_ev.push_back({g0, g->events.record(s)});
+      which ^= 1;
+      com = W.vcom.p;
+      tot = W.vtot.p;
+      launch_level_init(CN, W.vtot.p, W.vcom.p, ctot, W.vaff.p, s);
+      E /= o.toleranceDrop;
+    }
+    cudaEvent_t eend = g->events.record(s);
+    LVG_CUDA(cudaStreamSynchronize(s));
+    info.ti += elapsed(e0, e1);
+    info.tm += elapsed(e1, e2);
+    info.tp += elapsed(e2, ep1 ? ep1 : eend);
+    for (auto &pr : tl_ev) info.tl += elapsed(pr.first, pr.second);
+    for (auto &pr : ta_ev) info.ta += elapsed(pr.first, pr.second);
+    info.t += elapsed(e0, eend);
+  }
+  launch_union_affected(n, U.vb0.p, U.aff.p, U.ctl.p, s);
+  LVG_CUDA(cudaMemcpyAsync(U.hctl.p, U.ctl.p, n * sizeof(GraphCtl), cudaMemcpyDeviceToHost, s));
+  read_counters(g);
+  info.t /= rep; info.tm /= rep; info.ti /= rep; info.tp /= rep; info.tl /= rep; info.ta /= rep;
+  g->stats.move_vertices = g->hctr.p->vertices;
+  g->stats.move_edges = g->hctr.p->edges;
+  g->stats.moves = g->hctr.p->moves;
+  g->stats.aggregate_edges = g->hctr.p->agg_edges;
+  for (int b = 0; b < NUM_BINS; ++b) {
+    g->stats.move_bin_vertices[b] = g->hctr.p->bin_vertices[b];
+    g->stats.move_bin_edges[b] = g->hctr.p->bin_edges[b];
+    g->stats.move_bin_overflow[b] = g->hctr.p->bin_over[b];
+  }
+  g->stats.hub_chunk_overflow = g->hctr.p->hub_chunk_over;
   g->stats.kernel_launches = launch_counter() - launches0;
 }
 
@@ -1400,6 +1585,150 @@ int lvg_graph_clone(lvg_graph *x, lvg_graph **out) {
   return LVG_OK;
 }
 
+int lvg_graph_create_union(lvg_graph *const *graphs, size_t n, lvg_graph **out) {
+  if (!graphs || !n || !out) return lvg::fail(LVG_EINVAL, "null argument or no graphs");
+  *out = nullptr;
+  for (size_t i = 0; i < n; ++i) {
+    if (!graphs[i]) return lvg::fail(LVG_EINVAL, "null graph");
+    if (graphs[i]->uni) return lvg::fail(LVG_EINVAL, "a graph union cannot be part of a union");
+    if (graphs[i]->device != graphs[0]->device) return lvg::fail(LVG_EINVAL, "graphs on different devices");
+  }
+  std::unique_ptr<lvg_graph> g(new lvg_graph());
+  lvg::AcctScope acct_(&g->bytes);
+  int rc = lvg::guarded([&] {
+    using namespace lvg;
+    LVG_CUDA(cudaSetDevice(graphs[0]->device));
+    g->device = graphs[0]->device;
+    LVG_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+    cudaStream_t s = g->stream;
+    auto U = std::make_unique<UnionInfo>();
+    U->n = n;
+    U->vb.assign(n + 1, 0);
+    U->M.resize(n);
+    std::vector<uint64_t> order(n);
+    size_t ord = 0;
+    for (size_t i = 0; i < n; ++i) {
+      const lvg_graph *x = graphs[i];
+      LVG_CUDA(cudaStreamSynchronize(x->stream));
+      U->vb[i + 1] = U->vb[i] + x->base.span;
+      order[i] = x->base.order;
+      ord += x->base.order;
+      U->M[i] = x->total_weight / 2;
+    }
+    const size_t S = U->vb[n];
+    if (S >= size_t(EMPTY)) throw Error(LVG_EINVAL, "graph union: more than 2^32-2 vertices");
+    // compact union CSR: degrees, their scan, rows with ids shifted by the graph's first vertex
+    DBuf<uint64_t> coff, sc;
+    DBuf<uint32_t> ckey;
+    DBuf<float> cw;
+    coff.ensure(S + 1);
+    sc.ensure(scan_scratch_elems(S + 1));
+    g->ex.ensure(S);
+    for (size_t i = 0; i < n; ++i) {
+      const lvg_graph *x = graphs[i];
+      const size_t sp = x->base.span;
+      launch_union_degrees(x->base.deg, sp, coff.p + U->vb[i], s);
+      if (!sp) continue;
+      if (x->base.ex) LVG_CUDA(cudaMemcpyAsync(g->ex.p + U->vb[i], x->base.ex, sp, cudaMemcpyDeviceToDevice, s));
+      else LVG_CUDA(cudaMemsetAsync(g->ex.p + U->vb[i], 1, sp, s));
+    }
+    exclusive_scan_u64(coff.p, coff.p, S, coff.p + S, sc.p, s);
+    uint64_t X = 0;  // edges: the degrees' sum
+    LVG_CUDA(cudaMemcpyAsync(&X, coff.p + S, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    LVG_CUDA(cudaStreamSynchronize(s));
+    ckey.ensure(std::max<size_t>(X, 1));
+    cw.ensure(std::max<size_t>(X, 1));
+    for (size_t i = 0; i < n; ++i) {
+      const lvg_graph *x = graphs[i];
+      launch_union_rows(x->base.off, x->base.deg, x->base.key, x->base.w, x->base.span, uint32_t(U->vb[i]), coff.p,
+                        ckey.p, cw.p, s);
+    }
+    std::vector<uint32_t> vb32(n + 1);
+    for (size_t i = 0; i <= n; ++i) vb32[i] = uint32_t(U->vb[i]);
+    U->vb0.ensure(n + 1);
+    U->gid0.ensure(S);
+    U->order.ensure(n);
+    U->Md.ensure(n);
+    LVG_CUDA(cudaMemcpyAsync(U->vb0.p, vb32.data(), (n + 1) * 4, cudaMemcpyHostToDevice, s));
+    LVG_CUDA(cudaMemcpyAsync(U->order.p, order.data(), n * 8, cudaMemcpyHostToDevice, s));
+    LVG_CUDA(cudaMemcpyAsync(U->Md.p, U->M.data(), n * 8, cudaMemcpyHostToDevice, s));
+    launch_fill_gid(U->vb0.p, n, U->gid0.p, s);
+    LVG_CUDA(cudaStreamSynchronize(s));
+    init_graph(g.get(), S, ord, X, coff.p, ckey.p, cw.p, true);
+    // colour classes by each graph's own vertex ids
+    g->base.gid = U->gid0.p;
+    g->base.gbase = U->vb0.p;
+    DBuf<uint32_t> scratch;
+    scratch.ensure(bin_scratch_elems(S + 1, DEFAULT_COLORS_ASYNC));
+    compute_bins(g.get(), g->base, g->deg.p, g->bins.p, scratch.p, DEFAULT_COLORS_ASYNC);
+    build_hub_plan(g.get(), g->base, g->hubplan);
+    g->uni = std::move(U);
+    return LVG_OK;
+  });
+  if (rc != LVG_OK) {
+    if (g->stream) cudaStreamDestroy(g->stream);
+    return rc;
+  }
+  *out = g.release();
+  return LVG_OK;
+}
+
+int lvg_union_graphs(const lvg_graph *u, size_t *n) {
+  if (!u || !n) return lvg::fail(LVG_EINVAL, "null argument");
+  *n = u->uni ? u->uni->n : 0;
+  return LVG_OK;
+}
+
+int lvg_static_union(lvg_graph *u, const lvg_options *o, lvg_result *results) {
+  lvg::AcctScope acct_(u ? &u->bytes : nullptr);
+  if (!u || !results) return lvg::fail(LVG_EINVAL, "null graph or results");
+  if (!u->uni) return lvg::fail(LVG_EINVAL, "not a graph union (lvg_graph_create_union)");
+  return lvg::guarded([&] {
+    using namespace lvg;
+    LVG_CUDA(cudaSetDevice(u->device));
+    lvg_options opt;
+    if (o) opt = *o; else lvg_options_default(&opt);
+    const auto t0 = std::chrono::steady_clock::now();
+    RunInfo info;
+    run_union(u, opt, info);
+    const auto t1 = std::chrono::steady_clock::now();
+    UnionInfo &U = *u->uni;
+    Workspace &W = *u->ws;
+    cudaStream_t s = u->stream;
+    const size_t S = u->base.span;
+    W.stage_a.ensure(S);
+    W.stage_b.ensure(S);
+    launch_f32_to_f64(W.utot.p, W.stage_a.p, S, s);
+    launch_f32_to_f64(U.ct.p, W.stage_b.p, S, s);
+    for (size_t i = 0; i < U.n; ++i) {
+      lvg_result *r = &results[i];
+      const size_t b = U.vb[i], sp = U.vb[i + 1] - U.vb[i];
+      if (!r->membership) { r->membership = (uint32_t *)std::malloc(sp * 4 + 1); r->owned |= 1; }
+      if (!r->vertexWeight) { r->vertexWeight = (double *)std::malloc(sp * 8 + 1); r->owned |= 2; }
+      if (!r->communityWeight) { r->communityWeight = (double *)std::malloc(sp * 8 + 1); r->owned |= 4; }
+      if (!r->membership || !r->vertexWeight || !r->communityWeight) throw std::bad_alloc();
+      if (sp) {
+        LVG_CUDA(cudaMemcpyAsync(r->membership, U.q.p + b, sp * 4, cudaMemcpyDeviceToHost, s));
+        LVG_CUDA(cudaMemcpyAsync(r->vertexWeight, W.stage_a.p + b, sp * 8, cudaMemcpyDeviceToHost, s));
+        LVG_CUDA(cudaMemcpyAsync(r->communityWeight, W.stage_b.p + b, sp * 8, cudaMemcpyDeviceToHost, s));
+      }
+      const GraphCtl &c = U.hctl.p[i];
+      RunInfo ri = info;
+      ri.iterations = int(c.l);
+      ri.passes = int(c.p);
+      ri.affected = c.aff;
+      fill_result(r, ri, sp);
+    }
+    LVG_CUDA(cudaStreamSynchronize(s));
+    const auto t2 = std::chrono::steady_clock::now();
+    using ms = std::chrono::duration<double, std::milli>;
+    u->stats.call_upload_ms = 0;
+    u->stats.call_run_ms = ms(t1 - t0).count();
+    u->stats.call_download_ms = ms(t2 - t1).count();
+    return LVG_OK;
+  });
+}
+
 int lvg_graph_destroy(lvg_graph *g) {
   if (!g) return LVG_OK;
   cudaSetDevice(g->device);
@@ -1722,6 +2051,7 @@ int lvg_device_batch_create(lvg_graph *g, const lvg_batch *b, lvg_device_batch *
 int lvg_graph_apply_batch(lvg_graph *g, const lvg_batch *b, lvg_batch_buf *tidy) {
   lvg::AcctScope acct_(g ? &g->bytes : nullptr);
   if (!g) return lvg::fail(LVG_EINVAL, "null graph");
+  if (g->uni) return lvg::fail(LVG_EINVAL, "batch updates of a graph union are not supported");
   if (tidy && b &&
       ((b->num_deletions && (!tidy->del_src || !tidy->del_dst || !tidy->del_w)) ||
        (b->num_insertions && (!tidy->ins_src || !tidy->ins_dst || !tidy->ins_w))))
@@ -1760,6 +2090,7 @@ int lvg_graph_apply_batch(lvg_graph *g, const lvg_batch *b, lvg_batch_buf *tidy)
 
 int lvg_graph_apply_device_batch(lvg_graph *g, lvg_device_batch *b) {
   if (!g || !b) return lvg::fail(LVG_EINVAL, "null argument");
+  if (g->uni) return lvg::fail(LVG_EINVAL, "batch updates of a graph union are not supported");
   if (b->g != g) return lvg::fail(LVG_EINVAL, "the batch was created on another graph");
   if (b->applied) return lvg::fail(LVG_EINVAL, "the batch has already been applied");
   return lvg::guarded([&] {

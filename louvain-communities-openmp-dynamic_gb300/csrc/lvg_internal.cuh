@@ -82,14 +82,14 @@ struct HBuf {  // pinned host buffer, grows on demand
 // level: each hub's edge list is cut into chunks of HUB_CHUNK edges that
 // different blocks aggregate at once; a second kernel merges a hub's chunks.
 // Hubs are ordered by colour class; chunks by hub.
-constexpr uint32_t HUB_CHUNK = 16384;
+constexpr uint32_t HUB_CHUNK = 4096;
 struct HubPlan {
   size_t hubs = 0, chunks = 0, part = 0;        // counts; part = partial-entry capacity
   size_t hub_begin[MAX_COLORS + 1] = {};        // hubs of colour k: [hub_begin[k], hub_begin[k+1])
   size_t chunk_begin[MAX_COLORS + 1] = {};      // chunks of colour k
   const uint32_t *hub_vertex = nullptr;         // [hubs] vertex id
   const uint32_t *hub_first = nullptr;          // [hubs+1] first chunk of each hub
-  const uint4 *chunk = nullptr;                 // [chunks] (hub, first edge, end edge, -)
+  const uint4 *chunk = nullptr;                 // [chunks] (hub, first edge, end edge, hub vertex)
   const uint64_t *chunk_part = nullptr;         // [chunks] offset of the chunk's partial entries
 };
 
@@ -104,6 +104,10 @@ struct Level {
   uint32_t *key = nullptr;
   float *w = nullptr;
   const uint8_t *ex = nullptr;
+  // Graph unions (lvg_graph_create_union): the graph of each vertex, and each
+  // graph's first vertex on this level ([graphs+1]); nullptr for one graph.
+  const uint32_t *gid = nullptr;
+  const uint32_t *gbase = nullptr;
   // Vertices grouped by (colour class, degree bin), ascending id within a
   // group: group (k, b) is bins[bin_start[k*NUM_BINS+b] .. bin_start[k*NUM_BINS+b+1]).
   uint32_t *bins = nullptr;
@@ -130,6 +134,22 @@ struct Counters {
   double fp64[4];                // FP64 reductions (total weight, modularity terms)
   unsigned long long bin_vertices[NUM_BINS];  // processed vertices per degree bin
   unsigned long long bin_edges[NUM_BINS];     // scanned edges per degree bin
+  unsigned long long bin_over[NUM_BINS];      // vertices redone with an HBM table per bin
+  unsigned long long hub_chunk_over;          // hub chunks that wrote raw pairs
+  unsigned int gactive;                       // graph unions: graphs still moving after an iteration
+};
+
+// Per-graph control of a graph-union run (lvg_static_union), on the device:
+// the pass driver of inc/louvain.hxx:1180-1215 kept for each graph.
+struct GraphCtl {
+  double el;             // last iteration's Σ best gains / M (the reference's el)
+  unsigned long long aff;  // residual affected flags at the end (affectedVertices)
+  uint32_t it;           // iterations of the current pass
+  uint32_t l, p;         // iterations and passes so far
+  uint32_t cn;           // communities counted at the end of the last pass
+  uint8_t done;          // finished: its result is final
+  uint8_t fin;           // finishes at the end of the current pass
+  uint8_t pad[6];
 };
 
 // Arguments of the local-moving kernels (inc/louvain.hxx:588-609).
@@ -161,6 +181,14 @@ struct MoveArgs {
   float *part_val;
   float *hub_kd;         // [span] weight to the own community, summed over chunks
   int color;             // colour class of the launch
+  // Graph unions (nullptr for one graph): graph of each vertex, per graph
+  // R/(2M), the id of its vertex 0 on this level (never a move target, as
+  // community 0 of a graph alone), Σ best gains, and whether it still moves.
+  const uint32_t *gid = nullptr;
+  const float *gkr = nullptr;
+  const uint32_t *gzero = nullptr;
+  unsigned long long *gfix = nullptr;
+  const uint8_t *gact = nullptr;
 };
 
 // Arguments of the aggregation kernels (inc/louvain.hxx:897-912, 987-992).
@@ -196,12 +224,15 @@ void exclusive_scan_u64(const uint64_t *in, uint64_t *out, size_t n, uint64_t *t
 // Stable multi-split of items [0,n) into `list` by (colour class of the id,
 // degree bin), colour-major, ascending id within a group; items with
 // ex[i] == 0 (ex != nullptr) are left out. Writes the colors*NUM_BINS+1 group
-// starts and the per-bin max degree to the host arrays (synchronises).
+// starts and the per-bin max degree to the host arrays (synchronises). For a
+// graph union (gid != nullptr) the class of item j is that of j - gbase[gid[j]],
+// its id within its own graph.
 constexpr int BIN_CHUNK = 2048;
 size_t bin_scratch_elems(size_t n, int colors);
 size_t bin_host_elems(int colors);
 void bin_items_u32(const uint32_t *deg, const uint8_t *ex, size_t n, int colors, uint32_t *list, size_t *bin_start,
-                   uint64_t *bin_maxdeg, uint32_t *scratch, uint32_t *host_pinned, cudaStream_t s);
+                   uint64_t *bin_maxdeg, uint32_t *scratch, uint32_t *host_pinned, cudaStream_t s,
+                   const uint32_t *gid = nullptr, const uint32_t *gbase = nullptr);
 void bin_items_u64(const uint64_t *deg, const uint8_t *ex, size_t n, int colors, uint32_t *list,
                    size_t *bin_start, uint64_t *bin_maxdeg, uint32_t *scratch, uint32_t *host_pinned,
                    cudaStream_t s);
@@ -238,8 +269,10 @@ void launch_merge_marks(uint8_t *vaff, uint8_t *mark, size_t n, cudaStream_t s);
 struct BinBounds {
   uint64_t start[NUM_BINS + 1];
 };
+// Graph unions: only vertices whose graph still moves (gact[gid[u]]).
 void launch_compact_active(const uint32_t *bins, const BinBounds &bb, const uint8_t *vaff, const uint8_t *fa,
-                           uint32_t *wl, uint32_t *wl_count, cudaStream_t s);
+                           uint32_t *wl, uint32_t *wl_count, cudaStream_t s, const uint32_t *gid = nullptr,
+                           const uint8_t *gact = nullptr);
 // Deterministic mode: apply the decisions of one colour class (list of its vertices).
 void launch_apply_moves(const uint32_t *list, size_t n, uint32_t *dec, uint32_t *vcom, float *ctot,
                         const float *vtot, cudaStream_t s);
@@ -377,5 +410,53 @@ int device_sms();
 // Grid of the local-moving kernel of a large-degree bin (9, 10; 11 = the hub
 // merge) for `count` vertices: the size of its per-block global fallback.
 int move_grid_blocks(int bin, bool sync, size_t count);
+
+
+// ---------------------------------------------------------------- graph unions (lvg_union.cu)
+// Level-0 vertices of graph i: [vb[i], vb[i+1]); gid[x] = i for those.
+void launch_fill_gid(const uint32_t *vb, size_t n, uint32_t *gid, cudaStream_t s);
+// Union CSR assembly: widened degrees, then rows copied with ids shifted by the graph's base.
+void launch_union_degrees(const uint32_t *deg, size_t span, uint64_t *dst, cudaStream_t s);
+void launch_union_rows(const uint64_t *off, const uint32_t *deg, const uint32_t *key, const float *w, size_t span,
+                       uint32_t vbase, const uint64_t *coff, uint32_t *ckey, float *cw, cudaStream_t s);
+// After an iteration: per-graph el, iteration count, stop test; counts the
+// graphs still moving into ctr->gactive.
+void launch_iter_control(size_t n, GraphCtl *ctl, uint8_t *gact, unsigned long long *fix, const double *M, double E,
+                         int L, Counters *ctr, cudaStream_t s);
+// At the start of a pass: gact = graph not done; iteration counts reset.
+void launch_pass_begin(size_t n, GraphCtl *ctl, uint8_t *gact, cudaStream_t s);
+// After a pass's local moving: iterations/passes, and fin for m <= 1 or p >= P.
+void launch_pass_end(size_t n, GraphCtl *ctl, int P, cudaStream_t s);
+// Graphs with nothing to do (M = 0 or no passes) finish before the first pass.
+void launch_pass_skip(size_t n, GraphCtl *ctl, const double *M, int P, cudaStream_t s);
+// Community flags of the graphs that go on (not fin, not done).
+void launch_union_flags(const uint8_t *ex, size_t span, const uint32_t *vcom, const uint32_t *gid,
+                        const GraphCtl *ctl, uint32_t *cext, cudaStream_t s);
+// Per graph: communities counted; fin when CN/GN >= tol (GN = existing
+// vertices on the first pass, else the graph's vertices on the level), and
+// then its flags cleared.
+void launch_union_tolerance(size_t n, const uint32_t *gbase, uint32_t *cext, GraphCtl *ctl, const uint64_t *order,
+                            bool first, double tol, cudaStream_t s);
+// Copies of the level's Σtot and affected flags into each graph's result
+// slice (the reference's arrays keep earlier levels' entries past the level's
+// span).
+void launch_union_snapshot(size_t span, const uint32_t *gid, const uint32_t *gbase, const uint32_t *vb0,
+                           const GraphCtl *ctl, const float *ctot, const uint8_t *vaff, float *ct_res,
+                           uint8_t *aff_res, cudaStream_t s);
+// Final membership of the graphs finishing now: (vcom ? vcom[ucom[v]] : ucom[v]) - gbase[g]; then done.
+void launch_union_finalize(size_t S, const uint32_t *gid0, const uint32_t *ucom, const uint32_t *vcom,
+                           const uint32_t *gbase, GraphCtl *ctl, uint32_t *q, cudaStream_t s);
+void launch_union_mark_done(size_t n, GraphCtl *ctl, cudaStream_t s);
+// ucom[v] = map[ucom[v]] for vertices of graphs not done.
+void launch_union_lookup(uint32_t *ucom, const uint32_t *map, size_t S, const uint32_t *gid0, const GraphCtl *ctl,
+                         cudaStream_t s);
+// Next level's bases: gbase_new[i] = cext[gbase[i]] (the total past the end).
+void launch_union_bases(size_t n, const uint32_t *gbase, size_t span, const uint32_t *cext, const uint32_t *total,
+                        uint32_t *gbase_new, cudaStream_t s);
+// Aggregation mask of a level: existing vertices of graphs that go on.
+void launch_union_aggex(const uint8_t *ex, size_t span, const uint32_t *gid, const GraphCtl *ctl, uint8_t *aggex,
+                        cudaStream_t s);
+// affectedVertices of each graph from its result flags.
+void launch_union_affected(size_t n, const uint32_t *vb0, const uint8_t *aff_res, GraphCtl *ctl, cudaStream_t s);
 
 }  // namespace lvg

@@ -45,7 +45,8 @@ __global__ void degrees_kernel(const uint64_t *off, uint32_t *deg, size_t n) {
 // louvainVertexWeightsOmpW (inc/louvain.hxx:210) + louvainInitializeOmpW
 // (:285) for level 0: one warp per vertex (lane-strided rows).
 __global__ void init_static_kernel(const uint64_t *off, const uint32_t *deg, const float *w, const uint8_t *ex,
-                                   size_t n, uint32_t *ucom, float *utot, float *ctot) {
+                                   size_t n, const uint32_t *gid, const uint32_t *gbase, uint32_t *ucom, float *utot,
+                                   float *ctot) {
   const size_t warps = size_t(gridDim.x) * blockDim.x / 32;
   const int lane = threadIdx.x & 31;
   for (size_t u = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32; u < n; u += warps) {
@@ -59,7 +60,8 @@ __global__ void init_static_kernel(const uint64_t *off, const uint32_t *deg, con
       for (int k = 16; k > 0; k >>= 1) s += __shfl_xor_sync(0xffffffffu, s, k);
     }
     if (lane == 0) {
-      ucom[u] = has ? uint32_t(u) : 0u;
+      // an absent vertex starts in community 0 (of its own graph in a union)
+      ucom[u] = has ? uint32_t(u) : (gid ? gbase[gid[u]] : 0u);
       utot[u] = s;
       ctot[u] = s;
     }
@@ -369,7 +371,7 @@ __global__ void level_init_kernel(size_t n, const float *vtot, uint32_t *vcom, f
 // Active vertices of one colour class into per-bin worklists (warp-aggregated
 // appends; the order within a worklist is unspecified).
 __global__ void compact_active_kernel(const uint32_t *bins, BinBounds bb, const uint8_t *vaff, const uint8_t *fa,
-                                      uint32_t *wl, uint32_t *wl_count) {
+                                      const uint32_t *gid, const uint8_t *gact, uint32_t *wl, uint32_t *wl_count) {
   const uint64_t begin = bb.start[1], end = bb.start[NUM_BINS - 1];
   const int lane = threadIdx.x & 31;
   for (uint64_t base = begin + (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32 * 32; base < end;
@@ -379,7 +381,7 @@ __global__ void compact_active_kernel(const uint32_t *bins, BinBounds bb, const 
     uint32_t u = 0;
     if (pos < end) {
       u = bins[pos];
-      if (vaff[u] && (!fa || fa[u])) {
+      if (vaff[u] && (!fa || fa[u]) && (!gact || gact[gid[u]])) {
         b = 1;
         while (pos >= bb.start[b + 1]) ++b;
       }
@@ -469,7 +471,8 @@ void launch_fill_f32(float *p, size_t n, float v, cudaStream_t s) {
 
 void launch_init_static(const Level &g, uint32_t *ucom, float *utot, float *ctot, cudaStream_t s) {
   if (!g.span) return;
-  init_static_kernel<<<grid_for(g.span * 32, 256), 256, 0, s>>>(g.off, g.deg, g.w, g.ex, g.span, ucom, utot, ctot);
+  init_static_kernel<<<grid_for(g.span * 32, 256), 256, 0, s>>>(g.off, g.deg, g.w, g.ex, g.span, g.gid, g.gbase,
+                                                                 ucom, utot, ctot);
   LVG_CHECK_LAUNCH();
 }
 
@@ -595,10 +598,11 @@ void launch_level_init(size_t n, const float *vtot, uint32_t *vcom, float *ctot,
 }
 
 void launch_compact_active(const uint32_t *bins, const BinBounds &bb, const uint8_t *vaff, const uint8_t *fa,
-                           uint32_t *wl, uint32_t *wl_count, cudaStream_t s) {
+                           uint32_t *wl, uint32_t *wl_count, cudaStream_t s, const uint32_t *gid,
+                           const uint8_t *gact) {
   const uint64_t n = bb.start[NUM_BINS - 1] - bb.start[1];
   if (!n) return;
-  compact_active_kernel<<<grid_for(n, 256), 256, 0, s>>>(bins, bb, vaff, fa, wl, wl_count);
+  compact_active_kernel<<<grid_for(n, 256), 256, 0, s>>>(bins, bb, vaff, fa, gid, gact, wl, wl_count);
   LVG_CHECK_LAUNCH();
 }
 

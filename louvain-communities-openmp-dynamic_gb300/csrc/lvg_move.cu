@@ -35,9 +35,12 @@ __host__ __device__ constexpr int ilog2c(int x) { return x <= 1 ? 0 : 1 + ilog2c
 
 template <int T>
 __device__ __forceinline__ unsigned tile_mask() {
-  if (T == 32) return 0xffffffffu;
-  const int lane = threadIdx.x & 31;
-  return ((1u << T) - 1u) << (lane & ~(T - 1));
+  if constexpr (T == 32) {
+    return 0xffffffffu;
+  } else {
+    const int lane = threadIdx.x & 31;
+    return ((1u << T) - 1u) << (lane & ~(T - 1));
+  }
 }
 
 // Insert (c, w) into an open-addressing table of 2^log2cap slots (linear
@@ -64,14 +67,39 @@ __device__ __forceinline__ void take_better(float &bg, uint32_t &bc, float og, u
   if (better(og, oc, bg, bc)) { bg = og; bc = oc; }
 }
 
+// The graph-dependent constants of vertex u: R/(2M) and the community that is
+// never a move target (the reference's `if (c)`, inc/louvain.hxx:602). For a
+// graph union they are those of u's own graph (MoveArgs::gid), so each graph
+// moves exactly as it would alone.
+struct GraphOf {
+  float kr;
+  uint32_t zero, g;
+  __device__ __forceinline__ GraphOf(const MoveArgs &a, uint32_t u) : kr(a.kr), zero(0), g(0) {
+    if (a.gid) {
+      g = a.gid[u];
+      kr = a.gkr[g];
+      zero = a.gzero[g];
+    }
+  }
+};
+
+// Adds a vertex's best gain to the iteration's sum: per thread (flushed per
+// block) for one graph, per graph for a union.
+__device__ __forceinline__ void add_gain(const MoveArgs &a, const GraphOf &G, unsigned long long &fix, float bg) {
+  if (a.gfix) atomicAdd(&a.gfix[G.g], gain_to_fix(bg));
+  else fix += gain_to_fix(bg);
+}
+
 __device__ __forceinline__ void flush_counters(Counters *ctr, int bin, unsigned long long fix, unsigned long long nv,
-                                               unsigned long long ne, unsigned long long nm, bool bad) {
+                                               unsigned long long ne, unsigned long long nm, bool bad,
+                                               unsigned long long no = 0) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     fix += __shfl_xor_sync(0xffffffffu, fix, o);
     nv += __shfl_xor_sync(0xffffffffu, nv, o);
     ne += __shfl_xor_sync(0xffffffffu, ne, o);
     nm += __shfl_xor_sync(0xffffffffu, nm, o);
+    no += __shfl_xor_sync(0xffffffffu, no, o);
   }
   bool anybad = __any_sync(0xffffffffu, bad);
   if ((threadIdx.x & 31) == 0) {
@@ -79,6 +107,7 @@ __device__ __forceinline__ void flush_counters(Counters *ctr, int bin, unsigned 
     if (nv) { atomicAdd(&ctr->vertices, nv); atomicAdd(&ctr->bin_vertices[bin], nv); }
     if (ne) { atomicAdd(&ctr->edges, ne); atomicAdd(&ctr->bin_edges[bin], ne); }
     if (nm) atomicAdd(&ctr->moves, nm);
+    if (no) atomicAdd(&ctr->bin_over[bin], no);
     if (anybad) atomicOr(&ctr->err, ERR_TABLE_FULL);
   }
 }
@@ -123,14 +152,11 @@ __device__ __forceinline__ void tile_loop(const MoveArgs &a, const uint32_t *lis
   uint32_t *keys = reinterpret_cast<uint32_t *>(smem) + tib * C;
   float *vals = reinterpret_cast<float *>(smem + size_t(TPB) * C * sizeof(uint32_t)) + tib * C;
   const unsigned m = tile_mask<T>();
-  unsigned long long fix = 0, nv = 0, ne = 0, nm = 0;
+  unsigned long long fix = 0, nv = 0, ne = 0, nm = 0, no = 0;
   bool bad = false;
   for (uint32_t i = first + tib; i < count; i += ntiles) {
-    const uint32_t u = list[i];
-    int act = 0;
-    if (tl == 0) act = a.vaff[u] && (!a.fa || a.fa[u]);
-    act = __shfl_sync(m, act, 0, T);
-    if (!act) continue;
+    const uint32_t u = list[i];  // active (compacted worklist)
+    const GraphOf G(a, u);
     const uint64_t o = a.off[u];
     const uint32_t dg = a.deg[u];
     const uint32_t d = a.vcom[u];
@@ -150,8 +176,8 @@ __device__ __forceinline__ void tile_loop(const MoveArgs &a, const uint32_t *lis
 #pragma unroll
       for (int k = 0; k < U; ++k) {
         const uint32_t j = k * 32 + tl;
-        nv[k] = j < dg ? a.key[o + j] : u;
-        nw[k] = j < dg ? a.w[o + j] : 0.f;
+        nv[k] = j < dg ? __ldcs(a.key + o + j) : u;
+        nw[k] = j < dg ? __ldcs(a.w + o + j) : 0.f;
       }
       for (uint32_t base = 0; base < dg; base += U * 32) {
         uint32_t v[U];
@@ -162,8 +188,8 @@ __device__ __forceinline__ void tile_loop(const MoveArgs &a, const uint32_t *lis
 #pragma unroll
           for (int k = 0; k < U; ++k) {
             const uint32_t j = base + U * 32 + k * 32 + tl;
-            nv[k] = j < dg ? a.key[o + j] : u;
-            nw[k] = j < dg ? a.w[o + j] : 0.f;
+            nv[k] = j < dg ? __ldcs(a.key + o + j) : u;
+            nw[k] = j < dg ? __ldcs(a.w + o + j) : 0.f;
           }
         }
         uint32_t c[U];
@@ -183,8 +209,8 @@ __device__ __forceinline__ void tile_loop(const MoveArgs &a, const uint32_t *lis
 #pragma unroll
       for (int k = 0; k < U; ++k) {
         const uint32_t j = j0 + k * T;
-        v[k] = j < dg ? a.key[o + j] : u;
-        w[k] = j < dg ? a.w[o + j] : 0.f;
+        v[k] = j < dg ? __ldcs(a.key + o + j) : u;
+        w[k] = j < dg ? __ldcs(a.w + o + j) : 0.f;
       }
       uint32_t c[U];
 #pragma unroll
@@ -209,7 +235,7 @@ __device__ __forceinline__ void tile_loop(const MoveArgs &a, const uint32_t *lis
     for (int s = tl; s < C; s += T) {
       const uint32_t c = keys[s];
       if (c == EMPTY) continue;
-      const float g = gain_f32(vals[s], kd, wu, a.ctot[c], td, a.kr);
+      const float g = gain_f32(vals[s], kd, wu, a.ctot[c], td, G.kr);
       if (g > 0.f) take_better(bg, bc, g, c);
     }
 #pragma unroll
@@ -218,9 +244,9 @@ __device__ __forceinline__ void tile_loop(const MoveArgs &a, const uint32_t *lis
       const uint32_t oc = __shfl_xor_sync(m, bc, sh, T);
       take_better(bg, bc, og, oc);
     }
-    const bool moved = bc != EMPTY && bc != 0;
+    const bool moved = bc != EMPTY && bc != G.zero;
     if (tl == 0) {
-      if (bc != EMPTY) fix += gain_to_fix(bg);
+      if (bc != EMPTY) add_gain(a, G, fix, bg);
       if (moved) {
         if (SYNC) {
           a.dec[u] = bc;
@@ -234,7 +260,7 @@ __device__ __forceinline__ void tile_loop(const MoveArgs &a, const uint32_t *lis
     if (moved) {
       uint8_t *mk = SYNC ? a.mark : a.vaff;
       for (uint32_t j = tl; j < dg; j += T) {
-        const uint32_t v = a.key[o + j];
+        const uint32_t v = __ldcs(a.key + o + j);
         if (v != u) mk[v] = 1;
       }
     }
@@ -247,7 +273,7 @@ __device__ __forceinline__ void tile_loop(const MoveArgs &a, const uint32_t *lis
     bad |= !ok;
     __syncwarp(m);
   }
-  flush_counters(a.ctr, bin, fix, nv, ne, nm, bad);
+  flush_counters(a.ctr, bin, fix, nv, ne, nm, bad, no);
 }
 
 template <int T, int C, bool SYNC>
@@ -394,7 +420,9 @@ __device__ __forceinline__ void lt_reset(const ListedTable &t, unsigned n) {
 // independent loads in flight per lane) into a table via add(c, w), called
 // once per distinct key per warp batch. Edges into the own community d are
 // summed in the lane-private return value. Stops (block-uniformly per warp)
-// as soon as an add() fails.
+// as soon as an add() fails. Edge ids and weights are read with the
+// streaming hint (evict first): each is read once per scan, while the
+// membership array that every edge gathers from should stay in L2.
 template <int B, class Add>
 __device__ __forceinline__ float scan_edges(const MoveArgs &a, uint32_t u, uint64_t o, uint32_t n, uint32_t d,
                                             Add add) {
@@ -410,8 +438,8 @@ __device__ __forceinline__ float scan_edges(const MoveArgs &a, uint32_t u, uint6
 #pragma unroll
   for (int k = 0; k < U; ++k) {
     const uint32_t j = base0 + k * B + lane;
-    nv[k] = j < n ? a.key[o + j] : u;
-    nw[k] = j < n ? a.w[o + j] : 0.f;
+    nv[k] = j < n ? __ldcs(a.key + o + j) : u;
+    nw[k] = j < n ? __ldcs(a.w + o + j) : 0.f;
   }
   for (uint32_t base = base0; base < n; base += U * B) {
     uint32_t v[U];
@@ -423,8 +451,8 @@ __device__ __forceinline__ float scan_edges(const MoveArgs &a, uint32_t u, uint6
 #pragma unroll
       for (int k = 0; k < U; ++k) {
         const uint32_t j = next + k * B + lane;
-        nv[k] = j < n ? a.key[o + j] : u;
-        nw[k] = j < n ? a.w[o + j] : 0.f;
+        nv[k] = j < n ? __ldcs(a.key + o + j) : u;
+        nw[k] = j < n ? __ldcs(a.w + o + j) : 0.f;
       }
     }
     uint32_t c[U];
@@ -454,7 +482,6 @@ __global__ void __launch_bounds__(B) move_big_kernel(MoveArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
   __shared__ float red_g[B / 32];
   __shared__ uint32_t red_c[B / 32];
-  __shared__ int s_act;
   __shared__ unsigned s_used;
   __shared__ int s_over;
   constexpr uint32_t CS = 1u << LOGS;
@@ -466,22 +493,20 @@ __global__ void __launch_bounds__(B) move_big_kernel(MoveArgs a) {
   for (uint32_t s2 = threadIdx.x; s2 < CS; s2 += B) { t.keys[s2] = EMPTY; t.vals[s2] = 0.f; }
   uint32_t *gkeys = a.gkeys ? a.gkeys + (size_t(blockIdx.x) << a.glog2) : nullptr;
   float *gvals = a.gvals ? a.gvals + (size_t(blockIdx.x) << a.glog2) : nullptr;
-  unsigned long long fix = 0, nv = 0, ne = 0, nm = 0;
+  unsigned long long fix = 0, nv = 0, ne = 0, nm = 0, no = 0;
   bool bad = false;
   const uint32_t count = a.count_ptr ? *a.count_ptr : a.count;
   __syncthreads();
   for (uint32_t i = blockIdx.x; i < count; i += gridDim.x) {
+    // the worklist holds only active vertices (compact_active_kernel), and
+    // only the vertex itself clears its flag
     const uint32_t u = a.list[i];
+    const GraphOf G(a, u);
     if (threadIdx.x == 0) {
-      s_act = a.vaff[u] && (!a.fa || a.fa[u]);
       s_used = 0;
       s_over = 0;
     }
     __syncthreads();
-    if (!s_act) {
-      __syncthreads();
-      continue;
-    }
     const uint64_t o = a.off[u];
     const uint32_t dg = a.deg[u];
     const uint32_t d = a.vcom[u];
@@ -520,22 +545,22 @@ __global__ void __launch_bounds__(B) move_big_kernel(MoveArgs a) {
         const uint32_t s2 = t.list[j];
         if (s2 == EMPTY) continue;
         const uint32_t c = t.keys[s2];
-        const float g = gain_f32(t.vals[s2], kd, wu, a.ctot[c], td, a.kr);
+        const float g = gain_f32(t.vals[s2], kd, wu, a.ctot[c], td, G.kr);
         if (g > 0.f) take_better(bg, bc, g, c);
       }
     } else {
       for (uint32_t s2 = threadIdx.x; s2 < gcap; s2 += B) {
         const uint32_t c = gkeys[s2];
         if (c == EMPTY) continue;
-        const float g = gain_f32(gvals[s2], kd, wu, a.ctot[c], td, a.kr);
+        const float g = gain_f32(gvals[s2], kd, wu, a.ctot[c], td, G.kr);
         if (g > 0.f) take_better(bg, bc, g, c);
       }
     }
     block_argmax<B>(bg, bc, red_g, red_c);
     if (!over) lt_reset<B>(t, nlist);
-    const bool moved = bc != EMPTY && bc != 0;
+    const bool moved = bc != EMPTY && bc != G.zero;
     if (threadIdx.x == 0) {
-      if (bc != EMPTY) fix += gain_to_fix(bg);
+      if (bc != EMPTY) add_gain(a, G, fix, bg);
       if (moved) {
         if (SYNC) {
           a.dec[u] = bc;
@@ -549,7 +574,7 @@ __global__ void __launch_bounds__(B) move_big_kernel(MoveArgs a) {
     if (moved) {
       uint8_t *mk = SYNC ? a.mark : a.vaff;
       for (uint32_t j = threadIdx.x; j < dg; j += B) {
-        const uint32_t v = a.key[o + j];
+        const uint32_t v = __ldcs(a.key + o + j);
         if (v != u) mk[v] = 1;
       }
     }
@@ -558,11 +583,12 @@ __global__ void __launch_bounds__(B) move_big_kernel(MoveArgs a) {
       ++nv;
       ne += dg;
       nm += moved;
+      no += over;
     }
     bad |= !ok;
     __syncthreads();
   }
-  flush_counters(a.ctr, a.bin, fix, nv, ne, nm, bad);
+  flush_counters(a.ctr, a.bin, fix, nv, ne, nm, bad, no);
 }
 
 // ------------------------------------------------------------ chunked hubs
@@ -588,9 +614,9 @@ __global__ void __launch_bounds__(B) hub_chunk_kernel(MoveArgs a) {
   t.used = &s_used;
   const size_t ci = a.hub.chunk_begin[a.color] + blockIdx.x;
   const uint4 ch = a.hub.chunk[ci];
-  const uint32_t u = a.hub.hub_vertex[ch.x];
+  const uint32_t u = ch.w;  // the hub vertex
   if (threadIdx.x == 0) {
-    s_act = a.vaff[u] && (!a.fa || a.fa[u]);
+    s_act = a.vaff[u] && (!a.fa || a.fa[u]) && (!a.gact || a.gact[a.gid[u]]);
     s_used = 0;
     s_over = 0;
     s_cnt = 0;
@@ -629,9 +655,9 @@ __global__ void __launch_bounds__(B) hub_chunk_kernel(MoveArgs a) {
     // too many distinct communities in this chunk: hand its raw pairs on
     kd = 0.f;
     for (uint32_t j = threadIdx.x; j < n; j += B) {
-      const uint32_t v = a.key[o + j];
+      const uint32_t v = __ldcs(a.key + o + j);
       const uint32_t c = v != u ? a.vcom[v] : EMPTY;
-      const float w = a.w[o + j];
+      const float w = __ldcs(a.w + o + j);
       if (c == d) kd += w;
       if (c != EMPTY && c != d) {
         const uint32_t pos = atomicAdd(&s_cnt, 1u);
@@ -644,6 +670,7 @@ __global__ void __launch_bounds__(B) hub_chunk_kernel(MoveArgs a) {
   if (threadIdx.x == 0) {
     if (kd != 0.f) atomicAdd(&a.hub_kd[u], kd);
     a.chunk_cnt[ci] = s_cnt;
+    if (s_over) atomicAdd(&a.ctr->hub_chunk_over, 1ull);
   }
 }
 
@@ -669,11 +696,12 @@ __global__ void __launch_bounds__(B) hub_merge_kernel(MoveArgs a) {
   uint32_t *gkeys = a.gkeys ? a.gkeys + (size_t(blockIdx.x) << a.glog2) : nullptr;
   float *gvals = a.gvals ? a.gvals + (size_t(blockIdx.x) << a.glog2) : nullptr;
   const size_t h0 = a.hub.hub_begin[a.color], h1 = a.hub.hub_begin[a.color + 1];
-  unsigned long long fix = 0, nv = 0, ne = 0, nm = 0;
+  unsigned long long fix = 0, nv = 0, ne = 0, nm = 0, no = 0;
   bool bad = false;
   __syncthreads();
   for (size_t g = h0 + blockIdx.x; g < h1; g += gridDim.x) {
     const uint32_t u = a.hub.hub_vertex[g];
+    const GraphOf G(a, u);
     const uint32_t c0 = a.hub.hub_first[g], c1 = a.hub.hub_first[g + 1];
     if (threadIdx.x == 0) {
       s_used = 0;
@@ -744,23 +772,23 @@ __global__ void __launch_bounds__(B) hub_merge_kernel(MoveArgs a) {
         const uint32_t s2 = t.list[j];
         if (s2 == EMPTY) continue;
         const uint32_t c = t.keys[s2];
-        const float g2 = gain_f32(t.vals[s2], kd, wu, a.ctot[c], td, a.kr);
+        const float g2 = gain_f32(t.vals[s2], kd, wu, a.ctot[c], td, G.kr);
         if (g2 > 0.f) take_better(bg, bc, g2, c);
       }
     } else {
       for (uint32_t s2 = threadIdx.x; s2 < gcap; s2 += B) {
         const uint32_t c = gkeys[s2];
         if (c == EMPTY) continue;
-        const float g2 = gain_f32(gvals[s2], kd, wu, a.ctot[c], td, a.kr);
+        const float g2 = gain_f32(gvals[s2], kd, wu, a.ctot[c], td, G.kr);
         if (g2 > 0.f) take_better(bg, bc, g2, c);
       }
     }
     block_argmax<B>(bg, bc, red_g, red_c);
     if (!over) lt_reset<B>(t, nlist);
-    const bool moved = bc != EMPTY && bc != 0;
+    const bool moved = bc != EMPTY && bc != G.zero;
     if (threadIdx.x == 0) {
       a.hub_kd[u] = 0.f;
-      if (bc != EMPTY) fix += gain_to_fix(bg);
+      if (bc != EMPTY) add_gain(a, G, fix, bg);
       if (moved) {
         if (SYNC) {
           a.dec[u] = bc;
@@ -775,7 +803,7 @@ __global__ void __launch_bounds__(B) hub_merge_kernel(MoveArgs a) {
       uint8_t *mk = SYNC ? a.mark : a.vaff;
       const uint64_t o = a.off[u];
       for (uint32_t j = threadIdx.x; j < dg; j += B) {
-        const uint32_t v = a.key[o + j];
+        const uint32_t v = __ldcs(a.key + o + j);
         if (v != u) mk[v] = 1;
       }
     }
@@ -784,11 +812,12 @@ __global__ void __launch_bounds__(B) hub_merge_kernel(MoveArgs a) {
       ++nv;
       ne += dg;
       nm += moved;
+      no += over;
     }
     bad |= !ok;
     __syncthreads();
   }
-  flush_counters(a.ctr, a.bin, fix, nv, ne, nm, bad);
+  flush_counters(a.ctr, a.bin, fix, nv, ne, nm, bad, no);
 }
 
 int num_sms() {  // SM count of the device, queried once (thread-safe static init)
@@ -841,7 +870,7 @@ void launch_tile(const MoveArgs &a, cudaStream_t s) {
 // a high-degree vertex's neighbours fall into few communities.
 constexpr int BIG9_B = 256, BIG9_LOGS = 11;     // degree 513-2048
 constexpr int BIG10_B = 256, BIG10_LOGS = 11;   // degree 2049-8192
-constexpr int HUBC_B = 512, HUBC_LOGS = 11;     // hub chunks (HUB_CHUNK edges each)
+constexpr int HUBC_B = 256, HUBC_LOGS = 11;     // hub chunks (HUB_CHUNK edges each)
 constexpr int HUBM_B = 512, HUBM_LOGS = 13;     // hub merge
 
 // Resident blocks of a large-degree kernel on the whole device, queried once.

@@ -105,7 +105,8 @@ class _Stats(C.Structure):
                 ("aggregate_edges", C.c_uint64), ("aggregate_launches", C.c_uint64),
                 ("kernel_launches", C.c_uint64), ("move_bin_ms", C.c_double * 12),
                 ("move_bin_vertices", C.c_uint64 * 12), ("move_bin_edges", C.c_uint64 * 12),
-                ("call_upload_ms", C.c_double), ("call_run_ms", C.c_double), ("call_download_ms", C.c_double)]
+                ("call_upload_ms", C.c_double), ("call_run_ms", C.c_double), ("call_download_ms", C.c_double),
+                ("move_bin_overflow", C.c_uint64 * 12), ("hub_chunk_overflow", C.c_uint64)]
 
 
 class _Csr(C.Structure):
@@ -212,6 +213,9 @@ def load_library() -> C.CDLL:
     L.lvg_server_membership.argtypes = [vp, i32, vp, vp, vp]
     L.lvg_server_destroy.argtypes = [vp]
     L.lvg_static_many.argtypes = [C.POINTER(vp), sz, C.POINTER(_Options), i32, i32, C.POINTER(_Result)]
+    L.lvg_graph_create_union.argtypes = [C.POINTER(vp), sz, C.POINTER(vp)]
+    L.lvg_union_graphs.argtypes = [vp, C.POINTER(sz)]
+    L.lvg_static_union.argtypes = [vp, C.POINTER(_Options), C.POINTER(_Result)]
     _lib = L
     return L
 
@@ -590,6 +594,22 @@ class Graph:
         G = Graph(None)
         _check(self._L.lvg_graph_clone(self.h, C.byref(G.h)))
         return G
+
+    @classmethod
+    def union(cls, graphs: "list[Graph]") -> "Graph":
+        """The graphs' CSRs back to back in one graph in HBM (lvg_graph_create_union),
+        for lvg_static_union; graph i's ids are shifted by the spans before it."""
+        L = load_library()
+        hs = (C.c_void_p * max(len(graphs), 1))(*[g.h for g in graphs])
+        G = Graph(None)
+        _check(L.lvg_graph_create_union(hs, len(graphs), C.byref(G.h)))
+        return G
+
+    @property
+    def union_graphs(self) -> int:
+        n = C.c_size_t()
+        _check(self._L.lvg_union_graphs(self.h, C.byref(n)))
+        return n.value
 
     def close(self) -> None:
         if self.h:
@@ -981,6 +1001,27 @@ class Server:
 
 def graph_footprint(span: int, edges: int) -> int:
     return int(load_library().lvg_graph_footprint(span, edges))
+
+
+def louvain_static_union(u: Graph, o: "LouvainOptions | None" = None) -> "list[LouvainResult]":
+    """Static Louvain on every graph of a union in one run (lvg_static_union):
+    one LouvainResult per graph, as louvain_static gives it for the graph alone."""
+    L = load_library()
+    n = u.union_graphs
+    res = (_Result * max(n, 1))()
+    opt = (o or LouvainOptions())._struct()
+    _check(L.lvg_static_union(u.h, C.byref(opt), res))
+    st = u.stats()
+    out = []
+    for i in range(n):
+        r = res[i]
+        S = r.span
+        m = np.ctypeslib.as_array(r.membership, (S,)).copy() if S else np.zeros(0, np.uint32)
+        vw = np.ctypeslib.as_array(r.vertexWeight, (S,)).copy() if S else np.zeros(0)
+        cw = np.ctypeslib.as_array(r.communityWeight, (S,)).copy() if S else np.zeros(0)
+        L.lvg_result_free(C.byref(r))
+        out.append(LouvainResult(m, vw, cw, **_scalars(r), stats=st))
+    return out
 
 
 def louvain_static_many(graphs: "list[Graph]", o: "LouvainOptions | None" = None, workers: int = 16,
