@@ -14,6 +14,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include <cuda_profiler_api.h>
@@ -1355,6 +1356,62 @@ int fail_noalloc(int code, const char *msg) { return fail(code, msg); }
 
 // ==================================================================== C-ABI
 
+namespace lvg {
+namespace {
+
+// Copy a device array of n elements to per-graph host arrays (graph i gets
+// elements [vb[i], vb[i+1]) into dst(i)) through two pinned staging chunks:
+// each chunk is copied off the device while the previous one is spread into
+// the (pageable) host arrays by a few threads.
+template <class Dst>
+void copy_out_slices(cudaStream_t s, const void *dev, size_t elem, const std::vector<uint64_t> &vb, Dst dst) {
+  const size_t n = vb.back(), G = vb.size() - 1;
+  if (!n) return;
+  const size_t per = std::max<size_t>(1, (size_t(64) << 20) / elem);  // elements per chunk
+  HBuf<uint8_t> stage[2];
+  stage[0].ensure(per * elem);
+  stage[1].ensure(per * elem);
+  cudaEvent_t ev[2];
+  LVG_CUDA(cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming));
+  LVG_CUDA(cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming));
+  const size_t chunks = (n + per - 1) / per;
+  auto issue = [&](size_t k) {
+    const size_t b = k * per, m = std::min(per, n - b);
+    LVG_CUDA(cudaMemcpyAsync(stage[k & 1].p, static_cast<const uint8_t *>(dev) + b * elem, m * elem,
+                             cudaMemcpyDeviceToHost, s));
+    LVG_CUDA(cudaEventRecord(ev[k & 1], s));
+  };
+  const unsigned T = std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
+  size_t g0 = 0;  // first graph that may overlap the current chunk
+  issue(0);
+  for (size_t k = 0; k < chunks; ++k) {
+    if (k + 1 < chunks) issue(k + 1);
+    LVG_CUDA(cudaEventSynchronize(ev[k & 1]));
+    const size_t b = k * per, e = std::min(n, b + per);
+    while (g0 < G && vb[g0 + 1] <= b) ++g0;
+    auto spread = [&](size_t lo, size_t hi) {  // element range [lo, hi) of the chunk
+      size_t g = std::upper_bound(vb.begin(), vb.end(), lo) - vb.begin() - 1;
+      for (; g < G && vb[g] < hi; ++g) {
+        const size_t x0 = std::max<size_t>(lo, vb[g]), x1 = std::min<size_t>(hi, vb[g + 1]);
+        if (x1 > x0)
+          std::memcpy(static_cast<uint8_t *>(dst(g)) + (x0 - vb[g]) * elem, stage[k & 1].p + (x0 - b) * elem,
+                      (x1 - x0) * elem);
+      }
+    };
+    std::vector<std::thread> th;
+    const size_t step = (e - b + T - 1) / T;
+    for (unsigned t = 1; t < T && b + t * step < e; ++t)
+      th.emplace_back(spread, b + t * step, std::min(e, b + (t + 1) * step));
+    spread(b, std::min(e, b + step));
+    for (auto &x : th) x.join();
+  }
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+}
+
+}  // namespace
+}  // namespace lvg
+
 extern "C" {
 
 const char *lvg_last_error(void) { return lvg::g_err.c_str(); }
@@ -1702,16 +1759,18 @@ int lvg_static_union(lvg_graph *u, const lvg_options *o, lvg_result *results) {
     launch_f32_to_f64(U.ct.p, W.stage_b.p, S, s);
     for (size_t i = 0; i < U.n; ++i) {
       lvg_result *r = &results[i];
-      const size_t b = U.vb[i], sp = U.vb[i + 1] - U.vb[i];
+      const size_t sp = U.vb[i + 1] - U.vb[i];
       if (!r->membership) { r->membership = (uint32_t *)std::malloc(sp * 4 + 1); r->owned |= 1; }
       if (!r->vertexWeight) { r->vertexWeight = (double *)std::malloc(sp * 8 + 1); r->owned |= 2; }
       if (!r->communityWeight) { r->communityWeight = (double *)std::malloc(sp * 8 + 1); r->owned |= 4; }
       if (!r->membership || !r->vertexWeight || !r->communityWeight) throw std::bad_alloc();
-      if (sp) {
-        LVG_CUDA(cudaMemcpyAsync(r->membership, U.q.p + b, sp * 4, cudaMemcpyDeviceToHost, s));
-        LVG_CUDA(cudaMemcpyAsync(r->vertexWeight, W.stage_a.p + b, sp * 8, cudaMemcpyDeviceToHost, s));
-        LVG_CUDA(cudaMemcpyAsync(r->communityWeight, W.stage_b.p + b, sp * 8, cudaMemcpyDeviceToHost, s));
-      }
+    }
+    copy_out_slices(s, U.q.p, 4, U.vb, [&](size_t i) -> void * { return results[i].membership; });
+    copy_out_slices(s, W.stage_a.p, 8, U.vb, [&](size_t i) -> void * { return results[i].vertexWeight; });
+    copy_out_slices(s, W.stage_b.p, 8, U.vb, [&](size_t i) -> void * { return results[i].communityWeight; });
+    for (size_t i = 0; i < U.n; ++i) {
+      lvg_result *r = &results[i];
+      const size_t sp = U.vb[i + 1] - U.vb[i];
       const GraphCtl &c = U.hctl.p[i];
       RunInfo ri = info;
       ri.iterations = int(c.l);
