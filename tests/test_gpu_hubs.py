@@ -57,3 +57,16 @@ def test_async_on_hubs_quality_and_totals(cuda, orc, hubgraph):
     # the vertex weights are the weighted degrees (louvainVertexWeightsOmpW)
     deg_w = np.add.reduceat(x.weights.astype(np.float64), x.offsets[:-1].astype(np.int64)) * (np.diff(x.offsets) > 0)
     assert np.array_equal(r0.vertexWeight, deg_w)
+
+
+def test_half_integer_weights_match_cpu_replay(cuda, orc, hubgraph):
+    # Non-integer weights whose FP32 sums stay exact (multiples of 1/2 below
+    # 2^23): the deterministic replay still matches bit for bit, hubs included.
+    x, _, _ = hubgraph
+    xh = type(x)(x.offsets, x.keys, (x.weights * 0.5).astype(np.float32), x.exists)
+    o = cuda.LouvainOptions(deterministic=True, colors=16)
+    r = cuda.louvain_static(cuda.Graph(xh), o)
+    m, vt, ct, info = orc.louvain(xh, 0, threads=8, sync=True, colors=16)
+    assert np.array_equal(r.membership, m)
+    assert np.array_equal(r.communityWeight, ct)
+    assert (r.iterations, r.passes) == (info["iterations"], info["passes"])
