@@ -58,6 +58,8 @@ def parse():
     p.add_argument("--batch-fraction", type=float, default=1e-4)
     p.add_argument("--seed", type=int, default=42)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-tune", action="store_true",
+                   help="skip lvg_autotune (launch shapes and frontier colour classes) before the timed steps")
     p.add_argument("--cpu-steps", type=int, default=2)
     p.add_argument("--workload", default="df", choices=["df", "serving", "temporal", "batched"],
                    help="df: the headline (R-MAT scale 24, one graph); serving: many resident graphs under "
@@ -293,6 +295,14 @@ def run_gpu(args):
     st_prior.set(prior.membership, prior.vertexWeight, prior.communityWeight)
     db = lvg.DeviceBatch(Y, b)
     o = lvg.LouvainOptions()
+    # the library's autotuner picks the launch shapes (and the frontier colour
+    # classes, within 1e-3 modularity) on this workload, untimed
+    tuning = lvg.get_tuning(Y)
+    tune_s = 0.0
+    if not args.no_tune:
+        t0 = time.perf_counter()
+        tuning, _ = lvg.autotune(Y, lvg.METHOD_FRONTIER, db, st_prior, o, repeats=3)
+        tune_s = time.perf_counter() - t0
 
     if args.ncu_steps:
         lvg.run_resident(Y, lvg.METHOD_FRONTIER, db, st_prior, st_out, o)  # warm: graph capture
@@ -388,6 +398,7 @@ def run_gpu(args):
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms_max,
                 "call": "lvg_frontier (drop-in for louvainDynamicFrontierOmp), pinned host arrays",
                 "last_call_parts": e2e_parts},
+        "tuning": dict(tuning, by="lvg_autotune" if not args.no_tune else "defaults", seconds=round(tune_s, 2)),
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
@@ -667,6 +678,13 @@ def run_batched(args):
     small = lvg.Graph.union(graphs[:8])
     lvg.louvain_static_union(small, o)  # warm-up (kernel attributes, first launches)
     small.close()
+    # launch shapes from the autotuner, tuned on a union of the first 64 graphs
+    t0 = time.perf_counter()
+    sample_u = lvg.Graph.union(graphs[:64])
+    tuning, _ = lvg.autotune(sample_u, lvg.METHOD_STATIC, o=o, repeats=1)
+    sample_u.close()
+    lvg.set_tuning(U, **tuning)
+    tune_s = time.perf_counter() - t0
     with Clocks(local) as clk:
         t0 = time.perf_counter()
         ures = lvg.louvain_static_union(U, o)
@@ -682,6 +700,7 @@ def run_batched(args):
                        "graphs": n, "vertices": int(sizes.sum()), "edges": E, "generate_s": tgen,
                        "union_build_s": union_build_s},
             "graphs_per_s": n / union_s,
+            "tuning": dict(tuning, by="lvg_autotune on a union of 64 of the graphs", seconds=round(tune_s, 2)),
             "union": {"wall_s": union_s, "device_run_ms": run_ms,
                       "download_ms": U.stats()["call_download_ms"],
                       "iterations_max": int(max(r.iterations for r in ures)),

@@ -391,6 +391,34 @@ typedef struct lvg_stats {
 } lvg_stats;
 /* Enable (1) or disable (0) per-launch event timing for calls on g. */
 int lvg_set_profiling(lvg_graph *g, int enable);
+
+/* ---- Tuning (no reference counterpart). Launch-shape choices of a graph's
+ * local-moving launches that leave Louvain's arithmetic unchanged, except
+ * frontier_colors (the colour classes of the frontier methods in
+ * asynchronous mode, whose choice lvg_autotune guards by modularity). */
+typedef struct lvg_tuning {
+  int      frontier_colors;    /* colour classes of DF and DS when lvg_options.colors == 0
+                                  and deterministic == 0 (default 8) */
+  int      concurrent_bins;    /* 1: a class's degree bins run concurrently on side streams (default 1) */
+  int      fused_small;        /* 1: the frontier methods' first pass runs bins 1-8 as two launches
+                                  per class (default 1) */
+  uint32_t hub_chunk;          /* edges per chunk of a vertex above degree 8192 (256..1<<20; default 4096) */
+  int      big_blocks_per_sm;  /* resident blocks per SM of the degree 513-8192 kernels (0 = as many
+                                  as fit; default 0) */
+} lvg_tuning;
+void lvg_tuning_default(lvg_tuning *t);
+int lvg_graph_get_tuning(const lvg_graph *g, lvg_tuning *t);
+int lvg_graph_set_tuning(lvg_graph *g, const lvg_tuning *t);
+/* The autotuner: coordinate descent over the knobs of lvg_tuning on this
+ * graph and workload (method, batch and prior as lvg_run_resident takes
+ * them; a graph union takes LVG_METHOD_STATIC and runs lvg_static_union).
+ * Each candidate is run once to warm up and then `repeats` times; the
+ * fastest (minimum of LouvainResult::time) is kept when it beats the current
+ * choice by 2 %, and a frontier_colors candidate only when its modularity is
+ * within 1e-3 of the default's. The result is set on the graph and returned
+ * in *best (time in *best_ms). */
+int lvg_autotune(lvg_graph *g, int method, const lvg_device_batch *b, const lvg_state *prior, const lvg_options *o,
+                 int repeats, lvg_tuning *best, double *best_ms);
 int lvg_get_stats(const lvg_graph *g, lvg_stats *out);
 
 /* ---- Modularity without device allocation. No counterpart in the reference.

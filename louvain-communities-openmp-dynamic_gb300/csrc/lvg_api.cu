@@ -161,6 +161,16 @@ struct UnionCall {
   int L;
 };
 
+inline lvg_tuning default_tuning() {
+  lvg_tuning t;
+  t.frontier_colors = DEFAULT_COLORS_ASYNC;
+  t.concurrent_bins = 1;
+  t.fused_small = 1;
+  t.hub_chunk = HUB_CHUNK;
+  t.big_blocks_per_sm = 0;
+  return t;
+}
+
 struct RunInfo {
   int iterations = 0, passes = 0;
   float t = 0, tm = 0, ti = 0, tp = 0, tl = 0, ta = 0;
@@ -228,6 +238,7 @@ struct lvg_graph {
   DBuf<uint32_t> b_ds, b_dd, b_is, b_id, b_seg;
   DBuf<float> b_dw, b_iw;
   std::unique_ptr<UnionInfo> uni;  // set for graph unions
+  lvg_tuning tuning = default_tuning();
 };
 
 // A state or a device batch may outlive its graph (it keeps its own device
@@ -334,8 +345,9 @@ void build_hub_plan(lvg_graph *g, Level &lv, HubPlanBuffers &hb) {
     P.chunk_begin[k] = chunks.size();
     for (size_t h = P.hub_begin[k]; h < P.hub_begin[k + 1]; ++h) {
       first[h] = uint32_t(chunks.size());
-      for (uint32_t lo = 0; lo < degs[h]; lo += HUB_CHUNK) {
-        chunks.push_back(make_uint4(uint32_t(h), lo, std::min<uint32_t>(degs[h], lo + HUB_CHUNK), verts[h]));
+      const uint32_t step = g->tuning.hub_chunk;
+      for (uint32_t lo = 0; lo < degs[h]; lo += step) {
+        chunks.push_back(make_uint4(uint32_t(h), lo, std::min<uint32_t>(degs[h], lo + step), verts[h]));
         parts.push_back(part + lo);
       }
       part += degs[h];
@@ -358,8 +370,15 @@ void build_hub_plan(lvg_graph *g, Level &lv, HubPlanBuffers &hb) {
   P.chunk_part = hb.chunk_part.p;
 }
 
-int colors_for(const lvg_options &o) {
-  int k = o.colors > 0 ? o.colors : (o.deterministic ? DEFAULT_COLORS_SYNC : DEFAULT_COLORS_ASYNC);
+// Colour classes of a run: the options' count, else 16 (deterministic), else
+// the graph's tuned count for the frontier methods, else 8.
+int colors_for(const lvg_options &o, int method, const lvg_tuning &t) {
+  int k = o.colors;
+  if (k <= 0) {
+    if (o.deterministic) k = DEFAULT_COLORS_SYNC;
+    else if (method == LVG_METHOD_FRONTIER || method == LVG_METHOD_DELTA) k = t.frontier_colors;
+    else k = DEFAULT_COLORS_ASYNC;
+  }
   return k < 1 ? 1 : (k > MAX_COLORS ? MAX_COLORS : k);
 }
 
@@ -404,7 +423,7 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot
   // the reference's threads do, and in deterministic mode nothing they read
   // changes before the class's moves are applied), so they run concurrently.
   // Per-bin profiling keeps them on one stream to time each launch.
-  const bool conc = bin_ev == nullptr;
+  const bool conc = bin_ev == nullptr && g->tuning.concurrent_bins;
   if (conc) ensure_aux(g);
   auto stream_of = [&](int b) { const int i = bin_stream(b); return conc && i >= 0 ? g->aux[i] : s; };
   LVG_CUDA(cudaMemsetAsync(&g->ctr.p->el_fix, 0, sizeof(unsigned long long), s));
@@ -464,6 +483,7 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot
       a.gkeys = need ? W.gkeys.p + goff[b] : nullptr;
       a.gvals = need ? W.gvals.p + goff[b] : nullptr;
       a.glog2 = glog2[b];
+      a.big_cap = g->tuning.big_blocks_per_sm;
       set_union(a);
       cudaEvent_t b0 = bin_ev ? g->events.record(s) : nullptr;
       if (b == NUM_BINS - 1) {
@@ -565,7 +585,7 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const 
     if (!most) continue;
     glog2[b] = global_table_log2(lv.bin_maxdeg[b]);
     goff[b] = need;  // each bin its own regions: the bins' kernels run concurrently
-    need += size_t(move_grid_blocks(b, sync, most)) << glog2[b];
+    need += size_t(move_grid_blocks(b, sync, most, g->tuning.big_blocks_per_sm)) << glog2[b];
   }
   if (need) {
     W.gkeys.ensure(need);
@@ -714,7 +734,7 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
   const int L = o.maxIterations, P = o.maxPasses;
   const bool sync = o.deterministic != 0;
   const int rep = std::max(1, o.repeat);
-  const int K = colors_for(o);
+  const int K = colors_for(o, method, g->tuning);
   if (g->base.colors != K) {
     compute_bins(g, g->base, g->deg.p, g->bins.p, W.binscratch.p, K);
     build_hub_plan(g, g->base, g->hubplan);
@@ -777,7 +797,8 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
       cudaEvent_t a0 = g->events.record(s);
       // the frontier methods' first pass works on short per-class worklists:
       // the small degree bins go in two fused launches per class
-      const bool fused = first && (method == LVG_METHOD_FRONTIER || method == LVG_METHOD_DELTA);
+      const bool fused =
+          first && (method == LVG_METHOD_FRONTIER || method == LVG_METHOD_DELTA) && g->tuning.fused_small;
       const int m = move_phase(g, lv, com, ctot, tot, first ? fa : nullptr, M, kr, L, E, sync, fused);
       tl_ev.push_back({a0, g->events.record(s)});
       l += std::max(m, 1);
@@ -849,7 +870,7 @@ void run_union(lvg_graph *g, const lvg_options &o, RunInfo &info) {
   const int L = o.maxIterations, P = o.maxPasses;
   const bool sync = o.deterministic != 0;
   const int rep = std::max(1, o.repeat);
-  const int K = colors_for(o);
+  const int K = colors_for(o, LVG_METHOD_STATIC, g->tuning);
   if (g->base.colors != K) {
     compute_bins(g, g->base, g->deg.p, g->bins.p, W.binscratch.p, K);
     build_hub_plan(g, g->base, g->hubplan);
@@ -1412,6 +1433,44 @@ void copy_out_slices(cudaStream_t s, const void *dev, size_t elem, const std::ve
 }  // namespace
 }  // namespace lvg
 
+namespace lvg {
+namespace {
+
+void check_tuning(const lvg_tuning &t) {
+  if (t.frontier_colors < 1 || t.frontier_colors > MAX_COLORS)
+    throw Error(LVG_EINVAL, "tuning: frontier_colors out of 1..32");
+  if (t.hub_chunk < 256 || t.hub_chunk > (1u << 20)) throw Error(LVG_EINVAL, "tuning: hub_chunk out of 256..2^20");
+  if (t.big_blocks_per_sm < 0 || t.big_blocks_per_sm > 64) throw Error(LVG_EINVAL, "tuning: big_blocks_per_sm");
+}
+
+// Set a graph's tuning: the hub plan of the uploaded level follows the chunk
+// size, and a captured iteration (launch shapes baked in) is dropped.
+void apply_tuning(lvg_graph *g, const lvg_tuning &t) {
+  check_tuning(t);
+  const bool chunks = t.hub_chunk != g->tuning.hub_chunk;
+  g->tuning = t;
+  if (chunks) build_hub_plan(g, g->base, g->hubplan);
+  if (g->iter_exec) {
+    cudaGraphExecDestroy(g->iter_exec);
+    g->iter_exec = nullptr;
+  }
+}
+
+// Modularity of a membership already in HBM (the uploaded level's graph).
+double modularity_device(lvg_graph *g, const uint32_t *dq, double M, double R) {
+  Workspace &W = *g->ws;
+  cudaStream_t s = g->stream;
+  W.ctot64.ensure(g->base.span);
+  launch_modularity(g->base, dq, W.ctot64.p, g->ctr.p, s);
+  launch_sq_sum(W.ctot64.p, g->base.span, g->ctr.p, s);
+  read_counters(g);
+  const double intra = g->hctr.p->fp64[1], sq = g->hctr.p->fp64[2];
+  return intra / (2 * M) - R * sq / (4 * M * M);
+}
+
+}  // namespace
+}  // namespace lvg
+
 extern "C" {
 
 const char *lvg_last_error(void) { return lvg::g_err.c_str(); }
@@ -1622,6 +1681,7 @@ int lvg_graph_clone(lvg_graph *x, lvg_graph **out) {
     g->pool_cursor = x->pool_cursor;
     g->rows_sorted = x->rows_sorted;
     g->total_weight = x->total_weight;
+    g->tuning = x->tuning;
     g->ctr.ensure(1);
     g->hctr.ensure(1);
     LVG_CUDA(cudaMemsetAsync(g->ctr.p, 0, sizeof(Counters), s));
@@ -2281,6 +2341,97 @@ int lvg_device_batch_destroy(lvg_device_batch *b) {
   cudaSetDevice(b->device);
   delete b;  // cudaFree waits for the work that uses the buffers
   return LVG_OK;
+}
+
+void lvg_tuning_default(lvg_tuning *t) {
+  if (t) *t = lvg::default_tuning();
+}
+
+int lvg_graph_get_tuning(const lvg_graph *g, lvg_tuning *t) {
+  if (!g || !t) return lvg::fail(LVG_EINVAL, "null argument");
+  *t = g->tuning;
+  return LVG_OK;
+}
+
+int lvg_graph_set_tuning(lvg_graph *g, const lvg_tuning *t) {
+  lvg::AcctScope acct_(g ? &g->bytes : nullptr);
+  if (!g || !t) return lvg::fail(LVG_EINVAL, "null argument");
+  return lvg::guarded([&] {
+    LVG_CUDA(cudaSetDevice(g->device));
+    LVG_CUDA(cudaStreamSynchronize(g->stream));
+    lvg::apply_tuning(g, *t);
+    return LVG_OK;
+  });
+}
+
+int lvg_autotune(lvg_graph *g, int method, const lvg_device_batch *b, const lvg_state *prior, const lvg_options *o,
+                 int repeats, lvg_tuning *best, double *best_ms) {
+  lvg::AcctScope acct_(g ? &g->bytes : nullptr);
+  if (!g || method < 0 || method > 3 || repeats < 1) return lvg::fail(LVG_EINVAL, "bad argument");
+  if (g->uni && method != LVG_METHOD_STATIC) return lvg::fail(LVG_EINVAL, "a graph union runs static Louvain only");
+  if (!g->uni && method != LVG_METHOD_STATIC && !prior)
+    return lvg::fail(LVG_EINVAL, "dynamic methods need a prior state");
+  if ((b && b->g != g) || (prior && prior->g != g)) return lvg::fail(LVG_EINVAL, "state/batch belongs to another graph");
+  return lvg::guarded([&] {
+    using namespace lvg;
+    LVG_CUDA(cudaSetDevice(g->device));
+    lvg_options opt;
+    if (o) opt = *o; else lvg_options_default(&opt);
+    opt.repeat = 1;
+    ensure_ws(g);
+    Workspace &W = *g->ws;
+    DBatch db;
+    if (b && method != LVG_METHOD_STATIC) db = b->b;
+    StateRef pr{nullptr, nullptr, nullptr};
+    if (prior) pr = StateRef{prior->q.p, prior->vt.p, prior->ct.p};
+    StateRef st{W.ucom.p, W.utot.p, W.ctot.p};
+    const bool profiling = g->profiling;
+    g->profiling = false;
+    auto once = [&] {
+      RunInfo ri;
+      if (g->uni) run_union(g, opt, ri);
+      else run(g, method, db, pr, st, opt, ri);
+      return double(ri.t);
+    };
+    // time of a candidate (min over the repeats, after one warm-up run); q:
+    // the modularity of its last run, when asked (frontier colour classes)
+    auto measure = [&](const lvg_tuning &t, double *q) {
+      apply_tuning(g, t);
+      once();
+      double tm = 1e300;
+      for (int r = 0; r < repeats; ++r) tm = std::min(tm, once());
+      if (q) *q = modularity_device(g, st.q, g->total_weight / 2, opt.resolution);
+      return tm;
+    };
+    const bool colours = !g->uni && !opt.deterministic && opt.colors <= 0 &&
+                         (method == LVG_METHOD_FRONTIER || method == LVG_METHOD_DELTA);
+    lvg_tuning cur = g->tuning;
+    double qref = 0;
+    double tcur = measure(cur, colours ? &qref : nullptr);
+    auto try_knob = [&](auto set, std::initializer_list<long> values, bool guard) {
+      for (long v : values) {
+        lvg_tuning t = cur;
+        set(t, v);
+        if (!std::memcmp(&t, &cur, sizeof(t))) continue;
+        double q = 0;
+        const double tm = measure(t, guard ? &q : nullptr);
+        if (tm < 0.98 * tcur && (!guard || q >= qref - 1e-3)) {
+          cur = t;
+          tcur = tm;
+        }
+      }
+    };
+    try_knob([](lvg_tuning &t, long v) { t.hub_chunk = uint32_t(v); }, {2048, 4096, 8192, 16384}, false);
+    try_knob([](lvg_tuning &t, long v) { t.concurrent_bins = int(v); }, {1, 0}, false);
+    try_knob([](lvg_tuning &t, long v) { t.fused_small = int(v); }, {1, 0}, false);
+    try_knob([](lvg_tuning &t, long v) { t.big_blocks_per_sm = int(v); }, {0, 2, 3, 4}, false);
+    if (colours) try_knob([](lvg_tuning &t, long v) { t.frontier_colors = int(v); }, {8, 4, 2}, true);
+    apply_tuning(g, cur);
+    g->profiling = profiling;
+    if (best) *best = cur;
+    if (best_ms) *best_ms = tcur;
+    return LVG_OK;
+  });
 }
 
 int lvg_run_resident(lvg_graph *g, int method, const lvg_device_batch *b, const lvg_state *prior, lvg_state *out,

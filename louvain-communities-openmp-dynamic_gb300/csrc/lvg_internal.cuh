@@ -189,6 +189,8 @@ struct MoveArgs {
   const uint32_t *gzero = nullptr;
   unsigned long long *gfix = nullptr;
   const uint8_t *gact = nullptr;
+  // resident blocks per SM of the degree 513-8192 kernels (0 = as many as fit)
+  int big_cap = 0;
 };
 
 // Arguments of the aggregation kernels (inc/louvain.hxx:897-912, 987-992).
@@ -409,7 +411,7 @@ void launch_move_small(int lo, int hi, bool sync, const MoveArgs &a, const Small
 int device_sms();
 // Grid of the local-moving kernel of a large-degree bin (9, 10; 11 = the hub
 // merge) for `count` vertices: the size of its per-block global fallback.
-int move_grid_blocks(int bin, bool sync, size_t count);
+int move_grid_blocks(int bin, bool sync, size_t count, int big_cap = 0);
 
 
 // ---------------------------------------------------------------- graph unions (lvg_union.cu)

@@ -882,19 +882,21 @@ unsigned resident_blocks(K kernel, int block, size_t smem) {
 }
 
 template <int B, int LOGS, bool SYNC>
-unsigned big_grid(size_t count) {
+unsigned big_grid(size_t count, int cap_per_sm) {
   const size_t smem = (size_t(1) << LOGS) * 10;  // keys, values, claimed list
   static const unsigned resident = [&] {
     set_smem(move_big_kernel<B, LOGS, SYNC>, smem);
     return resident_blocks(move_big_kernel<B, LOGS, SYNC>, B, smem);
   }();
-  return unsigned(std::min<size_t>(count, resident));
+  size_t r = resident;
+  if (cap_per_sm > 0) r = std::min(r, size_t(cap_per_sm) * size_t(num_sms()));
+  return unsigned(std::min<size_t>(count, r));
 }
 
 template <int B, int LOGS, bool SYNC>
 void launch_big(const MoveArgs &a, cudaStream_t s) {
   const size_t smem = (size_t(1) << LOGS) * 10;
-  const unsigned grid = big_grid<B, LOGS, SYNC>(a.count);
+  const unsigned grid = big_grid<B, LOGS, SYNC>(a.count, a.big_cap);
   if (!grid) return;
   move_big_kernel<B, LOGS, SYNC><<<grid, B, smem, s>>>(a);
   LVG_CHECK_LAUNCH();
@@ -935,10 +937,13 @@ void launch_bin(int b, const MoveArgs &a, cudaStream_t s) {
 
 }  // namespace
 
-int move_grid_blocks(int bin, bool sync, size_t count) {
-  if (bin == 9) return int(sync ? big_grid<BIG9_B, BIG9_LOGS, true>(count) : big_grid<BIG9_B, BIG9_LOGS, false>(count));
+int move_grid_blocks(int bin, bool sync, size_t count, int big_cap) {
+  if (bin == 9)
+    return int(sync ? big_grid<BIG9_B, BIG9_LOGS, true>(count, big_cap)
+                    : big_grid<BIG9_B, BIG9_LOGS, false>(count, big_cap));
   if (bin == 10)
-    return int(sync ? big_grid<BIG10_B, BIG10_LOGS, true>(count) : big_grid<BIG10_B, BIG10_LOGS, false>(count));
+    return int(sync ? big_grid<BIG10_B, BIG10_LOGS, true>(count, big_cap)
+                    : big_grid<BIG10_B, BIG10_LOGS, false>(count, big_cap));
   return global_table_blocks(count);  // the hub merge
 }
 

@@ -99,6 +99,14 @@ class _ServerStats(C.Structure):
                 ("mean_apply_ms", C.c_double), ("mean_run_ms", C.c_double)]
 
 
+class _Tuning(C.Structure):
+    _fields_ = [("frontier_colors", C.c_int), ("concurrent_bins", C.c_int), ("fused_small", C.c_int),
+                ("hub_chunk", C.c_uint32), ("big_blocks_per_sm", C.c_int)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class _Stats(C.Structure):
     _fields_ = [("move_kernel_ms", C.c_double), ("move_launches", C.c_uint64), ("move_vertices", C.c_uint64),
                 ("move_edges", C.c_uint64), ("moves", C.c_uint64), ("aggregate_kernel_ms", C.c_double),
@@ -169,6 +177,12 @@ def load_library() -> C.CDLL:
     L.lvg_host_alloc.restype = vp
     L.lvg_host_free.argtypes = [vp]
     L.lvg_set_profiling.argtypes = [vp, i32]
+    L.lvg_tuning_default.argtypes = [C.POINTER(_Tuning)]
+    L.lvg_tuning_default.restype = None
+    L.lvg_graph_get_tuning.argtypes = [vp, C.POINTER(_Tuning)]
+    L.lvg_graph_set_tuning.argtypes = [vp, C.POINTER(_Tuning)]
+    L.lvg_autotune.argtypes = [vp, i32, vp, vp, C.POINTER(_Options), i32, C.POINTER(_Tuning),
+                               C.POINTER(C.c_double)]
     L.lvg_set_device.argtypes = [i32]
     L.lvg_modularity_noalloc.argtypes = [sz, vp, vp, vp, vp, vp, f64, f64, vp, vp]
     L.lvg_get_stats.argtypes = [vp, C.POINTER(_Stats)]
@@ -880,6 +894,42 @@ def run_resident(g: Graph, method: int, batch: DeviceBatch | None, prior: State 
     _check(L.lvg_run_resident(g.h, method, batch.h if batch else None, prior.h if prior else None, out.h,
                               C.byref(opt), C.byref(r)))
     return _scalars(r)
+
+
+def tuning_default() -> dict:
+    t = _Tuning()
+    load_library().lvg_tuning_default(C.byref(t))
+    return t.as_dict()
+
+
+def get_tuning(g: Graph) -> dict:
+    t = _Tuning()
+    _check(load_library().lvg_graph_get_tuning(g.h, C.byref(t)))
+    return t.as_dict()
+
+
+def set_tuning(g: Graph, **knobs) -> dict:
+    """Change some knobs of a graph's tuning (lvg_graph_set_tuning); returns the new tuning."""
+    L = load_library()
+    t = _Tuning()
+    _check(L.lvg_graph_get_tuning(g.h, C.byref(t)))
+    for k, v in knobs.items():
+        setattr(t, k, v)
+    _check(L.lvg_graph_set_tuning(g.h, C.byref(t)))
+    return t.as_dict()
+
+
+def autotune(g: Graph, method: int, batch: "DeviceBatch | None" = None, prior: "State | None" = None,
+             o: "LouvainOptions | None" = None, repeats: int = 3) -> "tuple[dict, float]":
+    """lvg_autotune: the fastest launch-shape choices for this graph and workload, set on
+    the graph; returns (tuning, ms)."""
+    L = load_library()
+    t = _Tuning()
+    ms = C.c_double()
+    opt = (o or LouvainOptions())._struct()
+    _check(L.lvg_autotune(g.h, method, batch.h if batch else None, prior.h if prior else None, C.byref(opt),
+                          repeats, C.byref(t), C.byref(ms)))
+    return t.as_dict(), ms.value
 
 
 def profiler_start() -> None:
