@@ -562,18 +562,26 @@ void capture_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot
 // iteration is captured once into a CUDA graph and replayed, one graph
 // launch per iteration instead of ~12 launches per colour class.
 int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const float *tot, const uint8_t *fa,
-               double M, float kr, int L, double E, bool sync, bool fused, const UnionCall *uc = nullptr) {
+               double M, float kr, int L, double E, bool sync, bool fused, const UnionCall *uc = nullptr,
+               const DBatch *endpoints = nullptr) {
   Workspace &W = *g->ws;
   cudaStream_t s = g->stream;
   const int K = lv.colors;
-  // Existing degree-0 vertices are processed once and never re-marked.
-  IsolatedLists iso{};
-  iso.k = K;
-  for (int k = 0; k < K; ++k) {
-    iso.list[k] = lv.bins + lv.bucket_begin(k, 0);
-    iso.n[k] = lv.bucket_size(k, 0);
+  // Existing degree-0 vertices are processed once and never re-marked. In
+  // the dynamic-frontier first pass only batch endpoints can be such
+  // vertices with their flag set (`endpoints`).
+  if (endpoints) {
+    launch_clear_isolated_endpoints(endpoints->ds, endpoints->nd, endpoints->is, endpoints->ni, lv.deg, lv.ex,
+                                    W.vaff.p, s);
+  } else {
+    IsolatedLists iso{};
+    iso.k = K;
+    for (int k = 0; k < K; ++k) {
+      iso.list[k] = lv.bins + lv.bucket_begin(k, 0);
+      iso.n[k] = lv.bucket_size(k, 0);
+    }
+    launch_clear_isolated_multi(iso, W.vaff.p, fa, s);
   }
-  launch_clear_isolated_multi(iso, W.vaff.p, fa, s);
   // Global fallback regions of the large-degree bins (9-11): each launch's
   // blocks get 2^glog2[b] slots, enough for the bin's largest degree.
   int glog2[NUM_BINS] = {};
@@ -799,7 +807,8 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
       // the small degree bins go in two fused launches per class
       const bool fused =
           first && (method == LVG_METHOD_FRONTIER || method == LVG_METHOD_DELTA) && g->tuning.fused_small;
-      const int m = move_phase(g, lv, com, ctot, tot, first ? fa : nullptr, M, kr, L, E, sync, fused);
+      const int m = move_phase(g, lv, com, ctot, tot, first ? fa : nullptr, M, kr, L, E, sync, fused, nullptr,
+                               first && method == LVG_METHOD_FRONTIER ? &b : nullptr);
       tl_ev.push_back({a0, g->events.record(s)});
       l += std::max(m, 1);
       ++p;

@@ -264,6 +264,9 @@ struct IsolatedLists {
   int k;
 };
 void launch_clear_isolated_multi(const IsolatedLists &L, uint8_t *vaff, const uint8_t *fa, cudaStream_t s);
+// vaff[u] = 0 for the endpoints u (a, b) of degree 0 that exist.
+void launch_clear_isolated_endpoints(const uint32_t *a, size_t na, const uint32_t *b, size_t nb,
+                                     const uint32_t *deg, const uint8_t *ex, uint8_t *vaff, cudaStream_t s);
 void launch_merge_marks(uint8_t *vaff, uint8_t *mark, size_t n, cudaStream_t s);
 // Worklists of one colour class: the active vertices of degree bins
 // 1..NUM_BINS-2 (positions bins[start[1] .. start[NUM_BINS-1])) are copied to

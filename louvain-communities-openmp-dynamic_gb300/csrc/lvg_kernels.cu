@@ -274,6 +274,17 @@ __global__ void clear_isolated_multi_kernel(IsolatedLists L, uint8_t *vaff, cons
   }
 }
 
+// The dynamic-frontier first pass: its only affected vertices of degree 0
+// are batch endpoints (the marking touches nothing else, and moves mark
+// neighbours only), so the clearing of isolated vertices needs only those.
+__global__ void clear_isolated_endpoints_kernel(const uint32_t *a, size_t na, const uint32_t *b, size_t nb,
+                                                const uint32_t *deg, const uint8_t *ex, uint8_t *vaff) {
+  GRID_STRIDE(i, na + nb) {
+    const uint32_t u = i < na ? a[i] : b[i - na];
+    if (deg[u] == 0 && (!ex || ex[u])) vaff[u] = 0;
+  }
+}
+
 __global__ void merge_marks_kernel(uint8_t *vaff, uint8_t *mark, size_t n) {
   GRID_STRIDE(i, n) {
     if (mark[i]) { vaff[i] = 1; mark[i] = 0; }
@@ -405,9 +416,18 @@ __global__ void check_ids_kernel(const uint32_t *a, size_t n, uint32_t limit, un
   if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(err, ERR_BAD_ID);
 }
 
+// Flags equal to 1, sixteen bytes per load (bytewise compares); the tail
+// past the last whole 16-byte word bytewise.
 __global__ void count_flags_kernel(const uint8_t *f, size_t n, unsigned long long *dst) {
   unsigned long long c = 0;
-  GRID_STRIDE(i, n) c += f[i] == 1;
+  const size_t n16 = n / 16;
+  const uint4 *f16 = reinterpret_cast<const uint4 *>(f);
+  GRID_STRIDE(i, n16) {
+    const uint4 v = f16[i];
+    c += __popc(__vcmpeq4(v.x, 0x01010101u)) / 8 + __popc(__vcmpeq4(v.y, 0x01010101u)) / 8 +
+         __popc(__vcmpeq4(v.z, 0x01010101u)) / 8 + __popc(__vcmpeq4(v.w, 0x01010101u)) / 8;
+  }
+  GRID_STRIDE(i, n - n16 * 16) c += f[n16 * 16 + i] == 1;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
   if ((threadIdx.x & 31) == 0 && c) atomicAdd(dst, c);
@@ -615,6 +635,13 @@ void launch_gather_u32(const uint32_t *idx, size_t n, const uint32_t *src, uint3
 void launch_check_ids(const uint32_t *a, size_t n, uint32_t limit, Counters *ctr, cudaStream_t s) {
   if (!n) return;
   check_ids_kernel<<<grid_for(n, 256), 256, 0, s>>>(a, n, limit, &ctr->err);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_clear_isolated_endpoints(const uint32_t *a, size_t na, const uint32_t *b, size_t nb,
+                                     const uint32_t *deg, const uint8_t *ex, uint8_t *vaff, cudaStream_t s) {
+  if (!na && !nb) return;
+  clear_isolated_endpoints_kernel<<<grid_for(na + nb, 256), 256, 0, s>>>(a, na, b, nb, deg, ex, vaff);
   LVG_CHECK_LAUNCH();
 }
 
