@@ -403,11 +403,12 @@ def run_gpu(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
                      "traffic": traffic,
-                     "traffic_note": ("DRAM bytes of the local-moving kernels per step, ncu capture on R-MAT "
-                                      "scale 22 (profiles/move_traffic.json, ratio to algorithmic bytes) scaled "
-                                      "by this step's algorithmic bytes") if tr else None,
+                     "traffic_note": ("DRAM bytes of the local-moving kernels per step: their ratio to the "
+                                      "algorithmic bytes in an ncu capture (" + tr.get("measured_on", "") +
+                                      "; profiles/move_traffic.json) times this step's algorithmic bytes")
+                                     if tr else None,
                      "algorithmic_bytes_per_step": int(alg_per_step),
-                     "kernel": "local-moving kernels (move_tile/move_block, all degree bins)",
+                     "kernel": "local-moving kernels (move_small/move_big/hub_chunk/hub_merge, all degree bins)",
                      "launches_per_step": klaunch / args.steps, "ms_per_step": kms / args.steps,
                      "per_bin_ms_per_step": [round(v / args.steps, 4) for v in bin_ms],
                      "per_bin_edges_per_step": [int(v / args.steps) for v in bin_edges],
