@@ -61,8 +61,9 @@ def parse():
     p.add_argument("--no-tune", action="store_true",
                    help="skip lvg_autotune (launch shapes and frontier colour classes) before the timed steps")
     p.add_argument("--cpu-steps", type=int, default=2)
-    p.add_argument("--workload", default="df", choices=["df", "serving", "temporal", "batched"],
-                   help="df: the headline (R-MAT scale 24, one graph); serving: many resident graphs under "
+    p.add_argument("--workload", default="df", choices=["df", "sweep", "serving", "temporal", "batched"],
+                   help="df: the headline (R-MAT scale 24, one graph); sweep: the same graph, batches of "
+                        "1e-7..1e-1 |E|, all four methods; serving: many resident graphs under "
                         "Poisson batch-update arrivals through lvg_server; temporal: a drifting-community "
                         "temporal stream, insertion-only batches, all four methods")
     p.add_argument("--batched-graphs", type=int, default=4096)
@@ -119,6 +120,15 @@ class Dist:
 
         t = torch.tensor([x], dtype=torch.float64)
         self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if not self.dist:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
         return float(t.item())
 
     def close(self):
@@ -659,6 +669,84 @@ def run_temporal(args):
     return 0
 
 
+def run_sweep(args):
+    """Batch-size sweep on the headline graph: R-MAT (scale --scale, ef 16), its
+    static result as the prior; for each batch fraction 1e-7 .. 1e-1 of |E|, a
+    random batch (80 % uniform-pair insertions, 20 % deletions of existing
+    edges, drawn in HBM as the reference's generators draw them) tidied and
+    applied to a copy of the base graph, then static, naive-dynamic,
+    delta-screening and dynamic-frontier Louvain through the drop-in calls
+    (time = LouvainResult::time, median of 3; modularity of each result). The
+    frontier methods' launch shapes come from lvg_autotune at 1e-4 |E|.
+    value = DF ms at 1e-4 |E|."""
+    rank, world, local = dist_info()
+    import lvg
+    import lvg_build
+
+    lvg_build.build()
+    lvg.set_device(local)
+    t0 = time.time()
+    G = lvg.Graph.rmat(args.scale, 16, seed=args.seed)
+    tgen = time.time() - t0
+    E = G.size
+    o = lvg.LouvainOptions()
+    prior = lvg.louvain_static(G, lvg.LouvainOptions(deterministic=True))
+
+    def updated(f, seed):
+        nupd = max(1, int(round(f * E / 2)))
+        Y = G.clone()
+        db = lvg.DeviceBatch.generate(Y, nupd // 5, nupd - nupd // 5, seed=seed)
+        t1 = time.perf_counter()
+        Y.apply_batch(db)
+        apply_ms = (time.perf_counter() - t1) * 1e3
+        return Y, db, nupd, apply_ms
+
+    # launch shapes for the frontier methods, tuned at 1e-4 |E| and inherited by the copies
+    t0 = time.perf_counter()
+    Y, db, _, _ = updated(1e-4, args.seed + 1)
+    st = lvg.State(Y)
+    st.set(prior.membership, prior.vertexWeight, prior.communityWeight)
+    tuning, _ = lvg.autotune(Y, lvg.METHOD_FRONTIER, db, st, o, repeats=3)
+    lvg.set_tuning(G, **tuning)
+    del st
+    db.close()
+    Y.close()
+    tune_s = time.perf_counter() - t0
+    rows = []
+    with Clocks(local) as clk:
+        for i, f in enumerate((1e-7, 1e-6, 1e-5, 1e-4, 1e-3, 1e-2, 1e-1)):
+            Y, db, nupd, apply_ms = updated(f, args.seed + 10 + i)
+            tb = db.download()
+            db.close()
+            row = {"batch_fraction": f, "updates": nupd, "tidied_entries": tb.num_deletions + tb.num_insertions,
+                   "apply_ms": apply_ms}
+            for name, fn in (("static", None), ("nd", lvg.louvain_naive_dynamic),
+                             ("ds", lvg.louvain_dynamic_delta_screening), ("df", lvg.louvain_dynamic_frontier)):
+                ms = []
+                for _ in range(3):
+                    r = lvg.louvain_static(Y, o) if fn is None else fn(Y, tb, prior.membership, prior.vertexWeight,
+                                                                        prior.communityWeight, o)
+                    ms.append(r.time)
+                row[name + "_ms"] = float(np.median(ms))
+                row[name + "_q"] = Y.modularity(r.membership)
+            row["df_speedup_vs_static"] = row["static_ms"] / row["df_ms"]
+            row["df_minus_static_q"] = row["df_q"] - row["static_q"]
+            rows.append(row)
+            Y.close()
+    mid = [r for r in rows if r["batch_fraction"] == 1e-4][0]
+    line = {"metric": "DF-Louvain ms per batch across batch sizes (R-MAT)", "value": mid["df_ms"], "unit": "ms",
+            "n_gpus": world, "steps": 3, "warmup": 0, "ms_per_step": mid["df_ms"], "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"R-MAT scale {args.scale} (ef 16, a/b/c/d .57/.19/.19/.05), batches of "
+                                   f"1e-7..1e-1 |E| (80 % insertions / 20 % deletions) on copies of the base",
+                       "vertices": G.span - 1, "edges": E, "generate_s": tgen},
+            "tuning": dict(tuning, by="lvg_autotune (DF at 1e-4 |E|)", seconds=round(tune_s, 2)),
+            "batches": rows, "clocks": clk.summary()}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_batched(args):
     """Batched: planted-partition graphs with |V| log-uniform in [1k, 256k],
     average degree uniform in [8, 32], blocks of 128 (C = |V|/128), p_in
@@ -668,23 +756,29 @@ def run_batched(args):
     still moving) against lvg_static one graph after another on a prefix, and
     against lvg_static_many (graphs overlapped on the GPU, one stream each).
     value = edges/s of the union run (the union's layout is the input; its
-    build from the separate graphs is timed apart)."""
+    build from the separate graphs is timed apart). On N GPUs the graphs are
+    placed round-robin, one union per GPU, no collective but the timing's
+    (total work fixed: strong scaling)."""
     rank, world, local = dist_info()
     import lvg
     import lvg_build
 
     lvg_build.build()
     lvg.set_device(local)
+    dist = Dist(world)
     rng = np.random.default_rng(args.seed)
-    n = args.batched_graphs
-    sizes = np.exp(rng.uniform(np.log(1000), np.log(256_000), n)).astype(np.int64)
-    degs = rng.uniform(8, 32, n)
-    pins = rng.uniform(0.6, 0.9, n)
+    n_all = args.batched_graphs
+    sizes = np.exp(rng.uniform(np.log(1000), np.log(256_000), n_all)).astype(np.int64)
+    degs = rng.uniform(8, 32, n_all)
+    pins = rng.uniform(0.6, 0.9, n_all)
+    mine = list(range(rank, n_all, world))  # this GPU's graphs
     t0 = time.time()
-    graphs = [lvg.Graph.planted_partition(int(v), 128, float(d), float(p), args.seed + i)
-              for i, (v, d, p) in enumerate(zip(sizes, degs, pins))]
+    graphs = [lvg.Graph.planted_partition(int(sizes[i]), 128, float(degs[i]), float(pins[i]), args.seed + i)
+              for i in mine]
     tgen = time.time() - t0
+    n = len(graphs)
     E = sum(g.size for g in graphs)
+    E_all = dist.sum(E)
     o = lvg.LouvainOptions()
     k = min(args.batched_loop, n)
     lvg.louvain_static_many(graphs[:32], o, workers=args.workers, trim=2)  # warm-up
@@ -713,21 +807,24 @@ def run_batched(args):
     sample_u.close()
     lvg.set_tuning(U, **tuning)
     tune_s = time.perf_counter() - t0
+    dist.barrier()
     with Clocks(local) as clk:
         t0 = time.perf_counter()
         ures = lvg.louvain_static_union(U, o)
         union_s = time.perf_counter() - t0
+    union_s = dist.max(union_s)
     run_ms = ures[0].time if ures else 0.0
     qs = [graphs[i].modularity(ures[i].membership) for i in sample]
-    line = {"metric": "batched static Louvain edges/s (many graphs)", "value": E / union_s, "unit": "edges/s",
+    line = {"metric": "batched static Louvain edges/s (many graphs)", "value": E_all / union_s, "unit": "edges/s",
             "n_gpus": world, "steps": 1, "warmup": 1, "ms_per_step": union_s * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "scaling": "strong", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"batched: {n} planted-partition graphs, |V| log-uniform [1k, 256k], degree "
                                    f"U[8, 32], blocks of 128, p_in U[0.6, 0.9], packed back to back as one graph "
                                    f"union; lvg_static_union vs lvg_static one by one",
-                       "graphs": n, "vertices": int(sizes.sum()), "edges": E, "generate_s": tgen,
+                       "graphs": n_all, "graphs_per_gpu": n, "vertices": int(sizes.sum()), "edges": int(E_all),
+                       "generate_s": tgen,
                        "union_build_s": union_build_s},
-            "graphs_per_s": n / union_s,
+            "graphs_per_s": n_all / union_s,
             "tuning": dict(tuning, by="lvg_autotune on a union of 64 of the graphs", seconds=round(tune_s, 2)),
             "union": {"wall_s": union_s, "device_run_ms": run_ms,
                       "download_ms": U.stats()["call_download_ms"],
@@ -742,6 +839,7 @@ def run_batched(args):
             "clocks": clk.summary()}
     if rank == 0:
         print(json.dumps(line), flush=True)
+    dist.close()
     return 0
 
 
@@ -755,6 +853,8 @@ def main():
         return run_temporal(args)
     if args.workload == "batched":
         return run_batched(args)
+    if args.workload == "sweep":
+        return run_sweep(args)
     return run_gpu(args)
 
 
