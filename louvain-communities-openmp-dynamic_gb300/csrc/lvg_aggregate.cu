@@ -290,6 +290,195 @@ __global__ void __launch_bounds__(B) agg_block_kernel(AggArgs a) {
   }
 }
 
+// ------------------------------------------------------------ communities above total degree 8192
+//
+// A community's members' edges, flattened in member order, are the range
+// [mpre[m0], mpre[m1]) of the member-degree prefix mpre. The largest
+// communities (after the first pass of a power-law graph, a handful hold
+// most of the edges) are cut into AGG_CHUNK-edge chunks, one block each; a
+// block merges its chunk in a listed shared table with warp-aggregated
+// inserts and adds the distinct (community, weight) pairs to the community's
+// table in global memory, which agg_gfinish_kernel then writes out as the
+// community's row. Each block finds the member of every edge of a batch by a
+// binary search over the batch's window of member prefixes in shared memory.
+
+// Warp-aggregated insert (the lanes holding the same key sum their weights
+// in lane order; the lowest of them calls ins).
+template <class Ins>
+__device__ __forceinline__ void agg_warp_insert(uint32_t c, float w, Ins ins) {
+  const unsigned grp = __match_any_sync(0xffffffffu, c);
+  const int lane = threadIdx.x & 31;
+  const unsigned cnt = c == EMPTY ? 0u : unsigned(__popc(grp));
+  const unsigned most = __reduce_max_sync(0xffffffffu, cnt);
+  float sum = 0.f;
+  unsigned rem = grp;
+  for (unsigned it = 0; it < most; ++it) {
+    const int src = rem ? __ffs(rem) - 1 : lane;
+    rem &= rem - 1u;
+    const float x = __shfl_sync(0xffffffffu, w, src);
+    if (it < cnt) sum += x;
+  }
+  if (c != EMPTY && (grp & ((1u << lane) - 1u)) == 0u) ins(c, sum);
+}
+
+template <int B, int LOGS>
+__global__ void __launch_bounds__(B) agg_chunk_kernel(AggArgs a, AggChunks ch) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  constexpr uint32_t CS = 1u << LOGS;
+  __shared__ uint64_t win[B + 1];
+  __shared__ unsigned s_used;
+  __shared__ uint32_t s_mi;
+  uint32_t *skeys = reinterpret_cast<uint32_t *>(smem);
+  float *svals = reinterpret_cast<float *>(smem + size_t(CS) * 4);
+  uint32_t *slist = reinterpret_cast<uint32_t *>(smem + size_t(CS) * 8);
+  for (uint32_t s2 = threadIdx.x; s2 < CS; s2 += B) { skeys[s2] = EMPTY; svals[s2] = 0.f; }
+  const uint2 cj = ch.chunk[blockIdx.x];  // (community slot, chunk index)
+  const uint32_t j = cj.x;
+  const uint32_t c = ch.comm[j];
+  const uint32_t m0 = a.coff[c], m1 = a.coff[c + 1];
+  const uint64_t ebeg = ch.mpre[m0], eend = ch.mpre[m1];
+  const uint64_t e0 = ebeg + uint64_t(cj.y) * AGG_CHUNK;
+  const uint64_t e1 = min(eend, e0 + AGG_CHUNK);
+  uint32_t *gk = ch.gkeys + ch.toff[j];
+  float *gv = ch.gvals + ch.toff[j];
+  const int glg = ch.tlog[j];
+  const unsigned limit = CS >> 1;
+  if (threadIdx.x == 0) {
+    s_used = 0;
+    // the member holding edge e0: the last m in [m0, m1) with mpre[m] <= e0
+    uint32_t lo = m0, hi = m1 - 1;
+    while (lo < hi) {
+      const uint32_t mid = lo + (hi - lo + 1) / 2;
+      if (ch.mpre[mid] <= e0) lo = mid; else hi = mid - 1;
+    }
+    s_mi = lo;
+  }
+  __syncthreads();
+  unsigned long long nread = 0;
+  bool ok = true;
+  uint64_t base = e0;
+  while (base < e1) {  // block-uniform
+    const uint32_t mi = s_mi;
+    const uint32_t nw = min(uint32_t(B), m1 - mi);  // members staged: mi .. mi+nw-1
+    for (uint32_t t = threadIdx.x; t <= nw; t += B) win[t] = ch.mpre[mi + t];
+    __syncthreads();
+    // this round: edges [base, stop), all inside the staged members
+    const uint64_t stop = min(e1, min(base + B, win[nw]));
+    const uint64_t e = base + threadIdx.x;
+    uint32_t key = EMPTY;
+    float w = 0.f;
+    if (e < stop) {
+      uint32_t lo = 0, hi = nw - 1;  // last window entry <= e
+      while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (win[mid] <= e) lo = mid; else hi = mid - 1;
+      }
+      const uint32_t u = a.cmem[mi + lo];
+      const uint64_t x = a.off[u] + (e - win[lo]);
+      key = a.vcom[__ldcs(a.key + x)];
+      w = __ldcs(a.w + x);
+      ++nread;
+    }
+    agg_warp_insert(key, w, [&](uint32_t k, float v) {
+      // the shared table while its claim budget lasts, then the global one
+      const uint32_t mask = CS - 1u;
+      uint32_t sl = hash_hi(k, LOGS);
+      for (uint32_t probe = 0; probe <= mask; ++probe) {
+        const uint32_t kk = skeys[sl];
+        if (kk == k) { atomicAdd(&svals[sl], v); return; }
+        if (kk == EMPTY) {
+          const unsigned r = atomicAdd(&s_used, 1u);
+          if (r >= limit) break;
+          const uint32_t prev = atomicCAS(&skeys[sl], EMPTY, k);
+          if (prev == EMPTY) { slist[r] = sl; atomicAdd(&svals[sl], v); return; }
+          slist[r] = EMPTY;
+          if (prev == k) { atomicAdd(&svals[sl], v); return; }
+        }
+        sl = (sl + 1u) & mask;
+      }
+      ok &= table_add(gk, gv, glg, k, v);
+    });
+    __syncthreads();  // every thread has read win[] and s_mi
+    // the next round starts at the member holding edge `stop`
+    if (threadIdx.x == 0) {
+      if (stop < win[nw]) {
+        uint32_t lo = 0, hi = nw - 1;
+        while (lo < hi) {
+          const uint32_t mid = (lo + hi + 1) >> 1;
+          if (win[mid] <= stop) lo = mid; else hi = mid - 1;
+        }
+        s_mi = mi + lo;
+      } else {
+        s_mi = mi + nw;  // past the staged members (also when they had no edges left)
+      }
+    }
+    base = stop;
+    __syncthreads();
+  }
+  // the shared table into the community's global table
+  const unsigned nl = min(s_used, limit);
+  for (unsigned i = threadIdx.x; i < nl; i += B) {
+    const uint32_t sl = slist[i];
+    if (sl != EMPTY) ok &= table_add(gk, gv, glg, skeys[sl], svals[sl]);
+  }
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) nread += __shfl_xor_sync(0xffffffffu, nread, o);
+  const bool bad = __any_sync(0xffffffffu, !ok);
+  if (lane == 0) {
+    if (nread) atomicAdd(&a.ctr->agg_edges, nread);
+    if (bad) atomicOr(&a.ctr->err, ERR_TABLE_FULL);
+  }
+}
+
+// The global tables of the chunked communities into their rows: a thread
+// per slot, output positions by a warp-aggregated cursor per community
+// (ydeg), the row sums into vtot.
+__global__ void agg_gfinish_kernel(AggArgs a, AggChunks ch, uint64_t slots) {
+  const int lane = threadIdx.x & 31;
+  for (uint64_t base = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32 * 32; base < slots;
+       base += uint64_t(gridDim.x) * blockDim.x) {
+    const uint64_t t = base + lane;
+    uint32_t jj = EMPTY, k = EMPTY;
+    float v = 0.f;
+    if (t < slots) {
+      uint32_t lo = 0, hi = ch.n - 1;  // the community whose region holds slot t
+      while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (ch.toff[mid] <= t) lo = mid; else hi = mid - 1;
+      }
+      k = ch.gkeys[t];
+      if (k != EMPTY) { jj = lo; v = ch.gvals[t]; }
+    }
+    const unsigned grp = __match_any_sync(0xffffffffu, jj);
+    const int leader = __ffs(grp) - 1;
+    float sum = 0.f;
+    for (unsigned r = grp; r; r &= r - 1u) sum += __shfl_sync(grp, v, __ffs(r) - 1);
+    uint32_t at = 0;
+    const uint32_t c = jj != EMPTY ? ch.comm[jj] : 0u;
+    if (jj != EMPTY && lane == leader) {
+      at = atomicAdd(&a.ydeg[c], uint32_t(__popc(grp)));
+      atomicAdd(&a.vtot[c], sum);
+    }
+    at = __shfl_sync(grp, at, leader);
+    if (jj != EMPTY) {
+      const uint64_t y = a.yoff[c] + at + __popc(grp & ((1u << lane) - 1u));
+      a.ykey[y] = k;
+      a.yw[y] = v;
+    }
+  }
+}
+
+__global__ void comm_tdeg_kernel(const uint32_t *list, size_t n, const uint64_t *yoff, uint64_t *out) {
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
+    out[i] = yoff[list[i] + 1] - yoff[list[i]];
+}
+
+__global__ void member_degrees_kernel(const uint32_t *cmem, const uint32_t *deg, size_t n, uint64_t *dst) {
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
+    dst[i] = deg[cmem[i]];
+}
+
 int sms() {  // SM count of the device, queried once (thread-safe static init)
   static const int n = [] {
     int dev = 0, c = 0;
@@ -333,6 +522,29 @@ void launch_big(const AggArgs &a, cudaStream_t s) {
 }
 
 }  // namespace
+
+void launch_comm_tdeg(const uint32_t *list, size_t n, const uint64_t *yoff, uint64_t *out, cudaStream_t s) {
+  if (!n) return;
+  comm_tdeg_kernel<<<grid_for(n, 256), 256, 0, s>>>(list, n, yoff, out);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_member_degrees(const uint32_t *cmem, const uint32_t *deg, size_t n, uint64_t *dst, cudaStream_t s) {
+  if (!n) return;
+  member_degrees_kernel<<<grid_for(n, 256), 256, 0, s>>>(cmem, deg, n, dst);
+  LVG_CHECK_LAUNCH();
+}
+
+constexpr int AGG_CHUNK_B = 256, AGG_CHUNK_LOGS = 11;
+
+void launch_aggregate_chunks(const AggArgs &a, const AggChunks &ch, size_t chunks, uint64_t slots, cudaStream_t s) {
+  if (!chunks) return;
+  const size_t smem = (size_t(1) << AGG_CHUNK_LOGS) * 10;  // keys, values, claimed list
+  agg_chunk_kernel<AGG_CHUNK_B, AGG_CHUNK_LOGS><<<unsigned(chunks), AGG_CHUNK_B, smem, s>>>(a, ch);
+  LVG_CHECK_LAUNCH();
+  agg_gfinish_kernel<<<grid_for(slots, 256), 256, 0, s>>>(a, ch, slots);
+  LVG_CHECK_LAUNCH();
+}
 
 void launch_aggregate_bin(int b, const AggArgs &a, cudaStream_t s) {
   switch (b) {

@@ -55,6 +55,12 @@ struct Workspace {
   // chunked hub path
   DBuf<uint32_t> chunk_cnt, part_key;
   DBuf<float> part_val, hub_kd;
+  // chunked aggregation of the largest communities
+  DBuf<uint64_t> mpre, agg_toff, agg_tdeg;
+  DBuf<uint2> agg_chunk;
+  DBuf<int> agg_tlog;
+  DBuf<uint32_t> agg_gk;
+  DBuf<float> agg_gv;
 
   void allocate(size_t S_, size_t X_, cudaStream_t st) {
     S = S_;
@@ -682,10 +688,10 @@ Level aggregate(lvg_graph *g, const Level &lv, const uint32_t *com, size_t CN, i
   // Empty communities never reach a kernel: zero their rows and weights first.
   LVG_CUDA(cudaMemsetAsync(nl.deg, 0, CN * sizeof(uint32_t), s));
   LVG_CUDA(cudaMemsetAsync(W.vtot.p, 0, CN * sizeof(float), s));
-  // Global fallback regions of the large bins (9-11), as in move_phase.
+  // Global fallback regions of bins 9-10 (bin 11 is chunked below).
   int glog2[NUM_BINS] = {};
   size_t need = 0;
-  for (int b = 9; b < NUM_BINS; ++b) {
+  for (int b = 9; b < NUM_BINS - 1; ++b) {
     const size_t cnt = cb[b + 1] - cb[b];
     if (!cnt) continue;
     glog2[b] = global_table_log2(std::min<uint64_t>(cmax[b], CN));
@@ -697,7 +703,7 @@ Level aggregate(lvg_graph *g, const Level &lv, const uint32_t *com, size_t CN, i
   }
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (g->profiling) e0 = g->events.record(s);
-  for (int b = 1; b < NUM_BINS; ++b) {
+  for (int b = 1; b < NUM_BINS - 1; ++b) {
     const size_t cnt = cb[b + 1] - cb[b];
     if (!cnt) continue;
     AggArgs a;
@@ -710,6 +716,55 @@ Level aggregate(lvg_graph *g, const Level &lv, const uint32_t *com, size_t CN, i
     a.gkeys = need ? W.gkeys.p : nullptr; a.gvals = need ? W.gvals.p : nullptr; a.glog2 = glog2[b];
     launch_aggregate_bin(b, a, s);
     ++g->stats.aggregate_launches;
+  }
+  // communities above total degree 8192: chunks of AGG_CHUNK edges over many
+  // blocks, merged in per-community tables in HBM
+  if (const size_t n11 = cb[NUM_BINS] - cb[NUM_BINS - 1]) {
+    const uint32_t *list = W.cbins.p + cb[NUM_BINS - 1];
+    uint32_t members = 0;
+    LVG_CUDA(cudaMemcpyAsync(&members, W.csize.p + CN, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    W.agg_tdeg.ensure(n11);
+    launch_comm_tdeg(list, n11, nl.off, W.agg_tdeg.p, s);
+    std::vector<uint64_t> tdeg(n11);
+    LVG_CUDA(cudaMemcpyAsync(tdeg.data(), W.agg_tdeg.p, n11 * 8, cudaMemcpyDeviceToHost, s));
+    LVG_CUDA(cudaStreamSynchronize(s));
+    W.mpre.ensure(size_t(members) + 1);
+    launch_member_degrees(W.cmem.p, lv.deg, members, W.mpre.p, s);
+    exclusive_scan_u64(W.mpre.p, W.mpre.p, members, W.mpre.p + members, W.scan64.p, s);
+    std::vector<uint2> chunks;
+    std::vector<uint64_t> toff(n11 + 1, 0);
+    std::vector<int> tlog(n11);
+    for (size_t j = 0; j < n11; ++j) {
+      const uint64_t want = 2 * std::min<uint64_t>(tdeg[j], CN);
+      int lg = 1;
+      while ((uint64_t(1) << lg) < want) ++lg;
+      tlog[j] = lg;
+      toff[j + 1] = toff[j] + (uint64_t(1) << lg);
+      for (uint64_t k = 0; k * AGG_CHUNK < tdeg[j]; ++k) chunks.push_back(make_uint2(uint32_t(j), uint32_t(k)));
+    }
+    const uint64_t slots = toff[n11];
+    W.agg_chunk.ensure(chunks.size());
+    W.agg_toff.ensure(n11 + 1);
+    W.agg_tlog.ensure(n11);
+    W.agg_gk.ensure(slots);
+    W.agg_gv.ensure(slots);
+    LVG_CUDA(cudaMemcpyAsync(W.agg_chunk.p, chunks.data(), chunks.size() * sizeof(uint2), cudaMemcpyHostToDevice, s));
+    LVG_CUDA(cudaMemcpyAsync(W.agg_toff.p, toff.data(), (n11 + 1) * 8, cudaMemcpyHostToDevice, s));
+    LVG_CUDA(cudaMemcpyAsync(W.agg_tlog.p, tlog.data(), n11 * sizeof(int), cudaMemcpyHostToDevice, s));
+    LVG_CUDA(cudaMemsetAsync(W.agg_gk.p, 0xFF, slots * 4, s));
+    LVG_CUDA(cudaMemsetAsync(W.agg_gv.p, 0, slots * 4, s));
+    AggArgs a;
+    a.off = lv.off; a.deg = lv.deg; a.key = lv.key; a.w = lv.w;
+    a.vcom = com; a.coff = W.csize.p; a.cmem = W.cmem.p;
+    a.list = list;
+    a.count = uint32_t(n11);
+    a.yoff = nl.off; a.ydeg = nl.deg; a.ykey = nl.key; a.yw = nl.w;
+    a.vtot = W.vtot.p; a.ctr = g->ctr.p; a.cn = uint32_t(CN);
+    a.gkeys = nullptr; a.gvals = nullptr; a.glog2 = 0;
+    AggChunks ch{W.agg_chunk.p, list, W.agg_toff.p, W.agg_tlog.p, W.mpre.p, W.agg_gk.p, W.agg_gv.p, uint32_t(n11)};
+    launch_aggregate_chunks(a, ch, chunks.size(), slots, s);
+    g->stats.aggregate_launches += 2;
+    LVG_CUDA(cudaStreamSynchronize(s));  // the host vectors above are freed next
   }
   if (g->profiling) {
     e1 = g->events.record(s);
@@ -2434,7 +2489,7 @@ int lvg_autotune(lvg_graph *g, int method, const lvg_device_batch *b, const lvg_
     try_knob([](lvg_tuning &t, long v) { t.concurrent_bins = int(v); }, {1, 0}, false);
     try_knob([](lvg_tuning &t, long v) { t.fused_small = int(v); }, {1, 0}, false);
     try_knob([](lvg_tuning &t, long v) { t.big_blocks_per_sm = int(v); }, {0, 2, 3, 4}, false);
-    if (colours) try_knob([](lvg_tuning &t, long v) { t.frontier_colors = int(v); }, {8, 4, 2}, true);
+    if (colours) try_knob([](lvg_tuning &t, long v) { t.frontier_colors = int(v); }, {8, 4, 2, 1}, true);
     apply_tuning(g, cur);
     g->profiling = profiling;
     if (best) *best = cur;

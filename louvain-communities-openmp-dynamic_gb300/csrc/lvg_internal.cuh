@@ -216,6 +216,22 @@ struct AggArgs {
   int glog2;
 };
 
+// Aggregation of the communities above total degree 8192 in AGG_CHUNK-edge
+// chunks (lvg_aggregate.cu): community slot j is community comm[j]; its
+// global table holds 2^tlog[j] slots at toff[j] (toff[n] = all slots); mpre
+// is the prefix of member degrees in member-list order.
+constexpr uint32_t AGG_CHUNK = 16384;
+struct AggChunks {
+  const uint2 *chunk;     // [chunks] (community slot, chunk index)
+  const uint32_t *comm;   // [n]
+  const uint64_t *toff;   // [n+1]
+  const int *tlog;        // [n]
+  const uint64_t *mpre;   // [members+1]
+  uint32_t *gkeys;        // [toff[n]] EMPTY-initialised
+  float *gvals;           // [toff[n]] zero-initialised
+  uint32_t n;
+};
+
 // ---------------------------------------------------------------- scans (lvg_scan.cu)
 size_t scan_scratch_elems(size_t n);
 // Exclusive scan; out may alias in. If total != nullptr the sum is written there.
@@ -300,6 +316,12 @@ void launch_move_bin(int b, bool sync, const MoveArgs &a, cudaStream_t s);
 
 // ---------------------------------------------------------------- aggregation (lvg_aggregate.cu)
 void launch_aggregate_bin(int b, const AggArgs &a, cudaStream_t s);
+// out[i] = total degree of community list[i] (from the row offsets yoff).
+void launch_comm_tdeg(const uint32_t *list, size_t n, const uint64_t *yoff, uint64_t *out, cudaStream_t s);
+// dst[i] = deg[cmem[i]] for the member list.
+void launch_member_degrees(const uint32_t *cmem, const uint32_t *deg, size_t n, uint64_t *dst, cudaStream_t s);
+// The chunked communities: chunk merges into the global tables, then the rows.
+void launch_aggregate_chunks(const AggArgs &a, const AggChunks &ch, size_t chunks, uint64_t slots, cudaStream_t s);
 
 // Record a failure message for lvg_last_error() and return `code` (for entry
 // points outside lvg_api.cu).

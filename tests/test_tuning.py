@@ -62,7 +62,7 @@ def test_autotune_frontier(cuda, orc, hubcase):
                                                                  r0.communityWeight).membership)
     t, ms = cuda.autotune(Y, cuda.METHOD_FRONTIER, db, prior, repeats=2)
     assert ms > 0 and cuda.get_tuning(Y) == t
-    assert t["hub_chunk"] in (2048, 4096, 8192, 16384) and t["frontier_colors"] in (8, 4, 2)
+    assert t["hub_chunk"] in (2048, 4096, 8192, 16384) and t["frontier_colors"] in (8, 4, 2, 1)
     r = cuda.louvain_dynamic_frontier(Y, b, r0.membership, r0.vertexWeight, r0.communityWeight)
     assert orc.modularity(y, r.membership) >= q_default - 5e-3
 
