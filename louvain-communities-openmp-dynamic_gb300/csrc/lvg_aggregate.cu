@@ -49,6 +49,26 @@ __device__ __forceinline__ bool table_add(KP keys, VP vals, int log2cap, uint32_
   return false;
 }
 
+// Warp-aggregated insert (the lanes holding the same key sum their weights
+// in lane order; the lowest of them calls ins).
+template <class Ins>
+__device__ __forceinline__ bool agg_warp_insert(uint32_t c, float w, Ins ins) {
+  const unsigned grp = __match_any_sync(0xffffffffu, c);
+  const int lane = threadIdx.x & 31;
+  const unsigned cnt = c == EMPTY ? 0u : unsigned(__popc(grp));
+  const unsigned most = __reduce_max_sync(0xffffffffu, cnt);
+  float sum = 0.f;
+  unsigned rem = grp;
+  for (unsigned it = 0; it < most; ++it) {
+    const int src = rem ? __ffs(rem) - 1 : lane;
+    rem &= rem - 1u;
+    const float x = __shfl_sync(0xffffffffu, w, src);
+    if (it < cnt) sum += x;
+  }
+  if (c != EMPTY && (grp & ((1u << lane) - 1u)) == 0u) return ins(c, sum);
+  return true;
+}
+
 // Visit all edges of members cmem[m0..m1), T lanes cooperating (tile mask
 // m). Edges into the community itself (`self`, the hottest key: every
 // internal edge) are summed in the lane-private `self_w`; the others go to
@@ -88,12 +108,19 @@ __device__ __forceinline__ uint64_t visit_members(const AggArgs &a, uint32_t m0,
       const uint32_t oincl = __shfl_sync(m, incl, lo, T);
       const uint32_t odeg = __shfl_sync(m, dg, lo, T);
       const uint64_t oo = __shfl_sync(m, o, lo, T);
+      uint32_t c = EMPTY;
+      float w = 0.f;
       if (go && k < total) {
         const uint64_t e = oo + (k - (oincl - odeg));
-        const uint32_t c = a.vcom[a.key[e]];
-        const float w = a.w[e];
-        if (c == self) self_w += w;
-        else go = add(c, w);
+        c = a.vcom[a.key[e]];
+        w = a.w[e];
+        if (c == self) { self_w += w; c = EMPTY; }
+      }
+      if constexpr (T == 32) {
+        // a whole warp: lanes holding the same community add once
+        go = __all_sync(0xffffffffu, agg_warp_insert(c, w, add)) && go;
+      } else {
+        if (c != EMPTY) go = add(c, w);
       }
     }
   }
@@ -302,25 +329,6 @@ __global__ void __launch_bounds__(B) agg_block_kernel(AggArgs a) {
 // community's row. Each block finds the member of every edge of a batch by a
 // binary search over the batch's window of member prefixes in shared memory.
 
-// Warp-aggregated insert (the lanes holding the same key sum their weights
-// in lane order; the lowest of them calls ins).
-template <class Ins>
-__device__ __forceinline__ void agg_warp_insert(uint32_t c, float w, Ins ins) {
-  const unsigned grp = __match_any_sync(0xffffffffu, c);
-  const int lane = threadIdx.x & 31;
-  const unsigned cnt = c == EMPTY ? 0u : unsigned(__popc(grp));
-  const unsigned most = __reduce_max_sync(0xffffffffu, cnt);
-  float sum = 0.f;
-  unsigned rem = grp;
-  for (unsigned it = 0; it < most; ++it) {
-    const int src = rem ? __ffs(rem) - 1 : lane;
-    rem &= rem - 1u;
-    const float x = __shfl_sync(0xffffffffu, w, src);
-    if (it < cnt) sum += x;
-  }
-  if (c != EMPTY && (grp & ((1u << lane) - 1u)) == 0u) ins(c, sum);
-}
-
 template <int B, int LOGS>
 __global__ void __launch_bounds__(B) agg_chunk_kernel(AggArgs a, AggChunks ch) {
   extern __shared__ __align__(16) uint8_t smem[];
@@ -385,18 +393,19 @@ __global__ void __launch_bounds__(B) agg_chunk_kernel(AggArgs a, AggChunks ch) {
       uint32_t sl = hash_hi(k, LOGS);
       for (uint32_t probe = 0; probe <= mask; ++probe) {
         const uint32_t kk = skeys[sl];
-        if (kk == k) { atomicAdd(&svals[sl], v); return; }
+        if (kk == k) { atomicAdd(&svals[sl], v); return true; }
         if (kk == EMPTY) {
           const unsigned r = atomicAdd(&s_used, 1u);
           if (r >= limit) break;
           const uint32_t prev = atomicCAS(&skeys[sl], EMPTY, k);
-          if (prev == EMPTY) { slist[r] = sl; atomicAdd(&svals[sl], v); return; }
+          if (prev == EMPTY) { slist[r] = sl; atomicAdd(&svals[sl], v); return true; }
           slist[r] = EMPTY;
-          if (prev == k) { atomicAdd(&svals[sl], v); return; }
+          if (prev == k) { atomicAdd(&svals[sl], v); return true; }
         }
         sl = (sl + 1u) & mask;
       }
       ok &= table_add(gk, gv, glg, k, v);
+      return true;
     });
     __syncthreads();  // every thread has read win[] and s_mi
     // the next round starts at the member holding edge `stop`
