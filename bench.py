@@ -151,10 +151,16 @@ class Clocks:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # the sampler's first line before the timed region starts (a short
+            # region would otherwise end before nvidia-smi prints anything)
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 3.0:
+                time.sleep(0.01)
+            self.lines.clear()
         except Exception:
             self.proc = None
         return self
@@ -165,6 +171,10 @@ class Clocks:
 
     def __exit__(self, *a):
         if self.proc:
+            # at least one sample taken from the region's start on
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 1.0:
+                time.sleep(0.01)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -827,6 +837,9 @@ def run_batched(args):
             "graphs_per_s": n_all / union_s,
             "tuning": dict(tuning, by="lvg_autotune on a union of 64 of the graphs", seconds=round(tune_s, 2)),
             "union": {"wall_s": union_s, "device_run_ms": run_ms,
+                      "local_move_ms": ures[0].localMoveTime if ures else 0.0,
+                      "aggregation_ms": ures[0].aggregationTime if ures else 0.0,
+                      "first_pass_ms": ures[0].firstPassTime if ures else 0.0,
                       "download_ms": U.stats()["call_download_ms"],
                       "iterations_max": int(max(r.iterations for r in ures)),
                       "passes_max": int(max(r.passes for r in ures))},

@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <memory>
 #include <string>
 #include <thread>
@@ -230,7 +231,10 @@ struct lvg_graph {
   // concurrently (fork/join with events)
   cudaStream_t aux[4] = {};
   cudaEvent_t fork_ev = nullptr, join_ev[4] = {};
+  // result copies that overlap the run (host-array entry points)
+  cudaStream_t copy_stream = nullptr;
   ~lvg_graph() {
+    if (copy_stream) cudaStreamDestroy(copy_stream);
     if (iter_exec) cudaGraphExecDestroy(iter_exec);
     for (auto &a : aux)
       if (a) cudaStreamDestroy(a);
@@ -784,8 +788,10 @@ struct StateRef {
 
 // One call of a method. prior: device FP32 prior state (dynamic methods);
 // out: where the first level's membership/weights and final totals live.
+// on_init (optional) is called once, in the last repetition, with an event
+// recorded when the first level's vertex weights (out.vt) are final.
 void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out, const lvg_options &o,
-         RunInfo &info) {
+         RunInfo &info, const std::function<void(cudaEvent_t)> *on_init = nullptr) {
   if (g->uni) throw Error(LVG_EINVAL, "graph union: run it with lvg_static_union");
   ensure_ws(g);
   Workspace &W = *g->ws;
@@ -826,6 +832,7 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
       launch_batch_weights(b.is, b.iw, b.ni, +1.f, ucom, utot, ctot, s);
     }
     cudaEvent_t e1 = g->events.record(s);
+    if (on_init && r == rep - 1) (*on_init)(e1);
     // fm: mark affected vertices.
     const uint8_t *fa = nullptr;
     if (method == LVG_METHOD_STATIC || method == LVG_METHOD_NAIVE) {
@@ -1109,7 +1116,8 @@ void fill_result(lvg_result *out, const RunInfo &info, size_t span) {
 
 // Download the first-level membership/weights and final totals to the
 // result's host arrays (allocating the ones left NULL).
-void download_result(lvg_graph *g, lvg_result *out, StateRef st) {
+// skip_vw: the vertex weights were copied out during the run.
+void download_result(lvg_graph *g, lvg_result *out, StateRef st, bool skip_vw = false) {
   Workspace &W = *g->ws;
   cudaStream_t s = g->stream;
   const size_t S = g->base.span;
@@ -1119,10 +1127,10 @@ void download_result(lvg_graph *g, lvg_result *out, StateRef st) {
   if (!out->membership || !out->vertexWeight || !out->communityWeight) throw std::bad_alloc();
   W.stage_a.ensure(S);
   W.stage_b.ensure(S);
-  launch_f32_to_f64(st.vt, W.stage_a.p, S, s);
+  if (!skip_vw) launch_f32_to_f64(st.vt, W.stage_a.p, S, s);
   launch_f32_to_f64(st.ct, W.stage_b.p, S, s);
   LVG_CUDA(cudaMemcpyAsync(out->membership, st.q, S * 4, cudaMemcpyDeviceToHost, s));
-  LVG_CUDA(cudaMemcpyAsync(out->vertexWeight, W.stage_a.p, S * 8, cudaMemcpyDeviceToHost, s));
+  if (!skip_vw) LVG_CUDA(cudaMemcpyAsync(out->vertexWeight, W.stage_a.p, S * 8, cudaMemcpyDeviceToHost, s));
   LVG_CUDA(cudaMemcpyAsync(out->communityWeight, W.stage_b.p, S * 8, cudaMemcpyDeviceToHost, s));
   LVG_CUDA(cudaStreamSynchronize(s));
 }
@@ -1151,6 +1159,8 @@ int run_host(lvg_graph *g, int method, const lvg_batch *b, const uint32_t *q, co
   if (!g || !out) return fail(LVG_EINVAL, "null graph or result");
   return guarded([&] {
     LVG_CUDA(cudaSetDevice(g->device));
+    // a copy left in flight by a call that failed
+    if (g->copy_stream) LVG_CUDA(cudaStreamSynchronize(g->copy_stream));
     lvg_options opt;
     if (o) opt = *o; else lvg_options_default(&opt);
     const auto t0 = std::chrono::steady_clock::now();
@@ -1170,10 +1180,27 @@ int run_host(lvg_graph *g, int method, const lvg_batch *b, const uint32_t *q, co
     const auto t1 = std::chrono::steady_clock::now();
     StateRef st{W.ucom.p, W.utot.p, W.ctot.p};
     RunInfo info;
-    run(g, method, db, prior, st, opt, info);
+    // The vertex weights are final once the run has initialised: into a
+    // pinned result array they are copied out on a side stream while the
+    // local moving runs (the host link is full duplex).
+    cudaPointerAttributes pa{};
+    const bool early = out->vertexWeight &&
+                       cudaPointerGetAttributes(&pa, out->vertexWeight) == cudaSuccess &&
+                       pa.type == cudaMemoryTypeHost;
+    cudaGetLastError();
+    std::function<void(cudaEvent_t)> hook = [&](cudaEvent_t ready) {
+      if (!g->copy_stream) LVG_CUDA(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
+      const size_t S = g->base.span;
+      W.stage_a.ensure(S);
+      LVG_CUDA(cudaStreamWaitEvent(g->copy_stream, ready, 0));
+      launch_f32_to_f64(st.vt, W.stage_a.p, S, g->copy_stream);
+      LVG_CUDA(cudaMemcpyAsync(out->vertexWeight, W.stage_a.p, S * 8, cudaMemcpyDeviceToHost, g->copy_stream));
+    };
+    run(g, method, db, prior, st, opt, info, early ? &hook : nullptr);
     fill_result(out, info, g->base.span);
     const auto t2 = std::chrono::steady_clock::now();
-    download_result(g, out, st);
+    download_result(g, out, st, early);
+    if (early) LVG_CUDA(cudaStreamSynchronize(g->copy_stream));
     const auto t3 = std::chrono::steady_clock::now();
     using ms = std::chrono::duration<double, std::milli>;
     g->stats.call_upload_ms = ms(t1 - t0).count();
