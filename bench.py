@@ -84,8 +84,11 @@ def parse():
     p.add_argument("--coalesce", type=int, default=1 << 18,
                    help="serving: serve a graph's queued requests as one batch of up to this many entries (0: off)")
     p.add_argument("--ncu-steps", type=int, default=0,
-                   help="profiling mode: set up as usual, then run this many DF steps between "
+                   help="profiling mode: set up as usual, then run this many steps between "
                         "cudaProfilerStart/Stop (for ncu --profile-from-start off) and exit")
+    p.add_argument("--ncu-method", default="df", choices=["df", "static"],
+                   help="profiling mode of the df workload: the method profiled (static: the plain "
+                        "GPU static Louvain on the updated graph)")
     return p.parse_args()
 
 
@@ -325,10 +328,11 @@ def run_gpu(args):
         tune_s = time.perf_counter() - t0
 
     if args.ncu_steps:
-        lvg.run_resident(Y, lvg.METHOD_FRONTIER, db, st_prior, st_out, o)  # warm: graph capture
+        meth = lvg.METHOD_STATIC if args.ncu_method == "static" else lvg.METHOD_FRONTIER
+        lvg.run_resident(Y, meth, db, st_prior, st_out, o)  # warm: graph capture
         lvg.profiler_start()
         for _ in range(args.ncu_steps):
-            info = lvg.run_resident(Y, lvg.METHOD_FRONTIER, db, st_prior, st_out, o)
+            info = lvg.run_resident(Y, meth, db, st_prior, st_out, o)
         lvg.profiler_stop()
         if rank == 0:
             st = Y.stats()
@@ -787,6 +791,19 @@ def run_batched(args):
               for i in mine]
     tgen = time.time() - t0
     n = len(graphs)
+    o = lvg.LouvainOptions()
+    if args.ncu_steps:  # profiling mode: the union's static runs only
+        U = lvg.Graph.union(graphs)
+        lvg.louvain_static_union(U, o)
+        lvg.profiler_start()
+        for _ in range(args.ncu_steps):
+            ures = lvg.louvain_static_union(U, o)
+        lvg.profiler_stop()
+        if rank == 0:
+            print(json.dumps({"profiled_union_runs": args.ncu_steps, "graphs": n, "edges": U.size,
+                              "last_ms": ures[0].time}), flush=True)
+        dist.close()
+        return 0
     E = sum(g.size for g in graphs)
     E_all = dist.sum(E)
     o = lvg.LouvainOptions()

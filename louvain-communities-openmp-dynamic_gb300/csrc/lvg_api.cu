@@ -320,8 +320,9 @@ void compute_bins(lvg_graph *g, Level &lv, const uint32_t *deg, uint32_t *list, 
 }
 
 // Chunked work of degree bin 11 (see HubPlan): hubs in colour order, each
-// hub's edges cut into HUB_CHUNK-edge chunks with a partial region of the
-// chunk's size. Built on the host from the hubs' degrees (synchronises).
+// hub's edges cut into chunks of the graph's hub_chunk edges, each with a
+// partial region of the chunk's size. Built on the host from the hubs'
+// degrees (synchronises).
 void build_hub_plan(lvg_graph *g, Level &lv, HubPlanBuffers &hb) {
   cudaStream_t s = g->stream;
   HubPlan &P = lv.hub;
@@ -2476,7 +2477,12 @@ int lvg_autotune(lvg_graph *g, int method, const lvg_device_batch *b, const lvg_
     StateRef pr{nullptr, nullptr, nullptr};
     if (prior) pr = StateRef{prior->q.p, prior->vt.p, prior->ct.p};
     StateRef st{W.ucom.p, W.utot.p, W.ctot.p};
-    const bool profiling = g->profiling;
+    // per-launch timing off while tuning (restored however the call ends)
+    struct Restore {
+      lvg_graph *g;
+      bool was;
+      ~Restore() { g->profiling = was; }
+    } restore{g, g->profiling};
     g->profiling = false;
     auto once = [&] {
       RunInfo ri;
@@ -2518,7 +2524,6 @@ int lvg_autotune(lvg_graph *g, int method, const lvg_device_batch *b, const lvg_
     try_knob([](lvg_tuning &t, long v) { t.big_blocks_per_sm = int(v); }, {0, 2, 3, 4}, false);
     if (colours) try_knob([](lvg_tuning &t, long v) { t.frontier_colors = int(v); }, {8, 4, 2, 1}, true);
     apply_tuning(g, cur);
-    g->profiling = profiling;
     if (best) *best = cur;
     if (best_ms) *best_ms = tcur;
     return LVG_OK;

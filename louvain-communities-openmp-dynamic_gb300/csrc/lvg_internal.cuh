@@ -79,9 +79,10 @@ struct HBuf {  // pinned host buffer, grows on demand
 
 
 // Work plan of the chunked path for the largest vertices (degree bin 11) of a
-// level: each hub's edge list is cut into chunks of HUB_CHUNK edges that
-// different blocks aggregate at once; a second kernel merges a hub's chunks.
-// Hubs are ordered by colour class; chunks by hub.
+// level: each hub's edge list is cut into chunks (the graph's
+// lvg_tuning::hub_chunk edges, HUB_CHUNK by default) that different blocks
+// aggregate at once; a second kernel merges a hub's chunks. Hubs are ordered
+// by colour class; chunks by hub.
 constexpr uint32_t HUB_CHUNK = 4096;
 struct HubPlan {
   size_t hubs = 0, chunks = 0, part = 0;        // counts; part = partial-entry capacity

@@ -593,7 +593,7 @@ __global__ void __launch_bounds__(B) move_big_kernel(MoveArgs a) {
 
 // ------------------------------------------------------------ chunked hubs
 
-// Hub path, step 1: one block per chunk of HUB_CHUNK edges of one hub of the
+// Hub path, step 1: one block per chunk (lvg_tuning::hub_chunk edges) of one hub of the
 // colour class. The chunk is merged in a listed shared table with a claim
 // budget and its distinct (community, weight) pairs are written to the
 // chunk's partial region; a chunk with more distinct communities than the
@@ -870,7 +870,7 @@ void launch_tile(const MoveArgs &a, cudaStream_t s) {
 // a high-degree vertex's neighbours fall into few communities.
 constexpr int BIG9_B = 256, BIG9_LOGS = 11;     // degree 513-2048
 constexpr int BIG10_B = 256, BIG10_LOGS = 11;   // degree 2049-8192
-constexpr int HUBC_B = 256, HUBC_LOGS = 11;     // hub chunks (HUB_CHUNK edges each)
+constexpr int HUBC_B = 256, HUBC_LOGS = 11;     // hub chunks (lvg_tuning::hub_chunk edges each)
 constexpr int HUBM_B = 512, HUBM_LOGS = 13;     // hub merge
 
 // Resident blocks of a large-degree kernel on the whole device, queried once.
