@@ -584,6 +584,33 @@ def run_serving(args):
     n_req = st["requests"]
     entries = st["batch_entries"]
     offered_s = n_req / st["offered_requests_per_s"]
+
+    # the plain per-graph loop the server is compared with: requests of the
+    # same kind one at a time on one thread (tidy + apply, then DF from the
+    # graph's current state, each call synchronous); the states come from the
+    # server first (untimed)
+    sv.drain()
+    nb = 400
+    _, lwhich, lpays = payloads_for(nb, args.rate, args.seed + 11)
+    o_loop = lvg.LouvainOptions()
+    states = []
+    for gi, G in enumerate(graphs):
+        m, vt, ct = sv.state(ids[gi])
+        a, b = lvg.State(G), lvg.State(G)
+        a.set(m, vt, ct)
+        states.append([a, b])
+    t0 = time.perf_counter()
+    for k in range(nb):
+        gi = int(lwhich[k])
+        G = graphs[gi]
+        tb = G.apply_batch(lpays[k])
+        db = lvg.DeviceBatch(G, tb)
+        lvg.run_resident(G, lvg.METHOD_FRONTIER, db, states[gi][0], states[gi][1], o_loop)
+        states[gi].reverse()
+        db.close()
+    loop_s = time.perf_counter() - t0
+    loop_entries = int(sum(p.num_deletions + p.num_insertions for p in lpays))
+    del states
     line = {
         "metric": "serving p99 update latency (tidy + apply + DF per request)", "value": st["p99_ms"],
         "unit": "ms", "n_gpus": world, "steps": n_req, "warmup": len(ids), "ms_per_step": st["mean_ms"],
@@ -601,6 +628,9 @@ def run_serving(args):
         "updates_per_s": st["updates_per_s"], "requests_per_s": st["requests_per_s"],
         "offered_requests_per_s": n_req / offered_s, "completed": st["completed"], "failed": st["failed"],
         "sweep": sweep,
+        "one_at_a_time": {"requests": nb, "requests_per_s": nb / loop_s, "batch_entries_per_s": loop_entries / loop_s,
+                          "call": "Graph.apply_batch + lvg_run_resident (DF), one request after another"},
+        "requests_per_s_vs_one_at_a_time": st["requests_per_s"] / (nb / loop_s),
         "clocks": clk.summary(),
     }
     sv.close()

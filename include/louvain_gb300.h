@@ -175,6 +175,14 @@ int lvg_modularity(lvg_graph *g, const uint32_t *membership, double M, double R,
 /* Total edge weight of g (FP64 on the GPU). Replaces edgeWeightOmp
  * (inc/properties.hxx:96). */
 int lvg_edge_weight(lvg_graph *g, double *out);
+/* louvainVertexWeightsOmpW (inc/louvain.hxx:210-218): vtot[u] = sum of u's
+ * edge weights (self-loops included), accumulated in FP64; vtot[span]. */
+int lvg_vertex_weights(lvg_graph *g, double *vtot);
+/* louvainCommunityWeightsOmpW (inc/louvain.hxx:247-256) and the totals of
+ * louvainInitializeFromOmpW (:325-335): ctot[c] = sum of vtot[u] over the
+ * vertices u with membership[u] == c, in FP64; vtot NULL = the graph's
+ * vertex weights. membership, vtot, ctot: [span]; ids must be < span. */
+int lvg_community_weights(lvg_graph *g, const uint32_t *membership, const double *vtot, double *ctot);
 
 /* Pinned host memory for result buffers and batches (no reference counterpart). */
 void *lvg_host_alloc(size_t bytes);
@@ -405,6 +413,10 @@ typedef struct lvg_tuning {
   uint32_t hub_chunk;          /* edges per chunk of a vertex above degree 8192 (256..1<<20; default 4096) */
   int      big_blocks_per_sm;  /* resident blocks per SM of the degree 513-8192 kernels (0 = as many
                                   as fit; default 0) */
+  double   frontier_max_fraction;  /* frontier_colors applies to batches of at most this many
+                                      entries per edge of the graph; larger batches (whose
+                                      frontiers cover much of the graph) keep 8 classes
+                                      (default 1e-3) */
 } lvg_tuning;
 void lvg_tuning_default(lvg_tuning *t);
 int lvg_graph_get_tuning(const lvg_graph *g, lvg_tuning *t);
@@ -415,8 +427,9 @@ int lvg_graph_set_tuning(lvg_graph *g, const lvg_tuning *t);
  * Each candidate is run once to warm up and then `repeats` times; the
  * fastest (minimum of LouvainResult::time) is kept when it beats the current
  * choice by 2 %, and a frontier_colors candidate only when its modularity is
- * within 1e-3 of the default's. The result is set on the graph and returned
- * in *best (time in *best_ms). */
+ * within 1e-3 of the starting choice's. Two rounds over the knobs, the colour
+ * classes first. The result is set on the graph and returned in *best (time
+ * in *best_ms). */
 int lvg_autotune(lvg_graph *g, int method, const lvg_device_batch *b, const lvg_state *prior, const lvg_options *o,
                  int repeats, lvg_tuning *best, double *best_ms);
 int lvg_get_stats(const lvg_graph *g, lvg_stats *out);

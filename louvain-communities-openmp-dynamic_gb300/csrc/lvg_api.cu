@@ -175,6 +175,7 @@ inline lvg_tuning default_tuning() {
   t.fused_small = 1;
   t.hub_chunk = HUB_CHUNK;
   t.big_blocks_per_sm = 0;
+  t.frontier_max_fraction = 1e-3;
   return t;
 }
 
@@ -382,12 +383,15 @@ void build_hub_plan(lvg_graph *g, Level &lv, HubPlanBuffers &hb) {
 }
 
 // Colour classes of a run: the options' count, else 16 (deterministic), else
-// the graph's tuned count for the frontier methods, else 8.
-int colors_for(const lvg_options &o, int method, const lvg_tuning &t) {
+// the graph's tuned count for the frontier methods on batches of at most
+// frontier_max_fraction entries per edge, else 8.
+int colors_for(const lvg_options &o, int method, const lvg_tuning &t, size_t batch_entries = 0,
+               size_t edges = 0) {
   int k = o.colors;
   if (k <= 0) {
+    const bool small = double(batch_entries) <= t.frontier_max_fraction * double(edges);
     if (o.deterministic) k = DEFAULT_COLORS_SYNC;
-    else if (method == LVG_METHOD_FRONTIER || method == LVG_METHOD_DELTA) k = t.frontier_colors;
+    else if ((method == LVG_METHOD_FRONTIER || method == LVG_METHOD_DELTA) && small) k = t.frontier_colors;
     else k = DEFAULT_COLORS_ASYNC;
   }
   return k < 1 ? 1 : (k > MAX_COLORS ? MAX_COLORS : k);
@@ -804,7 +808,7 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
   const int L = o.maxIterations, P = o.maxPasses;
   const bool sync = o.deterministic != 0;
   const int rep = std::max(1, o.repeat);
-  const int K = colors_for(o, method, g->tuning);
+  const int K = colors_for(o, method, g->tuning, b.nd + b.ni, g->base.edges);
   if (g->base.colors != K) {
     compute_bins(g, g->base, g->deg.p, g->bins.p, W.binscratch.p, K);
     build_hub_plan(g, g->base, g->hubplan);
@@ -1533,6 +1537,8 @@ void check_tuning(const lvg_tuning &t) {
     throw Error(LVG_EINVAL, "tuning: frontier_colors out of 1..32");
   if (t.hub_chunk < 256 || t.hub_chunk > (1u << 20)) throw Error(LVG_EINVAL, "tuning: hub_chunk out of 256..2^20");
   if (t.big_blocks_per_sm < 0 || t.big_blocks_per_sm > 64) throw Error(LVG_EINVAL, "tuning: big_blocks_per_sm");
+  if (!(t.frontier_max_fraction >= 0 && t.frontier_max_fraction <= 1))
+    throw Error(LVG_EINVAL, "tuning: frontier_max_fraction out of 0..1");
 }
 
 // Set a graph's tuning: the hub plan of the uploaded level follows the chunk
@@ -2023,6 +2029,45 @@ int lvg_edge_weight(lvg_graph *g, double *out) {
   if (!g || !out) return lvg::fail(LVG_EINVAL, "null argument");
   *out = g->total_weight;
   return LVG_OK;
+}
+
+int lvg_vertex_weights(lvg_graph *g, double *vtot) {
+  lvg::AcctScope acct_(g ? &g->bytes : nullptr);
+  if (!g || !vtot) return lvg::fail(LVG_EINVAL, "null argument");
+  return lvg::guarded([&] {
+    LVG_CUDA(cudaSetDevice(g->device));
+    lvg::ensure_ws(g);
+    lvg::Workspace &W = *g->ws;
+    const size_t S = g->base.span;
+    W.stage_a.ensure(S);
+    lvg::launch_vertex_weights_f64(g->base, W.stage_a.p, g->stream);
+    LVG_CUDA(cudaMemcpyAsync(vtot, W.stage_a.p, S * 8, cudaMemcpyDeviceToHost, g->stream));
+    LVG_CUDA(cudaStreamSynchronize(g->stream));
+    return LVG_OK;
+  });
+}
+
+int lvg_community_weights(lvg_graph *g, const uint32_t *membership, const double *vtot, double *ctot) {
+  lvg::AcctScope acct_(g ? &g->bytes : nullptr);
+  if (!g || !membership || !ctot) return lvg::fail(LVG_EINVAL, "null argument");
+  return lvg::guarded([&] {
+    LVG_CUDA(cudaSetDevice(g->device));
+    const size_t S = g->base.span;
+    for (size_t u = 0; u < S; ++u)
+      if (membership[u] >= S) throw lvg::Error(LVG_EINVAL, "membership id >= span");
+    lvg::ensure_ws(g);
+    lvg::Workspace &W = *g->ws;
+    cudaStream_t s = g->stream;
+    W.stage_a.ensure(S);
+    W.stage_b.ensure(S);
+    LVG_CUDA(cudaMemcpyAsync(W.com_next.p, membership, S * 4, cudaMemcpyHostToDevice, s));
+    if (vtot) LVG_CUDA(cudaMemcpyAsync(W.stage_a.p, vtot, S * 8, cudaMemcpyHostToDevice, s));
+    else lvg::launch_vertex_weights_f64(g->base, W.stage_a.p, s);
+    lvg::launch_community_weights_f64(W.com_next.p, W.stage_a.p, S, W.stage_b.p, s);
+    LVG_CUDA(cudaMemcpyAsync(ctot, W.stage_b.p, S * 8, cudaMemcpyDeviceToHost, s));
+    LVG_CUDA(cudaStreamSynchronize(s));
+    return LVG_OK;
+  });
 }
 
 int lvg_modularity(lvg_graph *g, const uint32_t *membership, double M, double R, double *out) {
@@ -2518,11 +2563,15 @@ int lvg_autotune(lvg_graph *g, int method, const lvg_device_batch *b, const lvg_
         }
       }
     };
-    try_knob([](lvg_tuning &t, long v) { t.hub_chunk = uint32_t(v); }, {2048, 4096, 8192, 16384}, false);
-    try_knob([](lvg_tuning &t, long v) { t.concurrent_bins = int(v); }, {1, 0}, false);
-    try_knob([](lvg_tuning &t, long v) { t.fused_small = int(v); }, {1, 0}, false);
-    try_knob([](lvg_tuning &t, long v) { t.big_blocks_per_sm = int(v); }, {0, 2, 3, 4}, false);
-    if (colours) try_knob([](lvg_tuning &t, long v) { t.frontier_colors = int(v); }, {8, 4, 2, 1}, true);
+    // the class count first (the largest effect), then the launch shapes; twice,
+    // since each knob's best value can depend on the others
+    for (int round = 0; round < 2; ++round) {
+      if (colours) try_knob([](lvg_tuning &t, long v) { t.frontier_colors = int(v); }, {8, 4, 2, 1}, true);
+      try_knob([](lvg_tuning &t, long v) { t.hub_chunk = uint32_t(v); }, {2048, 4096, 8192, 16384}, false);
+      try_knob([](lvg_tuning &t, long v) { t.concurrent_bins = int(v); }, {1, 0}, false);
+      try_knob([](lvg_tuning &t, long v) { t.fused_small = int(v); }, {1, 0}, false);
+      try_knob([](lvg_tuning &t, long v) { t.big_blocks_per_sm = int(v); }, {0, 2, 3, 4}, false);
+    }
     apply_tuning(g, cur);
     if (best) *best = cur;
     if (best_ms) *best_ms = tcur;

@@ -263,6 +263,9 @@ void launch_fill_u8(uint8_t *p, uint8_t v, size_t n, cudaStream_t s);
 void launch_fill_f32(float *p, size_t n, float v, cudaStream_t s);
 void launch_init_static(const Level &g, uint32_t *ucom, float *utot, float *ctot, cudaStream_t s);
 void launch_total_weight(const float *w, size_t n, Counters *ctr, cudaStream_t s);  // -> ctr->fp64[0]
+// louvainVertexWeightsOmpW / louvainCommunityWeightsOmpW in FP64 (the C-ABI utilities).
+void launch_vertex_weights_f64(const Level &g, double *vtot, cudaStream_t s);
+void launch_community_weights_f64(const uint32_t *q, const double *vtot, size_t n, double *ctot, cudaStream_t s);
 void launch_prior_to_f32(const double *src, float *dst, size_t n, cudaStream_t s);
 void launch_f32_to_f64(const float *src, double *dst, size_t n, cudaStream_t s);
 void launch_batch_weights(const uint32_t *src, const float *w, size_t n, float sign, const uint32_t *vcom,

@@ -74,6 +74,27 @@ __global__ void total_weight_kernel(const float *w, size_t m, double *dst) {
   block_add_double(s, dst);
 }
 
+// louvainVertexWeightsOmpW in FP64: a warp per row.
+__global__ void vertex_weights_f64_kernel(const uint64_t *off, const uint32_t *deg, const float *w, const uint8_t *ex,
+                                          size_t n, double *vtot) {
+  const size_t warps = size_t(gridDim.x) * blockDim.x / 32;
+  const int lane = threadIdx.x & 31;
+  for (size_t u = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32; u < n; u += warps) {
+    double s = 0;
+    if (!ex || ex[u]) {
+      const uint64_t o = off[u];
+      for (uint32_t j = lane; j < deg[u]; j += 32) s += double(w[o + j]);
+      s = warp_sum_d(s);
+    }
+    if (lane == 0) vtot[u] = s;
+  }
+}
+
+// louvainCommunityWeightsOmpW in FP64: ctot[q[u]] += vtot[u].
+__global__ void community_weights_f64_kernel(const uint32_t *q, const double *vtot, size_t n, double *ctot) {
+  GRID_STRIDE(u, n) if (vtot[u] != 0.0) atomicAdd(&ctot[q[u]], vtot[u]);
+}
+
 __global__ void fill_f32_kernel(float *p, size_t n, float v) {
   GRID_STRIDE(i, n) p[i] = v;
 }
@@ -493,6 +514,19 @@ void launch_init_static(const Level &g, uint32_t *ucom, float *utot, float *ctot
   if (!g.span) return;
   init_static_kernel<<<grid_for(g.span * 32, 256), 256, 0, s>>>(g.off, g.deg, g.w, g.ex, g.span, g.gid, g.gbase,
                                                                  ucom, utot, ctot);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_vertex_weights_f64(const Level &g, double *vtot, cudaStream_t s) {
+  if (!g.span) return;
+  vertex_weights_f64_kernel<<<grid_for(g.span * 32, 256), 256, 0, s>>>(g.off, g.deg, g.w, g.ex, g.span, vtot);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_community_weights_f64(const uint32_t *q, const double *vtot, size_t n, double *ctot, cudaStream_t s) {
+  LVG_CUDA(cudaMemsetAsync(ctot, 0, n * sizeof(double), s));
+  if (!n) return;
+  community_weights_f64_kernel<<<grid_for(n, 256), 256, 0, s>>>(q, vtot, n, ctot);
   LVG_CHECK_LAUNCH();
 }
 

@@ -101,7 +101,7 @@ class _ServerStats(C.Structure):
 
 class _Tuning(C.Structure):
     _fields_ = [("frontier_colors", C.c_int), ("concurrent_bins", C.c_int), ("fused_small", C.c_int),
-                ("hub_chunk", C.c_uint32), ("big_blocks_per_sm", C.c_int)]
+                ("hub_chunk", C.c_uint32), ("big_blocks_per_sm", C.c_int), ("frontier_max_fraction", C.c_double)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -228,6 +228,8 @@ def load_library() -> C.CDLL:
     L.lvg_server_destroy.argtypes = [vp]
     L.lvg_static_many.argtypes = [C.POINTER(vp), sz, C.POINTER(_Options), i32, i32, C.POINTER(_Result)]
     L.lvg_graph_create_union.argtypes = [C.POINTER(vp), sz, C.POINTER(vp)]
+    L.lvg_vertex_weights.argtypes = [vp, vp]
+    L.lvg_community_weights.argtypes = [vp, vp, vp, vp]
     L.lvg_union_graphs.argtypes = [vp, C.POINTER(sz)]
     L.lvg_static_union.argtypes = [vp, C.POINTER(_Options), C.POINTER(_Result)]
     _lib = L
@@ -608,6 +610,22 @@ class Graph:
         G = Graph(None)
         _check(self._L.lvg_graph_clone(self.h, C.byref(G.h)))
         return G
+
+    def vertex_weights(self) -> np.ndarray:
+        """louvainVertexWeightsOmpW in FP64 (lvg_vertex_weights)."""
+        out = np.zeros(self.span, np.float64)
+        _check(self._L.lvg_vertex_weights(self.h, out.ctypes.data))
+        return out
+
+    def community_weights(self, membership, vtot=None) -> np.ndarray:
+        """louvainCommunityWeightsOmpW in FP64 (lvg_community_weights); vtot None = the
+        graph's vertex weights."""
+        m = np.ascontiguousarray(membership, np.uint32)
+        v = None if vtot is None else np.ascontiguousarray(vtot, np.float64)
+        out = np.zeros(self.span, np.float64)
+        _check(self._L.lvg_community_weights(self.h, m.ctypes.data, None if v is None else v.ctypes.data,
+                                             out.ctypes.data))
+        return out
 
     @classmethod
     def union(cls, graphs: "list[Graph]") -> "Graph":

@@ -44,6 +44,17 @@ def test_vertex_weights_bit_exact(cuda, golden, dev):
     assert r.passes == 0 and r.iterations == 0
 
 
+def test_vertex_and_community_weight_utilities(cuda, golden, dev):
+    # louvainVertexWeightsOmpW and louvainCommunityWeightsOmpW through the C-ABI utilities
+    X, _ = dev
+    vt = X.vertex_weights()
+    assert np.array_equal(vt, golden["x_vtot"])
+    m = golden["static_m"]
+    expect = np.bincount(m, weights=golden["x_vtot"], minlength=golden.x.span)
+    assert np.array_equal(X.community_weights(m), expect)
+    assert np.array_equal(X.community_weights(m, 2 * vt), 2 * expect)
+
+
 def test_batch_weight_update_bit_exact(cuda, golden, dev):
     _, Y = dev
     r = cuda.louvain_dynamic_frontier(Y, golden.b, *prior(golden), cuda.LouvainOptions(maxPasses=0))
@@ -206,3 +217,18 @@ def test_empty_batch_and_empty_graph(cuda, golden, dev):
     r = cuda.louvain_static(G)
     assert r.passes == 0 and r.iterations == 0
     assert r.membership.tolist() == [0] + list(range(1, S))
+
+
+def test_pinned_result_buffers_match(cuda, golden, dev):
+    # Into pinned result arrays the vertex weights are copied out on a side
+    # stream during the run; the results must equal those into pageable arrays.
+    _, Y = dev
+    S = golden.y.span
+    o = cuda.LouvainOptions(deterministic=True)
+    ref = cuda.louvain_dynamic_frontier(Y, golden.b, *prior(golden), o)
+    bufs = [cuda.PinnedArray(S, np.uint32), cuda.PinnedArray(S, np.float64), cuda.PinnedArray(S, np.float64)]
+    for _ in range(2):
+        r = cuda.louvain_dynamic_frontier(Y, golden.b, *prior(golden), o, out_buffers=[b.array for b in bufs])
+        assert np.array_equal(r.membership, ref.membership)
+        assert np.array_equal(r.vertexWeight, ref.vertexWeight)
+        assert np.array_equal(r.communityWeight, ref.communityWeight)

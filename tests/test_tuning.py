@@ -12,7 +12,8 @@ import pytest
 
 def test_tuning_defaults(lvg):
     t = lvg.tuning_default()
-    assert t == dict(frontier_colors=8, concurrent_bins=1, fused_small=1, hub_chunk=4096, big_blocks_per_sm=0)
+    assert t == dict(frontier_colors=8, concurrent_bins=1, fused_small=1, hub_chunk=4096, big_blocks_per_sm=0,
+                     frontier_max_fraction=1e-3)
 
 
 @pytest.fixture(scope="module")
@@ -43,7 +44,8 @@ def test_launch_knobs_keep_deterministic_results(cuda, hubcase):
 @pytest.mark.gpu
 def test_invalid_tuning_is_rejected(cuda, hubcase):
     Y = cuda.Graph(hubcase[2])
-    for bad in [dict(hub_chunk=100), dict(frontier_colors=0), dict(frontier_colors=33), dict(big_blocks_per_sm=-1)]:
+    for bad in [dict(hub_chunk=100), dict(frontier_colors=0), dict(frontier_colors=33), dict(big_blocks_per_sm=-1),
+                dict(frontier_max_fraction=2.0)]:
         with pytest.raises(RuntimeError):
             cuda.set_tuning(Y, **bad)
     assert cuda.get_tuning(Y) == cuda.tuning_default()
