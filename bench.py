@@ -324,7 +324,7 @@ def run_gpu(args):
     tune_s = 0.0
     if not args.no_tune:
         t0 = time.perf_counter()
-        tuning, _ = lvg.autotune(Y, lvg.METHOD_FRONTIER, db, st_prior, o, repeats=3)
+        tuning, _ = lvg.autotune(Y, lvg.METHOD_FRONTIER, db, st_prior, o, repeats=5)
         tune_s = time.perf_counter() - t0
 
     if args.ncu_steps:
