@@ -854,7 +854,8 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
         ensure_global_tables(W, size_t(global_table_blocks(b.ni)), dlog, true);
       }
       launch_ds_mark(g->base, b.ds, b.dd, b.nd, b.is, b.id, b.iw, b.ni, b.seg, b.ni, ucom, utot, ctot, M, R,
-                     W.fv.p, W.fn.p, W.fc.p, W.gkeys.p, W.gvals.p, W.gfirst.p, dlog, g->ctr.p, s);
+                     W.fv.p, W.fn.p, W.fc.p, W.gkeys.p, W.gvals.p, W.gfirst.p, dlog, g->ctr.p, W.wl.p,
+                     W.wl_count.p, s);
       LVG_CUDA(cudaMemcpyAsync(W.vaff.p, W.fv.p, S, cudaMemcpyDeviceToDevice, s));
       fa = W.fv.p;
     }

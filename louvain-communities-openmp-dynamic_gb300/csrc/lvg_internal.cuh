@@ -276,7 +276,7 @@ void launch_ds_mark(const Level &g, const uint32_t *ds, const uint32_t *dd, size
                     const uint32_t *id, const float *iw, size_t ni, const uint32_t *seg, size_t nseg,
                     const uint32_t *vcom, const float *vtot, const float *ctot, double M, double R,
                     uint8_t *vertices, uint8_t *neighbors, uint8_t *communities, uint32_t *gkeys, float *gvals,
-                    uint32_t *gfirst, int glog2, Counters *ctr, cudaStream_t s);
+                    uint32_t *gfirst, int glog2, Counters *ctr, uint32_t *list, uint32_t *count, cudaStream_t s);
 void launch_clear_isolated(const uint32_t *list, size_t n, uint8_t *vaff, const uint8_t *fa, cudaStream_t s);
 struct IsolatedLists {
   const uint32_t *list[MAX_COLORS];

@@ -188,8 +188,11 @@ __global__ void __launch_bounds__(DS_BLOCK) ds_ins_kernel(const uint32_t *is, co
       if (is[mid] <= u) lo = mid + 1; else hi = mid;
     }
     const size_t s1 = lo, len = s1 - s0;
+    if (len <= 32) continue;  // ds_ins_warp_kernel's (block-uniform)
     const bool global = len * 2 > (size_t(1) << DS_LOG);
-    const int lg = global ? glog2 : DS_LOG;
+    // a table sized for the segment: most sources have one or two insertions,
+    // and clearing and scanning a fixed 2048-slot table per source dominated
+    const int lg = global ? glog2 : max(1, ceil_log2(2 * len));
     const uint32_t cap = 1u << lg, mask = cap - 1u;
     uint32_t *keys = global ? gkeys + size_t(blockIdx.x) * cap : skeys;
     float *vals = global ? gvals + size_t(blockIdx.x) * cap : svals;
@@ -253,26 +256,87 @@ __global__ void __launch_bounds__(DS_BLOCK) ds_ins_kernel(const uint32_t *is, co
   }
 }
 
-// Delta-screening expansion (inc/louvain.hxx:1480-1485): neighbours of flagged
-// sources, and members of flagged communities. One warp per vertex.
-__global__ void ds_expand_kernel(const uint64_t *off, const uint32_t *deg, const uint32_t *key, const uint8_t *ex,
-                                 size_t n, const uint32_t *vcom, const uint8_t *neighbors,
-                                 const uint8_t *communities, uint8_t *vertices) {
-  const size_t warps = size_t(gridDim.x) * blockDim.x / 32;
+// The same for sources with at most 32 insertions (nearly all of them): a
+// warp per source, lane k holding insertion k; lanes of the same community
+// sum their weights in batch order and the lowest of them (the community's
+// first insertion) carries it into the argmax.
+__global__ void ds_ins_warp_kernel(const uint32_t *is, const uint32_t *id, const float *iw, size_t ni,
+                                   const uint32_t *seg, const unsigned int *nseg, const uint32_t *vcom,
+                                   const float *vtot, const float *ctot, double M, double R, uint8_t *vertices,
+                                   uint8_t *neighbors, uint8_t *communities) {
+  const unsigned ns = *nseg;
   const int lane = threadIdx.x & 31;
-  for (size_t base = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32 * 32; base < n; base += warps * 32) {
-    const size_t u0 = base + lane;
-    const bool has = u0 < n && (!ex || ex[u0]);
-    if (has && communities[vcom[u0]]) vertices[u0] = 1;
-    unsigned todo = __ballot_sync(0xffffffffu, has && neighbors[u0]);
-    while (todo) {
-      const int l = __ffs(todo) - 1;
-      todo &= todo - 1;
-      const size_t u = base + l;
-      const uint64_t o = off[u];
-      const uint32_t d = deg[u];
-      for (uint32_t j = lane; j < d; j += 32) vertices[key[o + j]] = 1;
+  const size_t warps = size_t(gridDim.x) * blockDim.x / 32;
+  for (size_t sidx = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32; sidx < ns; sidx += warps) {
+    const size_t s0 = seg[sidx];
+    const uint32_t u = is[s0];
+    const size_t j = s0 + 1 + lane;
+    const unsigned past = __ballot_sync(0xffffffffu, j >= ni || is[j] != u);
+    if (!past) continue;  // more than 32 insertions: ds_ins_kernel's (warp-uniform)
+    const uint32_t len = uint32_t(__ffs(past));  // 1 + the lanes still in the segment
+    const uint32_t d = vcom[u];
+    uint32_t c = EMPTY;
+    float w = 0.f;
+    if (uint32_t(lane) < len) {
+      c = vcom[id[s0 + lane]];
+      w = iw[s0 + lane];
+      if (c == d) c = EMPTY;
     }
+    const unsigned grp = __match_any_sync(0xffffffffu, c);
+    float sum = 0.f;
+    for (unsigned r = grp; r; r &= r - 1u) sum += __shfl_sync(grp, w, __ffs(r) - 1);
+    const bool leader = c != EMPTY && (grp & ((1u << lane) - 1u)) == 0u;
+    double be = 0;
+    uint32_t bf = 0xffffffffu, bc = 0;
+    if (leader) {
+      const double e = delta_modularity(double(sum), 0.0, double(vtot[u]), double(ctot[c]), double(ctot[d]), M, R);
+      if (e > 0) { be = e; bf = uint32_t(lane); bc = c; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double oe = __shfl_xor_sync(0xffffffffu, be, o);
+      const uint32_t of = __shfl_xor_sync(0xffffffffu, bf, o);
+      const uint32_t oc = __shfl_xor_sync(0xffffffffu, bc, o);
+      if (oe > be || (oe == be && oe > 0 && of < bf)) { be = oe; bf = of; bc = oc; }
+    }
+    if (lane == 0 && be > 0) {
+      vertices[u] = 1;
+      neighbors[u] = 1;
+      communities[bc] = 1;
+    }
+  }
+}
+
+// Delta-screening expansion (inc/louvain.hxx:1480-1485): members of flagged
+// communities (a thread per vertex), and the vertices flagged for their
+// neighbours, listed for ds_neighbors_kernel.
+__global__ void ds_expand_kernel(const uint8_t *ex, size_t n, const uint32_t *vcom, const uint8_t *neighbors,
+                                 const uint8_t *communities, uint8_t *vertices, uint32_t *list, uint32_t *count) {
+  const int lane = threadIdx.x & 31;
+  for (size_t base = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32 * 32; base < n;
+       base += size_t(gridDim.x) * blockDim.x) {
+    const size_t u = base + lane;
+    const bool has = u < n && (!ex || ex[u]);
+    if (has && communities[vcom[u]]) vertices[u] = 1;
+    const bool nb = has && neighbors[u];
+    const unsigned m = __ballot_sync(0xffffffffu, nb);
+    uint32_t at = 0;
+    if (m && lane == __ffs(m) - 1) at = atomicAdd(count, uint32_t(__popc(m)));
+    at = __shfl_sync(0xffffffffu, at, __ffs(m ? m : 1u) - 1);
+    if (nb) list[at + __popc(m & ((1u << lane) - 1u))] = uint32_t(u);
+  }
+}
+
+// The neighbours of the listed vertices: a block per vertex, so a hub's
+// adjacency is spread over a block rather than a warp.
+__global__ void ds_neighbors_kernel(const uint64_t *off, const uint32_t *deg, const uint32_t *key,
+                                    const uint32_t *list, const uint32_t *count, uint8_t *vertices) {
+  const uint32_t n = *count;
+  for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
+    const uint32_t u = list[i];
+    const uint64_t o = off[u];
+    const uint32_t d = deg[u];
+    for (uint32_t j = threadIdx.x; j < d; j += blockDim.x) vertices[key[o + j]] = 1;
   }
 }
 
@@ -567,7 +631,7 @@ void launch_ds_mark(const Level &g, const uint32_t *ds, const uint32_t *dd, size
                     const uint32_t *id, const float *iw, size_t ni, const uint32_t *seg, size_t nseg_cap,
                     const uint32_t *vcom, const float *vtot, const float *ctot, double M, double R,
                     uint8_t *vertices, uint8_t *neighbors, uint8_t *communities, uint32_t *gkeys, float *gvals,
-                    uint32_t *gfirst, int glog2, Counters *ctr, cudaStream_t s) {
+                    uint32_t *gfirst, int glog2, Counters *ctr, uint32_t *list, uint32_t *count, cudaStream_t s) {
   (void)nseg_cap;
   if (nd) {
     ds_del_kernel<<<grid_for(nd, 256), 256, 0, s>>>(ds, dd, nd, vcom, vertices, neighbors, communities);
@@ -578,14 +642,20 @@ void launch_ds_mark(const Level &g, const uint32_t *ds, const uint32_t *dd, size
     LVG_CUDA(cudaMemsetAsync(nseg, 0, sizeof(unsigned int), s));
     ds_heads_kernel<<<grid_for(ni, 256), 256, 0, s>>>(is, ni, const_cast<uint32_t *>(seg), nseg);
     LVG_CHECK_LAUNCH();
+    ds_ins_warp_kernel<<<grid_for(ni * 32, 256), 256, 0, s>>>(is, id, iw, ni, seg, nseg, vcom, vtot, ctot, M, R,
+                                                                vertices, neighbors, communities);
+    LVG_CHECK_LAUNCH();
     ds_ins_kernel<<<global_table_blocks(ni), DS_BLOCK, 0, s>>>(is, id, iw, ni, seg, nseg, vcom, vtot, ctot, M, R,
                                                               vertices, neighbors, communities, gkeys, gvals,
                                                               gfirst, glog2, ctr);
     LVG_CHECK_LAUNCH();
   }
   if (g.span) {
-    ds_expand_kernel<<<grid_for(g.span, 256), 256, 0, s>>>(g.off, g.deg, g.key, g.ex, g.span, vcom, neighbors,
-                                                            communities, vertices);
+    LVG_CUDA(cudaMemsetAsync(count, 0, sizeof(uint32_t), s));
+    ds_expand_kernel<<<grid_for(g.span, 256), 256, 0, s>>>(g.ex, g.span, vcom, neighbors, communities, vertices,
+                                                            list, count);
+    LVG_CHECK_LAUNCH();
+    ds_neighbors_kernel<<<unsigned(sms()) * 16, 256, 0, s>>>(g.off, g.deg, g.key, list, count, vertices);
     LVG_CHECK_LAUNCH();
   }
 }

@@ -232,3 +232,31 @@ def test_pinned_result_buffers_match(cuda, golden, dev):
         assert np.array_equal(r.membership, ref.membership)
         assert np.array_equal(r.vertexWeight, ref.vertexWeight)
         assert np.array_equal(r.communityWeight, ref.communityWeight)
+
+
+def test_delta_screening_flags_with_large_source_groups(cuda, orc):
+    # Sources with more than 32 inserted edges take the block path of the
+    # insertion screening, the others the warp path; both equal the reference.
+    x = cuda.planted_partition(3000, 64, 10, 0.8, seed=21)
+    rb = cuda.random_batch(x, 400, 0.8, seed=22)
+    rng = np.random.default_rng(23)
+    extra_s, extra_d = [], []
+    for src, k in ((1, 120), (2, 40), (3, 33), (4, 32)):
+        for v in rng.choice(np.arange(5, 3001), k, replace=False):
+            extra_s += [src, v]
+            extra_d += [v, src]
+    raw = cuda.HostBatch(rb.del_src, rb.del_dst, rb.del_w,
+                         np.concatenate([rb.ins_src, np.array(extra_s, np.uint32)]),
+                         np.concatenate([rb.ins_dst, np.array(extra_d, np.uint32)]),
+                         np.ones(len(rb.ins_src) + len(extra_s), np.float32))
+    X = cuda.Graph(x)
+    p = cuda.louvain_static(X, cuda.LouvainOptions(deterministic=True))
+    Y = X.clone()
+    tb = Y.apply_batch(raw)
+    q = (p.membership, p.vertexWeight, p.communityWeight)
+    upd = cuda.louvain_dynamic_frontier(Y, tb, *q, cuda.LouvainOptions(maxPasses=0))
+    v, n, c = cuda.affected_vertices(Y, cuda.METHOD_DELTA, tb, *q)
+    rv, rn, rc = orc.ds_mark(Y.download(), tb, p.membership, upd.vertexWeight, upd.communityWeight,
+                             Y.edge_weight() / 2)
+    assert np.array_equal(v, rv) and np.array_equal(n, rn) and np.array_equal(c, rc)
+    assert n[1] or n[2] or n[3] or c.any()  # the large groups were screened
