@@ -144,10 +144,19 @@ __global__ void ds_del_kernel(const uint32_t *ds, const uint32_t *dd, size_t nd,
   }
 }
 
-// Segment heads of the source-sorted insertions.
+// Segment heads of the source-sorted insertions (appended in no particular
+// order; one counter atomic per warp).
 __global__ void ds_heads_kernel(const uint32_t *is, size_t ni, uint32_t *seg, unsigned int *nseg) {
-  GRID_STRIDE(i, ni) {
-    if (i == 0 || is[i] != is[i - 1]) seg[atomicAdd(nseg, 1u)] = uint32_t(i);
+  const int lane = threadIdx.x & 31;
+  for (size_t base = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32 * 32; base < ni;
+       base += size_t(gridDim.x) * blockDim.x) {
+    const size_t i = base + lane;
+    const bool head = i < ni && (i == 0 || is[i] != is[i - 1]);
+    const unsigned m = __ballot_sync(0xffffffffu, head);
+    unsigned at = 0;
+    if (m && lane == __ffs(m) - 1) at = atomicAdd(nseg, unsigned(__popc(m)));
+    at = __shfl_sync(0xffffffffu, at, __ffs(m ? m : 1u) - 1);
+    if (head) seg[at + __popc(m & ((1u << lane) - 1u))] = uint32_t(i);
   }
 }
 
