@@ -138,6 +138,7 @@ struct Counters {
   unsigned long long bin_over[NUM_BINS];      // vertices redone with an HBM table per bin
   unsigned long long hub_chunk_over;          // hub chunks that wrote raw pairs
   unsigned int gactive;                       // graph unions: graphs still moving after an iteration
+  unsigned int ds_long;                       // delta-screening sources with more than 32 insertions
 };
 
 // Per-graph control of a graph-union run (lvg_static_union), on the device:
@@ -272,6 +273,8 @@ void launch_batch_weights(const uint32_t *src, const float *w, size_t n, float s
                           float *vtot, float *ctot, cudaStream_t s);
 void launch_df_mark(const uint32_t *ds, const uint32_t *dd, size_t nd, const uint32_t *is, const uint32_t *id,
                     size_t ni, const uint32_t *vcom, uint8_t *vaff, cudaStream_t s);
+// seg: ni entries (segment heads, then the sources with more than 32
+// insertions); list: g.span entries; count: 2 entries.
 void launch_ds_mark(const Level &g, const uint32_t *ds, const uint32_t *dd, size_t nd, const uint32_t *is,
                     const uint32_t *id, const float *iw, size_t ni, const uint32_t *seg, size_t nseg,
                     const uint32_t *vcom, const float *vtot, const float *ctot, double M, double R,

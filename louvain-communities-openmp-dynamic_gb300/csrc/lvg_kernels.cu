@@ -173,34 +173,35 @@ __device__ __forceinline__ double delta_modularity(double vcout, double vdout, d
 // batch sized; it makes the flags match the reference bit for bit.
 constexpr int DS_BLOCK = 128;
 constexpr int DS_LOG = 11;  // shared table: 2048 slots, sources with <= 1024 insertions
+// The sources with more than 32 insertions come listed by ds_ins_warp_kernel
+// after the segment heads (seg[ns + k] = first insertion of long source k).
 __global__ void __launch_bounds__(DS_BLOCK) ds_ins_kernel(const uint32_t *is, const uint32_t *id, const float *iw,
                                                           size_t ni, const uint32_t *seg, const unsigned int *nseg,
-                                                          const uint32_t *vcom, const float *vtot,
-                                                          const float *ctot, double M, double R, uint8_t *vertices,
-                                                          uint8_t *neighbors, uint8_t *communities,
-                                                          uint32_t *gkeys, float *gvals, uint32_t *gfirst, int glog2,
-                                                          Counters *ctr) {
+                                                          const unsigned int *nlong, const uint32_t *vcom,
+                                                          const float *vtot, const float *ctot, double M, double R,
+                                                          uint8_t *vertices, uint8_t *neighbors,
+                                                          uint8_t *communities, uint32_t *gkeys, float *gvals,
+                                                          uint32_t *gfirst, int glog2, Counters *ctr) {
   __shared__ uint32_t skeys[1 << DS_LOG];
   __shared__ float svals[1 << DS_LOG];
   __shared__ uint32_t sfirst[1 << DS_LOG];
   __shared__ double rb[DS_BLOCK / 32];
   __shared__ uint32_t rf[DS_BLOCK / 32], rc[DS_BLOCK / 32];
-  const unsigned ns = *nseg;
+  const unsigned ns = *nseg, nl = *nlong;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (unsigned sidx = blockIdx.x; sidx < ns; sidx += gridDim.x) {
-    const size_t s0 = seg[sidx];
+  for (unsigned k = blockIdx.x; k < nl; k += gridDim.x) {
+    const size_t s0 = seg[ns + k];
     const uint32_t u = is[s0];
     // segment end: first index with a larger source (the batch is sorted)
-    size_t lo = s0, hi = ni;
+    size_t lo = s0 + 33, hi = ni;
     while (lo < hi) {
       size_t mid = (lo + hi) >> 1;
       if (is[mid] <= u) lo = mid + 1; else hi = mid;
     }
     const size_t s1 = lo, len = s1 - s0;
-    if (len <= 32) continue;  // ds_ins_warp_kernel's (block-uniform)
     const bool global = len * 2 > (size_t(1) << DS_LOG);
-    // a table sized for the segment: most sources have one or two insertions,
-    // and clearing and scanning a fixed 2048-slot table per source dominated
+    // a table sized for the segment: clearing and scanning all 2048 slots
+    // would cost more than the insertions of a source with a few dozen
     const int lg = global ? glog2 : max(1, ceil_log2(2 * len));
     const uint32_t cap = 1u << lg, mask = cap - 1u;
     uint32_t *keys = global ? gkeys + size_t(blockIdx.x) * cap : skeys;
@@ -270,7 +271,7 @@ __global__ void __launch_bounds__(DS_BLOCK) ds_ins_kernel(const uint32_t *is, co
 // sum their weights in batch order and the lowest of them (the community's
 // first insertion) carries it into the argmax.
 __global__ void ds_ins_warp_kernel(const uint32_t *is, const uint32_t *id, const float *iw, size_t ni,
-                                   const uint32_t *seg, const unsigned int *nseg, const uint32_t *vcom,
+                                   uint32_t *seg, const unsigned int *nseg, unsigned int *nlong, const uint32_t *vcom,
                                    const float *vtot, const float *ctot, double M, double R, uint8_t *vertices,
                                    uint8_t *neighbors, uint8_t *communities) {
   const unsigned ns = *nseg;
@@ -281,7 +282,12 @@ __global__ void ds_ins_warp_kernel(const uint32_t *is, const uint32_t *id, const
     const uint32_t u = is[s0];
     const size_t j = s0 + 1 + lane;
     const unsigned past = __ballot_sync(0xffffffffu, j >= ni || is[j] != u);
-    if (!past) continue;  // more than 32 insertions: ds_ins_kernel's (warp-uniform)
+    if (!past) {  // more than 32 insertions: listed for ds_ins_kernel (warp-uniform)
+      // ns segments of which L have 33 or more insertions: ns + L <= ni, the
+      // capacity of seg
+      if (lane == 0) seg[ns + atomicAdd(nlong, 1u)] = uint32_t(s0);
+      continue;
+    }
     const uint32_t len = uint32_t(__ffs(past));  // 1 + the lanes still in the segment
     const uint32_t d = vcom[u];
     uint32_t c = EMPTY;
@@ -318,9 +324,13 @@ __global__ void ds_ins_warp_kernel(const uint32_t *is, const uint32_t *id, const
 
 // Delta-screening expansion (inc/louvain.hxx:1480-1485): members of flagged
 // communities (a thread per vertex), and the vertices flagged for their
-// neighbours, listed for ds_neighbors_kernel.
-__global__ void ds_expand_kernel(const uint8_t *ex, size_t n, const uint32_t *vcom, const uint8_t *neighbors,
-                                 const uint8_t *communities, uint8_t *vertices, uint32_t *list, uint32_t *count) {
+// neighbours, listed for ds_neighbors_kernel: those of degree up to
+// DS_WARP_DEG from the front of the list (count[0]), the others from its back
+// (count[1]); the list holds n entries.
+constexpr uint32_t DS_WARP_DEG = 256;
+__global__ void ds_expand_kernel(const uint8_t *ex, size_t n, const uint32_t *vcom, const uint32_t *deg,
+                                 const uint8_t *neighbors, const uint8_t *communities, uint8_t *vertices,
+                                 uint32_t *list, uint32_t *count) {
   const int lane = threadIdx.x & 31;
   for (size_t base = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32 * 32; base < n;
        base += size_t(gridDim.x) * blockDim.x) {
@@ -328,24 +338,38 @@ __global__ void ds_expand_kernel(const uint8_t *ex, size_t n, const uint32_t *vc
     const bool has = u < n && (!ex || ex[u]);
     if (has && communities[vcom[u]]) vertices[u] = 1;
     const bool nb = has && neighbors[u];
-    const unsigned m = __ballot_sync(0xffffffffu, nb);
-    uint32_t at = 0;
-    if (m && lane == __ffs(m) - 1) at = atomicAdd(count, uint32_t(__popc(m)));
+    const bool big = nb && deg[u] > DS_WARP_DEG;
+    const unsigned m = __ballot_sync(0xffffffffu, nb && !big), mb = __ballot_sync(0xffffffffu, big);
+    uint32_t at = 0, atb = 0;
+    if (m && lane == __ffs(m) - 1) at = atomicAdd(&count[0], uint32_t(__popc(m)));
+    if (mb && lane == __ffs(mb) - 1) atb = atomicAdd(&count[1], uint32_t(__popc(mb)));
     at = __shfl_sync(0xffffffffu, at, __ffs(m ? m : 1u) - 1);
-    if (nb) list[at + __popc(m & ((1u << lane) - 1u))] = uint32_t(u);
+    atb = __shfl_sync(0xffffffffu, atb, __ffs(mb ? mb : 1u) - 1);
+    const unsigned below = (1u << lane) - 1u;
+    if (nb && !big) list[at + __popc(m & below)] = uint32_t(u);
+    if (big) list[n - 1 - (atb + __popc(mb & below))] = uint32_t(u);
   }
 }
 
-// The neighbours of the listed vertices: a block per vertex, so a hub's
-// adjacency is spread over a block rather than a warp.
+// The neighbours of the listed vertices: a block per vertex above degree
+// DS_WARP_DEG (so a hub's adjacency is spread over a block), then a warp per
+// vertex for the rest.
 __global__ void ds_neighbors_kernel(const uint64_t *off, const uint32_t *deg, const uint32_t *key,
-                                    const uint32_t *list, const uint32_t *count, uint8_t *vertices) {
-  const uint32_t n = *count;
-  for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
-    const uint32_t u = list[i];
+                                    const uint32_t *list, const uint32_t *count, size_t n, uint8_t *vertices) {
+  const uint32_t nw = count[0], nb = count[1];
+  for (uint32_t i = blockIdx.x; i < nb; i += gridDim.x) {
+    const uint32_t u = list[n - 1 - i];
     const uint64_t o = off[u];
     const uint32_t d = deg[u];
     for (uint32_t j = threadIdx.x; j < d; j += blockDim.x) vertices[key[o + j]] = 1;
+  }
+  const int lane = threadIdx.x & 31;
+  const size_t warps = size_t(gridDim.x) * blockDim.x / 32;
+  for (size_t i = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32; i < nw; i += warps) {
+    const uint32_t u = list[i];
+    const uint64_t o = off[u];
+    const uint32_t d = deg[u];
+    for (uint32_t j = lane; j < d; j += 32) vertices[key[o + j]] = 1;
   }
 }
 
@@ -647,24 +671,27 @@ void launch_ds_mark(const Level &g, const uint32_t *ds, const uint32_t *dd, size
     LVG_CHECK_LAUNCH();
   }
   if (ni) {
-    unsigned int *nseg = &ctr->cn;  // scratch counter
+    unsigned int *nseg = &ctr->cn, *nlong = &ctr->ds_long;  // scratch counters
     LVG_CUDA(cudaMemsetAsync(nseg, 0, sizeof(unsigned int), s));
+    LVG_CUDA(cudaMemsetAsync(nlong, 0, sizeof(unsigned int), s));
     ds_heads_kernel<<<grid_for(ni, 256), 256, 0, s>>>(is, ni, const_cast<uint32_t *>(seg), nseg);
     LVG_CHECK_LAUNCH();
-    ds_ins_warp_kernel<<<grid_for(ni * 32, 256), 256, 0, s>>>(is, id, iw, ni, seg, nseg, vcom, vtot, ctot, M, R,
-                                                                vertices, neighbors, communities);
+    ds_ins_warp_kernel<<<grid_for(ni * 32, 256), 256, 0, s>>>(is, id, iw, ni, const_cast<uint32_t *>(seg), nseg,
+                                                                nlong, vcom, vtot, ctot, M, R, vertices, neighbors,
+                                                                communities);
     LVG_CHECK_LAUNCH();
-    ds_ins_kernel<<<global_table_blocks(ni), DS_BLOCK, 0, s>>>(is, id, iw, ni, seg, nseg, vcom, vtot, ctot, M, R,
-                                                              vertices, neighbors, communities, gkeys, gvals,
-                                                              gfirst, glog2, ctr);
+    ds_ins_kernel<<<global_table_blocks(ni / 33 + 1), DS_BLOCK, 0, s>>>(is, id, iw, ni, seg, nseg, nlong, vcom,
+                                                                       vtot, ctot, M, R, vertices, neighbors,
+                                                                       communities, gkeys, gvals, gfirst, glog2,
+                                                                       ctr);
     LVG_CHECK_LAUNCH();
   }
   if (g.span) {
-    LVG_CUDA(cudaMemsetAsync(count, 0, sizeof(uint32_t), s));
-    ds_expand_kernel<<<grid_for(g.span, 256), 256, 0, s>>>(g.ex, g.span, vcom, neighbors, communities, vertices,
-                                                            list, count);
+    LVG_CUDA(cudaMemsetAsync(count, 0, 2 * sizeof(uint32_t), s));
+    ds_expand_kernel<<<grid_for(g.span, 256), 256, 0, s>>>(g.ex, g.span, vcom, g.deg, neighbors, communities,
+                                                            vertices, list, count);
     LVG_CHECK_LAUNCH();
-    ds_neighbors_kernel<<<unsigned(sms()) * 16, 256, 0, s>>>(g.off, g.deg, g.key, list, count, vertices);
+    ds_neighbors_kernel<<<unsigned(sms()) * 16, 256, 0, s>>>(g.off, g.deg, g.key, list, count, g.span, vertices);
     LVG_CHECK_LAUNCH();
   }
 }

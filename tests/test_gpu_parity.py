@@ -241,8 +241,9 @@ def test_delta_screening_flags_with_large_source_groups(cuda, orc):
     rb = cuda.random_batch(x, 400, 0.8, seed=22)
     rng = np.random.default_rng(23)
     extra_s, extra_d = [], []
-    for src, k in ((1, 120), (2, 40), (3, 33), (4, 32)):
-        for v in rng.choice(np.arange(5, 3001), k, replace=False):
+    # 1500 insertions: the per-block HBM table; 120, 40, 33: the shared one; 32: a warp
+    for src, k in ((1, 120), (2, 40), (3, 33), (4, 32), (5, 1500)):
+        for v in rng.choice(np.arange(6, 3001), k, replace=False):
             extra_s += [src, v]
             extra_d += [v, src]
     raw = cuda.HostBatch(rb.del_src, rb.del_dst, rb.del_w,
@@ -259,4 +260,4 @@ def test_delta_screening_flags_with_large_source_groups(cuda, orc):
     rv, rn, rc = orc.ds_mark(Y.download(), tb, p.membership, upd.vertexWeight, upd.communityWeight,
                              Y.edge_weight() / 2)
     assert np.array_equal(v, rv) and np.array_equal(n, rn) and np.array_equal(c, rc)
-    assert n[1] or n[2] or n[3] or c.any()  # the large groups were screened
+    assert n[1] or n[2] or n[3] or n[5] or c.any()  # the large groups were screened
