@@ -855,7 +855,7 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
       }
       launch_ds_mark(g->base, b.ds, b.dd, b.nd, b.is, b.id, b.iw, b.ni, b.seg, b.ni, ucom, utot, ctot, M, R,
                      W.fv.p, W.fn.p, W.fc.p, W.gkeys.p, W.gvals.p, W.gfirst.p, dlog, g->ctr.p, W.wl.p,
-                     W.wl_count.p, s);
+                     W.wl_count.p, W.cext.p, W.scan32.p, s);
       LVG_CUDA(cudaMemcpyAsync(W.vaff.p, W.fv.p, S, cudaMemcpyDeviceToDevice, s));
       fa = W.fv.p;
     }

@@ -139,6 +139,7 @@ struct Counters {
   unsigned long long hub_chunk_over;          // hub chunks that wrote raw pairs
   unsigned int gactive;                       // graph unions: graphs still moving after an iteration
   unsigned int ds_long;                       // delta-screening sources with more than 32 insertions
+  uint32_t ds_chunks;                         // delta-screening neighbour chunks of the high-degree vertices
 };
 
 // Per-graph control of a graph-union run (lvg_static_union), on the device:
@@ -273,13 +274,15 @@ void launch_batch_weights(const uint32_t *src, const float *w, size_t n, float s
                           float *vtot, float *ctot, cudaStream_t s);
 void launch_df_mark(const uint32_t *ds, const uint32_t *dd, size_t nd, const uint32_t *is, const uint32_t *id,
                     size_t ni, const uint32_t *vcom, uint8_t *vaff, cudaStream_t s);
-// seg: ni entries (segment heads, then the sources with more than 32
-// insertions); list: g.span entries; count: 2 entries.
+// seg: ni entries (sources left to the per-source pass, then those with more
+// than 32 insertions); list: g.span entries; count: 2 entries; chunks: g.span
+// entries and scan_scratch for exclusive_scan_u32 over them.
 void launch_ds_mark(const Level &g, const uint32_t *ds, const uint32_t *dd, size_t nd, const uint32_t *is,
                     const uint32_t *id, const float *iw, size_t ni, const uint32_t *seg, size_t nseg,
                     const uint32_t *vcom, const float *vtot, const float *ctot, double M, double R,
                     uint8_t *vertices, uint8_t *neighbors, uint8_t *communities, uint32_t *gkeys, float *gvals,
-                    uint32_t *gfirst, int glog2, Counters *ctr, uint32_t *list, uint32_t *count, cudaStream_t s);
+                    uint32_t *gfirst, int glog2, Counters *ctr, uint32_t *list, uint32_t *count, uint32_t *chunks,
+                    uint32_t *scan_scratch, cudaStream_t s);
 void launch_clear_isolated(const uint32_t *list, size_t n, uint8_t *vaff, const uint8_t *fa, cudaStream_t s);
 struct IsolatedLists {
   const uint32_t *list[MAX_COLORS];

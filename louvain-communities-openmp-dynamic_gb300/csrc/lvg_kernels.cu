@@ -109,13 +109,31 @@ __global__ void f32_to_f64_kernel(const float *src, double *dst, size_t n) {
 
 // louvainUpdateWeightsFromOmpU (inc/louvain.hxx:374-388): per directed batch
 // edge, the source's weight and its community's total move by the weight.
+// Lanes of a warp with the same source (the batch is source-sorted) or the
+// same community add their weights first and the lowest of them adds the sum:
+// a large community would otherwise take thousands of atomics on one word.
+__device__ __forceinline__ void group_add(float *p, uint32_t key, float x, int lane) {
+  const unsigned grp = __match_any_sync(0xffffffffu, key);
+  float sum = 0.f;
+  for (unsigned r = grp; r; r &= r - 1u) sum += __shfl_sync(grp, x, __ffs(r) - 1);
+  if (key != EMPTY && (grp & ((1u << lane) - 1u)) == 0u) atomicAdd(p + key, sum);
+}
+
 __global__ void batch_weights_kernel(const uint32_t *src, const float *w, size_t n, float sign,
                                      const uint32_t *vcom, float *vtot, float *ctot) {
-  GRID_STRIDE(i, n) {
-    const uint32_t u = src[i];
-    const float x = sign * w[i];
-    atomicAdd(&vtot[u], x);
-    atomicAdd(&ctot[vcom[u]], x);
+  const int lane = threadIdx.x & 31;
+  for (size_t base = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32 * 32; base < n;
+       base += size_t(gridDim.x) * blockDim.x) {
+    const size_t i = base + lane;
+    uint32_t u = EMPTY, c = EMPTY;
+    float x = 0.f;
+    if (i < n) {
+      u = src[i];
+      x = sign * w[i];
+      c = vcom[u];
+    }
+    group_add(vtot, u, x, lane);
+    group_add(ctot, c, x, lane);
   }
 }
 
@@ -141,22 +159,6 @@ __global__ void ds_del_kernel(const uint32_t *ds, const uint32_t *dd, size_t nd,
     vertices[u] = 1;
     neighbors[u] = 1;
     communities[vcom[v]] = 1;
-  }
-}
-
-// Segment heads of the source-sorted insertions (appended in no particular
-// order; one counter atomic per warp).
-__global__ void ds_heads_kernel(const uint32_t *is, size_t ni, uint32_t *seg, unsigned int *nseg) {
-  const int lane = threadIdx.x & 31;
-  for (size_t base = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32 * 32; base < ni;
-       base += size_t(gridDim.x) * blockDim.x) {
-    const size_t i = base + lane;
-    const bool head = i < ni && (i == 0 || is[i] != is[i - 1]);
-    const unsigned m = __ballot_sync(0xffffffffu, head);
-    unsigned at = 0;
-    if (m && lane == __ffs(m) - 1) at = atomicAdd(nseg, unsigned(__popc(m)));
-    at = __shfl_sync(0xffffffffu, at, __ffs(m ? m : 1u) - 1);
-    if (head) seg[at + __popc(m & ((1u << lane) - 1u))] = uint32_t(i);
   }
 }
 
@@ -266,14 +268,30 @@ __global__ void __launch_bounds__(DS_BLOCK) ds_ins_kernel(const uint32_t *is, co
   }
 }
 
+// Constants of the FP32 screen of ds_ins_warp_kernel. In range (ok), every
+// intermediate stays a normal float: M in [1e-15, 1e15], R in (0, 1e6], and
+// |vtot|, |ctot| <= 2M. The screened gain x - y, x = vcout/M, y =
+// R vtot (vtot + ctot_c - ctot_d) / (2M^2), takes about ten roundings of
+// 2^-24 relative to |x| and to yb = R |vtot| (|vtot| + |ctot_c| + |ctot_d|) /
+// (2M^2) (the constants' conversions included; the cancellation in
+// vtot + ctot_c - ctot_d is bounded by yb's terms), and the reference's FP64
+// value differs from the exact one by about 2^-50 of the same; 2^-20 covers
+// both with room. DS_SCREEN_ABS covers results below the normal range.
+struct DsScreen {
+  float invM, inv2MM, R;
+  bool ok;
+};
+constexpr float DS_SCREEN_REL = 9.5367431640625e-07f;  // 2^-20
+constexpr float DS_SCREEN_ABS = 1e-36f;
+
 // The same for sources with at most 32 insertions (nearly all of them): a
 // warp per source, lane k holding insertion k; lanes of the same community
 // sum their weights in batch order and the lowest of them (the community's
 // first insertion) carries it into the argmax.
 __global__ void ds_ins_warp_kernel(const uint32_t *is, const uint32_t *id, const float *iw, size_t ni,
                                    uint32_t *seg, const unsigned int *nseg, unsigned int *nlong, const uint32_t *vcom,
-                                   const float *vtot, const float *ctot, double M, double R, uint8_t *vertices,
-                                   uint8_t *neighbors, uint8_t *communities) {
+                                   const float *vtot, const float *ctot, double M, double R, DsScreen sc,
+                                   uint8_t *vertices, uint8_t *neighbors, uint8_t *communities) {
   const unsigned ns = *nseg;
   const int lane = threadIdx.x & 31;
   const size_t warps = size_t(gridDim.x) * blockDim.x / 32;
@@ -301,20 +319,144 @@ __global__ void ds_ins_warp_kernel(const uint32_t *is, const uint32_t *id, const
     float sum = 0.f;
     for (unsigned r = grp; r; r &= r - 1u) sum += __shfl_sync(grp, w, __ffs(r) - 1);
     const bool leader = c != EMPTY && (grp & ((1u << lane) - 1u)) == 0u;
-    double be = 0;
-    uint32_t bf = 0xffffffffu, bc = 0;
+    // FP32 screen: e32 is the gain within er of the exact value, and of the
+    // reference's FP64 value too; when every sign and the winner are clear by
+    // more than the bound, FP64 (slow on this part) is skipped
+    const float vu = vtot[u], td = ctot[d];
+    float e32 = 0.f, er = 0.f;
     if (leader) {
-      const double e = delta_modularity(double(sum), 0.0, double(vtot[u]), double(ctot[c]), double(ctot[d]), M, R);
-      if (e > 0) { be = e; bf = uint32_t(lane); bc = c; }
+      const float tc = ctot[c];
+      const float x = sum * sc.invM;
+      const float y = sc.R * vu * (vu + tc - td) * sc.inv2MM;
+      const float yb = sc.R * fabsf(vu) * (fabsf(vu) + fabsf(tc) + fabsf(td)) * sc.inv2MM;
+      e32 = x - y;
+      er = DS_SCREEN_REL * (fabsf(x) + yb) + DS_SCREEN_ABS;
     }
+    const unsigned cand = __ballot_sync(0xffffffffu, leader);
+    const unsigned pos = __ballot_sync(0xffffffffu, leader && e32 > er);
+    const unsigned neg = __ballot_sync(0xffffffffu, leader && e32 < -er);
+    bool slow = !sc.ok || (pos | neg) != cand;
+    bool flag = false;
+    uint32_t bc = 0;
+    if (!slow && pos) {
+      const bool mine = (pos >> lane) & 1u;
+      float bv = mine ? e32 : -INFINITY;
+      int bl = lane;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const double oe = __shfl_xor_sync(0xffffffffu, be, o);
-      const uint32_t of = __shfl_xor_sync(0xffffffffu, bf, o);
-      const uint32_t oc = __shfl_xor_sync(0xffffffffu, bc, o);
-      if (oe > be || (oe == be && oe > 0 && of < bf)) { be = oe; bf = of; bc = oc; }
+      for (int o = 16; o > 0; o >>= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+        const int ol = __shfl_xor_sync(0xffffffffu, bl, o);
+        if (ov > bv || (ov == bv && ol < bl)) { bv = ov; bl = ol; }
+      }
+      const float lo = __shfl_sync(0xffffffffu, e32 - er, bl);
+      const unsigned amb = __ballot_sync(0xffffffffu, mine && lane != bl && e32 + er >= lo);
+      slow = amb != 0u;
+      flag = !slow;
+      bc = __shfl_sync(0xffffffffu, c, bl);
     }
-    if (lane == 0 && be > 0) {
+    if (slow) {  // the reference's FP64 rule (warp-uniform branch)
+      double be = 0;
+      uint32_t bf = 0xffffffffu;
+      bc = 0;
+      if (leader) {
+        const double e = delta_modularity(double(sum), 0.0, double(vu), double(ctot[c]), double(td), M, R);
+        if (e > 0) { be = e; bf = uint32_t(lane); bc = c; }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double oe = __shfl_xor_sync(0xffffffffu, be, o);
+        const uint32_t of = __shfl_xor_sync(0xffffffffu, bf, o);
+        const uint32_t oc = __shfl_xor_sync(0xffffffffu, bc, o);
+        if (oe > be || (oe == be && oe > 0 && of < bf)) { be = oe; bf = of; bc = oc; }
+      }
+      flag = be > 0;
+    }
+    if (lane == 0 && flag) {
+      vertices[u] = 1;
+      neighbors[u] = 1;
+      communities[bc] = 1;
+    }
+  }
+}
+
+// The insertions, a warp per 32 consecutive entries (the first pass): a
+// source whose insertions all lie in the warp's window and whose screen is
+// clear (no gain within the bound of zero, the best clear of the others) is
+// settled here; the others' first insertions are listed in seg (count nseg)
+// for ds_ins_warp_kernel. Lanes of the same source and community sum their
+// weights in batch order (the reference's vcout); the lowest of them stands
+// for the community, so lane order is the reference's scan order.
+__global__ void ds_ins_lane_kernel(const uint32_t *is, const uint32_t *id, const float *iw, size_t ni,
+                                   uint32_t *seg, unsigned int *nseg, const uint32_t *vcom, const float *vtot,
+                                   const float *ctot, DsScreen sc, uint8_t *vertices, uint8_t *neighbors,
+                                   uint8_t *communities) {
+  const int lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
+  for (size_t base = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32 * 32; base < ni;
+       base += size_t(gridDim.x) * blockDim.x) {
+    const size_t j = base + lane;
+    const bool in = j < ni;
+    const uint32_t u = in ? is[j] : EMPTY;
+    // the source before the window (lane 0) and after it (lane 31)
+    uint32_t edge = EMPTY;
+    if (lane == 0 && base > 0) edge = is[base - 1];
+    if (lane == 31 && j + 1 < ni) edge = is[j + 1];
+    const uint32_t before = __shfl_sync(0xffffffffu, edge, 0), after = __shfl_sync(0xffffffffu, edge, 31);
+    const uint32_t u0 = __shfl_sync(0xffffffffu, u, 0), u31 = __shfl_sync(0xffffffffu, u, 31);
+    const bool foreign = in && u == u0 && before == u0;  // its head is in an earlier window
+    const bool crossing = in && u == u31 && after == u31;  // it goes on past the window
+    const bool local = in && !foreign && !crossing;
+    const unsigned segm = __match_any_sync(0xffffffffu, u);  // the source's lanes (contiguous)
+    const int h = __ffs(segm) - 1, t = 31 - __clz(segm);
+    uint32_t c = EMPTY, d = 0;
+    float w = 0.f;
+    if (local) {
+      d = vcom[u];
+      c = vcom[id[j]];
+      w = iw[j];
+      if (c == d) c = EMPTY;
+    }
+    const unsigned grp = __match_any_sync(0xffffffffu, (uint64_t(u) << 32) | c);
+    float sum = 0.f;
+    for (unsigned r = grp; r; r &= r - 1u) sum += __shfl_sync(grp, w, __ffs(r) - 1);
+    const bool leader = c != EMPTY && (grp & below) == 0u;
+    float e32 = 0.f, er = 0.f;
+    if (leader) {
+      const float vu = vtot[u], td = ctot[d], tc = ctot[c];
+      const float x = sum * sc.invM;
+      const float y = sc.R * vu * (vu + tc - td) * sc.inv2MM;
+      const float yb = sc.R * fabsf(vu) * (fabsf(vu) + fabsf(tc) + fabsf(td)) * sc.inv2MM;
+      e32 = x - y;
+      er = DS_SCREEN_REL * (fabsf(x) + yb) + DS_SCREEN_ABS;
+    }
+    const bool pos = leader && e32 > er;
+    const unsigned cand = __ballot_sync(0xffffffffu, leader);
+    const unsigned unc = __ballot_sync(0xffffffffu, leader && !pos && !(e32 < -er));
+    const unsigned posm = __ballot_sync(0xffffffffu, pos);
+    // the largest screened gain of each source (lowest lane on ties): a scan
+    // over the source's lanes, read at its last lane
+    float bv = pos ? e32 : -INFINITY;
+    int bl = lane;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const float ov = __shfl_up_sync(0xffffffffu, bv, o);
+      const int ol = __shfl_up_sync(0xffffffffu, bl, o);
+      if (lane - o >= h && (ov > bv || (ov == bv && ol < bl))) { bv = ov; bl = ol; }
+    }
+    const int best = __shfl_sync(0xffffffffu, bl, t);
+    const float lo = __shfl_sync(0xffffffffu, e32 - er, best);
+    const uint32_t bc = __shfl_sync(0xffffffffu, c, best);
+    const unsigned amb = __ballot_sync(0xffffffffu, pos && lane != best && e32 + er >= lo);
+    const bool slow = ((unc | amb) & segm) != 0u || (!sc.ok && (cand & segm) != 0u);
+    // heads of the sources left to the per-source pass
+    const bool head = lane == h && in && !foreign;
+    const bool list = head && (crossing || slow);
+    const unsigned lm = __ballot_sync(0xffffffffu, list);
+    unsigned at = 0;
+    if (lm && lane == __ffs(lm) - 1) at = atomicAdd(nseg, unsigned(__popc(lm)));
+    at = __shfl_sync(0xffffffffu, at, __ffs(lm ? lm : 1u) - 1);
+    if (list) seg[at + __popc(lm & below)] = uint32_t(j);
+    if (head && local && !slow && (posm & segm)) {
       vertices[u] = 1;
       neighbors[u] = 1;
       communities[bc] = 1;
@@ -351,25 +493,66 @@ __global__ void ds_expand_kernel(const uint8_t *ex, size_t n, const uint32_t *vc
   }
 }
 
-// The neighbours of the listed vertices: a block per vertex above degree
-// DS_WARP_DEG (so a hub's adjacency is spread over a block), then a warp per
-// vertex for the rest.
+// Set a flag that is most often set already (the neighbours of hubs repeat):
+// the read usually hits L1, where the plain store would go to L2 every time.
+// A stale 0 only costs a redundant store; a flag is never cleared here.
+__device__ __forceinline__ void mark_once(uint8_t *flags, uint32_t v) {
+  if (!flags[v]) flags[v] = 1;
+}
+
+// The neighbours of the listed vertices: a warp per vertex up to degree
+// DS_WARP_DEG (ds_neighbors_kernel); above it, chunks of DS_WARP_DEG edges
+// balanced over the blocks (ds_neighbors_big_kernel).
 __global__ void ds_neighbors_kernel(const uint64_t *off, const uint32_t *deg, const uint32_t *key,
-                                    const uint32_t *list, const uint32_t *count, size_t n, uint8_t *vertices) {
-  const uint32_t nw = count[0], nb = count[1];
-  for (uint32_t i = blockIdx.x; i < nb; i += gridDim.x) {
-    const uint32_t u = list[n - 1 - i];
-    const uint64_t o = off[u];
-    const uint32_t d = deg[u];
-    for (uint32_t j = threadIdx.x; j < d; j += blockDim.x) vertices[key[o + j]] = 1;
-  }
+                                    const uint32_t *list, const uint32_t *count, uint8_t *vertices) {
+  const uint32_t nw = count[0];
   const int lane = threadIdx.x & 31;
   const size_t warps = size_t(gridDim.x) * blockDim.x / 32;
   for (size_t i = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32; i < nw; i += warps) {
     const uint32_t u = list[i];
     const uint64_t o = off[u];
     const uint32_t d = deg[u];
-    for (uint32_t j = lane; j < d; j += 32) vertices[key[o + j]] = 1;
+    for (uint32_t j = lane; j < d; j += 32) mark_once(vertices, key[o + j]);
+  }
+}
+
+// Per listed vertex above DS_WARP_DEG (list[n - 1 - i], i < count[1]), its
+// 256-edge chunks; zero past the list (the whole array is scanned).
+__global__ void ds_big_chunks_kernel(const uint32_t *deg, const uint32_t *list, const uint32_t *count, size_t n,
+                                     uint32_t *chunks) {
+  const uint32_t nb = count[1];
+  GRID_STRIDE(i, n) chunks[i] = i < nb ? (deg[list[n - 1 - i]] + DS_WARP_DEG - 1) / DS_WARP_DEG : 0u;
+}
+
+// The adjacencies of those vertices with each block taking an equal range of
+// the chunks (chunks = their exclusive prefix, total = the chunk count): a hub
+// is spread over many blocks, and no block waits on one.
+__global__ void ds_neighbors_big_kernel(const uint64_t *off, const uint32_t *deg, const uint32_t *key,
+                                        const uint32_t *list, const uint32_t *count, size_t n,
+                                        const uint32_t *chunks, const uint32_t *total, uint8_t *vertices) {
+  __shared__ uint32_t first;
+  const uint32_t nb = count[1], T = *total;
+  const uint32_t t0 = uint32_t(uint64_t(T) * blockIdx.x / gridDim.x);
+  const uint32_t t1 = uint32_t(uint64_t(T) * (blockIdx.x + 1) / gridDim.x);
+  if (t0 >= t1) return;  // block-uniform
+  if (threadIdx.x == 0) {  // the vertex holding chunk t0: the last i with chunks[i] <= t0
+    uint32_t lo = 0, hi = nb;
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (chunks[mid] <= t0) lo = mid; else hi = mid;
+    }
+    first = lo;
+  }
+  __syncthreads();
+  for (uint32_t i = first, t = t0; t < t1; ++i) {
+    const uint32_t u = list[n - 1 - i];
+    const uint64_t o = off[u];
+    const uint32_t d = deg[u];
+    const uint32_t cb = chunks[i], ce = i + 1 < nb ? chunks[i + 1] : T;
+    const uint32_t stop = min(ce, t1);
+    const uint32_t e1 = min(d, (stop - cb) * DS_WARP_DEG);
+    for (uint32_t j = (t - cb) * DS_WARP_DEG + threadIdx.x; j < e1; j += blockDim.x) mark_once(vertices, key[o + j]);
+    t = stop;
   }
 }
 
@@ -664,21 +847,28 @@ void launch_ds_mark(const Level &g, const uint32_t *ds, const uint32_t *dd, size
                     const uint32_t *id, const float *iw, size_t ni, const uint32_t *seg, size_t nseg_cap,
                     const uint32_t *vcom, const float *vtot, const float *ctot, double M, double R,
                     uint8_t *vertices, uint8_t *neighbors, uint8_t *communities, uint32_t *gkeys, float *gvals,
-                    uint32_t *gfirst, int glog2, Counters *ctr, uint32_t *list, uint32_t *count, cudaStream_t s) {
+                    uint32_t *gfirst, int glog2, Counters *ctr, uint32_t *list, uint32_t *count, uint32_t *chunks,
+                    uint32_t *scan_scratch, cudaStream_t s) {
   (void)nseg_cap;
   if (nd) {
     ds_del_kernel<<<grid_for(nd, 256), 256, 0, s>>>(ds, dd, nd, vcom, vertices, neighbors, communities);
     LVG_CHECK_LAUNCH();
   }
   if (ni) {
+    DsScreen sc;
+    sc.ok = M >= 1e-15 && M <= 1e15 && R > 0 && R <= 1e6;
+    sc.invM = sc.ok ? float(1.0 / M) : 0.f;
+    sc.inv2MM = sc.ok ? float(1.0 / (2 * M * M)) : 0.f;
+    sc.R = float(R);
     unsigned int *nseg = &ctr->cn, *nlong = &ctr->ds_long;  // scratch counters
     LVG_CUDA(cudaMemsetAsync(nseg, 0, sizeof(unsigned int), s));
     LVG_CUDA(cudaMemsetAsync(nlong, 0, sizeof(unsigned int), s));
-    ds_heads_kernel<<<grid_for(ni, 256), 256, 0, s>>>(is, ni, const_cast<uint32_t *>(seg), nseg);
+    ds_ins_lane_kernel<<<grid_for(ni, 256), 256, 0, s>>>(is, id, iw, ni, const_cast<uint32_t *>(seg), nseg, vcom,
+                                                          vtot, ctot, sc, vertices, neighbors, communities);
     LVG_CHECK_LAUNCH();
     ds_ins_warp_kernel<<<grid_for(ni * 32, 256), 256, 0, s>>>(is, id, iw, ni, const_cast<uint32_t *>(seg), nseg,
-                                                                nlong, vcom, vtot, ctot, M, R, vertices, neighbors,
-                                                                communities);
+                                                                nlong, vcom, vtot, ctot, M, R, sc, vertices,
+                                                                neighbors, communities);
     LVG_CHECK_LAUNCH();
     ds_ins_kernel<<<global_table_blocks(ni / 33 + 1), DS_BLOCK, 0, s>>>(is, id, iw, ni, seg, nseg, nlong, vcom,
                                                                        vtot, ctot, M, R, vertices, neighbors,
@@ -691,7 +881,13 @@ void launch_ds_mark(const Level &g, const uint32_t *ds, const uint32_t *dd, size
     ds_expand_kernel<<<grid_for(g.span, 256), 256, 0, s>>>(g.ex, g.span, vcom, g.deg, neighbors, communities,
                                                             vertices, list, count);
     LVG_CHECK_LAUNCH();
-    ds_neighbors_kernel<<<unsigned(sms()) * 16, 256, 0, s>>>(g.off, g.deg, g.key, list, count, g.span, vertices);
+    ds_neighbors_kernel<<<unsigned(sms()) * 8, 256, 0, s>>>(g.off, g.deg, g.key, list, count, vertices);
+    LVG_CHECK_LAUNCH();
+    ds_big_chunks_kernel<<<grid_for(g.span, 256), 256, 0, s>>>(g.deg, list, count, g.span, chunks);
+    LVG_CHECK_LAUNCH();
+    exclusive_scan_u32(chunks, chunks, g.span, &ctr->ds_chunks, scan_scratch, s);
+    ds_neighbors_big_kernel<<<unsigned(sms()) * 8, 256, 0, s>>>(g.off, g.deg, g.key, list, count, g.span, chunks,
+                                                               &ctr->ds_chunks, vertices);
     LVG_CHECK_LAUNCH();
   }
 }

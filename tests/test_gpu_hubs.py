@@ -70,3 +70,39 @@ def test_half_integer_weights_match_cpu_replay(cuda, orc, hubgraph):
     assert np.array_equal(r.membership, m)
     assert np.array_equal(r.communityWeight, ct)
     assert (r.iterations, r.passes) == (info["iterations"], info["passes"])
+
+
+def test_delta_screening_on_hubs_matches_cpu_replay(cuda, orc, hubgraph):
+    # The eight largest hubs each gain 20 edges, so the neighbour screening
+    # runs over hub adjacencies (chunked over many blocks); flags and the
+    # whole deterministic run equal the reference's.
+    x, b, _ = hubgraph
+    hubs = np.argsort(np.diff(x.offsets).astype(np.int64))[-8:]
+    rng = np.random.default_rng(79)
+    s, d = [], []
+    for h in hubs:
+        for v in rng.choice(np.arange(1, x.span), 20, replace=False):
+            if v != h:
+                s += [h, v]
+                d += [v, h]
+    ins_s = np.concatenate([b.ins_src, np.array(s, np.uint32)])
+    ins_d = np.concatenate([b.ins_dst, np.array(d, np.uint32)])
+    raw = cuda.HostBatch(b.del_src, b.del_dst, b.del_w, ins_s, ins_d, np.ones(len(ins_s), np.float32))
+    o = cuda.LouvainOptions(deterministic=True)
+    X = cuda.Graph(x)
+    r0 = cuda.louvain_static(X, o)
+    q = (r0.membership, r0.vertexWeight, r0.communityWeight)
+    Y = X.clone()
+    tb = Y.apply_batch(raw)
+    y = Y.download()
+    upd = cuda.louvain_dynamic_frontier(Y, tb, *q, cuda.LouvainOptions(maxPasses=0))
+    v, n, c = cuda.affected_vertices(Y, cuda.METHOD_DELTA, tb, *q)
+    rv, rn, rc = orc.ds_mark(y, tb, r0.membership, upd.vertexWeight, upd.communityWeight, Y.edge_weight() / 2)
+    assert np.array_equal(v, rv) and np.array_equal(n, rn) and np.array_equal(c, rc)
+    assert n[hubs].any()
+    r = cuda.louvain_dynamic_delta_screening(Y, tb, *q, o)
+    m, vt, ct, info = orc.louvain(y, 2, tb, *q, threads=8, sync=True)
+    assert np.array_equal(r.membership, m)
+    assert np.array_equal(r.communityWeight, ct)
+    assert (r.iterations, r.passes, r.affectedVertices) == (info["iterations"], info["passes"],
+                                                            info["affectedVertices"])

@@ -261,3 +261,36 @@ def test_delta_screening_flags_with_large_source_groups(cuda, orc):
                              Y.edge_weight() / 2)
     assert np.array_equal(v, rv) and np.array_equal(n, rn) and np.array_equal(c, rc)
     assert n[1] or n[2] or n[3] or n[5] or c.any()  # the large groups were screened
+
+
+@pytest.mark.parametrize("swap", [False, True])
+def test_delta_screening_exact_tie_takes_first_community(cuda, orc, swap):
+    # Three 5-cliques (vertices 1-5, 6-10, 11-15); vertex 11 gains one edge
+    # into each of the other two, whose totals are equal: the gains tie
+    # exactly, the FP32 screen cannot separate them, and the reference's FP64
+    # rule gives the community of the first insertion in batch order (to
+    # vertex 3), whichever of the two community ids is smaller.
+    src, dst = [], []
+    for base in (1, 6, 11):
+        for a in range(base, base + 5):
+            for b in range(base, base + 5):
+                if a != b:
+                    src.append(a)
+                    dst.append(b)
+    x = cuda.csr_from_edges(16, np.array(src, np.uint32), np.array(dst, np.uint32))
+    la, lb = (6, 1) if swap else (1, 6)
+    q = np.array([0] + [la] * 5 + [lb] * 5 + [11] * 5, np.uint32)
+    vt = np.array([0] + [4.0] * 15)
+    ct = np.zeros(16)
+    ct[[1, 6, 11]] = 20.0
+    ins = [(3, 11), (8, 11), (11, 3), (11, 8)]
+    e = np.zeros(0, np.uint32)
+    raw = cuda.HostBatch(e, e, np.zeros(0, np.float32), np.array([a for a, _ in ins], np.uint32),
+                         np.array([b for _, b in ins], np.uint32), np.ones(4, np.float32))
+    Y = cuda.Graph(x)
+    tb = Y.apply_batch(raw)
+    upd = cuda.louvain_dynamic_frontier(Y, tb, q, vt, ct, cuda.LouvainOptions(maxPasses=0))
+    v, n, c = cuda.affected_vertices(Y, cuda.METHOD_DELTA, tb, q, upd.vertexWeight, upd.communityWeight)
+    rv, rn, rc = orc.ds_mark(Y.download(), tb, q, upd.vertexWeight, upd.communityWeight, Y.edge_weight() / 2)
+    assert np.array_equal(v, rv) and np.array_equal(n, rn) and np.array_equal(c, rc)
+    assert n[11] and c[la] and not c[lb]
