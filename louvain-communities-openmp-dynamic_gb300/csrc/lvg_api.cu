@@ -423,7 +423,7 @@ void ensure_aux(lvg_graph *g) {
 int bin_stream(int b) { return b <= 4 ? 0 : b <= 8 ? 1 : b == 9 ? 2 : b == 10 ? 3 : -1; }
 
 void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const float *tot,
-                       const uint8_t *fa, float kr, bool sync, bool fused, const int *glog2, const size_t *goff,
+                       const uint8_t *fa, float kr, bool sync, int fused, const int *glog2, const size_t *goff,
                        size_t need, std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> *bin_ev,
                        const UnionCall *uc) {
   auto set_union = [&](MoveArgs &a) {
@@ -456,9 +456,9 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot
     }
     if (fused) {
       // bins 1-6 and 7-8 in one launch each; each bin gets blocks for its
-      // bucket, at most two per SM (its worklist is short)
+      // bucket, at most `fused` per SM (few where the worklists are short)
       static const int tpb[NUM_BINS] = {0, 64, 32, 16, 8, 8, 8, 8, 8, 0, 0, 0};
-      const size_t cap = size_t(device_sms()) * 2;
+      const size_t cap = size_t(device_sms()) * size_t(fused);
       for (const auto &grp : {std::pair<int, int>{1, 6}, std::pair<int, int>{7, 8}}) {
         SmallBins sb{};
         uint32_t nb = 0;
@@ -534,7 +534,7 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot
 // eager iteration, so every kernel's attributes are already set). A capture
 // failure disables graphs for this handle; the eager path stays correct.
 void capture_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const float *tot,
-                       const uint8_t *fa, float kr, bool sync, bool fused, const int *glog2, const size_t *goff,
+                       const uint8_t *fa, float kr, bool sync, int fused, const int *glog2, const size_t *goff,
                        size_t need, const IterKey &key, const UnionCall *uc) {
   cudaStream_t s = g->stream;
   if (g->iter_exec) {
@@ -577,7 +577,7 @@ void capture_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot
 // iteration is captured once into a CUDA graph and replayed, one graph
 // launch per iteration instead of ~12 launches per colour class.
 int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const float *tot, const uint8_t *fa,
-               double M, float kr, int L, double E, bool sync, bool fused, const UnionCall *uc = nullptr,
+               double M, float kr, int L, double E, bool sync, int fused, const UnionCall *uc = nullptr,
                const DBatch *endpoints = nullptr) {
   Workspace &W = *g->ws;
   cudaStream_t s = g->stream;
@@ -871,10 +871,15 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
       if (p == 1) ep1 = g->events.record(s);
       const bool first = p == 0;
       cudaEvent_t a0 = g->events.record(s);
-      // the frontier methods' first pass works on short per-class worklists:
-      // the small degree bins go in two fused launches per class
-      const bool fused =
-          first && (method == LVG_METHOD_FRONTIER || method == LVG_METHOD_DELTA) && g->tuning.fused_small;
+      // the frontier methods' first pass: the small degree bins go in two
+      // fused launches per class, with blocks per SM and bin for DF's short
+      // worklists (2) or for delta-screening's whole communities (8: with
+      // two, its first pass took 2.8x as long on a 4M-vertex graph of
+      // average degree 87)
+      const int fused = !first || !g->tuning.fused_small ? 0
+                        : method == LVG_METHOD_FRONTIER  ? 2
+                        : method == LVG_METHOD_DELTA     ? 8
+                                                         : 0;
       const int m = move_phase(g, lv, com, ctot, tot, first ? fa : nullptr, M, kr, L, E, sync, fused, nullptr,
                                first && method == LVG_METHOD_FRONTIER ? &b : nullptr);
       tl_ev.push_back({a0, g->events.record(s)});
@@ -999,7 +1004,7 @@ void run_union(lvg_graph *g, const lvg_options &o, RunInfo &info) {
       UnionCall uc = uc0;
       uc.E = E;
       cudaEvent_t a0 = g->events.record(s);
-      move_phase(g, lv, com, ctot, tot, nullptr, 0.0, 0.f, L, E, sync, false, &uc);
+      move_phase(g, lv, com, ctot, tot, nullptr, 0.0, 0.f, L, E, sync, 0, &uc);
       tl_ev.push_back({a0, g->events.record(s)});
       launch_pass_end(n, U.ctl.p, P, s);
       launch_union_snapshot(lv.span, lv.gid, lv.gbase, U.vb0.p, U.ctl.p, ctot, W.vaff.p, U.ct.p, U.aff.p, s);
