@@ -689,6 +689,8 @@ def run_temporal(args):
         row = {"batch_fraction": f, "lines": k, "tidied_insertions": tb.num_insertions, "apply_ms": apply_ms}
         for name, fn in (("static", None), ("nd", lvg.louvain_naive_dynamic),
                          ("ds", lvg.louvain_dynamic_delta_screening), ("df", lvg.louvain_dynamic_frontier)):
+            # the shapes were tuned on DF: the full sweeps keep the default ones
+            lvg.set_tuning(Y, **(tuning if name in ("ds", "df") else lvg.tuning_default()))
             ms = []
             for _ in range(3):
                 r = lvg.louvain_static(Y, o) if fn is None else fn(Y, tb, prior.membership, prior.vertexWeight,
@@ -766,6 +768,8 @@ def run_sweep(args):
                    "apply_ms": apply_ms}
             for name, fn in (("static", None), ("nd", lvg.louvain_naive_dynamic),
                              ("ds", lvg.louvain_dynamic_delta_screening), ("df", lvg.louvain_dynamic_frontier)):
+                # the shapes were tuned on DF: the full sweeps keep the default ones
+                lvg.set_tuning(Y, **(tuning if name in ("ds", "df") else lvg.tuning_default()))
                 ms = []
                 for _ in range(3):
                     r = lvg.louvain_static(Y, o) if fn is None else fn(Y, tb, prior.membership, prior.vertexWeight,

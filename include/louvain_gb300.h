@@ -409,7 +409,8 @@ typedef struct lvg_tuning {
                                   and deterministic == 0 (default 8) */
   int      concurrent_bins;    /* 1: a class's degree bins run concurrently on side streams (default 1) */
   int      fused_small;        /* 1: the frontier methods' first pass runs bins 1-8 as two launches
-                                  per class (default 1) */
+                                  per class (default 0: with the iterations replayed as CUDA
+                                  graphs the separate launches were faster on R-MAT s24) */
   uint32_t hub_chunk;          /* edges per chunk of a vertex above degree 8192 (256..1<<20; default 4096) */
   int      big_blocks_per_sm;  /* resident blocks per SM of the degree 513-8192 kernels (0 = as many
                                   as fit; default 0) */

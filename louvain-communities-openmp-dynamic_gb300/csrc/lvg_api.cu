@@ -172,7 +172,7 @@ inline lvg_tuning default_tuning() {
   lvg_tuning t;
   t.frontier_colors = DEFAULT_COLORS_ASYNC;
   t.concurrent_bins = 1;
-  t.fused_small = 1;
+  t.fused_small = 0;
   t.hub_chunk = HUB_CHUNK;
   t.big_blocks_per_sm = 0;
   t.frontier_max_fraction = 1e-3;
@@ -2571,12 +2571,35 @@ int lvg_autotune(lvg_graph *g, int method, const lvg_device_batch *b, const lvg_
     };
     // the class count first (the largest effect), then the launch shapes; twice,
     // since each knob's best value can depend on the others
+    const lvg_tuning start = cur;
     for (int round = 0; round < 2; ++round) {
       if (colours) try_knob([](lvg_tuning &t, long v) { t.frontier_colors = int(v); }, {8, 4, 2, 1}, true);
       try_knob([](lvg_tuning &t, long v) { t.hub_chunk = uint32_t(v); }, {2048, 4096, 8192, 16384}, false);
-      try_knob([](lvg_tuning &t, long v) { t.concurrent_bins = int(v); }, {1, 0}, false);
-      try_knob([](lvg_tuning &t, long v) { t.fused_small = int(v); }, {1, 0}, false);
+      // concurrent bins and fused small bins together: each one's best value
+      // depends on the other (R-MAT s24, DF at 1e-4 |E|, one class: 0.62 ms
+      // with concurrent and unfused, 0.78 ms for the best of one at a time)
+      try_knob([](lvg_tuning &t, long v) { t.concurrent_bins = int(v >> 1); t.fused_small = int(v & 1); },
+               {3, 2, 1, 0}, false);
       try_knob([](lvg_tuning &t, long v) { t.big_blocks_per_sm = int(v); }, {0, 2, 3, 4}, false);
+    }
+    // confirm the launch shapes against the starting ones (with the chosen
+    // class count), measured in turn, since a sub-millisecond run drifts
+    // between measurements: shapes that are not 2 % faster on this second
+    // look are dropped
+    lvg_tuning base = start;
+    base.frontier_colors = cur.frontier_colors;
+    if (std::memcmp(&cur, &base, sizeof(cur))) {
+      double a = 1e300, z = 1e300;
+      for (int r = 0; r < 3; ++r) {
+        a = std::min(a, measure(cur, nullptr));
+        z = std::min(z, measure(base, nullptr));
+      }
+      if (a < 0.98 * z) {
+        tcur = a;
+      } else {
+        cur = base;
+        tcur = z;
+      }
     }
     apply_tuning(g, cur);
     if (best) *best = cur;

@@ -12,7 +12,7 @@ import pytest
 
 def test_tuning_defaults(lvg):
     t = lvg.tuning_default()
-    assert t == dict(frontier_colors=8, concurrent_bins=1, fused_small=1, hub_chunk=4096, big_blocks_per_sm=0,
+    assert t == dict(frontier_colors=8, concurrent_bins=1, fused_small=0, hub_chunk=4096, big_blocks_per_sm=0,
                      frontier_max_fraction=1e-3)
 
 
@@ -30,7 +30,7 @@ def test_launch_knobs_keep_deterministic_results(cuda, hubcase):
     r0 = cuda.louvain_static(cuda.Graph(x), o)
     Y = cuda.Graph(y)
     ref = cuda.louvain_dynamic_frontier(Y, b, r0.membership, r0.vertexWeight, r0.communityWeight, o)
-    for knobs in [dict(hub_chunk=1024), dict(hub_chunk=16384, concurrent_bins=0), dict(fused_small=0),
+    for knobs in [dict(hub_chunk=1024), dict(hub_chunk=16384, concurrent_bins=0), dict(fused_small=1),
                   dict(big_blocks_per_sm=1), dict(big_blocks_per_sm=3, hub_chunk=2048)]:
         cuda.set_tuning(Y, **knobs)
         r = cuda.louvain_dynamic_frontier(Y, b, r0.membership, r0.vertexWeight, r0.communityWeight, o)
