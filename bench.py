@@ -86,6 +86,9 @@ def parse():
     p.add_argument("--ncu-steps", type=int, default=0,
                    help="profiling mode: set up as usual, then run this many steps between "
                         "cudaProfilerStart/Stop (for ncu --profile-from-start off) and exit")
+    p.add_argument("--set-tuning", default="",
+                   help="df workload: launch shapes as knob=value,... (lvg_tuning fields) instead of "
+                        "running the autotuner, e.g. to profile the shapes a timed run picked")
     p.add_argument("--ncu-method", default="df", choices=["df", "static"],
                    help="profiling mode of the df workload: the method profiled (static: the plain "
                         "GPU static Louvain on the updated graph)")
@@ -322,7 +325,13 @@ def run_gpu(args):
     # classes, within 1e-3 modularity) on this workload, untimed
     tuning = lvg.get_tuning(Y)
     tune_s = 0.0
-    if not args.no_tune:
+    if args.set_tuning:
+        knobs = {}
+        for kv in args.set_tuning.split(","):
+            k, v = kv.split("=")
+            knobs[k.strip()] = float(v) if k.strip() == "frontier_max_fraction" else int(v)
+        tuning = lvg.set_tuning(Y, **knobs)
+    elif not args.no_tune:
         t0 = time.perf_counter()
         tuning, _ = lvg.autotune(Y, lvg.METHOD_FRONTIER, db, st_prior, o, repeats=5)
         tune_s = time.perf_counter() - t0
@@ -339,7 +348,9 @@ def run_gpu(args):
             print(json.dumps({"profiled_df_steps": args.ncu_steps, "last_ms": info["time"],
                               "kernel_launches_per_step": st["kernel_launches"],
                               "algorithmic_bytes_per_step": MOVE_BYTES_PER_EDGE * st["move_edges"] +
-                              MOVE_BYTES_PER_VERTEX * st["move_vertices"]}), flush=True)
+                              MOVE_BYTES_PER_VERTEX * st["move_vertices"],
+                              "hub_algorithmic_bytes_per_step": MOVE_BYTES_PER_EDGE * st["move_bin_edges"][11] +
+                              MOVE_BYTES_PER_VERTEX * st["move_bin_vertices"][11]}), flush=True)
         dist.close()
         return 0
 
@@ -364,7 +375,8 @@ def run_gpu(args):
     dist.barrier()
     # the same steps again with per-launch events around the local-moving kernels (roofline)
     Y.set_profiling(True)
-    kms, kedges, kverts, klaunch, bin_ms, bin_edges = 0.0, 0, 0, 0, np.zeros(12), np.zeros(12)
+    kms, kedges, kverts, klaunch = 0.0, 0, 0, 0
+    bin_ms, bin_edges, bin_verts = np.zeros(12), np.zeros(12), np.zeros(12)
     for _ in range(args.steps):
         lvg.run_resident(Y, lvg.METHOD_FRONTIER, db, st_prior, st_out, o)
         s = Y.stats()
@@ -374,6 +386,7 @@ def run_gpu(args):
         klaunch += s["move_launches"]
         bin_ms += np.array(s["move_bin_ms"])
         bin_edges += np.array(s["move_bin_edges"])
+        bin_verts += np.array(s["move_bin_vertices"])
     Y.set_profiling(False)
     m_df = st_out.membership()
     q_df = Y.modularity(m_df)
@@ -411,6 +424,12 @@ def run_gpu(args):
         achieved = alg_per_step / (kms / args.steps / 1e3) / 1e9
     tr = traffic_per_launch()
     traffic = int(tr["traffic_ratio"] * alg_per_step) if tr else None
+    # the dominant kernel: the hub path (hub_chunk_kernel + hub_merge_kernel, the
+    # vertices above degree 8192), timed by the events around its two launches
+    hub_ms = bin_ms[11] / args.steps
+    hub_alg = (MOVE_BYTES_PER_EDGE * bin_edges[11] + MOVE_BYTES_PER_VERTEX * bin_verts[11]) / args.steps
+    hub_achieved = hub_alg / (hub_ms / 1e3) / 1e9 if hub_ms > 0 else None
+    hub_traffic = int(tr["hub_traffic_ratio"] * hub_alg) if tr and "hub_traffic_ratio" in tr else None
     line = {
         "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
@@ -422,22 +441,29 @@ def run_gpu(args):
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms_max,
                 "call": "lvg_frontier (drop-in for louvainDynamicFrontierOmp), pinned host arrays",
                 "last_call_parts": e2e_parts},
-        "tuning": dict(tuning, by="lvg_autotune" if not args.no_tune else "defaults", seconds=round(tune_s, 2)),
+        "tuning": dict(tuning, by="--set-tuning" if args.set_tuning else "lvg_autotune" if not args.no_tune else "defaults",
+                       seconds=round(tune_s, 2)),
         "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None,
-                     "traffic": traffic,
-                     "traffic_note": ("DRAM bytes of the local-moving kernels per step: their ratio to the "
-                                      "algorithmic bytes in an ncu capture (" + tr.get("measured_on", "") +
-                                      "; profiles/move_traffic.json) times this step's algorithmic bytes")
-                                     if tr else None,
-                     "algorithmic_bytes_per_step": int(alg_per_step),
-                     "kernel": "local-moving kernels (move_small/move_big/hub_chunk/hub_merge, all degree bins)",
-                     "launches_per_step": klaunch / args.steps, "ms_per_step": kms / args.steps,
-                     "per_bin_ms_per_step": [round(v / args.steps, 4) for v in bin_ms],
-                     "per_bin_edges_per_step": [int(v / args.steps) for v in bin_edges],
+        "roofline": {"bound": "hbm", "achieved": hub_achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (hub_achieved / peak) if hub_achieved else None,
+                     "traffic": hub_traffic,
+                     "kernel": "hub path of the vertices above degree 8192 (hub_chunk_kernel + hub_merge_kernel, "
+                               "one launch each per colour class): the step's largest kernel time",
+                     "algorithmic_bytes_per_step": int(hub_alg), "ms_per_step": hub_ms,
+                     "traffic_note": ("DRAM bytes of the hub pair per step: their ratio to its algorithmic bytes in "
+                                      "an ncu capture (" + tr.get("measured_on", "") + "; profiles/move_traffic.json) "
+                                      "times this step's algorithmic bytes; below 1 when the community gathers hit L2")
+                                     if hub_traffic else None,
                      "peak_kind": peak_kind,
-                     "algorithmic_bytes": "12 B/scanned edge + 17 B/processed vertex"},
+                     "algorithmic_bytes": "12 B/scanned edge + 17 B/processed vertex",
+                     "all_local_moving": {
+                         "achieved": achieved, "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                         "algorithmic_bytes_per_step": int(alg_per_step),
+                         "kernels": "every degree bin (move_tile/move_small/move_big/hub_chunk/hub_merge), "
+                                    "durations summed as profiled one after another",
+                         "launches_per_step": klaunch / args.steps, "ms_per_step": kms / args.steps,
+                         "per_bin_ms_per_step": [round(v / args.steps, 4) for v in bin_ms],
+                         "per_bin_edges_per_step": [int(v / args.steps) for v in bin_edges]}},
         "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
         "batch_apply_ms": {"p50": float(np.percentile(apply_ms, 50)), "max": float(np.max(apply_ms)),
                            "call": "lvg_graph_apply_device_batch (tidy + apply in HBM, host wall clock)"},
