@@ -71,6 +71,8 @@ def parse():
                    help="batched: graphs the one-by-one comparator runs (a prefix of the batch)")
     p.add_argument("--drift-vertices", type=int, default=4_000_000)
     p.add_argument("--drift-communities", type=int, default=4000)
+    p.add_argument("--stream-batches", type=int, default=1000,
+                   help="temporal: consecutive batches of the 1e-5 stream (1e-4: a tenth, 1e-3: a hundredth)")
     p.add_argument("--drift-edges", type=int, default=200_000_000)
     p.add_argument("--graphs", type=int, default=64)
     p.add_argument("--scale-min", type=int, default=18)
@@ -672,7 +674,14 @@ def run_temporal(args):
     first 90 % form the base graph (main.cxx:159-161), then insertion-only
     batches of 1e-5, 1e-4 and 1e-3 of the stream's lines are tidied and
     applied to a copy of the base (main.cxx:102-109) and static, ND, DS and DF
-    Louvain run from the base's static result. value = DF ms at 1e-4."""
+    Louvain run from the base's static result. value = DF ms at 1e-4.
+
+    Then the stream itself, as main.cxx:101-137 walks it: per batch size,
+    --stream-batches consecutive batches (a tenth of that at 1e-4, a
+    hundredth at 1e-3) read in order, each tidied and applied in place, with
+    ND, DS and DF each starting from its own result on the previous batch;
+    static Louvain runs on the final graph, against which the three final
+    memberships are compared."""
     rank, world, local = dist_info()
     import lvg
     import lvg_build
@@ -727,6 +736,50 @@ def run_temporal(args):
         row["df_speedup_vs_static"] = row["static_ms"] / row["df_ms"]
         rows.append(row)
         Y.close()
+    streams = []
+    for f, nb in ((1e-5, args.stream_batches), (1e-4, max(1, args.stream_batches // 10)),
+                  (1e-3, max(1, args.stream_batches // 100))):
+        k = int(f * E)
+        nb = min(nb, (E - base) // max(k, 1))
+        Y = X.clone()
+        st = {}
+        for m in ("nd", "ds", "df"):
+            st[m] = [lvg.State(Y), lvg.State(Y)]
+            st[m][0].set(prior.membership, prior.vertexWeight, prior.communityWeight)
+        db = None
+        apply_ms, run_ms = [], {m: [] for m in st}
+        pos = base
+        for i in range(nb):
+            a, b = src[pos:pos + k], dst[pos:pos + k]
+            pos += k
+            ins = lvg.HostBatch(np.zeros(0, np.uint32), np.zeros(0, np.uint32), np.zeros(0, np.float32),
+                                np.concatenate([a, b]), np.concatenate([b, a]), np.ones(2 * k, np.float32))
+            t0 = time.perf_counter()
+            tb = Y.apply_batch(ins)
+            apply_ms.append((time.perf_counter() - t0) * 1e3)
+            if db is None:
+                db = lvg.DeviceBatch(Y, tb)
+            else:
+                db.set(tb)
+            for m, meth in (("nd", lvg.METHOD_NAIVE), ("ds", lvg.METHOD_DELTA), ("df", lvg.METHOD_FRONTIER)):
+                r = lvg.run_resident(Y, meth, db, st[m][0], st[m][1], o)
+                run_ms[m].append(r["time"])
+                st[m].reverse()  # this batch's result is the next batch's prior
+        rs = lvg.louvain_static(Y, o)
+        row = {"batch_fraction": f, "batches": nb, "lines_per_batch": k,
+               "apply_ms_mean": float(np.mean(apply_ms)), "static_final_ms": rs.time,
+               "static_final_q": Y.modularity(rs.membership)}
+        for m in st:
+            row[m + "_ms_mean"] = float(np.mean(run_ms[m]))
+            row[m + "_ms_p99"] = float(np.percentile(run_ms[m], 99))
+            row[m + "_final_q"] = Y.modularity(st[m][0].membership())
+        row["df_final_minus_static_q"] = row["df_final_q"] - row["static_final_q"]
+        streams.append(row)
+        for m in st:
+            for x in st[m]:
+                x.close()
+        db.close()
+        Y.close()
     mid = rows[1]
     line = {"metric": "temporal drift: DF-Louvain ms per insertion batch", "value": mid["df_ms"], "unit": "ms",
             "n_gpus": world, "steps": 3, "warmup": 0, "ms_per_step": mid["df_ms"], "higher_is_better": False,
@@ -735,7 +788,7 @@ def run_temporal(args):
                                    f"{E} stream edges (90 % base), insertion-only batches 1e-5/1e-4/1e-3",
                        "base_edges": X.size, "generate_s": tgen, "build_graph_s": tbuild},
             "tuning": dict(tuning, by="lvg_autotune (DF, first batch)", seconds=round(tune_s, 2)),
-            "batches": rows}
+            "batches": rows, "stream": streams}
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
