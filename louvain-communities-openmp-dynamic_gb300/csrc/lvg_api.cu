@@ -1433,7 +1433,10 @@ void apply_plan(lvg_graph *g, const PlanCounts &pc) {
     g->iter_exec = nullptr;
   }
   ensure_ws(g);
-  if (b.edges > g->ws->X) g->ws->allocate(b.span, b.edges, s);
+  // the aggregation levels' edge buffers grow with 1/16 headroom: sized to the
+  // exact count, a stream of insertion batches reallocated them (GBs freed
+  // and allocated again) on every apply
+  if (b.edges > g->ws->X) g->ws->allocate(b.span, b.edges + b.edges / 16, s);
   compute_bins(g, b, g->deg.p, g->bins.p, g->ws->binscratch.p, b.colors);  // synchronises
   build_hub_plan(g, b, g->hubplan);
 }
