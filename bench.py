@@ -601,7 +601,8 @@ def run_serving(args):
         sv.submit(g, lvg.HostBatch.empty())
     sv.drain()
     sweep = []
-    for i, rate in enumerate(sorted({args.rate / 8, args.rate / 4, args.rate / 2})):
+    # below the offered rate, and above it (2x, 4x) to find the rate the server sustains
+    for i, rate in enumerate(sorted({args.rate / 8, args.rate / 4, args.rate / 2, args.rate * 2, args.rate * 4})):
         st = offered(rate, args.seed + 100 + i)
         sweep.append({"offered_rps": st["offered_requests_per_s"], "achieved_rps": st["requests_per_s"],
                       "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "updates_per_s": st["updates_per_s"],
@@ -659,6 +660,9 @@ def run_serving(args):
         "one_at_a_time": {"requests": nb, "requests_per_s": nb / loop_s, "batch_entries_per_s": loop_entries / loop_s,
                           "call": "Graph.apply_batch + lvg_run_resident (DF), one request after another"},
         "requests_per_s_vs_one_at_a_time": st["requests_per_s"] / (nb / loop_s),
+        "max_sustained_rps": max([st["requests_per_s"]] + [x["achieved_rps"] for x in sweep]),
+        "max_sustained_vs_one_at_a_time": max([st["requests_per_s"]] + [x["achieved_rps"] for x in sweep]) /
+                                          (nb / loop_s),
         "clocks": clk.summary(),
     }
     sv.close()
