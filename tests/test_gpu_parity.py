@@ -294,3 +294,32 @@ def test_delta_screening_exact_tie_takes_first_community(cuda, orc, swap):
     rv, rn, rc = orc.ds_mark(Y.download(), tb, q, upd.vertexWeight, upd.communityWeight, Y.edge_weight() / 2)
     assert np.array_equal(v, rv) and np.array_equal(n, rn) and np.array_equal(c, rc)
     assert n[11] and c[la] and not c[lb]
+
+
+def test_delta_screening_flags_with_fractional_weights(cuda, orc):
+    # Random weights in (0, 1] on the graph and the batch: the FP32 screen of
+    # the insertion gains meets close candidates and near-zero gains at
+    # varied magnitudes; its flags must still equal the reference's FP64 rule.
+    x = cuda.planted_partition(20000, 100, 12, 0.7, seed=31)
+    # symmetric weights: a hash of the unordered pair
+    src = np.repeat(np.arange(x.span, dtype=np.uint64), np.diff(x.offsets).astype(np.int64))
+    lo = np.minimum(src, x.keys.astype(np.uint64))
+    hi = np.maximum(src, x.keys.astype(np.uint64))
+    h = (lo * np.uint64(2654435761) + hi * np.uint64(40503)) % np.uint64(1000003)
+    x = cuda.HostGraph(x.offsets, x.keys, (0.05 + 0.95 * h / 1000003.0).astype(np.float32), x.exists)
+    rb = cuda.random_batch(x, 6000, 0.8, seed=33)
+    a, b = rb.ins_src.astype(np.uint64), rb.ins_dst.astype(np.uint64)
+    hb = (np.minimum(a, b) * np.uint64(40503) + np.maximum(a, b) * np.uint64(2654435761)) % np.uint64(999983)
+    raw = cuda.HostBatch(rb.del_src, rb.del_dst, rb.del_w, rb.ins_src, rb.ins_dst,
+                         (0.01 + 0.99 * hb / 999983.0).astype(np.float32))
+    X = cuda.Graph(x)
+    p = cuda.louvain_static(X)
+    Y = X.clone()
+    tb = Y.apply_batch(raw)
+    q = (p.membership, p.vertexWeight, p.communityWeight)
+    upd = cuda.louvain_dynamic_frontier(Y, tb, *q, cuda.LouvainOptions(maxPasses=0))
+    v, n, c = cuda.affected_vertices(Y, cuda.METHOD_DELTA, tb, *q)
+    rv, rn, rc = orc.ds_mark(Y.download(), tb, p.membership, upd.vertexWeight, upd.communityWeight,
+                             Y.edge_weight() / 2)
+    assert np.array_equal(v, rv) and np.array_equal(n, rn) and np.array_equal(c, rc)
+    assert n.sum() > 100
