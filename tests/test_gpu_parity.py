@@ -297,9 +297,10 @@ def test_delta_screening_exact_tie_takes_first_community(cuda, orc, swap):
 
 
 def test_delta_screening_flags_with_fractional_weights(cuda, orc):
-    # Random weights in (0, 1] on the graph and the batch: the FP32 screen of
-    # the insertion gains meets close candidates and near-zero gains at
-    # varied magnitudes; its flags must still equal the reference's FP64 rule.
+    # Weights in (0, 1] from a hash of each unordered pair, on the graph and
+    # the batch: the FP32 screen of the insertion gains meets close
+    # candidates and near-zero gains at varied magnitudes; its flags must
+    # still equal the reference's FP64 rule.
     x = cuda.planted_partition(20000, 100, 12, 0.7, seed=31)
     # symmetric weights: a hash of the unordered pair
     src = np.repeat(np.arange(x.span, dtype=np.uint64), np.diff(x.offsets).astype(np.int64))
