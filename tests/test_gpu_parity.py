@@ -263,13 +263,16 @@ def test_delta_screening_flags_with_large_source_groups(cuda, orc):
     assert n[1] or n[2] or n[3] or n[5] or c.any()  # the large groups were screened
 
 
+@pytest.mark.parametrize("scale", [1.0, 2.0 ** -10, 1e-20, 1e20])
 @pytest.mark.parametrize("swap", [False, True])
-def test_delta_screening_exact_tie_takes_first_community(cuda, orc, swap):
+def test_delta_screening_exact_tie_takes_first_community(cuda, orc, swap, scale):
     # Three 5-cliques (vertices 1-5, 6-10, 11-15); vertex 11 gains one edge
     # into each of the other two, whose totals are equal: the gains tie
     # exactly, the FP32 screen cannot separate them, and the reference's FP64
     # rule gives the community of the first insertion in batch order (to
-    # vertex 3), whichever of the two community ids is smaller.
+    # vertex 3), whichever of the two community ids is smaller. Every weight
+    # is `scale`: at 1e-20 and 1e20 the total weight is outside the FP32
+    # screen's range and every source takes the FP64 rule.
     src, dst = [], []
     for base in (1, 6, 11):
         for a in range(base, base + 5):
@@ -277,16 +280,18 @@ def test_delta_screening_exact_tie_takes_first_community(cuda, orc, swap):
                 if a != b:
                     src.append(a)
                     dst.append(b)
-    x = cuda.csr_from_edges(16, np.array(src, np.uint32), np.array(dst, np.uint32))
+    x = cuda.csr_from_edges(16, np.array(src, np.uint32), np.array(dst, np.uint32),
+                            np.full(len(src), scale, np.float32))
     la, lb = (6, 1) if swap else (1, 6)
     q = np.array([0] + [la] * 5 + [lb] * 5 + [11] * 5, np.uint32)
-    vt = np.array([0] + [4.0] * 15)
+    sw = float(np.float32(scale))
+    vt = np.array([0] + [4.0 * sw] * 15)
     ct = np.zeros(16)
-    ct[[1, 6, 11]] = 20.0
+    ct[[1, 6, 11]] = 20.0 * sw
     ins = [(3, 11), (8, 11), (11, 3), (11, 8)]
     e = np.zeros(0, np.uint32)
     raw = cuda.HostBatch(e, e, np.zeros(0, np.float32), np.array([a for a, _ in ins], np.uint32),
-                         np.array([b for _, b in ins], np.uint32), np.ones(4, np.float32))
+                         np.array([b for _, b in ins], np.uint32), np.full(4, scale, np.float32))
     Y = cuda.Graph(x)
     tb = Y.apply_batch(raw)
     upd = cuda.louvain_dynamic_frontier(Y, tb, q, vt, ct, cuda.LouvainOptions(maxPasses=0))
