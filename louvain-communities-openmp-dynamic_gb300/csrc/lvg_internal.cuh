@@ -334,7 +334,7 @@ void launch_member_degrees(const uint32_t *cmem, const uint32_t *deg, size_t n, 
 void launch_aggregate_chunks(const AggArgs &a, const AggChunks &ch, size_t chunks, uint64_t slots, cudaStream_t s);
 
 // Record a failure message for lvg_last_error() and return `code` (for entry
-// points outside lvg_api.cu).
+// points outside the driver and the C-ABI files).
 int fail_noalloc(int code, const char *msg);
 
 // ---------------------------------------------------------------- batch apply (lvg_update.cu)
