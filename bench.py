@@ -144,8 +144,42 @@ class Dist:
             self.dist.destroy_process_group()
 
 
+class _NvmlReader:
+    """Read-only NVML queries through ctypes (SM clock, its maximum, and the
+    active clock-event reasons); None when NVML cannot be loaded."""
+
+    # nvmlClocksEventReasons bits
+    BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20, "hw_thermal_slowdown": 0x40}
+
+    def __init__(self, index: int):
+        import ctypes
+        self.c = ctypes
+        self.lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        self.h = ctypes.c_void_p()
+        if self.lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(index), ctypes.byref(self.h)) != 0:
+            raise RuntimeError("no NVML device")
+        fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None)
+        self.reasons_fn = fn or self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        v = ctypes.c_uint()
+        self.max_mhz = float(v.value) if self.lib.nvmlDeviceGetMaxClockInfo(self.h, 1, ctypes.byref(v)) == 0 else None
+
+    def sample(self):
+        v, r = self.c.c_uint(), self.c.c_ulonglong()
+        if self.lib.nvmlDeviceGetClockInfo(self.h, 1, self.c.byref(v)) != 0:  # 1 = NVML_CLOCK_SM
+            return None
+        self.reasons_fn(self.h, self.c.byref(r))
+        return float(v.value), {n for n, bit in self.BITS.items() if r.value & bit}
+
+    def close(self):
+        self.lib.nvmlShutdown()
+
+
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """Clock sampling during the timed region: in-process NVML reads every
+    2 ms (a timed region can be a few milliseconds long), and nvidia-smi at
+    100 ms as the fallback where NVML cannot be loaded."""
 
     Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -155,8 +189,19 @@ class Clocks:
         self.index = index
         self.proc = None
         self.lines = []
+        self.nvml = None
+        self.samples = []
+        self.stop = threading.Event()
 
     def __enter__(self):
+        try:
+            self.nvml = _NvmlReader(self.index)
+        except Exception:
+            self.nvml = None
+        if self.nvml:
+            self.t = threading.Thread(target=self._poll, daemon=True)
+            self.t.start()
+            return self
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "100"],
@@ -173,11 +218,26 @@ class Clocks:
             self.proc = None
         return self
 
+    def _poll(self):
+        while not self.stop.is_set():
+            x = self.nvml.sample()
+            if x:
+                self.samples.append(x)
+            time.sleep(0.002)
+
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
     def __exit__(self, *a):
+        if self.nvml:
+            self.stop.set()
+            self.t.join(timeout=2)
+            if not self.samples:
+                x = self.nvml.sample()
+                if x:
+                    self.samples.append(x)
+            self.nvml.close()
         if self.proc:
             # at least one sample taken from the region's start on
             t0 = time.time()
@@ -190,6 +250,12 @@ class Clocks:
                 self.proc.kill()
 
     def summary(self):
+        if self.nvml is not None:
+            if not self.samples:
+                return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0, "source": "nvml"}
+            reasons = set().union(*(r for _, r in self.samples))
+            return {"sm_mhz": statistics.median(m for m, _ in self.samples), "sm_max_mhz": self.nvml.max_mhz,
+                    "reasons": sorted(reasons), "samples": len(self.samples), "source": "nvml, 2 ms"}
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in self.lines:
@@ -205,9 +271,9 @@ class Clocks:
                 if v.lower().startswith("active"):
                     reasons.add(n)
         if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0, "source": "nvidia-smi"}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "source": "nvidia-smi, 100 ms"}
 
 
 def make_inputs(lvg, args):
