@@ -172,8 +172,10 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot
     BinBounds bb;
     for (int b = 0; b <= NUM_BINS; ++b) bb.start[b] = lv.bin_start[k * NUM_BINS + b];
     uint32_t *wlc = W.wl_count.p + size_t(k) * NUM_BINS;
-    if (bb.start[NUM_BINS - 1] > bb.start[1])
-      launch_compact_active(lv.bins, bb, W.vaff.p, fa, W.wl.p, wlc, s, uc ? lv.gid : nullptr, uc ? uc->gact : nullptr);
+    if (bb.start[NUM_BINS - 1] > bb.start[1]) {
+      if (K == 1 && !uc) launch_compact_active_scan(lv, bb, W.vaff.p, fa, W.wl.p, wlc, s);
+      else launch_compact_active(lv.bins, bb, W.vaff.p, fa, W.wl.p, wlc, s, uc ? lv.gid : nullptr, uc ? uc->gact : nullptr);
+    }
     if (conc) {  // fork
       LVG_CUDA(cudaEventRecord(g->fork_ev, s));
       for (auto a : g->aux) LVG_CUDA(cudaStreamWaitEvent(a, g->fork_ev, 0));

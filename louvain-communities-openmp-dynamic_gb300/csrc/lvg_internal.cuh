@@ -300,6 +300,10 @@ void launch_merge_marks(uint8_t *vaff, uint8_t *mark, size_t n, cudaStream_t s);
 struct BinBounds {
   uint64_t start[NUM_BINS + 1];
 };
+// One colour class, no graph union: the same worklists from a sequential
+// pass over the level's flags.
+void launch_compact_active_scan(const Level &g, const BinBounds &bb, const uint8_t *vaff, const uint8_t *fa,
+                                uint32_t *wl, uint32_t *wl_count, cudaStream_t s);
 // Graph unions: only vertices whose graph still moves (gact[gid[u]]).
 void launch_compact_active(const uint32_t *bins, const BinBounds &bb, const uint8_t *vaff, const uint8_t *fa,
                            uint32_t *wl, uint32_t *wl_count, cudaStream_t s, const uint32_t *gid = nullptr,

@@ -707,6 +707,67 @@ __global__ void compact_active_kernel(const uint32_t *bins, BinBounds bb, const 
   }
 }
 
+// The same for a level with one colour class (no graph union): a sequential
+// pass over the flags (and existence bytes), sixteen per lane and load, in
+// place of a gather of every listed vertex's flag; the degree is read only
+// for the active vertices, which a warp appends in rounds (one active vertex
+// per lane and round, warp-aggregated per bin). The worklists get the same
+// vertices: existing ones of bins 1..NUM_BINS-2.
+__global__ void compact_active_scan_kernel(const uint32_t *deg, const uint8_t *ex, size_t span, BinBounds bb,
+                                           const uint8_t *vaff, const uint8_t *fa, uint32_t *wl,
+                                           uint32_t *wl_count) {
+  const int lane = threadIdx.x & 31;
+  const size_t words = (span + 15) / 16;
+  for (size_t wbase = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32 * 32; wbase < words;
+       wbase += size_t(gridDim.x) * blockDim.x) {
+    const size_t w = wbase + lane;
+    unsigned act = 0;  // bit j: vertex 16 w + j is active
+    if (w < words) {
+      const size_t u0 = w * 16;
+      if (u0 + 16 <= span) {
+        const uint4 f = reinterpret_cast<const uint4 *>(vaff)[w];
+        const uint32_t fw[4] = {f.x, f.y, f.z, f.w};
+        uint32_t ew[4] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu};
+        uint32_t aw[4] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu};
+        if ((fw[0] | fw[1] | fw[2] | fw[3]) && ex) {
+          const uint4 e = reinterpret_cast<const uint4 *>(ex)[w];
+          ew[0] = e.x; ew[1] = e.y; ew[2] = e.z; ew[3] = e.w;
+        }
+        if ((fw[0] | fw[1] | fw[2] | fw[3]) && fa) {
+          const uint4 e = reinterpret_cast<const uint4 *>(fa)[w];
+          aw[0] = e.x; aw[1] = e.y; aw[2] = e.z; aw[3] = e.w;
+        }
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const uint32_t sh = 8u * (j & 3);
+          if (((fw[j >> 2] >> sh) & 0xffu) && ((ew[j >> 2] >> sh) & 0xffu) && ((aw[j >> 2] >> sh) & 0xffu))
+            act |= 1u << j;
+        }
+      } else {
+        for (size_t u = u0; u < span; ++u)
+          if (vaff[u] && (!ex || ex[u]) && (!fa || fa[u])) act |= 1u << (u - u0);
+      }
+    }
+    while (__any_sync(0xffffffffu, act != 0u)) {
+      int b = -1;
+      uint32_t u = 0;
+      if (act) {
+        const int j = __ffs(act) - 1;
+        act &= act - 1u;
+        u = uint32_t(w * 16 + j);
+        const int x = degree_bin(deg[u]);
+        if (x >= 1 && x <= NUM_BINS - 2) b = x;
+      }
+      const unsigned grp = __match_any_sync(0xffffffffu, b);
+      const int leader = __ffs(grp) - 1;
+      uint32_t at = 0;
+      if (b >= 0 && lane == leader) at = atomicAdd(&wl_count[b], uint32_t(__popc(grp)));
+      at = __shfl_sync(0xffffffffu, at, leader);
+      if (b >= 0) wl[bb.start[b] + at + __popc(grp & ((1u << lane) - 1u))] = u;
+    }
+  }
+}
+
 __global__ void gather_u32_kernel(const uint32_t *idx, size_t n, const uint32_t *src, uint32_t *dst) {
   GRID_STRIDE(i, n) dst[i] = src[idx[i]];
 }
@@ -959,6 +1020,14 @@ void launch_compact_active(const uint32_t *bins, const BinBounds &bb, const uint
   const uint64_t n = bb.start[NUM_BINS - 1] - bb.start[1];
   if (!n) return;
   compact_active_kernel<<<grid_for(n, 256), 256, 0, s>>>(bins, bb, vaff, fa, gid, gact, wl, wl_count);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_compact_active_scan(const Level &g, const BinBounds &bb, const uint8_t *vaff, const uint8_t *fa,
+                                uint32_t *wl, uint32_t *wl_count, cudaStream_t s) {
+  if (!g.span) return;
+  compact_active_scan_kernel<<<grid_for((g.span + 15) / 16, 256), 256, 0, s>>>(g.deg, g.ex, g.span, bb, vaff, fa, wl,
+                                                                                  wl_count);
   LVG_CHECK_LAUNCH();
 }
 
