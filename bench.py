@@ -17,8 +17,11 @@ Arms:
                        with host arrays (pinned): batch + prior state uploaded,
                        result downloaded, inside the timed region.
   --impl reference     the CPU implementation of the path on this host's
-                       cores (the oracle's port of the reference, OpenMP, all
-                       threads), same graph, batch and metric.
+                       cores, all threads: the reference's own headers
+                       compiled here (from its checkout, or from the copy the
+                       oracle recipe stages beside the tree), else the
+                       oracle's port; same graph, batch and metric, the prior
+                       from its own static Louvain (main.cxx:89).
 
 Multi-GPU: the path does not shard (replicas only); under torchrun every rank
 runs an independent replica on its own GPU and rank 0 reports the aggregate.
@@ -83,8 +86,12 @@ def parse():
     p.add_argument("--size-max", type=int, default=100000)
     p.add_argument("--workers", type=int, default=16)
     p.add_argument("--budget-gb", type=float, default=120.0)
-    p.add_argument("--coalesce", type=int, default=1 << 18,
-                   help="serving: serve a graph's queued requests as one batch of up to this many entries (0: off)")
+    p.add_argument("--coalesce", type=int, default=0,
+                   help="serving headline: serve a graph's queued requests as one batch of up to this many "
+                        "entries (default 0: every request runs alone, with its own result)")
+    p.add_argument("--coalesced-mode", type=int, default=1 << 18,
+                   help="serving: after the headline, the same arrivals again with coalescing up to this many "
+                        "entries, reported as its own labelled mode (0: skip)")
     p.add_argument("--ncu-steps", type=int, default=0,
                    help="profiling mode: set up as usual, then run this many steps between "
                         "cudaProfilerStart/Stop (for ncu --profile-from-start off) and exit")
@@ -155,21 +162,37 @@ class _NvmlReader:
         import ctypes
         self.c = ctypes
         self.lib = ctypes.CDLL("libnvidia-ml.so.1")
-        if self.lib.nvmlInit_v2() != 0:
+        L, h, u, ull = self.lib, ctypes.c_void_p, ctypes.c_uint, ctypes.c_ulonglong
+        L.nvmlInit_v2.argtypes = []
+        L.nvmlInit_v2.restype = ctypes.c_int
+        L.nvmlShutdown.argtypes = []
+        L.nvmlShutdown.restype = ctypes.c_int
+        L.nvmlDeviceGetHandleByIndex_v2.argtypes = [u, ctypes.POINTER(h)]
+        L.nvmlDeviceGetHandleByIndex_v2.restype = ctypes.c_int
+        L.nvmlDeviceGetClockInfo.argtypes = [h, ctypes.c_int, ctypes.POINTER(u)]
+        L.nvmlDeviceGetClockInfo.restype = ctypes.c_int
+        L.nvmlDeviceGetMaxClockInfo.argtypes = [h, ctypes.c_int, ctypes.POINTER(u)]
+        L.nvmlDeviceGetMaxClockInfo.restype = ctypes.c_int
+        if L.nvmlInit_v2() != 0:
             raise RuntimeError("nvmlInit failed")
-        self.h = ctypes.c_void_p()
-        if self.lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(index), ctypes.byref(self.h)) != 0:
+        self.h = h()
+        if L.nvmlDeviceGetHandleByIndex_v2(u(index), ctypes.byref(self.h)) != 0:
             raise RuntimeError("no NVML device")
-        fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None)
-        self.reasons_fn = fn or self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
-        v = ctypes.c_uint()
-        self.max_mhz = float(v.value) if self.lib.nvmlDeviceGetMaxClockInfo(self.h, 1, ctypes.byref(v)) == 0 else None
+        fn = getattr(L, "nvmlDeviceGetCurrentClocksEventReasons", None)
+        self.reasons_fn = fn or L.nvmlDeviceGetCurrentClocksThrottleReasons
+        self.reasons_fn.argtypes = [h, ctypes.POINTER(ull)]
+        self.reasons_fn.restype = ctypes.c_int
+        v = u()
+        self.max_mhz = float(v.value) if L.nvmlDeviceGetMaxClockInfo(self.h, 1, ctypes.byref(v)) == 0 else None
 
     def sample(self):
+        """(SM MHz, set of active reasons) — the set is None when the reasons
+        could not be read, so an unread sample never looks unthrottled."""
         v, r = self.c.c_uint(), self.c.c_ulonglong()
         if self.lib.nvmlDeviceGetClockInfo(self.h, 1, self.c.byref(v)) != 0:  # 1 = NVML_CLOCK_SM
             return None
-        self.reasons_fn(self.h, self.c.byref(r))
+        if self.reasons_fn(self.h, self.c.byref(r)) != 0:
+            return float(v.value), None
         return float(v.value), {n for n, bit in self.BITS.items() if r.value & bit}
 
     def close(self):
@@ -252,10 +275,16 @@ class Clocks:
     def summary(self):
         if self.nvml is not None:
             if not self.samples:
-                return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0, "source": "nvml"}
-            reasons = set().union(*(r for _, r in self.samples))
-            return {"sm_mhz": statistics.median(m for m, _ in self.samples), "sm_max_mhz": self.nvml.max_mhz,
-                    "reasons": sorted(reasons), "samples": len(self.samples), "source": "nvml, 2 ms"}
+                return {"sm_mhz": None, "sm_max_mhz": None, "reasons": None, "samples": 0, "source": "nvml"}
+            read = [r for _, r in self.samples if r is not None]
+            unread = len(self.samples) - len(read)
+            # reasons None: no sample's reasons could be read (unknown, not "none")
+            reasons = sorted(set().union(*read)) if read else None
+            out = {"sm_mhz": statistics.median(m for m, _ in self.samples), "sm_max_mhz": self.nvml.max_mhz,
+                   "reasons": reasons, "samples": len(self.samples), "source": "nvml, 2 ms"}
+            if unread:
+                out["reasons_unread_samples"] = unread
+            return out
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in self.lines:
@@ -271,7 +300,7 @@ class Clocks:
                 if v.lower().startswith("active"):
                     reasons.add(n)
         if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0, "source": "nvidia-smi"}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": None, "samples": 0, "source": "nvidia-smi"}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
                 "samples": len(sm), "source": "nvidia-smi, 100 ms"}
 
@@ -315,8 +344,39 @@ def cpu_threads() -> int:
         return os.cpu_count() or 1
 
 
+PRIOR = "the arm's own static Louvain result on the base graph (main.cxx:89)"
+
+
+def bench_config(args, y, nupd, batch_entries, world):
+    """The workload's config, identical in both arms."""
+    return {"workload": workload_name(args), "vertices": y.order, "edges": y.num_edges, "batch_updates": nupd,
+            "batch_entries": batch_entries, "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2 (CSR %.1f GB)" % (y.num_edges * 8 / 1e9), "prior": PRIOR}
+
+
+def reference_harness():
+    """The harness over the reference's own headers (oracle/ref_harness.cxx),
+    built from the checkout or from the headers staged next to it, or None
+    where neither exists (then the oracle's port stands in)."""
+    from oracle import oracle as O
+
+    try:
+        O.build(ref=None)
+    except Exception:
+        return None
+    return O.Reference() if O.reference_available() else None
+
+
 def run_reference(args):
-    """The CPU implementation (oracle's port of the reference), all host threads."""
+    """The CPU implementation on this host's cores (all threads): the
+    reference's own louvainStaticOmp / louvainDynamicFrontierOmp compiled from
+    its headers where they are available (kind "reference"), else the oracle's
+    port (kind "port"). As main.cxx:89-125 runs it: static Louvain on the base
+    graph gives the prior, the batch is tidied and applied in place, then
+    dynamic-frontier Louvain. The warm-up and the timed steps are each one call
+    with `repeat` repetitions (the reference's LouvainResult::time is the mean
+    over them), since every call also allocates span- and edge-sized buffers
+    outside its timer."""
     rank, world, _ = dist_info()
     if world > 1 and rank != 0:
         return 0
@@ -326,27 +386,66 @@ def run_reference(args):
 
     lvg_build.build_graphgen()
     O.build(ref=False)
-    orc = O.Oracle()
     x, b, y, nupd, tgen = make_inputs(lvg, args)
     T = cpu_threads()
-    opts = O.options()
-    m, vt, ct, info = orc.louvain(x, 0, threads=T, opts=opts)  # prior (untimed), as main.cxx:89
-    times = []
-    for i in range(args.warmup + args.steps):
-        _, _, _, inf = orc.louvain(y, 3, b, m, vt, ct, threads=T, opts=opts)
-        if i >= args.warmup:
-            times.append(inf["time"])
-    ms = float(np.mean(times))
+    ref = reference_harness()
+    orc = O.Oracle()
+    extra = {}
+    if ref is not None:
+        kind = "reference"
+        ref.threads(T)
+        t0 = time.time()
+        R = ref.graph(x)
+        t_build = time.time() - t0
+        m, vt, ct, sinfo = R.louvain(0)                      # the prior (untimed), main.cxx:89
+        q_base = R.modularity(m)
+        _, tidy = R.apply_batch(b, csr=False)                # main.cxx:108-109, in place
+        tb = lvg.HostBatch(*tidy)
+        assert R.size() == y.num_edges
+        R.louvain(3, tb, m, vt, ct, opts=O.options(repeat=max(1, args.warmup)))
+        md, _, _, inf = R.louvain(3, tb, m, vt, ct, opts=O.options(repeat=args.steps))
+        ms = float(inf["time"])
+        q_df = R.modularity(md)
+        ms_static, q_static = None, None
+        if not args.no_cpu_baseline:
+            ms2, _, _, sinf = R.louvain(0)
+            ms_static, q_static = float(sinf["time"]), R.modularity(ms2)
+        # the port beside it, from the same prior (a cross-check of the port)
+        pt, pq = [], None
+        for _ in range(2):
+            pm, _, _, pinf = orc.louvain(y, 3, tb, m, vt, ct, threads=T)
+            pt.append(pinf["time"])
+            pq = pm
+        extra = {"modularity": {"df": q_df, "static_base": q_base, "static_updated": q_static},
+                 "static_reference": {"ms": ms_static, "modularity": q_static,
+                                      "call": "louvainStaticOmp on the updated graph, one run"},
+                 "port_cross_check": {"ms_per_step": float(np.mean(pt)), "modularity": orc.modularity(y, pq),
+                                      "call": "the oracle's port (orc_louvain, DF) from the same prior"},
+                 "setup_s": {"generate": round(tgen, 1), "reference_graph_build": round(t_build, 1)}}
+        sample = (f"louvainDynamicFrontierOmp of the reference's own headers (main.sh:54 flags), one call of "
+                  f"{args.steps} repetitions after one of {max(1, args.warmup)} (LouvainResult::time, mean over "
+                  f"the repetitions), from its own static result on the base graph")
+    else:
+        kind = "port"
+        opts = O.options()
+        m, vt, ct, info = orc.louvain(x, 0, threads=T, opts=opts)  # prior (untimed), as main.cxx:89
+        times = []
+        for i in range(args.warmup + args.steps):
+            md, _, _, inf = orc.louvain(y, 3, b, m, vt, ct, threads=T, opts=opts)
+            if i >= args.warmup:
+                times.append(inf["time"])
+        ms = float(np.mean(times))
+        extra = {"modularity": {"df": orc.modularity(y, md), "static_base": orc.modularity(x, m)}}
+        sample = (f"{args.steps} dynamic-frontier runs of the oracle's port on the full graph (LouvainResult::time: "
+                  f"init + mark + passes), from its own static result; the reference's headers were not available")
     value = y.num_edges / (ms / 1e3)
     line = {"metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": workload_name(args), "vertices": x.order, "edges": y.num_edges,
-                       "batch_updates": nupd, "l2": "inputs larger than L2"},
-            "cpu_baseline": {"value": value, "unit": "edges/s", "cores": T, "kind": "port",
-                             "sample": f"{args.steps} dynamic-frontier runs on the full graph (the port's "
-                                       f"LouvainResult::time: init + mark + passes)"},
+            "config": bench_config(args, y, nupd, b.num_deletions + b.num_insertions, world),
+            "cpu_baseline": {"value": value, "unit": "edges/s", "cores": T, "kind": kind, "sample": sample},
             "e2e": {"value": value, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    line.update(extra)
     print(json.dumps(line), flush=True)
     return 0
 
@@ -502,9 +601,7 @@ def run_gpu(args):
         "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": workload_name(args), "vertices": y.order, "edges": E, "batch_updates": nupd,
-                   "batch_entries": b.num_deletions + b.num_insertions, "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2 (CSR %.1f GB)" % (E * 8 / 1e9)},
+        "config": bench_config(args, y, nupd, b.num_deletions + b.num_insertions, world),
         "e2e": {"value": world * E / (e2e_ms_max / 1e3), "unit": "edges/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms_max,
                 "call": "lvg_frontier (drop-in for louvainDynamicFrontierOmp), pinned host arrays",
@@ -544,6 +641,10 @@ def run_gpu(args):
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args, y, b, prior)
+        qs = line["cpu_baseline"].pop("static_modularity", None)
+        if qs is not None:
+            line["static_gpu"]["modularity_cpu_static"] = qs
+            line["static_gpu"]["abs_diff_vs_cpu_static"] = abs(q_static - qs)
     if rank == 0:
         print(json.dumps(line), flush=True)
     dist.close()
@@ -551,23 +652,42 @@ def run_gpu(args):
 
 
 def cpu_baseline(args, y, b, prior):
-    """The oracle's port of the reference, on the same updated graph, batch and prior."""
+    """The CPU implementation on the same updated graph, batch and prior (the
+    GPU's static result): the reference's own louvainDynamicFrontierOmp where
+    its headers are available, else the oracle's port; plus one static run on
+    the updated graph, whose modularity the GPU's static result is compared
+    with."""
     from oracle import oracle as O
 
     O.build(ref=False)
-    orc = O.Oracle()
     T = cpu_threads()
-    times, q = [], None
-    for _ in range(max(1, args.cpu_steps)):
-        m, _, _, inf = orc.louvain(y, 3, b, prior.membership, prior.vertexWeight, prior.communityWeight,
-                                   threads=T)
-        times.append(inf["time"])
-        q = m
-    ms = float(np.mean(times))
-    return {"value": y.num_edges / (ms / 1e3), "unit": "edges/s", "cores": T, "kind": "port",
-            "sample": f"{len(times)} dynamic-frontier runs on the full graph from the GPU's static prior "
-                      f"(LouvainResult::time of the port: init + mark + passes)",
-            "ms_per_step": ms, "modularity": orc.modularity(y, q)}
+    q = (prior.membership, prior.vertexWeight, prior.communityWeight)
+    ref = reference_harness()
+    reps = max(1, args.cpu_steps)
+    if ref is not None:
+        ref.threads(T)
+        R = ref.graph(y)
+        m, _, _, inf = R.louvain(3, b, *q, opts=O.options(repeat=reps))
+        ms, qd = float(inf["time"]), R.modularity(m)
+        sm = R.louvain(0)[0]
+        qs = R.modularity(sm)
+        kind = "reference"
+        sample = (f"louvainDynamicFrontierOmp of the reference's own headers, one call of {reps} repetitions "
+                  f"(LouvainResult::time, mean) on the full graph from the GPU's static prior; "
+                  f"static_modularity: one louvainStaticOmp run on the updated graph")
+    else:
+        orc = O.Oracle()
+        times = []
+        for _ in range(reps):
+            m, _, _, inf = orc.louvain(y, 3, b, *q, threads=T)
+            times.append(inf["time"])
+        ms, qd = float(np.mean(times)), orc.modularity(y, m)
+        qs = orc.modularity(y, orc.louvain(y, 0, threads=T)[0])
+        kind = "port"
+        sample = (f"{reps} dynamic-frontier runs of the oracle's port on the full graph from the GPU's static "
+                  f"prior (LouvainResult::time); static_modularity: one static run on the updated graph")
+    return {"value": y.num_edges / (ms / 1e3), "unit": "edges/s", "cores": T, "kind": kind, "sample": sample,
+            "ms_per_step": ms, "modularity": qd, "static_modularity": qs}
 
 
 def run_serving(args):
@@ -679,6 +799,21 @@ def run_serving(args):
     n_req = st["requests"]
     entries = st["batch_entries"]
     offered_s = n_req / st["offered_requests_per_s"]
+    coalesced = None
+    if args.coalesced_mode and not args.coalesce:
+        # the same kind of arrivals with coalescing: queued requests of a graph
+        # share one run (and its result), a throughput mode, labelled as such
+        sv.set_coalesce(args.coalesced_mode)
+        cst = offered(args.rate, args.seed + 8)
+        ovl = offered(args.rate * 4, args.seed + 9)
+        sv.set_coalesce(0)
+        coalesced = {"mode": f"coalescing up to {args.coalesced_mode} entries: a graph's queued requests run as "
+                             "one batch and share its result (a group ends at a conflicting request)",
+                     "offered_rps": cst["offered_requests_per_s"], "achieved_rps": cst["requests_per_s"],
+                     "p50_ms": cst["p50_ms"], "p99_ms": cst["p99_ms"], "updates_per_s": cst["updates_per_s"],
+                     "at_4x_rate": {"offered_rps": ovl["offered_requests_per_s"],
+                                    "achieved_rps": ovl["requests_per_s"], "p50_ms": ovl["p50_ms"],
+                                    "p99_ms": ovl["p99_ms"], "updates_per_s": ovl["updates_per_s"]}}
 
     # the plain per-graph loop the server is compared with: requests of the
     # same kind one at a time on one thread (tidy + apply, then DF from the
@@ -713,7 +848,8 @@ def run_serving(args):
         "config": {"workload": f"serving: {len(ids)} resident R-MAT graphs scale {args.scale_min}-{args.scale_max} "
                                f"ef16, Poisson {args.rate:g} req/s for {args.duration:g} s, log-uniform "
                                f"[{args.size_min}, {args.size_max}] updates 80/20, {args.workers} workers, "
-                               f"coalescing up to {args.coalesce} entries",
+                               + (f"coalescing up to {args.coalesce} entries" if args.coalesce
+                                  else "every request served alone (no coalescing)"),
                    "graphs": len(ids), "refused_by_admission": refused, "hbm_budget_gb": args.budget_gb,
                    "hbm_reserved_gb": st["hbm_reserved"] / 2**30, "requests": n_req, "batch_entries": entries,
                    "setup_s": t_setup},
@@ -731,6 +867,8 @@ def run_serving(args):
                                           (nb / loop_s),
         "clocks": clk.summary(),
     }
+    if coalesced:
+        line["coalesced_mode"] = coalesced
     sv.close()
     if rank == 0:
         print(json.dumps(line), flush=True)

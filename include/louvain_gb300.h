@@ -304,8 +304,12 @@ typedef struct lvg_server_options {
   size_t      hbm_budget;  /* admission budget in bytes for resident graphs (default 120 GiB) */
   int         method;      /* LVG_METHOD_NAIVE / _DELTA / _FRONTIER (default FRONTIER) */
   lvg_options louvain;     /* options of every run */
-  size_t      coalesce;    /* 0: one request per run; else serve a graph's queued requests as one batch of
-                              up to this many entries (their union, tidied and applied at once) */
+  size_t      coalesce;    /* 0 (default): one request per run; else serve a graph's queued requests as
+                              one batch of up to this many entries (their union, tidied and applied at
+                              once). Every request of such a group gets the group's result; a group
+                              ends before a request that inserts or deletes an edge an earlier
+                              request of the group inserts, or inserts one it deletes, so the graph
+                              after a group equals the graph after its requests one by one */
 } lvg_server_options;
 typedef struct lvg_request_info {
   uint64_t ticket;
@@ -314,6 +318,8 @@ typedef struct lvg_request_info {
   int      iterations, passes;
   uint64_t affected;
   size_t   tidy_deletions, tidy_insertions;         /* the batch after the tidy */
+  uint64_t group;      /* ticket of the first request of the run that answered this one */
+  int      coalesced;  /* requests answered by that run (1: served alone) */
 } lvg_request_info;
 typedef struct lvg_server_stats_t {
   uint64_t completed, failed, updates;  /* updates = batch entries of completed requests */
@@ -331,6 +337,9 @@ int lvg_server_create(const lvg_server_options *o, lvg_server **out);
  * With take_ownership the server destroys the graph at the end. */
 int lvg_server_add_graph(lvg_server *sv, lvg_graph *g, int take_ownership, const uint32_t *q, const double *qvtot,
                          const double *qctot, int *graph_id);
+/* Change the coalescing cap (lvg_server_options.coalesce) of a running
+ * server; groups formed afterwards use it. */
+int lvg_server_set_coalesce(lvg_server *sv, size_t coalesce);
 /* Queue a batch for a graph (copied; the caller's arrays may be reused). */
 int lvg_server_submit(lvg_server *sv, int graph_id, const lvg_batch *b, uint64_t *ticket);
 /* Wait for a request; returns its status. Each ticket can be waited once. */
@@ -441,8 +450,9 @@ int lvg_get_stats(const lvg_graph *g, lvg_stats *out);
  * latency-critical loop that must not pay cudaMalloc's cost and implicit
  * synchronisation, or a deployment that forbids allocation after start-up).
  * Same result as lvg_modularity, but every pointer is a caller-owned DEVICE
- * pointer: offsets[span+1], keys/weights[offsets[span]], exists[span] (may be
- * NULL: every slot exists), membership[span], and out (one double, written on
+ * pointer: offsets[span+1], keys/weights[offsets[span]] (never NULL, even for
+ * a graph without edges), exists[span] (may be NULL: every slot exists),
+ * membership[span], and out (one double, written on
  * the device). M <= 0 means half the total edge weight. `stream` is a
  * cudaStream_t (NULL: the default stream); the call is asynchronous on it.
  * The function allocates nothing: its scratch is a fixed device array of

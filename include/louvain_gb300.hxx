@@ -60,6 +60,30 @@ struct LouvainResult {
   float localMoveTime = 0;
   float aggregationTime = 0;
   size_t affectedVertices = 0;
+
+  LouvainResult() = default;
+  /** From vectors the caller hands over (rvalues); scalar fields as given.
+   * Same parameters and defaults as the reference's constructor
+   * (inc/louvain.hxx:118-119). */
+  LouvainResult(std::vector<K> &&membership, std::vector<W> &&vertexWeight, std::vector<W> &&communityWeight,
+                int iterations = 0, int passes = 0, float time = 0, float markingTime = 0,
+                float initializationTime = 0, float firstPassTime = 0, float localMoveTime = 0,
+                float aggregationTime = 0, size_t affectedVertices = 0)
+      : membership(std::move(membership)), vertexWeight(std::move(vertexWeight)),
+        communityWeight(std::move(communityWeight)), iterations(iterations), passes(passes), time(time),
+        markingTime(markingTime), initializationTime(initializationTime), firstPassTime(firstPassTime),
+        localMoveTime(localMoveTime), aggregationTime(aggregationTime), affectedVertices(affectedVertices) {}
+  /** From the caller's vectors (lvalues), whose contents are moved in and
+   * which are left empty, as the reference's second constructor does
+   * (inc/louvain.hxx:139-140). */
+  LouvainResult(std::vector<K> &membership, std::vector<W> &vertexWeight, std::vector<W> &communityWeight,
+                int iterations = 0, int passes = 0, float time = 0, float markingTime = 0,
+                float initializationTime = 0, float firstPassTime = 0, float localMoveTime = 0,
+                float aggregationTime = 0, size_t affectedVertices = 0)
+      : membership(std::move(membership)), vertexWeight(std::move(vertexWeight)),
+        communityWeight(std::move(communityWeight)), iterations(iterations), passes(passes), time(time),
+        markingTime(markingTime), initializationTime(initializationTime), firstPassTime(firstPassTime),
+        localMoveTime(localMoveTime), aggregationTime(aggregationTime), affectedVertices(affectedVertices) {}
 };
 
 namespace detail {

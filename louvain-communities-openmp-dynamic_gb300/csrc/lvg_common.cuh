@@ -52,6 +52,7 @@ constexpr double GAIN_FIX = 65536.0;
 // Device error flags (bit set in Engine::d_err).
 constexpr uint32_t ERR_TABLE_FULL = 1u;
 constexpr uint32_t ERR_BAD_ID = 2u;  // an input id was >= span
+constexpr uint32_t ERR_WORKLIST = 4u;  // a worklist append fell outside its degree bin's slice
 
 // Degree bins of the per-vertex (and per-community) reduce kernels.
 //   bin 0: degree 0 (nothing to scan)

@@ -32,6 +32,7 @@ void read_counters(lvg_graph *g) {
     unsigned e = g->hctr.p->err;
     LVG_CUDA(cudaMemsetAsync(&g->ctr.p->err, 0, sizeof(unsigned), g->stream));
     if (e & ERR_BAD_ID) throw Error(LVG_EINVAL, "prior membership id >= span");
+    if (e & ERR_WORKLIST) throw Error(LVG_ECUDA, "worklist append outside its degree bin (stale degree bins)");
     throw Error(LVG_ETIMEOUT, "device hash table overflow guard tripped (err=" + std::to_string(e) + ")");
   }
 }
@@ -173,7 +174,7 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot
     for (int b = 0; b <= NUM_BINS; ++b) bb.start[b] = lv.bin_start[k * NUM_BINS + b];
     uint32_t *wlc = W.wl_count.p + size_t(k) * NUM_BINS;
     if (bb.start[NUM_BINS - 1] > bb.start[1]) {
-      if (K == 1 && !uc) launch_compact_active_scan(lv, bb, W.vaff.p, fa, W.wl.p, wlc, s);
+      if (K == 1 && !uc) launch_compact_active_scan(lv, bb, W.vaff.p, fa, W.wl.p, wlc, g->ctr.p, s);
       else launch_compact_active(lv.bins, bb, W.vaff.p, fa, W.wl.p, wlc, s, uc ? lv.gid : nullptr, uc ? uc->gact : nullptr);
     }
     if (conc) {  // fork

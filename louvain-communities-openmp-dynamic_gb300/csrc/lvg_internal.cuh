@@ -301,9 +301,10 @@ struct BinBounds {
   uint64_t start[NUM_BINS + 1];
 };
 // One colour class, no graph union: the same worklists from a sequential
-// pass over the level's flags.
+// pass over the level's flags. An append outside its bin's slice sets
+// ERR_WORKLIST in ctr->err (degrees changed without recomputing the bins).
 void launch_compact_active_scan(const Level &g, const BinBounds &bb, const uint8_t *vaff, const uint8_t *fa,
-                                uint32_t *wl, uint32_t *wl_count, cudaStream_t s);
+                                uint32_t *wl, uint32_t *wl_count, Counters *ctr, cudaStream_t s);
 // Graph unions: only vertices whose graph still moves (gact[gid[u]]).
 void launch_compact_active(const uint32_t *bins, const BinBounds &bb, const uint8_t *vaff, const uint8_t *fa,
                            uint32_t *wl, uint32_t *wl_count, cudaStream_t s, const uint32_t *gid = nullptr,

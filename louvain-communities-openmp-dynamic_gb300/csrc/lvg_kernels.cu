@@ -713,9 +713,13 @@ __global__ void compact_active_kernel(const uint32_t *bins, BinBounds bb, const 
 // for the active vertices, which a warp appends in rounds (one active vertex
 // per lane and round, warp-aggregated per bin). The worklists get the same
 // vertices: existing ones of bins 1..NUM_BINS-2.
+// The bin is recomputed from deg[u], so the append is bounded by the bin's
+// slice [bb.start[b], bb.start[b+1]) as well: should deg ever change without
+// the bins being recomputed, an append past the slice is dropped and flagged
+// (ERR_WORKLIST) instead of writing into the next bin's slice.
 __global__ void compact_active_scan_kernel(const uint32_t *deg, const uint8_t *ex, size_t span, BinBounds bb,
                                            const uint8_t *vaff, const uint8_t *fa, uint32_t *wl,
-                                           uint32_t *wl_count) {
+                                           uint32_t *wl_count, unsigned int *err) {
   const int lane = threadIdx.x & 31;
   const size_t words = (span + 15) / 16;
   for (size_t wbase = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32 * 32; wbase < words;
@@ -763,7 +767,11 @@ __global__ void compact_active_scan_kernel(const uint32_t *deg, const uint8_t *e
       uint32_t at = 0;
       if (b >= 0 && lane == leader) at = atomicAdd(&wl_count[b], uint32_t(__popc(grp)));
       at = __shfl_sync(0xffffffffu, at, leader);
-      if (b >= 0) wl[bb.start[b] + at + __popc(grp & ((1u << lane) - 1u))] = u;
+      if (b >= 0) {
+        const uint32_t slot = at + __popc(grp & ((1u << lane) - 1u));
+        if (slot < bb.start[b + 1] - bb.start[b]) wl[bb.start[b] + slot] = u;
+        else atomicOr(err, ERR_WORKLIST);
+      }
     }
   }
 }
@@ -1024,10 +1032,10 @@ void launch_compact_active(const uint32_t *bins, const BinBounds &bb, const uint
 }
 
 void launch_compact_active_scan(const Level &g, const BinBounds &bb, const uint8_t *vaff, const uint8_t *fa,
-                                uint32_t *wl, uint32_t *wl_count, cudaStream_t s) {
+                                uint32_t *wl, uint32_t *wl_count, Counters *ctr, cudaStream_t s) {
   if (!g.span) return;
   compact_active_scan_kernel<<<grid_for((g.span + 15) / 16, 256), 256, 0, s>>>(g.deg, g.ex, g.span, bb, vaff, fa, wl,
-                                                                                  wl_count);
+                                                                                  wl_count, &ctr->err);
   LVG_CHECK_LAUNCH();
 }
 

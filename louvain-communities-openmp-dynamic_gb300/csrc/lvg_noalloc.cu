@@ -106,7 +106,10 @@ __global__ void noalloc_final_kernel(const double *scratch, double M, double R, 
 extern "C" int lvg_modularity_noalloc(size_t span, const uint64_t *offsets, const uint32_t *keys,
                                       const float *weights, const uint8_t *exists, const uint32_t *membership,
                                       double M, double R, double *out, void *stream) {
-  if (!offsets || !membership || !out || span == 0)
+  // keys and weights are read for every vertex with edges: a null one would be
+  // a device fault, not an error code, so it is refused here (a caller with an
+  // edgeless graph passes any valid device pointer).
+  if (!offsets || !keys || !weights || !membership || !out || span == 0)
     return lvg::fail_noalloc(LVG_EINVAL, "lvg_modularity_noalloc: null argument or empty span");
   if (span > LVG_NOALLOC_MAX_SPAN)
     return lvg::fail_noalloc(LVG_EINVAL, "lvg_modularity_noalloc: span exceeds LVG_NOALLOC_MAX_SPAN (1048576)");

@@ -9,11 +9,17 @@
 // replaces. Requests for one graph run in arrival order, one at a time;
 // requests for different graphs run concurrently on the graphs' own streams
 // (one host worker thread per request in flight). With `coalesce` set, a
-// worker that picks a graph takes every request queued for it (up to
+// worker that picks a graph takes the requests queued for it (up to
 // `coalesce` batch entries) and serves them as one batch — their union, tidied
 // and applied at once — so that fixed per-request costs are paid once under
-// load; every one of them then completes with that run's result. Admission
-// control keeps
+// load; every one of them then completes with that run's result (the info's
+// `group` and `coalesced` fields say which requests ran together). The tidy
+// applies every deletion of a batch before every insertion and drops an
+// insertion of an edge already present, so a group closes at the first request
+// that touches an edge an earlier request of the group inserts or deletes
+// (insert-then-delete, delete-then-insert, or a second insertion of one edge):
+// the graph after a group is then the graph after its requests one by one.
+// Admission control keeps
 // the device bytes of the resident graphs under a budget: a graph is admitted
 // on its measured bytes after its first run (graph, workspace, state) plus
 // the per-request scratch, and only while the device has that much free.
@@ -29,6 +35,7 @@
 #include <mutex>
 #include <thread>
 #include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 #include "lvg_internal.cuh"
@@ -95,6 +102,27 @@ int pick(lvg_server *sv) {
   return -1;
 }
 
+// Directed edges a coalesced group inserts and deletes so far.
+struct GroupEdges {
+  std::unordered_set<uint64_t> ins, del;
+  static uint64_t key(uint32_t u, uint32_t v) { return uint64_t(u) << 32 | v; }
+  // Whether r touches an edge the group already inserts or deletes in a way
+  // the union's tidy would resolve differently from r applied after it.
+  bool conflicts(const Request &r) const {
+    for (size_t i = 0; i < r.ds.size(); ++i)
+      if (ins.count(key(r.ds[i], r.dd[i]))) return true;
+    for (size_t i = 0; i < r.is.size(); ++i) {
+      const uint64_t k = key(r.is[i], r.id[i]);
+      if (ins.count(k) || del.count(k)) return true;
+    }
+    return false;
+  }
+  void add(const Request &r) {
+    for (size_t i = 0; i < r.ds.size(); ++i) del.insert(key(r.ds[i], r.dd[i]));
+    for (size_t i = 0; i < r.is.size(); ++i) ins.insert(key(r.is[i], r.id[i]));
+  }
+};
+
 // The union of several requests' batches (deletions, then insertions, in
 // arrival order).
 Request merge(std::vector<Request> &rs) {
@@ -148,12 +176,19 @@ void worker(lvg_server *sv) {
     Slot &s = *sv->slots[size_t(i)];
     std::vector<Request> rs;
     size_t entries = 0;
-    do {  // one request, or (coalescing) every queued one up to the entry cap
-      entries += s.q.front().ds.size() + s.q.front().is.size();
+    GroupEdges seen;
+    // one request, or (coalescing) the queued ones up to the entry cap and the
+    // first conflicting request
+    for (;;) {
+      const Request &r = s.q.front();
+      const size_t n = r.ds.size() + r.is.size();
+      if (!rs.empty() && (entries + n > sv->opt.coalesce || seen.conflicts(r))) break;
+      if (sv->opt.coalesce) seen.add(r);
+      entries += n;
       rs.push_back(std::move(s.q.front()));
       s.q.pop_front();
-    } while (sv->opt.coalesce && !s.q.empty() &&
-             entries + s.q.front().ds.size() + s.q.front().is.size() <= sv->opt.coalesce);
+      if (!sv->opt.coalesce || s.q.empty()) break;
+    }
     s.busy = true;
     lk.unlock();
     std::vector<uint64_t> tickets;
@@ -170,6 +205,8 @@ void worker(lvg_server *sv) {
     for (size_t k = 0; k < tickets.size(); ++k) {
       lvg_request_info ik = info;
       ik.ticket = tickets[k];
+      ik.group = tickets[0];
+      ik.coalesced = int(tickets.size());
       ik.latency_ms = t - submitted[k];
       ik.queue_ms = info.queue_ms + (submitted[0] - submitted[k]);
       --sv->pending;
@@ -268,6 +305,13 @@ int lvg_server_add_graph(lvg_server *sv, lvg_graph *g, int take_ownership, const
   s->bytes = bytes;
   sv->slots.push_back(std::move(s));
   *graph_id = int(sv->slots.size() - 1);
+  return LVG_OK;
+}
+
+int lvg_server_set_coalesce(lvg_server *sv, size_t coalesce) {
+  if (!sv) return lvg::fail_noalloc(LVG_EINVAL, "null argument");
+  std::lock_guard<std::mutex> lk(sv->mu);
+  sv->opt.coalesce = coalesce;
   return LVG_OK;
 }
 

@@ -88,7 +88,8 @@ class _RequestInfo(C.Structure):
     _fields_ = [("ticket", C.c_uint64), ("graph", C.c_int), ("status", C.c_int), ("queue_ms", C.c_double),
                 ("apply_ms", C.c_double), ("run_ms", C.c_double), ("latency_ms", C.c_double),
                 ("iterations", C.c_int), ("passes", C.c_int), ("affected", C.c_uint64),
-                ("tidy_deletions", C.c_size_t), ("tidy_insertions", C.c_size_t)]
+                ("tidy_deletions", C.c_size_t), ("tidy_insertions", C.c_size_t), ("group", C.c_uint64),
+                ("coalesced", C.c_int)]
 
 
 class _ServerStats(C.Structure):
@@ -222,6 +223,7 @@ def load_library() -> C.CDLL:
     L.lvg_server_add_graph.argtypes = [vp, vp, i32, vp, vp, vp, C.POINTER(i32)]
     L.lvg_server_submit.argtypes = [vp, i32, C.POINTER(_Batch), C.POINTER(C.c_uint64)]
     L.lvg_server_wait.argtypes = [vp, C.c_uint64, C.POINTER(_RequestInfo)]
+    L.lvg_server_set_coalesce.argtypes = [vp, sz]
     L.lvg_server_drain.argtypes = [vp]
     L.lvg_server_stats.argtypes = [vp, i32, C.POINTER(_ServerStats)]
     L.lvg_server_membership.argtypes = [vp, i32, vp, vp, vp]
@@ -1043,6 +1045,10 @@ class Server:
 
     def drain(self) -> None:
         _check(self._L.lvg_server_drain(self.h))
+
+    def set_coalesce(self, entries: int) -> None:
+        """Coalescing cap for the groups formed from now on (0: one request per run)."""
+        _check(self._L.lvg_server_set_coalesce(self.h, entries))
 
     def stats(self, reset: bool = False) -> dict:
         st = _ServerStats()

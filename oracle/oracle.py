@@ -25,7 +25,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "liblouvain_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libref_louvain.so")
-REF_DIR = os.environ.get("LVG_REFERENCE_DIR", "/root/reference")
+STAGED_INC = os.path.join(HERE, "_ref", "src", "inc")
 
 _u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
 _u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
@@ -36,13 +36,49 @@ _vp = C.c_void_p
 _sz = C.c_size_t
 
 
-def build(ref: bool | None = None) -> None:
-    """Compile the oracle (and, if the reference checkout is present, the harness)."""
+def build(ref: bool | None = None, ref_dir: str | None = None) -> None:
+    """Compile the oracle and, where possible, the harness over the reference's headers.
+
+    ref_dir: the reference checkout (default: $LVG_REFERENCE_DIR). With a
+    checkout the harness is compiled from the headers where they lie, and the
+    headers are also staged, unmodified, into the git-ignored _ref/src/ so that
+    a machine without the checkout can build the harness itself. Without one,
+    previously staged headers are used. ref=None builds the harness whenever
+    either source exists; ref=True requires one; ref=False skips it.
+    """
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    if ref is None:
-        ref = os.path.isdir(os.path.join(REF_DIR, "inc"))
-    if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_DIR={REF_DIR}"], check=True)
+    ref_dir = ref_dir or os.environ.get("LVG_REFERENCE_DIR")
+    have_checkout = bool(ref_dir) and os.path.isdir(os.path.join(ref_dir, "inc"))
+    have_staged = os.path.isfile(os.path.join(STAGED_INC, "main.hxx"))
+    if ref is False:
+        return
+    if have_checkout:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_DIR={ref_dir}"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "stage", f"REF_DIR={ref_dir}"], check=True)
+    elif have_staged:
+        if _stale(REF_SO, [os.path.join(HERE, "ref_harness.cxx")]
+                  + [os.path.join(STAGED_INC, f) for f in os.listdir(STAGED_INC)]):
+            subprocess.run(["make", "-s", "-C", HERE, "ref-staged"], check=True)
+    elif ref:
+        raise FileNotFoundError("no reference checkout (LVG_REFERENCE_DIR) and no staged headers in " + STAGED_INC)
+
+
+def _stale(target: str, deps: list[str]) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def reference_available() -> bool:
+    """Whether the harness over the reference's own headers is built and loads here."""
+    if not os.path.exists(REF_SO):
+        return False
+    try:
+        C.CDLL(REF_SO)
+        return True
+    except OSError:
+        return False
 
 
 class Options(C.Structure):
@@ -309,10 +345,11 @@ class _RefGraph:
         CN = self.ref.L.ref_aggregate(self.h, vc, yoff, ydeg, yk, yw)
         return vc, CN, _rows(CN, yoff, ydeg, yk, yw)
 
-    def apply_batch(self, b):
+    def apply_batch(self, b, csr: bool = True):
         """tidyBatchUpdateU + applyBatchUpdateOmpU on this graph, in place, as
         main.cxx runs them. Returns the graph as (offsets, keys, weights,
-        exists) and the tidied batch as (ds, dd, dw, is, id, iw)."""
+        exists) (None with csr=False) and the tidied batch as
+        (ds, dd, dw, is, id, iw)."""
         a = _batch_args(b)
         nd, ni = max(a[0], 1), max(a[4], 1)
         t = [np.zeros(nd, np.uint32), np.zeros(nd, np.uint32), np.zeros(nd, np.float32),
@@ -320,7 +357,10 @@ class _RefGraph:
         tnd, tni = C.c_size_t(), C.c_size_t()
         self.ref.L.ref_apply_batch(self.h, *a, t[0], t[1], t[2], C.byref(tnd), t[3], t[4], t[5], C.byref(tni))
         tidy = tuple(x[:tnd.value].copy() for x in t[:3]) + tuple(x[:tni.value].copy() for x in t[3:])
-        return self.csr(), tidy
+        return (self.csr() if csr else None), tidy
+
+    def size(self) -> int:
+        return int(self.ref.L.ref_graph_size(self.h))
 
     def csr(self):
         S = self.g.span
@@ -336,6 +376,8 @@ class _RefGraph:
         return self.ref.L.ref_modularity(self.h, np.ascontiguousarray(membership, np.uint32), M, R)
 
     def louvain(self, method=0, batch=None, q=None, qvtot=None, qctot=None, opts=None):
+        """One call of the reference's entry point (opts.repeat repetitions
+        inside it; info["time"] is their mean, the reference's own timer)."""
         S = self.g.span
         o = opts or options()
         q = np.zeros(S, np.uint32) if q is None else np.ascontiguousarray(q, np.uint32)

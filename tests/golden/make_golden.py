@@ -1,9 +1,9 @@
 """Generate the golden fixtures of tests/golden/ from the reference's own code.
 
-Run in a checkout where the reference is available (it compiles
+Run where the reference checkout is available (it compiles
 oracle/ref_harness.cxx against the reference's unmodified headers):
 
-    python tests/golden/make_golden.py
+    LVG_REFERENCE_DIR=<reference checkout> python tests/golden/make_golden.py
 
 Every expected value below comes from a call into the reference harness
 (oracle/_ref/libref_louvain.so): weighted degrees, the batch weight update,
@@ -173,6 +173,8 @@ def flat_rows(rows):
 
 def main() -> None:
     lvg_build.build_graphgen()
+    # the reference checkout: $LVG_REFERENCE_DIR (the fixtures are generated
+    # where the checkout is; the committed .npz files are what the tests read)
     O.build(ref=True)
     ref = O.Reference()
     apply_fixtures(ref)

@@ -6,10 +6,17 @@ edges inside a community; one update batch of 1e-4 |E| (80 % insertions,
 Deterministic mode: static and dynamic-frontier Louvain on the GPU equal the
 CPU replay of the same rule bit for bit. Asynchronous mode (the reference's
 semantics): the GPU's modularity is within 0.005 of the mean of 5 runs of the
-oracle's OpenMP port, for static and for all three dynamic methods.
+oracle's OpenMP port, for static and for all three dynamic methods; and, on
+the graph and batch of tests/golden/pp131k_quality.npz, within 0.005 of the
+mean of 5 runs of the reference's own code (the fixture), the dynamic methods
+starting from the reference's own static result.
 """
+import os
+
 import numpy as np
 import pytest
+
+from conftest import GOLDEN
 
 pytestmark = pytest.mark.gpu
 
@@ -49,3 +56,23 @@ def test_async_modularity_within_tolerance_of_reference_mean(cuda, orc, case):
         ref = [orc.modularity(y, orc.louvain(y, method, b, *prior, threads=8)[0]) for _ in range(5)]
         q = orc.modularity(y, fn(Y, b, *prior).membership)
         assert abs(q - np.mean(ref)) <= tol, (method, q, ref)
+
+
+def test_async_modularity_within_tolerance_of_reference_fixture(cuda):
+    """Against the reference itself: its 5-run modularities on this graph and
+    batch (seeded as in tests/golden/make_golden.py), the dynamic methods from
+    its own static result, stored in the fixture."""
+    d = np.load(os.path.join(GOLDEN, "pp131k_quality.npz"))
+    x = cuda.planted_partition(131072, 128, 16, 0.8, 42)
+    b = cuda.random_batch(x, x.num_edges // 2 // 10000, 0.8, seed=7)
+    assert b.num_deletions + b.num_insertions == int(d["num_updates"])
+    y = cuda.apply_batch(x, b)
+    tol = 0.005
+    X, Y = cuda.Graph(x), cuda.Graph(y)
+    q = X.modularity(cuda.louvain_static(X).membership)
+    assert abs(q - d["static_q"].mean()) <= tol, (q, d["static_q"])
+    prior = (d["prior_m"], d["prior_vt"], d["prior_ct"])
+    for tag, fn in (("nd", cuda.louvain_naive_dynamic), ("ds", cuda.louvain_dynamic_delta_screening),
+                    ("df", cuda.louvain_dynamic_frontier)):
+        q = Y.modularity(fn(Y, b, *prior).membership)
+        assert abs(q - d[f"{tag}_q"].mean()) <= tol, (tag, q, d[f"{tag}_q"])

@@ -44,6 +44,7 @@ def s24(cuda):
     Y.apply_batch(db)
     st = cuda.State(Y)
     st.set(prior.membership, prior.vertexWeight, ct0)
+    prior.ct0 = ct0  # the prior's community weights indexed by its final ids
     yield Y, db, st, prior
     st.close()
     db.close()
@@ -87,3 +88,26 @@ def test_deterministic_frontier_quality_at_full_size(cuda, s24):
     _, m_async, _, _ = _run(cuda, Y, db, st, cuda.METHOD_FRONTIER, cuda.LouvainOptions())
     assert np.array_equal(vt, Y.vertex_weights())
     assert abs(Y.modularity(m_det) - Y.modularity(m_async)) <= 0.005
+
+
+def test_quality_against_the_port_at_full_size(cuda, orc, s24):
+    """The tolerance gate at full size: on the updated graph, the GPU's
+    asynchronous static Louvain and its naive-dynamic, delta-screening and
+    dynamic-frontier runs from the (deterministic GPU) static prior are each
+    within 0.005 of the mean of 5 runs of the oracle's OpenMP port (all host
+    threads) on the same graph, from the same prior and the same tidied batch."""
+    Y, db, st, prior = s24
+    y, tb = Y.download(), db.download()
+    q_prior = (prior.membership, prior.vertexWeight, prior.ct0)
+    tol = 0.005
+    report = {}
+    q_gpu = Y.modularity(cuda.louvain_static(Y).membership)
+    q_ref = [Y.modularity(orc.louvain(y, 0, threads=0)[0]) for _ in range(5)]
+    report["static"] = (q_gpu, float(np.mean(q_ref)))
+    for method, meth in (("nd", cuda.METHOD_NAIVE), ("ds", cuda.METHOD_DELTA), ("df", cuda.METHOD_FRONTIER)):
+        _, m, _, _ = _run(cuda, Y, db, st, meth, cuda.LouvainOptions())
+        ref = [Y.modularity(orc.louvain(y, meth, tb, *q_prior, threads=0)[0]) for _ in range(5)]
+        report[method] = (Y.modularity(m), float(np.mean(ref)))
+    print("R-MAT s24 modularity (gpu, port mean of 5):", report)
+    for k, (g, r) in report.items():
+        assert abs(g - r) <= tol, (k, report)

@@ -24,3 +24,32 @@ def test_shim_program_runs(cuda, tmp_path):
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "bad 0" in r.stdout
+
+
+def _reference_headers():
+    """The reference's headers: its checkout, else the copy the oracle recipe
+    staged (oracle/_ref/src, git-ignored; present where the checkout was when
+    the tree was built)."""
+    d = os.environ.get("LVG_REFERENCE_DIR")
+    if d and os.path.isfile(os.path.join(d, "inc", "main.hxx")):
+        return d
+    d = os.path.join(ROOT, "oracle", "_ref", "src")
+    return d if os.path.isfile(os.path.join(d, "inc", "main.hxx")) else None
+
+
+@pytest.mark.gpu
+def test_shim_with_reference_digraph(cuda, tmp_path):
+    """The shim's entry points take the reference's own DiGraph, batch
+    generators and tidy/apply, and land within 0.005 of the reference's own
+    templates' modularity on the same inputs (tests/cpp/shim_refgraph_test.cpp)."""
+    inc = _reference_headers()
+    if inc is None:
+        pytest.skip("reference headers not available")
+    exe = tmp_path / "shim_refgraph_test"
+    libdir = os.path.join(PKG, "lib")
+    subprocess.run(["g++", "-std=c++17", "-O3", "-fopenmp", "-DTYPE=float", "-I", inc, "-I",
+                    os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "cpp", "shim_refgraph_test.cpp"),
+                    "-L", libdir, "-llouvain_gb300", f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "bad 0" in r.stdout

@@ -5,10 +5,12 @@ tests/golden/make_golden.py). Integer and index results must match bit for
 bit; the 1-thread runs of the reference are deterministic (sequential sweep),
 so the oracle's 1-thread runs must reproduce them exactly.
 """
+import os
+
 import numpy as np
 import pytest
 
-from conftest import rows_sorted
+from conftest import GOLDEN, rows_sorted
 
 
 def test_edge_weight_and_vertex_weights(golden, orc):
@@ -97,3 +99,20 @@ def test_deterministic_replay_quality(golden, orc):
 def test_rows_sorted_helper():
     r, k, w = rows_sorted(2, np.array([0, 2, 3]), np.array([5, 1, 4]), np.array([1.0, 2.0, 3.0]))
     assert r.tolist() == [0, 0, 1] and k.tolist() == [1, 5, 4] and w.tolist() == [2.0, 1.0, 3.0]
+
+
+def test_port_quality_matches_reference_at_config1_size(lvg, orc):
+    """The port's asynchronous modularity (mean of 5 runs, 8 threads) is
+    within 0.005 of the reference's own 5-run mean on the 131072-vertex
+    planted partition, static and the three dynamic methods from the
+    reference's static result (tests/golden/pp131k_quality.npz)."""
+    d = np.load(os.path.join(GOLDEN, "pp131k_quality.npz"))
+    x = lvg.planted_partition(131072, 128, 16, 0.8, 42)
+    b = lvg.random_batch(x, x.num_edges // 2 // 10000, 0.8, seed=7)
+    y = lvg.apply_batch(x, b)
+    qs = [orc.modularity(x, orc.louvain(x, 0, threads=8)[0]) for _ in range(5)]
+    assert abs(np.mean(qs) - d["static_q"].mean()) <= 0.005, (qs, d["static_q"])
+    prior = (d["prior_m"], d["prior_vt"], d["prior_ct"])
+    for meth, tag in ((1, "nd"), (2, "ds"), (3, "df")):
+        qs = [orc.modularity(y, orc.louvain(y, meth, b, *prior, threads=8)[0]) for _ in range(5)]
+        assert abs(np.mean(qs) - d[f"{tag}_q"].mean()) <= 0.005, (tag, qs, d[f"{tag}_q"])

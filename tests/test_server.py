@@ -93,27 +93,102 @@ def test_server_admission_control(cuda):
     sv.close()
 
 
+def _edges(b):
+    """Directed (src, dst) keys a batch deletes and inserts."""
+    return (set(zip(b.del_src.tolist(), b.del_dst.tolist())), set(zip(b.ins_src.tolist(), b.ins_dst.tolist())))
+
+
+def _conflict(earlier, b):
+    """b touches an edge the earlier requests insert, or inserts one they delete."""
+    dels, ins = set(), set()
+    for e in earlier:
+        d, i = _edges(e)
+        dels |= d
+        ins |= i
+    d, i = _edges(b)
+    return bool(d & ins) or bool(i & (ins | dels))
+
+
+def _pair(lvg, u, v, w):
+    return lvg.HostBatch(np.zeros(0, np.uint32), np.zeros(0, np.uint32), np.zeros(0, np.float32),
+                         np.array([u, v], np.uint32), np.array([v, u], np.uint32), np.array([w, w], np.float32))
+
+
+def _unpair(lvg, u, v, w):
+    return lvg.HostBatch(np.array([u, v], np.uint32), np.array([v, u], np.uint32), np.array([w, w], np.float32),
+                         np.zeros(0, np.uint32), np.zeros(0, np.uint32), np.zeros(0, np.float32))
+
+
+def _union(lvg, bs):
+    """The batch a coalesced group runs: deletions, then insertions, in arrival order."""
+    cat = lambda f: np.concatenate([getattr(b, f) for b in bs])
+    return lvg.HostBatch(cat("del_src"), cat("del_dst"), cat("del_w"), cat("ins_src"), cat("ins_dst"), cat("ins_w"))
+
+
 @pytest.mark.gpu
 def test_server_coalescing_serves_the_union(cuda, orc):
-    """With coalescing, queued requests of one graph run as one batch: every
-    ticket completes, and the graph ends as after the batches one by one."""
-    x = cuda.planted_partition(4000, 100, 12, 0.8, 9)
-    seq = [cuda.reference_batch(x, 0, 300, seed=50 + k) for k in range(12)]  # insertion-only
+    """With coalescing, queued requests of one graph run as one batch, and a
+    group ends before a request that conflicts with it: an edge inserted and
+    then deleted, deleted and then inserted, or inserted twice with different
+    weights. So the graph after all requests equals the graph after each
+    request one by one (the reference's tidy + apply, weights included), and
+    the memberships equal those of each group's union applied alone in the
+    same order (deterministic mode, bit for bit)."""
+    o = cuda.LouvainOptions(deterministic=True)
+    x = cuda.planted_partition(6000, 100, 12, 0.8, 9)
+    adj = [set(x.keys[x.offsets[u]:x.offsets[u + 1]].tolist()) for u in range(x.span)]
+    rng = np.random.default_rng(3)
+    free = []
+    while len(free) < 2:
+        u, v = (int(t) for t in rng.integers(1, x.span, 2))
+        if u != v and v not in adj[u] and (u, v) not in free:
+            free.append((u, v))
+    (a, b), (c, d) = free
+    # a long first request, so the rest queue up behind it and coalesce
+    seq = [cuda.reference_batch(x, 2000, 8000, seed=40)]
+    seq += [_pair(cuda, a, b, 1.0), _unpair(cuda, a, b, 1.0),   # insert, then delete
+            _pair(cuda, c, d, 1.0), _pair(cuda, c, d, 2.0),     # insert twice, different weights
+            _unpair(cuda, c, d, 1.0), _pair(cuda, c, d, 3.0)]   # delete, then insert again
     cur = x
-    for b in seq:
-        cur = cuda.HostGraph(*orc.apply_batch(cur, b)[0])
+    for b_ in seq:
+        cur = cuda.HostGraph(*orc.apply_batch(cur, b_)[0])
+    for k in range(6):
+        nb = cuda.reference_batch(cur, 30, 120, seed=60 + k)
+        seq.append(nb)
+        cur = cuda.HostGraph(*orc.apply_batch(cur, nb)[0])
     G = cuda.Graph(x)
-    sv = cuda.Server(workers=2, coalesce=1 << 20)
+    sv = cuda.Server(workers=1, coalesce=1 << 20, o=o)
     gid = sv.add_graph(G)
-    tickets = [sv.submit(gid, b) for b in seq]
+    tickets = [sv.submit(gid, b_) for b_ in seq]
     infos = [sv.wait(t) for t in tickets]
     assert all(i["status"] == 0 for i in infos)
-    st = sv.stats()
-    assert st["completed"] == len(seq)
-    sv.drain()
+    assert sv.stats()["completed"] == len(seq)
+    groups = {}
+    for k, i in enumerate(infos):
+        groups.setdefault(i["group"], []).append(k)
+    order = sorted(groups)
+    assert any(len(groups[g]) > 1 for g in order), "no request was coalesced"
+    for g in order:
+        ks = groups[g]
+        assert ks == list(range(ks[0], ks[0] + len(ks)))          # consecutive requests
+        assert all(infos[k]["coalesced"] == len(ks) for k in ks)
+        for j in range(1, len(ks)):
+            assert not _conflict([seq[k] for k in ks[:j]], seq[ks[j]])
+    m, vt, ct = sv.state(gid)
     h = G.download()
     assert np.array_equal(h.offsets, cur.offsets) and np.array_equal(h.keys, cur.keys)
+    assert np.array_equal(h.weights, cur.weights)
     sv.close()
+    # each group's union, alone and in order, from the same static start
+    R = cuda.Graph(x)
+    st = cuda.State(R)
+    cuda.run_resident(R, cuda.METHOD_STATIC, None, None, st, o)
+    for g in order:
+        db = cuda.DeviceBatch(R, _union(cuda, [seq[k] for k in groups[g]]))
+        R.apply_batch(db)
+        cuda.run_resident(R, cuda.METHOD_FRONTIER, db, st, st, o)
+    rm, rvt, rct = st.get()
+    assert np.array_equal(m, rm) and np.array_equal(vt, rvt) and np.array_equal(ct, rct)
 
 
 @pytest.mark.gpu

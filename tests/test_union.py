@@ -74,13 +74,15 @@ def test_union_with_hubs(cuda, lvg):
 
 
 def test_async_union_quality(cuda, orc):
-    gs = _mix(cuda)[:4]
+    """Asynchronous mode: each graph's modularity in the union is within 0.005
+    of the mean of 5 runs of the oracle's OpenMP port on that graph alone."""
+    gs = _mix(cuda)[:4] + [_mix(cuda)[6]]
     U = cuda.Graph.union([cuda.Graph(g) for g in gs])
     rs = cuda.louvain_static_union(U)
     for i, g in enumerate(gs):
         q_union = orc.modularity(g, rs[i].membership)
-        q_alone = orc.modularity(g, _alone(cuda, g, None).membership)
-        assert abs(q_union - q_alone) <= 0.02, (i, q_union, q_alone)
+        ref = [orc.modularity(g, orc.louvain(g, 0, threads=8)[0]) for _ in range(5)]
+        assert abs(q_union - np.mean(ref)) <= 0.005, (i, q_union, ref)
 
 
 def test_union_is_static_only(cuda):

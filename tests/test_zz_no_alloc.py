@@ -54,3 +54,38 @@ def test_noalloc_rejects_spans_above_its_limit(cuda):
     with pytest.raises(cuda.LvgError) as e:
         cuda.modularity_noalloc(cuda.NOALLOC_MAX_SPAN + 1, 1, 1, 1, None, 1, 1)
     assert e.value.code == cuda.LVG_EINVAL
+
+
+def test_noalloc_out_of_range_id_gives_nan(cuda):
+    """A membership id >= span is not a valid community: the result is NaN,
+    not a read past the caller's buffers. A call after it is correct again
+    (the shared scratch is cleared by every call)."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("torch without CUDA")
+    g = Golden("pp2k", cuda)
+    S = g.x.span
+    off = _dev(torch, g.x.offsets.astype(np.uint64), np.int64)
+    key = _dev(torch, g.x.keys.astype(np.uint32), np.int32)
+    w = _dev(torch, g.x.weights.astype(np.float32), np.float32)
+    out = torch.full((1,), -7.0, dtype=torch.float64, device="cuda:0")
+    memb = g["static_m"].astype(np.uint32).copy()
+    bad = memb.copy()
+    bad[int(np.flatnonzero(g.x.exists)[0])] = S  # one id past the span
+    m = _dev(torch, bad, np.int32)
+    torch.cuda.synchronize()
+    cuda.modularity_noalloc(S, off.data_ptr(), key.data_ptr(), w.data_ptr(), None, m.data_ptr(), out.data_ptr())
+    torch.cuda.synchronize()
+    assert np.isnan(out.item())
+    m = _dev(torch, memb, np.int32)
+    cuda.modularity_noalloc(S, off.data_ptr(), key.data_ptr(), w.data_ptr(), None, m.data_ptr(), out.data_ptr())
+    torch.cuda.synchronize()
+    assert abs(out.item() - cuda.Graph(g.x).modularity(memb)) <= TOL
+
+
+def test_noalloc_rejects_null_edge_arrays(cuda):
+    # checked on the host before anything is launched
+    for keys, weights in ((0, 1), (1, 0)):
+        with pytest.raises(cuda.LvgError) as e:
+            cuda.modularity_noalloc(16, 1, keys, weights, None, 1, 1)
+        assert e.value.code == cuda.LVG_EINVAL
