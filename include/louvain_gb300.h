@@ -56,11 +56,13 @@ typedef struct lvg_options {
    * decision reads the previous iteration's state, ties go to the lowest
    * community id), reproducible bit for bit. */
   int    deterministic;
-  /* Extension: colour classes per local-moving sweep (1..32; 0 = default,
-   * 8 asynchronous / 16 deterministic). Vertices are split into classes by a
-   * hash of their id and each iteration visits the classes in turn, so most
-   * neighbours see each other's moves within the iteration, as in the
-   * reference's sequential sweep. */
+  /* Extension: colour classes per local-moving sweep (1..64; 0 = default:
+   * 16 deterministic; asynchronous static Louvain 64 in its first iteration,
+   * where every vertex is a singleton, then 16; the other asynchronous
+   * methods 8, or the graph's tuned frontier_colors for DF and DS). Vertices
+   * are split into classes by a hash of their id and each iteration visits
+   * the classes in turn, so most neighbours see each other's moves within
+   * the iteration, as in the reference's sequential sweep. */
   int    colors;
 } lvg_options;
 

@@ -8,8 +8,10 @@
 // edges, self-loops included (louvainScanCommunitiesW<true>), into a hash
 // table sized by the community's total degree, then writes the distinct
 // (community, summed weight) pairs to its row at yoff[c] and the row's degree
-// to ydeg[c] (the reference's gapped DiGraphCsr). The row sum is the
-// super-vertex's weight (louvainVertexWeightsOmpW on the new level, :1209).
+// to ydeg[c] (the reference's gapped DiGraphCsr). The super-vertex's weight
+// (louvainVertexWeightsOmpW on the new level, :1209: the row sum, self-loop
+// included) equals the community's total and is taken from the FP64 totals
+// by the driver (launch_next_vertex_weights), not re-summed here.
 //
 // Communities are binned by total degree like vertices in the move kernels:
 // sub-warp tiles / warps with shared tables for small communities, blocks
@@ -161,7 +163,6 @@ __global__ void __launch_bounds__(TILE_BLOCK) agg_tile_kernel(AggArgs a) {
     __syncwarp(m);
     const uint64_t y0 = a.yoff[c];
     uint32_t cnt = 0;
-    float vsum = 0.f;
 #pragma unroll
     for (int s0 = 0; s0 < C; s0 += T) {
       const int s = s0 + tl;
@@ -173,13 +174,10 @@ __global__ void __launch_bounds__(TILE_BLOCK) agg_tile_kernel(AggArgs a) {
         const float v = vals[s];
         a.ykey[y0 + cnt + r] = k;
         a.yw[y0 + cnt + r] = v;
-        vsum += v;
       }
       cnt += __popc(bal);
     }
-#pragma unroll
-    for (int sh = T / 2; sh > 0; sh >>= 1) vsum += __shfl_xor_sync(m, vsum, sh, T);
-    if (tl == 0) { a.ydeg[c] = cnt; a.vtot[c] = vsum; }
+    if (tl == 0) a.ydeg[c] = cnt;
     __syncwarp(m);
   }
   if (tl != 0) nread = 0;
@@ -219,7 +217,6 @@ template <int B, int LOGS>
 __global__ void __launch_bounds__(B) agg_block_kernel(AggArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
   __shared__ uint32_t s_cnt;
-  __shared__ float s_sum[B / 32];
   __shared__ unsigned s_used;
   __shared__ int s_over;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -278,7 +275,6 @@ __global__ void __launch_bounds__(B) agg_block_kernel(AggArgs a) {
     for (int o = 16; o > 0; o >>= 1) self_w += __shfl_xor_sync(0xffffffffu, self_w, o);
     if (lane == 0 && self_w != 0.f && ccap) ok &= table_add(keys, vals, lg, c, self_w);
     __syncthreads();
-    float vsum = 0.f;
     for (uint32_t s0 = 0; s0 < ccap; s0 += B) {
       const uint32_t s = s0 + threadIdx.x;
       const uint32_t k = s < ccap ? keys[s] : EMPTY;
@@ -292,19 +288,10 @@ __global__ void __launch_bounds__(B) agg_block_kernel(AggArgs a) {
         const float v = vals[s];
         a.ykey[y0 + base + r] = k;
         a.yw[y0 + base + r] = v;
-        vsum += v;
       }
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) vsum += __shfl_xor_sync(0xffffffffu, vsum, o);
-    if (lane == 0) s_sum[wid] = vsum;
     __syncthreads();
-    if (threadIdx.x == 0) {
-      float t = 0.f;
-      for (int k = 0; k < B / 32; ++k) t += s_sum[k];
-      a.ydeg[c] = s_cnt;
-      a.vtot[c] = t;
-    }
+    if (threadIdx.x == 0) a.ydeg[c] = s_cnt;
     __syncthreads();
   }
   if (lane != 0) nread = 0;
@@ -442,7 +429,7 @@ __global__ void __launch_bounds__(B) agg_chunk_kernel(AggArgs a, AggChunks ch) {
 
 // The global tables of the chunked communities into their rows: a thread
 // per slot, output positions by a warp-aggregated cursor per community
-// (ydeg), the row sums into vtot.
+// (ydeg).
 __global__ void agg_gfinish_kernel(AggArgs a, AggChunks ch, uint64_t slots) {
   const int lane = threadIdx.x & 31;
   for (uint64_t base = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32 * 32; base < slots;
@@ -461,14 +448,9 @@ __global__ void agg_gfinish_kernel(AggArgs a, AggChunks ch, uint64_t slots) {
     }
     const unsigned grp = __match_any_sync(0xffffffffu, jj);
     const int leader = __ffs(grp) - 1;
-    float sum = 0.f;
-    for (unsigned r = grp; r; r &= r - 1u) sum += __shfl_sync(grp, v, __ffs(r) - 1);
     uint32_t at = 0;
     const uint32_t c = jj != EMPTY ? ch.comm[jj] : 0u;
-    if (jj != EMPTY && lane == leader) {
-      at = atomicAdd(&a.ydeg[c], uint32_t(__popc(grp)));
-      atomicAdd(&a.vtot[c], sum);
-    }
+    if (jj != EMPTY && lane == leader) at = atomicAdd(&a.ydeg[c], uint32_t(__popc(grp)));
     at = __shfl_sync(grp, at, leader);
     if (jj != EMPTY) {
       const uint64_t y = a.yoff[c] + at + __popc(grp & ((1u << lane) - 1u));

@@ -65,7 +65,7 @@ namespace {
 
 void check_tuning(const lvg_tuning &t) {
   if (t.frontier_colors < 1 || t.frontier_colors > MAX_COLORS)
-    throw Error(LVG_EINVAL, "tuning: frontier_colors out of 1..32");
+    throw Error(LVG_EINVAL, "tuning: frontier_colors out of 1.." + std::to_string(MAX_COLORS));
   if (t.hub_chunk < 256 || t.hub_chunk > (1u << 20)) throw Error(LVG_EINVAL, "tuning: hub_chunk out of 256..2^20");
   if (t.big_blocks_per_sm < 0 || t.big_blocks_per_sm > 64) throw Error(LVG_EINVAL, "tuning: big_blocks_per_sm");
   if (!(t.frontier_max_fraction >= 0 && t.frontier_max_fraction <= 1))
@@ -441,11 +441,6 @@ int lvg_static_union(lvg_graph *u, const lvg_options *o, lvg_result *results) {
     UnionInfo &U = *u->uni;
     Workspace &W = *u->ws;
     cudaStream_t s = u->stream;
-    const size_t S = u->base.span;
-    W.stage_a.ensure(S);
-    W.stage_b.ensure(S);
-    launch_f32_to_f64(W.utot.p, W.stage_a.p, S, s);
-    launch_f32_to_f64(U.ct.p, W.stage_b.p, S, s);
     for (size_t i = 0; i < U.n; ++i) {
       lvg_result *r = &results[i];
       const size_t sp = U.vb[i + 1] - U.vb[i];
@@ -455,8 +450,8 @@ int lvg_static_union(lvg_graph *u, const lvg_options *o, lvg_result *results) {
       if (!r->membership || !r->vertexWeight || !r->communityWeight) throw std::bad_alloc();
     }
     copy_out_slices(s, U.q.p, 4, U.vb, [&](size_t i) -> void * { return results[i].membership; });
-    copy_out_slices(s, W.stage_a.p, 8, U.vb, [&](size_t i) -> void * { return results[i].vertexWeight; });
-    copy_out_slices(s, W.stage_b.p, 8, U.vb, [&](size_t i) -> void * { return results[i].communityWeight; });
+    copy_out_slices(s, W.utot.p, sizeof(tot_t), U.vb, [&](size_t i) -> void * { return results[i].vertexWeight; });
+    copy_out_slices(s, U.ct.p, sizeof(tot_t), U.vb, [&](size_t i) -> void * { return results[i].communityWeight; });
     for (size_t i = 0; i < U.n; ++i) {
       lvg_result *r = &results[i];
       const size_t sp = U.vb[i + 1] - U.vb[i];
@@ -760,8 +755,8 @@ int lvg_state_create(lvg_graph *g, lvg_state **out) {
     st->device = g->device;
     st->q.ensure(S); st->vt.ensure(S); st->ct.ensure(S);
     LVG_CUDA(cudaMemsetAsync(st->q.p, 0, S * 4, g->stream));
-    LVG_CUDA(cudaMemsetAsync(st->vt.p, 0, S * 4, g->stream));
-    LVG_CUDA(cudaMemsetAsync(st->ct.p, 0, S * 4, g->stream));
+    LVG_CUDA(cudaMemsetAsync(st->vt.p, 0, S * sizeof(tot_t), g->stream));
+    LVG_CUDA(cudaMemsetAsync(st->ct.p, 0, S * sizeof(tot_t), g->stream));
     LVG_CUDA(cudaStreamSynchronize(g->stream));
     return LVG_OK;
   });
@@ -786,21 +781,11 @@ int lvg_state_get(const lvg_state *st, uint32_t *membership, double *vtot, doubl
   return lvg::guarded([&] {
     lvg_graph *g = st->g;
     LVG_CUDA(cudaSetDevice(g->device));
-    lvg::ensure_ws(g);
-    lvg::Workspace &W = *g->ws;
     cudaStream_t s = g->stream;
     const size_t S = g->base.span;
-    W.stage_a.ensure(S);
-    W.stage_b.ensure(S);
     if (membership) LVG_CUDA(cudaMemcpyAsync(membership, st->q.p, S * 4, cudaMemcpyDeviceToHost, s));
-    if (vtot) {
-      lvg::launch_f32_to_f64(st->vt.p, W.stage_a.p, S, s);
-      LVG_CUDA(cudaMemcpyAsync(vtot, W.stage_a.p, S * 8, cudaMemcpyDeviceToHost, s));
-    }
-    if (ctot) {
-      lvg::launch_f32_to_f64(st->ct.p, W.stage_b.p, S, s);
-      LVG_CUDA(cudaMemcpyAsync(ctot, W.stage_b.p, S * 8, cudaMemcpyDeviceToHost, s));
-    }
+    if (vtot) LVG_CUDA(cudaMemcpyAsync(vtot, st->vt.p, S * sizeof(tot_t), cudaMemcpyDeviceToHost, s));
+    if (ctot) LVG_CUDA(cudaMemcpyAsync(ctot, st->ct.p, S * sizeof(tot_t), cudaMemcpyDeviceToHost, s));
     LVG_CUDA(cudaStreamSynchronize(s));
     return LVG_OK;
   });

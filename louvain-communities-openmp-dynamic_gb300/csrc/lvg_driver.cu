@@ -109,7 +109,8 @@ void build_hub_plan(lvg_graph *g, Level &lv, HubPlanBuffers &hb) {
 
 // Colour classes of a run: the options' count, else 16 (deterministic), else
 // the graph's tuned count for the frontier methods on batches of at most
-// frontier_max_fraction entries per edge, else 8.
+// frontier_max_fraction entries per edge, else 16 for static Louvain (after
+// its first iteration, see first_colors) and 8 for the others.
 int colors_for(const lvg_options &o, int method, const lvg_tuning &t, size_t batch_entries = 0,
                size_t edges = 0) {
   int k = o.colors;
@@ -117,9 +118,26 @@ int colors_for(const lvg_options &o, int method, const lvg_tuning &t, size_t bat
     const bool small = double(batch_entries) <= t.frontier_max_fraction * double(edges);
     if (o.deterministic) k = DEFAULT_COLORS_SYNC;
     else if ((method == LVG_METHOD_FRONTIER || method == LVG_METHOD_DELTA) && small) k = t.frontier_colors;
+    else if (method == LVG_METHOD_STATIC) k = STATIC_COLORS_ASYNC;
     else k = DEFAULT_COLORS_ASYNC;
   }
   return k < 1 ? 1 : (k > MAX_COLORS ? MAX_COLORS : k);
+}
+
+// Classes of the first iteration of the first pass (0: as the rest): static
+// Louvain in asynchronous mode with the default count starts from singletons,
+// where nearly every vertex moves at once and neighbours that decide
+// together join each other's old communities; a finer first sweep keeps the
+// reference's sequential quality.
+int first_colors(const lvg_options &o, int method) {
+  return method == LVG_METHOD_STATIC && !o.deterministic && o.colors <= 0 ? FIRST_COLORS_STATIC : 0;
+}
+
+// Degree bins and hub plan of the uploaded level for k colour classes.
+void set_base_colors(lvg_graph *g, int k) {
+  if (g->base.colors == k) return;
+  compute_bins(g, g->base, g->deg.p, g->bins.p, g->ws->binscratch.p, k);
+  build_hub_plan(g, g->base, g->hubplan);
 }
 
 void ensure_global_tables(Workspace &W, size_t blocks, int log2cap, bool first_too) {
@@ -147,7 +165,7 @@ void ensure_aux(lvg_graph *g) {
 // side streams, bins 9 and 10 on two more, the hubs on the main stream.
 int bin_stream(int b) { return b <= 4 ? 0 : b <= 8 ? 1 : b == 9 ? 2 : b == 10 ? 3 : -1; }
 
-void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const float *tot,
+void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const tot_t *tot,
                        const uint8_t *fa, float kr, bool sync, int fused, const int *glog2, const size_t *goff,
                        size_t need, std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> *bin_ev,
                        const UnionCall *uc) {
@@ -260,7 +278,7 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot
 // Capture one iteration of the uploaded level into a CUDA graph (after an
 // eager iteration, so every kernel's attributes are already set). A capture
 // failure disables graphs for this handle; the eager path stays correct.
-void capture_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const float *tot,
+void capture_iteration(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const tot_t *tot,
                        const uint8_t *fa, float kr, bool sync, int fused, const int *glog2, const size_t *goff,
                        size_t need, const IterKey &key, const UnionCall *uc) {
   cudaStream_t s = g->stream;
@@ -303,9 +321,15 @@ void capture_iteration(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot
 // colour classes in order (enqueue_iteration). For the uploaded level the
 // iteration is captured once into a CUDA graph and replayed, one graph
 // launch per iteration instead of ~12 launches per colour class.
-int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const float *tot, const uint8_t *fa,
+// The raw outcome of move_phase: iterations run and the last iteration's el.
+struct PhaseEnd {
+  int l = 0;
+  double el = 0;
+};
+
+int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const tot_t *tot, const uint8_t *fa,
                double M, float kr, int L, double E, bool sync, int fused, const UnionCall *uc = nullptr,
-               const DBatch *endpoints = nullptr) {
+               const DBatch *endpoints = nullptr, PhaseEnd *end = nullptr, bool capture = true) {
   Workspace &W = *g->ws;
   cudaStream_t s = g->stream;
   const int K = lv.colors;
@@ -358,7 +382,7 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const 
     key.kr = kr;
     key.E = uc ? E : 0.0;
   }
-  const bool graphs = base && !g->profiling && !g->no_graphs;
+  const bool graphs = base && capture && !g->profiling && !g->no_graphs;
   int l = 0;
   double el = 0;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> bin_ev;
@@ -392,6 +416,7 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, float *ctot, const 
     el = double(g->hctr.p->el_fix) / GAIN_FIX / M;
     if (el <= E) break;
   }
+  if (end) { end->l = l; end->el = el; }
   return (l > 1 || el != 0) ? l : 0;
 }
 
@@ -421,9 +446,8 @@ Level aggregate(lvg_graph *g, const Level &lv, const uint32_t *com, size_t CN, i
   exclusive_scan_u32(W.csize.p, W.csize.p, CN, W.csize.p + CN, W.scan32.p, s);
   exclusive_scan_u64(nl.off, nl.off, CN, nl.off + CN, W.scan64.p, s);
   launch_community_scatter(lv, com, W.csize.p, W.ccur.p, W.cmem.p, s);
-  // Empty communities never reach a kernel: zero their rows and weights first.
+  // Empty communities never reach a kernel: zero their rows first.
   LVG_CUDA(cudaMemsetAsync(nl.deg, 0, CN * sizeof(uint32_t), s));
-  LVG_CUDA(cudaMemsetAsync(W.vtot.p, 0, CN * sizeof(float), s));
   // Global fallback regions of bins 9-10 (bin 11 is chunked below).
   int glog2[NUM_BINS] = {};
   size_t need = 0;
@@ -448,7 +472,7 @@ Level aggregate(lvg_graph *g, const Level &lv, const uint32_t *com, size_t CN, i
     a.list = W.cbins.p + cb[b];
     a.count = uint32_t(cnt);
     a.yoff = nl.off; a.ydeg = nl.deg; a.ykey = nl.key; a.yw = nl.w;
-    a.vtot = W.vtot.p; a.ctr = g->ctr.p; a.cn = uint32_t(CN);
+    a.ctr = g->ctr.p; a.cn = uint32_t(CN);
     a.gkeys = need ? W.gkeys.p : nullptr; a.gvals = need ? W.gvals.p : nullptr; a.glog2 = glog2[b];
     launch_aggregate_bin(b, a, s);
     ++g->stats.aggregate_launches;
@@ -495,7 +519,7 @@ Level aggregate(lvg_graph *g, const Level &lv, const uint32_t *com, size_t CN, i
     a.list = list;
     a.count = uint32_t(n11);
     a.yoff = nl.off; a.ydeg = nl.deg; a.ykey = nl.key; a.yw = nl.w;
-    a.vtot = W.vtot.p; a.ctr = g->ctr.p; a.cn = uint32_t(CN);
+    a.ctr = g->ctr.p; a.cn = uint32_t(CN);
     a.gkeys = nullptr; a.gvals = nullptr; a.glog2 = 0;
     AggChunks ch{W.agg_chunk.p, list, W.agg_toff.p, W.agg_tlog.p, W.mpre.p, W.agg_gk.p, W.agg_gv.p, uint32_t(n11)};
     launch_aggregate_chunks(a, ch, chunks.size(), slots, s);
@@ -514,7 +538,7 @@ Level aggregate(lvg_graph *g, const Level &lv, const uint32_t *com, size_t CN, i
 // ---------------------------------------------------------------- driver
 
 
-// One call of a method. prior: device FP32 prior state (dynamic methods);
+// One call of a method. prior: device prior state (dynamic methods);
 // out: where the first level's membership/weights and final totals live.
 // on_init (optional) is called once, in the last repetition, with an event
 // recorded when the first level's vertex weights (out.vt) are final.
@@ -532,30 +556,35 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
   const bool sync = o.deterministic != 0;
   const int rep = std::max(1, o.repeat);
   const int K = colors_for(o, method, g->tuning, b.nd + b.ni, g->base.edges);
-  if (g->base.colors != K) {
-    compute_bins(g, g->base, g->deg.p, g->bins.p, W.binscratch.p, K);
-    build_hub_plan(g, g->base, g->hubplan);
-  }
+  const int K1 = first_colors(o, method);
   uint32_t *ucom = out.q;
-  float *utot = out.vt, *ctot = out.ct;
+  tot_t *utot = out.vt, *ctot = out.ct;
   g->stats = lvg_stats{};
   const unsigned long long launches0 = launch_counter();
   LVG_CUDA(cudaMemsetAsync(g->ctr.p, 0, sizeof(Counters), s));
   int l = 0, p = 0;
   for (int r = 0; r < rep; ++r) {
     g->events.reset();
+    set_base_colors(g, K1 ? K1 : K);
     // Reset buffers, as the reference does before each repetition.
     LVG_CUDA(cudaMemsetAsync(W.vaff.p, 0, S, s));
     LVG_CUDA(cudaMemsetAsync(W.vcom.p, 0, S * sizeof(uint32_t), s));
-    LVG_CUDA(cudaMemsetAsync(W.vtot.p, 0, S * sizeof(float), s));
+    LVG_CUDA(cudaMemsetAsync(W.vtot.p, 0, S * sizeof(tot_t), s));
+    // The prior state into place: the reference moves its copies of it
+    // (louvainSetupInitialsW, inc/louvain.hxx:1240) in without copying, so
+    // the copy stays outside the timed section as its copies do.
+    if (method != LVG_METHOD_STATIC) {
+      if (prior.q != ucom) LVG_CUDA(cudaMemcpyAsync(ucom, prior.q, S * 4, cudaMemcpyDeviceToDevice, s));
+      if (prior.vt != utot)
+        LVG_CUDA(cudaMemcpyAsync(utot, prior.vt, S * sizeof(tot_t), cudaMemcpyDeviceToDevice, s));
+      if (prior.ct != ctot)
+        LVG_CUDA(cudaMemcpyAsync(ctot, prior.ct, S * sizeof(tot_t), cudaMemcpyDeviceToDevice, s));
+    }
     cudaEvent_t e0 = g->events.record(s);
     // fi: initial membership and weights.
     if (method == LVG_METHOD_STATIC) {
       launch_init_static(g->base, ucom, utot, ctot, s);
     } else {
-      if (prior.q != ucom) LVG_CUDA(cudaMemcpyAsync(ucom, prior.q, S * 4, cudaMemcpyDeviceToDevice, s));
-      if (prior.vt != utot) LVG_CUDA(cudaMemcpyAsync(utot, prior.vt, S * 4, cudaMemcpyDeviceToDevice, s));
-      if (prior.ct != ctot) LVG_CUDA(cudaMemcpyAsync(ctot, prior.ct, S * 4, cudaMemcpyDeviceToDevice, s));
       launch_batch_weights(b.ds, b.dw, b.nd, -1.f, ucom, utot, ctot, s);
       launch_batch_weights(b.is, b.iw, b.ni, +1.f, ucom, utot, ctot, s);
     }
@@ -588,7 +617,7 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
     double E = o.tolerance;
     Level lv = g->base;
     uint32_t *com = ucom;
-    const float *tot = utot;
+    const tot_t *tot = utot;
     int which = 0;
     for (l = 0, p = 0; M > 0 && P > 0;) {
       if (p == 1) ep1 = g->events.record(s);
@@ -603,8 +632,25 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
                         : method == LVG_METHOD_FRONTIER  ? 2
                         : method == LVG_METHOD_DELTA     ? 8
                                                          : 0;
-      const int m = move_phase(g, lv, com, ctot, tot, first ? fa : nullptr, M, kr, L, E, sync, fused, nullptr,
-                               first && method == LVG_METHOD_FRONTIER ? &b : nullptr);
+      const DBatch *ends = first && method == LVG_METHOD_FRONTIER ? &b : nullptr;
+      int m;
+      if (first && K1 && K1 != K) {
+        // the first iteration over K1 classes (not captured: it runs once per
+        // call), the rest of the pass over K
+        PhaseEnd e1, e2;
+        move_phase(g, lv, com, ctot, tot, fa, M, kr, 1, E, sync, fused, nullptr, ends, &e1, false);
+        set_base_colors(g, K);
+        lv = g->base;
+        if (e1.el <= E || L <= 1) {
+          m = (e1.l > 1 || e1.el != 0) ? e1.l : 0;
+        } else {
+          move_phase(g, lv, com, ctot, tot, fa, M, kr, L - 1, E, sync, fused, nullptr, ends, &e2);
+          const int lt = 1 + e2.l;
+          m = (lt > 1 || e2.el != 0) ? lt : 0;
+        }
+      } else {
+        m = move_phase(g, lv, com, ctot, tot, first ? fa : nullptr, M, kr, L, E, sync, fused, nullptr, ends);
+      }
       tl_ev.push_back({a0, g->events.record(s)});
       l += std::max(m, 1);
       ++p;
@@ -616,6 +662,8 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
       read_counters(g);
       const size_t CN = g->hctr.p->cn;
       if (double(CN) / double(GN) >= o.aggregationTolerance) break;
+      // the next level's vertex weights: the communities' FP64 totals
+      launch_next_vertex_weights(W.cext.p, lv.span, &g->ctr.p->cn, ctot, W.vtot.p, s);
       launch_lookup(com, W.cext.p, S, s);
       if (!first) launch_lookup(ucom, W.vcom.p, S, s);
       cudaEvent_t g0 = g->events.record(s);
@@ -676,10 +724,7 @@ void run_union(lvg_graph *g, const lvg_options &o, RunInfo &info) {
   const bool sync = o.deterministic != 0;
   const int rep = std::max(1, o.repeat);
   const int K = colors_for(o, LVG_METHOD_STATIC, g->tuning);
-  if (g->base.colors != K) {
-    compute_bins(g, g->base, g->deg.p, g->bins.p, W.binscratch.p, K);
-    build_hub_plan(g, g->base, g->hubplan);
-  }
+  const int K1 = first_colors(o, LVG_METHOD_STATIC);
   {
     std::vector<float> kr(n);
     for (size_t i = 0; i < n; ++i) kr[i] = U.M[i] > 0 ? float(R / (2.0 * U.M[i])) : 0.f;
@@ -691,16 +736,17 @@ void run_union(lvg_graph *g, const lvg_options &o, RunInfo &info) {
   U.gid[0].ensure(S); U.gid[1].ensure(S); U.gbase[0].ensure(n + 1); U.gbase[1].ensure(n + 1);
   U.aggex.ensure(S); U.q.ensure(S); U.ct.ensure(S); U.aff.ensure(S);
   uint32_t *ucom = W.ucom.p;
-  float *utot = W.utot.p, *ctot = W.ctot.p;
+  tot_t *utot = W.utot.p, *ctot = W.ctot.p;
   g->stats = lvg_stats{};
   const unsigned long long launches0 = launch_counter();
   LVG_CUDA(cudaMemsetAsync(g->ctr.p, 0, sizeof(Counters), s));
   const UnionCall uc0{n, U.kr.p, U.fix.p, U.gact.p, U.ctl.p, U.Md.p, 0.0, L};
   for (int r = 0; r < rep; ++r) {
     g->events.reset();
+    set_base_colors(g, K1 ? K1 : K);
     LVG_CUDA(cudaMemsetAsync(W.vaff.p, 0, S, s));
     LVG_CUDA(cudaMemsetAsync(W.vcom.p, 0, S * sizeof(uint32_t), s));
-    LVG_CUDA(cudaMemsetAsync(W.vtot.p, 0, S * sizeof(float), s));
+    LVG_CUDA(cudaMemsetAsync(W.vtot.p, 0, S * sizeof(tot_t), s));
     LVG_CUDA(cudaMemsetAsync(U.ctl.p, 0, n * sizeof(GraphCtl), s));
     LVG_CUDA(cudaMemsetAsync(U.fix.p, 0, n * sizeof(unsigned long long), s));
     cudaEvent_t e0 = g->events.record(s);
@@ -718,7 +764,7 @@ void run_union(lvg_graph *g, const lvg_options &o, RunInfo &info) {
     double E = o.tolerance;
     Level lv = g->base;
     uint32_t *com = ucom;
-    const float *tot = utot;
+    const tot_t *tot = utot;
     int which = 0;
     for (int p = 0;; ++p) {
       if (p == 1) ep1 = g->events.record(s);
@@ -727,7 +773,16 @@ void run_union(lvg_graph *g, const lvg_options &o, RunInfo &info) {
       UnionCall uc = uc0;
       uc.E = E;
       cudaEvent_t a0 = g->events.record(s);
-      move_phase(g, lv, com, ctot, tot, nullptr, 0.0, 0.f, L, E, sync, 0, &uc);
+      if (first && K1 && K1 != K) {
+        // as run(): the first iteration over K1 classes, the rest over K (each
+        // graph's iteration count and stop test carry on on the device)
+        move_phase(g, lv, com, ctot, tot, nullptr, 0.0, 0.f, 1, E, sync, 0, &uc, nullptr, nullptr, false);
+        set_base_colors(g, K);
+        lv = g->base;
+        if (g->hctr.p->gactive && L > 1) move_phase(g, lv, com, ctot, tot, nullptr, 0.0, 0.f, L - 1, E, sync, 0, &uc);
+      } else {
+        move_phase(g, lv, com, ctot, tot, nullptr, 0.0, 0.f, L, E, sync, 0, &uc);
+      }
       tl_ev.push_back({a0, g->events.record(s)});
       launch_pass_end(n, U.ctl.p, P, s);
       launch_union_snapshot(lv.span, lv.gid, lv.gbase, U.vb0.p, U.ctl.p, ctot, W.vaff.p, U.ct.p, U.aff.p, s);
@@ -746,6 +801,7 @@ void run_union(lvg_graph *g, const lvg_options &o, RunInfo &info) {
       uint32_t *ngid = U.gid[which].p, *ngbase = U.gbase[which].p;
       launch_union_bases(n, lv.gbase, lv.span, W.cext.p, &g->ctr.p->cn, ngbase, s);
       launch_fill_gid(ngbase, n, ngid, s);
+      launch_next_vertex_weights(W.cext.p, lv.span, &g->ctr.p->cn, ctot, W.vtot.p, s);
       launch_lookup(com, W.cext.p, lv.span, s);
       if (!first) launch_union_lookup(ucom, W.vcom.p, S, U.gid0.p, U.ctl.p, s);
       Level am = lv;
@@ -859,29 +915,21 @@ void download_result(lvg_graph *g, lvg_result *out, StateRef st, bool skip_vw = 
   if (!out->vertexWeight) { out->vertexWeight = (double *)std::malloc(S * 8 + 1); out->owned |= 2; }
   if (!out->communityWeight) { out->communityWeight = (double *)std::malloc(S * 8 + 1); out->owned |= 4; }
   if (!out->membership || !out->vertexWeight || !out->communityWeight) throw std::bad_alloc();
-  W.stage_a.ensure(S);
-  W.stage_b.ensure(S);
-  if (!skip_vw) launch_f32_to_f64(st.vt, W.stage_a.p, S, s);
-  launch_f32_to_f64(st.ct, W.stage_b.p, S, s);
   LVG_CUDA(cudaMemcpyAsync(out->membership, st.q, S * 4, cudaMemcpyDeviceToHost, s));
-  if (!skip_vw) LVG_CUDA(cudaMemcpyAsync(out->vertexWeight, W.stage_a.p, S * 8, cudaMemcpyDeviceToHost, s));
-  LVG_CUDA(cudaMemcpyAsync(out->communityWeight, W.stage_b.p, S * 8, cudaMemcpyDeviceToHost, s));
+  if (!skip_vw) LVG_CUDA(cudaMemcpyAsync(out->vertexWeight, st.vt, S * sizeof(tot_t), cudaMemcpyDeviceToHost, s));
+  LVG_CUDA(cudaMemcpyAsync(out->communityWeight, st.ct, S * sizeof(tot_t), cudaMemcpyDeviceToHost, s));
   LVG_CUDA(cudaStreamSynchronize(s));
 }
 
 void upload_prior(lvg_graph *g, const uint32_t *q, const double *qvtot, const double *qctot, uint32_t *dq,
-                  float *dvt, float *dct) {
-  Workspace &W = *g->ws;
+                  tot_t *dvt, tot_t *dct) {
   cudaStream_t s = g->stream;
   const size_t S = g->base.span;
   if (!q || !qvtot || !qctot) throw Error(LVG_EINVAL, "prior state: null array");
-  W.stage_a.ensure(S);
-  W.stage_b.ensure(S);
+  // the device keeps the totals in FP64, as the caller passes them
   LVG_CUDA(cudaMemcpyAsync(dq, q, S * 4, cudaMemcpyHostToDevice, s));
-  LVG_CUDA(cudaMemcpyAsync(W.stage_a.p, qvtot, S * 8, cudaMemcpyHostToDevice, s));
-  LVG_CUDA(cudaMemcpyAsync(W.stage_b.p, qctot, S * 8, cudaMemcpyHostToDevice, s));
-  launch_prior_to_f32(W.stage_a.p, dvt, S, s);
-  launch_prior_to_f32(W.stage_b.p, dct, S, s);
+  LVG_CUDA(cudaMemcpyAsync(dvt, qvtot, S * sizeof(tot_t), cudaMemcpyHostToDevice, s));
+  LVG_CUDA(cudaMemcpyAsync(dct, qctot, S * sizeof(tot_t), cudaMemcpyHostToDevice, s));
   // every prior id must be < span (checked on the device; read back before any use)
   launch_check_ids(dq, S, uint32_t(S), g->ctr.p, s);
   read_counters(g);
@@ -904,15 +952,21 @@ int run_host(lvg_graph *g, int method, const lvg_batch *b, const uint32_t *q, co
     DBatch db;
     upload_batch(g, method == LVG_METHOD_STATIC ? nullptr : b, g->b_ds, g->b_dd, g->b_dw, g->b_is, g->b_id,
                  g->b_iw, g->b_seg, db);
+    StateRef st{W.ucom.p, W.utot.p, W.ctot.p};
     StateRef prior{nullptr, nullptr, nullptr};
     if (method != LVG_METHOD_STATIC) {
-      W.prior_q.ensure(W.S); W.prior_vt.ensure(W.S); W.prior_ct.ensure(W.S);
-      upload_prior(g, q, qvtot, qctot, W.prior_q.p, W.prior_vt.p, W.prior_ct.p);
-      prior = StateRef{W.prior_q.p, W.prior_vt.p, W.prior_ct.p};
+      if (opt.repeat <= 1) {
+        // one run: the prior goes straight where the run starts from
+        upload_prior(g, q, qvtot, qctot, st.q, st.vt, st.ct);
+        prior = st;
+      } else {  // every repetition starts from the same prior
+        W.prior_q.ensure(W.S); W.prior_vt.ensure(W.S); W.prior_ct.ensure(W.S);
+        upload_prior(g, q, qvtot, qctot, W.prior_q.p, W.prior_vt.p, W.prior_ct.p);
+        prior = StateRef{W.prior_q.p, W.prior_vt.p, W.prior_ct.p};
+      }
     }
     LVG_CUDA(cudaStreamSynchronize(g->stream));
     const auto t1 = std::chrono::steady_clock::now();
-    StateRef st{W.ucom.p, W.utot.p, W.ctot.p};
     RunInfo info;
     // The vertex weights are final once the run has initialised: into a
     // pinned result array they are copied out on a side stream while the
@@ -925,10 +979,9 @@ int run_host(lvg_graph *g, int method, const lvg_batch *b, const uint32_t *q, co
     std::function<void(cudaEvent_t)> hook = [&](cudaEvent_t ready) {
       if (!g->copy_stream) LVG_CUDA(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
       const size_t S = g->base.span;
-      W.stage_a.ensure(S);
       LVG_CUDA(cudaStreamWaitEvent(g->copy_stream, ready, 0));
-      launch_f32_to_f64(st.vt, W.stage_a.p, S, g->copy_stream);
-      LVG_CUDA(cudaMemcpyAsync(out->vertexWeight, W.stage_a.p, S * 8, cudaMemcpyDeviceToHost, g->copy_stream));
+      LVG_CUDA(cudaMemcpyAsync(out->vertexWeight, st.vt, S * sizeof(tot_t), cudaMemcpyDeviceToHost,
+                               g->copy_stream));
     };
     run(g, method, db, prior, st, opt, info, early ? &hook : nullptr);
     fill_result(out, info, g->base.span);

@@ -38,7 +38,7 @@ struct Workspace {
   size_t S = 0, X = 0;
   DBuf<uint8_t> vaff, mark, fv, fn, fc;
   DBuf<uint32_t> ucom, vcom, com_next, dec, cext, csize, ccur, cmem, cbins, wl, wl_count;
-  DBuf<float> utot, vtot, ctot;
+  DBuf<tot_t> utot, vtot, ctot;  // vertex weights (level 0 / current level) and community totals
   DBuf<uint64_t> scan64;
   DBuf<uint32_t> scan32, binscratch;
   LevelBuffers lv[2];
@@ -46,7 +46,7 @@ struct Workspace {
   DBuf<float> gvals;
   DBuf<double> ctot64;
   DBuf<uint32_t> prior_q;
-  DBuf<float> prior_vt, prior_ct;
+  DBuf<tot_t> prior_vt, prior_ct;
   DBuf<double> stage_a, stage_b;
   // chunked hub path
   DBuf<uint32_t> chunk_cnt, part_key;
@@ -147,7 +147,7 @@ struct UnionInfo {
   HBuf<GraphCtl> hctl;
   DBuf<uint8_t> gact, aggex;
   DBuf<uint32_t> q;             // results (level-0 sized)
-  DBuf<float> ct;
+  DBuf<tot_t> ct;
   DBuf<uint8_t> aff;
 };
 
@@ -254,7 +254,7 @@ struct lvg_state {
   lvg_graph *g = nullptr;
   int device = 0;
   DBuf<uint32_t> q;
-  DBuf<float> vt, ct;
+  DBuf<tot_t> vt, ct;
 };
 
 struct lvg_device_batch {
@@ -273,7 +273,7 @@ namespace lvg {
 // A first-level state on the device: membership, vertex and community weights.
 struct StateRef {
   uint32_t *q;
-  float *vt, *ct;
+  tot_t *vt, *ct;
 };
 
 // Sizes of a tidied batch (deletions, insertions, touched rows, longest
@@ -315,7 +315,7 @@ void upload_batch(lvg_graph *g, const lvg_batch *b, DBuf<uint32_t> &ds, DBuf<uin
                   DBuf<uint32_t> &is, DBuf<uint32_t> &id, DBuf<float> &iw, DBuf<uint32_t> &seg, DBatch &out);
 void fill_result(lvg_result *out, const RunInfo &info, size_t span);
 void upload_prior(lvg_graph *g, const uint32_t *q, const double *qvtot, const double *qctot, uint32_t *dq,
-                  float *dvt, float *dct);
+                  tot_t *dvt, tot_t *dct);
 int run_host(lvg_graph *g, int method, const lvg_batch *b, const uint32_t *q, const double *qvtot,
              const double *qctot, const lvg_options *o, lvg_result *out);
 void init_graph(lvg_graph *g, size_t span, size_t order, size_t X, const uint64_t *coff, const uint32_t *ckey,

@@ -165,12 +165,12 @@ struct MoveArgs {
   uint32_t count;        // list length (an upper bound when count_ptr is set)
   const uint32_t *count_ptr;  // device-side list length (worklists), or nullptr
   uint32_t *vcom;        // membership (async: read/write; sync: snapshot, read only)
-  float *ctot;           // community totals (async: read/write; sync: snapshot)
+  tot_t *ctot;           // community totals (async: read/write; sync: snapshot)
   uint32_t *dec;         // sync: decided community per vertex (EMPTY = stay)
   uint8_t *vaff;         // affected flags
   uint8_t *mark;         // sync: neighbour marks of this iteration
   const uint8_t *fa;     // may the vertex move (delta-screening pass 0), or nullptr
-  const float *vtot;     // vertex weights
+  const tot_t *vtot;     // vertex weights
   float kr;              // R / (2M)
   int bin;               // degree bin of the list (statistics)
   Counters *ctr;
@@ -211,7 +211,6 @@ struct AggArgs {
   uint32_t *ydeg;        // output row degrees
   uint32_t *ykey;
   float *yw;
-  float *vtot;           // output level's vertex weights (row sums)
   uint32_t cn;           // number of communities (distinct keys per row <= cn)
   Counters *ctr;
   uint32_t *gkeys;
@@ -263,15 +262,13 @@ int grid_for(size_t n, int block, int max_blocks_per_sm = 8);
 void launch_degrees(const uint64_t *off, uint32_t *deg, size_t span, cudaStream_t s);
 void launch_fill_u8(uint8_t *p, uint8_t v, size_t n, cudaStream_t s);
 void launch_fill_f32(float *p, size_t n, float v, cudaStream_t s);
-void launch_init_static(const Level &g, uint32_t *ucom, float *utot, float *ctot, cudaStream_t s);
+void launch_init_static(const Level &g, uint32_t *ucom, tot_t *utot, tot_t *ctot, cudaStream_t s);
 void launch_total_weight(const float *w, size_t n, Counters *ctr, cudaStream_t s);  // -> ctr->fp64[0]
 // louvainVertexWeightsOmpW / louvainCommunityWeightsOmpW in FP64 (the C-ABI utilities).
 void launch_vertex_weights_f64(const Level &g, double *vtot, cudaStream_t s);
 void launch_community_weights_f64(const uint32_t *q, const double *vtot, size_t n, double *ctot, cudaStream_t s);
-void launch_prior_to_f32(const double *src, float *dst, size_t n, cudaStream_t s);
-void launch_f32_to_f64(const float *src, double *dst, size_t n, cudaStream_t s);
 void launch_batch_weights(const uint32_t *src, const float *w, size_t n, float sign, const uint32_t *vcom,
-                          float *vtot, float *ctot, cudaStream_t s);
+                          tot_t *vtot, tot_t *ctot, cudaStream_t s);
 void launch_df_mark(const uint32_t *ds, const uint32_t *dd, size_t nd, const uint32_t *is, const uint32_t *id,
                     size_t ni, const uint32_t *vcom, uint8_t *vaff, cudaStream_t s);
 // seg: ni entries (sources left to the per-source pass, then those with more
@@ -279,7 +276,7 @@ void launch_df_mark(const uint32_t *ds, const uint32_t *dd, size_t nd, const uin
 // entries and scan_scratch for exclusive_scan_u32 over them.
 void launch_ds_mark(const Level &g, const uint32_t *ds, const uint32_t *dd, size_t nd, const uint32_t *is,
                     const uint32_t *id, const float *iw, size_t ni, const uint32_t *seg, size_t nseg,
-                    const uint32_t *vcom, const float *vtot, const float *ctot, double M, double R,
+                    const uint32_t *vcom, const tot_t *vtot, const tot_t *ctot, double M, double R,
                     uint8_t *vertices, uint8_t *neighbors, uint8_t *communities, uint32_t *gkeys, float *gvals,
                     uint32_t *gfirst, int glog2, Counters *ctr, uint32_t *list, uint32_t *count, uint32_t *chunks,
                     uint32_t *scan_scratch, cudaStream_t s);
@@ -310,15 +307,25 @@ void launch_compact_active(const uint32_t *bins, const BinBounds &bb, const uint
                            uint32_t *wl, uint32_t *wl_count, cudaStream_t s, const uint32_t *gid = nullptr,
                            const uint8_t *gact = nullptr);
 // Deterministic mode: apply the decisions of one colour class (list of its vertices).
-void launch_apply_moves(const uint32_t *list, size_t n, uint32_t *dec, uint32_t *vcom, float *ctot,
-                        const float *vtot, cudaStream_t s);
+void launch_apply_moves(const uint32_t *list, size_t n, uint32_t *dec, uint32_t *vcom, tot_t *ctot,
+                        const tot_t *vtot, cudaStream_t s);
 void launch_community_flags(const Level &g, const uint32_t *vcom, uint32_t *cext, cudaStream_t s);
 void launch_lookup(uint32_t *a, const uint32_t *map, size_t n, cudaStream_t s);  // a[u] = map[a[u]]
 void launch_community_sizes(const Level &g, const uint32_t *vcom, uint32_t *csize, uint64_t *ctdeg,
                             cudaStream_t s);
 void launch_community_scatter(const Level &g, const uint32_t *vcom, const uint32_t *coff, uint32_t *ccur,
                               uint32_t *cmem, cudaStream_t s);
-void launch_level_init(size_t n, const float *vtot, uint32_t *vcom, float *ctot, uint8_t *vaff, cudaStream_t s);
+void launch_level_init(size_t n, const tot_t *vtot, uint32_t *vcom, tot_t *ctot, uint8_t *vaff, cudaStream_t s);
+// The next level's vertex weights from this level's community totals: for
+// every live community c of the level (cext: exclusive scan of the community
+// flags over the level's span, whose sum is *total: c is live when the next
+// entry, or the sum after the last one, is larger), vtot_next[cext[c]] =
+// ctot[c]. A super-vertex's weight (its row sum with the self-loop,
+// louvainVertexWeightsOmpW on the aggregated graph) equals its community's
+// total; it is taken from the exact FP64 total instead of re-summing the
+// aggregated rows.
+void launch_next_vertex_weights(const uint32_t *cext, size_t span, const uint32_t *total, const tot_t *ctot,
+                                tot_t *vtot_next, cudaStream_t s);
 void launch_count_flags(const uint8_t *f, size_t n, Counters *ctr, cudaStream_t s);
 // Set ERR_BAD_ID in ctr->err if any a[i] >= limit.
 void launch_check_ids(const uint32_t *a, size_t n, uint32_t limit, Counters *ctr, cudaStream_t s);
@@ -483,7 +490,7 @@ void launch_union_tolerance(size_t n, const uint32_t *gbase, uint32_t *cext, Gra
 // slice (the reference's arrays keep earlier levels' entries past the level's
 // span).
 void launch_union_snapshot(size_t span, const uint32_t *gid, const uint32_t *gbase, const uint32_t *vb0,
-                           const GraphCtl *ctl, const float *ctot, const uint8_t *vaff, float *ct_res,
+                           const GraphCtl *ctl, const tot_t *ctot, const uint8_t *vaff, tot_t *ct_res,
                            uint8_t *aff_res, cudaStream_t s);
 // Final membership of the graphs finishing now: (vcom ? vcom[ucom[v]] : ucom[v]) - gbase[g]; then done.
 void launch_union_finalize(size_t S, const uint32_t *gid0, const uint32_t *ucom, const uint32_t *vcom,

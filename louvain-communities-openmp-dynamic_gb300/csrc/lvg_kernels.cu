@@ -45,17 +45,17 @@ __global__ void degrees_kernel(const uint64_t *off, uint32_t *deg, size_t n) {
 // louvainVertexWeightsOmpW (inc/louvain.hxx:210) + louvainInitializeOmpW
 // (:285) for level 0: one warp per vertex (lane-strided rows).
 __global__ void init_static_kernel(const uint64_t *off, const uint32_t *deg, const float *w, const uint8_t *ex,
-                                   size_t n, const uint32_t *gid, const uint32_t *gbase, uint32_t *ucom, float *utot,
-                                   float *ctot) {
+                                   size_t n, const uint32_t *gid, const uint32_t *gbase, uint32_t *ucom, tot_t *utot,
+                                   tot_t *ctot) {
   const size_t warps = size_t(gridDim.x) * blockDim.x / 32;
   const int lane = threadIdx.x & 31;
   for (size_t u = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32; u < n; u += warps) {
     const bool has = !ex || ex[u];
-    float s = 0.f;
+    double s = 0.0;  // FP64, as the reference's vector<W> (exact for integer weights)
     if (has) {
       const uint64_t o = off[u];
       const uint32_t d = deg[u];
-      for (uint32_t j = lane; j < d; j += 32) s += w[o + j];
+      for (uint32_t j = lane; j < d; j += 32) s += double(w[o + j]);
 #pragma unroll
       for (int k = 16; k > 0; k >>= 1) s += __shfl_xor_sync(0xffffffffu, s, k);
     }
@@ -99,37 +99,29 @@ __global__ void fill_f32_kernel(float *p, size_t n, float v) {
   GRID_STRIDE(i, n) p[i] = v;
 }
 
-__global__ void prior_to_f32_kernel(const double *src, float *dst, size_t n) {
-  GRID_STRIDE(i, n) dst[i] = float(src[i]);
-}
-
-__global__ void f32_to_f64_kernel(const float *src, double *dst, size_t n) {
-  GRID_STRIDE(i, n) dst[i] = double(src[i]);
-}
-
 // louvainUpdateWeightsFromOmpU (inc/louvain.hxx:374-388): per directed batch
 // edge, the source's weight and its community's total move by the weight.
 // Lanes of a warp with the same source (the batch is source-sorted) or the
 // same community add their weights first and the lowest of them adds the sum:
 // a large community would otherwise take thousands of atomics on one word.
-__device__ __forceinline__ void group_add(float *p, uint32_t key, float x, int lane) {
+__device__ __forceinline__ void group_add(tot_t *p, uint32_t key, double x, int lane) {
   const unsigned grp = __match_any_sync(0xffffffffu, key);
-  float sum = 0.f;
+  double sum = 0.0;
   for (unsigned r = grp; r; r &= r - 1u) sum += __shfl_sync(grp, x, __ffs(r) - 1);
   if (key != EMPTY && (grp & ((1u << lane) - 1u)) == 0u) atomicAdd(p + key, sum);
 }
 
 __global__ void batch_weights_kernel(const uint32_t *src, const float *w, size_t n, float sign,
-                                     const uint32_t *vcom, float *vtot, float *ctot) {
+                                     const uint32_t *vcom, tot_t *vtot, tot_t *ctot) {
   const int lane = threadIdx.x & 31;
   for (size_t base = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32 * 32; base < n;
        base += size_t(gridDim.x) * blockDim.x) {
     const size_t i = base + lane;
     uint32_t u = EMPTY, c = EMPTY;
-    float x = 0.f;
+    double x = 0.0;
     if (i < n) {
       u = src[i];
-      x = sign * w[i];
+      x = double(sign) * double(w[i]);
       c = vcom[u];
     }
     group_add(vtot, u, x, lane);
@@ -180,7 +172,7 @@ constexpr int DS_LOG = 11;  // shared table: 2048 slots, sources with <= 1024 in
 __global__ void __launch_bounds__(DS_BLOCK) ds_ins_kernel(const uint32_t *is, const uint32_t *id, const float *iw,
                                                           size_t ni, const uint32_t *seg, const unsigned int *nseg,
                                                           const unsigned int *nlong, const uint32_t *vcom,
-                                                          const float *vtot, const float *ctot, double M, double R,
+                                                          const tot_t *vtot, const tot_t *ctot, double M, double R,
                                                           uint8_t *vertices, uint8_t *neighbors,
                                                           uint8_t *communities, uint32_t *gkeys, float *gvals,
                                                           uint32_t *gfirst, int glog2, Counters *ctr) {
@@ -273,8 +265,9 @@ __global__ void __launch_bounds__(DS_BLOCK) ds_ins_kernel(const uint32_t *is, co
 // |vtot|, |ctot| <= 2M. The screened gain x - y, x = vcout/M, y =
 // R vtot (vtot + ctot_c - ctot_d) / (2M^2), takes about ten roundings of
 // 2^-24 relative to |x| and to yb = R |vtot| (|vtot| + |ctot_c| + |ctot_d|) /
-// (2M^2) (the constants' conversions included; the cancellation in
-// vtot + ctot_c - ctot_d is bounded by yb's terms), and the reference's FP64
+// (2M^2) (the constants' conversions and the FP32 roundings of the FP64
+// totals included; the cancellation in vtot + ctot_c - ctot_d is bounded by
+// yb's terms), and the reference's FP64
 // value differs from the exact one by about 2^-50 of the same; 2^-20 covers
 // both with room. DS_SCREEN_ABS covers results below the normal range.
 struct DsScreen {
@@ -290,7 +283,7 @@ constexpr float DS_SCREEN_ABS = 1e-36f;
 // first insertion) carries it into the argmax.
 __global__ void ds_ins_warp_kernel(const uint32_t *is, const uint32_t *id, const float *iw, size_t ni,
                                    uint32_t *seg, const unsigned int *nseg, unsigned int *nlong, const uint32_t *vcom,
-                                   const float *vtot, const float *ctot, double M, double R, DsScreen sc,
+                                   const tot_t *vtot, const tot_t *ctot, double M, double R, DsScreen sc,
                                    uint8_t *vertices, uint8_t *neighbors, uint8_t *communities) {
   const unsigned ns = *nseg;
   const int lane = threadIdx.x & 31;
@@ -322,10 +315,11 @@ __global__ void ds_ins_warp_kernel(const uint32_t *is, const uint32_t *id, const
     // FP32 screen: e32 is the gain within er of the exact value, and of the
     // reference's FP64 value too; when every sign and the winner are clear by
     // more than the bound, FP64 (slow on this part) is skipped
-    const float vu = vtot[u], td = ctot[d];
+    const double vu64 = vtot[u], td64 = ctot[d];
+    const float vu = float(vu64), td = float(td64);
     float e32 = 0.f, er = 0.f;
     if (leader) {
-      const float tc = ctot[c];
+      const float tc = float(ctot[c]);
       const float x = sum * sc.invM;
       const float y = sc.R * vu * (vu + tc - td) * sc.inv2MM;
       const float yb = sc.R * fabsf(vu) * (fabsf(vu) + fabsf(tc) + fabsf(td)) * sc.inv2MM;
@@ -359,7 +353,7 @@ __global__ void ds_ins_warp_kernel(const uint32_t *is, const uint32_t *id, const
       uint32_t bf = 0xffffffffu;
       bc = 0;
       if (leader) {
-        const double e = delta_modularity(double(sum), 0.0, double(vu), double(ctot[c]), double(td), M, R);
+        const double e = delta_modularity(double(sum), 0.0, vu64, ctot[c], td64, M, R);
         if (e > 0) { be = e; bf = uint32_t(lane); bc = c; }
       }
 #pragma unroll
@@ -387,8 +381,8 @@ __global__ void ds_ins_warp_kernel(const uint32_t *is, const uint32_t *id, const
 // weights in batch order (the reference's vcout); the lowest of them stands
 // for the community, so lane order is the reference's scan order.
 __global__ void ds_ins_lane_kernel(const uint32_t *is, const uint32_t *id, const float *iw, size_t ni,
-                                   uint32_t *seg, unsigned int *nseg, const uint32_t *vcom, const float *vtot,
-                                   const float *ctot, DsScreen sc, uint8_t *vertices, uint8_t *neighbors,
+                                   uint32_t *seg, unsigned int *nseg, const uint32_t *vcom, const tot_t *vtot,
+                                   const tot_t *ctot, DsScreen sc, uint8_t *vertices, uint8_t *neighbors,
                                    uint8_t *communities) {
   const int lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1u;
@@ -422,7 +416,7 @@ __global__ void ds_ins_lane_kernel(const uint32_t *is, const uint32_t *id, const
     const bool leader = c != EMPTY && (grp & below) == 0u;
     float e32 = 0.f, er = 0.f;
     if (leader) {
-      const float vu = vtot[u], td = ctot[d], tc = ctot[c];
+      const float vu = float(vtot[u]), td = float(ctot[d]), tc = float(ctot[c]);
       const float x = sum * sc.invM;
       const float y = sc.R * vu * (vu + tc - td) * sc.inv2MM;
       const float yb = sc.R * fabsf(vu) * (fabsf(vu) + fabsf(tc) + fabsf(td)) * sc.inv2MM;
@@ -595,8 +589,8 @@ __global__ void merge_marks_kernel(uint8_t *vaff, uint8_t *mark, size_t n) {
 // Deterministic mode: commit the decisions of one colour class (the moves of
 // louvainChangeCommunityOmpW, inc/louvain.hxx:496-503, applied after every
 // vertex of the class has decided from the same state).
-__global__ void apply_moves_kernel(const uint32_t *list, size_t n, uint32_t *dec, uint32_t *vcom, float *ctot,
-                                   const float *vtot) {
+__global__ void apply_moves_kernel(const uint32_t *list, size_t n, uint32_t *dec, uint32_t *vcom, tot_t *ctot,
+                                   const tot_t *vtot) {
   GRID_STRIDE(i, n) {
     const uint32_t u = list[i];
     const uint32_t c = dec[u];
@@ -672,7 +666,18 @@ __global__ void community_scatter_kernel(const uint8_t *ex, size_t n, const uint
 
 // louvainInitializeOmpW on an aggregated level + the driver's vaff fill
 // (inc/louvain.hxx:1207-1210).
-__global__ void level_init_kernel(size_t n, const float *vtot, uint32_t *vcom, float *ctot, uint8_t *vaff) {
+// The next level's vertex weights from this level's community totals (see
+// launch_next_vertex_weights).
+__global__ void next_vertex_weights_kernel(const uint32_t *cext, size_t span, const uint32_t *total,
+                                           const tot_t *ctot, tot_t *vnext) {
+  GRID_STRIDE(c, span) {
+    const uint32_t id = cext[c];
+    const uint32_t next = c + 1 < span ? cext[c + 1] : *total;
+    if (next > id) vnext[id] = ctot[c];
+  }
+}
+
+__global__ void level_init_kernel(size_t n, const tot_t *vtot, uint32_t *vcom, tot_t *ctot, uint8_t *vaff) {
   GRID_STRIDE(u, n) {
     vcom[u] = uint32_t(u);
     ctot[u] = vtot[u];
@@ -859,7 +864,7 @@ void launch_fill_f32(float *p, size_t n, float v, cudaStream_t s) {
   LVG_CHECK_LAUNCH();
 }
 
-void launch_init_static(const Level &g, uint32_t *ucom, float *utot, float *ctot, cudaStream_t s) {
+void launch_init_static(const Level &g, uint32_t *ucom, tot_t *utot, tot_t *ctot, cudaStream_t s) {
   if (!g.span) return;
   init_static_kernel<<<grid_for(g.span * 32, 256), 256, 0, s>>>(g.off, g.deg, g.w, g.ex, g.span, g.gid, g.gbase,
                                                                  ucom, utot, ctot);
@@ -886,20 +891,8 @@ void launch_total_weight(const float *w, size_t n, Counters *ctr, cudaStream_t s
   LVG_CHECK_LAUNCH();
 }
 
-void launch_prior_to_f32(const double *src, float *dst, size_t n, cudaStream_t s) {
-  if (!n) return;
-  prior_to_f32_kernel<<<grid_for(n, 256), 256, 0, s>>>(src, dst, n);
-  LVG_CHECK_LAUNCH();
-}
-
-void launch_f32_to_f64(const float *src, double *dst, size_t n, cudaStream_t s) {
-  if (!n) return;
-  f32_to_f64_kernel<<<grid_for(n, 256), 256, 0, s>>>(src, dst, n);
-  LVG_CHECK_LAUNCH();
-}
-
 void launch_batch_weights(const uint32_t *src, const float *w, size_t n, float sign, const uint32_t *vcom,
-                          float *vtot, float *ctot, cudaStream_t s) {
+                          tot_t *vtot, tot_t *ctot, cudaStream_t s) {
   if (!n) return;
   batch_weights_kernel<<<grid_for(n, 256), 256, 0, s>>>(src, w, n, sign, vcom, vtot, ctot);
   LVG_CHECK_LAUNCH();
@@ -914,7 +907,7 @@ void launch_df_mark(const uint32_t *ds, const uint32_t *dd, size_t nd, const uin
 
 void launch_ds_mark(const Level &g, const uint32_t *ds, const uint32_t *dd, size_t nd, const uint32_t *is,
                     const uint32_t *id, const float *iw, size_t ni, const uint32_t *seg, size_t nseg_cap,
-                    const uint32_t *vcom, const float *vtot, const float *ctot, double M, double R,
+                    const uint32_t *vcom, const tot_t *vtot, const tot_t *ctot, double M, double R,
                     uint8_t *vertices, uint8_t *neighbors, uint8_t *communities, uint32_t *gkeys, float *gvals,
                     uint32_t *gfirst, int glog2, Counters *ctr, uint32_t *list, uint32_t *count, uint32_t *chunks,
                     uint32_t *scan_scratch, cudaStream_t s) {
@@ -982,8 +975,8 @@ void launch_merge_marks(uint8_t *vaff, uint8_t *mark, size_t n, cudaStream_t s) 
   LVG_CHECK_LAUNCH();
 }
 
-void launch_apply_moves(const uint32_t *list, size_t n, uint32_t *dec, uint32_t *vcom, float *ctot,
-                        const float *vtot, cudaStream_t s) {
+void launch_apply_moves(const uint32_t *list, size_t n, uint32_t *dec, uint32_t *vcom, tot_t *ctot,
+                        const tot_t *vtot, cudaStream_t s) {
   if (!n) return;
   apply_moves_kernel<<<grid_for(n, 256), 256, 0, s>>>(list, n, dec, vcom, ctot, vtot);
   LVG_CHECK_LAUNCH();
@@ -1016,7 +1009,14 @@ void launch_community_scatter(const Level &g, const uint32_t *vcom, const uint32
   LVG_CHECK_LAUNCH();
 }
 
-void launch_level_init(size_t n, const float *vtot, uint32_t *vcom, float *ctot, uint8_t *vaff, cudaStream_t s) {
+void launch_next_vertex_weights(const uint32_t *cext, size_t span, const uint32_t *total, const tot_t *ctot,
+                                tot_t *vtot_next, cudaStream_t s) {
+  if (!span) return;
+  next_vertex_weights_kernel<<<grid_for(span, 256), 256, 0, s>>>(cext, span, total, ctot, vtot_next);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_level_init(size_t n, const tot_t *vtot, uint32_t *vcom, tot_t *ctot, uint8_t *vaff, cudaStream_t s) {
   if (!n) return;
   level_init_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, vtot, vcom, ctot, vaff);
   LVG_CHECK_LAUNCH();

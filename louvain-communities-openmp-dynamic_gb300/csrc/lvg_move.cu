@@ -225,17 +225,18 @@ __device__ __forceinline__ void tile_loop(const MoveArgs &a, const uint32_t *lis
 #pragma unroll
     for (int sh = T / 2; sh > 0; sh >>= 1) kd += __shfl_xor_sync(m, kd, sh, T);
     __syncwarp(m);
-    float wu = 0.f, td = 0.f;
+    double wu = 0.0, td = 0.0;
     if (tl == 0) { wu = a.vtot[u]; td = a.ctot[d]; }
     wu = __shfl_sync(m, wu, 0, T);
     td = __shfl_sync(m, td, 0, T);
+    const float wuf = __double2float_rn(wu);
     float bg = 0.f;
     uint32_t bc = EMPTY;
 #pragma unroll
     for (int s = tl; s < C; s += T) {
       const uint32_t c = keys[s];
       if (c == EMPTY) continue;
-      const float g = gain_f32(vals[s], kd, wu, a.ctot[c], td, G.kr);
+      const float g = gain_of(vals[s], kd, wu, wuf, a.ctot[c], td, G.kr);
       if (g > 0.f) take_better(bg, bc, g, c);
     }
 #pragma unroll
@@ -539,8 +540,9 @@ __global__ void __launch_bounds__(B) move_big_kernel(MoveArgs a) {
       });
     }
     kd = block_sum<B>(kd, red_g);  // barrier: table complete
-    const float wu = a.vtot[u];
-    const float td = a.ctot[d];
+    const double wu = a.vtot[u];
+    const float wuf = __double2float_rn(wu);
+    const double td = a.ctot[d];
     float bg = 0.f;
     uint32_t bc = EMPTY;
     if (!over) {
@@ -548,14 +550,14 @@ __global__ void __launch_bounds__(B) move_big_kernel(MoveArgs a) {
         const uint32_t s2 = t.list[j];
         if (s2 == EMPTY) continue;
         const uint32_t c = t.keys[s2];
-        const float g = gain_f32(t.vals[s2], kd, wu, a.ctot[c], td, G.kr);
+        const float g = gain_of(t.vals[s2], kd, wu, wuf, a.ctot[c], td, G.kr);
         if (g > 0.f) take_better(bg, bc, g, c);
       }
     } else {
       for (uint32_t s2 = threadIdx.x; s2 < gcap; s2 += B) {
         const uint32_t c = gkeys[s2];
         if (c == EMPTY) continue;
-        const float g = gain_f32(gvals[s2], kd, wu, a.ctot[c], td, G.kr);
+        const float g = gain_of(gvals[s2], kd, wu, wuf, a.ctot[c], td, G.kr);
         if (g > 0.f) take_better(bg, bc, g, c);
       }
     }
@@ -766,8 +768,9 @@ __global__ void __launch_bounds__(B) hub_merge_kernel(MoveArgs a) {
       __syncthreads();
     }
     const float kd = s_kd;
-    const float wu = a.vtot[u];
-    const float td = a.ctot[d];
+    const double wu = a.vtot[u];
+    const float wuf = __double2float_rn(wu);
+    const double td = a.ctot[d];
     float bg = 0.f;
     uint32_t bc = EMPTY;
     if (!over) {
@@ -775,14 +778,14 @@ __global__ void __launch_bounds__(B) hub_merge_kernel(MoveArgs a) {
         const uint32_t s2 = t.list[j];
         if (s2 == EMPTY) continue;
         const uint32_t c = t.keys[s2];
-        const float g2 = gain_f32(t.vals[s2], kd, wu, a.ctot[c], td, G.kr);
+        const float g2 = gain_of(t.vals[s2], kd, wu, wuf, a.ctot[c], td, G.kr);
         if (g2 > 0.f) take_better(bg, bc, g2, c);
       }
     } else {
       for (uint32_t s2 = threadIdx.x; s2 < gcap; s2 += B) {
         const uint32_t c = gkeys[s2];
         if (c == EMPTY) continue;
-        const float g2 = gain_f32(gvals[s2], kd, wu, a.ctot[c], td, G.kr);
+        const float g2 = gain_of(gvals[s2], kd, wu, wuf, a.ctot[c], td, G.kr);
         if (g2 > 0.f) take_better(bg, bc, g2, c);
       }
     }

@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(BIN_THREADS) bin_scatter_kernel(const D *deg, 
   for (int k = threadIdx.x; k < nbk; k += BIN_THREADS) run[k] = offs[size_t(k) * nb + blockIdx.x];
   size_t base = size_t(blockIdx.x) * BIN_CHUNK;
   for (int r = 0; r < BIN_CHUNK; r += BIN_THREADS) {
-    for (int k = threadIdx.x; k < NW * MAX_BUCKETS; k += BIN_THREADS) (&wcnt[0][0])[k] = 0;
+    for (int k = threadIdx.x; k < NW * nbk; k += BIN_THREADS) wcnt[k / nbk][k % nbk] = 0;
     __syncthreads();
     size_t j = base + r + threadIdx.x;
     int b = -1;

@@ -126,7 +126,7 @@ __global__ void union_tolerance_kernel(size_t n, const uint32_t *gbase, uint32_t
 }
 
 __global__ void union_snapshot_kernel(size_t span, const uint32_t *gid, const uint32_t *gbase, const uint32_t *vb0,
-                                      const GraphCtl *ctl, const float *ctot, const uint8_t *vaff, float *ct_res,
+                                      const GraphCtl *ctl, const tot_t *ctot, const uint8_t *vaff, tot_t *ct_res,
                                       uint8_t *aff_res) {
   GRID_STRIDE(x, span) {
     const uint32_t i = gid[x];
@@ -259,7 +259,7 @@ void launch_union_tolerance(size_t n, const uint32_t *gbase, uint32_t *cext, Gra
 }
 
 void launch_union_snapshot(size_t span, const uint32_t *gid, const uint32_t *gbase, const uint32_t *vb0,
-                           const GraphCtl *ctl, const float *ctot, const uint8_t *vaff, float *ct_res,
+                           const GraphCtl *ctl, const tot_t *ctot, const uint8_t *vaff, tot_t *ct_res,
                            uint8_t *aff_res, cudaStream_t s) {
   if (!span) return;
   union_snapshot_kernel<<<grid(span, 256), 256, 0, s>>>(span, gid, gbase, vb0, ctl, ctot, vaff, ct_res, aff_res);

@@ -535,8 +535,9 @@ class LouvainOptions:
                         int(self.colors))
 
     def effective_colors(self) -> int:
+        """Class count of the deterministic replay (deterministic mode's default is 16)."""
         k = self.colors if self.colors > 0 else (16 if self.deterministic else 8)
-        return max(1, min(32, k))
+        return max(1, min(64, k))
 
 
 @dataclass

@@ -546,17 +546,21 @@ int orc_louvain(size_t span, const uint64_t *off, const uint32_t *key, const flo
  * decides from the same state (membership, community totals and flags as
  * left by the previous classes), then all decisions of the class are applied
  * and the neighbour marks of its movers are merged into the flags.
- * Per vertex u the gain of joining community c is, in FP32 and in exactly
- * this operation order,
- *     g(c) = (k_c - k_d) - w_u * ((w_u + t_c) - t_d) * kr,   kr = (float)(R/(2M)),
+ * Per vertex u the gain of joining community c is, in exactly this
+ * operation order,
+ *     g(c) = (k_c - k_d) - (float)w_u * (float)((w_u + t_c) - t_d) * kr,   kr = (float)(R/(2M)),
+ * with the vertex weight w_u and the community totals t_c, t_d in FP64 (as the
+ * reference's W) and everything else in FP32;
  * which is M times the reference's ΔQ. The best c != d is the largest g > 0,
  * ties going to the lowest community id. A best c of 0 does not move (the
  * reference's "if (c)"). The convergence sum adds, per vertex, the best gain
  * as a 2^-16 fixed-point integer: el = (Σ llrint(g*65536)) / 65536 / M.
  * A processed vertex clears its flag; a mover marks its neighbours v != u.
- * All weights are FP32; sums of integer weights below 2^24 are exact in any
- * order, which is the domain in which the GPU's deterministic mode and this
- * replay agree bit for bit.
+ * Edge weights and the per-vertex link sums k_c are FP32, vertex weights and
+ * community totals FP64. A super-vertex's weight is its community's total.
+ * Sums of integer weights are exact in any order (below 2^24 in FP32, 2^53
+ * in FP64), which is the domain in which the GPU's deterministic mode and
+ * this replay agree bit for bit.
  * ==================================================================== */
 
 static inline uint32_t color_of(uint32_t u, uint32_t k) {
@@ -582,17 +586,16 @@ typedef struct TableF {
   uint8_t *seen;
 } TableF;
 
-static inline float gain_f32(float kc, float kd, float wu, float tc, float td, float kr) {
+static inline float gain_of(float kc, float kd, double wu, double tc, double td, float kr) {
   float a = kc - kd;
-  float b = wu + tc;
-  float c = b - td;
-  float d = wu * c;
+  float c = (float)((wu + tc) - td);
+  float d = (float)wu * c;
   float e = d * kr;
   return a - e;
 }
 
-static int move_sync(const GF *g, uint32_t *vcom, float *ctot, uint8_t *vaff, uint8_t *mark, uint32_t *dec,
-                     const float *vtot, double M, float kr, int L, double E, const uint8_t *fa, TableF *tabs,
+static int move_sync(const GF *g, uint32_t *vcom, double *ctot, uint8_t *vaff, uint8_t *mark, uint32_t *dec,
+                     const double *vtot, double M, float kr, int L, double E, const uint8_t *fa, TableF *tabs,
                      int K) {
   size_t S = g->span;
   int l = 0;
@@ -622,7 +625,7 @@ static int move_sync(const GF *g, uint32_t *vcom, float *ctot, uint8_t *vaff, ui
         for (size_t i = 0; i < t->n; ++i) {
           uint32_t c = t->keys[i];
           if (c == d) continue;
-          float gc = gain_f32(t->val[c], kd, vtot[u], ctot[c], ctot[d], kr);
+          float gc = gain_of(t->val[c], kd, vtot[u], ctot[c], ctot[d], kr);
           if (gc > 0 && (!found || gc > bg || (gc == bg && c < best))) { found = 1; bg = gc; best = c; }
         }
         for (size_t i = 0; i < t->n; ++i) t->seen[t->keys[i]] = 0;
@@ -738,7 +741,7 @@ int orc_louvain_sync(size_t span, const uint64_t *off, const uint32_t *key, cons
   }
   uint8_t *vaff = (uint8_t *)calloc(S, 1), *mark = (uint8_t *)calloc(S, 1);
   uint32_t *ucom = (uint32_t *)calloc(S, 4), *vcom = (uint32_t *)calloc(S, 4), *dec = (uint32_t *)calloc(S, 4);
-  float *utot = (float *)calloc(S, 4), *vtot = (float *)calloc(S, 4), *ctot = (float *)calloc(S, 4);
+  double *utot = (double *)calloc(S, 8), *vtot = (double *)calloc(S, 8), *ctot = (double *)calloc(S, 8);
   uint32_t *cext = (uint32_t *)calloc(S, 4);
   uint8_t *fv = NULL;
   size_t cap = X > 0 ? X : 1;
@@ -748,27 +751,25 @@ int orc_louvain_sync(size_t span, const uint64_t *off, const uint32_t *key, cons
   if (method == ORC_STATIC) {
     for (size_t u = 0; u < S; ++u) {
       if (!gf_has(&x, u)) continue;
-      float s = 0;
+      double s = 0;
       for (uint64_t i = off[u]; i < off[u + 1]; ++i) s += w[i];
       utot[u] = s; ucom[u] = (uint32_t)u; ctot[u] = s;
     }
     memset(vaff, 1, S);
   } else {
     memcpy(ucom, q, S * 4);
-    for (size_t u = 0; u < S; ++u) { utot[u] = (float)qvtot[u]; ctot[u] = (float)qctot[u]; }
+    for (size_t u = 0; u < S; ++u) { utot[u] = qvtot[u]; ctot[u] = qctot[u]; }
     for (size_t i = 0; i < nd; ++i) { utot[ds[i]] -= dw[i]; ctot[ucom[ds[i]]] -= dw[i]; }
     for (size_t i = 0; i < ni; ++i) { utot[is[i]] += iw[i]; ctot[ucom[is[i]]] += iw[i]; }
     if (method == ORC_NAIVE) memset(vaff, 1, S);
     else if (method == ORC_FRONTIER) orc_df_mark(S, nd, ds, dd, ni, is, id, ucom, vaff);
     else {
-      /* The delta-screening marking reads FP64 totals, as the reference does. */
-      double *vt = (double *)malloc(S * 8), *ct = (double *)malloc(S * 8);
-      for (size_t u = 0; u < S; ++u) { vt[u] = utot[u]; ct[u] = ctot[u]; }
+      /* The delta-screening marking reads the FP64 totals, as the reference does. */
       uint8_t *fn = (uint8_t *)calloc(S, 1), *fcm = (uint8_t *)calloc(S, 1);
       fv = (uint8_t *)calloc(S, 1);
-      orc_ds_mark(span, off, key, w, ex, nd, ds, dd, ni, is, id, iw, ucom, vt, ct, M, R, fv, fn, fcm);
+      orc_ds_mark(span, off, key, w, ex, nd, ds, dd, ni, is, id, iw, ucom, utot, ctot, M, R, fv, fn, fcm);
       memcpy(vaff, fv, S);
-      free(vt); free(ct); free(fn); free(fcm);
+      free(fn); free(fcm);
     }
   }
   double E = o->tolerance;
@@ -790,8 +791,14 @@ int orc_louvain_sync(size_t span, const uint64_t *off, const uint32_t *key, cons
       cext[cur[u]] = 1;
     }
     if ((double)CN / (double)GN >= o->aggregationTolerance) break;
+    /* renumber; a super-vertex's weight is its community's total */
     uint32_t acc = 0;
-    for (size_t c = 0; c < gx->span; ++c) { uint32_t t = cext[c]; cext[c] = acc; acc += t; }
+    for (size_t c = 0; c < gx->span; ++c) {
+      uint32_t t = cext[c];
+      cext[c] = acc;
+      if (t) vtot[acc] = ctot[c];
+      acc += t;
+    }
     for (size_t u = 0; u < S; ++u) cur[u] = cext[cur[u]];
     if (!first) for (size_t u = 0; u < S; ++u) ucom[u] = vcom[ucom[u]];
     aggregate_f(gx, cur, CN, zoff, zkey, zw, tabs);
@@ -800,11 +807,7 @@ int orc_louvain_sync(size_t span, const uint64_t *off, const uint32_t *key, cons
     float *t3 = yw; yw = zw; zw = t3;
     y.span = CN; y.order = CN; y.off = yoff; y.key = ykey; y.w = yw; y.ex = NULL;
     memset(vaff, 1, CN);
-    for (size_t u = 0; u < CN; ++u) {
-      float s = 0;
-      for (uint64_t i = yoff[u]; i < yoff[u + 1]; ++i) s += yw[i];
-      vtot[u] = s; vcom[u] = (uint32_t)u; ctot[u] = s;
-    }
+    for (size_t u = 0; u < CN; ++u) { vcom[u] = (uint32_t)u; ctot[u] = vtot[u]; }
     E /= o->toleranceDrop;
   }
   if (p > 1) for (size_t u = 0; u < S; ++u) ucom[u] = vcom[ucom[u]];

@@ -44,7 +44,7 @@ def test_launch_knobs_keep_deterministic_results(cuda, hubcase):
 @pytest.mark.gpu
 def test_invalid_tuning_is_rejected(cuda, hubcase):
     Y = cuda.Graph(hubcase[2])
-    for bad in [dict(hub_chunk=100), dict(frontier_colors=0), dict(frontier_colors=33), dict(big_blocks_per_sm=-1),
+    for bad in [dict(hub_chunk=100), dict(frontier_colors=0), dict(frontier_colors=65), dict(big_blocks_per_sm=-1),
                 dict(frontier_max_fraction=2.0)]:
         with pytest.raises(RuntimeError):
             cuda.set_tuning(Y, **bad)
