@@ -98,9 +98,10 @@ def parse():
     p.add_argument("--set-tuning", default="",
                    help="df workload: launch shapes as knob=value,... (lvg_tuning fields) instead of "
                         "running the autotuner, e.g. to profile the shapes a timed run picked")
-    p.add_argument("--ncu-method", default="df", choices=["df", "static"],
-                   help="profiling mode of the df workload: the method profiled (static: the plain "
-                        "GPU static Louvain on the updated graph)")
+    p.add_argument("--ncu-method", default="df", choices=["df", "static", "nd", "ds", "apply"],
+                   help="profiling mode of the df workload: the call profiled (static: the plain GPU static "
+                        "Louvain on the updated graph; nd / ds: naive-dynamic / delta-screening from the prior; "
+                        "apply: tidy + apply of the step's batch to a copy of the base graph in HBM)")
     return p.parse_args()
 
 
@@ -503,8 +504,28 @@ def run_gpu(args):
         tuning, _ = lvg.autotune(Y, lvg.METHOD_FRONTIER, db, st_prior, o, repeats=5)
         tune_s = time.perf_counter() - t0
 
+    if args.ncu_steps and args.ncu_method == "apply":
+        # tidy + apply of the step's batch, on fresh copies of the base graph
+        # (a batch applies once): one warm-up copy, then the profiled ones
+        X = lvg.Graph(x)
+        for k in range(1 + args.ncu_steps):
+            C = X.clone()
+            dbk = lvg.DeviceBatch(C, b)
+            if k:
+                lvg.profiler_start()
+            C.apply_batch(dbk)
+            if k:
+                lvg.profiler_stop()
+            dbk.close()
+            C.close()
+        if rank == 0:
+            print(json.dumps({"profiled_applies": args.ncu_steps, "batch_entries": b.num_deletions + b.num_insertions}),
+                  flush=True)
+        dist.close()
+        return 0
     if args.ncu_steps:
-        meth = lvg.METHOD_STATIC if args.ncu_method == "static" else lvg.METHOD_FRONTIER
+        meth = {"static": lvg.METHOD_STATIC, "nd": lvg.METHOD_NAIVE, "ds": lvg.METHOD_DELTA,
+                "df": lvg.METHOD_FRONTIER}[args.ncu_method]
         lvg.run_resident(Y, meth, db, st_prior, st_out, o)  # warm: graph capture
         lvg.profiler_start()
         for _ in range(args.ncu_steps):
@@ -1082,6 +1103,23 @@ def run_sweep(args):
     return 0
 
 
+def batched_specs(n_all: int, seed: int):
+    """The batched workload's graphs: |V| log-uniform in [1k, 256k], average
+    degree uniform in [8, 32], p_in uniform in [0.6, 0.9] (seeded; the same on
+    every rank)."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(1000), np.log(256_000), n_all)).astype(np.int64)
+    degs = rng.uniform(8, 32, n_all)
+    pins = rng.uniform(0.6, 0.9, n_all)
+    return sizes, degs, pins
+
+
+def rank_share(n_all: int, rank: int, world: int) -> list[int]:
+    """The graphs one GPU of `world` clusters: round robin, so the ranks'
+    shares are disjoint, cover every graph and differ in size by at most one."""
+    return list(range(rank, n_all, world))
+
+
 def run_batched(args):
     """Batched: planted-partition graphs with |V| log-uniform in [1k, 256k],
     average degree uniform in [8, 32], blocks of 128 (C = |V|/128), p_in
@@ -1101,12 +1139,9 @@ def run_batched(args):
     lvg_build.build()
     lvg.set_device(local)
     dist = Dist(world)
-    rng = np.random.default_rng(args.seed)
     n_all = args.batched_graphs
-    sizes = np.exp(rng.uniform(np.log(1000), np.log(256_000), n_all)).astype(np.int64)
-    degs = rng.uniform(8, 32, n_all)
-    pins = rng.uniform(0.6, 0.9, n_all)
-    mine = list(range(rank, n_all, world))  # this GPU's graphs
+    sizes, degs, pins = batched_specs(n_all, args.seed)
+    mine = rank_share(n_all, rank, world)  # this GPU's graphs
     t0 = time.time()
     graphs = [lvg.Graph.planted_partition(int(sizes[i]), 128, float(degs[i]), float(pins[i]), args.seed + i)
               for i in mine]
