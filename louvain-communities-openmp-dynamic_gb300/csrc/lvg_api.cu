@@ -317,6 +317,7 @@ int lvg_graph_clone(lvg_graph *x, lvg_graph **out) {
     lvg::Level &b = g->base;
     b.span = S; b.order = x->base.order; b.edges = x->base.edges;
     b.off = g->off.p; b.deg = g->deg.p; b.key = g->key.p; b.w = g->w.p; b.ex = x->base.ex ? g->ex.p : nullptr;
+    b.unit = x->base.unit;
     lvg::DBuf<uint32_t> scratch;
     scratch.ensure(lvg::bin_scratch_elems(S + 1, x->base.colors));
     lvg::compute_bins(g.get(), b, g->deg.p, g->bins.p, scratch.p, x->base.colors);  // synchronises

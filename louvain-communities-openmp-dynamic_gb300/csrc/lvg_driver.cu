@@ -221,7 +221,7 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot
         a.off = lv.off; a.deg = lv.deg; a.key = lv.key; a.w = lv.w;
         a.vcom = com; a.ctot = ctot; a.dec = W.dec.p;
         a.vaff = W.vaff.p; a.mark = W.mark.p; a.fa = fa; a.vtot = tot;
-        a.kr = kr; a.ctr = g->ctr.p; a.bin = grp.first;
+        a.kr = kr; a.ctr = g->ctr.p; a.unit = lv.unit; a.bin = grp.first;
         set_union(a);
         cudaEvent_t b0 = bin_ev ? g->events.record(s) : nullptr;
         launch_move_small(grp.first, grp.second, sync, a, sb, stream_of(grp.first));
@@ -239,7 +239,7 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot
       a.count_ptr = b == NUM_BINS - 1 ? nullptr : wlc + b;
       a.vcom = com; a.ctot = ctot; a.dec = W.dec.p;
       a.vaff = W.vaff.p; a.mark = W.mark.p; a.fa = fa; a.vtot = tot;
-      a.kr = kr; a.ctr = g->ctr.p; a.bin = b;
+      a.kr = kr; a.ctr = g->ctr.p; a.unit = lv.unit; a.bin = b;
       a.gkeys = need ? W.gkeys.p + goff[b] : nullptr;
       a.gvals = need ? W.gvals.p + goff[b] : nullptr;
       a.glog2 = glog2[b];
@@ -359,7 +359,7 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const 
     if (!most) continue;
     glog2[b] = global_table_log2(lv.bin_maxdeg[b]);
     goff[b] = need;  // each bin its own regions: the bins' kernels run concurrently
-    need += size_t(move_grid_blocks(b, sync, most, g->tuning.big_blocks_per_sm)) << glog2[b];
+    need += size_t(move_grid_blocks(b, sync, lv.unit, most, g->tuning.big_blocks_per_sm)) << glog2[b];
   }
   if (need) {
     W.gkeys.ensure(need);
@@ -378,7 +378,8 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const 
                           g->hctr.p, lv.hub.chunk, lv.hub.hub_vertex, lv.gid};
     std::memcpy(key.p, ps, sizeof(ps));
     key.n[0] = lv.span; key.n[1] = need; key.n[2] = lv.hub.chunks; key.n[3] = lv.bin_start[K * NUM_BINS];
-    key.k[0] = K; key.k[1] = sync; key.k[2] = glog2[9] | glog2[10] << 8 | glog2[11] << 16; key.k[3] = fused;
+    key.k[0] = K; key.k[1] = sync | int(lv.unit) << 1; key.k[2] = glog2[9] | glog2[10] << 8 | glog2[11] << 16;
+    key.k[3] = fused;
     key.kr = kr;
     key.E = uc ? E : 0.0;
   }
@@ -677,7 +678,14 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
     }
     if (p > 1) launch_lookup(ucom, W.vcom.p, S, s);
     cudaEvent_t eend = g->events.record(s);
+    if (r == rep - 1) {
+      // the residual affected count (inc/louvain.hxx:1220), read with the
+      // same synchronisation that ends the run
+      launch_count_flags(W.vaff.p, S, g->ctr.p, s);
+      LVG_CUDA(cudaMemcpyAsync(g->hctr.p, g->ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+    }
     LVG_CUDA(cudaStreamSynchronize(s));
+    if (r == rep - 1 && g->hctr.p->err) read_counters(g);  // raises the device error
     info.ti += elapsed(e0, e1);
     info.tm += elapsed(e1, e2);
     info.tp += elapsed(e2, ep1 ? ep1 : eend);
@@ -685,8 +693,6 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
     for (auto &pr : ta_ev) info.ta += elapsed(pr.first, pr.second);
     info.t += elapsed(e0, eend);
   }
-  launch_count_flags(W.vaff.p, S, g->ctr.p, s);
-  read_counters(g);
   info.affected = g->hctr.p->affected;
   info.iterations = l;
   info.passes = p;
@@ -1038,12 +1044,14 @@ void init_graph(lvg_graph *g, size_t span, size_t order, size_t X, const uint64_
   b.span = span; b.order = order; b.edges = X;
   b.off = g->off.p; b.deg = g->deg.p; b.key = g->key.p; b.w = g->w.p; b.ex = has_exists ? g->ex.p : nullptr;
   launch_total_weight(g->w.p, g->slots, g->ctr.p, s);
+  launch_count_nonunit(cw, X, g->ctr.p, s);
   DBuf<uint32_t> scratch;
   scratch.ensure(bin_scratch_elems(span + 1, DEFAULT_COLORS_ASYNC));
   compute_bins(g, b, g->deg.p, g->bins.p, scratch.p, DEFAULT_COLORS_ASYNC);  // synchronises
   build_hub_plan(g, b, g->hubplan);
   read_counters(g);
   g->total_weight = g->hctr.p->fp64[0];
+  b.unit = X > 0 && g->hctr.p->nonunit == 0;
 }
 
 // ---------------------------------------------------------------- batch apply
@@ -1192,11 +1200,18 @@ void apply_plan(lvg_graph *g, const PlanCounts &pc) {
   launch_finish_rows(g->off.p, g->deg.p, g->cap.p, g->key.p, g->w.p, rows, nrows, g->u_plan.p, g->u_grow.p,
                      g->u_gpos.p, pool, s);
   g->pool_cursor += GROW;
+  if (b.unit && ni) {  // an insertion of another weight ends the unit-weight fast path
+    LVG_CUDA(cudaMemsetAsync(&g->ctr.p->nonunit, 0, sizeof(unsigned long long), s));
+    launch_count_nonunit(iw, ni, g->ctr.p, s);
+    LVG_CUDA(cudaMemcpyAsync(&g->hctr.p->nonunit, &g->ctr.p->nonunit, sizeof(unsigned long long),
+                             cudaMemcpyDeviceToHost, s));
+  }
   if (ex) {
     launch_count_present(ex, b.span, g->upd.p, s);
     LVG_CUDA(cudaMemcpyAsync(g->hupd.p + UPD_ORDER, g->upd.p + UPD_ORDER, 8, cudaMemcpyDeviceToHost, s));
   }
   LVG_CUDA(cudaStreamSynchronize(s));
+  if (b.unit && ni && g->hctr.p->nonunit) b.unit = false;
   b.edges = size_t((long long)b.edges + edge_delta);
   if (ex) b.order = g->hupd.p[UPD_ORDER];
   g->total_weight += wdelta;

@@ -109,6 +109,12 @@ struct Level {
   // graph's first vertex on this level ([graphs+1]); nullptr for one graph.
   const uint32_t *gid = nullptr;
   const uint32_t *gbase = nullptr;
+  // Every edge weight is exactly 1 (set for the uploaded level when it is so;
+  // aggregated levels never): the local-moving kernels then read no weights
+  // and sum a group of equal keys by counting it. Sums of 1.0 are exact
+  // integers in FP32 below 2^24 whatever the order, so the results are those
+  // of the weighted path bit for bit.
+  bool unit = false;
   // Vertices grouped by (colour class, degree bin), ascending id within a
   // group: group (k, b) is bins[bin_start[k*NUM_BINS+b] .. bin_start[k*NUM_BINS+b+1]).
   uint32_t *bins = nullptr;
@@ -140,6 +146,7 @@ struct Counters {
   unsigned int gactive;                       // graph unions: graphs still moving after an iteration
   unsigned int ds_long;                       // delta-screening sources with more than 32 insertions
   uint32_t ds_chunks;                         // delta-screening neighbour chunks of the high-degree vertices
+  unsigned long long nonunit;                 // edge weights other than 1 (count_nonunit)
 };
 
 // Per-graph control of a graph-union run (lvg_static_union), on the device:
@@ -194,6 +201,9 @@ struct MoveArgs {
   const uint8_t *gact = nullptr;
   // resident blocks per SM of the degree 513-8192 kernels (0 = as many as fit)
   int big_cap = 0;
+  // the level's weights are all 1 (Level::unit): the launchers pick the
+  // kernels that do not read them
+  bool unit = false;
 };
 
 // Arguments of the aggregation kernels (inc/louvain.hxx:897-912, 987-992).
@@ -264,6 +274,8 @@ void launch_fill_u8(uint8_t *p, uint8_t v, size_t n, cudaStream_t s);
 void launch_fill_f32(float *p, size_t n, float v, cudaStream_t s);
 void launch_init_static(const Level &g, uint32_t *ucom, tot_t *utot, tot_t *ctot, cudaStream_t s);
 void launch_total_weight(const float *w, size_t n, Counters *ctr, cudaStream_t s);  // -> ctr->fp64[0]
+// ctr->nonunit += the count of w[0..n) other than 1.0f.
+void launch_count_nonunit(const float *w, size_t n, Counters *ctr, cudaStream_t s);
 // louvainVertexWeightsOmpW / louvainCommunityWeightsOmpW in FP64 (the C-ABI utilities).
 void launch_vertex_weights_f64(const Level &g, double *vtot, cudaStream_t s);
 void launch_community_weights_f64(const uint32_t *q, const double *vtot, size_t n, double *ctot, cudaStream_t s);
@@ -458,7 +470,7 @@ void launch_move_small(int lo, int hi, bool sync, const MoveArgs &a, const Small
 int device_sms();
 // Grid of the local-moving kernel of a large-degree bin (9, 10; 11 = the hub
 // merge) for `count` vertices: the size of its per-block global fallback.
-int move_grid_blocks(int bin, bool sync, size_t count, int big_cap = 0);
+int move_grid_blocks(int bin, bool sync, bool unit, size_t count, int big_cap = 0);
 
 
 // ---------------------------------------------------------------- graph unions (lvg_union.cu)

@@ -68,6 +68,14 @@ __global__ void init_static_kernel(const uint64_t *off, const uint32_t *deg, con
   }
 }
 
+__global__ void count_nonunit_kernel(const float *w, size_t m, unsigned long long *dst) {
+  unsigned long long c = 0;
+  GRID_STRIDE(i, m) c += w[i] != 1.0f;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(dst, c);
+}
+
 __global__ void total_weight_kernel(const float *w, size_t m, double *dst) {
   double s = 0;
   GRID_STRIDE(i, m) s += (double)w[i];
@@ -881,6 +889,12 @@ void launch_community_weights_f64(const uint32_t *q, const double *vtot, size_t 
   LVG_CUDA(cudaMemsetAsync(ctot, 0, n * sizeof(double), s));
   if (!n) return;
   community_weights_f64_kernel<<<grid_for(n, 256), 256, 0, s>>>(q, vtot, n, ctot);
+  LVG_CHECK_LAUNCH();
+}
+
+void launch_count_nonunit(const float *w, size_t n, Counters *ctr, cudaStream_t s) {
+  if (!n) return;
+  count_nonunit_kernel<<<grid_for(n, 256), 256, 0, s>>>(w, n, &ctr->nonunit);
   LVG_CHECK_LAUNCH();
 }
 

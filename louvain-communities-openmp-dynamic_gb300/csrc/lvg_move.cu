@@ -116,23 +116,35 @@ __device__ __forceinline__ void flush_counters(Counters *ctr, int bin, unsigned 
 // (c, w) pair (c == EMPTY: nothing). Lanes holding the same key are combined
 // (weights summed in lane order) and only the lowest such lane calls
 // ins(c, sum). Hot keys then cost one table atomic per warp instead of one
-// per lane. Returns false on the lanes whose ins() failed.
-template <class Ins>
+// per lane. With UNIT (every weight 1) the sum is the group's size. Returns
+// false on the lanes whose ins() failed.
+template <bool UNIT, class Ins>
 __device__ __forceinline__ bool warp_insert(uint32_t c, float w, Ins ins) {
   const unsigned grp = __match_any_sync(0xffffffffu, c);
   const int lane = threadIdx.x & 31;
-  const unsigned cnt = c == EMPTY ? 0u : unsigned(__popc(grp));
-  const unsigned most = __reduce_max_sync(0xffffffffu, cnt);
-  float sum = 0.f;
-  unsigned rem = grp;
-  for (unsigned it = 0; it < most; ++it) {
-    const int src = rem ? __ffs(rem) - 1 : lane;
-    rem &= rem - 1u;
-    const float x = __shfl_sync(0xffffffffu, w, src);
-    if (it < cnt) sum += x;
-  }
   const bool leader = (grp & ((1u << lane) - 1u)) == 0u;
-  return !(leader && c != EMPTY) || ins(c, sum);
+  if constexpr (UNIT) {
+    return !(leader && c != EMPTY) || ins(c, float(__popc(grp)));
+  } else {
+    const unsigned cnt = c == EMPTY ? 0u : unsigned(__popc(grp));
+    const unsigned most = __reduce_max_sync(0xffffffffu, cnt);
+    float sum = 0.f;
+    unsigned rem = grp;
+    for (unsigned it = 0; it < most; ++it) {
+      const int src = rem ? __ffs(rem) - 1 : lane;
+      rem &= rem - 1u;
+      const float x = __shfl_sync(0xffffffffu, w, src);
+      if (it < cnt) sum += x;
+    }
+    return !(leader && c != EMPTY) || ins(c, sum);
+  }
+}
+
+// Edge weight i of the level, or 1 for a unit-weight level (not read).
+template <bool UNIT>
+__device__ __forceinline__ float edge_weight(const MoveArgs &a, uint64_t i) {
+  if constexpr (UNIT) return 1.f;
+  else return __ldcs(a.w + i);
 }
 
 // ------------------------------------------------------------ tile / warp kernel
@@ -142,7 +154,7 @@ constexpr int TILE_BLOCK = 256;
 // The tiles of one block work through list[0..count): tile t of the block
 // takes items first + t, first + t + ntiles, ... (ntiles = tiles of all the
 // blocks sharing the list). Counters are flushed for degree bin `bin`.
-template <int T, int C, bool SYNC>
+template <int T, int C, bool SYNC, bool UNIT>
 __device__ __forceinline__ void tile_loop(const MoveArgs &a, const uint32_t *list, uint32_t count, uint32_t first,
                                           uint32_t ntiles, uint8_t *smem, int bin) {
   constexpr int LOGC = ilog2c(C);
@@ -177,7 +189,7 @@ __device__ __forceinline__ void tile_loop(const MoveArgs &a, const uint32_t *lis
       for (int k = 0; k < U; ++k) {
         const uint32_t j = k * 32 + tl;
         nv[k] = j < dg ? __ldcs(a.key + o + j) : u;
-        nw[k] = j < dg ? __ldcs(a.w + o + j) : 0.f;
+        nw[k] = j < dg ? edge_weight<UNIT>(a, o + j) : 0.f;
       }
       for (uint32_t base = 0; base < dg; base += U * 32) {
         uint32_t v[U];
@@ -189,7 +201,7 @@ __device__ __forceinline__ void tile_loop(const MoveArgs &a, const uint32_t *lis
           for (int k = 0; k < U; ++k) {
             const uint32_t j = base + U * 32 + k * 32 + tl;
             nv[k] = j < dg ? __ldcs(a.key + o + j) : u;
-            nw[k] = j < dg ? __ldcs(a.w + o + j) : 0.f;
+            nw[k] = j < dg ? edge_weight<UNIT>(a, o + j) : 0.f;
           }
         }
         uint32_t c[U];
@@ -200,7 +212,8 @@ __device__ __forceinline__ void tile_loop(const MoveArgs &a, const uint32_t *lis
         }
 #pragma unroll
         for (int k = 0; k < U; ++k)
-          ok &= warp_insert(c[k], w[k], [&](uint32_t cc, float ww) { return table_add(keys, vals, LOGC, cc, ww); });
+          ok &= warp_insert<UNIT>(c[k], w[k],
+                                  [&](uint32_t cc, float ww) { return table_add(keys, vals, LOGC, cc, ww); });
       }
     } else
     for (uint32_t j0 = tl; j0 < dg; j0 += U * T) {
@@ -210,7 +223,7 @@ __device__ __forceinline__ void tile_loop(const MoveArgs &a, const uint32_t *lis
       for (int k = 0; k < U; ++k) {
         const uint32_t j = j0 + k * T;
         v[k] = j < dg ? __ldcs(a.key + o + j) : u;
-        w[k] = j < dg ? __ldcs(a.w + o + j) : 0.f;
+        w[k] = j < dg ? edge_weight<UNIT>(a, o + j) : 0.f;
       }
       uint32_t c[U];
 #pragma unroll
@@ -280,12 +293,12 @@ __device__ __forceinline__ void tile_loop(const MoveArgs &a, const uint32_t *lis
 // Tiles with tables of up to 256 slots: registers capped for 8 resident
 // blocks per SM (these kernels wait on gathers; more warps hide more of it —
 // measured on graph unions: the degree 17-64 kernels ran 26 % faster).
-template <int T, int C, bool SYNC>
+template <int T, int C, bool SYNC, bool UNIT>
 __global__ void __launch_bounds__(TILE_BLOCK, (C <= 256 ? 8 : 1)) move_tile_kernel(MoveArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
   constexpr int TPB = TILE_BLOCK / T;
   const uint32_t count = a.count_ptr ? *a.count_ptr : a.count;
-  tile_loop<T, C, SYNC>(a, a.list, count, blockIdx.x * TPB, gridDim.x * TPB, smem, a.bin);
+  tile_loop<T, C, SYNC, UNIT>(a, a.list, count, blockIdx.x * TPB, gridDim.x * TPB, smem, a.bin);
 }
 
 // Several degree bins of one colour class in one launch (bins lo..hi of
@@ -294,7 +307,7 @@ __global__ void __launch_bounds__(TILE_BLOCK, (C <= 256 ? 8 : 1)) move_tile_kern
 // classes' worklists are short (dynamic-frontier and delta-screening passes
 // over the uploaded graph), where a launch per bin would cost more than its
 // work.
-template <int LO, int HI, bool SYNC>
+template <int LO, int HI, bool SYNC, bool UNIT>
 __global__ void __launch_bounds__(TILE_BLOCK, (HI <= 6 ? 8 : 1)) move_small_kernel(MoveArgs a, SmallBins sb) {
   extern __shared__ __align__(16) uint8_t smem[];
   int k = 0;
@@ -306,7 +319,7 @@ __global__ void __launch_bounds__(TILE_BLOCK, (HI <= 6 ? 8 : 1)) move_small_kern
     if (B >= LO && B <= HI) {                                                                            \
       constexpr int J = (B >= LO && B <= HI) ? B - LO : 0;                                              \
       const uint32_t b0 = sb.block_begin[J], nb = sb.block_begin[J + 1] - b0;                           \
-      tile_loop<T, C, SYNC>(a, sb.list[J], *sb.count_ptr[J], (blockIdx.x - b0) * (TILE_BLOCK / T),      \
+      tile_loop<T, C, SYNC, UNIT>(a, sb.list[J], *sb.count_ptr[J], (blockIdx.x - b0) * (TILE_BLOCK / T),\
                             nb * (TILE_BLOCK / T), smem, B);                                             \
     }                                                                                                    \
     break;
@@ -427,7 +440,7 @@ __device__ __forceinline__ void lt_reset(const ListedTable &t, unsigned n) {
 // as soon as an add() fails. Edge ids and weights are read with the
 // streaming hint (evict first): each is read once per scan, while the
 // membership array that every edge gathers from should stay in L2.
-template <int B, class Add>
+template <int B, bool UNIT, class Add>
 __device__ __forceinline__ float scan_edges(const MoveArgs &a, uint32_t u, uint64_t o, uint32_t n, uint32_t d,
                                             Add add) {
   constexpr int U = 4;
@@ -443,7 +456,7 @@ __device__ __forceinline__ float scan_edges(const MoveArgs &a, uint32_t u, uint6
   for (int k = 0; k < U; ++k) {
     const uint32_t j = base0 + k * B + lane;
     nv[k] = j < n ? __ldcs(a.key + o + j) : u;
-    nw[k] = j < n ? __ldcs(a.w + o + j) : 0.f;
+    nw[k] = j < n ? edge_weight<UNIT>(a, o + j) : 0.f;
   }
   for (uint32_t base = base0; base < n; base += U * B) {
     uint32_t v[U];
@@ -456,7 +469,7 @@ __device__ __forceinline__ float scan_edges(const MoveArgs &a, uint32_t u, uint6
       for (int k = 0; k < U; ++k) {
         const uint32_t j = next + k * B + lane;
         nv[k] = j < n ? __ldcs(a.key + o + j) : u;
-        nw[k] = j < n ? __ldcs(a.w + o + j) : 0.f;
+        nw[k] = j < n ? edge_weight<UNIT>(a, o + j) : 0.f;
       }
     }
     uint32_t c[U];
@@ -467,7 +480,7 @@ __device__ __forceinline__ float scan_edges(const MoveArgs &a, uint32_t u, uint6
     }
     bool fail = false;
 #pragma unroll
-    for (int k = 0; k < U; ++k) fail |= !warp_insert(c[k], w[k], add);
+    for (int k = 0; k < U; ++k) fail |= !warp_insert<UNIT>(c[k], w[k], add);
     if (__any_sync(0xffffffffu, fail)) break;
   }
   return kd;
@@ -481,7 +494,7 @@ __device__ __forceinline__ float scan_edges(const MoveArgs &a, uint32_t u, uint6
 // iterations a high-degree vertex's neighbours fall into few communities, so
 // the shared table almost always suffices and the argmax visits only the
 // claimed slots.
-template <int B, int LOGS, bool SYNC>
+template <int B, int LOGS, bool SYNC, bool UNIT>
 __global__ void __launch_bounds__(B) move_big_kernel(MoveArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
   __shared__ float red_g[B / 32];
@@ -516,7 +529,7 @@ __global__ void __launch_bounds__(B) move_big_kernel(MoveArgs a) {
     const uint32_t d = a.vcom[u];
     int lg = min(LOGS, max(1, ceil_log2(2ull * dg)));
     const unsigned limit = (1u << lg) >> 1;
-    float kd = scan_edges<B>(a, u, o, dg, d, [&](uint32_t c, float w) {
+    float kd = scan_edges<B, UNIT>(a, u, o, dg, d, [&](uint32_t c, float w) {
       if (lt_add(t, lg, c, w, limit)) return true;
       s_over = 1;
       return false;
@@ -534,7 +547,7 @@ __global__ void __launch_bounds__(B) move_big_kernel(MoveArgs a) {
       if (!gkeys) ok = false;
       for (uint32_t s2 = threadIdx.x; s2 < gcap; s2 += B) { gkeys[s2] = EMPTY; gvals[s2] = 0.f; }
       __syncthreads();
-      if (gkeys) kd = scan_edges<B>(a, u, o, dg, d, [&](uint32_t c, float w) {
+      if (gkeys) kd = scan_edges<B, UNIT>(a, u, o, dg, d, [&](uint32_t c, float w) {
         ok &= table_add(gkeys, gvals, lg, c, w);
         return true;
       });
@@ -604,7 +617,7 @@ __global__ void __launch_bounds__(B) move_big_kernel(MoveArgs a) {
 // chunk's partial region; a chunk with more distinct communities than the
 // budget writes its raw pairs instead. Edges into the hub's own community are
 // summed separately into hub_kd[u].
-template <int B, int LOGS>
+template <int B, int LOGS, bool UNIT>
 __global__ void __launch_bounds__(B) hub_chunk_kernel(MoveArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
   __shared__ float red_g[B / 32];
@@ -639,7 +652,7 @@ __global__ void __launch_bounds__(B) hub_chunk_kernel(MoveArgs a) {
   for (uint32_t s2 = threadIdx.x; s2 < vcap; s2 += B) { t.keys[s2] = EMPTY; t.vals[s2] = 0.f; }
   __syncthreads();
   const unsigned limit = vcap >> 1;
-  float kd = scan_edges<B>(a, u, o, n, d, [&](uint32_t c, float w) {
+  float kd = scan_edges<B, UNIT>(a, u, o, n, d, [&](uint32_t c, float w) {
     if (lt_add(t, lg, c, w, limit)) return true;
     s_over = 1;
     return false;
@@ -662,7 +675,7 @@ __global__ void __launch_bounds__(B) hub_chunk_kernel(MoveArgs a) {
     for (uint32_t j = threadIdx.x; j < n; j += B) {
       const uint32_t v = __ldcs(a.key + o + j);
       const uint32_t c = v != u ? a.vcom[v] : EMPTY;
-      const float w = __ldcs(a.w + o + j);
+      const float w = edge_weight<UNIT>(a, o + j);
       if (c == d) kd += w;
       if (c != EMPTY && c != d) {
         const uint32_t pos = atomicAdd(&s_cnt, 1u);
@@ -841,12 +854,12 @@ void set_smem(K kernel, size_t bytes) {
   if (bytes > 48 * 1024) LVG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)));
 }
 
-template <int LO, int HI, bool SYNC>
+template <int LO, int HI, bool SYNC, bool UNIT>
 void launch_small(const MoveArgs &a, SmallBins sb, cudaStream_t s) {
   // shared memory of the largest table among the bins (tiles x C x 8 bytes)
   constexpr size_t CMAX = size_t(TILE_BLOCK / (HI <= 1 ? 4 : HI == 2 ? 8 : HI == 3 ? 16 : 32)) *
                           (size_t(4) << HI) * 8;
-  auto k = move_small_kernel<LO, HI, SYNC>;
+  auto k = move_small_kernel<LO, HI, SYNC, UNIT>;
   static bool configured = false;
   if (!configured) { set_smem(k, CMAX); configured = true; }
   const unsigned grid = sb.block_begin[HI - LO + 1];
@@ -855,11 +868,11 @@ void launch_small(const MoveArgs &a, SmallBins sb, cudaStream_t s) {
   LVG_CHECK_LAUNCH();
 }
 
-template <int T, int C, bool SYNC>
+template <int T, int C, bool SYNC, bool UNIT>
 void launch_tile(const MoveArgs &a, cudaStream_t s) {
   constexpr int TPB = TILE_BLOCK / T;
   const size_t smem = size_t(TPB) * C * 8;
-  auto k = move_tile_kernel<T, C, SYNC>;
+  auto k = move_tile_kernel<T, C, SYNC, UNIT>;
   static bool configured = false;
   if (!configured) { set_smem(k, smem); configured = true; }
   size_t want = (a.count + TPB - 1) / TPB;
@@ -887,34 +900,34 @@ unsigned resident_blocks(K kernel, int block, size_t smem) {
   return unsigned(std::max(1, per_sm)) * unsigned(num_sms());
 }
 
-template <int B, int LOGS, bool SYNC>
+template <int B, int LOGS, bool SYNC, bool UNIT>
 unsigned big_grid(size_t count, int cap_per_sm) {
   const size_t smem = (size_t(1) << LOGS) * 10;  // keys, values, claimed list
   static const unsigned resident = [&] {
-    set_smem(move_big_kernel<B, LOGS, SYNC>, smem);
-    return resident_blocks(move_big_kernel<B, LOGS, SYNC>, B, smem);
+    set_smem(move_big_kernel<B, LOGS, SYNC, UNIT>, smem);
+    return resident_blocks(move_big_kernel<B, LOGS, SYNC, UNIT>, B, smem);
   }();
   size_t r = resident;
   if (cap_per_sm > 0) r = std::min(r, size_t(cap_per_sm) * size_t(num_sms()));
   return unsigned(std::min<size_t>(count, r));
 }
 
-template <int B, int LOGS, bool SYNC>
+template <int B, int LOGS, bool SYNC, bool UNIT>
 void launch_big(const MoveArgs &a, cudaStream_t s) {
   const size_t smem = (size_t(1) << LOGS) * 10;
-  const unsigned grid = big_grid<B, LOGS, SYNC>(a.count, a.big_cap);
+  const unsigned grid = big_grid<B, LOGS, SYNC, UNIT>(a.count, a.big_cap);
   if (!grid) return;
-  move_big_kernel<B, LOGS, SYNC><<<grid, B, smem, s>>>(a);
+  move_big_kernel<B, LOGS, SYNC, UNIT><<<grid, B, smem, s>>>(a);
   LVG_CHECK_LAUNCH();
 }
 
-template <bool SYNC>
+template <bool SYNC, bool UNIT>
 void launch_hubs(const MoveArgs &a, cudaStream_t s) {
   const size_t smem1 = (size_t(1) << HUBC_LOGS) * 10, smem2 = (size_t(1) << HUBM_LOGS) * 10;
   const size_t nch = a.hub.chunk_begin[a.color + 1] - a.hub.chunk_begin[a.color];
   const size_t nh = a.hub.hub_begin[a.color + 1] - a.hub.hub_begin[a.color];
   if (!nh) return;
-  auto k1 = hub_chunk_kernel<HUBC_B, HUBC_LOGS>;
+  auto k1 = hub_chunk_kernel<HUBC_B, HUBC_LOGS, UNIT>;
   auto k2 = hub_merge_kernel<HUBM_B, HUBM_LOGS, SYNC>;
   static bool configured = false;
   if (!configured) { set_smem(k1, smem1); set_smem(k2, smem2); configured = true; }
@@ -924,32 +937,39 @@ void launch_hubs(const MoveArgs &a, cudaStream_t s) {
   LVG_CHECK_LAUNCH();
 }
 
-template <bool SYNC>
+template <bool SYNC, bool UNIT>
 void launch_bin(int b, const MoveArgs &a, cudaStream_t s) {
   switch (b) {
-    case 1: launch_tile<4, 8, SYNC>(a, s); break;
-    case 2: launch_tile<8, 16, SYNC>(a, s); break;
-    case 3: launch_tile<16, 32, SYNC>(a, s); break;
-    case 4: launch_tile<32, 64, SYNC>(a, s); break;
-    case 5: launch_tile<32, 128, SYNC>(a, s); break;
-    case 6: launch_tile<32, 256, SYNC>(a, s); break;
-    case 7: launch_tile<32, 512, SYNC>(a, s); break;
-    case 8: launch_tile<32, 1024, SYNC>(a, s); break;
-    case 9: launch_big<BIG9_B, BIG9_LOGS, SYNC>(a, s); break;
-    case 10: launch_big<BIG10_B, BIG10_LOGS, SYNC>(a, s); break;
+    case 1: launch_tile<4, 8, SYNC, UNIT>(a, s); break;
+    case 2: launch_tile<8, 16, SYNC, UNIT>(a, s); break;
+    case 3: launch_tile<16, 32, SYNC, UNIT>(a, s); break;
+    case 4: launch_tile<32, 64, SYNC, UNIT>(a, s); break;
+    case 5: launch_tile<32, 128, SYNC, UNIT>(a, s); break;
+    case 6: launch_tile<32, 256, SYNC, UNIT>(a, s); break;
+    case 7: launch_tile<32, 512, SYNC, UNIT>(a, s); break;
+    case 8: launch_tile<32, 1024, SYNC, UNIT>(a, s); break;
+    case 9: launch_big<BIG9_B, BIG9_LOGS, SYNC, UNIT>(a, s); break;
+    case 10: launch_big<BIG10_B, BIG10_LOGS, SYNC, UNIT>(a, s); break;
     default: break;
   }
 }
 
 }  // namespace
 
-int move_grid_blocks(int bin, bool sync, size_t count, int big_cap) {
-  if (bin == 9)
-    return int(sync ? big_grid<BIG9_B, BIG9_LOGS, true>(count, big_cap)
-                    : big_grid<BIG9_B, BIG9_LOGS, false>(count, big_cap));
-  if (bin == 10)
-    return int(sync ? big_grid<BIG10_B, BIG10_LOGS, true>(count, big_cap)
-                    : big_grid<BIG10_B, BIG10_LOGS, false>(count, big_cap));
+// Blocks of a large-degree launch (the count of its global table regions).
+int move_grid_blocks(int bin, bool sync, bool unit, size_t count, int big_cap) {
+  if (bin == 9) {
+    if (sync) return int(unit ? big_grid<BIG9_B, BIG9_LOGS, true, true>(count, big_cap)
+                              : big_grid<BIG9_B, BIG9_LOGS, true, false>(count, big_cap));
+    return int(unit ? big_grid<BIG9_B, BIG9_LOGS, false, true>(count, big_cap)
+                    : big_grid<BIG9_B, BIG9_LOGS, false, false>(count, big_cap));
+  }
+  if (bin == 10) {
+    if (sync) return int(unit ? big_grid<BIG10_B, BIG10_LOGS, true, true>(count, big_cap)
+                              : big_grid<BIG10_B, BIG10_LOGS, true, false>(count, big_cap));
+    return int(unit ? big_grid<BIG10_B, BIG10_LOGS, false, true>(count, big_cap)
+                    : big_grid<BIG10_B, BIG10_LOGS, false, false>(count, big_cap));
+  }
   return global_table_blocks(count);  // the hub merge
 }
 
@@ -958,26 +978,34 @@ int global_table_blocks(size_t count) {
   return int(count < cap ? count : cap);
 }
 
+// The kernel variants: deterministic or not, unit weights (no weight
+// reads) or not.
 void launch_move_hubs(bool sync, const MoveArgs &a, cudaStream_t s) {
-  if (sync) launch_hubs<true>(a, s);
-  else launch_hubs<false>(a, s);
+  if (sync) { if (a.unit) launch_hubs<true, true>(a, s); else launch_hubs<true, false>(a, s); }
+  else if (a.unit) launch_hubs<false, true>(a, s);
+  else launch_hubs<false, false>(a, s);
 }
 
 int device_sms() { return num_sms(); }
 
 void launch_move_small(int lo, int hi, bool sync, const MoveArgs &a, const SmallBins &sb, cudaStream_t s) {
   if (lo == 1 && hi == 6) {
-    if (sync) launch_small<1, 6, true>(a, sb, s); else launch_small<1, 6, false>(a, sb, s);
+    if (sync) { if (a.unit) launch_small<1, 6, true, true>(a, sb, s); else launch_small<1, 6, true, false>(a, sb, s); }
+    else if (a.unit) launch_small<1, 6, false, true>(a, sb, s);
+    else launch_small<1, 6, false, false>(a, sb, s);
   } else if (lo == 7 && hi == 8) {
-    if (sync) launch_small<7, 8, true>(a, sb, s); else launch_small<7, 8, false>(a, sb, s);
+    if (sync) { if (a.unit) launch_small<7, 8, true, true>(a, sb, s); else launch_small<7, 8, true, false>(a, sb, s); }
+    else if (a.unit) launch_small<7, 8, false, true>(a, sb, s);
+    else launch_small<7, 8, false, false>(a, sb, s);
   } else {
     throw Error(LVG_EINVAL, "launch_move_small: unsupported bin range");
   }
 }
 
 void launch_move_bin(int b, bool sync, const MoveArgs &a, cudaStream_t s) {
-  if (sync) launch_bin<true>(b, a, s);
-  else launch_bin<false>(b, a, s);
+  if (sync) { if (a.unit) launch_bin<true, true>(b, a, s); else launch_bin<true, false>(b, a, s); }
+  else if (a.unit) launch_bin<false, true>(b, a, s);
+  else launch_bin<false, false>(b, a, s);
 }
 
 }  // namespace lvg
