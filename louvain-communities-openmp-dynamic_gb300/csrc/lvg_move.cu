@@ -486,6 +486,65 @@ __device__ __forceinline__ float scan_edges(const MoveArgs &a, uint32_t u, uint6
   return kd;
 }
 
+// The hot keys of a hub chunk (hub_chunk_kernel): up to HOT_KEYS of the
+// communities its first edges fell into most, held in registers by every
+// thread. Unused entries hold NO_KEY, which matches no community and not EMPTY.
+constexpr int HOT_KEYS = 8;
+constexpr uint32_t NO_KEY = 0xFFFFFFFEu;
+
+// scan_edges with a hot set: an edge into the own community or one of the
+// hot communities adds to a lane-private sum (kd / hc[h]); only the others go
+// through the warp-aggregated table insert, and a batch of 32 edges with none
+// left skips it. After static Louvain a hub's neighbours fall into few
+// communities (on R-MAT, the 8 most frequent of a chunk's first 1024 edges
+// take 99 % of the rest), so nearly every edge stays out of shared memory.
+template <int B, bool UNIT, class Add>
+__device__ __forceinline__ float scan_edges_hot(const MoveArgs &a, uint32_t u, uint64_t o, uint32_t n, uint32_t d,
+                                                const uint32_t (&hot)[HOT_KEYS], float (&hc)[HOT_KEYS], Add add) {
+  constexpr int U = 4;
+  const uint32_t lane = threadIdx.x & 31u;
+  float kd = 0.f;
+  uint32_t nv[U];
+  float nw[U];
+  const uint32_t base0 = threadIdx.x & ~31u;
+#pragma unroll
+  for (int k = 0; k < U; ++k) {
+    const uint32_t j = base0 + k * B + lane;
+    nv[k] = j < n ? __ldcs(a.key + o + j) : u;
+    nw[k] = j < n ? edge_weight<UNIT>(a, o + j) : 0.f;
+  }
+  for (uint32_t base = base0; base < n; base += U * B) {
+    uint32_t v[U];
+    float w[U];
+#pragma unroll
+    for (int k = 0; k < U; ++k) { v[k] = nv[k]; w[k] = nw[k]; }
+    const uint32_t next = base + U * B;
+    if (next < n) {
+#pragma unroll
+      for (int k = 0; k < U; ++k) {
+        const uint32_t j = next + k * B + lane;
+        nv[k] = j < n ? __ldcs(a.key + o + j) : u;
+        nw[k] = j < n ? edge_weight<UNIT>(a, o + j) : 0.f;
+      }
+    }
+    uint32_t c[U];
+#pragma unroll
+    for (int k = 0; k < U; ++k) {
+      c[k] = v[k] != u ? a.vcom[v[k]] : EMPTY;
+      if (c[k] == d) { kd += w[k]; c[k] = EMPTY; }
+#pragma unroll
+      for (int h = 0; h < HOT_KEYS; ++h)
+        if (c[k] == hot[h]) { hc[h] += w[k]; c[k] = EMPTY; }
+    }
+    bool fail = false;
+#pragma unroll
+    for (int k = 0; k < U; ++k)
+      if (__any_sync(0xffffffffu, c[k] != EMPTY)) fail |= !warp_insert<UNIT>(c[k], w[k], add);
+    if (__any_sync(0xffffffffu, fail)) break;
+  }
+  return kd;
+}
+
 // One block per vertex (degree 513..8192). The vertex is first aggregated in
 // a listed shared table of 2^LOGS slots (cleared once per block, then reset
 // slot by slot); if it has more distinct neighbour communities than the
@@ -621,8 +680,10 @@ template <int B, int LOGS, bool UNIT>
 __global__ void __launch_bounds__(B) hub_chunk_kernel(MoveArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
   __shared__ float red_g[B / 32];
+  __shared__ float red_h[B / 32][HOT_KEYS];
+  __shared__ uint32_t s_hot[HOT_KEYS];
   __shared__ int s_act;
-  __shared__ unsigned s_used, s_cnt;
+  __shared__ unsigned s_used, s_cnt, s_nhot;
   __shared__ int s_over;
   constexpr uint32_t CS = 1u << LOGS;
   ListedTable t;
@@ -638,6 +699,7 @@ __global__ void __launch_bounds__(B) hub_chunk_kernel(MoveArgs a) {
     s_used = 0;
     s_over = 0;
     s_cnt = 0;
+    s_nhot = 0;
   }
   __syncthreads();
   if (!s_act) {
@@ -652,11 +714,54 @@ __global__ void __launch_bounds__(B) hub_chunk_kernel(MoveArgs a) {
   for (uint32_t s2 = threadIdx.x; s2 < vcap; s2 += B) { t.keys[s2] = EMPTY; t.vals[s2] = 0.f; }
   __syncthreads();
   const unsigned limit = vcap >> 1;
-  float kd = scan_edges<B, UNIT>(a, u, o, n, d, [&](uint32_t c, float w) {
+  auto add = [&](uint32_t c, float w) {
     if (lt_add(t, lg, c, w, limit)) return true;
     s_over = 1;
     return false;
-  });
+  };
+  // the first edges (one batch per thread) through the table, then the hot
+  // set: the keys that took at least 1/64 of their weight
+  const uint32_t nA = min(n, uint32_t(4 * B));
+  float kd = scan_edges<B, UNIT>(a, u, o, nA, d, add);
+  __syncthreads();
+  if (n > nA && !s_over) {
+    const unsigned nl = min(s_used, limit);
+    float part = 0.f;
+    for (unsigned j = threadIdx.x; j < nl; j += B) {
+      const uint32_t s2 = t.list[j];
+      if (s2 != EMPTY) part += t.vals[s2];
+    }
+    const float thr = block_sum<B>(part, red_g) * (1.f / 64.f);
+    for (unsigned j = threadIdx.x; j < nl; j += B) {
+      const uint32_t s2 = t.list[j];
+      if (s2 != EMPTY && t.vals[s2] >= thr) {
+        const unsigned h = atomicAdd(&s_nhot, 1u);
+        if (h < HOT_KEYS) s_hot[h] = t.keys[s2];
+      }
+    }
+    __syncthreads();
+    uint32_t hot[HOT_KEYS];
+    float hc[HOT_KEYS];
+    const unsigned nh = min(s_nhot, unsigned(HOT_KEYS));
+#pragma unroll
+    for (int h = 0; h < HOT_KEYS; ++h) { hot[h] = unsigned(h) < nh ? s_hot[h] : NO_KEY; hc[h] = 0.f; }
+    kd += scan_edges_hot<B, UNIT>(a, u, o + nA, n - nA, d, hot, hc, add);
+    // the hot keys' sums into the table, where the keys are already
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int h = 0; h < HOT_KEYS; ++h) {
+      float x = hc[h];
+#pragma unroll
+      for (int of = 16; of > 0; of >>= 1) x += __shfl_xor_sync(0xffffffffu, x, of);
+      if (lane == 0) red_h[wid][h] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < nh) {
+      float x = 0.f;
+      for (int k = 0; k < B / 32; ++k) x += red_h[k][threadIdx.x];
+      if (x != 0.f) add(s_hot[threadIdx.x], x);
+    }
+  }
   __syncthreads();
   uint32_t *pk = a.part_key + a.hub.chunk_part[ci];
   float *pv = a.part_val + a.hub.chunk_part[ci];
