@@ -76,11 +76,21 @@ void build_hub_plan(lvg_graph *g, Level &lv, HubPlanBuffers &hb) {
   LVG_CUDA(cudaMemcpyAsync(verts.data(), hb.hub_vertex.p, H * 4, cudaMemcpyDeviceToHost, s));
   LVG_CUDA(cudaStreamSynchronize(s));
   std::vector<uint4> chunks;
-  std::vector<uint64_t> parts;
+  std::vector<uint64_t> parts, toff(H);
+  std::vector<uint8_t> tlog(H);
+  std::vector<uint32_t> pages;
   uint64_t part = 0;
   for (int k = 0; k < K; ++k) {
     P.chunk_begin[k] = chunks.size();
+    uint64_t slots = 0;  // the class's spill tables, back to back
+    P.page_begin[k] = pages.size();
     for (size_t h = P.hub_begin[k]; h < P.hub_begin[k + 1]; ++h) {
+      int lg = SPILL_PAGE_LOG;
+      while ((uint64_t(1) << lg) < 2ull * degs[h]) ++lg;
+      tlog[h] = uint8_t(lg);
+      toff[h] = slots;
+      slots += uint64_t(1) << lg;
+      pages.insert(pages.end(), size_t(1) << (lg - SPILL_PAGE_LOG), uint32_t(h));
       first[h] = uint32_t(chunks.size());
       const uint32_t step = g->tuning.hub_chunk;
       for (uint32_t lo = 0; lo < degs[h]; lo += step) {
@@ -89,7 +99,10 @@ void build_hub_plan(lvg_graph *g, Level &lv, HubPlanBuffers &hb) {
       }
       part += degs[h];
     }
+    P.spill_slots = std::max<size_t>(P.spill_slots, slots);
+    P.class_slots[k] = slots;
   }
+  P.page_begin[K] = pages.size();
   P.chunk_begin[K] = chunks.size();
   first[H] = uint32_t(chunks.size());
   P.chunks = chunks.size();
@@ -97,6 +110,12 @@ void build_hub_plan(lvg_graph *g, Level &lv, HubPlanBuffers &hb) {
   hb.hub_first.ensure(H + 1);
   hb.chunk.ensure(chunks.size());
   hb.chunk_part.ensure(chunks.size());
+  hb.hub_toff.ensure(H);
+  hb.hub_tlog.ensure(H);
+  LVG_CUDA(cudaMemcpyAsync(hb.hub_toff.p, toff.data(), H * 8, cudaMemcpyHostToDevice, s));
+  LVG_CUDA(cudaMemcpyAsync(hb.hub_tlog.p, tlog.data(), H, cudaMemcpyHostToDevice, s));
+  hb.page_hub.ensure(pages.size());
+  LVG_CUDA(cudaMemcpyAsync(hb.page_hub.p, pages.data(), pages.size() * 4, cudaMemcpyHostToDevice, s));
   LVG_CUDA(cudaMemcpyAsync(hb.hub_first.p, first.data(), (H + 1) * 4, cudaMemcpyHostToDevice, s));
   LVG_CUDA(cudaMemcpyAsync(hb.chunk.p, chunks.data(), chunks.size() * sizeof(uint4), cudaMemcpyHostToDevice, s));
   LVG_CUDA(cudaMemcpyAsync(hb.chunk_part.p, parts.data(), parts.size() * 8, cudaMemcpyHostToDevice, s));
@@ -105,6 +124,9 @@ void build_hub_plan(lvg_graph *g, Level &lv, HubPlanBuffers &hb) {
   P.hub_first = hb.hub_first.p;
   P.chunk = hb.chunk.p;
   P.chunk_part = hb.chunk_part.p;
+  P.hub_toff = hb.hub_toff.p;
+  P.hub_tlog = hb.hub_tlog.p;
+  P.page_hub = hb.page_hub.p;
 }
 
 // Colour classes of a run: the options' count, else 16 (deterministic), else
@@ -132,6 +154,24 @@ int colors_for(const lvg_options &o, int method, const lvg_tuning &t, size_t bat
 int first_colors(const lvg_options &o, int method) {
   return method == LVG_METHOD_STATIC && !o.deterministic && o.colors <= 0 ? FIRST_COLORS_STATIC : 0;
 }
+
+// Static Louvain's first pass (it starts from singletons, and a hub's
+// neighbours stay in thousands of communities for several iterations): the
+// hubs whose chunks overflow are merged through spill tables
+// (hub_spill_kernel), cleared here and left clear by the merge after each
+// class. Scoped: the flag is dropped however the phase ends.
+struct SpillScope {
+  Workspace &W;
+  SpillScope(lvg_graph *g, const Level &lv, bool on = true) : W(*g->ws) {
+    if (!on || !lv.hub.hubs || !lv.hub.spill_slots) return;
+    W.spill_keys.ensure(lv.hub.spill_slots);
+    W.spill_vals.ensure(lv.hub.spill_slots);
+    LVG_CUDA(cudaMemsetAsync(W.spill_keys.p, 0xFF, lv.hub.spill_slots * sizeof(uint32_t), g->stream));
+    LVG_CUDA(cudaMemsetAsync(W.spill_vals.p, 0, lv.hub.spill_slots * sizeof(float), g->stream));
+    W.spill_now = true;
+  }
+  ~SpillScope() { W.spill_now = false; }
+};
 
 // Degree bins and hub plan of the uploaded level for k colour classes.
 void set_base_colors(lvg_graph *g, int k) {
@@ -253,6 +293,10 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot
         a.part_key = W.part_key.p;
         a.part_val = W.part_val.p;
         a.hub_kd = W.hub_kd.p;
+        a.hub_over = W.hub_over.p;
+        a.spill_keys = W.spill_now ? W.spill_keys.p : nullptr;
+        a.spill_vals = W.spill_now ? W.spill_vals.p : nullptr;
+        a.hub_best = W.hub_best.p;
         launch_move_hubs(sync, a, s);
       } else {
         launch_move_bin(b, sync, a, stream_of(b));
@@ -369,11 +413,18 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const 
     W.chunk_cnt.ensure(lv.hub.chunks);
     W.part_key.ensure(lv.hub.part);
     W.part_val.ensure(lv.hub.part);
+    if (W.hub_over.n < lv.hub.hubs) {  // the merge resets each mark it reads
+      W.hub_over.ensure(lv.hub.hubs);
+      LVG_CUDA(cudaMemsetAsync(W.hub_over.p, 0, W.hub_over.n, s));
+      W.hub_best.ensure(lv.hub.hubs);
+      LVG_CUDA(cudaMemsetAsync(W.hub_best.p, 0, W.hub_best.n * 8, s));
+    }
   }
   const bool base = lv.off == g->base.off;
   IterKey key{};
   if (base) {
-    const void *ps[22] = {lv.off, lv.bins, com, ctot, tot, fa, W.vaff.p, W.mark.p, W.dec.p, W.wl.p, W.wl_count.p,
+    const void *ps[23] = {W.spill_now ? W.spill_keys.p : nullptr, lv.off, lv.bins, com, ctot, tot, fa, W.vaff.p,
+                          W.mark.p, W.dec.p, W.wl.p, W.wl_count.p,
                           W.gkeys.p, W.gvals.p, W.chunk_cnt.p, W.part_key.p, W.part_val.p, W.hub_kd.p, g->ctr.p,
                           g->hctr.p, lv.hub.chunk, lv.hub.hub_vertex, lv.gid};
     std::memcpy(key.p, ps, sizeof(ps));
@@ -639,17 +690,22 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
         // the first iteration over K1 classes (not captured: it runs once per
         // call), the rest of the pass over K
         PhaseEnd e1, e2;
-        move_phase(g, lv, com, ctot, tot, fa, M, kr, 1, E, sync, fused, nullptr, ends, &e1, false);
+        {
+          SpillScope spill(g, lv);
+          move_phase(g, lv, com, ctot, tot, fa, M, kr, 1, E, sync, fused, nullptr, ends, &e1, false);
+        }
         set_base_colors(g, K);
         lv = g->base;
         if (e1.el <= E || L <= 1) {
           m = (e1.l > 1 || e1.el != 0) ? e1.l : 0;
         } else {
+          SpillScope spill(g, lv);
           move_phase(g, lv, com, ctot, tot, fa, M, kr, L - 1, E, sync, fused, nullptr, ends, &e2);
           const int lt = 1 + e2.l;
           m = (lt > 1 || e2.el != 0) ? lt : 0;
         }
       } else {
+        SpillScope spill(g, lv, first && method == LVG_METHOD_STATIC);
         m = move_phase(g, lv, com, ctot, tot, first ? fa : nullptr, M, kr, L, E, sync, fused, nullptr, ends);
       }
       tl_ev.push_back({a0, g->events.record(s)});
@@ -782,11 +838,18 @@ void run_union(lvg_graph *g, const lvg_options &o, RunInfo &info) {
       if (first && K1 && K1 != K) {
         // as run(): the first iteration over K1 classes, the rest over K (each
         // graph's iteration count and stop test carry on on the device)
-        move_phase(g, lv, com, ctot, tot, nullptr, 0.0, 0.f, 1, E, sync, 0, &uc, nullptr, nullptr, false);
+        {
+          SpillScope spill(g, lv);
+          move_phase(g, lv, com, ctot, tot, nullptr, 0.0, 0.f, 1, E, sync, 0, &uc, nullptr, nullptr, false);
+        }
         set_base_colors(g, K);
         lv = g->base;
-        if (g->hctr.p->gactive && L > 1) move_phase(g, lv, com, ctot, tot, nullptr, 0.0, 0.f, L - 1, E, sync, 0, &uc);
+        if (g->hctr.p->gactive && L > 1) {
+          SpillScope spill(g, lv);
+          move_phase(g, lv, com, ctot, tot, nullptr, 0.0, 0.f, L - 1, E, sync, 0, &uc);
+        }
       } else {
+        SpillScope spill(g, lv, first);
         move_phase(g, lv, com, ctot, tot, nullptr, 0.0, 0.f, L, E, sync, 0, &uc);
       }
       tl_ev.push_back({a0, g->events.record(s)});

@@ -24,7 +24,9 @@ extern thread_local std::string g_err;  // the calling thread's last error (lvg_
 struct HubPlanBuffers {
   DBuf<uint32_t> hub_vertex, hub_first, degs;
   DBuf<uint4> chunk;
-  DBuf<uint64_t> chunk_part;
+  DBuf<uint64_t> chunk_part, hub_toff;
+  DBuf<uint8_t> hub_tlog;
+  DBuf<uint32_t> page_hub;
 };
 
 struct LevelBuffers {
@@ -51,6 +53,12 @@ struct Workspace {
   // chunked hub path
   DBuf<uint32_t> chunk_cnt, part_key;
   DBuf<float> part_val, hub_kd;
+  DBuf<uint8_t> hub_over;
+  DBuf<unsigned long long> hub_best;
+  // hub spill tables of static Louvain's first sweep (one colour class's worth)
+  DBuf<uint32_t> spill_keys;
+  DBuf<float> spill_vals;
+  bool spill_now = false;  // the iteration being enqueued spills overflowing hubs
   // chunked aggregation of the largest communities
   DBuf<uint64_t> mpre, agg_toff, agg_tdeg;
   DBuf<uint2> agg_chunk;
@@ -119,7 +127,7 @@ struct DBatch {
 // Everything an iteration's launches depend on; a captured iteration is
 // replayed only while all of it is unchanged.
 struct IterKey {
-  const void *p[22];
+  const void *p[23];
   size_t n[4];
   int k[4];
   float kr;

@@ -92,7 +92,19 @@ struct HubPlan {
   const uint32_t *hub_first = nullptr;          // [hubs+1] first chunk of each hub
   const uint4 *chunk = nullptr;                 // [chunks] (hub, first edge, end edge, hub vertex)
   const uint64_t *chunk_part = nullptr;         // [chunks] offset of the chunk's partial entries
+  // Spill tables (hub_spill_kernel): hub h's table holds 2^hub_tlog[h] >= 2
+  // deg slots at hub_toff[h] within its colour class's region; class k's
+  // tables take class_slots[k] slots, at most spill_slots. Every table is a
+  // whole number of pages of 2^SPILL_PAGE_LOG slots (a hub's degree is above
+  // 8192), and page_hub[page_begin[k] + p] is the hub of class k's page p.
+  const uint64_t *hub_toff = nullptr;           // [hubs]
+  const uint8_t *hub_tlog = nullptr;            // [hubs]
+  const uint32_t *page_hub = nullptr;
+  size_t spill_slots = 0;
+  size_t class_slots[MAX_COLORS] = {};
+  size_t page_begin[MAX_COLORS + 1] = {};
 };
+constexpr int SPILL_PAGE_LOG = 15;
 
 // A graph level in HBM: gapped CSR (row u = key/w[off[u] .. off[u]+deg[u])),
 // the layout of the reference's DiGraphCsr (inc/Graph.hxx:384-640). Level 0 is
@@ -190,6 +202,10 @@ struct MoveArgs {
   uint32_t *part_key;    // [part] partial (community, weight) entries
   float *part_val;
   float *hub_kd;         // [span] weight to the own community, summed over chunks
+  uint8_t *hub_over;     // [hubs] a chunk of the hub handed raw pairs on (reset by the merge)
+  uint32_t *spill_keys;  // the class's hub spill tables (nullptr: the merge merges the partials itself)
+  float *spill_vals;
+  unsigned long long *hub_best;  // [hubs] best (gain bits << 32 | ~community) of a spilled hub
   int color;             // colour class of the launch
   // Graph unions (nullptr for one graph): graph of each vertex, per graph
   // R/(2M), the id of its vertex 0 on this level (never a move target, as

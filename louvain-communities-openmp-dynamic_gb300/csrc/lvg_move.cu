@@ -793,7 +793,110 @@ __global__ void __launch_bounds__(B) hub_chunk_kernel(MoveArgs a) {
   if (threadIdx.x == 0) {
     if (kd != 0.f) atomicAdd(&a.hub_kd[u], kd);
     a.chunk_cnt[ci] = s_cnt;
-    if (s_over) atomicAdd(&a.ctr->hub_chunk_over, 1ull);
+    if (s_over) {
+      atomicAdd(&a.ctr->hub_chunk_over, 1ull);
+      a.hub_over[ch.x] = 1;
+    }
+  }
+}
+
+// Hub path, step 1b (launched when a.spill_keys is set: static Louvain's
+// first sweep, where every neighbour community starts as a singleton and a
+// hub's chunks hand on about as many raw pairs as the hub has edges): one
+// block per chunk of a hub that a chunk marked, inserting the chunk's partial
+// entries into the hub's spill table, so that a large hub is merged by as many
+// blocks as it has chunks instead of by one. The table holds at least twice
+// the hub's degree and its distinct keys are at most the degree, so the
+// probes stay bounded.
+template <int B>
+__global__ void __launch_bounds__(B) hub_spill_kernel(MoveArgs a) {
+  const size_t ci = a.hub.chunk_begin[a.color] + blockIdx.x;
+  const uint4 ch = a.hub.chunk[ci];
+  if (!a.hub_over[ch.x]) return;
+  const uint32_t cnt = a.chunk_cnt[ci];
+  if (cnt == EMPTY) return;
+  const uint64_t p = a.hub.chunk_part[ci];
+  const int lg = a.hub.hub_tlog[ch.x];
+  uint32_t *keys = a.spill_keys + a.hub.hub_toff[ch.x];
+  float *vals = a.spill_vals + a.hub.hub_toff[ch.x];
+  bool ok = true;
+  for (uint32_t q = threadIdx.x; q < cnt; q += B) ok &= table_add(keys, vals, lg, a.part_key[p + q], a.part_val[p + q]);
+  if (!ok) atomicOr(&a.ctr->err, ERR_TABLE_FULL);
+}
+
+// Hub path, step 1c (with step 1b): the best community of every spilled hub
+// of the class, over all of its spill table at once — a thread per slot, so a
+// hub of a million edges is searched by thousands of threads, not one block.
+// Each candidate's gain is packed with its id (gain bits above, ~id below: the
+// larger gain, then the lower id, as `better`; only positive gains, whose bits
+// order as the floats do) and the hub's best taken with a 64-bit atomicMax.
+// The slots are cleared behind the search for the next class.
+__global__ void hub_argmax_kernel(MoveArgs a) {
+  const size_t slots = a.hub.class_slots[a.color];
+  const uint32_t *pages = a.hub.page_hub + a.hub.page_begin[a.color];
+  const int lane = threadIdx.x & 31;
+  for (size_t base = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32 * 32; base < slots;
+       base += size_t(gridDim.x) * blockDim.x) {
+    const uint32_t g = pages[base >> SPILL_PAGE_LOG];  // one hub per warp (pages are whole warps)
+    if (!a.hub_over[g]) continue;
+    const size_t s = base + lane;
+    const uint32_t c = a.spill_keys[s];
+    unsigned long long best = 0;
+    if (c != EMPTY) {
+      const uint32_t u = a.hub.hub_vertex[g];
+      const GraphOf G(a, u);
+      const uint32_t d = a.vcom[u];
+      const double wu = a.vtot[u];
+      const float g2 = gain_of(a.spill_vals[s], a.hub_kd[u], wu, __double2float_rn(wu), a.ctot[c], a.ctot[d], G.kr);
+      if (g2 > 0.f) best = (static_cast<unsigned long long>(__float_as_uint(g2)) << 32) | (0xFFFFFFFFu - c);
+      a.spill_keys[s] = EMPTY;
+      a.spill_vals[s] = 0.f;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long x = __shfl_xor_sync(0xffffffffu, best, o);
+      best = x > best ? x : best;
+    }
+    if (lane == 0 && best) atomicMax(&a.hub_best[g], best);
+  }
+}
+
+// The move of a hub once its best community is known (either merge path):
+// the gain into the iteration's sum, the move (or, deterministic, the
+// decision), the neighbours marked, the hub's own flag cleared.
+template <int B, bool SYNC>
+__device__ __forceinline__ void hub_decide(const MoveArgs &a, const GraphOf &G, uint32_t u, uint32_t d, uint32_t dg,
+                                           double wu, float bg, uint32_t bc, bool over, unsigned long long &fix,
+                                           unsigned long long &nv, unsigned long long &ne, unsigned long long &nm,
+                                           unsigned long long &no) {
+  const bool moved = bc != EMPTY && bc != G.zero;
+  if (threadIdx.x == 0) {
+    a.hub_kd[u] = 0.f;
+    if (bc != EMPTY) add_gain(a, G, fix, bg);
+    if (moved) {
+      if (SYNC) {
+        a.dec[u] = bc;
+      } else {
+        atomicAdd(&a.ctot[d], -wu);
+        atomicAdd(&a.ctot[bc], wu);
+        a.vcom[u] = bc;
+      }
+    }
+  }
+  if (moved) {
+    uint8_t *mk = SYNC ? a.mark : a.vaff;
+    const uint64_t o = a.off[u];
+    for (uint32_t j = threadIdx.x; j < dg; j += B) {
+      const uint32_t v = __ldcs(a.key + o + j);
+      if (v != u) mk[v] = 1;
+    }
+  }
+  if (threadIdx.x == 0) {
+    a.vaff[u] = 0;
+    ++nv;
+    ne += dg;
+    nm += moved;
+    no += over;
   }
 }
 
@@ -839,13 +942,26 @@ __global__ void __launch_bounds__(B) hub_merge_kernel(MoveArgs a) {
     // dropped.
     bool stale = false;
     for (uint32_t c = c0 + threadIdx.x; c < c1; c += B) stale |= a.chunk_cnt[c] == EMPTY;
+    // spilled: the hub's partials went to its spill table (hub_spill_kernel)
+    // and its best community was found there (hub_argmax_kernel)
+    const bool spilled = a.spill_keys && a.hub_over[g];
     if (__syncthreads_or(stale)) {
-      if (threadIdx.x == 0) a.hub_kd[u] = 0.f;
+      if (threadIdx.x == 0) { a.hub_kd[u] = 0.f; a.hub_over[g] = 0; a.hub_best[g] = 0; }
       __syncthreads();
       continue;
     }
     const uint32_t dg = a.deg[u];
     const uint32_t d = a.vcom[u];
+    if (spilled) {
+      const unsigned long long best = a.hub_best[g];
+      const float bg = best ? __uint_as_float(uint32_t(best >> 32)) : 0.f;
+      const uint32_t bc = best ? 0xFFFFFFFFu - uint32_t(best) : EMPTY;
+      __syncthreads();  // every thread has read the best before it is reset
+      hub_decide<B, SYNC>(a, G, u, d, dg, a.vtot[u], bg, bc, false, fix, nv, ne, nm, no);
+      if (threadIdx.x == 0) { a.hub_over[g] = 0; a.hub_best[g] = 0; }
+      __syncthreads();
+      continue;
+    }
     int lg = min(LOGS, max(1, ceil_log2(2ull * dg)));
     const unsigned limit = (1u << lg) >> 1;
     // a warp per chunk: the chunks' partial lists merge in parallel (a hub of
@@ -909,35 +1025,8 @@ __global__ void __launch_bounds__(B) hub_merge_kernel(MoveArgs a) {
     }
     block_argmax<B>(bg, bc, red_g, red_c);
     if (!over) lt_reset<B>(t, nlist);
-    const bool moved = bc != EMPTY && bc != G.zero;
-    if (threadIdx.x == 0) {
-      a.hub_kd[u] = 0.f;
-      if (bc != EMPTY) add_gain(a, G, fix, bg);
-      if (moved) {
-        if (SYNC) {
-          a.dec[u] = bc;
-        } else {
-          atomicAdd(&a.ctot[d], -wu);
-          atomicAdd(&a.ctot[bc], wu);
-          a.vcom[u] = bc;
-        }
-      }
-    }
-    if (moved) {
-      uint8_t *mk = SYNC ? a.mark : a.vaff;
-      const uint64_t o = a.off[u];
-      for (uint32_t j = threadIdx.x; j < dg; j += B) {
-        const uint32_t v = __ldcs(a.key + o + j);
-        if (v != u) mk[v] = 1;
-      }
-    }
-    if (threadIdx.x == 0) {
-      a.vaff[u] = 0;
-      ++nv;
-      ne += dg;
-      nm += moved;
-      no += over;
-    }
+    hub_decide<B, SYNC>(a, G, u, d, dg, wu, bg, bc, over, fix, nv, ne, nm, no);
+    if (threadIdx.x == 0) a.hub_over[g] = 0;
     bad |= !ok;
     __syncthreads();
   }
@@ -996,6 +1085,7 @@ constexpr int BIG9_B = 256, BIG9_LOGS = 11;     // degree 513-2048
 constexpr int BIG10_B = 256, BIG10_LOGS = 11;   // degree 2049-8192
 constexpr int HUBC_B = 256, HUBC_LOGS = 11;     // hub chunks (lvg_tuning::hub_chunk edges each)
 constexpr int HUBM_B = 512, HUBM_LOGS = 13;     // hub merge
+constexpr int HUBS_B = 256;                     // hub spill
 
 // Resident blocks of a large-degree kernel on the whole device, queried once.
 template <class K>
@@ -1038,6 +1128,16 @@ void launch_hubs(const MoveArgs &a, cudaStream_t s) {
   if (!configured) { set_smem(k1, smem1); set_smem(k2, smem2); configured = true; }
   k1<<<unsigned(nch), HUBC_B, smem1, s>>>(a);
   LVG_CHECK_LAUNCH();
+  if (a.spill_keys) {
+    hub_spill_kernel<HUBS_B><<<unsigned(nch), HUBS_B, 0, s>>>(a);
+    LVG_CHECK_LAUNCH();
+    const size_t slots = a.hub.class_slots[a.color];
+    const unsigned grid = unsigned(std::min<size_t>((slots + 255) / 256, size_t(num_sms()) * 8));
+    if (grid) {
+      hub_argmax_kernel<<<grid, 256, 0, s>>>(a);
+      LVG_CHECK_LAUNCH();
+    }
+  }
   k2<<<unsigned(global_table_blocks(nh)), HUBM_B, smem2, s>>>(a);
   LVG_CHECK_LAUNCH();
 }
