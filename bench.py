@@ -47,7 +47,13 @@ for _p in (PKG, ROOT):
 
 METRIC = "DF-Louvain edges/s, HBM GB/s, p99 update latency vs plain GPU at |ΔQ|≤1e-3"
 MOVE_BYTES_PER_EDGE = 12   # neighbour id + weight + neighbour's community
-MOVE_BYTES_PER_VERTEX = 17  # offset + degree + community + weight + flag
+MOVE_BYTES_PER_EDGE_UNIT = 8  # the same when every weight is 1: the kernels read no weights
+MOVE_BYTES_PER_VERTEX = 25  # offset (8) + degree (4) + community (4) + FP64 vertex weight (8) + flag (1)
+
+
+def move_bytes_per_edge(g) -> int:
+    """Algorithmic bytes per scanned edge of the local-moving kernels on host graph g."""
+    return MOVE_BYTES_PER_EDGE_UNIT if len(g.weights) and bool(np.all(g.weights == 1.0)) else MOVE_BYTES_PER_EDGE
 
 
 def parse():
@@ -535,9 +541,9 @@ def run_gpu(args):
             st = Y.stats()
             print(json.dumps({"profiled_df_steps": args.ncu_steps, "last_ms": info["time"],
                               "kernel_launches_per_step": st["kernel_launches"],
-                              "algorithmic_bytes_per_step": MOVE_BYTES_PER_EDGE * st["move_edges"] +
+                              "algorithmic_bytes_per_step": move_bytes_per_edge(y) * st["move_edges"] +
                               MOVE_BYTES_PER_VERTEX * st["move_vertices"],
-                              "hub_algorithmic_bytes_per_step": MOVE_BYTES_PER_EDGE * st["move_bin_edges"][11] +
+                              "hub_algorithmic_bytes_per_step": move_bytes_per_edge(y) * st["move_bin_edges"][11] +
                               MOVE_BYTES_PER_VERTEX * st["move_bin_vertices"][11]}), flush=True)
         dist.close()
         return 0
@@ -606,7 +612,8 @@ def run_gpu(args):
 
     peak, peak_kind = peaks()
     achieved = None
-    alg_per_step = (MOVE_BYTES_PER_EDGE * kedges + MOVE_BYTES_PER_VERTEX * kverts) / args.steps
+    bpe = move_bytes_per_edge(y)
+    alg_per_step = (bpe * kedges + MOVE_BYTES_PER_VERTEX * kverts) / args.steps
     if kms > 0:
         # bytes and time of all local-moving launches of the profiled steps
         achieved = alg_per_step / (kms / args.steps / 1e3) / 1e9
@@ -615,7 +622,7 @@ def run_gpu(args):
     # the dominant kernel: the hub path (hub_chunk_kernel + hub_merge_kernel, the
     # vertices above degree 8192), timed by the events around its two launches
     hub_ms = bin_ms[11] / args.steps
-    hub_alg = (MOVE_BYTES_PER_EDGE * bin_edges[11] + MOVE_BYTES_PER_VERTEX * bin_verts[11]) / args.steps
+    hub_alg = (bpe * bin_edges[11] + MOVE_BYTES_PER_VERTEX * bin_verts[11]) / args.steps
     hub_achieved = hub_alg / (hub_ms / 1e3) / 1e9 if hub_ms > 0 else None
     hub_traffic = int(tr["hub_traffic_ratio"] * hub_alg) if tr and "hub_traffic_ratio" in tr else None
     line = {
@@ -641,7 +648,9 @@ def run_gpu(args):
                                       "times this step's algorithmic bytes; below 1 when the community gathers hit L2")
                                      if hub_traffic else None,
                      "peak_kind": peak_kind,
-                     "algorithmic_bytes": "12 B/scanned edge + 17 B/processed vertex",
+                     "algorithmic_bytes": f"{bpe} B/scanned edge (neighbour id + its community"
+                                          + (", no weight: every weight is 1)" if bpe == 8 else " + weight)")
+                                          + f" + {MOVE_BYTES_PER_VERTEX} B/processed vertex",
                      "all_local_moving": {
                          "achieved": achieved, "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                          "algorithmic_bytes_per_step": int(alg_per_step),

@@ -284,6 +284,7 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot
       a.gvals = need ? W.gvals.p + goff[b] : nullptr;
       a.glog2 = glog2[b];
       a.big_cap = g->tuning.big_blocks_per_sm;
+      a.big_direct = W.first_sweep;
       set_union(a);
       cudaEvent_t b0 = bin_ev ? g->events.record(s) : nullptr;
       if (b == NUM_BINS - 1) {
@@ -692,7 +693,14 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
         PhaseEnd e1, e2;
         {
           SpillScope spill(g, lv);
-          move_phase(g, lv, com, ctot, tot, fa, M, kr, 1, E, sync, fused, nullptr, ends, &e1, false);
+          W.first_sweep = true;
+          try {
+            move_phase(g, lv, com, ctot, tot, fa, M, kr, 1, E, sync, fused, nullptr, ends, &e1, false);
+          } catch (...) {
+            W.first_sweep = false;
+            throw;
+          }
+          W.first_sweep = false;
         }
         set_base_colors(g, K);
         lv = g->base;
@@ -840,7 +848,14 @@ void run_union(lvg_graph *g, const lvg_options &o, RunInfo &info) {
         // graph's iteration count and stop test carry on on the device)
         {
           SpillScope spill(g, lv);
-          move_phase(g, lv, com, ctot, tot, nullptr, 0.0, 0.f, 1, E, sync, 0, &uc, nullptr, nullptr, false);
+          W.first_sweep = true;
+          try {
+            move_phase(g, lv, com, ctot, tot, nullptr, 0.0, 0.f, 1, E, sync, 0, &uc, nullptr, nullptr, false);
+          } catch (...) {
+            W.first_sweep = false;
+            throw;
+          }
+          W.first_sweep = false;
         }
         set_base_colors(g, K);
         lv = g->base;

@@ -59,6 +59,7 @@ struct Workspace {
   DBuf<uint32_t> spill_keys;
   DBuf<float> spill_vals;
   bool spill_now = false;  // the iteration being enqueued spills overflowing hubs
+  bool first_sweep = false;  // static Louvain's first iteration (every neighbour a singleton)
   // chunked aggregation of the largest communities
   DBuf<uint64_t> mpre, agg_toff, agg_tdeg;
   DBuf<uint2> agg_chunk;

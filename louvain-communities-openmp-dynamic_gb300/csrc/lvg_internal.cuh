@@ -202,10 +202,11 @@ struct MoveArgs {
   uint32_t *part_key;    // [part] partial (community, weight) entries
   float *part_val;
   float *hub_kd;         // [span] weight to the own community, summed over chunks
-  uint8_t *hub_over;     // [hubs] a chunk of the hub handed raw pairs on (reset by the merge)
-  uint32_t *spill_keys;  // the class's hub spill tables (nullptr: the merge merges the partials itself)
-  float *spill_vals;
-  unsigned long long *hub_best;  // [hubs] best (gain bits << 32 | ~community) of a spilled hub
+  uint8_t *hub_over = nullptr;  // [hubs] a chunk of the hub handed raw pairs on (reset by the merge)
+  uint32_t *spill_keys = nullptr;  // the class's hub spill tables (nullptr: the merge merges the partials itself)
+  float *spill_vals = nullptr;
+  unsigned long long *hub_best = nullptr;  // [hubs] best (gain bits << 32 | ~community) of a spilled hub
+  bool big_direct = false;  // degree 513-8192 vertices above the shared claim budget go straight to HBM
   int color;             // colour class of the launch
   // Graph unions (nullptr for one graph): graph of each vertex, per graph
   // R/(2M), the id of its vertex 0 on this level (never a move target, as

@@ -588,11 +588,19 @@ __global__ void __launch_bounds__(B) move_big_kernel(MoveArgs a) {
     const uint32_t d = a.vcom[u];
     int lg = min(LOGS, max(1, ceil_log2(2ull * dg)));
     const unsigned limit = (1u << lg) >> 1;
-    float kd = scan_edges<B, UNIT>(a, u, o, dg, d, [&](uint32_t c, float w) {
-      if (lt_add(t, lg, c, w, limit)) return true;
-      s_over = 1;
-      return false;
-    });
+    // static Louvain's first iteration (a.big_direct): the neighbours are
+    // still singletons, so a vertex of more edges than the claim budget would
+    // overflow the shared table: straight to the table in global memory
+    float kd = 0.f;
+    if (a.big_direct && dg > limit) {
+      if (threadIdx.x == 0) s_over = 1;
+    } else {
+      kd = scan_edges<B, UNIT>(a, u, o, dg, d, [&](uint32_t c, float w) {
+        if (lt_add(t, lg, c, w, limit)) return true;
+        s_over = 1;
+        return false;
+      });
+    }
     __syncthreads();
     const unsigned nlist = min(s_used, limit);
     const bool over = s_over;
