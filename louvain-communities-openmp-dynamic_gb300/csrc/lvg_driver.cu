@@ -155,11 +155,12 @@ int first_colors(const lvg_options &o, int method) {
   return method == LVG_METHOD_STATIC && !o.deterministic && o.colors <= 0 ? FIRST_COLORS_STATIC : 0;
 }
 
-// Static Louvain's first pass (it starts from singletons, and a hub's
-// neighbours stay in thousands of communities for several iterations): the
-// hubs whose chunks overflow are merged through spill tables
-// (hub_spill_kernel), cleared here and left clear by the merge after each
-// class. Scoped: the flag is dropped however the phase ends.
+// Static Louvain (it starts from singletons; a hub's neighbours stay in
+// thousands of communities for several iterations, and the super-vertices of
+// the next levels see thousands of neighbour communities too): the hubs whose
+// chunks overflow are merged through spill tables (hub_spill_kernel), cleared
+// here and left clear by the merge after each class. Scoped: the flag is
+// dropped however the phase ends.
 struct SpillScope {
   Workspace &W;
   SpillScope(lvg_graph *g, const Level &lv, bool on = true) : W(*g->ws) {
@@ -713,7 +714,7 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
           m = (lt > 1 || e2.el != 0) ? lt : 0;
         }
       } else {
-        SpillScope spill(g, lv, first && method == LVG_METHOD_STATIC);
+        SpillScope spill(g, lv, method == LVG_METHOD_STATIC);
         m = move_phase(g, lv, com, ctot, tot, first ? fa : nullptr, M, kr, L, E, sync, fused, nullptr, ends);
       }
       tl_ev.push_back({a0, g->events.record(s)});
@@ -864,7 +865,7 @@ void run_union(lvg_graph *g, const lvg_options &o, RunInfo &info) {
           move_phase(g, lv, com, ctot, tot, nullptr, 0.0, 0.f, L - 1, E, sync, 0, &uc);
         }
       } else {
-        SpillScope spill(g, lv, first);
+        SpillScope spill(g, lv);
         move_phase(g, lv, com, ctot, tot, nullptr, 0.0, 0.f, L, E, sync, 0, &uc);
       }
       tl_ev.push_back({a0, g->events.record(s)});
