@@ -618,7 +618,7 @@ def run_gpu(args):
         # bytes and time of all local-moving launches of the profiled steps
         achieved = alg_per_step / (kms / args.steps / 1e3) / 1e9
     tr = traffic_per_launch()
-    traffic = int(tr["traffic_ratio"] * alg_per_step) if tr else None
+    traffic = int(tr["traffic_ratio"] * alg_per_step) if tr and "traffic_ratio" in tr else None
     # the dominant kernel: the hub path (hub_chunk_kernel + hub_merge_kernel, the
     # vertices above degree 8192), timed by the events around its two launches
     hub_ms = bin_ms[11] / args.steps
@@ -645,7 +645,8 @@ def run_gpu(args):
                      "algorithmic_bytes_per_step": int(hub_alg), "ms_per_step": hub_ms,
                      "traffic_note": ("DRAM bytes of the hub pair per step: their ratio to its algorithmic bytes in "
                                       "an ncu capture (" + tr.get("measured_on", "") + "; profiles/move_traffic.json) "
-                                      "times this step's algorithmic bytes; below 1 when the community gathers hit L2")
+                                      "times this step's algorithmic bytes: a lower bound at scale 24, where the "
+                                      "community gathers hit L2 less often than at scale 22")
                                      if hub_traffic else None,
                      "peak_kind": peak_kind,
                      "algorithmic_bytes": f"{bpe} B/scanned edge (neighbour id + its community"
