@@ -559,13 +559,15 @@ def run_gpu(args):
     # warm-up + timed DF steps (inputs resident in HBM; device time by CUDA events)
     for _ in range(args.warmup):
         lvg.run_resident(Y, lvg.METHOD_FRONTIER, db, st_prior, st_out, o)
-    step_ms, launches = [], 0
+    step_ms, launches, syncs = [], 0, 0
     dist.barrier()
     with Clocks(local) as clk:
         for _ in range(args.steps):
             info = lvg.run_resident(Y, lvg.METHOD_FRONTIER, db, st_prior, st_out, o)
             step_ms.append(info["time"])
-            launches += Y.stats()["kernel_launches"]
+            st = Y.stats()
+            launches += st["kernel_launches"]
+            syncs += st["host_syncs"]
     dist.barrier()
     # the same steps again with per-launch events around the local-moving kernels (roofline)
     Y.set_profiling(True)
@@ -637,6 +639,8 @@ def run_gpu(args):
         "tuning": dict(tuning, by="--set-tuning" if args.set_tuning else "lvg_autotune" if not args.no_tune else "defaults",
                        seconds=round(tune_s, 2)),
         "gpu_launches": launches,
+        "host_syncs_per_step": syncs / args.steps,
+        "df_passes_iterations": [info["passes"], info["iterations"]],
         "roofline": {"bound": "hbm", "achieved": hub_achieved, "peak": peak, "unit": "GB/s",
                      "frac": (hub_achieved / peak) if hub_achieved else None,
                      "traffic": hub_traffic,

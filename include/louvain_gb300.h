@@ -407,6 +407,10 @@ typedef struct lvg_stats {
    * hub merges), and hub chunks that handed their raw pairs on. */
   uint64_t move_bin_overflow[12];
   uint64_t hub_chunk_overflow;
+  /* Times the last call waited for the GPU (stream synchronisations of the
+   * run: with the local-moving phase replayed as one graph, a dynamic-frontier
+   * run that ends after one pass waits once). */
+  uint64_t host_syncs;
 } lvg_stats;
 /* Enable (1) or disable (0) per-launch event timing for calls on g. */
 int lvg_set_profiling(lvg_graph *g, int enable);

@@ -79,10 +79,7 @@ void apply_tuning(lvg_graph *g, const lvg_tuning &t) {
   const bool chunks = t.hub_chunk != g->tuning.hub_chunk;
   g->tuning = t;
   if (chunks) build_hub_plan(g, g->base, g->hubplan);
-  if (g->iter_exec) {
-    cudaGraphExecDestroy(g->iter_exec);
-    g->iter_exec = nullptr;
-  }
+  drop_graphs(g);
 }
 
 // Modularity of a membership already in HBM (the uploaded level's graph).
@@ -492,10 +489,7 @@ int lvg_graph_trim(lvg_graph *g, int level) {
   return lvg::guarded([&] {
     LVG_CUDA(cudaSetDevice(g->device));
     LVG_CUDA(cudaStreamSynchronize(g->stream));
-    if (g->iter_exec) {  // the captured iteration refers to the buffers released below
-      cudaGraphExecDestroy(g->iter_exec);
-      g->iter_exec = nullptr;
-    }
+    lvg::drop_graphs(g);  // the captured iteration refers to the buffers released below
     if (g->ws) {
       lvg::Workspace &W = *g->ws;
       W.gkeys.release(); W.gvals.release();

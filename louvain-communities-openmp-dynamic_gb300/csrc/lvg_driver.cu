@@ -18,6 +18,23 @@ int fail(int code, const std::string &msg) {
   return code;
 }
 
+// Wait for the graph's stream, counted in the call's statistics (host_syncs).
+void host_sync(lvg_graph *g) {
+  ++g->stats.host_syncs;
+  LVG_CUDA(cudaStreamSynchronize(g->stream));
+}
+
+void drop_graphs(lvg_graph *g) {
+  if (g->iter_exec) {
+    cudaGraphExecDestroy(g->iter_exec);
+    g->iter_exec = nullptr;
+  }
+  if (g->phase_exec) {
+    cudaGraphExecDestroy(g->phase_exec);
+    g->phase_exec = nullptr;
+  }
+}
+
 void ensure_ws(lvg_graph *g) {
   if (!g->ws) {
     g->ws = std::make_unique<Workspace>();
@@ -27,11 +44,11 @@ void ensure_ws(lvg_graph *g) {
 
 void read_counters(lvg_graph *g) {
   LVG_CUDA(cudaMemcpyAsync(g->hctr.p, g->ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, g->stream));
-  LVG_CUDA(cudaStreamSynchronize(g->stream));
+  host_sync(g);
   if (g->hctr.p->err) {
     unsigned e = g->hctr.p->err;
     LVG_CUDA(cudaMemsetAsync(&g->ctr.p->err, 0, sizeof(unsigned), g->stream));
-    if (e & ERR_BAD_ID) throw Error(LVG_EINVAL, "prior membership id >= span");
+    if (e & ERR_BAD_ID) throw Error(LVG_EINVAL, "prior membership id >= span (err=" + std::to_string(e) + ")");
     if (e & ERR_WORKLIST) throw Error(LVG_ECUDA, "worklist append outside its degree bin (stale degree bins)");
     throw Error(LVG_ETIMEOUT, "device hash table overflow guard tripped (err=" + std::to_string(e) + ")");
   }
@@ -42,6 +59,7 @@ void compute_bins(lvg_graph *g, Level &lv, const uint32_t *deg, uint32_t *list, 
   lv.colors = colors;
   bin_items_u32(deg, lv.ex, lv.span, colors, list, lv.bin_start, lv.bin_maxdeg, scratch, g->hbins.p, g->stream,
                 lv.gid, lv.gbase);
+  ++g->stats.host_syncs;  // the bin counts are read back
   lv.bins = list;
 }
 
@@ -74,7 +92,7 @@ void build_hub_plan(lvg_graph *g, Level &lv, HubPlanBuffers &hb) {
   std::vector<uint32_t> degs(H), verts(H), first(H + 1);
   LVG_CUDA(cudaMemcpyAsync(degs.data(), hb.degs.p, H * 4, cudaMemcpyDeviceToHost, s));
   LVG_CUDA(cudaMemcpyAsync(verts.data(), hb.hub_vertex.p, H * 4, cudaMemcpyDeviceToHost, s));
-  LVG_CUDA(cudaStreamSynchronize(s));
+  host_sync(g);
   std::vector<uint4> chunks;
   std::vector<uint64_t> parts, toff(H);
   std::vector<uint8_t> tlog(H);
@@ -119,7 +137,7 @@ void build_hub_plan(lvg_graph *g, Level &lv, HubPlanBuffers &hb) {
   LVG_CUDA(cudaMemcpyAsync(hb.hub_first.p, first.data(), (H + 1) * 4, cudaMemcpyHostToDevice, s));
   LVG_CUDA(cudaMemcpyAsync(hb.chunk.p, chunks.data(), chunks.size() * sizeof(uint4), cudaMemcpyHostToDevice, s));
   LVG_CUDA(cudaMemcpyAsync(hb.chunk_part.p, parts.data(), parts.size() * 8, cudaMemcpyHostToDevice, s));
-  LVG_CUDA(cudaStreamSynchronize(s));
+  host_sync(g);
   P.hub_vertex = hb.hub_vertex.p;
   P.hub_first = hb.hub_first.p;
   P.chunk = hb.chunk.p;
@@ -209,7 +227,7 @@ int bin_stream(int b) { return b <= 4 ? 0 : b <= 8 ? 1 : b == 9 ? 2 : b == 10 ? 
 void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const tot_t *tot,
                        const uint8_t *fa, float kr, bool sync, int fused, const int *glog2, const size_t *goff,
                        size_t need, std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> *bin_ev,
-                       const UnionCall *uc) {
+                       const UnionCall *uc, bool read_back = true) {
   auto set_union = [&](MoveArgs &a) {
     if (!uc) return;
     a.gid = lv.gid; a.gkr = uc->kr; a.gzero = lv.gbase; a.gfix = uc->fix; a.gact = uc->gact;
@@ -318,7 +336,62 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot
     }
   }
   if (uc) launch_iter_control(uc->n, uc->ctl, uc->gact, uc->fix, uc->M, uc->E, uc->L, g->ctr.p, s);
-  LVG_CUDA(cudaMemcpyAsync(g->hctr.p, g->ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+  if (read_back) LVG_CUDA(cudaMemcpyAsync(g->hctr.p, g->ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+}
+
+// The whole local-moving phase of the uploaded level as one graph: a
+// conditional while node whose body is one iteration (as enqueue_iteration
+// issues it) followed by iter_end_kernel, which evaluates the reference's
+// stop test (el <= E, or L iterations; inc/louvain.hxx:588-609) on the device
+// and sets the node's condition. The loop is bounded by L whatever the
+// kernels compute. A phase is then one graph launch and one synchronisation,
+// instead of one of each per iteration. Any failure to build it leaves the
+// per-iteration path in place for this handle.
+void capture_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const tot_t *tot, const uint8_t *fa,
+                   float kr, bool sync, int fused, const int *glog2, const size_t *goff, size_t need,
+                   const IterKey &key) {
+  cudaStream_t s = g->stream;
+  if (g->phase_exec) {
+    cudaGraphExecDestroy(g->phase_exec);
+    g->phase_exec = nullptr;
+  }
+  const unsigned long long l0 = launch_counter();
+  const unsigned long long m0 = g->stats.move_launches;
+  cudaGraph_t graph = nullptr;
+  bool fine = cudaGraphCreate(&graph, 0) == cudaSuccess;
+  cudaGraphConditionalHandle h{};
+  cudaGraphNodeParams cp{};
+  cudaGraphNode_t node = nullptr;
+  if (fine) fine = cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+  if (fine) {
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    fine = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp) == cudaSuccess;
+  }
+  if (fine) fine = cudaStreamBeginCaptureToGraph(s, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                                 cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+  if (fine) {
+    try {
+      enqueue_iteration(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, goff, need, nullptr, nullptr, false);
+      launch_iter_end(g->ctr.p, key.M, key.E, key.L, h, s);
+    } catch (const Error &) {
+      fine = false;
+    }
+    cudaGraph_t body = nullptr;
+    fine = cudaStreamEndCapture(s, &body) == cudaSuccess && fine;
+  }
+  launch_counter() = l0;
+  g->stats.move_launches = m0;
+  if (!fine || cudaGraphInstantiate(&g->phase_exec, graph, 0) != cudaSuccess) {
+    cudaGetLastError();
+    g->phase_exec = nullptr;
+    g->no_phase_graphs = true;
+  } else {
+    g->phase_key = key;
+  }
+  if (graph) cudaGraphDestroy(graph);
 }
 
 // Capture one iteration of the uploaded level into a CUDA graph (after an
@@ -373,9 +446,14 @@ struct PhaseEnd {
   double el = 0;
 };
 
+// tail (optional): work to enqueue after the phase and before its one
+// synchronisation when the phase runs as one graph; *tail_done tells whether
+// it was.
 int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const tot_t *tot, const uint8_t *fa,
                double M, float kr, int L, double E, bool sync, int fused, const UnionCall *uc = nullptr,
-               const DBatch *endpoints = nullptr, PhaseEnd *end = nullptr, bool capture = true) {
+               const DBatch *endpoints = nullptr, PhaseEnd *end = nullptr, bool capture = true,
+               const std::function<void()> *tail = nullptr, bool *tail_done = nullptr) {
+  if (tail_done) *tail_done = false;
   Workspace &W = *g->ws;
   cudaStream_t s = g->stream;
   const int K = lv.colors;
@@ -425,20 +503,41 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const 
   const bool base = lv.off == g->base.off;
   IterKey key{};
   if (base) {
-    const void *ps[23] = {W.spill_now ? W.spill_keys.p : nullptr, lv.off, lv.bins, com, ctot, tot, fa, W.vaff.p,
+    const void *ps[27] = {W.spill_now ? W.spill_keys.p : nullptr, lv.off, lv.bins, com, ctot, tot, fa, W.vaff.p,
                           W.mark.p, W.dec.p, W.wl.p, W.wl_count.p,
                           W.gkeys.p, W.gvals.p, W.chunk_cnt.p, W.part_key.p, W.part_val.p, W.hub_kd.p, g->ctr.p,
-                          g->hctr.p, lv.hub.chunk, lv.hub.hub_vertex, lv.gid};
+                          g->hctr.p, lv.hub.chunk, lv.hub.hub_vertex, lv.gid,
+                          W.spill_now ? W.spill_vals.p : nullptr, W.hub_over.p, W.hub_best.p, lv.deg};
     std::memcpy(key.p, ps, sizeof(ps));
     key.n[0] = lv.span; key.n[1] = need; key.n[2] = lv.hub.chunks; key.n[3] = lv.bin_start[K * NUM_BINS];
     key.k[0] = K; key.k[1] = sync | int(lv.unit) << 1; key.k[2] = glog2[9] | glog2[10] << 8 | glog2[11] << 16;
     key.k[3] = fused;
     key.kr = kr;
-    key.E = uc ? E : 0.0;
+    key.E = E;
+    key.M = M;
+    key.L = L;
   }
   const bool graphs = base && capture && !g->profiling && !g->no_graphs;
+  const bool phase_graphs = graphs && !uc && !g->no_phase_graphs && L > 0;
   int l = 0;
   double el = 0;
+  if (phase_graphs && g->phase_exec && g->phase_key == key) {
+    LVG_CUDA(cudaMemsetAsync(&g->ctr.p->dev_iters, 0, sizeof(unsigned int), s));
+    LVG_CUDA(cudaGraphLaunch(g->phase_exec, s));
+    LVG_CUDA(cudaMemcpyAsync(g->hctr.p, g->ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+    if (tail) {
+      (*tail)();
+      if (tail_done) *tail_done = true;
+    }
+    host_sync(g);
+    if (g->hctr.p->err) read_counters(g);  // raises the device error
+    l = int(g->hctr.p->dev_iters);
+    el = g->hctr.p->dev_el;
+    launch_counter() += (g->iter_nodes + 1) * unsigned(l);
+    g->stats.move_launches += g->iter_moves * unsigned(l);
+    if (end) { end->l = l; end->el = el; }
+    return (l > 1 || el != 0) ? l : 0;
+  }
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> bin_ev;
   while (l < L) {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -454,7 +553,7 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const 
                         g->profiling ? &bin_ev : nullptr, uc);
       if (g->profiling) e1 = g->events.record(s);
     }
-    LVG_CUDA(cudaStreamSynchronize(s));
+    host_sync(g);
     if (g->hctr.p->err) read_counters(g);  // raises the device error
     if (g->profiling) {
       g->stats.move_kernel_ms += elapsed(e0, e1);
@@ -470,6 +569,10 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const 
     el = double(g->hctr.p->el_fix) / GAIN_FIX / M;
     if (el <= E) break;
   }
+  // next time, the whole phase as one graph (every kernel's attributes are set
+  // by now)
+  if (phase_graphs && !(g->phase_exec && g->phase_key == key))
+    capture_phase(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, goff, need, key);
   if (end) { end->l = l; end->el = el; }
   return (l > 1 || el != 0) ? l : 0;
 }
@@ -541,7 +644,7 @@ Level aggregate(lvg_graph *g, const Level &lv, const uint32_t *com, size_t CN, i
     launch_comm_tdeg(list, n11, nl.off, W.agg_tdeg.p, s);
     std::vector<uint64_t> tdeg(n11);
     LVG_CUDA(cudaMemcpyAsync(tdeg.data(), W.agg_tdeg.p, n11 * 8, cudaMemcpyDeviceToHost, s));
-    LVG_CUDA(cudaStreamSynchronize(s));
+    host_sync(g);
     W.mpre.ensure(size_t(members) + 1);
     launch_member_degrees(W.cmem.p, lv.deg, members, W.mpre.p, s);
     exclusive_scan_u64(W.mpre.p, W.mpre.p, members, W.mpre.p + members, W.scan64.p, s);
@@ -578,7 +681,7 @@ Level aggregate(lvg_graph *g, const Level &lv, const uint32_t *com, size_t CN, i
     AggChunks ch{W.agg_chunk.p, list, W.agg_toff.p, W.agg_tlog.p, W.mpre.p, W.agg_gk.p, W.agg_gv.p, uint32_t(n11)};
     launch_aggregate_chunks(a, ch, chunks.size(), slots, s);
     g->stats.aggregate_launches += 2;
-    LVG_CUDA(cudaStreamSynchronize(s));  // the host vectors above are freed next
+    host_sync(g);  // the host vectors above are freed next
   }
   if (g->profiling) {
     e1 = g->events.record(s);
@@ -673,6 +776,7 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
     uint32_t *com = ucom;
     const tot_t *tot = utot;
     int which = 0;
+    bool ended_by_tail = false;
     for (l = 0, p = 0; M > 0 && P > 0;) {
       if (p == 1) ep1 = g->events.record(s);
       const bool first = p == 0;
@@ -687,6 +791,16 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
                         : method == LVG_METHOD_DELTA     ? 8
                                                          : 0;
       const DBatch *ends = first && method == LVG_METHOD_FRONTIER ? &b : nullptr;
+      // the end of the run, enqueued ahead of the first pass's one
+      // synchronisation: if the run ends after this pass (as a frontier run
+      // on a small batch does), it needs no other synchronisation
+      cudaEvent_t tail_ev = nullptr;
+      const std::function<void()> tail = [&] {
+        tail_ev = g->events.record(s);
+        launch_count_flags(W.vaff.p, S, g->ctr.p, s);
+        LVG_CUDA(cudaMemcpyAsync(g->hctr.p, g->ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+      };
+      bool tail_done = false;
       int m;
       if (first && K1 && K1 != K) {
         // the first iteration over K1 classes (not captured: it runs once per
@@ -715,12 +829,16 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
         }
       } else {
         SpillScope spill(g, lv, method == LVG_METHOD_STATIC);
-        m = move_phase(g, lv, com, ctot, tot, first ? fa : nullptr, M, kr, L, E, sync, fused, nullptr, ends);
+        m = move_phase(g, lv, com, ctot, tot, first ? fa : nullptr, M, kr, L, E, sync, fused, nullptr, ends,
+                       nullptr, true, first && r == rep - 1 ? &tail : nullptr, &tail_done);
       }
-      tl_ev.push_back({a0, g->events.record(s)});
+      tl_ev.push_back({a0, tail_done ? tail_ev : g->events.record(s)});
       l += std::max(m, 1);
       ++p;
-      if (m <= 1 || p >= P) break;
+      if (m <= 1 || p >= P) {
+        ended_by_tail = tail_done;
+        break;
+      }
       const size_t GN = first ? g->base.order : lv.span;
       LVG_CUDA(cudaMemsetAsync(W.cext.p, 0, (lv.span + 1) * sizeof(uint32_t), s));
       launch_community_flags(lv, com, W.cext.p, s);
@@ -742,14 +860,16 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
       E /= o.toleranceDrop;
     }
     if (p > 1) launch_lookup(ucom, W.vcom.p, S, s);
-    cudaEvent_t eend = g->events.record(s);
-    if (r == rep - 1) {
-      // the residual affected count (inc/louvain.hxx:1220), read with the
-      // same synchronisation that ends the run
-      launch_count_flags(W.vaff.p, S, g->ctr.p, s);
-      LVG_CUDA(cudaMemcpyAsync(g->hctr.p, g->ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+    cudaEvent_t eend = ended_by_tail ? tl_ev.back().second : g->events.record(s);
+    if (!ended_by_tail) {
+      if (r == rep - 1) {
+        // the residual affected count (inc/louvain.hxx:1220), read with the
+        // same synchronisation that ends the run
+        launch_count_flags(W.vaff.p, S, g->ctr.p, s);
+        LVG_CUDA(cudaMemcpyAsync(g->hctr.p, g->ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+      }
+      host_sync(g);
     }
-    LVG_CUDA(cudaStreamSynchronize(s));
     if (r == rep - 1 && g->hctr.p->err) read_counters(g);  // raises the device error
     info.ti += elapsed(e0, e1);
     info.tm += elapsed(e1, e2);
@@ -801,7 +921,7 @@ void run_union(lvg_graph *g, const lvg_options &o, RunInfo &info) {
     for (size_t i = 0; i < n; ++i) kr[i] = U.M[i] > 0 ? float(R / (2.0 * U.M[i])) : 0.f;
     U.kr.ensure(n);
     LVG_CUDA(cudaMemcpyAsync(U.kr.p, kr.data(), n * sizeof(float), cudaMemcpyHostToDevice, s));
-    LVG_CUDA(cudaStreamSynchronize(s));
+    host_sync(g);
   }
   U.fix.ensure(n); U.ctl.ensure(n); U.hctl.ensure(n); U.gact.ensure(n);
   U.gid[0].ensure(S); U.gid[1].ensure(S); U.gbase[0].ensure(n + 1); U.gbase[1].ensure(n + 1);
@@ -901,7 +1021,7 @@ void run_union(lvg_graph *g, const lvg_options &o, RunInfo &info) {
       E /= o.toleranceDrop;
     }
     cudaEvent_t eend = g->events.record(s);
-    LVG_CUDA(cudaStreamSynchronize(s));
+    host_sync(g);
     info.ti += elapsed(e0, e1);
     info.tm += elapsed(e1, e2);
     info.tp += elapsed(e2, ep1 ? ep1 : eend);
@@ -1295,10 +1415,7 @@ void apply_plan(lvg_graph *g, const PlanCounts &pc) {
   if (ex) b.order = g->hupd.p[UPD_ORDER];
   g->total_weight += wdelta;
   // degrees changed: new bins and hub plan; the captured iteration is stale
-  if (g->iter_exec) {
-    cudaGraphExecDestroy(g->iter_exec);
-    g->iter_exec = nullptr;
-  }
+  drop_graphs(g);
   ensure_ws(g);
   // the aggregation levels' edge buffers grow with 1/16 headroom: sized to the
   // exact count, a stream of insertion batches reallocated them (GBs freed

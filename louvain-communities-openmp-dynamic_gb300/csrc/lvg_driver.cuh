@@ -128,14 +128,16 @@ struct DBatch {
 // Everything an iteration's launches depend on; a captured iteration is
 // replayed only while all of it is unchanged.
 struct IterKey {
-  const void *p[23];
+  const void *p[27];
   size_t n[4];
   int k[4];
   float kr;
-  double E;  // graph unions: the tolerance the per-graph stop test uses
+  double E;  // the stop test's tolerance (graph unions, the device-side loop)
+  double M;  // the device-side loop: half the total weight, and the iteration cap
+  int L;
   bool operator==(const IterKey &o) const {
     return !std::memcmp(p, o.p, sizeof(p)) && !std::memcmp(n, o.n, sizeof(n)) && !std::memcmp(k, o.k, sizeof(k)) &&
-           kr == o.kr && E == o.E;
+           kr == o.kr && E == o.E && M == o.M && L == o.L;
   }
 };
 
@@ -232,6 +234,11 @@ struct lvg_graph {
   IterKey iter_key{};
   unsigned long long iter_nodes = 0, iter_moves = 0;
   bool no_graphs = false;
+  // the local-moving phase of the uploaded level as one graph: a conditional
+  // while node around one iteration, the stop test on the device
+  cudaGraphExec_t phase_exec = nullptr;
+  IterKey phase_key{};
+  bool no_phase_graphs = false;
   // side streams for the degree-bin kernels of one colour class, which run
   // concurrently (fork/join with events)
   cudaStream_t aux[4] = {};
@@ -241,6 +248,7 @@ struct lvg_graph {
   ~lvg_graph() {
     if (copy_stream) cudaStreamDestroy(copy_stream);
     if (iter_exec) cudaGraphExecDestroy(iter_exec);
+    if (phase_exec) cudaGraphExecDestroy(phase_exec);
     for (auto &a : aux)
       if (a) cudaStreamDestroy(a);
     if (fork_ev) cudaEventDestroy(fork_ev);
@@ -310,6 +318,10 @@ int guarded(F &&f) {
 }
 
 void ensure_ws(lvg_graph *g);
+// Wait for the graph's stream, counted in the call's statistics (host_syncs).
+void host_sync(lvg_graph *g);
+// Drop the captured local-moving graphs (their launch shapes and buffers are stale).
+void drop_graphs(lvg_graph *g);
 void read_counters(lvg_graph *g);
 void compute_bins(lvg_graph *g, Level &lv, const uint32_t *deg, uint32_t *list, uint32_t *scratch, int colors);
 void build_hub_plan(lvg_graph *g, Level &lv, HubPlanBuffers &hb);

@@ -159,6 +159,8 @@ struct Counters {
   unsigned int ds_long;                       // delta-screening sources with more than 32 insertions
   uint32_t ds_chunks;                         // delta-screening neighbour chunks of the high-degree vertices
   unsigned long long nonunit;                 // edge weights other than 1 (count_nonunit)
+  unsigned int dev_iters;                     // iterations run by the device-side loop (iter_end_kernel)
+  double dev_el;                              // its last iteration's el
 };
 
 // Per-graph control of a graph-union run (lvg_static_union), on the device:
@@ -356,6 +358,10 @@ void launch_level_init(size_t n, const tot_t *vtot, uint32_t *vcom, tot_t *ctot,
 void launch_next_vertex_weights(const uint32_t *cext, size_t span, const uint32_t *total, const tot_t *ctot,
                                 tot_t *vtot_next, cudaStream_t s);
 void launch_count_flags(const uint8_t *f, size_t n, Counters *ctr, cudaStream_t s);
+// The device-side iteration loop's test (louvainMoveOmpW, inc/louvain.hxx:588-609):
+// el = the iteration's gain sum / M; another iteration while el > E, fewer
+// than L have run and no error is flagged (ctr->dev_iters counts them).
+void launch_iter_end(Counters *ctr, double M, double E, int L, cudaGraphConditionalHandle h, cudaStream_t s);
 // Set ERR_BAD_ID in ctr->err if any a[i] >= limit.
 void launch_check_ids(const uint32_t *a, size_t n, uint32_t limit, Counters *ctr, cudaStream_t s);
 void launch_modularity(const Level &g, const uint32_t *memb, double *ctot64, Counters *ctr, cudaStream_t s);

@@ -1072,6 +1072,18 @@ void launch_clear_isolated_endpoints(const uint32_t *a, size_t na, const uint32_
   LVG_CHECK_LAUNCH();
 }
 
+__global__ void iter_end_kernel(Counters *ctr, double M, double E, int L, cudaGraphConditionalHandle h) {
+  const double el = double(ctr->el_fix) / GAIN_FIX / M;
+  ctr->dev_el = el;
+  const unsigned l = ++ctr->dev_iters;
+  cudaGraphSetConditional(h, (el > E && l < unsigned(L) && !ctr->err) ? 1u : 0u);
+}
+
+void launch_iter_end(Counters *ctr, double M, double E, int L, cudaGraphConditionalHandle h, cudaStream_t s) {
+  iter_end_kernel<<<1, 1, 0, s>>>(ctr, M, E, L, h);
+  LVG_CHECK_LAUNCH();
+}
+
 void launch_count_flags(const uint8_t *f, size_t n, Counters *ctr, cudaStream_t s) {
   LVG_CUDA(cudaMemsetAsync(&ctr->affected, 0, sizeof(unsigned long long), s));
   if (!n) return;

@@ -115,7 +115,8 @@ class _Stats(C.Structure):
                 ("kernel_launches", C.c_uint64), ("move_bin_ms", C.c_double * 12),
                 ("move_bin_vertices", C.c_uint64 * 12), ("move_bin_edges", C.c_uint64 * 12),
                 ("call_upload_ms", C.c_double), ("call_run_ms", C.c_double), ("call_download_ms", C.c_double),
-                ("move_bin_overflow", C.c_uint64 * 12), ("hub_chunk_overflow", C.c_uint64)]
+                ("move_bin_overflow", C.c_uint64 * 12), ("hub_chunk_overflow", C.c_uint64),
+                ("host_syncs", C.c_uint64)]
 
 
 class _Csr(C.Structure):
@@ -736,8 +737,8 @@ def affected_vertices(y: Graph, method: int, batch: HostBatch, q, qvtot, qctot, 
     f, nb, cm = np.zeros(S, np.uint8), np.zeros(S, np.uint8), np.zeros(S, np.uint8)
     b = (batch or HostBatch.empty())._struct()
     opt = (o or LouvainOptions())._struct()
-    _check(L.lvg_affected_vertices(y.h, method, C.byref(b), np.ascontiguousarray(q, np.uint32),
-                                   np.ascontiguousarray(qvtot, np.float64), np.ascontiguousarray(qctot, np.float64),
+    q, qvtot, qctot = _prior_arrays(S, q, qvtot, qctot)
+    _check(L.lvg_affected_vertices(y.h, method, C.byref(b), q, qvtot, qctot,
                                    C.byref(opt), f.ctypes.data, nb.ctypes.data, cm.ctypes.data))
     return (f, nb, cm) if method == METHOD_DELTA else f
 
@@ -758,6 +759,16 @@ def aggregate(g: Graph, membership):
     return ren, CN, off[:CN + 1].copy(), keys[:E].copy(), w[:E].copy()
 
 
+def _prior_arrays(S: int, q, qvtot, qctot):
+    """The prior state as the C types; the library reads span entries of each."""
+    q = np.ascontiguousarray(q, np.uint32)
+    qvtot = np.ascontiguousarray(qvtot, np.float64)
+    qctot = np.ascontiguousarray(qctot, np.float64)
+    if min(len(q), len(qvtot), len(qctot)) < S:
+        raise LvgError(LVG_EINVAL, f"prior state: arrays shorter than the graph's span {S}")
+    return q, qvtot, qctot
+
+
 def _run(fn_name: str, g: Graph, batch: HostBatch | None, q, qvtot, qctot, o: LouvainOptions | None,
          out_buffers=None) -> LouvainResult:
     L = load_library()
@@ -776,9 +787,8 @@ def _run(fn_name: str, g: Graph, batch: HostBatch | None, q, qvtot, qctot, o: Lo
     else:
         b = (batch or HostBatch.empty())._struct()
         keep.append(b)
-        _check(getattr(L, fn_name)(g.h, C.byref(b), np.ascontiguousarray(q, np.uint32),
-                                   np.ascontiguousarray(qvtot, np.float64), np.ascontiguousarray(qctot, np.float64),
-                                   C.byref(opt), C.byref(r)))
+        q, qvtot, qctot = _prior_arrays(S, q, qvtot, qctot)
+        _check(getattr(L, fn_name)(g.h, C.byref(b), q, qvtot, qctot, C.byref(opt), C.byref(r)))
     if out_buffers is not None:
         m, vw, cw = out_buffers
     else:
@@ -822,8 +832,8 @@ class State:
         _check(self._L.lvg_state_create(g.h, C.byref(self.h)))
 
     def set(self, q, qvtot, qctot) -> None:
-        _check(self._L.lvg_state_set(self.h, np.ascontiguousarray(q, np.uint32),
-                                     np.ascontiguousarray(qvtot, np.float64), np.ascontiguousarray(qctot, np.float64)))
+        q, qvtot, qctot = _prior_arrays(self.g.span, q, qvtot, qctot)
+        _check(self._L.lvg_state_set(self.h, q, qvtot, qctot))
 
     def get(self):
         S = self.g.span

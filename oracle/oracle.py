@@ -175,6 +175,7 @@ class Oracle:
         S = g.span
         v, n, c = np.zeros(S, np.uint8), np.zeros(S, np.uint8), np.zeros(S, np.uint8)
         a = _batch_args(b)
+        assert min(len(vcom), len(vtot), len(ctot)) >= S, "prior state shorter than the span"
         self.L.orc_ds_mark(*_graph_args(g), a[0], a[1], a[2], a[4], a[5], a[6], a[7],
                            np.ascontiguousarray(vcom, np.uint32), np.ascontiguousarray(vtot, np.float64),
                            np.ascontiguousarray(ctot, np.float64), M, R, v, n, c)
@@ -221,6 +222,7 @@ class Oracle:
         q = np.zeros(S, np.uint32) if q is None else np.ascontiguousarray(q, np.uint32)
         qvtot = np.zeros(S, np.float64) if qvtot is None else np.ascontiguousarray(qvtot, np.float64)
         qctot = np.zeros(S, np.float64) if qctot is None else np.ascontiguousarray(qctot, np.float64)
+        assert min(len(q), len(qvtot), len(qctot)) >= S, "prior state shorter than the span"
         m, vt, ct = np.zeros(S, np.uint32), np.zeros(S, np.float64), np.zeros(S, np.float64)
         info = Info()
         if sync:
@@ -330,6 +332,7 @@ class _RefGraph:
     def ds_mark(self, b, vcom, vtot, ctot, M, R=1.0):
         S = self.g.span
         v, n, c = np.zeros(S, np.uint8), np.zeros(S, np.uint8), np.zeros(S, np.uint8)
+        assert min(len(vcom), len(vtot), len(ctot)) >= S, "prior state shorter than the span"
         self.ref.L.ref_ds_mark(self.h, *_batch_args(b), np.ascontiguousarray(vcom, np.uint32),
                                np.ascontiguousarray(vtot, np.float64), np.ascontiguousarray(ctot, np.float64), M, R,
                                v, n, c)
@@ -383,6 +386,7 @@ class _RefGraph:
         q = np.zeros(S, np.uint32) if q is None else np.ascontiguousarray(q, np.uint32)
         qvtot = np.zeros(S, np.float64) if qvtot is None else np.ascontiguousarray(qvtot, np.float64)
         qctot = np.zeros(S, np.float64) if qctot is None else np.ascontiguousarray(qctot, np.float64)
+        assert min(len(q), len(qvtot), len(qctot)) >= S, "prior state shorter than the span"
         m, vt, ct = np.zeros(S, np.uint32), np.zeros(S, np.float64), np.zeros(S, np.float64)
         info = Info()
         rc = self.ref.L.ref_louvain(self.h, method, *_batch_args(batch), q, qvtot, qctot, o.repeat, o.resolution,

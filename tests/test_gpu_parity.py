@@ -280,13 +280,14 @@ def test_delta_screening_exact_tie_takes_first_community(cuda, orc, swap, scale)
                 if a != b:
                     src.append(a)
                     dst.append(b)
+    # span 17: the edge-list reader makes vertices 0..16 (16 isolated)
     x = cuda.csr_from_edges(16, np.array(src, np.uint32), np.array(dst, np.uint32),
                             np.full(len(src), scale, np.float32))
     la, lb = (6, 1) if swap else (1, 6)
-    q = np.array([0] + [la] * 5 + [lb] * 5 + [11] * 5, np.uint32)
+    q = np.array([0] + [la] * 5 + [lb] * 5 + [11] * 5 + [16], np.uint32)
     sw = float(np.float32(scale))
-    vt = np.array([0] + [4.0 * sw] * 15)
-    ct = np.zeros(16)
+    vt = np.array([0] + [4.0 * sw] * 15 + [0])
+    ct = np.zeros(17)
     ct[[1, 6, 11]] = 20.0 * sw
     ins = [(3, 11), (8, 11), (11, 3), (11, 8)]
     e = np.zeros(0, np.uint32)
