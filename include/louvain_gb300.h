@@ -407,6 +407,13 @@ typedef struct lvg_stats {
    * hub merges), and hub chunks that handed their raw pairs on. */
   uint64_t move_bin_overflow[12];
   uint64_t hub_chunk_overflow;
+  /* Resident hub tables (lvg_tuning.hub_tables): slots read by the table
+   * evaluations, tables that ran out of room (their hubs scanned their edges
+   * instead), and whether the call built the tables (1) or took them from
+   * its prior state (0). */
+  uint64_t hub_table_slots;
+  uint64_t hub_table_overflow;
+  uint64_t hub_tables_built;
   /* Times the last call waited for the GPU (stream synchronisations of the
    * run: with the local-moving phase replayed as one graph, a dynamic-frontier
    * run that ends after one pass waits once). */
@@ -433,6 +440,11 @@ typedef struct lvg_tuning {
                                       entries per edge of the graph; larger batches (whose
                                       frontiers cover much of the graph) keep 8 classes
                                       (default 1e-3) */
+  int      hub_tables;         /* 1: lvg_run_resident keeps, with each state, the neighbour
+                                  counts per community of every vertex above degree 8192 of a
+                                  unit-weight graph, so that the dynamic methods' first pass
+                                  evaluates such a vertex from its table instead of its edges
+                                  (same results; default 1) */
 } lvg_tuning;
 void lvg_tuning_default(lvg_tuning *t);
 int lvg_graph_get_tuning(const lvg_graph *g, lvg_tuning *t);

@@ -70,6 +70,7 @@ void check_tuning(const lvg_tuning &t) {
   if (t.big_blocks_per_sm < 0 || t.big_blocks_per_sm > 64) throw Error(LVG_EINVAL, "tuning: big_blocks_per_sm");
   if (!(t.frontier_max_fraction >= 0 && t.frontier_max_fraction <= 1))
     throw Error(LVG_EINVAL, "tuning: frontier_max_fraction out of 0..1");
+  if (t.hub_tables != 0 && t.hub_tables != 1) throw Error(LVG_EINVAL, "tuning: hub_tables is 0 or 1");
 }
 
 // Set a graph's tuning: the hub plan of the uploaded level follows the chunk
@@ -765,6 +766,7 @@ int lvg_state_set(lvg_state *st, const uint32_t *q, const double *qvtot, const d
     lvg_graph *g = st->g;
     LVG_CUDA(cudaSetDevice(g->device));
     lvg::ensure_ws(g);
+    st->ht.version = ~0ull;  // its hub tables described the old membership
     lvg::upload_prior(g, q, qvtot, qctot, st->q.p, st->vt.p, st->ct.p);
     LVG_CUDA(cudaStreamSynchronize(g->stream));
     return LVG_OK;
@@ -866,6 +868,7 @@ int lvg_graph_apply_device_batch(lvg_graph *g, lvg_device_batch *b) {
     // the dynamic methods then take, as main.cxx:108-125 does
     const lvg::DBatch &r = b->b;
     if (!(r.nd + r.ni)) {
+      b->b.applied_version = g->version;
       b->applied = true;
       return LVG_OK;
     }
@@ -876,6 +879,7 @@ int lvg_graph_apply_device_batch(lvg_graph *g, lvg_device_batch *b) {
     b->b.nd = t.nd;
     b->b.ni = t.ni;
     b->b.max_group = t.max_group;  // an upper bound after the filter
+    b->b.applied_version = g->version;
     b->applied = true;
     return LVG_OK;
   });
@@ -976,6 +980,7 @@ int lvg_device_batch_set(lvg_device_batch *db, const lvg_batch *b) {
     bool sorted = true;
     for (size_t i = 1; i < b->num_insertions; ++i) sorted &= b->ins_src[i] >= b->ins_src[i - 1];
     if (!sorted) db->b.max_group = ~size_t(0);
+    db->b.applied_version = ~0ull;
     db->applied = false;
     LVG_CUDA(cudaStreamSynchronize(g->stream));  // the caller may reuse its arrays
     return LVG_OK;
@@ -1041,7 +1046,8 @@ int lvg_autotune(lvg_graph *g, int method, const lvg_device_batch *b, const lvg_
     auto once = [&] {
       RunInfo ri;
       if (g->uni) run_union(g, opt, ri);
-      else run(g, method, db, pr, st, opt, ri);
+      else run(g, method, db, pr, st, opt, ri, nullptr, prior ? const_cast<HubTables *>(&prior->ht) : nullptr,
+               &g->ht_tune);
       return double(ri.t);
     };
     // time of a candidate (min over the repeats, after one warm-up run); q:
@@ -1130,7 +1136,9 @@ int lvg_run_resident(lvg_graph *g, int method, const lvg_device_batch *b, const 
     if (prior) pr = lvg::StateRef{prior->q.p, prior->vt.p, prior->ct.p};
     lvg::StateRef st{out->q.p, out->vt.p, out->ct.p};
     lvg::RunInfo ri;
-    lvg::run(g, method, db, pr, st, opt, ri);
+    // the prior's hub tables are a cache of its membership: filled, never changed in meaning
+    lvg::HubTables *tp = prior ? const_cast<lvg::HubTables *>(&prior->ht) : nullptr;
+    lvg::run(g, method, db, pr, st, opt, ri, nullptr, tp, &out->ht);
     if (info) lvg::fill_result(info, ri, g->base.span);
     return LVG_OK;
   });

@@ -222,6 +222,150 @@ void ensure_aux(lvg_graph *g) {
 
 // The stream of degree bin b within a colour class: the small bins on two
 // side streams, bins 9 and 10 on two more, the hubs on the main stream.
+// ------------------------------------------------------- resident hub tables
+
+// The uploaded level's hubs in id order and the vertex -> hub index map, for
+// the current graph version. The hubs are the hub plan's (degree bin 11, any
+// colour class); their degrees size the build's scratch tables.
+void ensure_hub_index(lvg_graph *g) {
+  if (g->hub_index_version == g->version) return;
+  cudaStream_t s = g->stream;
+  const HubPlan &P = g->base.hub;
+  const size_t H = P.hubs;
+  std::vector<uint32_t> ids(H), degs(H);
+  if (H) {
+    DBuf<uint32_t> d;
+    d.ensure(H);
+    launch_gather_u32(P.hub_vertex, H, g->base.deg, d.p, s);
+    LVG_CUDA(cudaMemcpyAsync(ids.data(), P.hub_vertex, H * 4, cudaMemcpyDeviceToHost, s));
+    LVG_CUDA(cudaMemcpyAsync(degs.data(), d.p, H * 4, cudaMemcpyDeviceToHost, s));
+    host_sync(g);
+    std::vector<size_t> ord(H);
+    for (size_t i = 0; i < H; ++i) ord[i] = i;
+    std::sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return ids[a] < ids[b]; });
+    std::vector<uint32_t> si(H), sd(H);
+    for (size_t i = 0; i < H; ++i) { si[i] = ids[ord[i]]; sd[i] = degs[ord[i]]; }
+    ids.swap(si);
+    degs.swap(sd);
+  }
+  g->hub_deg_h = degs;
+  if (ids != g->hub_ids_h || !g->hub_slot.p) {
+    const size_t S = g->base.span;
+    g->hub_slot.ensure(S);
+    LVG_CUDA(cudaMemsetAsync(g->hub_slot.p, 0xFF, S * sizeof(uint32_t), s));
+    if (H) {
+      g->hub_ids.ensure(H);
+      LVG_CUDA(cudaMemcpyAsync(g->hub_ids.p, ids.data(), H * 4, cudaMemcpyHostToDevice, s));
+      launch_ht_slots(g->hub_ids.p, H, g->hub_slot.p, s);
+    }
+    host_sync(g);  // ids is freed next
+    g->hub_ids_h.swap(ids);
+    ++g->hub_index_gen;
+  }
+  g->hub_index_version = g->version;
+}
+
+// Largest table of a hub: a hub with more than a quarter of this many
+// neighbour communities keeps scanning its edges.
+constexpr int HT_MAX_LOG = 16;
+
+// Hub tables T of membership q on the current graph version: every hub's
+// neighbours counted per community into a scratch table (at least twice its
+// degree in slots), the distinct communities counted, then each hub's table
+// laid out with four times that many slots (at least 64) and filled.
+void build_hub_tables(lvg_graph *g, const uint32_t *q, HubTables &T) {
+  ensure_hub_index(g);
+  Workspace &W = *g->ws;
+  cudaStream_t s = g->stream;
+  const size_t H = g->hub_ids_h.size();
+  T.hubs = H;
+  T.slots = 0;
+  if (H) {
+    std::vector<uint64_t> soff(H + 1, 0);
+    std::vector<uint8_t> slg(H);
+    for (size_t h = 0; h < H; ++h) {
+      int l = 1;
+      while ((uint64_t(1) << l) < 2ull * g->hub_deg_h[h]) ++l;
+      slg[h] = uint8_t(l);
+      soff[h + 1] = soff[h] + (uint64_t(1) << l);
+    }
+    const size_t stotal = soff[H];
+    W.ht_soff.ensure(H + 1);
+    W.ht_slg.ensure(H);
+    W.ht_skey.ensure(stotal);
+    W.ht_scnt.ensure(stotal);
+    W.ht_n.ensure(H);
+    LVG_CUDA(cudaMemcpyAsync(W.ht_soff.p, soff.data(), (H + 1) * 8, cudaMemcpyHostToDevice, s));
+    LVG_CUDA(cudaMemcpyAsync(W.ht_slg.p, slg.data(), H, cudaMemcpyHostToDevice, s));
+    LVG_CUDA(cudaMemsetAsync(W.ht_skey.p, 0xFF, stotal * 4, s));
+    LVG_CUDA(cudaMemsetAsync(W.ht_scnt.p, 0, stotal * 4, s));
+    launch_ht_scratch(g->base, q, g->hub_slot.p, W.ht_soff.p, W.ht_slg.p, W.ht_skey.p, W.ht_scnt.p, g->ctr.p, s);
+    launch_ht_count(H, W.ht_soff.p, W.ht_slg.p, W.ht_skey.p, W.ht_n.p, s);
+    std::vector<uint32_t> n(H);
+    LVG_CUDA(cudaMemcpyAsync(n.data(), W.ht_n.p, H * 4, cudaMemcpyDeviceToHost, s));
+    host_sync(g);
+    std::vector<uint64_t> off(H + 1, 0);
+    std::vector<uint8_t> lg(H), bad(H, 0);
+    for (size_t h = 0; h < H; ++h) {
+      int l = 6;
+      while ((uint64_t(1) << l) < 4ull * n[h]) ++l;
+      if (l > HT_MAX_LOG) {  // too many communities: this hub scans its edges
+        l = 1;
+        bad[h] = 1;
+      }
+      lg[h] = uint8_t(l);
+      off[h + 1] = off[h] + (uint64_t(1) << l);
+    }
+    T.slots = off[H];
+    T.off.ensure(H + 1);
+    T.lg.ensure(H);
+    T.bad.ensure(H);
+    T.key.ensure(T.slots);
+    T.cnt.ensure(T.slots);
+    LVG_CUDA(cudaMemcpyAsync(T.off.p, off.data(), (H + 1) * 8, cudaMemcpyHostToDevice, s));
+    LVG_CUDA(cudaMemcpyAsync(T.lg.p, lg.data(), H, cudaMemcpyHostToDevice, s));
+    LVG_CUDA(cudaMemcpyAsync(T.bad.p, bad.data(), H, cudaMemcpyHostToDevice, s));
+    LVG_CUDA(cudaMemsetAsync(T.key.p, 0xFF, T.slots * 4, s));
+    LVG_CUDA(cudaMemsetAsync(T.cnt.p, 0, T.slots * 4, s));
+    launch_ht_fill(H, W.ht_soff.p, W.ht_slg.p, W.ht_skey.p, W.ht_scnt.p, T.view(g->hub_slot.p), s);
+    host_sync(g);  // the host arrays above are freed next
+  }
+  T.version = g->version;
+  T.index = g->hub_index_gen;
+}
+
+// dst := src (same graph).
+void copy_hub_tables(lvg_graph *g, const HubTables &src, HubTables &dst) {
+  cudaStream_t s = g->stream;
+  const size_t H = src.hubs;
+  dst.hubs = H;
+  dst.slots = src.slots;
+  if (H) {
+    dst.off.ensure(H + 1);
+    dst.lg.ensure(H);
+    dst.bad.ensure(H);
+    dst.key.ensure(src.slots);
+    dst.cnt.ensure(src.slots);
+    LVG_CUDA(cudaMemcpyAsync(dst.off.p, src.off.p, (H + 1) * 8, cudaMemcpyDeviceToDevice, s));
+    LVG_CUDA(cudaMemcpyAsync(dst.lg.p, src.lg.p, H, cudaMemcpyDeviceToDevice, s));
+    LVG_CUDA(cudaMemcpyAsync(dst.bad.p, src.bad.p, H, cudaMemcpyDeviceToDevice, s));
+    LVG_CUDA(cudaMemcpyAsync(dst.key.p, src.key.p, src.slots * 4, cudaMemcpyDeviceToDevice, s));
+    LVG_CUDA(cudaMemcpyAsync(dst.cnt.p, src.cnt.p, src.slots * 4, cudaMemcpyDeviceToDevice, s));
+  }
+  dst.version = src.version;
+  dst.index = src.index;
+}
+
+// The tables the first pass keeps up to date while it is enqueued (scoped:
+// cleared however the pass ends).
+struct HubTabScope {
+  Workspace &W;
+  HubTabScope(lvg_graph *g, const HubTables *t) : W(*g->ws) {
+    W.ht_now = t && t->hubs ? t->view(g->hub_slot.p) : HubTabView{};
+  }
+  ~HubTabScope() { W.ht_now = HubTabView{}; }
+};
+
 int bin_stream(int b) { return b <= 4 ? 0 : b <= 8 ? 1 : b == 9 ? 2 : b == 10 ? 3 : -1; }
 
 void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const tot_t *tot,
@@ -281,6 +425,7 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot
         a.vcom = com; a.ctot = ctot; a.dec = W.dec.p;
         a.vaff = W.vaff.p; a.mark = W.mark.p; a.fa = fa; a.vtot = tot;
         a.kr = kr; a.ctr = g->ctr.p; a.unit = lv.unit; a.bin = grp.first;
+        a.ht = W.ht_now;
         set_union(a);
         cudaEvent_t b0 = bin_ev ? g->events.record(s) : nullptr;
         launch_move_small(grp.first, grp.second, sync, a, sb, stream_of(grp.first));
@@ -304,6 +449,7 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot
       a.glog2 = glog2[b];
       a.big_cap = g->tuning.big_blocks_per_sm;
       a.big_direct = W.first_sweep;
+      a.ht = W.ht_now;
       set_union(a);
       cudaEvent_t b0 = bin_ev ? g->events.record(s) : nullptr;
       if (b == NUM_BINS - 1) {
@@ -331,6 +477,9 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot
       }
     }
     if (sync) {
+      if (W.ht_now.key)  // the hubs' tables follow the decided moves before they are applied
+        launch_ht_sync_moves(lv, lv.bins + lv.color_begin(k), lv.color_end(k) - lv.color_begin(k), W.dec.p, com,
+                             W.ht_now, g->ctr.p, s);
       launch_apply_moves(lv.bins + lv.color_begin(k), lv.color_end(k) - lv.color_begin(k), W.dec.p, com, ctot, tot, s);
       launch_merge_marks(W.vaff.p, W.mark.p, lv.span, s);
     }
@@ -343,13 +492,14 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot
 // conditional while node whose body is one iteration (as enqueue_iteration
 // issues it) followed by iter_end_kernel, which evaluates the reference's
 // stop test (el <= E, or L iterations; inc/louvain.hxx:588-609) on the device
-// and sets the node's condition. The loop is bounded by L whatever the
-// kernels compute. A phase is then one graph launch and one synchronisation,
-// instead of one of each per iteration. Any failure to build it leaves the
-// per-iteration path in place for this handle.
+// and sets the node's condition (for a graph union: while any graph is still
+// moving, each graph's own test having run in iter_control_kernel). The loop
+// is bounded by L whatever the kernels compute. A phase is then one graph
+// launch and one synchronisation, instead of one of each per iteration. Any
+// failure to build it leaves the per-iteration path in place for this handle.
 void capture_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const tot_t *tot, const uint8_t *fa,
                    float kr, bool sync, int fused, const int *glog2, const size_t *goff, size_t need,
-                   const IterKey &key) {
+                   const IterKey &key, const UnionCall *uc) {
   cudaStream_t s = g->stream;
   if (g->phase_exec) {
     cudaGraphExecDestroy(g->phase_exec);
@@ -374,8 +524,8 @@ void capture_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, co
                                                  cudaStreamCaptureModeThreadLocal) == cudaSuccess;
   if (fine) {
     try {
-      enqueue_iteration(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, goff, need, nullptr, nullptr, false);
-      launch_iter_end(g->ctr.p, key.M, key.E, key.L, h, s);
+      enqueue_iteration(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, goff, need, nullptr, uc, false);
+      launch_iter_end(g->ctr.p, key.M, key.E, key.L, uc != nullptr, h, s);
     } catch (const Error &) {
       fine = false;
     }
@@ -503,11 +653,12 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const 
   const bool base = lv.off == g->base.off;
   IterKey key{};
   if (base) {
-    const void *ps[27] = {W.spill_now ? W.spill_keys.p : nullptr, lv.off, lv.bins, com, ctot, tot, fa, W.vaff.p,
+    const void *ps[32] = {W.spill_now ? W.spill_keys.p : nullptr, lv.off, lv.bins, com, ctot, tot, fa, W.vaff.p,
                           W.mark.p, W.dec.p, W.wl.p, W.wl_count.p,
                           W.gkeys.p, W.gvals.p, W.chunk_cnt.p, W.part_key.p, W.part_val.p, W.hub_kd.p, g->ctr.p,
                           g->hctr.p, lv.hub.chunk, lv.hub.hub_vertex, lv.gid,
-                          W.spill_now ? W.spill_vals.p : nullptr, W.hub_over.p, W.hub_best.p, lv.deg};
+                          W.spill_now ? W.spill_vals.p : nullptr, W.hub_over.p, W.hub_best.p, lv.deg,
+                          W.ht_now.key, W.ht_now.slot, W.ht_now.cnt, W.ht_now.off, W.ht_now.bad};
     std::memcpy(key.p, ps, sizeof(ps));
     key.n[0] = lv.span; key.n[1] = need; key.n[2] = lv.hub.chunks; key.n[3] = lv.bin_start[K * NUM_BINS];
     key.k[0] = K; key.k[1] = sync | int(lv.unit) << 1; key.k[2] = glog2[9] | glog2[10] << 8 | glog2[11] << 16;
@@ -518,7 +669,7 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const 
     key.L = L;
   }
   const bool graphs = base && capture && !g->profiling && !g->no_graphs;
-  const bool phase_graphs = graphs && !uc && !g->no_phase_graphs && L > 0;
+  const bool phase_graphs = graphs && !g->no_phase_graphs && L > 0;
   int l = 0;
   double el = 0;
   if (phase_graphs && g->phase_exec && g->phase_key == key) {
@@ -532,7 +683,7 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const 
     host_sync(g);
     if (g->hctr.p->err) read_counters(g);  // raises the device error
     l = int(g->hctr.p->dev_iters);
-    el = g->hctr.p->dev_el;
+    el = uc ? 0.0 : g->hctr.p->dev_el;  // graph unions: each graph's el is in its GraphCtl
     launch_counter() += (g->iter_nodes + 1) * unsigned(l);
     g->stats.move_launches += g->iter_moves * unsigned(l);
     if (end) { end->l = l; end->el = el; }
@@ -572,7 +723,7 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const 
   // next time, the whole phase as one graph (every kernel's attributes are set
   // by now)
   if (phase_graphs && !(g->phase_exec && g->phase_key == key))
-    capture_phase(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, goff, need, key);
+    capture_phase(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, goff, need, key, uc);
   if (end) { end->l = l; end->el = el; }
   return (l > 1 || el != 0) ? l : 0;
 }
@@ -700,7 +851,7 @@ Level aggregate(lvg_graph *g, const Level &lv, const uint32_t *com, size_t CN, i
 // on_init (optional) is called once, in the last repetition, with an event
 // recorded when the first level's vertex weights (out.vt) are final.
 void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out, const lvg_options &o,
-         RunInfo &info, const std::function<void(cudaEvent_t)> *on_init) {
+         RunInfo &info, const std::function<void(cudaEvent_t)> *on_init, HubTables *tprior, HubTables *tout) {
   if (g->uni) throw Error(LVG_EINVAL, "graph union: run it with lvg_static_union");
   ensure_ws(g);
   Workspace &W = *g->ws;
@@ -719,6 +870,9 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
   g->stats = lvg_stats{};
   const unsigned long long launches0 = launch_counter();
   LVG_CUDA(cudaMemsetAsync(g->ctr.p, 0, sizeof(Counters), s));
+  // resident hub tables: the dynamic methods on a unit-weight graph, between
+  // two states (lvg_run_resident)
+  const bool tabs0 = tprior && tout && method != LVG_METHOD_STATIC && g->tuning.hub_tables && g->base.unit;
   int l = 0, p = 0;
   for (int r = 0; r < rep; ++r) {
     g->events.reset();
@@ -737,7 +891,34 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
       if (prior.ct != ctot)
         LVG_CUDA(cudaMemcpyAsync(ctot, prior.ct, S * sizeof(tot_t), cudaMemcpyDeviceToDevice, s));
     }
+    // The prior's hub tables into the result state, like its membership and
+    // weights: as they are when they describe this graph version; plus this
+    // run's batch when they describe the version before it and the batch is
+    // the one that made this version; else built (in the timed section) from
+    // the prior membership.
+    const bool tabs = tabs0 && g->base.hub.hubs > 0;
+    int ht_mode = 0;  // 1 copied, 2 copied + the batch's edges, 3 built
+    if (tabs) {
+      ensure_hub_index(g);
+      const bool same_hubs = tprior->index == g->hub_index_gen;
+      if (same_hubs && tprior->version == g->version) ht_mode = 1;
+      else if (same_hubs && tprior->version != ~0ull && tprior->version + 1 == g->version &&
+               b.applied_version == g->version)
+        ht_mode = 2;
+      else ht_mode = 3;
+      if (ht_mode <= 2 && tprior != tout) copy_hub_tables(g, *tprior, *tout);
+    }
     cudaEvent_t e0 = g->events.record(s);
+    if (ht_mode == 2) {
+      const HubTabView v = tout->view(g->hub_slot.p);
+      launch_ht_batch(b.ds, b.dd, b.nd, false, ucom, v, g->ctr.p, s);
+      launch_ht_batch(b.is, b.id, b.ni, true, ucom, v, g->ctr.p, s);
+      tout->version = g->version;
+    } else if (ht_mode == 3) {
+      build_hub_tables(g, ucom, *tout);
+      if (tprior != tout) copy_hub_tables(g, *tout, *tprior);  // the prior's own cache, before any move
+      g->stats.hub_tables_built = 1;
+    }
     // fi: initial membership and weights.
     if (method == LVG_METHOD_STATIC) {
       launch_init_static(g->base, ucom, utot, ctot, s);
@@ -829,6 +1010,7 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
         }
       } else {
         SpillScope spill(g, lv, method == LVG_METHOD_STATIC);
+        HubTabScope hts(g, first && tabs ? tout : nullptr);  // kept up to date by the first pass's moves
         m = move_phase(g, lv, com, ctot, tot, first ? fa : nullptr, M, kr, L, E, sync, fused, nullptr, ends,
                        nullptr, true, first && r == rep - 1 ? &tail : nullptr, &tail_done);
       }
@@ -871,6 +1053,9 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
       host_sync(g);
     }
     if (r == rep - 1 && g->hctr.p->err) read_counters(g);  // raises the device error
+    // the result's hub tables describe its membership if no pass aggregated
+    // (which relabels it) and none ran out of room (then they are rebuilt)
+    if (tout && !(tabs && p <= 1 && !g->hctr.p->ht_over)) tout->version = ~0ull;
     info.ti += elapsed(e0, e1);
     info.tm += elapsed(e1, e2);
     info.tp += elapsed(e2, ep1 ? ep1 : eend);
@@ -892,6 +1077,8 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
     g->stats.move_bin_overflow[b] = g->hctr.p->bin_over[b];
   }
   g->stats.hub_chunk_overflow = g->hctr.p->hub_chunk_over;
+  g->stats.hub_table_slots = g->hctr.p->ht_slots;
+  g->stats.hub_table_overflow = g->hctr.p->ht_over;
   g->stats.kernel_launches = launch_counter() - launches0;
 }
 
@@ -1353,6 +1540,7 @@ void apply_plan(lvg_graph *g, const PlanCounts &pc) {
   const uint32_t *dd = g->u_dd.p, *id = g->u_id.p;
   const float *iw = g->u_iw.p;
   if (!nrows) return;
+  ++g->version;  // every cache of the old edges (hub tables) is stale from here on
   cudaStream_t s = g->stream;
   Level &b = g->base;
   g->u_pre.ensure(nd + ni);

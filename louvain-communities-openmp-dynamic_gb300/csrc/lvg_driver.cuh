@@ -60,6 +60,12 @@ struct Workspace {
   DBuf<float> spill_vals;
   bool spill_now = false;  // the iteration being enqueued spills overflowing hubs
   bool first_sweep = false;  // static Louvain's first iteration (every neighbour a singleton)
+  // resident hub tables: build scratch, and the tables the first pass of the
+  // run being enqueued keeps up to date (key == nullptr: none)
+  DBuf<uint64_t> ht_soff;
+  DBuf<uint8_t> ht_slg;
+  DBuf<uint32_t> ht_skey, ht_scnt, ht_n;
+  HubTabView ht_now;
   // chunked aggregation of the largest communities
   DBuf<uint64_t> mpre, agg_toff, agg_tdeg;
   DBuf<uint2> agg_chunk;
@@ -123,12 +129,35 @@ struct DBatch {
   uint32_t *seg = nullptr;
   size_t nd = 0, ni = 0;
   size_t max_group = 0;  // longest run of insertions sharing a source
+  // the graph version its batch apply produced (~0: not applied by this
+  // library); its edges are then exactly the change from the version before
+  uint64_t applied_version = ~0ull;
+};
+
+// Resident hub tables of a state (HubTabView): valid for graph version
+// `version` and hub index generation `index` (~0: not valid).
+struct HubTables {
+  DBuf<uint64_t> off;
+  DBuf<uint8_t> lg, bad;
+  DBuf<uint32_t> key, cnt;
+  size_t hubs = 0, slots = 0;
+  uint64_t version = ~0ull, index = ~0ull;
+  HubTabView view(const uint32_t *slot) const {
+    HubTabView v;
+    v.slot = slot;
+    v.off = off.p;
+    v.lg = lg.p;
+    v.key = key.p;
+    v.cnt = cnt.p;
+    v.bad = bad.p;
+    return v;
+  }
 };
 
 // Everything an iteration's launches depend on; a captured iteration is
 // replayed only while all of it is unchanged.
 struct IterKey {
-  const void *p[27];
+  const void *p[32];
   size_t n[4];
   int k[4];
   float kr;
@@ -182,6 +211,7 @@ inline lvg_tuning default_tuning() {
   t.hub_chunk = HUB_CHUNK;
   t.big_blocks_per_sm = 0;
   t.frontier_max_fraction = 1e-3;
+  t.hub_tables = 1;
   return t;
 }
 
@@ -200,6 +230,14 @@ struct lvg_graph {
   int device = 0;
   cudaStream_t stream = nullptr;
   Level base;
+  uint64_t version = 0;  // bumped by every batch apply that changes an edge
+  // the uploaded level's hubs (degree bin 11) in id order and each vertex's
+  // index among them (NO_HUB), taken at graph version hub_index_version;
+  // hub_index_gen changes only when the set of hubs does
+  DBuf<uint32_t> hub_ids, hub_slot;
+  std::vector<uint32_t> hub_ids_h, hub_deg_h;
+  uint64_t hub_index_version = ~0ull, hub_index_gen = 0;
+  HubTables ht_tune;  // the result tables of the autotuner's runs
   // Gapped CSR: row u holds deg[u] entries at off[u] with room for cap[u];
   // rows that outgrow their room move to the overflow pool, entries
   // [pool_begin, slots) of key/w. Unused entries hold (0, 0.0).
@@ -272,6 +310,9 @@ struct lvg_state {
   int device = 0;
   DBuf<uint32_t> q;
   DBuf<tot_t> vt, ct;
+  // the hub tables of membership q (a cache: built when a dynamic method
+  // first runs from this state, kept up to date by the runs that write it)
+  lvg::HubTables ht;
 };
 
 struct lvg_device_batch {
@@ -327,8 +368,11 @@ void compute_bins(lvg_graph *g, Level &lv, const uint32_t *deg, uint32_t *list, 
 void build_hub_plan(lvg_graph *g, Level &lv, HubPlanBuffers &hb);
 Level aggregate(lvg_graph *g, const Level &lv, const uint32_t *com, size_t CN, int which, int colors,
                 const uint32_t *ngid = nullptr, const uint32_t *ngbase = nullptr);
+// tprior/tout (optional): the hub tables of the prior and of the result
+// state (the same object for a run in place).
 void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out, const lvg_options &o,
-         RunInfo &info, const std::function<void(cudaEvent_t)> *on_init = nullptr);
+         RunInfo &info, const std::function<void(cudaEvent_t)> *on_init = nullptr, HubTables *tprior = nullptr,
+         HubTables *tout = nullptr);
 void run_union(lvg_graph *g, const lvg_options &o, RunInfo &info);
 void check_batch(const lvg_graph *g, const lvg_batch *b, bool need_sorted);
 size_t max_group(const lvg_batch *b);

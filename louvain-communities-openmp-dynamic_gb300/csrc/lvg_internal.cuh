@@ -161,7 +161,62 @@ struct Counters {
   unsigned long long nonunit;                 // edge weights other than 1 (count_nonunit)
   unsigned int dev_iters;                     // iterations run by the device-side loop (iter_end_kernel)
   double dev_el;                              // its last iteration's el
+  unsigned long long ht_slots;                // hub-table slots read by hub_table_kernel
+  unsigned long long ht_over;                 // hub tables that ran out of room (their hubs scan again)
 };
+
+// Resident hub tables (the uploaded level of a unit-weight graph, in the
+// first pass of a dynamic method): for every vertex above degree 8192 (a hub)
+// the communities of its neighbours with their neighbour counts, k_c of the
+// reference's louvainScanCommunitiesW (inc/louvain.hxx:423) kept up to date
+// by every move instead of recounted from the hub's edges. Hub h's table has
+// 2^lg[h] slots at off[h] (linear probing, keys never removed: a count can
+// drop to 0); bad[h] marks a table that ran out of room, whose hub then takes
+// the chunked scan path. The counts are exact integers, so a hub's gains are
+// those of a fresh scan whatever the order of the updates.
+constexpr uint32_t NO_HUB = 0xFFFFFFFFu;
+struct HubTabView {
+  const uint32_t *slot = nullptr;  // [span] hub index of each vertex, NO_HUB for the others
+  const uint64_t *off = nullptr;   // [hubs] first slot
+  const uint8_t *lg = nullptr;     // [hubs] log2 of the slot count
+  uint32_t *key = nullptr;         // community, EMPTY
+  uint32_t *cnt = nullptr;         // neighbours in it
+  uint8_t *bad = nullptr;          // [hubs]
+};
+
+// Hub v's table after a neighbour moved from community `from` to `to` (a no-op
+// when v is not a hub or its table is marked bad). `from` is present: it is
+// the neighbour's community, counted when the table was built or when the
+// neighbour moved in. A table without room for `to` is marked bad.
+__device__ __forceinline__ void ht_move(const HubTabView &t, uint32_t v, uint32_t from, uint32_t to, Counters *ctr) {
+  const uint32_t h = t.slot[v];
+  if (h == NO_HUB || t.bad[h]) return;
+  const uint64_t o = t.off[h];
+  const int lg = t.lg[h];
+  const uint32_t mask = (1u << lg) - 1u;
+  bool found = false, placed = false;
+  uint32_t s = hash_hi(from, lg);
+  for (uint32_t p = 0; p <= mask; ++p) {
+    const uint32_t k = ld_relaxed(t.key + o + s);
+    if (k == from) { atomicSub(t.cnt + o + s, 1u); found = true; break; }
+    if (k == EMPTY) break;
+    s = (s + 1u) & mask;
+  }
+  s = hash_hi(to, lg);
+  for (uint32_t p = 0; p <= mask; ++p) {
+    uint32_t k = ld_relaxed(t.key + o + s);
+    if (k == EMPTY) {
+      k = atomicCAS(t.key + o + s, EMPTY, to);
+      if (k == EMPTY) k = to;
+    }
+    if (k == to) { atomicAdd(t.cnt + o + s, 1u); placed = true; break; }
+    s = (s + 1u) & mask;
+  }
+  if (!found || !placed) {
+    t.bad[h] = 1;
+    atomicAdd(&ctr->ht_over, 1ull);
+  }
+}
 
 // Per-graph control of a graph-union run (lvg_static_union), on the device:
 // the pass driver of inc/louvain.hxx:1180-1215 kept for each graph.
@@ -223,6 +278,8 @@ struct MoveArgs {
   // the level's weights are all 1 (Level::unit): the launchers pick the
   // kernels that do not read them
   bool unit = false;
+  // resident hub tables (ht.key == nullptr: none; hubs take the chunked path)
+  HubTabView ht;
 };
 
 // Arguments of the aggregation kernels (inc/louvain.hxx:897-912, 987-992).
@@ -360,8 +417,11 @@ void launch_next_vertex_weights(const uint32_t *cext, size_t span, const uint32_
 void launch_count_flags(const uint8_t *f, size_t n, Counters *ctr, cudaStream_t s);
 // The device-side iteration loop's test (louvainMoveOmpW, inc/louvain.hxx:588-609):
 // el = the iteration's gain sum / M; another iteration while el > E, fewer
-// than L have run and no error is flagged (ctr->dev_iters counts them).
-void launch_iter_end(Counters *ctr, double M, double E, int L, cudaGraphConditionalHandle h, cudaStream_t s);
+// than L have run and no error is flagged (ctr->dev_iters counts them). With
+// by_graph (graph unions) each graph has run its own test and the loop goes on
+// while any graph is still moving (ctr->gactive).
+void launch_iter_end(Counters *ctr, double M, double E, int L, bool by_graph, cudaGraphConditionalHandle h,
+                     cudaStream_t s);
 // Set ERR_BAD_ID in ctr->err if any a[i] >= limit.
 void launch_check_ids(const uint32_t *a, size_t n, uint32_t limit, Counters *ctr, cudaStream_t s);
 void launch_modularity(const Level &g, const uint32_t *memb, double *ctot64, Counters *ctr, cudaStream_t s);
@@ -471,6 +531,28 @@ void launch_relayout_rows(const uint64_t *old_off, const uint32_t *deg, const ui
 // Chunked path of the largest vertices: per colour, one kernel aggregates
 // the chunks, a second merges each hub's chunks and moves it.
 void launch_move_hubs(bool sync, const MoveArgs &a, cudaStream_t s);
+// Resident hub tables. Building (from membership q, for the hubs of plan P of
+// the uploaded level): each chunk of a hub's edges counts its communities in
+// shared memory and adds them to the hub's scratch table (2^slg[h] >= 2 deg
+// slots at soff[h]); ht_count gives each hub's distinct communities; ht_fill
+// copies each scratch table into the hub's table of the final layout.
+void launch_ht_slots(const uint32_t *hubs, size_t n, uint32_t *slot, cudaStream_t s);
+void launch_ht_scratch(const Level &lv, const uint32_t *q, const uint32_t *slot, const uint64_t *soff,
+                       const uint8_t *slg, uint32_t *skey, uint32_t *scnt, Counters *ctr, cudaStream_t s);
+void launch_ht_count(size_t hubs, const uint64_t *soff, const uint8_t *slg, const uint32_t *skey, uint32_t *n,
+                     cudaStream_t s);
+void launch_ht_fill(size_t hubs, const uint64_t *soff, const uint8_t *slg, const uint32_t *skey,
+                    const uint32_t *scnt, const HubTabView &t, cudaStream_t s);
+// Deterministic mode: the table updates of a colour class's decided moves
+// (dec[u] != EMPTY), before they are applied (vcom still holds the old
+// communities).
+void launch_ht_sync_moves(const Level &lv, const uint32_t *list, size_t n, const uint32_t *dec, const uint32_t *vcom,
+                          const HubTabView &t, Counters *ctr, cudaStream_t s);
+// A tidied batch's edges (src[i], dst[i]) on the tables of hubs src[i], with
+// the membership q the tables describe: deletions (insert = false) lower the
+// count of q[dst], insertions raise it.
+void launch_ht_batch(const uint32_t *src, const uint32_t *dst, size_t n, bool insert, const uint32_t *q,
+                     const HubTabView &t, Counters *ctr, cudaStream_t s);
 // dst[i] = src[idx[i]]
 void launch_gather_u32(const uint32_t *idx, size_t n, const uint32_t *src, uint32_t *dst, cudaStream_t s);
 

@@ -1072,15 +1072,24 @@ void launch_clear_isolated_endpoints(const uint32_t *a, size_t na, const uint32_
   LVG_CHECK_LAUNCH();
 }
 
-__global__ void iter_end_kernel(Counters *ctr, double M, double E, int L, cudaGraphConditionalHandle h) {
-  const double el = double(ctr->el_fix) / GAIN_FIX / M;
-  ctr->dev_el = el;
+__global__ void iter_end_kernel(Counters *ctr, double M, double E, int L, bool by_graph,
+                                cudaGraphConditionalHandle h) {
   const unsigned l = ++ctr->dev_iters;
-  cudaGraphSetConditional(h, (el > E && l < unsigned(L) && !ctr->err) ? 1u : 0u);
+  bool more;
+  if (by_graph) {  // graph unions: iter_control_kernel ran each graph's test
+    ctr->dev_el = 0;
+    more = ctr->gactive != 0;
+  } else {
+    const double el = double(ctr->el_fix) / GAIN_FIX / M;
+    ctr->dev_el = el;
+    more = el > E;
+  }
+  cudaGraphSetConditional(h, (more && l < unsigned(L) && !ctr->err) ? 1u : 0u);
 }
 
-void launch_iter_end(Counters *ctr, double M, double E, int L, cudaGraphConditionalHandle h, cudaStream_t s) {
-  iter_end_kernel<<<1, 1, 0, s>>>(ctr, M, E, L, h);
+void launch_iter_end(Counters *ctr, double M, double E, int L, bool by_graph, cudaGraphConditionalHandle h,
+                     cudaStream_t s) {
+  iter_end_kernel<<<1, 1, 0, s>>>(ctr, M, E, L, by_graph, h);
   LVG_CHECK_LAUNCH();
 }
 

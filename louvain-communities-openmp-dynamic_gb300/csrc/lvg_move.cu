@@ -275,7 +275,10 @@ __device__ __forceinline__ void tile_loop(const MoveArgs &a, const uint32_t *lis
       uint8_t *mk = SYNC ? a.mark : a.vaff;
       for (uint32_t j = tl; j < dg; j += T) {
         const uint32_t v = __ldcs(a.key + o + j);
-        if (v != u) mk[v] = 1;
+        if (v != u) {
+          mk[v] = 1;
+          if (!SYNC && a.ht.key) ht_move(a.ht, v, d, bc, a.ctr);
+        }
       }
     }
     if (tl == 0) {
@@ -660,7 +663,10 @@ __global__ void __launch_bounds__(B) move_big_kernel(MoveArgs a) {
       uint8_t *mk = SYNC ? a.mark : a.vaff;
       for (uint32_t j = threadIdx.x; j < dg; j += B) {
         const uint32_t v = __ldcs(a.key + o + j);
-        if (v != u) mk[v] = 1;
+        if (v != u) {
+          mk[v] = 1;
+          if (!SYNC && a.ht.key) ht_move(a.ht, v, d, bc, a.ctr);
+        }
       }
     }
     if (threadIdx.x == 0) {
@@ -703,7 +709,8 @@ __global__ void __launch_bounds__(B) hub_chunk_kernel(MoveArgs a) {
   const uint4 ch = a.hub.chunk[ci];
   const uint32_t u = ch.w;  // the hub vertex
   if (threadIdx.x == 0) {
-    s_act = a.vaff[u] && (!a.fa || a.fa[u]) && (!a.gact || a.gact[a.gid[u]]);
+    s_act = a.vaff[u] && (!a.fa || a.fa[u]) && (!a.gact || a.gact[a.gid[u]]) &&
+            !(a.ht.key && !a.ht.bad[a.ht.slot[u]]);  // a hub with a good table is done by hub_table_kernel
     s_used = 0;
     s_over = 0;
     s_cnt = 0;
@@ -874,9 +881,9 @@ __global__ void hub_argmax_kernel(MoveArgs a) {
 // decision), the neighbours marked, the hub's own flag cleared.
 template <int B, bool SYNC>
 __device__ __forceinline__ void hub_decide(const MoveArgs &a, const GraphOf &G, uint32_t u, uint32_t d, uint32_t dg,
-                                           double wu, float bg, uint32_t bc, bool over, unsigned long long &fix,
-                                           unsigned long long &nv, unsigned long long &ne, unsigned long long &nm,
-                                           unsigned long long &no) {
+                                           uint32_t scanned, double wu, float bg, uint32_t bc, bool over,
+                                           unsigned long long &fix, unsigned long long &nv, unsigned long long &ne,
+                                           unsigned long long &nm, unsigned long long &no) {
   const bool moved = bc != EMPTY && bc != G.zero;
   if (threadIdx.x == 0) {
     a.hub_kd[u] = 0.f;
@@ -896,13 +903,16 @@ __device__ __forceinline__ void hub_decide(const MoveArgs &a, const GraphOf &G, 
     const uint64_t o = a.off[u];
     for (uint32_t j = threadIdx.x; j < dg; j += B) {
       const uint32_t v = __ldcs(a.key + o + j);
-      if (v != u) mk[v] = 1;
+      if (v != u) {
+        mk[v] = 1;
+        if (!SYNC && a.ht.key) ht_move(a.ht, v, d, bc, a.ctr);
+      }
     }
   }
   if (threadIdx.x == 0) {
     a.vaff[u] = 0;
     ++nv;
-    ne += dg;
+    ne += scanned;
     nm += moved;
     no += over;
   }
@@ -965,7 +975,7 @@ __global__ void __launch_bounds__(B) hub_merge_kernel(MoveArgs a) {
       const float bg = best ? __uint_as_float(uint32_t(best >> 32)) : 0.f;
       const uint32_t bc = best ? 0xFFFFFFFFu - uint32_t(best) : EMPTY;
       __syncthreads();  // every thread has read the best before it is reset
-      hub_decide<B, SYNC>(a, G, u, d, dg, a.vtot[u], bg, bc, false, fix, nv, ne, nm, no);
+      hub_decide<B, SYNC>(a, G, u, d, dg, dg, a.vtot[u], bg, bc, false, fix, nv, ne, nm, no);
       if (threadIdx.x == 0) { a.hub_over[g] = 0; a.hub_best[g] = 0; }
       __syncthreads();
       continue;
@@ -1033,12 +1043,68 @@ __global__ void __launch_bounds__(B) hub_merge_kernel(MoveArgs a) {
     }
     block_argmax<B>(bg, bc, red_g, red_c);
     if (!over) lt_reset<B>(t, nlist);
-    hub_decide<B, SYNC>(a, G, u, d, dg, wu, bg, bc, over, fix, nv, ne, nm, no);
+    hub_decide<B, SYNC>(a, G, u, d, dg, dg, wu, bg, bc, over, fix, nv, ne, nm, no);
     if (threadIdx.x == 0) a.hub_over[g] = 0;
     bad |= !ok;
     __syncthreads();
   }
   flush_counters(a.ctr, a.bin, fix, nv, ne, nm, bad, no);
+}
+
+// Hub path with resident tables (MoveArgs::ht): one block per hub of the
+// colour class (grid-stride) whose table is good. The candidates are the
+// table's communities with a nonzero count, k_d is the own community's count,
+// and the move is taken as on the chunked path (hub_decide), which also
+// brings the tables of the hub's neighbours that are hubs up to date. No edge
+// of the hub is read unless it moves. A hub whose table is bad is left to the
+// chunked path, launched after this kernel.
+template <int B, bool SYNC>
+__global__ void __launch_bounds__(B) hub_table_kernel(MoveArgs a) {
+  __shared__ float red_g[B / 32];
+  __shared__ uint32_t red_c[B / 32];
+  __shared__ int s_go;
+  __shared__ float s_kd;
+  const size_t h0 = a.hub.hub_begin[a.color], h1 = a.hub.hub_begin[a.color + 1];
+  unsigned long long fix = 0, nv = 0, ne = 0, nm = 0, no = 0, slots = 0;
+  for (size_t g = h0 + blockIdx.x; g < h1; g += gridDim.x) {
+    const uint32_t u = a.hub.hub_vertex[g];
+    if (threadIdx.x == 0) {
+      const uint32_t h = a.ht.slot[u];
+      s_go = a.vaff[u] && (!a.fa || a.fa[u]) && h != NO_HUB && !a.ht.bad[h];
+      s_kd = 0.f;
+    }
+    __syncthreads();
+    const bool go = s_go;
+    if (go) {
+      const GraphOf G(a, u);
+      const uint32_t h = a.ht.slot[u];
+      const uint32_t d = a.vcom[u];
+      const uint64_t o = a.ht.off[h];
+      const uint32_t n = 1u << a.ht.lg[h];
+      for (uint32_t s2 = threadIdx.x; s2 < n; s2 += B)
+        if (a.ht.key[o + s2] == d) s_kd = float(a.ht.cnt[o + s2]);
+      __syncthreads();
+      const float kd = s_kd;
+      const double wu = a.vtot[u], td = a.ctot[d];
+      const float wuf = __double2float_rn(wu);
+      float bg = 0.f;
+      uint32_t bc = EMPTY;
+      for (uint32_t s2 = threadIdx.x; s2 < n; s2 += B) {
+        const uint32_t c = a.ht.key[o + s2];
+        if (c == EMPTY || c == d) continue;
+        const uint32_t k = a.ht.cnt[o + s2];
+        if (!k) continue;
+        const float g2 = gain_of(float(k), kd, wu, wuf, a.ctot[c], td, G.kr);
+        if (g2 > 0.f) take_better(bg, bc, g2, c);
+      }
+      block_argmax<B>(bg, bc, red_g, red_c);
+      hub_decide<B, SYNC>(a, G, u, d, a.deg[u], 0, wu, bg, bc, false, fix, nv, ne, nm, no);
+      if (threadIdx.x == 0) slots += n;
+    }
+    __syncthreads();
+  }
+  flush_counters(a.ctr, NUM_BINS - 1, fix, nv, ne, nm, false, no);
+  if (threadIdx.x == 0 && slots) atomicAdd(&a.ctr->ht_slots, slots);
 }
 
 int num_sms() {  // SM count of the device, queried once (thread-safe static init)
@@ -1094,6 +1160,7 @@ constexpr int BIG10_B = 256, BIG10_LOGS = 11;   // degree 2049-8192
 constexpr int HUBC_B = 256, HUBC_LOGS = 11;     // hub chunks (lvg_tuning::hub_chunk edges each)
 constexpr int HUBM_B = 512, HUBM_LOGS = 13;     // hub merge
 constexpr int HUBS_B = 256;                     // hub spill
+constexpr int HUBT_B = 128;                     // resident hub tables
 
 // Resident blocks of a large-degree kernel on the whole device, queried once.
 template <class K>
@@ -1134,6 +1201,10 @@ void launch_hubs(const MoveArgs &a, cudaStream_t s) {
   auto k2 = hub_merge_kernel<HUBM_B, HUBM_LOGS, SYNC>;
   static bool configured = false;
   if (!configured) { set_smem(k1, smem1); set_smem(k2, smem2); configured = true; }
+  if (a.ht.key) {
+    hub_table_kernel<HUBT_B, SYNC><<<unsigned(std::min<size_t>(nh, size_t(num_sms()) * 8)), HUBT_B, 0, s>>>(a);
+    LVG_CHECK_LAUNCH();
+  }
   k1<<<unsigned(nch), HUBC_B, smem1, s>>>(a);
   LVG_CHECK_LAUNCH();
   if (a.spill_keys) {

@@ -102,7 +102,8 @@ class _ServerStats(C.Structure):
 
 class _Tuning(C.Structure):
     _fields_ = [("frontier_colors", C.c_int), ("concurrent_bins", C.c_int), ("fused_small", C.c_int),
-                ("hub_chunk", C.c_uint32), ("big_blocks_per_sm", C.c_int), ("frontier_max_fraction", C.c_double)]
+                ("hub_chunk", C.c_uint32), ("big_blocks_per_sm", C.c_int), ("frontier_max_fraction", C.c_double),
+                ("hub_tables", C.c_int)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -116,7 +117,8 @@ class _Stats(C.Structure):
                 ("move_bin_vertices", C.c_uint64 * 12), ("move_bin_edges", C.c_uint64 * 12),
                 ("call_upload_ms", C.c_double), ("call_run_ms", C.c_double), ("call_download_ms", C.c_double),
                 ("move_bin_overflow", C.c_uint64 * 12), ("hub_chunk_overflow", C.c_uint64),
-                ("host_syncs", C.c_uint64)]
+                ("hub_table_slots", C.c_uint64), ("hub_table_overflow", C.c_uint64),
+                ("hub_tables_built", C.c_uint64), ("host_syncs", C.c_uint64)]
 
 
 class _Csr(C.Structure):

@@ -13,7 +13,7 @@ import pytest
 def test_tuning_defaults(lvg):
     t = lvg.tuning_default()
     assert t == dict(frontier_colors=8, concurrent_bins=1, fused_small=0, hub_chunk=4096, big_blocks_per_sm=0,
-                     frontier_max_fraction=1e-3)
+                     frontier_max_fraction=1e-3, hub_tables=1)
 
 
 @pytest.fixture(scope="module")

@@ -96,3 +96,35 @@ def test_union_is_static_only(cuda):
         U.apply_batch(b)
     with pytest.raises(RuntimeError):
         cuda.Graph.union([U])
+
+
+def test_deterministic_union_matches_cpu_replay(cuda, orc):
+    """Each graph of a deterministic union against the oracle's CPU replay of
+    the same rule on that graph alone, bit for bit."""
+    gs = _mix(cuda)
+    o = cuda.LouvainOptions(deterministic=True)
+    U = cuda.Graph.union([cuda.Graph(g) for g in gs])
+    rs = cuda.louvain_static_union(U, o)
+    for i, g in enumerate(gs):
+        m, vt, ct, info = orc.louvain(g, 0, threads=4, sync=True, colors=o.effective_colors())
+        assert np.array_equal(rs[i].membership, m), i
+        assert np.array_equal(rs[i].vertexWeight, vt), i
+        assert np.array_equal(rs[i].communityWeight, ct), i
+        assert (rs[i].iterations, rs[i].passes, rs[i].affectedVertices) == (
+            info["iterations"], info["passes"], info["affectedVertices"]), i
+
+
+def test_union_phase_replay(cuda):
+    """The union's first local-moving phase is captured on the first call and
+    replayed as one graph (a conditional while node over every graph's stop
+    test) on later calls: the same results, fewer host synchronisations."""
+    gs = _mix(cuda)
+    o = cuda.LouvainOptions(deterministic=True)
+    U = cuda.Graph.union([cuda.Graph(g) for g in gs])
+    first = cuda.louvain_static_union(U, o)
+    s0 = U.stats()["host_syncs"]
+    for _ in range(2):
+        again = cuda.louvain_static_union(U, o)
+        for i in range(len(gs)):
+            _same(again[i], first[i], i)
+    assert U.stats()["host_syncs"] < s0
