@@ -49,6 +49,17 @@ METRIC = "DF-Louvain edges/s, HBM GB/s, p99 update latency vs plain GPU at |ΔQ|
 MOVE_BYTES_PER_EDGE = 12   # neighbour id + weight + neighbour's community
 MOVE_BYTES_PER_EDGE_UNIT = 8  # the same when every weight is 1: the kernels read no weights
 MOVE_BYTES_PER_VERTEX = 25  # offset (8) + degree (4) + community (4) + FP64 vertex weight (8) + flag (1)
+HUB_TABLE_BYTES_PER_SLOT = 8  # community (4) + neighbour count (4) of a resident hub table
+# the local-moving launches by degree bin: (name, bins); the fused small-bin
+# launches time under their first bin
+MOVE_GROUPS = [
+    ("degree 1-128 (move_small_kernel<1,6> or move_tile_kernel bins 1-6)", [1, 2, 3, 4, 5, 6]),
+    ("degree 129-512 (move_small_kernel<7,8> or move_tile_kernel bins 7-8)", [7, 8]),
+    ("degree 513-2048 (move_big_kernel, bin 9)", [9]),
+    ("degree 2049-8192 (move_big_kernel, bin 10)", [10]),
+    ("degree above 8192 (hub_table_kernel on resident tables; hub_chunk_kernel + hub_merge_kernel for the rest)",
+     [11]),
+]
 
 
 def move_bytes_per_edge(g) -> int:
@@ -532,7 +543,10 @@ def run_gpu(args):
     if args.ncu_steps:
         meth = {"static": lvg.METHOD_STATIC, "nd": lvg.METHOD_NAIVE, "ds": lvg.METHOD_DELTA,
                 "df": lvg.METHOD_FRONTIER}[args.ncu_method]
-        lvg.run_resident(Y, meth, db, st_prior, st_out, o)  # warm: graph capture
+        # launches one by one (no CUDA graphs: ncu lists the kernels of a
+        # graph's conditional node only as the graph), as ncu serialises them anyway
+        Y.set_profiling(True)
+        lvg.run_resident(Y, meth, db, st_prior, st_out, o)  # warm-up
         lvg.profiler_start()
         for _ in range(args.ncu_steps):
             info = lvg.run_resident(Y, meth, db, st_prior, st_out, o)
@@ -571,7 +585,7 @@ def run_gpu(args):
     dist.barrier()
     # the same steps again with per-launch events around the local-moving kernels (roofline)
     Y.set_profiling(True)
-    kms, kedges, kverts, klaunch = 0.0, 0, 0, 0
+    kms, kedges, kverts, klaunch, kslots = 0.0, 0, 0, 0, 0
     bin_ms, bin_edges, bin_verts = np.zeros(12), np.zeros(12), np.zeros(12)
     for _ in range(args.steps):
         lvg.run_resident(Y, lvg.METHOD_FRONTIER, db, st_prior, st_out, o)
@@ -580,6 +594,7 @@ def run_gpu(args):
         kedges += s["move_edges"]
         kverts += s["move_vertices"]
         klaunch += s["move_launches"]
+        kslots += s["hub_table_slots"]
         bin_ms += np.array(s["move_bin_ms"])
         bin_edges += np.array(s["move_bin_edges"])
         bin_verts += np.array(s["move_bin_vertices"])
@@ -615,18 +630,30 @@ def run_gpu(args):
     peak, peak_kind = peaks()
     achieved = None
     bpe = move_bytes_per_edge(y)
-    alg_per_step = (bpe * kedges + MOVE_BYTES_PER_VERTEX * kverts) / args.steps
+    alg_per_step = (bpe * kedges + MOVE_BYTES_PER_VERTEX * kverts + HUB_TABLE_BYTES_PER_SLOT * kslots) / args.steps
     if kms > 0:
         # bytes and time of all local-moving launches of the profiled steps
         achieved = alg_per_step / (kms / args.steps / 1e3) / 1e9
     tr = traffic_per_launch()
     traffic = int(tr["traffic_ratio"] * alg_per_step) if tr and "traffic_ratio" in tr else None
-    # the dominant kernel: the hub path (hub_chunk_kernel + hub_merge_kernel, the
-    # vertices above degree 8192), timed by the events around its two launches
-    hub_ms = bin_ms[11] / args.steps
-    hub_alg = (bpe * bin_edges[11] + MOVE_BYTES_PER_VERTEX * bin_verts[11]) / args.steps
-    hub_achieved = hub_alg / (hub_ms / 1e3) / 1e9 if hub_ms > 0 else None
-    hub_traffic = int(tr["hub_traffic_ratio"] * hub_alg) if tr and "hub_traffic_ratio" in tr else None
+    # the dominant kernel: the launch group of the degree bins with the largest
+    # time in the profiled steps (events around each launch). Its algorithmic
+    # bytes: per scanned edge and processed vertex as above, plus 8 B per
+    # hub-table slot read (community + count) for the vertices above degree 8192
+    groups = []
+    for name, bins in MOVE_GROUPS:
+        gms = sum(bin_ms[k] for k in bins) / args.steps
+        galg = sum(bpe * bin_edges[k] + MOVE_BYTES_PER_VERTEX * bin_verts[k] for k in bins) / args.steps
+        if 11 in bins:
+            galg += HUB_TABLE_BYTES_PER_SLOT * kslots / args.steps
+        groups.append((gms, galg, name, bins))
+    dom_ms, dom_alg, dom_name, dom_bins = max(groups)
+    dom_achieved = dom_alg / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else None
+    ratios = (tr or {}).get("group_traffic_ratio", {})
+    dom_key = "-".join(str(k) for k in (dom_bins[0], dom_bins[-1]))
+    if kslots:
+        dom_key += "-tables" if 11 in dom_bins else ""
+    dom_traffic = int(ratios[dom_key]["ratio"] * dom_alg) if dom_key in ratios else None
     line = {
         "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
@@ -641,29 +668,31 @@ def run_gpu(args):
         "gpu_launches": launches,
         "host_syncs_per_step": syncs / args.steps,
         "df_passes_iterations": [info["passes"], info["iterations"]],
-        "roofline": {"bound": "hbm", "achieved": hub_achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (hub_achieved / peak) if hub_achieved else None,
-                     "traffic": hub_traffic,
-                     "kernel": "hub path of the vertices above degree 8192 (hub_chunk_kernel + hub_merge_kernel, "
-                               "one launch each per colour class): the step's largest kernel time",
-                     "algorithmic_bytes_per_step": int(hub_alg), "ms_per_step": hub_ms,
-                     "traffic_note": ("DRAM bytes of the hub pair per step: their ratio to its algorithmic bytes in "
-                                      "an ncu capture (" + tr.get("measured_on", "") + "; profiles/move_traffic.json) "
-                                      "times this step's algorithmic bytes: a lower bound at scale 24, where the "
-                                      "community gathers hit L2 less often than at scale 22")
-                                     if hub_traffic else None,
+        "roofline": {"bound": "hbm", "achieved": dom_achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (dom_achieved / peak) if dom_achieved else None,
+                     "traffic": dom_traffic,
+                     "kernel": dom_name + ": the step's largest kernel time among the local-moving launches",
+                     "algorithmic_bytes_per_step": int(dom_alg), "ms_per_step": dom_ms,
+                     "traffic_note": ("DRAM bytes of this launch group per step: its ratio to its algorithmic bytes "
+                                      "in an ncu capture (" + ratios[dom_key].get("measured_on", "") +
+                                      "; profiles/move_traffic.json) times this step's algorithmic bytes")
+                                     if dom_traffic else None,
                      "peak_kind": peak_kind,
                      "algorithmic_bytes": f"{bpe} B/scanned edge (neighbour id + its community"
                                           + (", no weight: every weight is 1)" if bpe == 8 else " + weight)")
-                                          + f" + {MOVE_BYTES_PER_VERTEX} B/processed vertex",
+                                          + f" + {MOVE_BYTES_PER_VERTEX} B/processed vertex"
+                                          + f" + {HUB_TABLE_BYTES_PER_SLOT} B/hub-table slot read",
+                     "groups_ms_per_step": {name: round(gms, 4) for gms, _, name, _ in groups},
+                     "hub_table_slots_per_step": kslots / args.steps,
                      "all_local_moving": {
                          "achieved": achieved, "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                          "algorithmic_bytes_per_step": int(alg_per_step),
-                         "kernels": "every degree bin (move_tile/move_small/move_big/hub_chunk/hub_merge), "
+                         "kernels": "every degree bin (move_tile/move_small/move_big/hub_table/hub_chunk/hub_merge), "
                                     "durations summed as profiled one after another",
                          "launches_per_step": klaunch / args.steps, "ms_per_step": kms / args.steps,
                          "per_bin_ms_per_step": [round(v / args.steps, 4) for v in bin_ms],
-                         "per_bin_edges_per_step": [int(v / args.steps) for v in bin_edges]}},
+                         "per_bin_edges_per_step": [int(v / args.steps) for v in bin_edges],
+                         "per_bin_vertices_per_step": [int(v / args.steps) for v in bin_verts]}},
         "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
         "batch_apply_ms": {"p50": float(np.percentile(apply_ms, 50)), "max": float(np.max(apply_ms)),
                            "call": "lvg_graph_apply_device_batch (tidy + apply in HBM, host wall clock)"},

@@ -430,9 +430,10 @@ typedef struct lvg_tuning {
   int      frontier_colors;    /* colour classes of DF and DS when lvg_options.colors == 0
                                   and deterministic == 0 (default 8) */
   int      concurrent_bins;    /* 1: a class's degree bins run concurrently on side streams (default 1) */
-  int      fused_small;        /* 1: the frontier methods' first pass runs bins 1-8 as two launches
-                                  per class (default 0: with the iterations replayed as CUDA
-                                  graphs the separate launches were faster on R-MAT s24) */
+  int      fused_small;        /* the frontier methods' first pass runs bins 1-8 as two launches per
+                                  class: 0 no (separate launches), 1 yes with the method's blocks per
+                                  SM and bin (2 for DF's short worklists, 8 for delta-screening's whole
+                                  communities), k >= 2 yes with k (default 0) */
   uint32_t hub_chunk;          /* edges per chunk of a vertex above degree 8192 (256..1<<20; default 4096) */
   int      big_blocks_per_sm;  /* resident blocks per SM of the degree 513-8192 kernels (0 = as many
                                   as fit; default 0) */

@@ -71,6 +71,7 @@ void check_tuning(const lvg_tuning &t) {
   if (!(t.frontier_max_fraction >= 0 && t.frontier_max_fraction <= 1))
     throw Error(LVG_EINVAL, "tuning: frontier_max_fraction out of 0..1");
   if (t.hub_tables != 0 && t.hub_tables != 1) throw Error(LVG_EINVAL, "tuning: hub_tables is 0 or 1");
+  if (t.fused_small < 0 || t.fused_small > 64) throw Error(LVG_EINVAL, "tuning: fused_small out of 0..64");
 }
 
 // Set a graph's tuning: the hub plan of the uploaded level follows the chunk
@@ -1089,7 +1090,13 @@ int lvg_autotune(lvg_graph *g, int method, const lvg_device_batch *b, const lvg_
       // with concurrent and unfused, 0.78 ms for the best of one at a time)
       try_knob([](lvg_tuning &t, long v) { t.concurrent_bins = int(v >> 1); t.fused_small = int(v & 1); },
                {3, 2, 1, 0}, false);
+      // fused: its blocks per SM and bin (the worklists' lengths vary with the batch)
+      if (cur.fused_small) try_knob([](lvg_tuning &t, long v) { t.fused_small = int(v); }, {1, 4, 8, 16}, false);
       try_knob([](lvg_tuning &t, long v) { t.big_blocks_per_sm = int(v); }, {0, 2, 3, 4}, false);
+      // resident hub tables: a large saving where few vertices move (DF), a
+      // cost where millions do (each move updates its hub neighbours' tables)
+      if (prior && method != LVG_METHOD_STATIC)
+        try_knob([](lvg_tuning &t, long v) { t.hub_tables = int(v); }, {1, 0}, false);
     }
     // confirm the launch shapes against the starting ones (with the chosen
     // class count), measured in turn, since a sub-millisecond run drifts

@@ -320,6 +320,10 @@ void build_hub_tables(lvg_graph *g, const uint32_t *q, HubTables &T) {
     T.off.ensure(H + 1);
     T.lg.ensure(H);
     T.bad.ensure(H);
+    T.nbad.ensure(1);
+    uint32_t nb = 0;
+    for (size_t h = 0; h < H; ++h) nb += bad[h];
+    LVG_CUDA(cudaMemcpyAsync(T.nbad.p, &nb, 4, cudaMemcpyHostToDevice, s));
     T.key.ensure(T.slots);
     T.cnt.ensure(T.slots);
     LVG_CUDA(cudaMemcpyAsync(T.off.p, off.data(), (H + 1) * 8, cudaMemcpyHostToDevice, s));
@@ -344,6 +348,8 @@ void copy_hub_tables(lvg_graph *g, const HubTables &src, HubTables &dst) {
     dst.off.ensure(H + 1);
     dst.lg.ensure(H);
     dst.bad.ensure(H);
+    dst.nbad.ensure(1);
+    LVG_CUDA(cudaMemcpyAsync(dst.nbad.p, src.nbad.p, 4, cudaMemcpyDeviceToDevice, s));
     dst.key.ensure(src.slots);
     dst.cnt.ensure(src.slots);
     LVG_CUDA(cudaMemcpyAsync(dst.off.p, src.off.p, (H + 1) * 8, cudaMemcpyDeviceToDevice, s));
@@ -653,12 +659,15 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const 
   const bool base = lv.off == g->base.off;
   IterKey key{};
   if (base) {
-    const void *ps[32] = {W.spill_now ? W.spill_keys.p : nullptr, lv.off, lv.bins, com, ctot, tot, fa, W.vaff.p,
+    const void *ps[34] = {W.spill_now ? W.spill_keys.p : nullptr, lv.off, lv.bins, com, ctot, tot, fa, W.vaff.p,
                           W.mark.p, W.dec.p, W.wl.p, W.wl_count.p,
                           W.gkeys.p, W.gvals.p, W.chunk_cnt.p, W.part_key.p, W.part_val.p, W.hub_kd.p, g->ctr.p,
                           g->hctr.p, lv.hub.chunk, lv.hub.hub_vertex, lv.gid,
                           W.spill_now ? W.spill_vals.p : nullptr, W.hub_over.p, W.hub_best.p, lv.deg,
-                          W.ht_now.key, W.ht_now.slot, W.ht_now.cnt, W.ht_now.off, W.ht_now.bad};
+                          // every buffer of the resident hub tables (a state's tables are
+                          // separate allocations: one may move while the others stay)
+                          W.ht_now.key, W.ht_now.slot, W.ht_now.cnt, W.ht_now.off, W.ht_now.nbad,
+                          W.ht_now.lg, W.ht_now.bad};
     std::memcpy(key.p, ps, sizeof(ps));
     key.n[0] = lv.span; key.n[1] = need; key.n[2] = lv.hub.chunks; key.n[3] = lv.bin_start[K * NUM_BINS];
     key.k[0] = K; key.k[1] = sync | int(lv.unit) << 1; key.k[2] = glog2[9] | glog2[10] << 8 | glog2[11] << 16;
@@ -967,10 +976,11 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
       // worklists (2) or for delta-screening's whole communities (8: with
       // two, its first pass took 2.8x as long on a 4M-vertex graph of
       // average degree 87)
-      const int fused = !first || !g->tuning.fused_small ? 0
+      const int tf = g->tuning.fused_small;
+      const int fused = !first || !tf || (method != LVG_METHOD_FRONTIER && method != LVG_METHOD_DELTA) ? 0
+                        : tf >= 2                        ? tf
                         : method == LVG_METHOD_FRONTIER  ? 2
-                        : method == LVG_METHOD_DELTA     ? 8
-                                                         : 0;
+                                                         : 8;
       const DBatch *ends = first && method == LVG_METHOD_FRONTIER ? &b : nullptr;
       // the end of the run, enqueued ahead of the first pass's one
       // synchronisation: if the run ends after this pass (as a frontier run

@@ -139,7 +139,7 @@ struct DBatch {
 struct HubTables {
   DBuf<uint64_t> off;
   DBuf<uint8_t> lg, bad;
-  DBuf<uint32_t> key, cnt;
+  DBuf<uint32_t> key, cnt, nbad;
   size_t hubs = 0, slots = 0;
   uint64_t version = ~0ull, index = ~0ull;
   HubTabView view(const uint32_t *slot) const {
@@ -150,6 +150,7 @@ struct HubTables {
     v.key = key.p;
     v.cnt = cnt.p;
     v.bad = bad.p;
+    v.nbad = nbad.p;
     return v;
   }
 };
@@ -157,7 +158,7 @@ struct HubTables {
 // Everything an iteration's launches depend on; a captured iteration is
 // replayed only while all of it is unchanged.
 struct IterKey {
-  const void *p[32];
+  const void *p[34];
   size_t n[4];
   int k[4];
   float kr;

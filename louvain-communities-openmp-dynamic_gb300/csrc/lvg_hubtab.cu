@@ -131,7 +131,7 @@ __global__ void ht_fill_kernel(size_t hubs, const uint64_t *soff, const uint8_t 
     uint32_t *k = t.key + t.off[h], *c = t.cnt + t.off[h];
     for (uint32_t s = threadIdx.x; s < cap; s += blockDim.x) {
       const uint32_t x = skey[o + s];
-      if (x != EMPTY && !cnt_add(k, c, t.lg[h], x, scnt[o + s])) t.bad[h] = 1;
+      if (x != EMPTY && !cnt_add(k, c, t.lg[h], x, scnt[o + s])) ht_mark_bad(t, uint32_t(h));
     }
   }
 }
@@ -172,7 +172,7 @@ __global__ void ht_batch_kernel(const uint32_t *src, const uint32_t *dst, size_t
     const uint32_t mask = (1u << lg) - 1u;
     if (insert) {
       if (!cnt_add(k, cn, lg, c, 1u)) {
-        t.bad[h] = 1;
+        ht_mark_bad(t, h);
         atomicAdd(&ctr->ht_over, 1ull);
       }
     } else {
@@ -185,7 +185,7 @@ __global__ void ht_batch_kernel(const uint32_t *src, const uint32_t *dst, size_t
         s = (s + 1u) & mask;
       }
       if (!found) {
-        t.bad[h] = 1;
+        ht_mark_bad(t, h);
         atomicAdd(&ctr->ht_over, 1ull);
       }
     }

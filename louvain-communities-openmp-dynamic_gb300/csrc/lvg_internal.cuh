@@ -182,7 +182,16 @@ struct HubTabView {
   uint32_t *key = nullptr;         // community, EMPTY
   uint32_t *cnt = nullptr;         // neighbours in it
   uint8_t *bad = nullptr;          // [hubs]
+  uint32_t *nbad = nullptr;        // hubs marked bad (never lowered while the tables live)
 };
+
+// Mark hub h's table bad: the count first, so that whoever sees the mark
+// also sees a nonzero count.
+__device__ __forceinline__ void ht_mark_bad(const HubTabView &t, uint32_t h) {
+  atomicAdd(t.nbad, 1u);
+  __threadfence();
+  t.bad[h] = 1;
+}
 
 // Hub v's table after a neighbour moved from community `from` to `to` (a no-op
 // when v is not a hub or its table is marked bad). `from` is present: it is
@@ -213,7 +222,7 @@ __device__ __forceinline__ void ht_move(const HubTabView &t, uint32_t v, uint32_
     s = (s + 1u) & mask;
   }
   if (!found || !placed) {
-    t.bad[h] = 1;
+    ht_mark_bad(t, h);
     atomicAdd(&ctr->ht_over, 1ull);
   }
 }

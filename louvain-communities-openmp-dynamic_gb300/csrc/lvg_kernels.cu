@@ -735,15 +735,26 @@ __global__ void compact_active_scan_kernel(const uint32_t *deg, const uint8_t *e
                                            uint32_t *wl_count, unsigned int *err) {
   const int lane = threadIdx.x & 31;
   const size_t words = (span + 15) / 16;
-  for (size_t wbase = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32 * 32; wbase < words;
-       wbase += size_t(gridDim.x) * blockDim.x) {
-    const size_t w = wbase + lane;
-    unsigned act = 0;  // bit j: vertex 16 w + j is active
-    if (w < words) {
+  // a warp takes WPL * 32 consecutive words, their flag loads issued
+  // together; bit 16 k + j of a lane's mask: vertex 16 (wbase + 32 k + lane) + j
+  constexpr int WPL = 4;
+  for (size_t wbase = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32 * 32 * WPL; wbase < words;
+       wbase += size_t(gridDim.x) * blockDim.x * WPL) {
+    uint4 pre[WPL];
+#pragma unroll
+    for (int k = 0; k < WPL; ++k) {
+      const size_t w = wbase + size_t(k) * 32 + lane;
+      pre[k] = w < words && w * 16 + 16 <= span ? reinterpret_cast<const uint4 *>(vaff)[w] : make_uint4(0, 0, 0, 0);
+    }
+    unsigned long long act = 0;
+#pragma unroll
+    for (int k = 0; k < WPL; ++k) {
+      const size_t w = wbase + size_t(k) * 32 + lane;
+      if (w >= words) continue;
+      unsigned a16 = 0;
       const size_t u0 = w * 16;
       if (u0 + 16 <= span) {
-        const uint4 f = reinterpret_cast<const uint4 *>(vaff)[w];
-        const uint32_t fw[4] = {f.x, f.y, f.z, f.w};
+        const uint32_t fw[4] = {pre[k].x, pre[k].y, pre[k].z, pre[k].w};
         uint32_t ew[4] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu};
         uint32_t aw[4] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu};
         if ((fw[0] | fw[1] | fw[2] | fw[3]) && ex) {
@@ -758,20 +769,21 @@ __global__ void compact_active_scan_kernel(const uint32_t *deg, const uint8_t *e
         for (int j = 0; j < 16; ++j) {
           const uint32_t sh = 8u * (j & 3);
           if (((fw[j >> 2] >> sh) & 0xffu) && ((ew[j >> 2] >> sh) & 0xffu) && ((aw[j >> 2] >> sh) & 0xffu))
-            act |= 1u << j;
+            a16 |= 1u << j;
         }
       } else {
         for (size_t u = u0; u < span; ++u)
-          if (vaff[u] && (!ex || ex[u]) && (!fa || fa[u])) act |= 1u << (u - u0);
+          if (vaff[u] && (!ex || ex[u]) && (!fa || fa[u])) a16 |= 1u << (u - u0);
       }
+      act |= static_cast<unsigned long long>(a16) << (16 * k);
     }
-    while (__any_sync(0xffffffffu, act != 0u)) {
+    while (__any_sync(0xffffffffu, act != 0ull)) {
       int b = -1;
       uint32_t u = 0;
       if (act) {
-        const int j = __ffs(act) - 1;
-        act &= act - 1u;
-        u = uint32_t(w * 16 + j);
+        const int j = __ffsll(static_cast<long long>(act)) - 1;
+        act &= act - 1ull;
+        u = uint32_t((wbase + size_t(j >> 4) * 32 + lane) * 16 + (j & 15));
         const int x = degree_bin(deg[u]);
         if (x >= 1 && x <= NUM_BINS - 2) b = x;
       }
@@ -805,11 +817,18 @@ __global__ void count_flags_kernel(const uint8_t *f, size_t n, unsigned long lon
   unsigned long long c = 0;
   const size_t n16 = n / 16;
   const uint4 *f16 = reinterpret_cast<const uint4 *>(f);
-  GRID_STRIDE(i, n16) {
-    const uint4 v = f16[i];
-    c += __popc(__vcmpeq4(v.x, 0x01010101u)) / 8 + __popc(__vcmpeq4(v.y, 0x01010101u)) / 8 +
-         __popc(__vcmpeq4(v.z, 0x01010101u)) / 8 + __popc(__vcmpeq4(v.w, 0x01010101u)) / 8;
+  auto ones = [](const uint4 &v) {
+    return __popc(__vcmpeq4(v.x, 0x01010101u)) / 8 + __popc(__vcmpeq4(v.y, 0x01010101u)) / 8 +
+           __popc(__vcmpeq4(v.z, 0x01010101u)) / 8 + __popc(__vcmpeq4(v.w, 0x01010101u)) / 8;
+  };
+  // four loads in flight per thread
+  const size_t stride = size_t(gridDim.x) * blockDim.x;
+  size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  for (; i + 3 * stride < n16; i += 4 * stride) {
+    const uint4 v0 = f16[i], v1 = f16[i + stride], v2 = f16[i + 2 * stride], v3 = f16[i + 3 * stride];
+    c += ones(v0) + ones(v1) + ones(v2) + ones(v3);
   }
+  for (; i < n16; i += stride) c += ones(f16[i]);
   GRID_STRIDE(i, n - n16 * 16) c += f[n16 * 16 + i] == 1;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);

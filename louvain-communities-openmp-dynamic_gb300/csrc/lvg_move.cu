@@ -936,6 +936,12 @@ __global__ void __launch_bounds__(B) hub_merge_kernel(MoveArgs a) {
   t.vals = reinterpret_cast<float *>(smem + size_t(CS) * 4);
   t.list = reinterpret_cast<uint32_t *>(smem + size_t(CS) * 8);
   t.used = &s_used;
+  if (a.ht.key) {  // resident hub tables: nothing to merge while none is bad
+    if (threadIdx.x == 0) s_over = ld_relaxed(a.ht.nbad) != 0;
+    __syncthreads();
+    if (!s_over) return;
+    __syncthreads();
+  }
   for (uint32_t s2 = threadIdx.x; s2 < CS; s2 += B) { t.keys[s2] = EMPTY; t.vals[s2] = 0.f; }
   uint32_t *gkeys = a.gkeys ? a.gkeys + (size_t(blockIdx.x) << a.glog2) : nullptr;
   float *gvals = a.gvals ? a.gvals + (size_t(blockIdx.x) << a.glog2) : nullptr;

@@ -138,3 +138,29 @@ def test_static_run_invalidates_tables(cuda, base):
     ref = cuda.State(Y)
     cuda.run_resident(Y, cuda.METHOD_FRONTIER, db, st, ref, o)
     _same(out.get(), ref.get())
+
+
+def test_tables_with_fresh_result_states(cuda, base):
+    """Every call into a new result state (allocated and freed call by call,
+    so its buffers land at old or new addresses): the hubs are evaluated from
+    the tables on every call, and the results stay those of the first."""
+    x, r0 = base
+    Y, db = _graph_with_batch(cuda, x, 13)
+    o = cuda.LouvainOptions(deterministic=True)
+    prior = cuda.State(Y)
+    prior.set(r0.membership, r0.vertexWeight, r0.communityWeight)
+    first = None
+    keep = []
+    for k in range(8):
+        if k % 3 == 2:
+            keep.append(cuda.State(Y))  # shifts the next allocations
+        out = cuda.State(Y)
+        cuda.run_resident(Y, cuda.METHOD_FRONTIER, db, prior, out, o)
+        st = Y.stats()
+        assert st["hub_table_slots"] > 0 and st["move_bin_vertices"][11] > 0, (k, st["hub_table_slots"])
+        got = out.get()
+        if first is None:
+            first = got
+        else:
+            _same(first, got)
+        out.close()
