@@ -81,7 +81,7 @@ def parse():
     p.add_argument("--no-tune", action="store_true",
                    help="skip lvg_autotune (launch shapes and frontier colour classes) before the timed steps")
     p.add_argument("--cpu-steps", type=int, default=2)
-    p.add_argument("--workload", default="df", choices=["df", "sweep", "serving", "temporal", "batched"],
+    p.add_argument("--workload", default="df", choices=["df", "sweep", "serving", "temporal", "batched", "link"],
                    help="df: the headline (R-MAT scale 24, one graph); sweep: the same graph, batches of "
                         "1e-7..1e-1 |E|, all four methods; serving: many resident graphs under "
                         "Poisson batch-update arrivals through lvg_server; temporal: a drifting-community "
@@ -514,7 +514,10 @@ def run_gpu(args):
         knobs = {}
         for kv in args.set_tuning.split(","):
             k, v = kv.split("=")
-            knobs[k.strip()] = float(v) if k.strip() == "frontier_max_fraction" else int(v)
+            k = k.strip()
+            # bin_max_degree=a:b:c...: the degree bins' limits from bin 0 on
+            knobs[k] = (float(v) if k == "frontier_max_fraction" else
+                        [int(x) for x in v.split(":")] if k == "bin_max_degree" else int(v))
         tuning = lvg.set_tuning(Y, **knobs)
     elif not args.no_tune:
         t0 = time.perf_counter()
@@ -1239,6 +1242,16 @@ def run_batched(args):
         ures = lvg.louvain_static_union(U, o)
         union_s = time.perf_counter() - t0
     union_s = dist.max(union_s)
+    ust = U.stats()
+    # the same run with the aggregated levels' phases launched the other way
+    # (one graph launch per level, or iteration by iteration from the host)
+    lg = int(tuning.get("level_graphs", 1))
+    lvg.set_tuning(U, level_graphs=1 - lg)
+    t0 = time.perf_counter()
+    lvg.louvain_static_union(U, o)
+    other_s = time.perf_counter() - t0
+    ost = U.stats()
+    lvg.set_tuning(U, level_graphs=lg)
     run_ms = ures[0].time if ures else 0.0
     qs = [graphs[i].modularity(ures[i].membership) for i in sample]
     line = {"metric": "batched static Louvain edges/s (many graphs)", "value": E_all / union_s, "unit": "edges/s",
@@ -1258,7 +1271,11 @@ def run_batched(args):
                       "first_pass_ms": ures[0].firstPassTime if ures else 0.0,
                       "download_ms": U.stats()["call_download_ms"],
                       "iterations_max": int(max(r.iterations for r in ures)),
-                      "passes_max": int(max(r.passes for r in ures))},
+                      "passes_max": int(max(r.passes for r in ures)),
+                      "host_syncs": int(ust["host_syncs"]), "kernel_launches": int(ust["kernel_launches"]),
+                      "level_phase_graphs": int(ust["level_graphs"]),
+                      f"wall_s_with_level_graphs_{1 - lg}": other_s,
+                      f"host_syncs_with_level_graphs_{1 - lg}": int(ost["host_syncs"])},
             "one_by_one": {"graphs": k, "edges_per_s": Ek / loop_s, "graphs_per_s": k / loop_s},
             "speedup_vs_one_by_one": (E / union_s) / (Ek / loop_s),
             "streams": {"workers": args.workers, "edges_per_s": E / many_s,
@@ -1269,6 +1286,66 @@ def run_batched(args):
     if rank == 0:
         print(json.dumps(line), flush=True)
     dist.close()
+    return 0
+
+
+def run_link(args):
+    """The host link that bounds `e2e`: pinned host <-> device copies of the
+    bytes one drop-in call moves each way on R-MAT s24 (the 16.8M-entry prior
+    or result: membership u32 + two FP64 weight arrays, 336 MB), as one copy,
+    split over 2/4/8 streams, and both directions at once. Best of 5 after a
+    warm-up, CUDA events. value = H2D GB/s on one stream."""
+    import torch
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    nbytes = (1 << args.scale) * (4 + 8 + 8)
+    h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    h2 = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    d2 = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    h.fill_(1)
+    d2.fill_(2)
+    streams = [torch.cuda.Stream() for _ in range(8)]
+
+    def timed(ns, up, down):
+        best = 1e30
+        for rep in range(6):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            main = torch.cuda.current_stream()
+            e0.record(main)
+            chunk = (nbytes + ns - 1) // ns
+            for i in range(ns):
+                st = streams[i]
+                st.wait_event(e0)
+                a, b = i * chunk, min(nbytes, (i + 1) * chunk)
+                with torch.cuda.stream(st):
+                    if up:
+                        d[a:b].copy_(h[a:b], non_blocking=True)
+                    if down:
+                        h2[a:b].copy_(d2[a:b], non_blocking=True)
+                main.wait_stream(st)
+            e1.record(main)
+            e1.synchronize()
+            if rep:
+                best = min(best, e0.elapsed_time(e1))
+        return best
+
+    rows = {}
+    for name, up, down in (("h2d", True, False), ("d2h", False, True), ("both", True, True)):
+        for ns in (1, 2, 4, 8):
+            ms = timed(ns, up, down)
+            rows[f"{name}_streams{ns}"] = {"ms": ms, "gb_per_s_each_way": nbytes / ms / 1e6}
+    ok = bool((d[:16].cpu() == 1).all() and (h2[:16] == 2).all())
+    line = {"metric": "host link copy GB/s (pinned host <-> HBM)", "value": rows["h2d_streams1"]["gb_per_s_each_way"],
+            "unit": "GB/s", "n_gpus": 1, "steps": 5, "warmup": 1, "ms_per_step": rows["h2d_streams1"]["ms"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "config": {"workload": f"link: {nbytes} B each way (the drop-in call's prior or result at scale "
+                                   f"{args.scale})", "bytes": nbytes},
+            "copies": rows, "copied_correctly": ok}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
     return 0
 
 
@@ -1284,6 +1361,8 @@ def main():
         return run_batched(args)
     if args.workload == "sweep":
         return run_sweep(args)
+    if args.workload == "link":
+        return run_link(args)
     return run_gpu(args)
 
 

@@ -418,6 +418,9 @@ typedef struct lvg_stats {
    * run: with the local-moving phase replayed as one graph, a dynamic-frontier
    * run that ends after one pass waits once). */
   uint64_t host_syncs;
+  /* Aggregated levels whose local-moving iterations after the first ran as
+   * one graph launch (lvg_tuning.level_graphs). */
+  uint64_t level_graphs;
 } lvg_stats;
 /* Enable (1) or disable (0) per-launch event timing for calls on g. */
 int lvg_set_profiling(lvg_graph *g, int enable);
@@ -446,6 +449,23 @@ typedef struct lvg_tuning {
                                   unit-weight graph, so that the dynamic methods' first pass
                                   evaluates such a vertex from its table instead of its edges
                                   (same results; default 1) */
+  uint32_t bin_max_degree[12]; /* the local-moving degree bins: bin b (1..9) takes vertex degrees
+                                  up to bin_max_degree[b] (0 = its full reach: 4, 8, 16, 32, 64,
+                                  128, 256, 512, 2048 for b = 1..9), above the previous bin's;
+                                  each bin's tile width and hash-table capacity are those of its
+                                  full reach, so a lower limit hands the bin's upper degrees to
+                                  the next bin's wider tile and larger table, and a limit equal
+                                  to the previous bin's empties the bin. Entries 0, 10 and 11
+                                  are 0 (bin 10 ends at degree 8192, the hubs' threshold).
+                                  Same results in deterministic mode (default all 0) */
+  int      level_graphs;       /* 1: on every aggregated level, the local-moving iterations after
+                                  the first run as one CUDA graph launch (a conditional while
+                                  node with the stop test on the device) built for that level;
+                                  0: one launch sequence and one synchronisation per iteration
+                                  (same results; default 1) */
+  int      small_regs;         /* registers a thread of the fused launch of degree bins 1-6
+                                  (fused_small): 32 (8 resident blocks per SM, some values kept
+                                  in local memory) or 64 (4 blocks per SM, none); default 32 */
 } lvg_tuning;
 void lvg_tuning_default(lvg_tuning *t);
 int lvg_graph_get_tuning(const lvg_graph *g, lvg_tuning *t);

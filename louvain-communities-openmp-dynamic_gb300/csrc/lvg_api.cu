@@ -71,7 +71,20 @@ void check_tuning(const lvg_tuning &t) {
   if (!(t.frontier_max_fraction >= 0 && t.frontier_max_fraction <= 1))
     throw Error(LVG_EINVAL, "tuning: frontier_max_fraction out of 0..1");
   if (t.hub_tables != 0 && t.hub_tables != 1) throw Error(LVG_EINVAL, "tuning: hub_tables is 0 or 1");
+  if (t.level_graphs != 0 && t.level_graphs != 1) throw Error(LVG_EINVAL, "tuning: level_graphs is 0 or 1");
+  if (t.small_regs != 32 && t.small_regs != 64) throw Error(LVG_EINVAL, "tuning: small_regs is 32 or 64");
   if (t.fused_small < 0 || t.fused_small > 64) throw Error(LVG_EINVAL, "tuning: fused_small out of 0..64");
+  if (t.bin_max_degree[0] || t.bin_max_degree[10] || t.bin_max_degree[11])
+    throw Error(LVG_EINVAL, "tuning: bin_max_degree[0], [10] and [11] are 0");
+  uint32_t prev = 0;
+  for (int b = 1; b <= 10; ++b) {
+    const uint32_t hi = t.bin_max_degree[b] ? t.bin_max_degree[b] : uint32_t(BIN_MAX_DEGREE[b]);
+    if (hi > BIN_MAX_DEGREE[b] || hi < prev)
+      throw Error(LVG_EINVAL, "tuning: bin_max_degree[" + std::to_string(b) + "] = " + std::to_string(hi) +
+                                  " is beyond the bin's reach (" + std::to_string(BIN_MAX_DEGREE[b]) +
+                                  ") or below the previous bin's limit (" + std::to_string(prev) + ")");
+    prev = hi;
+  }
 }
 
 // Set a graph's tuning: the hub plan of the uploaded level follows the chunk
@@ -79,8 +92,13 @@ void check_tuning(const lvg_tuning &t) {
 void apply_tuning(lvg_graph *g, const lvg_tuning &t) {
   check_tuning(t);
   const bool chunks = t.hub_chunk != g->tuning.hub_chunk;
+  const bool bins = !(bin_limits_of(t) == bin_limits_of(g->tuning));
   g->tuning = t;
-  if (chunks) build_hub_plan(g, g->base, g->hubplan);
+  if (bins && g->base.bins) {  // the uploaded level regrouped by the new limits
+    ensure_ws(g);
+    compute_bins(g, g->base, g->deg.p, g->bins.p, g->ws->binscratch.p, g->base.colors);
+  }
+  if (chunks || bins) build_hub_plan(g, g->base, g->hubplan);
   drop_graphs(g);
 }
 
@@ -1090,9 +1108,26 @@ int lvg_autotune(lvg_graph *g, int method, const lvg_device_batch *b, const lvg_
       // with concurrent and unfused, 0.78 ms for the best of one at a time)
       try_knob([](lvg_tuning &t, long v) { t.concurrent_bins = int(v >> 1); t.fused_small = int(v & 1); },
                {3, 2, 1, 0}, false);
-      // fused: its blocks per SM and bin (the worklists' lengths vary with the batch)
-      if (cur.fused_small) try_knob([](lvg_tuning &t, long v) { t.fused_small = int(v); }, {1, 4, 8, 16}, false);
+      // fused: its blocks per SM and bin (the worklists' lengths vary with the
+      // batch), and the degree <= 128 launch's register budget (32 registers
+      // with spills and 8 blocks per SM, or 64 and 4)
+      if (cur.fused_small) {
+        try_knob([](lvg_tuning &t, long v) { t.fused_small = int(v); }, {1, 4, 8, 16}, false);
+        try_knob([](lvg_tuning &t, long v) { t.small_regs = int(v); }, {32, 64}, false);
+      }
       try_knob([](lvg_tuning &t, long v) { t.big_blocks_per_sm = int(v); }, {0, 2, 3, 4}, false);
+      // the degree bins: each bin at its full reach, or its degrees handed to
+      // the next bin (its wider tile and larger table); bin 9 also split at
+      // 1024. A limit of BIN_MAX_DEGREE[b-1] is never below the previous
+      // bin's, whatever that bin's own choice.
+      for (int b = 2; b <= 9; ++b) {
+        auto set = [b](lvg_tuning &t, long v) { t.bin_max_degree[b] = uint32_t(v); };
+        if (b == 9) try_knob(set, {0, 1024, long(BIN_MAX_DEGREE[8])}, false);
+        else try_knob(set, {0, long(BIN_MAX_DEGREE[b - 1])}, false);
+      }
+      // aggregated levels' iterations as one graph launch per level, or
+      // launched from the host iteration by iteration
+      try_knob([](lvg_tuning &t, long v) { t.level_graphs = int(v); }, {1, 0}, false);
       // resident hub tables: a large saving where few vertices move (DF), a
       // cost where millions do (each move updates its hub neighbours' tables)
       if (prior && method != LVG_METHOD_STATIC)

@@ -77,6 +77,33 @@ __host__ __device__ inline int degree_bin(uint64_t d) {
 }
 constexpr uint64_t BIN_MAX_DEGREE[NUM_BINS] = {0, 4, 8, 16, 32, 64, 128, 256, 512, 2048, 8192, ~0ull};
 
+// Degree bins of the local-moving kernels at run time: bin b (1..10) takes
+// the degrees (hi[b-1], hi[b]], with hi[b] <= BIN_MAX_DEGREE[b] so that every
+// vertex fits its bin's kernel (tile width, table capacity); hi[10] stays
+// 8192 (the hubs above it have their own plan and tables). Lowering hi[b]
+// hands the bin's upper degrees to the next bin's wider tile and larger
+// table; hi[b] == hi[b-1] empties bin b. The defaults are BIN_MAX_DEGREE.
+struct BinLimits {
+  uint32_t hi[NUM_BINS];
+};
+__host__ __device__ inline BinLimits default_bin_limits() {
+  // BIN_MAX_DEGREE, with the last bin's unbounded reach as 2^32-1
+  return BinLimits{{0, 4, 8, 16, 32, 64, 128, 256, 512, 2048, 8192, 0xffffffffu}};
+}
+__host__ __device__ inline bool operator==(const BinLimits &a, const BinLimits &b) {
+  for (int i = 0; i < NUM_BINS; ++i)
+    if (a.hi[i] != b.hi[i]) return false;
+  return true;
+}
+__host__ __device__ __forceinline__ int degree_bin(uint64_t d, const BinLimits &L) {
+  if (d == 0) return 0;
+  int b = NUM_BINS - 1;
+#pragma unroll
+  for (int i = NUM_BINS - 2; i >= 1; --i)
+    if (d <= L.hi[i]) b = i;
+  return b;
+}
+
 // Colour classes of the local-moving sweeps. Each iteration visits the
 // classes one after another, so a vertex sees the moves its neighbours in
 // earlier classes made in the same iteration (as in the reference's

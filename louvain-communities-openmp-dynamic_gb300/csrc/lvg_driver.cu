@@ -57,8 +57,9 @@ void read_counters(lvg_graph *g) {
 void compute_bins(lvg_graph *g, Level &lv, const uint32_t *deg, uint32_t *list, uint32_t *scratch, int colors) {
   g->hbins.ensure(bin_host_elems(MAX_COLORS));
   lv.colors = colors;
+  lv.lim = bin_limits_of(g->tuning);
   bin_items_u32(deg, lv.ex, lv.span, colors, list, lv.bin_start, lv.bin_maxdeg, scratch, g->hbins.p, g->stream,
-                lv.gid, lv.gbase);
+                lv.gid, lv.gbase, lv.lim);
   ++g->stats.host_syncs;  // the bin counts are read back
   lv.bins = list;
 }
@@ -194,7 +195,7 @@ struct SpillScope {
 
 // Degree bins and hub plan of the uploaded level for k colour classes.
 void set_base_colors(lvg_graph *g, int k) {
-  if (g->base.colors == k) return;
+  if (g->base.colors == k && g->base.lim == bin_limits_of(g->tuning)) return;
   compute_bins(g, g->base, g->deg.p, g->bins.p, g->ws->binscratch.p, k);
   build_hub_plan(g, g->base, g->hubplan);
 }
@@ -434,7 +435,7 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot
         a.ht = W.ht_now;
         set_union(a);
         cudaEvent_t b0 = bin_ev ? g->events.record(s) : nullptr;
-        launch_move_small(grp.first, grp.second, sync, a, sb, stream_of(grp.first));
+        launch_move_small(grp.first, grp.second, sync, a, sb, stream_of(grp.first), g->tuning.small_regs);
         if (bin_ev) bin_ev->push_back({grp.first, {b0, g->events.record(s)}});
         ++g->stats.move_launches;
       }
@@ -490,6 +491,9 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot
       launch_merge_marks(W.vaff.p, W.mark.p, lv.span, s);
     }
   }
+  // worklists filled while a dynamic-frontier batch was marked serve the
+  // first iteration only
+  if (K == 1 && !uc) LVG_CUDA(cudaMemsetAsync(&g->ctr.p->pre_flag, 0, sizeof(unsigned int), s));
   if (uc) launch_iter_control(uc->n, uc->ctl, uc->gact, uc->fix, uc->M, uc->E, uc->L, g->ctr.p, s);
   if (read_back) LVG_CUDA(cudaMemcpyAsync(g->hctr.p, g->ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
 }
@@ -503,14 +507,15 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot
 // is bounded by L whatever the kernels compute. A phase is then one graph
 // launch and one synchronisation, instead of one of each per iteration. Any
 // failure to build it leaves the per-iteration path in place for this handle.
-void capture_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const tot_t *tot, const uint8_t *fa,
-                   float kr, bool sync, int fused, const int *glog2, const size_t *goff, size_t need,
-                   const IterKey &key, const UnionCall *uc) {
+struct PhaseGraph {
+  cudaGraphExec_t exec = nullptr;
+  unsigned long long nodes = 0, moves = 0;  // kernel launches (all, local-moving) of one iteration
+};
+PhaseGraph build_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const tot_t *tot, const uint8_t *fa,
+                       float kr, bool sync, int fused, const int *glog2, const size_t *goff, size_t need, double M,
+                       double E, int L, const UnionCall *uc) {
   cudaStream_t s = g->stream;
-  if (g->phase_exec) {
-    cudaGraphExecDestroy(g->phase_exec);
-    g->phase_exec = nullptr;
-  }
+  PhaseGraph pg;
   const unsigned long long l0 = launch_counter();
   const unsigned long long m0 = g->stats.move_launches;
   cudaGraph_t graph = nullptr;
@@ -531,23 +536,80 @@ void capture_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, co
   if (fine) {
     try {
       enqueue_iteration(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, goff, need, nullptr, uc, false);
-      launch_iter_end(g->ctr.p, key.M, key.E, key.L, uc != nullptr, h, s);
+      launch_iter_end(g->ctr.p, M, E, L, uc != nullptr, h, s);
     } catch (const Error &) {
       fine = false;
     }
     cudaGraph_t body = nullptr;
     fine = cudaStreamEndCapture(s, &body) == cudaSuccess && fine;
   }
+  pg.nodes = launch_counter() - l0;  // the iteration's kernels and the stop test
+  pg.moves = g->stats.move_launches - m0;
   launch_counter() = l0;
   g->stats.move_launches = m0;
-  if (!fine || cudaGraphInstantiate(&g->phase_exec, graph, 0) != cudaSuccess) {
+  if (!fine || cudaGraphInstantiate(&pg.exec, graph, 0) != cudaSuccess) {
     cudaGetLastError();
-    g->phase_exec = nullptr;
-    g->no_phase_graphs = true;
-  } else {
-    g->phase_key = key;
+    pg.exec = nullptr;
   }
   if (graph) cudaGraphDestroy(graph);
+  return pg;
+}
+
+// The whole local-moving phase of the uploaded level as one graph: a
+// conditional while node whose body is one iteration (as enqueue_iteration
+// issues it) followed by iter_end_kernel, which evaluates the reference's
+// stop test (el <= E, or L iterations; inc/louvain.hxx:588-609) on the device
+// and sets the node's condition (for a graph union: while any graph is still
+// moving, each graph's own test having run in iter_control_kernel). The loop
+// is bounded by L whatever the kernels compute. A phase is then one graph
+// launch and one synchronisation, instead of one of each per iteration. Any
+// failure to build it leaves the per-iteration path in place for this handle.
+void capture_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const tot_t *tot, const uint8_t *fa,
+                   float kr, bool sync, int fused, const int *glog2, const size_t *goff, size_t need,
+                   const IterKey &key, const UnionCall *uc) {
+  if (g->phase_exec) {
+    cudaGraphExecDestroy(g->phase_exec);
+    g->phase_exec = nullptr;
+  }
+  const PhaseGraph pg = build_phase(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, goff, need, key.M, key.E,
+                                    key.L, uc);
+  g->phase_exec = pg.exec;
+  if (!pg.exec) g->no_phase_graphs = true;
+  else g->phase_key = key;
+}
+
+// The rest of an aggregated level's phase (after its first iteration, which
+// ran eagerly and set every kernel's attributes) as one graph built for this
+// call, launched once and dropped: the same loop and device-side stop test as
+// the uploaded level's phase graph, so the level's remaining iterations cost
+// one launch and one synchronisation instead of one of each per iteration
+// (an aggregated level's kernels are short, and issuing every class's
+// launches from the host each iteration took longer than running them).
+// Returns false, having run nothing, when the graph could not be built.
+bool run_level_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const tot_t *tot, const uint8_t *fa,
+                     float kr, bool sync, int fused, const int *glog2, const size_t *goff, size_t need, double M,
+                     double E, int L, const UnionCall *uc, int &iters, double &el) {
+  cudaStream_t s = g->stream;
+  const PhaseGraph pg = build_phase(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, goff, need, M, E, L, uc);
+  if (!pg.exec) {
+    g->no_level_graphs = true;
+    return false;
+  }
+  struct Drop {
+    cudaGraphExec_t e;
+    ~Drop() { cudaGraphExecDestroy(e); }
+  } drop{pg.exec};
+  LVG_CUDA(cudaMemsetAsync(&g->ctr.p->dev_iters, 0, sizeof(unsigned int), s));
+  LVG_CUDA(cudaGraphLaunch(pg.exec, s));
+  LVG_CUDA(cudaMemcpyAsync(g->hctr.p, g->ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+  host_sync(g);
+  if (g->hctr.p->err) read_counters(g);  // raises the device error
+  iters = int(g->hctr.p->dev_iters);
+  el = uc ? 0.0 : g->hctr.p->dev_el;
+  launch_counter() += pg.nodes * unsigned(iters);
+  g->stats.move_launches += pg.moves * unsigned(iters);
+  ++g->stats.level_graphs;
+  return true;
 }
 
 // Capture one iteration of the uploaded level into a CUDA graph (after an
@@ -607,19 +669,16 @@ struct PhaseEnd {
 // it was.
 int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const tot_t *tot, const uint8_t *fa,
                double M, float kr, int L, double E, bool sync, int fused, const UnionCall *uc = nullptr,
-               const DBatch *endpoints = nullptr, PhaseEnd *end = nullptr, bool capture = true,
+               bool iso_clear = false, PhaseEnd *end = nullptr, bool capture = true,
                const std::function<void()> *tail = nullptr, bool *tail_done = nullptr) {
   if (tail_done) *tail_done = false;
   Workspace &W = *g->ws;
   cudaStream_t s = g->stream;
   const int K = lv.colors;
-  // Existing degree-0 vertices are processed once and never re-marked. In
-  // the dynamic-frontier first pass only batch endpoints can be such
-  // vertices with their flag set (`endpoints`).
-  if (endpoints) {
-    launch_clear_isolated_endpoints(endpoints->ds, endpoints->nd, endpoints->is, endpoints->ni, lv.deg, lv.ex,
-                                    W.vaff.p, s);
-  } else {
+  // Existing degree-0 vertices are processed once and never re-marked: their
+  // flags are cleared here (the dynamic-frontier first pass: df_start_kernel
+  // left them unmarked, iso_clear).
+  if (!iso_clear) {
     IsolatedLists iso{};
     iso.k = K;
     for (int k = 0; k < K; ++k) {
@@ -679,6 +738,9 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const 
   }
   const bool graphs = base && capture && !g->profiling && !g->no_graphs;
   const bool phase_graphs = graphs && !g->no_phase_graphs && L > 0;
+  // an aggregated level: its iterations after the first as one graph
+  const bool level_graphs = !base && capture && !g->profiling && !g->no_graphs && !g->no_level_graphs &&
+                            g->tuning.level_graphs;
   int l = 0;
   double el = 0;
   if (phase_graphs && g->phase_exec && g->phase_key == key) {
@@ -724,10 +786,18 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const 
     ++l;
     if (uc) {  // each graph ran its own stop test (iter_control_kernel)
       if (g->hctr.p->gactive == 0) break;
-      continue;
+    } else {
+      el = double(g->hctr.p->el_fix) / GAIN_FIX / M;
+      if (el <= E) break;
     }
-    el = double(g->hctr.p->el_fix) / GAIN_FIX / M;
-    if (el <= E) break;
+    if (level_graphs && l == 1 && l < L) {
+      int more = 0;
+      if (run_level_phase(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, goff, need, M, E, L - l, uc, more,
+                          el)) {
+        l += more;
+        break;
+      }
+    }
   }
   // next time, the whole phase as one graph (every kernel's attributes are set
   // by now)
@@ -928,9 +998,19 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
       if (tprior != tout) copy_hub_tables(g, *tout, *tprior);  // the prior's own cache, before any move
       g->stats.hub_tables_built = 1;
     }
-    // fi: initial membership and weights.
+    // fi: initial membership and weights. Dynamic frontier: fm (the marking)
+    // runs in the same pass over the batch (df_start_kernel; its time counts
+    // as initialisation), and with one colour class it also lists the marked
+    // vertices for the first iteration.
     if (method == LVG_METHOD_STATIC) {
       launch_init_static(g->base, ucom, utot, ctot, s);
+    } else if (method == LVG_METHOD_FRONTIER) {
+      BinBounds bb{};
+      const bool lists = K == 1 && g->base.colors == 1;
+      if (lists)
+        for (int x = 0; x <= NUM_BINS; ++x) bb.start[x] = g->base.bin_start[x];
+      launch_df_start(b.ds, b.dd, b.dw, b.nd, b.is, b.id, b.iw, b.ni, ucom, utot, ctot, g->base, W.vaff.p,
+                      lists ? &bb : nullptr, W.wl.p, g->ctr.p, s);
     } else {
       launch_batch_weights(b.ds, b.dw, b.nd, -1.f, ucom, utot, ctot, s);
       launch_batch_weights(b.is, b.iw, b.ni, +1.f, ucom, utot, ctot, s);
@@ -942,7 +1022,7 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
     if (method == LVG_METHOD_STATIC || method == LVG_METHOD_NAIVE) {
       LVG_CUDA(cudaMemsetAsync(W.vaff.p, 1, S, s));
     } else if (method == LVG_METHOD_FRONTIER) {
-      launch_df_mark(b.ds, b.dd, b.nd, b.is, b.id, b.ni, ucom, W.vaff.p, s);
+      // marked by df_start_kernel
     } else {
       LVG_CUDA(cudaMemsetAsync(W.fv.p, 0, S, s));
       LVG_CUDA(cudaMemsetAsync(W.fn.p, 0, S, s));
@@ -981,7 +1061,7 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
                         : tf >= 2                        ? tf
                         : method == LVG_METHOD_FRONTIER  ? 2
                                                          : 8;
-      const DBatch *ends = first && method == LVG_METHOD_FRONTIER ? &b : nullptr;
+      const bool ends = first && method == LVG_METHOD_FRONTIER;  // df_start_kernel left isolated ones unmarked
       // the end of the run, enqueued ahead of the first pass's one
       // synchronisation: if the run ends after this pass (as a frontier run
       // on a small batch does), it needs no other synchronisation
@@ -1168,7 +1248,7 @@ void run_union(lvg_graph *g, const lvg_options &o, RunInfo &info) {
           SpillScope spill(g, lv);
           W.first_sweep = true;
           try {
-            move_phase(g, lv, com, ctot, tot, nullptr, 0.0, 0.f, 1, E, sync, 0, &uc, nullptr, nullptr, false);
+            move_phase(g, lv, com, ctot, tot, nullptr, 0.0, 0.f, 1, E, sync, 0, &uc, false, nullptr, false);
           } catch (...) {
             W.first_sweep = false;
             throw;

@@ -76,7 +76,8 @@ struct Workspace {
   void allocate(size_t S_, size_t X_, cudaStream_t st) {
     S = S_;
     X = X_;
-    vaff.ensure(S); mark.ensure(S); fv.ensure(S); fn.ensure(S); fc.ensure(S);
+    // vaff: whole 32-bit words (df_start_kernel sets flags by atomics on them)
+    vaff.ensure((S + 3) / 4 * 4); mark.ensure(S); fv.ensure(S); fn.ensure(S); fc.ensure(S);
     ucom.ensure(S); vcom.ensure(S); com_next.ensure(S); dec.ensure(S); wl.ensure(S + 1);
     wl_count.ensure(size_t(MAX_COLORS) * NUM_BINS);
     cext.ensure(S + 1); csize.ensure(S + 1); ccur.ensure(S + 1); cmem.ensure(S + 1); cbins.ensure(S + 1);
@@ -213,7 +214,20 @@ inline lvg_tuning default_tuning() {
   t.big_blocks_per_sm = 0;
   t.frontier_max_fraction = 1e-3;
   t.hub_tables = 1;
+  for (auto &x : t.bin_max_degree) x = 0;
+  t.level_graphs = 1;
+  t.small_regs = 32;
   return t;
+}
+
+// The local-moving degree bins a tuning asks for (0 entries: the bin's full
+// reach). The tuning was checked (check_tuning): every limit is within its
+// bin's reach and at least the previous bin's.
+inline BinLimits bin_limits_of(const lvg_tuning &t) {
+  BinLimits L = default_bin_limits();
+  for (int b = 1; b <= 9; ++b)
+    if (t.bin_max_degree[b]) L.hi[b] = t.bin_max_degree[b];
+  return L;
 }
 
 struct RunInfo {
@@ -278,6 +292,7 @@ struct lvg_graph {
   cudaGraphExec_t phase_exec = nullptr;
   IterKey phase_key{};
   bool no_phase_graphs = false;
+  bool no_level_graphs = false;  // a level's phase graph could not be built: eager from then on
   // side streams for the degree-bin kernels of one colour class, which run
   // concurrently (fork/join with events)
   cudaStream_t aux[4] = {};

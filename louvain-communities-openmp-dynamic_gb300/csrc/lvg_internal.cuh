@@ -131,6 +131,7 @@ struct Level {
   // group: group (k, b) is bins[bin_start[k*NUM_BINS+b] .. bin_start[k*NUM_BINS+b+1]).
   uint32_t *bins = nullptr;
   int colors = 1;
+  BinLimits lim = default_bin_limits();  // the degree bins' limits the grouping used
   size_t bin_start[MAX_BUCKETS + 1] = {};
   uint64_t bin_maxdeg[NUM_BINS] = {};
   HubPlan hub;  // chunked work for degree bin 11
@@ -161,6 +162,11 @@ struct Counters {
   unsigned long long nonunit;                 // edge weights other than 1 (count_nonunit)
   unsigned int dev_iters;                     // iterations run by the device-side loop (iter_end_kernel)
   double dev_el;                              // its last iteration's el
+  // Worklists of the first local-moving iteration filled by df_start_kernel
+  // (one colour class): pre_flag set, the per-bin counts in pre_count; the
+  // first compaction takes them instead of scanning the flags.
+  unsigned int pre_flag;
+  uint32_t pre_count[NUM_BINS];
   unsigned long long ht_slots;                // hub-table slots read by hub_table_kernel
   unsigned long long ht_over;                 // hub tables that ran out of room (their hubs scan again)
 };
@@ -347,7 +353,8 @@ size_t bin_scratch_elems(size_t n, int colors);
 size_t bin_host_elems(int colors);
 void bin_items_u32(const uint32_t *deg, const uint8_t *ex, size_t n, int colors, uint32_t *list, size_t *bin_start,
                    uint64_t *bin_maxdeg, uint32_t *scratch, uint32_t *host_pinned, cudaStream_t s,
-                   const uint32_t *gid = nullptr, const uint32_t *gbase = nullptr);
+                   const uint32_t *gid = nullptr, const uint32_t *gbase = nullptr,
+                   const BinLimits &lim = default_bin_limits());
 void bin_items_u64(const uint64_t *deg, const uint8_t *ex, size_t n, int colors, uint32_t *list,
                    size_t *bin_start, uint64_t *bin_maxdeg, uint32_t *scratch, uint32_t *host_pinned,
                    cudaStream_t s);
@@ -366,6 +373,16 @@ void launch_vertex_weights_f64(const Level &g, double *vtot, cudaStream_t s);
 void launch_community_weights_f64(const uint32_t *q, const double *vtot, size_t n, double *ctot, cudaStream_t s);
 void launch_batch_weights(const uint32_t *src, const float *w, size_t n, float sign, const uint32_t *vcom,
                           tot_t *vtot, tot_t *ctot, cudaStream_t s);
+struct BinBounds;
+// Dynamic-frontier Louvain's start in one pass over the batch (the weight
+// update and the marking of affected vertices; existing degree-0 vertices are
+// left unmarked). With bb (one colour class, no graph union), every vertex it
+// marks in degree bins 1..NUM_BINS-2 is appended to the class's worklists
+// (ctr->pre_count, ctr->pre_flag) for the first iteration.
+void launch_df_start(const uint32_t *ds, const uint32_t *dd, const float *dw, size_t nd, const uint32_t *is,
+                     const uint32_t *id, const float *iw, size_t ni, const uint32_t *vcom, tot_t *vtot, tot_t *ctot,
+                     const Level &g, uint8_t *vaff, const BinBounds *bb, uint32_t *wl, Counters *ctr,
+                     cudaStream_t s);
 void launch_df_mark(const uint32_t *ds, const uint32_t *dd, size_t nd, const uint32_t *is, const uint32_t *id,
                     size_t ni, const uint32_t *vcom, uint8_t *vaff, cudaStream_t s);
 // seg: ni entries (sources left to the per-source pass, then those with more
@@ -580,7 +597,9 @@ struct SmallBins {
   const uint32_t *count_ptr[6];
   uint32_t block_begin[7];
 };
-void launch_move_small(int lo, int hi, bool sync, const MoveArgs &a, const SmallBins &sb, cudaStream_t s);
+// small_regs: registers a thread of the bins 1-6 launch (32 or 64, lvg_tuning.small_regs).
+void launch_move_small(int lo, int hi, bool sync, const MoveArgs &a, const SmallBins &sb, cudaStream_t s,
+                       int small_regs = 32);
 int device_sms();
 // Grid of the local-moving kernel of a large-degree bin (9, 10; 11 = the hub
 // merge) for `count` vertices: the size of its per-block global fallback.

@@ -150,6 +150,75 @@ __global__ void df_mark_kernel(const uint32_t *ds, const uint32_t *dd, size_t nd
   }
 }
 
+// Dynamic-frontier Louvain's start: louvainUpdateWeightsFromOmpU
+// (inc/louvain.hxx:374-388, deletions subtracted, insertions added, summed
+// per warp by vertex and by community as batch_weights_kernel does) and
+// louvainAffectedVerticesFrontierOmpW (:1606-1624) in one pass over the
+// batch, entry i < nd a deletion, else insertion i - nd. Both read only the
+// prior membership. A source that exists with degree 0 is left unmarked: the
+// local-moving sweep would clear its flag without moving it, and no move marks
+// it again (it has no neighbours), so the residual flags are the same.
+// With wl (one colour class), a vertex's first marker (an atomic OR on the
+// flag's word, so the vertex is listed once) appends it to the worklist of its
+// degree bin, at the class's bin offsets, bounded by the bin's slice like the
+// compaction's appends; pre_flag then tells the first compaction to take
+// these lists.
+__global__ void df_start_kernel(const uint32_t *ds, const uint32_t *dd, const float *dw, size_t nd,
+                                const uint32_t *is, const uint32_t *id, const float *iw, size_t ni,
+                                const uint32_t *vcom, tot_t *vtot, tot_t *ctot, const uint32_t *deg,
+                                const uint8_t *ex, BinLimits lim, uint8_t *vaff, BinBounds bb, uint32_t *wl,
+                                Counters *ctr) {
+  const int lane = threadIdx.x & 31;
+  const size_t n = nd + ni;
+  if (wl && blockIdx.x == 0 && threadIdx.x == 0) ctr->pre_flag = 1u;
+  for (size_t base = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32 * 32; base < n;
+       base += size_t(gridDim.x) * blockDim.x) {
+    const size_t i = base + lane;
+    uint32_t u = EMPTY, c = EMPTY;
+    double x = 0.0;
+    bool mark = false;
+    if (i < n) {
+      const bool del = i < nd;
+      const size_t j = del ? i : i - nd;
+      u = del ? ds[j] : is[j];
+      const uint32_t v = del ? dd[j] : id[j];
+      x = del ? -double(dw[j]) : double(iw[j]);
+      c = vcom[u];
+      mark = del ? c == vcom[v] : c != vcom[v];
+    }
+    group_add(vtot, u, x, lane);
+    group_add(ctot, c, x, lane);
+    int b = -1;
+    if (mark) {
+      const uint32_t d = deg[u];
+      if (d == 0 && (!ex || ex[u])) {
+        mark = false;
+      } else if (!wl) {
+        vaff[u] = 1;
+      } else {
+        const unsigned sh = 8u * (u & 3u);
+        const unsigned old = atomicOr(reinterpret_cast<unsigned int *>(vaff) + (u >> 2), 1u << sh);
+        if (!((old >> sh) & 0xffu)) {  // the first to mark u lists it
+          const int x2 = degree_bin(d, lim);
+          if (x2 >= 1 && x2 <= NUM_BINS - 2) b = x2;
+        }
+      }
+    }
+    if (wl) {
+      const unsigned grp = __match_any_sync(0xffffffffu, b);
+      const int leader = __ffs(grp) - 1;
+      uint32_t at = 0;
+      if (b >= 0 && lane == leader) at = atomicAdd(&ctr->pre_count[b], uint32_t(__popc(grp)));
+      at = __shfl_sync(0xffffffffu, at, leader);
+      if (b >= 0) {
+        const uint32_t slot = at + __popc(grp & ((1u << lane) - 1u));
+        if (slot < bb.start[b + 1] - bb.start[b]) wl[bb.start[b] + slot] = u;
+        else atomicOr(&ctr->err, ERR_WORKLIST);
+      }
+    }
+  }
+}
+
 // Delta-screening, deletions (inc/louvain.hxx:1448-1456).
 __global__ void ds_del_kernel(const uint32_t *ds, const uint32_t *dd, size_t nd, const uint32_t *vcom,
                               uint8_t *vertices, uint8_t *neighbors, uint8_t *communities) {
@@ -731,8 +800,19 @@ __global__ void compact_active_kernel(const uint32_t *bins, BinBounds bb, const 
 // the bins being recomputed, an append past the slice is dropped and flagged
 // (ERR_WORKLIST) instead of writing into the next bin's slice.
 __global__ void compact_active_scan_kernel(const uint32_t *deg, const uint8_t *ex, size_t span, BinBounds bb,
-                                           const uint8_t *vaff, const uint8_t *fa, uint32_t *wl,
-                                           uint32_t *wl_count, unsigned int *err) {
+                                           BinLimits lim, const uint8_t *vaff, const uint8_t *fa, uint32_t *wl,
+                                           uint32_t *wl_count, Counters *ctr) {
+  // the first iteration of a dynamic-frontier run: its worklists were filled
+  // while the batch was marked (df_start_kernel); take their counts (the
+  // flag is cleared after the iteration, in stream order)
+  if (ctr->pre_flag) {
+    if (blockIdx.x == 0 && threadIdx.x < NUM_BINS) {
+      wl_count[threadIdx.x] = ctr->pre_count[threadIdx.x];
+      ctr->pre_count[threadIdx.x] = 0;
+    }
+    return;
+  }
+  unsigned int *err = &ctr->err;
   const int lane = threadIdx.x & 31;
   const size_t words = (span + 15) / 16;
   // a warp takes WPL * 32 consecutive words, their flag loads issued
@@ -784,7 +864,7 @@ __global__ void compact_active_scan_kernel(const uint32_t *deg, const uint8_t *e
         const int j = __ffsll(static_cast<long long>(act)) - 1;
         act &= act - 1ull;
         u = uint32_t((wbase + size_t(j >> 4) * 32 + lane) * 16 + (j & 15));
-        const int x = degree_bin(deg[u]);
+        const int x = degree_bin(deg[u], lim);
         if (x >= 1 && x <= NUM_BINS - 2) b = x;
       }
       const unsigned grp = __match_any_sync(0xffffffffu, b);
@@ -931,6 +1011,19 @@ void launch_batch_weights(const uint32_t *src, const float *w, size_t n, float s
   LVG_CHECK_LAUNCH();
 }
 
+void launch_df_start(const uint32_t *ds, const uint32_t *dd, const float *dw, size_t nd, const uint32_t *is,
+                     const uint32_t *id, const float *iw, size_t ni, const uint32_t *vcom, tot_t *vtot, tot_t *ctot,
+                     const Level &g, uint8_t *vaff, const BinBounds *bb, uint32_t *wl, Counters *ctr,
+                     cudaStream_t s) {
+  // with lists, the first compaction takes them even for an empty batch
+  const size_t n = nd + ni;
+  if (!n && !bb) return;
+  df_start_kernel<<<n ? grid_for(n, 256) : 1, 256, 0, s>>>(ds, dd, dw, nd, is, id, iw, ni, vcom, vtot, ctot, g.deg,
+                                                          g.ex, g.lim, vaff, bb ? *bb : BinBounds{},
+                                                          bb ? wl : nullptr, ctr);
+  LVG_CHECK_LAUNCH();
+}
+
 void launch_df_mark(const uint32_t *ds, const uint32_t *dd, size_t nd, const uint32_t *is, const uint32_t *id,
                     size_t ni, const uint32_t *vcom, uint8_t *vaff, cudaStream_t s) {
   if (!(nd + ni)) return;
@@ -1067,8 +1160,8 @@ void launch_compact_active(const uint32_t *bins, const BinBounds &bb, const uint
 void launch_compact_active_scan(const Level &g, const BinBounds &bb, const uint8_t *vaff, const uint8_t *fa,
                                 uint32_t *wl, uint32_t *wl_count, Counters *ctr, cudaStream_t s) {
   if (!g.span) return;
-  compact_active_scan_kernel<<<grid_for((g.span + 15) / 16, 256), 256, 0, s>>>(g.deg, g.ex, g.span, bb, vaff, fa, wl,
-                                                                                  wl_count, &ctr->err);
+  compact_active_scan_kernel<<<grid_for((g.span + 15) / 16, 256), 256, 0, s>>>(g.deg, g.ex, g.span, bb, g.lim, vaff,
+                                                                                  fa, wl, wl_count, ctr);
   LVG_CHECK_LAUNCH();
 }
 

@@ -172,6 +172,11 @@ __device__ __forceinline__ void tile_loop(const MoveArgs &a, const uint32_t *lis
     const uint64_t o = a.off[u];
     const uint32_t dg = a.deg[u];
     const uint32_t d = a.vcom[u];
+    // the vertex's weight and its community's total, loaded while the edges
+    // are scanned (a racy snapshot in asynchronous mode, as any read of them
+    // is; fixed within a class in deterministic mode)
+    double wu = 0.0, td = 0.0;
+    if (tl == 0) { wu = a.vtot[u]; td = a.ctot[d]; }
 #pragma unroll
     for (int s = tl; s < C; s += T) { keys[s] = EMPTY; vals[s] = 0.f; }
     __syncwarp(m);
@@ -238,8 +243,6 @@ __device__ __forceinline__ void tile_loop(const MoveArgs &a, const uint32_t *lis
 #pragma unroll
     for (int sh = T / 2; sh > 0; sh >>= 1) kd += __shfl_xor_sync(m, kd, sh, T);
     __syncwarp(m);
-    double wu = 0.0, td = 0.0;
-    if (tl == 0) { wu = a.vtot[u]; td = a.ctot[d]; }
     wu = __shfl_sync(m, wu, 0, T);
     td = __shfl_sync(m, td, 0, T);
     const float wuf = __double2float_rn(wu);
@@ -310,8 +313,11 @@ __global__ void __launch_bounds__(TILE_BLOCK, (C <= 256 ? 8 : 1)) move_tile_kern
 // classes' worklists are short (dynamic-frontier and delta-screening passes
 // over the uploaded graph), where a launch per bin would cost more than its
 // work.
-template <int LO, int HI, bool SYNC, bool UNIT>
-__global__ void __launch_bounds__(TILE_BLOCK, (HI <= 6 ? 8 : 1)) move_small_kernel(MoveArgs a, SmallBins sb) {
+// MINB: resident blocks per SM the kernel is compiled for. Bins 1-6 come in
+// two variants (lvg_tuning.small_regs): 8 blocks (32 registers a thread,
+// some values spilled to local memory) or 4 (64 registers, none spilled).
+template <int LO, int HI, bool SYNC, bool UNIT, int MINB>
+__global__ void __launch_bounds__(TILE_BLOCK, MINB) move_small_kernel(MoveArgs a, SmallBins sb) {
   extern __shared__ __align__(16) uint8_t smem[];
   int k = 0;
   while (k < HI - LO && blockIdx.x >= sb.block_begin[k + 1]) ++k;
@@ -1128,12 +1134,12 @@ void set_smem(K kernel, size_t bytes) {
   if (bytes > 48 * 1024) LVG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)));
 }
 
-template <int LO, int HI, bool SYNC, bool UNIT>
+template <int LO, int HI, bool SYNC, bool UNIT, int MINB>
 void launch_small(const MoveArgs &a, SmallBins sb, cudaStream_t s) {
   // shared memory of the largest table among the bins (tiles x C x 8 bytes)
   constexpr size_t CMAX = size_t(TILE_BLOCK / (HI <= 1 ? 4 : HI == 2 ? 8 : HI == 3 ? 16 : 32)) *
                           (size_t(4) << HI) * 8;
-  auto k = move_small_kernel<LO, HI, SYNC, UNIT>;
+  auto k = move_small_kernel<LO, HI, SYNC, UNIT, MINB>;
   static bool configured = false;
   if (!configured) { set_smem(k, CMAX); configured = true; }
   const unsigned grid = sb.block_begin[HI - LO + 1];
@@ -1278,15 +1284,32 @@ void launch_move_hubs(bool sync, const MoveArgs &a, cudaStream_t s) {
 
 int device_sms() { return num_sms(); }
 
-void launch_move_small(int lo, int hi, bool sync, const MoveArgs &a, const SmallBins &sb, cudaStream_t s) {
+template <int MINB>
+void launch_small_1_6(bool sync, const MoveArgs &a, const SmallBins &sb, cudaStream_t s) {
+  if (sync) {
+    if (a.unit) launch_small<1, 6, true, true, MINB>(a, sb, s);
+    else launch_small<1, 6, true, false, MINB>(a, sb, s);
+  } else if (a.unit) {
+    launch_small<1, 6, false, true, MINB>(a, sb, s);
+  } else {
+    launch_small<1, 6, false, false, MINB>(a, sb, s);
+  }
+}
+
+void launch_move_small(int lo, int hi, bool sync, const MoveArgs &a, const SmallBins &sb, cudaStream_t s,
+                       int small_regs) {
   if (lo == 1 && hi == 6) {
-    if (sync) { if (a.unit) launch_small<1, 6, true, true>(a, sb, s); else launch_small<1, 6, true, false>(a, sb, s); }
-    else if (a.unit) launch_small<1, 6, false, true>(a, sb, s);
-    else launch_small<1, 6, false, false>(a, sb, s);
+    if (small_regs == 64) launch_small_1_6<4>(sync, a, sb, s);
+    else launch_small_1_6<8>(sync, a, sb, s);
   } else if (lo == 7 && hi == 8) {
-    if (sync) { if (a.unit) launch_small<7, 8, true, true>(a, sb, s); else launch_small<7, 8, true, false>(a, sb, s); }
-    else if (a.unit) launch_small<7, 8, false, true>(a, sb, s);
-    else launch_small<7, 8, false, false>(a, sb, s);
+    if (sync) {
+      if (a.unit) launch_small<7, 8, true, true, 1>(a, sb, s);
+      else launch_small<7, 8, true, false, 1>(a, sb, s);
+    } else if (a.unit) {
+      launch_small<7, 8, false, true, 1>(a, sb, s);
+    } else {
+      launch_small<7, 8, false, false, 1>(a, sb, s);
+    }
   } else {
     throw Error(LVG_EINVAL, "launch_move_small: unsupported bin range");
   }

@@ -120,16 +120,16 @@ constexpr int BIN_THREADS = 256;
 // their own graph (gbase[g] = the graph's first item), so that each graph's
 // classes are those it has alone.
 __device__ __forceinline__ int bucket_of(size_t j, unsigned long long d, int colors, const uint32_t *gid,
-                                         const uint32_t *gbase) {
+                                         const uint32_t *gbase, const BinLimits &lim) {
   const uint32_t id = gid ? uint32_t(j) - gbase[gid[j]] : uint32_t(j);
-  return int(vertex_color(id, uint32_t(colors))) * NUM_BINS + degree_bin(d);
+  return int(vertex_color(id, uint32_t(colors))) * NUM_BINS + degree_bin(d, lim);
 }
 
 template <class D>
 __global__ void __launch_bounds__(BIN_THREADS) bin_count_kernel(const D *deg, const uint8_t *ex, size_t n, int colors,
                                                                 const uint32_t *gid, const uint32_t *gbase,
                                                                 uint32_t *counts, unsigned long long *maxdeg,
-                                                                unsigned nb) {
+                                                                unsigned nb, BinLimits lim) {
   __shared__ uint32_t cnt[MAX_BUCKETS];
   __shared__ unsigned long long mx[NUM_BINS];
   const int nbk = colors * NUM_BINS;
@@ -141,8 +141,8 @@ __global__ void __launch_bounds__(BIN_THREADS) bin_count_kernel(const D *deg, co
     size_t j = base + k;
     if (j >= n || (ex && !ex[j])) continue;
     unsigned long long d = deg[j];
-    atomicAdd(&cnt[bucket_of(j, d, colors, gid, gbase)], 1u);
-    atomicMax(&mx[degree_bin(d)], d);
+    atomicAdd(&cnt[bucket_of(j, d, colors, gid, gbase, lim)], 1u);
+    atomicMax(&mx[degree_bin(d, lim)], d);
   }
   __syncthreads();
   for (int k = threadIdx.x; k < nbk; k += BIN_THREADS) counts[size_t(k) * nb + blockIdx.x] = cnt[k];
@@ -153,7 +153,7 @@ template <class D>
 __global__ void __launch_bounds__(BIN_THREADS) bin_scatter_kernel(const D *deg, const uint8_t *ex, size_t n,
                                                                   int colors, const uint32_t *gid,
                                                                   const uint32_t *gbase, const uint32_t *offs,
-                                                                  unsigned nb, uint32_t *list) {
+                                                                  unsigned nb, uint32_t *list, BinLimits lim) {
   constexpr int NW = BIN_THREADS / 32;
   __shared__ uint32_t wcnt[NW][MAX_BUCKETS];
   __shared__ uint32_t run[MAX_BUCKETS];
@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(BIN_THREADS) bin_scatter_kernel(const D *deg, 
     __syncthreads();
     size_t j = base + r + threadIdx.x;
     int b = -1;
-    if (j < n && (!ex || ex[j])) b = bucket_of(j, (unsigned long long)deg[j], colors, gid, gbase);
+    if (j < n && (!ex || ex[j])) b = bucket_of(j, (unsigned long long)deg[j], colors, gid, gbase, lim);
     unsigned m = __match_any_sync(0xffffffffu, b);
     unsigned rank = __popc(m & ((1u << lane) - 1));
     if (b >= 0 && rank == 0) wcnt[wid][b] = __popc(m);
@@ -194,7 +194,7 @@ __global__ void bin_starts_kernel(const uint32_t *offs, unsigned nb, int nbk, co
 template <class D>
 void bin_items_impl(const D *deg, const uint8_t *ex, size_t n, int colors, const uint32_t *gid,
                     const uint32_t *gbase, uint32_t *list, size_t *bin_start, uint64_t *bin_maxdeg, uint32_t *scratch,
-                    uint32_t *host, cudaStream_t s) {
+                    uint32_t *host, cudaStream_t s, const BinLimits &lim) {
   const int nbk = colors * NUM_BINS;
   if (n == 0) {
     for (int b = 0; b <= nbk; ++b) bin_start[b] = 0;
@@ -210,10 +210,10 @@ void bin_items_impl(const D *deg, const uint8_t *ex, size_t n, int colors, const
   uint32_t *counts = total + 1;
   uint32_t *sscratch = counts + nc;
   LVG_CUDA(cudaMemsetAsync(maxdeg, 0, NUM_BINS * sizeof(unsigned long long), s));
-  bin_count_kernel<D><<<nb, BIN_THREADS, 0, s>>>(deg, ex, n, colors, gid, gbase, counts, maxdeg, nb);
+  bin_count_kernel<D><<<nb, BIN_THREADS, 0, s>>>(deg, ex, n, colors, gid, gbase, counts, maxdeg, nb, lim);
   LVG_CHECK_LAUNCH();
   exclusive_scan_impl<uint32_t>(counts, counts, nc, total, sscratch, s);
-  bin_scatter_kernel<D><<<nb, BIN_THREADS, 0, s>>>(deg, ex, n, colors, gid, gbase, counts, nb, list);
+  bin_scatter_kernel<D><<<nb, BIN_THREADS, 0, s>>>(deg, ex, n, colors, gid, gbase, counts, nb, list, lim);
   LVG_CHECK_LAUNCH();
   bin_starts_kernel<<<1, 256, 0, s>>>(counts, nb, nbk, total, starts);
   LVG_CHECK_LAUNCH();
@@ -260,15 +260,16 @@ size_t bin_host_elems(int colors) { return 2 * NUM_BINS + size_t(colors) * NUM_B
 
 void bin_items_u32(const uint32_t *deg, const uint8_t *ex, size_t n, int colors, uint32_t *list, size_t *bin_start,
                    uint64_t *bin_maxdeg, uint32_t *scratch, uint32_t *host_pinned, cudaStream_t s,
-                   const uint32_t *gid, const uint32_t *gbase) {
-  bin_items_impl<uint32_t>(deg, ex, n, colors, gid, gbase, list, bin_start, bin_maxdeg, scratch, host_pinned, s);
+                   const uint32_t *gid, const uint32_t *gbase, const BinLimits &lim) {
+  bin_items_impl<uint32_t>(deg, ex, n, colors, gid, gbase, list, bin_start, bin_maxdeg, scratch, host_pinned, s,
+                           lim);
 }
 
 void bin_items_u64(const uint64_t *deg, const uint8_t *ex, size_t n, int colors, uint32_t *list, size_t *bin_start,
                    uint64_t *bin_maxdeg, uint32_t *scratch, uint32_t *host_pinned, cudaStream_t s) {
   bin_items_impl<unsigned long long>(reinterpret_cast<const unsigned long long *>(deg), ex, n, colors, nullptr,
                                      nullptr, list,
-                                     bin_start, bin_maxdeg, scratch, host_pinned, s);
+                                     bin_start, bin_maxdeg, scratch, host_pinned, s, default_bin_limits());
 }
 
 }  // namespace lvg

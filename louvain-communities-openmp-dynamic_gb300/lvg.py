@@ -103,10 +103,12 @@ class _ServerStats(C.Structure):
 class _Tuning(C.Structure):
     _fields_ = [("frontier_colors", C.c_int), ("concurrent_bins", C.c_int), ("fused_small", C.c_int),
                 ("hub_chunk", C.c_uint32), ("big_blocks_per_sm", C.c_int), ("frontier_max_fraction", C.c_double),
-                ("hub_tables", C.c_int)]
+                ("hub_tables", C.c_int), ("bin_max_degree", C.c_uint32 * 12),
+                ("level_graphs", C.c_int), ("small_regs", C.c_int)]
 
     def as_dict(self) -> dict:
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        return {k: (list(v) if k == "bin_max_degree" else v)
+                for k, v in ((k, getattr(self, k)) for k, _ in self._fields_)}
 
 
 class _Stats(C.Structure):
@@ -118,7 +120,7 @@ class _Stats(C.Structure):
                 ("call_upload_ms", C.c_double), ("call_run_ms", C.c_double), ("call_download_ms", C.c_double),
                 ("move_bin_overflow", C.c_uint64 * 12), ("hub_chunk_overflow", C.c_uint64),
                 ("hub_table_slots", C.c_uint64), ("hub_table_overflow", C.c_uint64),
-                ("hub_tables_built", C.c_uint64), ("host_syncs", C.c_uint64)]
+                ("hub_tables_built", C.c_uint64), ("host_syncs", C.c_uint64), ("level_graphs", C.c_uint64)]
 
 
 class _Csr(C.Structure):
@@ -641,6 +643,7 @@ class Graph:
         hs = (C.c_void_p * max(len(graphs), 1))(*[g.h for g in graphs])
         G = Graph(None)
         _check(L.lvg_graph_create_union(hs, len(graphs), C.byref(G.h)))
+        G._union_spans = [g.span for g in graphs]
         return G
 
     @property
@@ -947,6 +950,9 @@ def set_tuning(g: Graph, **knobs) -> dict:
     t = _Tuning()
     _check(L.lvg_graph_get_tuning(g.h, C.byref(t)))
     for k, v in knobs.items():
+        if k == "bin_max_degree":  # a list of up to 12 limits (the rest 0)
+            v = list(v) + [0] * (12 - len(v))
+            v = (C.c_uint32 * 12)(*v)
         setattr(t, k, v)
     _check(L.lvg_graph_set_tuning(g.h, C.byref(t)))
     return t.as_dict()
@@ -1097,18 +1103,26 @@ def louvain_static_union(u: Graph, o: "LouvainOptions | None" = None) -> "list[L
     n = u.union_graphs
     res = (_Result * max(n, 1))()
     opt = (o or LouvainOptions())._struct()
+    # every graph's result arrays are views into three arrays for the whole
+    # union, passed as caller buffers: the library writes them in place
+    spans = getattr(u, "_union_spans", None)
+    if spans is None or len(spans) != n:
+        raise RuntimeError("graph union without its graphs' spans (build it with Graph.union)")
+    vb = np.concatenate([[0], np.cumsum(spans, dtype=np.int64)])
+    allm = np.empty(int(vb[-1]) + 1, np.uint32)
+    allv = np.empty(int(vb[-1]) + 1, np.float64)
+    allc = np.empty(int(vb[-1]) + 1, np.float64)
+    views = []
+    for i in range(n):
+        a, b = int(vb[i]), int(vb[i + 1])
+        views.append((allm[a:b], allv[a:b], allc[a:b]))
+        res[i].span = b - a
+        res[i].membership = allm[a:].ctypes.data_as(C.POINTER(C.c_uint32))
+        res[i].vertexWeight = allv[a:].ctypes.data_as(C.POINTER(C.c_double))
+        res[i].communityWeight = allc[a:].ctypes.data_as(C.POINTER(C.c_double))
     _check(L.lvg_static_union(u.h, C.byref(opt), res))
     st = u.stats()
-    out = []
-    for i in range(n):
-        r = res[i]
-        S = r.span
-        m = np.ctypeslib.as_array(r.membership, (S,)).copy() if S else np.zeros(0, np.uint32)
-        vw = np.ctypeslib.as_array(r.vertexWeight, (S,)).copy() if S else np.zeros(0)
-        cw = np.ctypeslib.as_array(r.communityWeight, (S,)).copy() if S else np.zeros(0)
-        L.lvg_result_free(C.byref(r))
-        out.append(LouvainResult(m, vw, cw, **_scalars(r), stats=st))
-    return out
+    return [LouvainResult(*views[i], **_scalars(res[i]), stats=st) for i in range(n)]
 
 
 def louvain_static_many(graphs: "list[Graph]", o: "LouvainOptions | None" = None, workers: int = 16,

@@ -79,3 +79,50 @@ def test_resident_frontier_waits_once(cuda, golden):
     m, vt, ct = st_out.get()
     ex = golden.y.exists.astype(bool)
     assert (m[ex] < golden.y.span).all()
+
+
+@pytest.mark.parametrize("method", [0, 3])
+def test_level_phase_graphs(cuda, orc, golden, method):
+    """Aggregated levels: the iterations after a level's first run as one
+    graph launch built for the level (lvg_tuning.level_graphs). Deterministic
+    results equal the oracle's replay with the graphs on and off, and the
+    graphs never add synchronisations."""
+    o = cuda.LouvainOptions(deterministic=True)
+    x = golden.x if method == 0 else golden.y
+    if method == 0:
+        m, vt, ct, info = orc.louvain(x, 0, threads=4, sync=True, colors=o.effective_colors())
+    else:
+        m, vt, ct, info = orc.louvain(x, method, golden.b, *prior(golden), threads=4, sync=True,
+                                      colors=o.effective_colors())
+    syncs, graphs = {}, {}
+    for on in (1, 0, 1):
+        G = cuda.Graph(x)
+        cuda.set_tuning(G, level_graphs=on)
+        r = cuda.louvain_static(G, o) if method == 0 else \
+            cuda.louvain_dynamic_frontier(G, golden.b, *prior(golden), o)
+        assert np.array_equal(r.membership, m), on
+        assert np.array_equal(r.vertexWeight, vt), on
+        assert np.array_equal(r.communityWeight, ct), on
+        assert (r.iterations, r.passes, r.affectedVertices) == (info["iterations"], info["passes"],
+                                                                info["affectedVertices"]), on
+        st = G.stats()
+        syncs[on], graphs[on] = st["host_syncs"], st["level_graphs"]
+    assert graphs[0] == 0
+    assert syncs[1] <= syncs[0], (syncs, graphs)
+
+
+def test_level_phase_graphs_in_a_union(cuda, orc, lvg):
+    """A graph union's aggregated levels run their later iterations as one
+    graph too (the loop goes on while any graph still moves); each graph's
+    deterministic result equals the oracle's replay of it alone."""
+    gs = [lvg.planted_partition(3000 + 2000 * i, 48, 12, 0.75, seed=90 + i) for i in range(4)]
+    o = cuda.LouvainOptions(deterministic=True)
+    U = cuda.Graph.union([cuda.Graph(g) for g in gs])
+    cuda.set_tuning(U, level_graphs=1)
+    rs = cuda.louvain_static_union(U, o)
+    assert U.stats()["level_graphs"] > 0
+    for i, g in enumerate(gs):
+        m, vt, ct, info = orc.louvain(g, 0, threads=4, sync=True, colors=o.effective_colors())
+        assert np.array_equal(rs[i].membership, m), i
+        assert np.array_equal(rs[i].communityWeight, ct), i
+        assert (rs[i].iterations, rs[i].passes) == (info["iterations"], info["passes"]), i
