@@ -1089,6 +1089,11 @@ int lvg_autotune(lvg_graph *g, int method, const lvg_device_batch *b, const lvg_
         lvg_tuning t = cur;
         set(t, v);
         if (!std::memcmp(&t, &cur, sizeof(t))) continue;
+        try {  // e.g. a bin's full reach above a later bin's lowered limit
+          check_tuning(t);
+        } catch (const Error &) {
+          continue;
+        }
         double q = 0;
         const double tm = measure(t, guard ? &q : nullptr);
         if (tm < 0.98 * tcur && (!guard || q >= qref - 1e-3)) {
@@ -1116,14 +1121,27 @@ int lvg_autotune(lvg_graph *g, int method, const lvg_device_batch *b, const lvg_
         try_knob([](lvg_tuning &t, long v) { t.small_regs = int(v); }, {32, 64}, false);
       }
       try_knob([](lvg_tuning &t, long v) { t.big_blocks_per_sm = int(v); }, {0, 2, 3, 4}, false);
-      // the degree bins: each bin at its full reach, or its degrees handed to
-      // the next bin (its wider tile and larger table); bin 9 also split at
-      // 1024. A limit of BIN_MAX_DEGREE[b-1] is never below the previous
-      // bin's, whatever that bin's own choice.
+      // the degree from which a block per vertex (bin 9's kernel) serves:
+      // every warp bin (6-8) reaching above it is emptied into bin 9 (on
+      // R-MAT s24 DF, degrees 129-512 took 46 us as a warp per vertex and the
+      // step 0.178 ms; in bin 9's blocks the step took 0.161 ms)
+      try_knob(
+          [](lvg_tuning &t, long v) {
+            for (int b = 6; b <= 8; ++b)
+              t.bin_max_degree[b] = v && BIN_MAX_DEGREE[b] > uint64_t(v) ? uint32_t(v) : 0u;
+          },
+          {0, 256, 128, 64}, false);
+      // the degree bins: each bin at its full reach, at the previous bin's
+      // reach, or emptied (all its degrees handed on to the next bin's wider
+      // tile and larger table; after the previous bin was emptied too, a run
+      // of bins goes to one kernel); bin 9 also split at 1024. Each candidate
+      // is at least the previous bin's limit.
       for (int b = 2; b <= 9; ++b) {
         auto set = [b](lvg_tuning &t, long v) { t.bin_max_degree[b] = uint32_t(v); };
-        if (b == 9) try_knob(set, {0, 1024, long(BIN_MAX_DEGREE[8])}, false);
-        else try_knob(set, {0, long(BIN_MAX_DEGREE[b - 1])}, false);
+        const long prev = long(bin_limits_of(cur).hi[b - 1]);
+        const long half = std::max(prev, long(BIN_MAX_DEGREE[b - 1]));
+        if (b == 9) try_knob(set, {0, 1024, half, prev}, false);
+        else try_knob(set, {0, half, prev}, false);
       }
       // aggregated levels' iterations as one graph launch per level, or
       // launched from the host iteration by iteration

@@ -177,7 +177,10 @@ __device__ __forceinline__ void tile_loop(const MoveArgs &a, const uint32_t *lis
     // is; fixed within a class in deterministic mode)
     double wu = 0.0, td = 0.0;
     if (tl == 0) { wu = a.vtot[u]; td = a.ctot[d]; }
-#pragma unroll
+    // (the table loops unrolled by at most 8: the 512- and 1024-slot tables'
+    // fully unrolled loops stalled the fused degree 129-512 launch on
+    // instruction fetch)
+#pragma unroll 8
     for (int s = tl; s < C; s += T) { keys[s] = EMPTY; vals[s] = 0.f; }
     __syncwarp(m);
     float kd = 0.f;
@@ -248,7 +251,7 @@ __device__ __forceinline__ void tile_loop(const MoveArgs &a, const uint32_t *lis
     const float wuf = __double2float_rn(wu);
     float bg = 0.f;
     uint32_t bc = EMPTY;
-#pragma unroll
+#pragma unroll 8
     for (int s = tl; s < C; s += T) {
       const uint32_t c = keys[s];
       if (c == EMPTY) continue;
@@ -712,6 +715,10 @@ __global__ void __launch_bounds__(B) hub_chunk_kernel(MoveArgs a) {
   t.list = reinterpret_cast<uint32_t *>(smem + size_t(CS) * 8);
   t.used = &s_used;
   const size_t ci = a.hub.chunk_begin[a.color] + blockIdx.x;
+  if (a.ht.key && ld_relaxed(a.ht.nbad) == 0) {  // every hub is done by hub_table_kernel
+    if (threadIdx.x == 0) a.chunk_cnt[ci] = EMPTY;  // (the merge may still find a table gone bad)
+    return;
+  }
   const uint4 ch = a.hub.chunk[ci];
   const uint32_t u = ch.w;  // the hub vertex
   if (threadIdx.x == 0) {
