@@ -394,8 +394,9 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot
   const bool conc = bin_ev == nullptr && g->tuning.concurrent_bins;
   if (conc) ensure_aux(g);
   auto stream_of = [&](int b) { const int i = bin_stream(b); return conc && i >= 0 ? g->aux[i] : s; };
-  LVG_CUDA(cudaMemsetAsync(&g->ctr.p->el_fix, 0, sizeof(unsigned long long), s));
-  LVG_CUDA(cudaMemsetAsync(W.wl_count.p, 0, size_t(K) * NUM_BINS * sizeof(uint32_t), s));
+  // (kernels, not memsets: a memset waits for the copies in flight)
+  launch_fill_bytes(&g->ctr.p->el_fix, 0, sizeof(unsigned long long), s);
+  launch_fill_bytes(W.wl_count.p, 0, size_t(K) * NUM_BINS * sizeof(uint32_t), s);
   for (int k = 0; k < K; ++k) {
     // this class's active vertices of bins 1..NUM_BINS-2 -> worklists
     BinBounds bb;
@@ -493,7 +494,7 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot
   }
   // worklists filled while a dynamic-frontier batch was marked serve the
   // first iteration only
-  if (K == 1 && !uc) LVG_CUDA(cudaMemsetAsync(&g->ctr.p->pre_flag, 0, sizeof(unsigned int), s));
+  if (K == 1 && !uc) launch_fill_bytes(&g->ctr.p->pre_flag, 0, sizeof(unsigned int), s);
   if (uc) launch_iter_control(uc->n, uc->ctl, uc->gact, uc->fix, uc->M, uc->E, uc->L, g->ctr.p, s);
   if (read_back) LVG_CUDA(cudaMemcpyAsync(g->hctr.p, g->ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
 }
@@ -599,7 +600,7 @@ bool run_level_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, 
     cudaGraphExec_t e;
     ~Drop() { cudaGraphExecDestroy(e); }
   } drop{pg.exec};
-  LVG_CUDA(cudaMemsetAsync(&g->ctr.p->dev_iters, 0, sizeof(unsigned int), s));
+  launch_fill_bytes(&g->ctr.p->dev_iters, 0, sizeof(unsigned int), s);
   LVG_CUDA(cudaGraphLaunch(pg.exec, s));
   LVG_CUDA(cudaMemcpyAsync(g->hctr.p, g->ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
   host_sync(g);
@@ -744,7 +745,7 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const 
   int l = 0;
   double el = 0;
   if (phase_graphs && g->phase_exec && g->phase_key == key) {
-    LVG_CUDA(cudaMemsetAsync(&g->ctr.p->dev_iters, 0, sizeof(unsigned int), s));
+    launch_fill_bytes(&g->ctr.p->dev_iters, 0, sizeof(unsigned int), s);
     LVG_CUDA(cudaGraphLaunch(g->phase_exec, s));
     LVG_CUDA(cudaMemcpyAsync(g->hctr.p, g->ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
     if (tail) {
@@ -930,7 +931,8 @@ Level aggregate(lvg_graph *g, const Level &lv, const uint32_t *com, size_t CN, i
 // on_init (optional) is called once, in the last repetition, with an event
 // recorded when the first level's vertex weights (out.vt) are final.
 void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out, const lvg_options &o,
-         RunInfo &info, const std::function<void(cudaEvent_t)> *on_init, HubTables *tprior, HubTables *tout) {
+         RunInfo &info, const std::function<void(cudaEvent_t)> *on_init, HubTables *tprior, HubTables *tout,
+         bool vt_ready) {
   if (g->uni) throw Error(LVG_EINVAL, "graph union: run it with lvg_static_union");
   ensure_ws(g);
   Workspace &W = *g->ws;
@@ -948,7 +950,7 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
   tot_t *utot = out.vt, *ctot = out.ct;
   g->stats = lvg_stats{};
   const unsigned long long launches0 = launch_counter();
-  LVG_CUDA(cudaMemsetAsync(g->ctr.p, 0, sizeof(Counters), s));
+  launch_fill_bytes(g->ctr.p, 0, sizeof(Counters), s);
   // resident hub tables: the dynamic methods on a unit-weight graph, between
   // two states (lvg_run_resident)
   const bool tabs0 = tprior && tout && method != LVG_METHOD_STATIC && g->tuning.hub_tables && g->base.unit;
@@ -957,9 +959,9 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
     g->events.reset();
     set_base_colors(g, K1 ? K1 : K);
     // Reset buffers, as the reference does before each repetition.
-    LVG_CUDA(cudaMemsetAsync(W.vaff.p, 0, S, s));
-    LVG_CUDA(cudaMemsetAsync(W.vcom.p, 0, S * sizeof(uint32_t), s));
-    LVG_CUDA(cudaMemsetAsync(W.vtot.p, 0, S * sizeof(tot_t), s));
+    launch_fill_bytes(W.vaff.p, 0, S, s);
+    launch_fill_bytes(W.vcom.p, 0, S * sizeof(uint32_t), s);
+    launch_fill_bytes(W.vtot.p, 0, S * sizeof(tot_t), s);
     // The prior state into place: the reference moves its copies of it
     // (louvainSetupInitialsW, inc/louvain.hxx:1240) in without copying, so
     // the copy stays outside the timed section as its copies do.
@@ -998,6 +1000,9 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
       if (tprior != tout) copy_hub_tables(g, *tout, *tprior);  // the prior's own cache, before any move
       g->stats.hub_tables_built = 1;
     }
+    // the vertex weights' side of the batch update, unless the caller made it
+    // (vt_ready: one run, its prior's weights updated before it started)
+    tot_t *vt_upd = vt_ready && r == 0 ? nullptr : utot;
     // fi: initial membership and weights. Dynamic frontier: fm (the marking)
     // runs in the same pass over the batch (df_start_kernel; its time counts
     // as initialisation), and with one colour class it also lists the marked
@@ -1009,11 +1014,11 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
       const bool lists = K == 1 && g->base.colors == 1;
       if (lists)
         for (int x = 0; x <= NUM_BINS; ++x) bb.start[x] = g->base.bin_start[x];
-      launch_df_start(b.ds, b.dd, b.dw, b.nd, b.is, b.id, b.iw, b.ni, ucom, utot, ctot, g->base, W.vaff.p,
+      launch_df_start(b.ds, b.dd, b.dw, b.nd, b.is, b.id, b.iw, b.ni, ucom, vt_upd, ctot, g->base, W.vaff.p,
                       lists ? &bb : nullptr, W.wl.p, g->ctr.p, s);
     } else {
-      launch_batch_weights(b.ds, b.dw, b.nd, -1.f, ucom, utot, ctot, s);
-      launch_batch_weights(b.is, b.iw, b.ni, +1.f, ucom, utot, ctot, s);
+      launch_batch_weights(b.ds, b.dw, b.nd, -1.f, ucom, vt_upd, ctot, s);
+      launch_batch_weights(b.is, b.iw, b.ni, +1.f, ucom, vt_upd, ctot, s);
     }
     cudaEvent_t e1 = g->events.record(s);
     if (on_init && r == rep - 1) (*on_init)(e1);
@@ -1403,18 +1408,50 @@ void download_result(lvg_graph *g, lvg_result *out, StateRef st, bool skip_vw = 
   LVG_CUDA(cudaStreamSynchronize(s));
 }
 
+// cq[k] (optional): cached memberships to compare the uploaded one with
+// (g->hctr.p->qdiff[k] after the call).
 void upload_prior(lvg_graph *g, const uint32_t *q, const double *qvtot, const double *qctot, uint32_t *dq,
-                  tot_t *dvt, tot_t *dct) {
+                  tot_t *dvt, tot_t *dct, const uint32_t *const *cq) {
   cudaStream_t s = g->stream;
   const size_t S = g->base.span;
   if (!q || !qvtot || !qctot) throw Error(LVG_EINVAL, "prior state: null array");
-  // the device keeps the totals in FP64, as the caller passes them
+  // the device keeps the totals in FP64, as the caller passes them (dvt
+  // nullptr: the vertex weights were uploaded already)
   LVG_CUDA(cudaMemcpyAsync(dq, q, S * 4, cudaMemcpyHostToDevice, s));
-  LVG_CUDA(cudaMemcpyAsync(dvt, qvtot, S * sizeof(tot_t), cudaMemcpyHostToDevice, s));
+  if (dvt) LVG_CUDA(cudaMemcpyAsync(dvt, qvtot, S * sizeof(tot_t), cudaMemcpyHostToDevice, s));
   LVG_CUDA(cudaMemcpyAsync(dct, qctot, S * sizeof(tot_t), cudaMemcpyHostToDevice, s));
   // every prior id must be < span (checked on the device; read back before any use)
-  launch_check_ids(dq, S, uint32_t(S), g->ctr.p, s);
+  if (cq) launch_check_prior(dq, S, uint32_t(S), cq[0], cq[1], g->ctr.p, s);
+  else launch_check_ids(dq, S, uint32_t(S), g->ctr.p, s);
   read_counters(g);
+}
+
+// The host-call table caches after a batch apply made graph version
+// g->version from g->version - 1 with the tidied batch (ds, dd | is, id):
+// a cache of the old version gets the batch's edges (each changes one
+// neighbour count of a hub), as long as the set of hubs is the same; any
+// other cache is dropped.
+void advance_host_tables(lvg_graph *g, const uint32_t *ds, const uint32_t *dd, size_t nd, const uint32_t *is,
+                         const uint32_t *id, size_t ni) {
+  bool any = false;
+  for (auto &e : g->htab) {
+    if (e.t.version != ~0ull && e.t.version + 1 == g->version) any = true;
+    else e.t.version = ~0ull;
+  }
+  if (!any) return;
+  ensure_hub_index(g);
+  cudaStream_t s = g->stream;
+  for (auto &e : g->htab) {
+    if (e.t.version == ~0ull) continue;
+    if (e.t.index != g->hub_index_gen || e.t.hubs != g->hub_ids_h.size()) {
+      e.t.version = ~0ull;
+      continue;
+    }
+    const HubTabView v = e.t.view(g->hub_slot.p);
+    launch_ht_batch(ds, dd, nd, false, e.q.p, v, g->ctr.p, s);
+    launch_ht_batch(is, id, ni, true, e.q.p, v, g->ctr.p, s);
+    e.t.version = g->version;
+  }
 }
 
 int run_host(lvg_graph *g, int method, const lvg_batch *b, const uint32_t *q, const double *qvtot,
@@ -1436,11 +1473,64 @@ int run_host(lvg_graph *g, int method, const lvg_batch *b, const uint32_t *q, co
                  g->b_iw, g->b_seg, db);
     StateRef st{W.ucom.p, W.utot.p, W.ctot.p};
     StateRef prior{nullptr, nullptr, nullptr};
+    // resident hub tables for a prior that comes from the host: those of a
+    // cached membership equal to it (exactly: compared on the device with
+    // the upload's id check), else built for it by the run into the least
+    // recently used cache
+    const bool tabs = method != LVG_METHOD_STATIC && opt.repeat <= 1 && g->tuning.hub_tables && g->base.unit &&
+                      g->base.hub.hubs > 0;
+    HubTables *tprior = nullptr;
+    int slot = -1;
+    // The vertex weights of a dynamic run are the prior's plus the batch's
+    // (louvainUpdateWeightsFromOmpU) and final from there on. Into a pinned
+    // result array they are uploaded first, updated, and copied back on a
+    // side stream while the rest of the prior uploads (the host link carries
+    // both directions at once); their download is over before the run starts
+    // (a download in flight slowed the run's kernels several-fold).
+    cudaPointerAttributes pa{};
+    const bool early = method != LVG_METHOD_STATIC && opt.repeat <= 1 && qvtot && out->vertexWeight &&
+                       cudaPointerGetAttributes(&pa, out->vertexWeight) == cudaSuccess &&
+                       pa.type == cudaMemoryTypeHost;
+    cudaGetLastError();
+    if (early) {
+      for (auto &e : g->vt_ev)
+        if (!e) LVG_CUDA(cudaEventCreate(&e));
+      if (!g->copy_stream) LVG_CUDA(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
+      LVG_CUDA(cudaMemcpyAsync(st.vt, qvtot, W.S * sizeof(tot_t), cudaMemcpyHostToDevice, g->stream));
+      LVG_CUDA(cudaEventRecord(g->vt_ev[0], g->stream));
+      launch_batch_weights(db.ds, db.dw, db.nd, -1.f, nullptr, st.vt, nullptr, g->stream);
+      launch_batch_weights(db.is, db.iw, db.ni, +1.f, nullptr, st.vt, nullptr, g->stream);
+      LVG_CUDA(cudaEventRecord(g->vt_ev[1], g->stream));
+      LVG_CUDA(cudaStreamWaitEvent(g->copy_stream, g->vt_ev[1], 0));
+      LVG_CUDA(cudaMemcpyAsync(out->vertexWeight, st.vt, W.S * sizeof(tot_t), cudaMemcpyDeviceToHost,
+                               g->copy_stream));
+    }
     if (method != LVG_METHOD_STATIC) {
       if (opt.repeat <= 1) {
         // one run: the prior goes straight where the run starts from
-        upload_prior(g, q, qvtot, qctot, st.q, st.vt, st.ct);
+        const uint32_t *cq[2] = {nullptr, nullptr};
+        if (tabs) {
+          ensure_hub_index(g);
+          for (int k = 0; k < 2; ++k) {
+            const HubTables &t = g->htab[k].t;
+            if (t.version == g->version && t.index == g->hub_index_gen && g->htab[k].q.n >= W.S)
+              cq[k] = g->htab[k].q.p;
+          }
+        }
+        upload_prior(g, q, qvtot, qctot, st.q, early ? nullptr : st.vt, st.ct, tabs ? cq : nullptr);
         prior = st;
+        if (tabs) {
+          for (int k = 0; k < 2; ++k)
+            if (cq[k] && !g->hctr.p->qdiff[k]) slot = k;
+          if (slot < 0) {  // the run builds the tables of this prior into the older cache
+            slot = g->htab[0].stamp <= g->htab[1].stamp ? 0 : 1;
+            g->htab[slot].q.ensure(W.S);
+            LVG_CUDA(cudaMemcpyAsync(g->htab[slot].q.p, st.q, W.S * 4, cudaMemcpyDeviceToDevice, g->stream));
+            g->htab[slot].t.version = ~0ull;
+          }
+          g->htab[slot].stamp = ++g->htab_clock;
+          tprior = &g->htab[slot].t;
+        }
       } else {  // every repetition starts from the same prior
         W.prior_q.ensure(W.S); W.prior_vt.ensure(W.S); W.prior_ct.ensure(W.S);
         upload_prior(g, q, qvtot, qctot, W.prior_q.p, W.prior_vt.p, W.prior_ct.p);
@@ -1448,24 +1538,25 @@ int run_host(lvg_graph *g, int method, const lvg_batch *b, const uint32_t *q, co
       }
     }
     LVG_CUDA(cudaStreamSynchronize(g->stream));
+    // the early weight download ends before the run's kernels start
+    if (early) LVG_CUDA(cudaStreamSynchronize(g->copy_stream));
     const auto t1 = std::chrono::steady_clock::now();
     RunInfo info;
-    // The vertex weights are final once the run has initialised: into a
-    // pinned result array they are copied out on a side stream while the
-    // local moving runs (the host link is full duplex).
-    cudaPointerAttributes pa{};
-    const bool early = out->vertexWeight &&
-                       cudaPointerGetAttributes(&pa, out->vertexWeight) == cudaSuccess &&
-                       pa.type == cudaMemoryTypeHost;
-    cudaGetLastError();
-    std::function<void(cudaEvent_t)> hook = [&](cudaEvent_t ready) {
-      if (!g->copy_stream) LVG_CUDA(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
-      const size_t S = g->base.span;
-      LVG_CUDA(cudaStreamWaitEvent(g->copy_stream, ready, 0));
-      LVG_CUDA(cudaMemcpyAsync(out->vertexWeight, st.vt, S * sizeof(tot_t), cudaMemcpyDeviceToHost,
-                               g->copy_stream));
-    };
-    run(g, method, db, prior, st, opt, info, early ? &hook : nullptr);
+    run(g, method, db, prior, st, opt, info, nullptr, tprior, tabs ? &g->hwork : nullptr, early);
+    if (early) {  // the weight update belongs to the run's initialisation
+      const float vt_ms = elapsed(g->vt_ev[0], g->vt_ev[1]);
+      info.t += vt_ms;
+      info.ti += vt_ms;
+    }
+    if (tabs && g->hwork.version == g->version) {
+      // the result's tables, in the other cache (the next call's prior is
+      // often this result)
+      auto &e = g->htab[1 - slot];
+      e.q.ensure(W.S);
+      LVG_CUDA(cudaMemcpyAsync(e.q.p, st.q, W.S * 4, cudaMemcpyDeviceToDevice, g->stream));
+      copy_hub_tables(g, g->hwork, e.t);
+      e.stamp = ++g->htab_clock;
+    }
     fill_result(out, info, g->base.span);
     const auto t2 = std::chrono::steady_clock::now();
     download_result(g, out, st, early);
@@ -1733,6 +1824,7 @@ PlanCounts tidy_apply(lvg_graph *g, const uint32_t *ds, const uint32_t *dd, cons
     out.nd = g->hcnt.p[0];
     out.ni = g->hcnt.p[1] - g->hcnt.p[0];
   }
+  if (pc.nrows) advance_host_tables(g, tds, tdd, out.nd, tis, tid, out.ni);
   return out;
 }
 

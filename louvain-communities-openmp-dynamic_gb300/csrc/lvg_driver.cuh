@@ -253,6 +253,21 @@ struct lvg_graph {
   std::vector<uint32_t> hub_ids_h, hub_deg_h;
   uint64_t hub_index_version = ~0ull, hub_index_gen = 0;
   HubTables ht_tune;  // the result tables of the autotuner's runs
+  // Resident hub tables for the host-array entry points (lvg_naive_dynamic,
+  // lvg_delta_screening, lvg_frontier), whose prior comes from host memory
+  // on every call: two memberships (a device copy of each) with their
+  // tables, taken when a call's uploaded prior equals one of them exactly,
+  // the least recently used replaced otherwise; a batch apply carries the
+  // current ones to the new graph version. hwork: a call's result tables.
+  struct HostTables {
+    DBuf<uint32_t> q;
+    HubTables t;
+    uint64_t stamp = 0;
+  };
+  HostTables htab[2];
+  HubTables hwork;
+  uint64_t htab_clock = 0;
+  cudaEvent_t vt_ev[2] = {nullptr, nullptr};  // the host entry points' early vertex-weight update
   // Gapped CSR: row u holds deg[u] entries at off[u] with room for cap[u];
   // rows that outgrow their room move to the overflow pool, entries
   // [pool_begin, slots) of key/w. Unused entries hold (0, 0.0).
@@ -307,6 +322,8 @@ struct lvg_graph {
       if (a) cudaStreamDestroy(a);
     if (fork_ev) cudaEventDestroy(fork_ev);
     for (auto &e : join_ev)
+      if (e) cudaEventDestroy(e);
+    for (auto &e : vt_ev)
       if (e) cudaEventDestroy(e);
   }
   bool profiling = false;
@@ -388,7 +405,7 @@ Level aggregate(lvg_graph *g, const Level &lv, const uint32_t *com, size_t CN, i
 // state (the same object for a run in place).
 void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out, const lvg_options &o,
          RunInfo &info, const std::function<void(cudaEvent_t)> *on_init = nullptr, HubTables *tprior = nullptr,
-         HubTables *tout = nullptr);
+         HubTables *tout = nullptr, bool vt_ready = false);
 void run_union(lvg_graph *g, const lvg_options &o, RunInfo &info);
 void check_batch(const lvg_graph *g, const lvg_batch *b, bool need_sorted);
 size_t max_group(const lvg_batch *b);
@@ -396,7 +413,8 @@ void upload_batch(lvg_graph *g, const lvg_batch *b, DBuf<uint32_t> &ds, DBuf<uin
                   DBuf<uint32_t> &is, DBuf<uint32_t> &id, DBuf<float> &iw, DBuf<uint32_t> &seg, DBatch &out);
 void fill_result(lvg_result *out, const RunInfo &info, size_t span);
 void upload_prior(lvg_graph *g, const uint32_t *q, const double *qvtot, const double *qctot, uint32_t *dq,
-                  tot_t *dvt, tot_t *dct);
+                  tot_t *dvt, tot_t *dct,
+                  const uint32_t *const *cq = nullptr);
 int run_host(lvg_graph *g, int method, const lvg_batch *b, const uint32_t *q, const double *qvtot,
              const double *qctot, const lvg_options *o, lvg_result *out);
 void init_graph(lvg_graph *g, size_t span, size_t order, size_t X, const uint64_t *coff, const uint32_t *ckey,

@@ -167,6 +167,7 @@ struct Counters {
   // first compaction takes them instead of scanning the flags.
   unsigned int pre_flag;
   uint32_t pre_count[NUM_BINS];
+  unsigned int qdiff[2];  // an uploaded prior differs from the host-call table caches' memberships
   unsigned long long ht_slots;                // hub-table slots read by hub_table_kernel
   unsigned long long ht_over;                 // hub tables that ran out of room (their hubs scan again)
 };
@@ -363,6 +364,9 @@ void bin_items_u64(const uint64_t *deg, const uint8_t *ex, size_t n, int colors,
 int grid_for(size_t n, int block, int max_blocks_per_sm = 8);
 void launch_degrees(const uint64_t *off, uint32_t *deg, size_t span, cudaStream_t s);
 void launch_fill_u8(uint8_t *p, uint8_t v, size_t n, cudaStream_t s);
+// n bytes of value v at p, stored by a kernel (never queued behind the copy
+// engines' transfers, as a memset is)
+void launch_fill_bytes(void *p, uint8_t v, size_t n, cudaStream_t s);
 void launch_fill_f32(float *p, size_t n, float v, cudaStream_t s);
 void launch_init_static(const Level &g, uint32_t *ucom, tot_t *utot, tot_t *ctot, cudaStream_t s);
 void launch_total_weight(const float *w, size_t n, Counters *ctr, cudaStream_t s);  // -> ctr->fp64[0]
@@ -450,6 +454,10 @@ void launch_iter_end(Counters *ctr, double M, double E, int L, bool by_graph, cu
                      cudaStream_t s);
 // Set ERR_BAD_ID in ctr->err if any a[i] >= limit.
 void launch_check_ids(const uint32_t *a, size_t n, uint32_t limit, Counters *ctr, cudaStream_t s);
+// launch_check_ids on a prior membership q, and ctr->qdiff[k] = whether q
+// differs from the cached membership c0 / c1 (nullptr: not compared).
+void launch_check_prior(const uint32_t *q, size_t n, uint32_t limit, const uint32_t *c0, const uint32_t *c1,
+                        Counters *ctr, cudaStream_t s);
 void launch_modularity(const Level &g, const uint32_t *memb, double *ctot64, Counters *ctr, cudaStream_t s);
 void launch_sq_sum(const double *x, size_t n, Counters *ctr, cudaStream_t s);  // -> ctr->fp64[2]
 

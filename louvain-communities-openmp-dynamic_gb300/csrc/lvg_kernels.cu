@@ -130,10 +130,10 @@ __global__ void batch_weights_kernel(const uint32_t *src, const float *w, size_t
     if (i < n) {
       u = src[i];
       x = double(sign) * double(w[i]);
-      c = vcom[u];
+      if (ctot) c = vcom[u];
     }
-    group_add(vtot, u, x, lane);
-    group_add(ctot, c, x, lane);
+    if (vtot) group_add(vtot, u, x, lane);  // either side may be left out
+    if (ctot) group_add(ctot, c, x, lane);
   }
 }
 
@@ -186,7 +186,7 @@ __global__ void df_start_kernel(const uint32_t *ds, const uint32_t *dd, const fl
       c = vcom[u];
       mark = del ? c == vcom[v] : c != vcom[v];
     }
-    group_add(vtot, u, x, lane);
+    if (vtot) group_add(vtot, u, x, lane);  // (nullptr: updated before the run)
     group_add(ctot, c, x, lane);
     int b = -1;
     if (mark) {
@@ -891,6 +891,23 @@ __global__ void check_ids_kernel(const uint32_t *a, size_t n, uint32_t limit, un
   if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(err, ERR_BAD_ID);
 }
 
+// check_ids_kernel, and whether q equals the cached memberships c0 / c1
+// (nullptr: not compared): diff[k] is set if any entry differs.
+__global__ void check_prior_kernel(const uint32_t *q, size_t n, uint32_t limit, const uint32_t *c0,
+                                   const uint32_t *c1, unsigned int *err, unsigned int *diff) {
+  bool bad = false, d0 = false, d1 = false;
+  GRID_STRIDE(i, n) {
+    const uint32_t x = q[i];
+    bad |= x >= limit;
+    if (c0) d0 |= __ldcs(c0 + i) != x;
+    if (c1) d1 |= __ldcs(c1 + i) != x;
+  }
+  const bool lead = (threadIdx.x & 31) == 0;
+  if (__any_sync(0xffffffffu, bad) && lead) atomicOr(err, ERR_BAD_ID);
+  if (__any_sync(0xffffffffu, d0) && lead) atomicOr(&diff[0], 1u);
+  if (__any_sync(0xffffffffu, d1) && lead) atomicOr(&diff[1], 1u);
+}
+
 // Flags equal to 1, sixteen bytes per load (bytewise compares); the tail
 // past the last whole 16-byte word bytewise.
 __global__ void count_flags_kernel(const uint8_t *f, size_t n, unsigned long long *dst) {
@@ -963,6 +980,30 @@ void launch_degrees(const uint64_t *off, uint32_t *deg, size_t span, cudaStream_
 
 void launch_fill_u8(uint8_t *p, uint8_t v, size_t n, cudaStream_t s) {
   if (n) LVG_CUDA(cudaMemsetAsync(p, v, n, s));
+}
+
+// Byte fill by the SMs: 16-byte stores over the aligned middle, bytes at
+// the ends. A memset queues behind the copies in flight on the device's copy
+// engines (a result download on a side stream held the dynamic-frontier
+// step's in-graph resets for its whole 0.7 ms); a kernel does not.
+__global__ void fill_bytes_kernel(uint8_t *p, size_t n, uint8_t v) {
+  const size_t head = (16 - (reinterpret_cast<uintptr_t>(p) & 15)) & 15;
+  const size_t h = head < n ? head : n;
+  const size_t words = (n - h) / 16;
+  const size_t tail = h + words * 16;
+  const uint32_t b4 = 0x01010101u * v;
+  const uint4 w = make_uint4(b4, b4, b4, b4);
+  uint4 *q = reinterpret_cast<uint4 *>(p + h);
+  const size_t t0 = size_t(blockIdx.x) * blockDim.x + threadIdx.x, st = size_t(gridDim.x) * blockDim.x;
+  for (size_t i = t0; i < words; i += st) q[i] = w;
+  for (size_t i = t0; i < h; i += st) p[i] = v;
+  for (size_t i = tail + t0; i < n; i += st) p[i] = v;
+}
+
+void launch_fill_bytes(void *p, uint8_t v, size_t n, cudaStream_t s) {
+  if (!n) return;
+  fill_bytes_kernel<<<grid_for((n + 15) / 16, 256), 256, 0, s>>>(static_cast<uint8_t *>(p), n, v);
+  LVG_CHECK_LAUNCH();
 }
 
 void launch_fill_f32(float *p, size_t n, float v, cudaStream_t s) {
@@ -1177,6 +1218,14 @@ void launch_check_ids(const uint32_t *a, size_t n, uint32_t limit, Counters *ctr
   LVG_CHECK_LAUNCH();
 }
 
+void launch_check_prior(const uint32_t *q, size_t n, uint32_t limit, const uint32_t *c0, const uint32_t *c1,
+                        Counters *ctr, cudaStream_t s) {
+  LVG_CUDA(cudaMemsetAsync(ctr->qdiff, 0, sizeof(ctr->qdiff), s));
+  if (!n) return;
+  check_prior_kernel<<<grid_for(n, 256), 256, 0, s>>>(q, n, limit, c0, c1, &ctr->err, ctr->qdiff);
+  LVG_CHECK_LAUNCH();
+}
+
 void launch_clear_isolated_endpoints(const uint32_t *a, size_t na, const uint32_t *b, size_t nb,
                                      const uint32_t *deg, const uint8_t *ex, uint8_t *vaff, cudaStream_t s) {
   if (!na && !nb) return;
@@ -1206,7 +1255,7 @@ void launch_iter_end(Counters *ctr, double M, double E, int L, bool by_graph, cu
 }
 
 void launch_count_flags(const uint8_t *f, size_t n, Counters *ctr, cudaStream_t s) {
-  LVG_CUDA(cudaMemsetAsync(&ctr->affected, 0, sizeof(unsigned long long), s));
+  launch_fill_bytes(&ctr->affected, 0, sizeof(unsigned long long), s);
   if (!n) return;
   count_flags_kernel<<<grid_for(n, 256), 256, 0, s>>>(f, n, &ctr->affected);
   LVG_CHECK_LAUNCH();

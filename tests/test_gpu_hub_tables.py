@@ -164,3 +164,73 @@ def test_tables_with_fresh_result_states(cuda, base):
         else:
             _same(first, got)
         out.close()
+
+
+def _host_df(cuda, G, hb, prior, o):
+    return cuda.louvain_dynamic_frontier(G, hb, prior[0], prior[1], prior[2], o)
+
+
+def test_host_calls_reuse_tables(cuda, orc, base):
+    """The host-array entry points (lvg_frontier …) cache the tables of two
+    memberships: the last prior that needed a build and the last result. A
+    call whose uploaded prior equals one of them exactly takes its tables (no
+    build), any other prior gets tables built for it. Deterministic results
+    equal a graph that scans and the oracle's replay on every call."""
+    x, r0 = base
+    o = cuda.LouvainOptions(deterministic=True)
+    y_hb = cuda.random_batch(x, 3000, seed=21)
+    A, B = cuda.Graph(x), cuda.Graph(x)
+    A.apply_batch(y_hb)
+    tb = B.apply_batch(y_hb)  # the tidied batch, as main.cxx hands it to the methods
+    cuda.set_tuning(A, hub_tables=1)
+    cuda.set_tuning(B, hub_tables=0)
+    y = B.download()
+    prior0 = (r0.membership, r0.vertexWeight, r0.communityWeight)
+    m, vt, ct, info = orc.louvain(y, 3, tb, *prior0, threads=4, sync=True, colors=o.effective_colors())
+    other = cuda.louvain_static(cuda.Graph(y), o)  # a second, different prior
+    prior1 = (other.membership, other.vertexWeight, other.communityWeight)
+    built = []
+    for prior in (prior0, prior0, prior1, prior1, prior0):
+        ra = _host_df(cuda, A, tb, prior, o)
+        built.append(A.stats()["hub_tables_built"])
+        assert A.stats()["hub_table_slots"] > 0
+        rb = _host_df(cuda, B, tb, prior, o)
+        _same((ra.membership, ra.vertexWeight, ra.communityWeight),
+              (rb.membership, rb.vertexWeight, rb.communityWeight))
+        assert (ra.iterations, ra.passes, ra.affectedVertices) == (rb.iterations, rb.passes, rb.affectedVertices)
+        if prior is prior0:
+            _same((ra.membership, ra.vertexWeight, ra.communityWeight), (m, vt, ct))
+    # built for prior0, taken; built for prior1 (in place of prior0: the
+    # other cache holds the last result), taken; built for prior0 again
+    assert built == [1, 0, 1, 0, 1], built
+
+
+def test_host_calls_through_a_stream(cuda, base):
+    """main.cxx's loop through the host entry points: each batch applied to
+    the graph (lvg_graph_apply_batch), then DF from the previous call's
+    result. The result's tables were cached by that call and took the
+    batch's edges when it was applied, so no call after the first builds
+    tables while the runs end after one pass; results equal a scanning graph."""
+    x, r0 = base
+    o = cuda.LouvainOptions(deterministic=True)
+    A, B = cuda.Graph(x), cuda.Graph(x)
+    cuda.set_tuning(A, hub_tables=1)
+    cuda.set_tuning(B, hub_tables=0)
+    pa = pb = (r0.membership, r0.vertexWeight, r0.communityWeight)
+    g = x
+    prev_passes = None
+    for step in range(5):
+        hb = cuda.random_batch(g, 2000, seed=300 + step)
+        ta, tb = A.apply_batch(hb), B.apply_batch(hb)
+        ra = _host_df(cuda, A, ta, pa, o)
+        built = A.stats()["hub_tables_built"]
+        rb = _host_df(cuda, B, tb, pb, o)
+        _same((ra.membership, ra.vertexWeight, ra.communityWeight),
+              (rb.membership, rb.vertexWeight, rb.communityWeight))
+        assert (ra.iterations, ra.passes) == (rb.iterations, rb.passes)
+        if prev_passes == 1:
+            assert built == 0, step
+        prev_passes = ra.passes
+        pa = (ra.membership, ra.vertexWeight, ra.communityWeight)
+        pb = (rb.membership, rb.vertexWeight, rb.communityWeight)
+        g = A.download()
