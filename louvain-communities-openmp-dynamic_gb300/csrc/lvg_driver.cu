@@ -394,7 +394,6 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot
   const bool conc = bin_ev == nullptr && g->tuning.concurrent_bins;
   if (conc) ensure_aux(g);
   auto stream_of = [&](int b) { const int i = bin_stream(b); return conc && i >= 0 ? g->aux[i] : s; };
-  // (kernels, not memsets: a memset waits for the copies in flight)
   launch_fill_bytes(&g->ctr.p->el_fix, 0, sizeof(unsigned long long), s);
   launch_fill_bytes(W.wl_count.p, 0, size_t(K) * NUM_BINS * sizeof(uint32_t), s);
   for (int k = 0; k < K; ++k) {
@@ -1486,7 +1485,7 @@ int run_host(lvg_graph *g, int method, const lvg_batch *b, const uint32_t *q, co
     // result array they are uploaded first, updated, and copied back on a
     // side stream while the rest of the prior uploads (the host link carries
     // both directions at once); their download is over before the run starts
-    // (a download in flight slowed the run's kernels several-fold).
+    // (with it in flight, the local-moving phase took 0.70 ms instead of 0.13).
     cudaPointerAttributes pa{};
     const bool early = method != LVG_METHOD_STATIC && opt.repeat <= 1 && qvtot && out->vertexWeight &&
                        cudaPointerGetAttributes(&pa, out->vertexWeight) == cudaSuccess &&

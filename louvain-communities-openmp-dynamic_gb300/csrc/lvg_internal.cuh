@@ -364,8 +364,7 @@ void bin_items_u64(const uint64_t *deg, const uint8_t *ex, size_t n, int colors,
 int grid_for(size_t n, int block, int max_blocks_per_sm = 8);
 void launch_degrees(const uint64_t *off, uint32_t *deg, size_t span, cudaStream_t s);
 void launch_fill_u8(uint8_t *p, uint8_t v, size_t n, cudaStream_t s);
-// n bytes of value v at p, stored by a kernel (never queued behind the copy
-// engines' transfers, as a memset is)
+// n bytes of value v at p, stored by a kernel (not by the copy engines)
 void launch_fill_bytes(void *p, uint8_t v, size_t n, cudaStream_t s);
 void launch_fill_f32(float *p, size_t n, float v, cudaStream_t s);
 void launch_init_static(const Level &g, uint32_t *ucom, tot_t *utot, tot_t *ctot, cudaStream_t s);

@@ -983,9 +983,8 @@ void launch_fill_u8(uint8_t *p, uint8_t v, size_t n, cudaStream_t s) {
 }
 
 // Byte fill by the SMs: 16-byte stores over the aligned middle, bytes at
-// the ends. A memset queues behind the copies in flight on the device's copy
-// engines (a result download on a side stream held the dynamic-frontier
-// step's in-graph resets for its whole 0.7 ms); a kernel does not.
+// the ends; stream-ordered stores that do not depend on the copy engines,
+// which carry the host transfers of the drop-in calls.
 __global__ void fill_bytes_kernel(uint8_t *p, size_t n, uint8_t v) {
   const size_t head = (16 - (reinterpret_cast<uintptr_t>(p) & 15)) & 15;
   const size_t h = head < n ? head : n;

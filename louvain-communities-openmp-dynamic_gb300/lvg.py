@@ -18,8 +18,10 @@ Host graphs and batches come from :mod:`graphgen` helpers in this module
 """
 from __future__ import annotations
 
+import atexit
 import ctypes as C
 import os
+import weakref
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -153,6 +155,25 @@ def lib_path() -> str:
 
 def gen_path() -> str:
     return os.path.join(LIBDIR, "liblvg_graphgen.so")
+
+
+# Handles still alive at interpreter exit are released by _close_all, in
+# dependency order (servers, batches and states before their graphs), while
+# the CUDA runtime is still up: handles kept in module globals would otherwise
+# be destroyed in an arbitrary order during finalisation.
+_LIVE = {k: weakref.WeakSet() for k in ("server", "batch", "state", "pinned", "graph")}
+
+
+def _close_all() -> None:
+    for kind in ("server", "batch", "state", "pinned", "graph"):
+        for obj in list(_LIVE[kind]):
+            try:
+                obj.close()
+            except Exception:
+                pass
+
+
+atexit.register(_close_all)
 
 
 def load_library() -> C.CDLL:
@@ -579,6 +600,7 @@ class Graph:
         L = load_library()
         self._L = L
         self.h = C.c_void_p()
+        _LIVE["graph"].add(self)
         if g is None:  # filled by a generator classmethod
             return
         w = g.weights if g.num_edges else np.zeros(1, np.float32)
@@ -834,6 +856,7 @@ class State:
         self._L = load_library()
         self.g = g
         self.h = C.c_void_p()
+        _LIVE["state"].add(self)
         _check(self._L.lvg_state_create(g.h, C.byref(self.h)))
 
     def set(self, q, qvtot, qctot) -> None:
@@ -873,6 +896,7 @@ class DeviceBatch:
         self.g = g
         self.batch = b
         self.h = C.c_void_p()
+        _LIVE["batch"].add(self)
         if b is None:  # filled by generate()
             return
         s = b._struct()
@@ -1000,6 +1024,8 @@ class PinnedArray:
 
     def __init__(self, n: int, dtype):
         self._L = load_library()
+        self.ptr = None
+        _LIVE["pinned"].add(self)
         dt = np.dtype(dtype)
         self.ptr = self._L.lvg_host_alloc(max(1, n * dt.itemsize))
         if not self.ptr:
@@ -1033,6 +1059,7 @@ class Server:
             opt.louvain = o._struct()
         self.h = C.c_void_p()
         self.graphs: list[Graph] = []
+        _LIVE["server"].add(self)
         _check(self._L.lvg_server_create(C.byref(opt), C.byref(self.h)))
 
     def add_graph(self, g: Graph, prior=None) -> int:
