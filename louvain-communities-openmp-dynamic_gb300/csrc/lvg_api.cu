@@ -527,6 +527,17 @@ int lvg_graph_trim(lvg_graph *g, int level) {
     g->u_rows.release();
     g->u_plan.release();
     g->u_wdelta.release();
+    // the host calls' hub-table caches (rebuilt by the next call that needs them)
+    auto drop = [](lvg::HubTables &t) {
+      t.off.release(); t.lg.release(); t.bad.release(); t.key.release(); t.cnt.release(); t.nbad.release();
+      t.hubs = t.slots = 0;
+      t.version = t.index = ~0ull;
+    };
+    for (auto &e : g->htab) {
+      e.q.release();
+      drop(e.t);
+    }
+    drop(g->hwork);
     if (level == 2) g->ws.reset();
     return LVG_OK;
   });
