@@ -521,7 +521,7 @@ def run_gpu(args):
         tuning = lvg.set_tuning(Y, **knobs)
     elif not args.no_tune:
         t0 = time.perf_counter()
-        tuning, _ = lvg.autotune(Y, lvg.METHOD_FRONTIER, db, st_prior, o, repeats=5)
+        tuning, _ = lvg.autotune(Y, lvg.METHOD_FRONTIER, db, st_prior, o, repeats=9)
         tune_s = time.perf_counter() - t0
 
     if args.ncu_steps and args.ncu_method == "apply":

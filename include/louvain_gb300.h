@@ -465,7 +465,7 @@ typedef struct lvg_tuning {
                                   (same results; default 1) */
   int      small_regs;         /* registers a thread of the fused launch of degree bins 1-6
                                   (fused_small): 32 (8 resident blocks per SM, some values kept
-                                  in local memory) or 64 (4 blocks per SM, none); default 32 */
+                                  in local memory) or 64 (4 blocks per SM, none); default 64 */
 } lvg_tuning;
 void lvg_tuning_default(lvg_tuning *t);
 int lvg_graph_get_tuning(const lvg_graph *g, lvg_tuning *t);

@@ -216,7 +216,7 @@ inline lvg_tuning default_tuning() {
   t.hub_tables = 1;
   for (auto &x : t.bin_max_degree) x = 0;
   t.level_graphs = 1;
-  t.small_regs = 32;
+  t.small_regs = 64;  // 32 spills ~450 B a thread (R-MAT s24 DF: 0.169 -> 0.166 ms with 64)
   return t;
 }
 

@@ -14,7 +14,7 @@ import pytest
 def test_tuning_defaults(lvg):
     t = lvg.tuning_default()
     assert t == dict(frontier_colors=8, concurrent_bins=1, fused_small=0, hub_chunk=4096, big_blocks_per_sm=0,
-                     frontier_max_fraction=1e-3, hub_tables=1, bin_max_degree=[0] * 12, level_graphs=1, small_regs=32)
+                     frontier_max_fraction=1e-3, hub_tables=1, bin_max_degree=[0] * 12, level_graphs=1, small_regs=64)
 
 
 @pytest.fixture(scope="module")
