@@ -779,6 +779,7 @@ int lvg_state_create(lvg_graph *g, lvg_state **out) {
     const size_t S = g->base.span;
     st->g = g;
     st->device = g->device;
+    st->ht.acct = &st->bytes;  // filled by calls on g, released with the state
     st->q.ensure(S); st->vt.ensure(S); st->ct.ensure(S);
     LVG_CUDA(cudaMemsetAsync(st->q.p, 0, S * 4, g->stream));
     LVG_CUDA(cudaMemsetAsync(st->vt.p, 0, S * sizeof(tot_t), g->stream));

@@ -318,6 +318,7 @@ void build_hub_tables(lvg_graph *g, const uint32_t *q, HubTables &T) {
       off[h + 1] = off[h] + (uint64_t(1) << l);
     }
     T.slots = off[H];
+    AcctScope owner(T.acct ? T.acct : acct_target());  // the tables' own buffers
     T.off.ensure(H + 1);
     T.lg.ensure(H);
     T.bad.ensure(H);
@@ -346,6 +347,7 @@ void copy_hub_tables(lvg_graph *g, const HubTables &src, HubTables &dst) {
   dst.hubs = H;
   dst.slots = src.slots;
   if (H) {
+    AcctScope owner(dst.acct ? dst.acct : acct_target());
     dst.off.ensure(H + 1);
     dst.lg.ensure(H);
     dst.bad.ensure(H);
@@ -378,7 +380,7 @@ int bin_stream(int b) { return b <= 4 ? 0 : b <= 8 ? 1 : b == 9 ? 2 : b == 10 ? 
 void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const tot_t *tot,
                        const uint8_t *fa, float kr, bool sync, int fused, const int *glog2, const size_t *goff,
                        size_t need, std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> *bin_ev,
-                       const UnionCall *uc, bool read_back = true) {
+                       const UnionCall *uc, bool read_back = true, bool clear_pre = true) {
   auto set_union = [&](MoveArgs &a) {
     if (!uc) return;
     a.gid = lv.gid; a.gkr = uc->kr; a.gzero = lv.gbase; a.gfix = uc->fix; a.gact = uc->gact;
@@ -394,8 +396,7 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot
   const bool conc = bin_ev == nullptr && g->tuning.concurrent_bins;
   if (conc) ensure_aux(g);
   auto stream_of = [&](int b) { const int i = bin_stream(b); return conc && i >= 0 ? g->aux[i] : s; };
-  launch_fill_bytes(&g->ctr.p->el_fix, 0, sizeof(unsigned long long), s);
-  launch_fill_bytes(W.wl_count.p, 0, size_t(K) * NUM_BINS * sizeof(uint32_t), s);
+  launch_iter_begin(&g->ctr.p->el_fix, W.wl_count.p, K * NUM_BINS, s);
   for (int k = 0; k < K; ++k) {
     // this class's active vertices of bins 1..NUM_BINS-2 -> worklists
     BinBounds bb;
@@ -492,8 +493,8 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot
     }
   }
   // worklists filled while a dynamic-frontier batch was marked serve the
-  // first iteration only
-  if (K == 1 && !uc) launch_fill_bytes(&g->ctr.p->pre_flag, 0, sizeof(unsigned int), s);
+  // first iteration only (in a phase graph iter_end_kernel clears the flag)
+  if (K == 1 && !uc && clear_pre) launch_fill_bytes(&g->ctr.p->pre_flag, 0, sizeof(unsigned int), s);
   if (uc) launch_iter_control(uc->n, uc->ctl, uc->gact, uc->fix, uc->M, uc->E, uc->L, g->ctr.p, s);
   if (read_back) LVG_CUDA(cudaMemcpyAsync(g->hctr.p, g->ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
 }
@@ -535,7 +536,7 @@ PhaseGraph build_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot
                                                  cudaStreamCaptureModeThreadLocal) == cudaSuccess;
   if (fine) {
     try {
-      enqueue_iteration(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, goff, need, nullptr, uc, false);
+      enqueue_iteration(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, goff, need, nullptr, uc, false, false);
       launch_iter_end(g->ctr.p, M, E, L, uc != nullptr, h, s);
     } catch (const Error &) {
       fine = false;

@@ -143,6 +143,10 @@ struct HubTables {
   DBuf<uint32_t> key, cnt, nbad;
   size_t hubs = 0, slots = 0;
   uint64_t version = ~0ull, index = ~0ull;
+  // the byte counter of the tables' owner (a state's tables are filled by
+  // calls on its graph, and a state may outlive the graph); nullptr: the
+  // calling handle's
+  size_t *acct = nullptr;
   HubTabView view(const uint32_t *slot) const {
     HubTabView v;
     v.slot = slot;

@@ -366,6 +366,8 @@ void launch_degrees(const uint64_t *off, uint32_t *deg, size_t span, cudaStream_
 void launch_fill_u8(uint8_t *p, uint8_t v, size_t n, cudaStream_t s);
 // n bytes of value v at p, stored by a kernel (not by the copy engines)
 void launch_fill_bytes(void *p, uint8_t v, size_t n, cudaStream_t s);
+// *el_fix = 0 and wl_count[0..n) = 0 in one launch
+void launch_iter_begin(unsigned long long *el_fix, uint32_t *wl_count, int n, cudaStream_t s);
 void launch_fill_f32(float *p, size_t n, float v, cudaStream_t s);
 void launch_init_static(const Level &g, uint32_t *ucom, tot_t *utot, tot_t *ctot, cudaStream_t s);
 void launch_total_weight(const float *w, size_t n, Counters *ctr, cudaStream_t s);  // -> ctr->fp64[0]

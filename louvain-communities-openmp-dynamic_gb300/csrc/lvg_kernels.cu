@@ -999,6 +999,18 @@ __global__ void fill_bytes_kernel(uint8_t *p, size_t n, uint8_t v) {
   for (size_t i = tail + t0; i < n; i += st) p[i] = v;
 }
 
+// The start of a local-moving iteration: the gain sum and the classes'
+// worklist counts to zero (one launch for both).
+__global__ void iter_begin_kernel(unsigned long long *el_fix, uint32_t *wl_count, int n) {
+  if (threadIdx.x == 0) *el_fix = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) wl_count[i] = 0;
+}
+
+void launch_iter_begin(unsigned long long *el_fix, uint32_t *wl_count, int n, cudaStream_t s) {
+  iter_begin_kernel<<<1, 256, 0, s>>>(el_fix, wl_count, n);
+  LVG_CHECK_LAUNCH();
+}
+
 void launch_fill_bytes(void *p, uint8_t v, size_t n, cudaStream_t s) {
   if (!n) return;
   fill_bytes_kernel<<<grid_for((n + 15) / 16, 256), 256, 0, s>>>(static_cast<uint8_t *>(p), n, v);
@@ -1200,7 +1212,7 @@ void launch_compact_active(const uint32_t *bins, const BinBounds &bb, const uint
 void launch_compact_active_scan(const Level &g, const BinBounds &bb, const uint8_t *vaff, const uint8_t *fa,
                                 uint32_t *wl, uint32_t *wl_count, Counters *ctr, cudaStream_t s) {
   if (!g.span) return;
-  compact_active_scan_kernel<<<grid_for((g.span + 15) / 16, 256), 256, 0, s>>>(g.deg, g.ex, g.span, bb, g.lim, vaff,
+  compact_active_scan_kernel<<<grid_for((g.span + 15) / 16, 256, 4), 256, 0, s>>>(g.deg, g.ex, g.span, bb, g.lim, vaff,
                                                                                   fa, wl, wl_count, ctr);
   LVG_CHECK_LAUNCH();
 }
@@ -1244,6 +1256,7 @@ __global__ void iter_end_kernel(Counters *ctr, double M, double E, int L, bool b
     ctr->dev_el = el;
     more = el > E;
   }
+  ctr->pre_flag = 0;  // the first iteration's listed worklists are used up
   cudaGraphSetConditional(h, (more && l < unsigned(L) && !ctr->err) ? 1u : 0u);
 }
 

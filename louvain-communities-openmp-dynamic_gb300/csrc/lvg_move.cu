@@ -714,10 +714,18 @@ __global__ void __launch_bounds__(B) hub_chunk_kernel(MoveArgs a) {
   t.vals = reinterpret_cast<float *>(smem + size_t(CS) * 4);
   t.list = reinterpret_cast<uint32_t *>(smem + size_t(CS) * 8);
   t.used = &s_used;
-  const size_t ci = a.hub.chunk_begin[a.color] + blockIdx.x;
-  if (a.ht.key && ld_relaxed(a.ht.nbad) == 0) {  // every hub is done by hub_table_kernel
+  __shared__ int s_skip;
+  // a block per chunk, or (resident hub tables: most blocks have nothing to
+  // do) fewer blocks looping over the chunks
+  const size_t c0 = a.hub.chunk_begin[a.color], nch = a.hub.chunk_begin[a.color + 1] - c0;
+  for (size_t k = blockIdx.x; k < nch; k += gridDim.x) {
+  const size_t ci = c0 + k;
+  __syncthreads();  // the previous chunk's readers of the shared state are done
+  if (threadIdx.x == 0) s_skip = a.ht.key && ld_relaxed(a.ht.nbad) == 0;
+  __syncthreads();  // (one decision for the block: nbad may change meanwhile)
+  if (s_skip) {  // every hub is done by hub_table_kernel
     if (threadIdx.x == 0) a.chunk_cnt[ci] = EMPTY;  // (the merge may still find a table gone bad)
-    return;
+    continue;
   }
   const uint4 ch = a.hub.chunk[ci];
   const uint32_t u = ch.w;  // the hub vertex
@@ -732,7 +740,7 @@ __global__ void __launch_bounds__(B) hub_chunk_kernel(MoveArgs a) {
   __syncthreads();
   if (!s_act) {
     if (threadIdx.x == 0) a.chunk_cnt[ci] = EMPTY;  // tells step 2 the hub was inactive
-    return;
+    continue;
   }
   const uint64_t o = a.off[u] + ch.y;
   const uint32_t n = ch.z - ch.y;
@@ -825,6 +833,7 @@ __global__ void __launch_bounds__(B) hub_chunk_kernel(MoveArgs a) {
       atomicAdd(&a.ctr->hub_chunk_over, 1ull);
       a.hub_over[ch.x] = 1;
     }
+  }
   }
 }
 
@@ -1224,7 +1233,10 @@ void launch_hubs(const MoveArgs &a, cudaStream_t s) {
     hub_table_kernel<HUBT_B, SYNC><<<unsigned(std::min<size_t>(nh, size_t(num_sms()) * 8)), HUBT_B, 0, s>>>(a);
     LVG_CHECK_LAUNCH();
   }
-  k1<<<unsigned(nch), HUBC_B, smem1, s>>>(a);
+  // with resident tables the chunks only mark themselves empty (unless a
+  // table went bad): a few blocks per SM loop over them
+  const size_t g1 = a.ht.key ? std::min<size_t>(nch, size_t(num_sms()) * 2) : nch;
+  k1<<<unsigned(g1), HUBC_B, smem1, s>>>(a);
   LVG_CHECK_LAUNCH();
   if (a.spill_keys) {
     hub_spill_kernel<HUBS_B><<<unsigned(nch), HUBS_B, 0, s>>>(a);

@@ -876,6 +876,10 @@ class State:
         _check(self._L.lvg_state_get(self.h, m.ctypes.data, None, None))
         return m
 
+    def device_bytes(self) -> int:
+        """Device bytes held by the state, its hub tables included (lvg_state_device_bytes)."""
+        return int(self._L.lvg_state_device_bytes(self.h))
+
     def close(self) -> None:
         if self.h:
             self._L.lvg_state_destroy(self.h)

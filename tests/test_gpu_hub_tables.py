@@ -234,3 +234,24 @@ def test_host_calls_through_a_stream(cuda, base):
         pa = (ra.membership, ra.vertexWeight, ra.communityWeight)
         pb = (rb.membership, rb.vertexWeight, rb.communityWeight)
         g = A.download()
+
+
+def test_state_tables_belong_to_the_state(cuda, base):
+    """A state's hub tables are filled by calls on its graph but owned by the
+    state: counted in the state's device bytes (not the graph's) and released
+    with the state, which may outlive its graph."""
+    x, r0 = base
+    Y, db = _graph_with_batch(cuda, x, 9)
+    cuda.set_tuning(Y, hub_tables=1)
+    prior, out = cuda.State(Y), cuda.State(Y)
+    prior.set(r0.membership, r0.vertexWeight, r0.communityWeight)
+    before = (prior.device_bytes(), out.device_bytes())
+    cuda.run_resident(Y, cuda.METHOD_FRONTIER, db, prior, out, cuda.LouvainOptions(deterministic=True))
+    assert Y.stats()["hub_tables_built"] == 1
+    assert prior.device_bytes() > before[0] and out.device_bytes() > before[1]
+    g_bytes = Y.device_bytes()
+    out.close()  # its tables go with it; the graph's count is untouched
+    assert Y.device_bytes() == g_bytes
+    db.close()
+    Y.close()
+    prior.close()  # after its graph
