@@ -1096,7 +1096,7 @@ int lvg_autotune(lvg_graph *g, int method, const lvg_device_batch *b, const lvg_
     lvg_tuning cur = g->tuning;
     double qref = 0;
     double tcur = measure(cur, colours ? &qref : nullptr);
-    auto try_knob = [&](auto set, std::initializer_list<long> values, bool guard) {
+    auto try_knob_list = [&](auto set, const std::vector<long> &values, bool guard) {
       for (long v : values) {
         lvg_tuning t = cur;
         set(t, v);
@@ -1113,6 +1113,9 @@ int lvg_autotune(lvg_graph *g, int method, const lvg_device_batch *b, const lvg_
           tcur = tm;
         }
       }
+    };
+    auto try_knob = [&](auto set, std::initializer_list<long> values, bool guard) {
+      try_knob_list(set, std::vector<long>(values), guard);
     };
     // the class count first (the largest effect), then the launch shapes; twice,
     // since each knob's best value can depend on the others
@@ -1132,17 +1135,26 @@ int lvg_autotune(lvg_graph *g, int method, const lvg_device_batch *b, const lvg_
         try_knob([](lvg_tuning &t, long v) { t.fused_small = int(v); }, {1, 4, 8, 16}, false);
         try_knob([](lvg_tuning &t, long v) { t.small_regs = int(v); }, {32, 64}, false);
       }
-      try_knob([](lvg_tuning &t, long v) { t.big_blocks_per_sm = int(v); }, {0, 2, 3, 4}, false);
-      // the degree from which a block per vertex (bin 9's kernel) serves:
-      // every warp bin (6-8) reaching above it is emptied into bin 9 (on
-      // R-MAT s24 DF, degrees 129-512 took 46 us as a warp per vertex and the
-      // step 0.178 ms; in bin 9's blocks the step took 0.161 ms)
-      try_knob(
-          [](lvg_tuning &t, long v) {
-            for (int b = 6; b <= 8; ++b)
-              t.bin_max_degree[b] = v && BIN_MAX_DEGREE[b] > uint64_t(v) ? uint32_t(v) : 0u;
-          },
-          {0, 256, 128, 64}, false);
+      // the degree from which a block per vertex (bin 9's kernel) serves —
+      // every warp bin (6-8) reaching above it emptied into bin 9 — jointly
+      // with the blocks per SM of those block kernels, since each one's best
+      // value depends on the other (R-MAT s24 DF: degrees 129-512 took 46 us
+      // as a warp per vertex and the step 0.178 ms, in bin 9's blocks 0.161 ms
+      // with as many blocks as fit, but slower with 4 blocks per SM).
+      // v = blocks per SM * 1024 + the degree (0: no bin emptied).
+      {
+        std::vector<long> vs;
+        for (long bb : {0, 2, 3, 4})
+          for (long from : {0, 256, 128, 64}) vs.push_back(bb * 1024 + from);
+        try_knob_list(
+            [](lvg_tuning &t, long v) {
+              t.big_blocks_per_sm = int(v / 1024);
+              const long from = v % 1024;
+              for (int b = 6; b <= 8; ++b)
+                t.bin_max_degree[b] = from && BIN_MAX_DEGREE[b] > uint64_t(from) ? uint32_t(from) : 0u;
+            },
+            vs, false);
+      }
       // the degree bins: each bin at its full reach, at the previous bin's
       // reach, or emptied (all its degrees handed on to the next bin's wider
       // tile and larger table; after the previous bin was emptied too, a run

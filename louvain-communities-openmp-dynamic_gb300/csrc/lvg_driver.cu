@@ -739,9 +739,12 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const 
   }
   const bool graphs = base && capture && !g->profiling && !g->no_graphs;
   const bool phase_graphs = graphs && !g->no_phase_graphs && L > 0;
-  // an aggregated level: its iterations after the first as one graph
-  const bool level_graphs = !base && capture && !g->profiling && !g->no_graphs && !g->no_level_graphs &&
-                            g->tuning.level_graphs;
+  // an aggregated level, or the uploaded level on a call that has no phase
+  // graph to replay yet: its iterations after the first as one graph built
+  // for this call (the uploaded level's phase graph for later calls is
+  // captured at the end)
+  const bool level_graphs = (!base || phase_graphs) && capture && !g->profiling && !g->no_graphs &&
+                            !g->no_level_graphs && g->tuning.level_graphs;
   int l = 0;
   double el = 0;
   if (phase_graphs && g->phase_exec && g->phase_key == key) {

@@ -1248,7 +1248,11 @@ void launch_hubs(const MoveArgs &a, cudaStream_t s) {
       LVG_CHECK_LAUNCH();
     }
   }
-  k2<<<unsigned(global_table_blocks(nh)), HUBM_B, smem2, s>>>(a);
+  // (with resident tables the merge has only the hubs of bad tables to do:
+  // a block per SM, looping over the hubs)
+  const size_t g2 = a.ht.key ? std::min<size_t>(size_t(global_table_blocks(nh)), size_t(num_sms()))
+                             : size_t(global_table_blocks(nh));
+  k2<<<unsigned(g2), HUBM_B, smem2, s>>>(a);
   LVG_CHECK_LAUNCH();
 }
 
