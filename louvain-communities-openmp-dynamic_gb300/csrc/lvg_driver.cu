@@ -961,10 +961,10 @@ void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out
   for (int r = 0; r < rep; ++r) {
     g->events.reset();
     set_base_colors(g, K1 ? K1 : K);
-    // Reset buffers, as the reference does before each repetition.
+    // Reset the flags, as the reference does before each repetition (the
+    // aggregated levels' membership and weights need no reset:
+    // Workspace::allocate).
     launch_fill_bytes(W.vaff.p, 0, S, s);
-    launch_fill_bytes(W.vcom.p, 0, S * sizeof(uint32_t), s);
-    launch_fill_bytes(W.vtot.p, 0, S * sizeof(tot_t), s);
     // The prior state into place: the reference moves its copies of it
     // (louvainSetupInitialsW, inc/louvain.hxx:1240) in without copying, so
     // the copy stays outside the timed section as its copies do.

@@ -94,6 +94,12 @@ struct Workspace {
     }
     LVG_CUDA(cudaMemsetAsync(mark.p, 0, S, st));
     LVG_CUDA(cudaMemsetAsync(dec.p, 0xFF, S * sizeof(uint32_t), st));
+    // the aggregated levels' membership and weights: every entry a run reads
+    // is written by it first, except that the lookups over the whole span
+    // also map the entries past the level's live ids, so those must hold ids
+    // below the span: zero here, and ids of an earlier run after it
+    LVG_CUDA(cudaMemsetAsync(vcom.p, 0, S * sizeof(uint32_t), st));
+    LVG_CUDA(cudaMemsetAsync(vtot.p, 0, S * sizeof(tot_t), st));
     hub_kd.ensure(S);
     LVG_CUDA(cudaMemsetAsync(hub_kd.p, 0, S * sizeof(float), st));
   }
