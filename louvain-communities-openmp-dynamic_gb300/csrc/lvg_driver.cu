@@ -25,6 +25,7 @@ void host_sync(lvg_graph *g) {
 }
 
 void drop_graphs(lvg_graph *g) {
+  g->key_seen = false;
   if (g->iter_exec) {
     cudaGraphExecDestroy(g->iter_exec);
     g->iter_exec = nullptr;
@@ -745,6 +746,15 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const 
   // captured at the end)
   const bool level_graphs = (!base || phase_graphs) && capture && !g->profiling && !g->no_graphs &&
                             !g->no_level_graphs && g->tuning.level_graphs;
+  // Graphs of the uploaded level are captured only for a key that the
+  // previous call on the handle had too: a call after a batch apply (whose
+  // degrees and bins change the key) would build graphs that no call replays,
+  // as a serving loop that applies and runs in turn would on every request.
+  const bool key_again = base && g->key_seen && g->seen_key == key;
+  if (base) {
+    g->seen_key = key;
+    g->key_seen = true;
+  }
   int l = 0;
   double el = 0;
   if (phase_graphs && g->phase_exec && g->phase_key == key) {
@@ -785,7 +795,7 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const 
       g->stats.move_kernel_ms += elapsed(e0, e1);
       for (auto &be : bin_ev) g->stats.move_bin_ms[be.first] += elapsed(be.second.first, be.second.second);
     }
-    if (graphs && !replay)
+    if (graphs && !replay && key_again)
       capture_iteration(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, goff, need, key, uc);
     ++l;
     if (uc) {  // each graph ran its own stop test (iter_control_kernel)
@@ -805,7 +815,7 @@ int move_phase(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot, const 
   }
   // next time, the whole phase as one graph (every kernel's attributes are set
   // by now)
-  if (phase_graphs && !(g->phase_exec && g->phase_key == key))
+  if (phase_graphs && key_again && !(g->phase_exec && g->phase_key == key))
     capture_phase(g, lv, com, ctot, tot, fa, kr, sync, fused, glog2, goff, need, key, uc);
   if (end) { end->l = l; end->el = el; }
   return (l > 1 || el != 0) ? l : 0;

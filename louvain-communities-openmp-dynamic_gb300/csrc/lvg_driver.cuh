@@ -318,6 +318,10 @@ struct lvg_graph {
   IterKey phase_key{};
   bool no_phase_graphs = false;
   bool no_level_graphs = false;  // a level's phase graph could not be built: eager from then on
+  // the uploaded level's key of the last call (graphs are captured when a
+  // call repeats it)
+  IterKey seen_key{};
+  bool key_seen = false;
   // side streams for the degree-bin kernels of one colour class, which run
   // concurrently (fork/join with events)
   cudaStream_t aux[4] = {};

@@ -1,9 +1,10 @@
 """The local-moving phase of the uploaded level replayed as one CUDA graph.
 
-A handle's first call of a method runs the phase iteration by iteration (one
-synchronisation per iteration, for the reference's stop test el <= E,
-inc/louvain.hxx:588-609) and then captures the whole phase as a graph whose
-conditional while node evaluates that test on the device. Later calls with the
+A handle's first call of a method runs the phase's first iteration on its own
+(one synchronisation, for the reference's stop test el <= E,
+inc/louvain.hxx:588-609) and the rest as a graph built for the call; a call
+that repeats the previous call's configuration captures the whole phase as a
+graph whose conditional while node evaluates that test on the device. Later calls with the
 same level and options replay it: one launch and one synchronisation per
 phase. The replay must give the per-iteration path's results: bit-exact with
 the oracle's CPU replay in deterministic mode, on every call. A frontier call
@@ -34,7 +35,7 @@ def test_replayed_phase_matches_cpu_replay(cuda, orc, golden, method):
                                       colors=o.effective_colors())
         call = lambda: getattr(cuda, FN[method])(G, golden.b, *prior(golden), o)  # noqa: E731
     syncs = []
-    for _ in range(3):  # per-iteration + capture, then two replays
+    for _ in range(3):  # no capture, capture, replay
         r = call()
         syncs.append(G.stats()["host_syncs"])
         assert np.array_equal(r.membership, m)

@@ -115,9 +115,10 @@ def test_deterministic_union_matches_cpu_replay(cuda, orc):
 
 
 def test_union_phase_replay(cuda):
-    """The union's first local-moving phase is captured on the first call and
-    replayed as one graph (a conditional while node over every graph's stop
-    test) on later calls: the same results, fewer host synchronisations."""
+    """The union's first local-moving phase is captured on the call that
+    repeats the first one's configuration and replayed as one graph (a
+    conditional while node over every graph's stop test) on later calls: the
+    same results, fewer host synchronisations."""
     gs = _mix(cuda)
     o = cuda.LouvainOptions(deterministic=True)
     U = cuda.Graph.union([cuda.Graph(g) for g in gs])
