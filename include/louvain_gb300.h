@@ -444,10 +444,12 @@ typedef struct lvg_tuning {
                                       entries per edge of the graph; larger batches (whose
                                       frontiers cover much of the graph) keep 8 classes
                                       (default 1e-3) */
-  int      hub_tables;         /* 1: lvg_run_resident keeps, with each state, the neighbour
-                                  counts per community of every vertex above degree 8192 of a
-                                  unit-weight graph, so that the dynamic methods' first pass
-                                  evaluates such a vertex from its table instead of its edges
+  int      hub_tables;         /* 1: the neighbour counts per community of every vertex above
+                                  degree 8192 of a unit-weight graph are kept with each state
+                                  (lvg_run_resident) and cached by the graph for the host-array
+                                  calls, so that the delta-screening and dynamic-frontier first
+                                  passes evaluate such a vertex from its table instead of its
+                                  edges; naive-dynamic, whose every vertex moves, always scans
                                   (same results; default 1) */
   uint32_t bin_max_degree[12]; /* the local-moving degree bins: bin b (1..9) takes vertex degrees
                                   up to bin_max_degree[b] (0 = its full reach: 4, 8, 16, 32, 64,

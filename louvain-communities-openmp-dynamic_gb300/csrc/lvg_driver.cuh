@@ -415,6 +415,7 @@ void compute_bins(lvg_graph *g, Level &lv, const uint32_t *deg, uint32_t *list, 
 void build_hub_plan(lvg_graph *g, Level &lv, HubPlanBuffers &hb);
 Level aggregate(lvg_graph *g, const Level &lv, const uint32_t *com, size_t CN, int which, int colors,
                 const uint32_t *ngid = nullptr, const uint32_t *ngbase = nullptr);
+bool uses_hub_tables(const lvg_graph *g, int method);
 // tprior/tout (optional): the hub tables of the prior and of the result
 // state (the same object for a run in place).
 void run(lvg_graph *g, int method, const DBatch &b, StateRef prior, StateRef out, const lvg_options &o,

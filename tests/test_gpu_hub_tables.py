@@ -55,8 +55,11 @@ def test_tables_equal_scans_deterministic(cuda, orc, base, method):
         outs.append((out.get(), info, st))
     (a, ia, sa), (b, ib, sb), (c, ic, sc) = outs
     assert sa["hub_table_slots"] == 0
-    assert sb["hub_table_slots"] > 0 and sb["hub_tables_built"] == 1
-    assert sc["hub_table_slots"] > 0 and sc["hub_tables_built"] == 0
+    if method == "nd":  # naive-dynamic scans its hubs whatever the tuning (every vertex moves)
+        assert sb["hub_table_slots"] == 0 and sc["hub_table_slots"] == 0
+    else:
+        assert sb["hub_table_slots"] > 0 and sb["hub_tables_built"] == 1
+        assert sc["hub_table_slots"] > 0 and sc["hub_tables_built"] == 0
     _same(a, b)
     _same(a, c)
     for i in (ib, ic):
