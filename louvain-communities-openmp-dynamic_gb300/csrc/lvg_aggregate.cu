@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(B) agg_chunk_kernel(AggArgs a, AggChunks ch) {
     const uint32_t nw = min(uint32_t(B), m1 - mi);  // members staged: mi .. mi+nw-1
     for (uint32_t t = threadIdx.x; t <= nw; t += B) win[t] = ch.mpre[mi + t];
     __syncthreads();
-    // this round: edges [base, stop), all inside the staged members
+    // this pass of the loop: edges [base, stop), all inside the staged members
     const uint64_t stop = min(e1, min(base + B, win[nw]));
     const uint64_t e = base + threadIdx.x;
     uint32_t key = EMPTY;
