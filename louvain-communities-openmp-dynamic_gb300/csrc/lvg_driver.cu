@@ -472,7 +472,9 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot
         a.spill_keys = W.spill_now ? W.spill_keys.p : nullptr;
         a.spill_vals = W.spill_now ? W.spill_vals.p : nullptr;
         a.hub_best = W.hub_best.p;
-        launch_move_hubs(sync, a, s);
+        // (with resident tables the table kernel runs on its own side
+        // stream beside the chunked pair, which only takes bad tables' hubs)
+        launch_move_hubs(sync, a, s, conc ? g->aux[4] : nullptr);
       } else {
         launch_move_bin(b, sync, a, stream_of(b));
       }
@@ -480,7 +482,7 @@ void enqueue_iteration(lvg_graph *g, const Level &lv, uint32_t *com, tot_t *ctot
       ++g->stats.move_launches;
     }
     if (conc) {  // join
-      for (int i = 0; i < 4; ++i) {
+      for (int i = 0; i < 5; ++i) {
         LVG_CUDA(cudaEventRecord(g->join_ev[i], g->aux[i]));
         LVG_CUDA(cudaStreamWaitEvent(s, g->join_ev[i], 0));
       }

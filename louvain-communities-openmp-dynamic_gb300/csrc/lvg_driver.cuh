@@ -323,9 +323,10 @@ struct lvg_graph {
   IterKey seen_key{};
   bool key_seen = false;
   // side streams for the degree-bin kernels of one colour class, which run
-  // concurrently (fork/join with events)
-  cudaStream_t aux[4] = {};
-  cudaEvent_t fork_ev = nullptr, join_ev[4] = {};
+  // concurrently (fork/join with events): bins 1-4 (or the fused 1-6), 5-8
+  // (7-8), 9, 10, and the hubs' resident tables
+  cudaStream_t aux[5] = {};
+  cudaEvent_t fork_ev = nullptr, join_ev[5] = {};
   // result copies that overlap the run (host-array entry points)
   cudaStream_t copy_stream = nullptr;
   ~lvg_graph() {

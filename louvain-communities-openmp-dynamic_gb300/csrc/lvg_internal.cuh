@@ -564,8 +564,10 @@ void launch_relayout_rows(const uint64_t *old_off, const uint32_t *deg, const ui
                           size_t n, const uint64_t *off, const uint32_t *cap, uint32_t *key, float *w, cudaStream_t s);
 
 // Chunked path of the largest vertices: per colour, one kernel aggregates
-// the chunks, a second merges each hub's chunks and moves it.
-void launch_move_hubs(bool sync, const MoveArgs &a, cudaStream_t s);
+// the chunks, a second merges each hub's chunks and moves it. With resident
+// tables (a.ht) the hubs of good tables are done by hub_table_kernel, on
+// s_tab when given (else on s, before the pair).
+void launch_move_hubs(bool sync, const MoveArgs &a, cudaStream_t s, cudaStream_t s_tab = nullptr);
 // Resident hub tables. Building (from membership q, for the hubs of plan P of
 // the uploaded level): each chunk of a hub's edges counts its communities in
 // shared memory and adds them to the hub's scratch table (2^slg[h] >= 2 deg

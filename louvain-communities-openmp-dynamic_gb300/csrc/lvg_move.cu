@@ -1220,7 +1220,7 @@ void launch_big(const MoveArgs &a, cudaStream_t s) {
 }
 
 template <bool SYNC, bool UNIT>
-void launch_hubs(const MoveArgs &a, cudaStream_t s) {
+void launch_hubs(const MoveArgs &a, cudaStream_t s, cudaStream_t s_tab) {
   const size_t smem1 = (size_t(1) << HUBC_LOGS) * 10, smem2 = (size_t(1) << HUBM_LOGS) * 10;
   const size_t nch = a.hub.chunk_begin[a.color + 1] - a.hub.chunk_begin[a.color];
   const size_t nh = a.hub.hub_begin[a.color + 1] - a.hub.hub_begin[a.color];
@@ -1230,7 +1230,8 @@ void launch_hubs(const MoveArgs &a, cudaStream_t s) {
   static bool configured = false;
   if (!configured) { set_smem(k1, smem1); set_smem(k2, smem2); configured = true; }
   if (a.ht.key) {
-    hub_table_kernel<HUBT_B, SYNC><<<unsigned(std::min<size_t>(nh, size_t(num_sms()) * 8)), HUBT_B, 0, s>>>(a);
+    hub_table_kernel<HUBT_B, SYNC><<<unsigned(std::min<size_t>(nh, size_t(num_sms()) * 8)), HUBT_B, 0,
+                                     s_tab ? s_tab : s>>>(a);
     LVG_CHECK_LAUNCH();
   }
   // with resident tables the chunks only mark themselves empty (unless a
@@ -1299,10 +1300,10 @@ int global_table_blocks(size_t count) {
 
 // The kernel variants: deterministic or not, unit weights (no weight
 // reads) or not.
-void launch_move_hubs(bool sync, const MoveArgs &a, cudaStream_t s) {
-  if (sync) { if (a.unit) launch_hubs<true, true>(a, s); else launch_hubs<true, false>(a, s); }
-  else if (a.unit) launch_hubs<false, true>(a, s);
-  else launch_hubs<false, false>(a, s);
+void launch_move_hubs(bool sync, const MoveArgs &a, cudaStream_t s, cudaStream_t s_tab) {
+  if (sync) { if (a.unit) launch_hubs<true, true>(a, s, s_tab); else launch_hubs<true, false>(a, s, s_tab); }
+  else if (a.unit) launch_hubs<false, true>(a, s, s_tab);
+  else launch_hubs<false, false>(a, s, s_tab);
 }
 
 int device_sms() { return num_sms(); }
