@@ -719,121 +719,121 @@ __global__ void __launch_bounds__(B) hub_chunk_kernel(MoveArgs a) {
   // do) fewer blocks looping over the chunks
   const size_t c0 = a.hub.chunk_begin[a.color], nch = a.hub.chunk_begin[a.color + 1] - c0;
   for (size_t k = blockIdx.x; k < nch; k += gridDim.x) {
-  const size_t ci = c0 + k;
-  __syncthreads();  // the previous chunk's readers of the shared state are done
-  if (threadIdx.x == 0) s_skip = a.ht.key && ld_relaxed(a.ht.nbad) == 0;
-  __syncthreads();  // (one decision for the block: nbad may change meanwhile)
-  if (s_skip) {  // every hub is done by hub_table_kernel
-    if (threadIdx.x == 0) a.chunk_cnt[ci] = EMPTY;  // (the merge may still find a table gone bad)
-    continue;
-  }
-  const uint4 ch = a.hub.chunk[ci];
-  const uint32_t u = ch.w;  // the hub vertex
-  if (threadIdx.x == 0) {
-    s_act = a.vaff[u] && (!a.fa || a.fa[u]) && (!a.gact || a.gact[a.gid[u]]) &&
-            !(a.ht.key && !a.ht.bad[a.ht.slot[u]]);  // a hub with a good table is done by hub_table_kernel
-    s_used = 0;
-    s_over = 0;
-    s_cnt = 0;
-    s_nhot = 0;
-  }
-  __syncthreads();
-  if (!s_act) {
-    if (threadIdx.x == 0) a.chunk_cnt[ci] = EMPTY;  // tells step 2 the hub was inactive
-    continue;
-  }
-  const uint64_t o = a.off[u] + ch.y;
-  const uint32_t n = ch.z - ch.y;
-  const uint32_t d = a.vcom[u];
-  const int lg = min(LOGS, max(1, ceil_log2(2ull * n)));
-  const uint32_t vcap = 1u << lg;
-  for (uint32_t s2 = threadIdx.x; s2 < vcap; s2 += B) { t.keys[s2] = EMPTY; t.vals[s2] = 0.f; }
-  __syncthreads();
-  const unsigned limit = vcap >> 1;
-  auto add = [&](uint32_t c, float w) {
-    if (lt_add(t, lg, c, w, limit)) return true;
-    s_over = 1;
-    return false;
-  };
-  // the first edges (one batch per thread) through the table, then the hot
-  // set: the keys that took at least 1/64 of their weight
-  const uint32_t nA = min(n, uint32_t(4 * B));
-  float kd = scan_edges<B, UNIT>(a, u, o, nA, d, add);
-  __syncthreads();
-  if (n > nA && !s_over) {
-    const unsigned nl = min(s_used, limit);
-    float part = 0.f;
-    for (unsigned j = threadIdx.x; j < nl; j += B) {
-      const uint32_t s2 = t.list[j];
-      if (s2 != EMPTY) part += t.vals[s2];
+    const size_t ci = c0 + k;
+    __syncthreads();  // the previous chunk's readers of the shared state are done
+    if (threadIdx.x == 0) s_skip = a.ht.key && ld_relaxed(a.ht.nbad) == 0;
+    __syncthreads();  // (one decision for the block: nbad may change meanwhile)
+    if (s_skip) {  // every hub is done by hub_table_kernel
+      if (threadIdx.x == 0) a.chunk_cnt[ci] = EMPTY;  // (the merge may still find a table gone bad)
+      continue;
     }
-    const float thr = block_sum<B>(part, red_g) * (1.f / 64.f);
-    for (unsigned j = threadIdx.x; j < nl; j += B) {
-      const uint32_t s2 = t.list[j];
-      if (s2 != EMPTY && t.vals[s2] >= thr) {
-        const unsigned h = atomicAdd(&s_nhot, 1u);
-        if (h < HOT_KEYS) s_hot[h] = t.keys[s2];
+    const uint4 ch = a.hub.chunk[ci];
+    const uint32_t u = ch.w;  // the hub vertex
+    if (threadIdx.x == 0) {
+      s_act = a.vaff[u] && (!a.fa || a.fa[u]) && (!a.gact || a.gact[a.gid[u]]) &&
+              !(a.ht.key && !a.ht.bad[a.ht.slot[u]]);  // a hub with a good table is done by hub_table_kernel
+      s_used = 0;
+      s_over = 0;
+      s_cnt = 0;
+      s_nhot = 0;
+    }
+    __syncthreads();
+    if (!s_act) {
+      if (threadIdx.x == 0) a.chunk_cnt[ci] = EMPTY;  // tells step 2 the hub was inactive
+      continue;
+    }
+    const uint64_t o = a.off[u] + ch.y;
+    const uint32_t n = ch.z - ch.y;
+    const uint32_t d = a.vcom[u];
+    const int lg = min(LOGS, max(1, ceil_log2(2ull * n)));
+    const uint32_t vcap = 1u << lg;
+    for (uint32_t s2 = threadIdx.x; s2 < vcap; s2 += B) { t.keys[s2] = EMPTY; t.vals[s2] = 0.f; }
+    __syncthreads();
+    const unsigned limit = vcap >> 1;
+    auto add = [&](uint32_t c, float w) {
+      if (lt_add(t, lg, c, w, limit)) return true;
+      s_over = 1;
+      return false;
+    };
+    // the first edges (one batch per thread) through the table, then the hot
+    // set: the keys that took at least 1/64 of their weight
+    const uint32_t nA = min(n, uint32_t(4 * B));
+    float kd = scan_edges<B, UNIT>(a, u, o, nA, d, add);
+    __syncthreads();
+    if (n > nA && !s_over) {
+      const unsigned nl = min(s_used, limit);
+      float part = 0.f;
+      for (unsigned j = threadIdx.x; j < nl; j += B) {
+        const uint32_t s2 = t.list[j];
+        if (s2 != EMPTY) part += t.vals[s2];
+      }
+      const float thr = block_sum<B>(part, red_g) * (1.f / 64.f);
+      for (unsigned j = threadIdx.x; j < nl; j += B) {
+        const uint32_t s2 = t.list[j];
+        if (s2 != EMPTY && t.vals[s2] >= thr) {
+          const unsigned h = atomicAdd(&s_nhot, 1u);
+          if (h < HOT_KEYS) s_hot[h] = t.keys[s2];
+        }
+      }
+      __syncthreads();
+      uint32_t hot[HOT_KEYS];
+      float hc[HOT_KEYS];
+      const unsigned nh = min(s_nhot, unsigned(HOT_KEYS));
+  #pragma unroll
+      for (int h = 0; h < HOT_KEYS; ++h) { hot[h] = unsigned(h) < nh ? s_hot[h] : NO_KEY; hc[h] = 0.f; }
+      kd += scan_edges_hot<B, UNIT>(a, u, o + nA, n - nA, d, hot, hc, add);
+      // the hot keys' sums into the table, where the keys are already
+      const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  #pragma unroll
+      for (int h = 0; h < HOT_KEYS; ++h) {
+        float x = hc[h];
+  #pragma unroll
+        for (int of = 16; of > 0; of >>= 1) x += __shfl_xor_sync(0xffffffffu, x, of);
+        if (lane == 0) red_h[wid][h] = x;
+      }
+      __syncthreads();
+      if (threadIdx.x < nh) {
+        float x = 0.f;
+        for (int k = 0; k < B / 32; ++k) x += red_h[k][threadIdx.x];
+        if (x != 0.f) add(s_hot[threadIdx.x], x);
       }
     }
     __syncthreads();
-    uint32_t hot[HOT_KEYS];
-    float hc[HOT_KEYS];
-    const unsigned nh = min(s_nhot, unsigned(HOT_KEYS));
-#pragma unroll
-    for (int h = 0; h < HOT_KEYS; ++h) { hot[h] = unsigned(h) < nh ? s_hot[h] : NO_KEY; hc[h] = 0.f; }
-    kd += scan_edges_hot<B, UNIT>(a, u, o + nA, n - nA, d, hot, hc, add);
-    // the hot keys' sums into the table, where the keys are already
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-    for (int h = 0; h < HOT_KEYS; ++h) {
-      float x = hc[h];
-#pragma unroll
-      for (int of = 16; of > 0; of >>= 1) x += __shfl_xor_sync(0xffffffffu, x, of);
-      if (lane == 0) red_h[wid][h] = x;
-    }
-    __syncthreads();
-    if (threadIdx.x < nh) {
-      float x = 0.f;
-      for (int k = 0; k < B / 32; ++k) x += red_h[k][threadIdx.x];
-      if (x != 0.f) add(s_hot[threadIdx.x], x);
-    }
-  }
-  __syncthreads();
-  uint32_t *pk = a.part_key + a.hub.chunk_part[ci];
-  float *pv = a.part_val + a.hub.chunk_part[ci];
-  if (!s_over) {
-    const unsigned nl = min(s_used, limit);
-    for (unsigned j = threadIdx.x; j < nl; j += B) {
-      const uint32_t s2 = t.list[j];
-      if (s2 == EMPTY) continue;
-      const uint32_t pos = atomicAdd(&s_cnt, 1u);
-      pk[pos] = t.keys[s2];
-      pv[pos] = t.vals[s2];
-    }
-  } else {
-    // too many distinct communities in this chunk: hand its raw pairs on
-    kd = 0.f;
-    for (uint32_t j = threadIdx.x; j < n; j += B) {
-      const uint32_t v = __ldcs(a.key + o + j);
-      const uint32_t c = v != u ? a.vcom[v] : EMPTY;
-      const float w = edge_weight<UNIT>(a, o + j);
-      if (c == d) kd += w;
-      if (c != EMPTY && c != d) {
+    uint32_t *pk = a.part_key + a.hub.chunk_part[ci];
+    float *pv = a.part_val + a.hub.chunk_part[ci];
+    if (!s_over) {
+      const unsigned nl = min(s_used, limit);
+      for (unsigned j = threadIdx.x; j < nl; j += B) {
+        const uint32_t s2 = t.list[j];
+        if (s2 == EMPTY) continue;
         const uint32_t pos = atomicAdd(&s_cnt, 1u);
-        pk[pos] = c;
-        pv[pos] = w;
+        pk[pos] = t.keys[s2];
+        pv[pos] = t.vals[s2];
+      }
+    } else {
+      // too many distinct communities in this chunk: hand its raw pairs on
+      kd = 0.f;
+      for (uint32_t j = threadIdx.x; j < n; j += B) {
+        const uint32_t v = __ldcs(a.key + o + j);
+        const uint32_t c = v != u ? a.vcom[v] : EMPTY;
+        const float w = edge_weight<UNIT>(a, o + j);
+        if (c == d) kd += w;
+        if (c != EMPTY && c != d) {
+          const uint32_t pos = atomicAdd(&s_cnt, 1u);
+          pk[pos] = c;
+          pv[pos] = w;
+        }
       }
     }
-  }
-  kd = block_sum<B>(kd, red_g);
-  if (threadIdx.x == 0) {
-    if (kd != 0.f) atomicAdd(&a.hub_kd[u], kd);
-    a.chunk_cnt[ci] = s_cnt;
-    if (s_over) {
-      atomicAdd(&a.ctr->hub_chunk_over, 1ull);
-      a.hub_over[ch.x] = 1;
+    kd = block_sum<B>(kd, red_g);
+    if (threadIdx.x == 0) {
+      if (kd != 0.f) atomicAdd(&a.hub_kd[u], kd);
+      a.chunk_cnt[ci] = s_cnt;
+      if (s_over) {
+        atomicAdd(&a.ctr->hub_chunk_over, 1ull);
+        a.hub_over[ch.x] = 1;
+      }
     }
-  }
   }
 }
 
