@@ -53,13 +53,25 @@ HUB_TABLE_BYTES_PER_SLOT = 8  # community (4) + neighbour count (4) of a residen
 # the local-moving launches by degree bin: (name, bins); the fused small-bin
 # launches time under their first bin
 MOVE_GROUPS = [
-    ("degree 1-128 (move_small_kernel<1,6> or move_tile_kernel bins 1-6)", [1, 2, 3, 4, 5, 6]),
-    ("degree 129-512 (move_small_kernel<7,8> or move_tile_kernel bins 7-8)", [7, 8]),
-    ("degree 513-2048 (move_big_kernel, bin 9)", [9]),
-    ("degree 2049-8192 (move_big_kernel, bin 10)", [10]),
-    ("degree above 8192 (hub_table_kernel on resident tables; hub_chunk_kernel + hub_merge_kernel for the rest)",
-     [11]),
+    ("move_small_kernel<1,6> or move_tile_kernel bins 1-6", [1, 2, 3, 4, 5, 6]),
+    ("move_small_kernel<7,8> or move_tile_kernel bins 7-8", [7, 8]),
+    ("move_big_kernel, bin 9", [9]),
+    ("move_big_kernel, bin 10", [10]),
+    ("hub_table_kernel on resident tables; hub_chunk_kernel + hub_merge_kernel for the rest", [11]),
 ]
+BIN_REACH = [0, 4, 8, 16, 32, 64, 128, 256, 512, 2048, 8192]
+
+
+def group_label(kernels: str, bins, tuning: dict) -> str:
+    """A launch group's degree range under the tuning's degree-bin limits."""
+    lim = list(tuning.get("bin_max_degree", [0] * 12)) + [0] * 12
+    hi = [0] + [lim[b] or BIN_REACH[b] for b in range(1, 11)]
+    if bins[0] == 11:
+        return f"degree above 8192 ({kernels})"
+    lo, top = hi[bins[0] - 1], hi[bins[-1]]
+    if top <= lo:
+        return f"no degrees: handed to the next bin ({kernels})"
+    return f"degree {lo + 1}-{top} ({kernels})"
 
 
 def move_bytes_per_edge(g) -> int:
@@ -654,7 +666,8 @@ def run_gpu(args):
     # bytes: per scanned edge and processed vertex as above, plus 8 B per
     # hub-table slot read (community + count) for the vertices above degree 8192
     groups = []
-    for name, bins in MOVE_GROUPS:
+    for kernels, bins in MOVE_GROUPS:
+        name = group_label(kernels, bins, tuning)
         gms = sum(bin_ms[k] for k in bins) / args.steps
         galg = sum(bpe * bin_edges[k] + MOVE_BYTES_PER_VERTEX * bin_verts[k] for k in bins) / args.steps
         if 11 in bins:
