@@ -74,13 +74,16 @@ def test_union_with_hubs(cuda, lvg):
 
 
 def test_async_union_quality(cuda, orc):
-    """Asynchronous mode: each graph's modularity in the union is within 0.005
-    of the mean of 5 runs of the oracle's OpenMP port on that graph alone."""
+    """Asynchronous mode: each graph's modularity in the union — the mean over
+    3 union runs, as the reference's side is the mean over 5 of its racing
+    runs — is within 0.005 of the mean of 5 runs of the oracle's OpenMP port
+    on that graph alone (a 1K-vertex R-MAT graph's single runs spread by
+    about that much)."""
     gs = _mix(cuda)[:4] + [_mix(cuda)[6]]
     U = cuda.Graph.union([cuda.Graph(g) for g in gs])
-    rs = cuda.louvain_static_union(U)
+    runs = [cuda.louvain_static_union(U) for _ in range(3)]
     for i, g in enumerate(gs):
-        q_union = orc.modularity(g, rs[i].membership)
+        q_union = float(np.mean([orc.modularity(g, rs[i].membership) for rs in runs]))
         ref = [orc.modularity(g, orc.louvain(g, 0, threads=8)[0]) for _ in range(5)]
         assert abs(q_union - np.mean(ref)) <= 0.005, (i, q_union, ref)
 
