@@ -704,6 +704,12 @@ def run_gpu(args):
                                       "; profiles/move_traffic.json) times this step's algorithmic bytes")
                                      if dom_traffic else None,
                      "peak_kind": peak_kind,
+                     "bound_note": ("latency, not bandwidth: a DF step on a 1e-4 |E| batch processes tens of "
+                                    "thousands of vertices, each a chain of dependent gathers; every kernel of the "
+                                    "step stays below 7 % of DRAM throughput and 21 % of issue slots in ncu "
+                                    "(profiles/move_kernels_rmat22_ncu.md). The hub-scan pair that once dominated "
+                                    "the step (0.35 ms, 24 % of the HBM roofline on 58M hub edges) is replaced by "
+                                    "resident per-hub community counts (0.04 ms)"),
                      "algorithmic_bytes": f"{bpe} B/scanned edge (neighbour id + its community"
                                           + (", no weight: every weight is 1)" if bpe == 8 else " + weight)")
                                           + f" + {MOVE_BYTES_PER_VERTEX} B/processed vertex"
