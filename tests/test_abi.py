@@ -69,3 +69,33 @@ def test_missing_library_fails_loudly(lvg, monkeypatch, tmp_path):
     monkeypatch.setattr(lvg, "_lib", None)
     with pytest.raises(lvg.LvgError):
         lvg.load_library()
+
+
+def _struct_fields(header: str, name: str) -> list[tuple[str, int]]:
+    """(field, array length) of `typedef struct name {...} name;` in a header."""
+    src = open(os.path.join(INCLUDE, header)).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    body = re.search(r"typedef struct " + name + r"\s*\{(.*?)\}\s*" + name + ";", src, flags=re.S).group(1)
+    fields = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        # "type a, *b, c[12]" -> every declarator
+        head = re.match(r"((?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\s*\**)\s*(.*)", decl, flags=re.S)
+        for d in head.group(2).split(","):
+            m = re.match(r"\s*\**\s*([A-Za-z_][A-Za-z0-9_]*)\s*(?:\[(\d+)\])?\s*$", d)
+            fields.append((m.group(1), int(m.group(2) or 0)))
+    return fields
+
+
+@pytest.mark.parametrize("cname,pyname", [("lvg_tuning", "_Tuning"), ("lvg_stats", "_Stats"),
+                                          ("lvg_options", "_Options"), ("lvg_result", "_Result")])
+def test_python_mirrors_follow_the_header(lvg, cname, pyname):
+    """The ctypes mirrors in lvg.py list the C structs' fields in the header's
+    order, with the same array lengths (a mismatch would shift every later
+    field across the boundary)."""
+    c_fields = _struct_fields("louvain_gb300.h", cname)
+    py = getattr(lvg, pyname)
+    py_fields = [(n, getattr(t, "_length_", 0)) for n, t in py._fields_]
+    assert py_fields == c_fields, (cname, c_fields, py_fields)
