@@ -89,13 +89,20 @@ def _struct_fields(header: str, name: str) -> list[tuple[str, int]]:
     return fields
 
 
-@pytest.mark.parametrize("cname,pyname", [("lvg_tuning", "_Tuning"), ("lvg_stats", "_Stats"),
-                                          ("lvg_options", "_Options"), ("lvg_result", "_Result")])
-def test_python_mirrors_follow_the_header(lvg, cname, pyname):
+@pytest.mark.parametrize("header,cname,pyname", [
+    ("louvain_gb300.h", "lvg_tuning", "_Tuning"), ("louvain_gb300.h", "lvg_stats", "_Stats"),
+    ("louvain_gb300.h", "lvg_options", "_Options"), ("louvain_gb300.h", "lvg_result", "_Result"),
+    ("louvain_gb300.h", "lvg_batch", "_Batch"), ("louvain_gb300.h", "lvg_batch_buf", "_BatchBuf"),
+    ("louvain_gb300.h", "lvg_server_options", "_ServerOptions"),
+    ("louvain_gb300.h", "lvg_request_info", "_RequestInfo"),
+    ("louvain_gb300.h", "lvg_server_stats_t", "_ServerStats"),
+    ("louvain_gb300_graphgen.h", "lvgg_csr", "_Csr"), ("louvain_gb300_graphgen.h", "lvgg_batch", "_GBatch"),
+    ("louvain_gb300_graphgen.h", "lvgg_edges", "_Edges")])
+def test_python_mirrors_follow_the_header(lvg, header, cname, pyname):
     """The ctypes mirrors in lvg.py list the C structs' fields in the header's
     order, with the same array lengths (a mismatch would shift every later
     field across the boundary)."""
-    c_fields = _struct_fields("louvain_gb300.h", cname)
+    c_fields = _struct_fields(header, cname)
     py = getattr(lvg, pyname)
     py_fields = [(n, getattr(t, "_length_", 0)) for n, t in py._fields_]
     assert py_fields == c_fields, (cname, c_fields, py_fields)
