@@ -74,6 +74,21 @@ def group_label(kernels: str, bins, tuning: dict) -> str:
     return f"degree {lo + 1}-{top} ({kernels})"
 
 
+def parse_tuning(spec: str) -> dict:
+    """--set-tuning's knob=value,... as lvg_tuning fields: integers, except
+    frontier_max_fraction (a float) and bin_max_degree=a:b:c... (the degree
+    bins' limits from bin 0 on)."""
+    knobs = {}
+    for kv in spec.split(","):
+        if not kv.strip():
+            continue
+        k, v = kv.split("=")
+        k = k.strip()
+        knobs[k] = (float(v) if k == "frontier_max_fraction" else
+                    [int(x) for x in v.split(":")] if k == "bin_max_degree" else int(v))
+    return knobs
+
+
 def move_bytes_per_edge(g) -> int:
     """Algorithmic bytes per scanned edge of the local-moving kernels on host graph g."""
     return MOVE_BYTES_PER_EDGE_UNIT if len(g.weights) and bool(np.all(g.weights == 1.0)) else MOVE_BYTES_PER_EDGE
@@ -532,14 +547,7 @@ def run_gpu(args):
     tuning = lvg.get_tuning(Y)
     tune_s = 0.0
     if args.set_tuning:
-        knobs = {}
-        for kv in args.set_tuning.split(","):
-            k, v = kv.split("=")
-            k = k.strip()
-            # bin_max_degree=a:b:c...: the degree bins' limits from bin 0 on
-            knobs[k] = (float(v) if k == "frontier_max_fraction" else
-                        [int(x) for x in v.split(":")] if k == "bin_max_degree" else int(v))
-        tuning = lvg.set_tuning(Y, **knobs)
+        tuning = lvg.set_tuning(Y, **parse_tuning(args.set_tuning))
     elif not args.no_tune:
         t0 = time.perf_counter()
         tuning, _ = lvg.autotune(Y, lvg.METHOD_FRONTIER, db, st_prior, o, repeats=9)
