@@ -106,3 +106,37 @@ def test_python_mirrors_follow_the_header(lvg, header, cname, pyname):
     py = getattr(lvg, pyname)
     py_fields = [(n, getattr(t, "_length_", 0)) for n, t in py._fields_]
     assert py_fields == c_fields, (cname, c_fields, py_fields)
+
+
+def _prototypes(header: str) -> dict[str, int]:
+    """Each function the header declares, with its parameter count."""
+    src = open(os.path.join(INCLUDE, header)).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    src = re.sub(r"//[^\n]*", "", src)
+    out = {}
+    for m in re.finditer(r"\b(lvgg?_[a-z0-9_]+)\s*\(([^;{()]*)\)\s*;", src):
+        params = m.group(2).strip()
+        out[m.group(1)] = 0 if params in ("", "void") else len(params.split(","))
+    return out
+
+
+@pytest.mark.parametrize("header,loader", [("louvain_gb300.h", "load_library"),
+                                           ("louvain_gb300_graphgen.h", "load_graphgen")])
+def test_python_binding_declares_every_argument(lvg, header, loader):
+    """Every entry point lvg.py calls with arguments has ctypes argtypes of the
+    header's arity (without them ctypes passes Python ints as C int, which
+    truncates pointers and sizes)."""
+    import lvg_build
+
+    if loader == "load_library":
+        lvg_build.build_cuda()
+    protos = _prototypes(header)
+    assert len(protos) == len(declared(header))
+    src = open(os.path.join(PKG, "lvg.py")).read()
+    # called directly, or by name through getattr
+    used = (set(re.findall(r"\b(lvgg?_[a-z0-9_]+)\(", src)) | set(re.findall(r'"(lvgg?_[a-z0-9_]+)"', src))) & set(protos)
+    assert used
+    L = getattr(lvg, loader)()
+    bad = [(n, protos[n], getattr(L, n).argtypes) for n in sorted(used)
+           if protos[n] and len(getattr(L, n).argtypes or ()) != protos[n]]
+    assert not bad, bad
