@@ -140,3 +140,36 @@ def test_python_binding_declares_every_argument(lvg, header, loader):
     bad = [(n, protos[n], getattr(L, n).argtypes) for n in sorted(used)
            if protos[n] and len(getattr(L, n).argtypes or ()) != protos[n]]
     assert not bad, bad
+
+
+def _return_types(header: str) -> dict[str, str]:
+    src = open(os.path.join(INCLUDE, header)).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    src = re.sub(r"//[^\n]*", "", src)
+    pat = r"(?:^|[;}\n])\s*((?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\s*\**)\s*\b(lvgg?_[a-z0-9_]+)\s*\(([^;{()]*)\)\s*;"
+    return {m.group(2): " ".join(m.group(1).split()) for m in re.finditer(pat, src)}
+
+
+@pytest.mark.parametrize("header,loader", [("louvain_gb300.h", "load_library"),
+                                           ("louvain_gb300_graphgen.h", "load_graphgen")])
+def test_python_binding_declares_wide_returns(lvg, header, loader):
+    """Entry points that return a size or a pointer have a ctypes restype that
+    holds it (the default, C int, would cut it to 32 bits)."""
+    import lvg_build
+
+    if loader == "load_library":
+        lvg_build.build_cuda()
+    rts = _return_types(header)
+    assert set(rts) == set(_prototypes(header))
+    src = open(os.path.join(PKG, "lvg.py")).read()
+    used = set(re.findall(r"\b(lvgg?_[a-z0-9_]+)\(", src)) & set(rts)
+    L = getattr(lvg, loader)()
+    wide = {"size_t": (ctypes.c_size_t, ctypes.c_uint64, ctypes.c_ulonglong),
+            "pointer": (ctypes.c_void_p, ctypes.c_char_p)}
+    bad = []
+    for n in sorted(used):
+        rt = rts[n]
+        kind = "pointer" if rt.endswith("*") else "size_t" if rt == "size_t" else None
+        if kind and getattr(L, n).restype not in wide[kind]:
+            bad.append((n, rt, getattr(L, n).restype))
+    assert not bad, bad
