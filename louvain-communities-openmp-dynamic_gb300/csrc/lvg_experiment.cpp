@@ -42,7 +42,10 @@ void log_prefix() {
 }
 
 [[noreturn]] void die(const char *what, const char *msg) {
-  std::fprintf(stderr, "%s: %s\n", what, msg);
+  // the libraries' messages may already open with the failing call's name
+  const size_t n = std::strlen(what);
+  if (std::strncmp(msg, what, n) == 0 && msg[n] == ':') std::fprintf(stderr, "%s\n", msg);
+  else std::fprintf(stderr, "%s: %s\n", what, msg);
   std::exit(1);
 }
 

@@ -90,6 +90,24 @@ def test_log_lines_and_csv(tmp_path):
     assert head[:3] == ["omp_num_threads", "graph", "order"] and head[-1] == "technique"
 
 
+def test_experiment_driver_rejects_bad_arguments(lvg, tmp_path):
+    """The experiment driver's command line (main.cxx's: file, rows, size,
+    unused, batch fraction; or --drift) fails before any device work: usage
+    and status 2 for too few arguments, status 1 naming the failing call for
+    an unreadable stream or a --drift line without its batch fraction."""
+    import lvg_build
+
+    lvg_build.build_cuda()
+    exe = lvg_build.build_experiment()
+    r = subprocess.run([exe, "a", "1", "2"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2 and "usage:" in r.stderr and "--drift" in r.stderr
+    r = subprocess.run([exe, str(tmp_path / "missing.txt"), "10", "100", "0", "0.01"], capture_output=True,
+                       text=True, timeout=60)
+    assert r.returncode == 1 and r.stderr.strip() == "lvgg_temporal_open: cannot open the file", r.stderr
+    r = subprocess.run([exe, "--drift", "100", "4", "1000", "7"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and r.stderr.strip() == "--drift: missing batchFraction", r.stderr
+
+
 @pytest.mark.gpu
 def test_device_graph_from_edges_equals_reference(cuda, tmp_path):
     d = _fixture()
