@@ -173,3 +173,48 @@ def test_python_binding_declares_wide_returns(lvg, header, loader):
         if kind and getattr(L, n).restype not in wide[kind]:
             bad.append((n, rt, getattr(L, n).restype))
     assert not bad, bad
+
+
+def _params(header: str) -> dict[str, list[str]]:
+    src = open(os.path.join(INCLUDE, header)).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    src = re.sub(r"//[^\n]*", "", src)
+    out = {}
+    for m in re.finditer(r"\b(lvgg?_[a-z0-9_]+)\s*\(([^;{()]*)\)\s*;", src):
+        p = m.group(2).strip()
+        out[m.group(1)] = [] if p in ("", "void") else [x.strip() for x in p.split(",")]
+    return out
+
+
+_NULL_SAFE = sorted(n for n, ps in _params("louvain_gb300.h").items()
+                    if _return_types("louvain_gb300.h")[n] == "int" and any("*" in p for p in ps))
+
+
+@pytest.mark.parametrize("name", _NULL_SAFE)
+def test_null_arguments_are_rejected_not_dereferenced(lvg, name):
+    """Every status-returning entry point with pointer arguments, called with
+    every pointer NULL (and every number 0), returns LVG_EINVAL with a message
+    before touching the device — except the destructors, which accept NULL
+    as free() does. Runs without a GPU."""
+    import lvg_build
+
+    lvg_build.build_cuda()
+    L = ctypes.CDLL(lvg.lib_path())  # its own function objects: no argtypes of lvg.py's
+    L.lvg_last_error.restype = ctypes.c_char_p
+    args = []
+    for p in _params("louvain_gb300.h")[name]:
+        t = p.split()[0] if not p.startswith("const ") else p.split()[1]
+        if "*" in p:
+            args.append(ctypes.c_void_p(None))
+        elif t in ("double", "float"):
+            args.append(ctypes.c_double(0.0) if t == "double" else ctypes.c_float(0.0))
+        elif t in ("size_t", "uint64_t"):
+            args.append(ctypes.c_uint64(0))
+        else:
+            args.append(ctypes.c_int(0))
+    rc = getattr(L, name)(*args)
+    if name.endswith("_destroy"):
+        assert rc == lvg.LVG_OK
+    else:
+        assert rc == lvg.LVG_EINVAL, (name, rc)
+        assert L.lvg_last_error(), name
