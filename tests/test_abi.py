@@ -186,23 +186,34 @@ def _params(header: str) -> dict[str, list[str]]:
     return out
 
 
-_NULL_SAFE = sorted(n for n, ps in _params("louvain_gb300.h").items()
-                    if _return_types("louvain_gb300.h")[n] == "int" and any("*" in p for p in ps))
+def _null_cases():
+    out = []
+    for header in ("louvain_gb300.h", "louvain_gb300_graphgen.h"):
+        rts = _return_types(header)
+        for n, ps in sorted(_params(header).items()):
+            if any("*" in p for p in ps) and (rts[n] == "int" or n.endswith(("_free", "_close"))):
+                out.append((header, n))
+    return out
 
 
-@pytest.mark.parametrize("name", _NULL_SAFE)
-def test_null_arguments_are_rejected_not_dereferenced(lvg, name):
+@pytest.mark.parametrize("header,name", _null_cases())
+def test_null_arguments_are_rejected_not_dereferenced(lvg, header, name):
     """Every status-returning entry point with pointer arguments, called with
     every pointer NULL (and every number 0), returns LVG_EINVAL with a message
-    before touching the device — except the destructors, which accept NULL
-    as free() does. Runs without a GPU."""
+    before touching the device; the destructors (and the graph generators'
+    free/close calls) accept NULL as free() does. Runs without a GPU."""
     import lvg_build
 
-    lvg_build.build_cuda()
-    L = ctypes.CDLL(lvg.lib_path())  # its own function objects: no argtypes of lvg.py's
-    L.lvg_last_error.restype = ctypes.c_char_p
+    if header == "louvain_gb300.h":
+        lvg_build.build_cuda()
+        L = ctypes.CDLL(lvg.lib_path())  # its own function objects: no argtypes of lvg.py's
+        err = L.lvg_last_error
+    else:
+        L = ctypes.CDLL(lvg.gen_path())
+        err = L.lvgg_last_error
+    err.restype = ctypes.c_char_p
     args = []
-    for p in _params("louvain_gb300.h")[name]:
+    for p in _params(header)[name]:
         t = p.split()[0] if not p.startswith("const ") else p.split()[1]
         if "*" in p:
             args.append(ctypes.c_void_p(None))
@@ -212,9 +223,14 @@ def test_null_arguments_are_rejected_not_dereferenced(lvg, name):
             args.append(ctypes.c_uint64(0))
         else:
             args.append(ctypes.c_int(0))
-    rc = getattr(L, name)(*args)
+    f = getattr(L, name)
+    if _return_types(header)[name] == "void":
+        f.restype = None
+        f(*args)
+        return
+    rc = f(*args)
     if name.endswith("_destroy"):
         assert rc == lvg.LVG_OK
     else:
         assert rc == lvg.LVG_EINVAL, (name, rc)
-        assert L.lvg_last_error(), name
+        assert err(), name
