@@ -105,3 +105,22 @@ def test_rmat_parameters_are_checked(lvg, L, scale, ef, a, b, c):
     g = ctypes.c_void_p()
     rc = L.lvg_graph_create_rmat(scale, ef, a, b, c, 1, 1, ctypes.byref(g))
     assert _outcome(lvg, L, rc, g) == (lvg.LVG_EINVAL, "lvg_graph_create_rmat: bad argument")
+
+
+def test_noalloc_modularity_refuses_before_any_launch(lvg, L):
+    """lvg_modularity_noalloc takes device pointers it cannot inspect: a NULL
+    keys or weights array, or a span above its fixed 2^20 cap, is refused on
+    the host (every case here fails its checks, so nothing is launched on any
+    machine)."""
+    f = L.lvg_modularity_noalloc
+    f.argtypes = [ctypes.c_size_t] + [ctypes.c_void_p] * 5 + [ctypes.c_double, ctypes.c_double, ctypes.c_void_p,
+                                                              ctypes.c_void_p]
+    dummy = ctypes.c_uint64(0)
+    p = ctypes.addressof(dummy)  # a non-NULL pointer; never dereferenced by a refused call
+    out = ctypes.c_double(0.0)
+    for keys, weights in ((None, p), (p, None)):
+        rc = f(16, p, keys, weights, None, p, 0.0, 1.0, ctypes.addressof(out), None)
+        assert (rc, L.lvg_last_error().decode()) == (
+            lvg.LVG_EINVAL, "lvg_modularity_noalloc: null argument or empty span")
+    rc = f((1 << 20) + 1, p, p, p, None, p, 0.0, 1.0, ctypes.addressof(out), None)
+    assert rc == lvg.LVG_EINVAL and "LVG_NOALLOC_MAX_SPAN" in L.lvg_last_error().decode()
