@@ -30,7 +30,9 @@
  *                        addEdge inc/Graph.hxx:318-357), as main.cxx:108-109
  *   orc_louvain_sync     the project's deterministic colour-class rule
  *                        (no reference counterpart; replays the GPU's
- *                        deterministic mode in FP32 with the same operation
+ *                        deterministic mode with the same types — FP64
+ *                        vertex weights and community totals, FP32 edge
+ *                        weights and link sums — and the same operation
  *                        order, so the two must agree bit for bit).
  */
 #include <math.h>
