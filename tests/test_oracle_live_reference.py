@@ -8,7 +8,9 @@ iterations, passes, residual affected count — runs on a sweep of seeded
 graphs the fixtures do not hold: planted partitions and R-MAT graphs of
 several sizes, with unit, dyadic and arbitrary FP32 edge weights, for the
 four entry points from the reference's own static result, plus the batch
-weight update, the DF and DS affected sets and one aggregation step.
+weight update, the DF and DS affected sets and one aggregation step; and the
+base graph of a temporal stream (the reader and CSR build of the package's
+host library against readTemporalOmpW + symmetrizeOmp).
 """
 import numpy as np
 import pytest
@@ -110,3 +112,28 @@ def test_oracle_aggregation_equals_reference(lvg, orc, ref, kind, size, seed, wk
     ren_r, cn_r, rows_r = ref.graph(x).aggregate(q)
     assert cn_o == cn_r and np.array_equal(ren_o, ren_r)
     assert rows_o == rows_r  # each super-vertex's row: neighbour community -> weight
+
+
+@pytest.mark.parametrize("rows,lines,communities,seed", [(500, 4000, 10, 3), (2000, 9000, 40, 4)])
+def test_temporal_base_graph_equals_reference(lvg, ref, tmp_path, rows, lines, communities, seed):
+    """The base graph main.cxx builds from the first 90 % of a temporal
+    stream (readTemporalOmpW + symmetrizeOmp), from the reference and from
+    the host reader + CSR build, on streams with repeated lines, self-loops
+    and ids at the row limit."""
+    src, dst, _ = lvg.temporal_drift(rows, communities, lines, seed=seed)
+    rng = np.random.default_rng(seed)
+    k = rng.choice(lines, lines // 20, replace=False)
+    src[k[: len(k) // 2]] = dst[k[: len(k) // 2]]              # self-loops
+    src[k[len(k) // 2:]] = src[(k[len(k) // 2:] + 1) % lines]  # repeats of the next line's source
+    dst[k[len(k) // 2:]] = dst[(k[len(k) // 2:] + 1) % lines]
+    src[0], dst[0] = rows, 1                                   # the largest id
+    path = str(tmp_path / "t.txt")
+    lvg.write_temporal(path, src, dst)
+    n = int(0.9 * lines)
+    off, key, w, ex = ref.read_temporal(path, rows, n)
+    r = lvg.TemporalReader(path)
+    s, t, wt = r.read(n, symmetric=True)
+    r.close()
+    x = lvg.csr_from_edges(rows, s, t, wt)
+    assert np.array_equal(x.offsets, off) and np.array_equal(x.keys, key)
+    assert np.array_equal(x.weights, w) and np.array_equal(x.exists, ex)
