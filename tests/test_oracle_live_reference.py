@@ -8,8 +8,9 @@ iterations, passes, residual affected count — runs on a sweep of seeded
 graphs the fixtures do not hold: planted partitions and R-MAT graphs of
 several sizes, with unit, dyadic and arbitrary FP32 edge weights, for the
 four entry points from the reference's own static result, plus the batch
-weight update, the DF and DS affected sets and one aggregation step; and the
-base graph of a temporal stream (the reader and CSR build of the package's
+weight update, the DF and DS affected sets and one aggregation step; untidy
+batches tidied and applied three in a row; and the base graph of a temporal
+stream (the reader and CSR build of the package's
 host library against readTemporalOmpW + symmetrizeOmp).
 """
 import numpy as np
@@ -137,3 +138,46 @@ def test_temporal_base_graph_equals_reference(lvg, ref, tmp_path, rows, lines, c
     x = lvg.csr_from_edges(rows, s, t, wt)
     assert np.array_equal(x.offsets, off) and np.array_equal(x.keys, key)
     assert np.array_equal(x.weights, w) and np.array_equal(x.exists, ex)
+
+
+def _untidy_batch(lvg, x, n, seed):
+    """About 3n entries in random order: deletions of present and absent
+    edges (some twice), insertions of new and present edges and of edges
+    touching absent slots (some twice). A repeated entry repeats its weight,
+    so the reference's unstable sort cannot make the result depend on which
+    copy survives."""
+    rng = np.random.default_rng(seed)
+    S = x.span
+    src = np.repeat(np.arange(S, dtype=np.uint32), np.diff(x.offsets).astype(np.int64))
+    n = min(n, x.num_edges)
+    e = rng.choice(x.num_edges, n, replace=False)
+    a = rng.integers(0, S, (n // 3, 2)).astype(np.uint32)
+    ds = np.concatenate([src[e], a[:, 0], src[e[: n // 6]]])
+    dd = np.concatenate([x.keys[e], a[:, 1], x.keys[e[: n // 6]]])
+    dw = np.concatenate([x.weights[e], np.ones(n // 3, np.float32), x.weights[e[: n // 6]]])
+    r = rng.integers(0, S, (n, 2)).astype(np.uint32)
+    rw = rng.integers(1, 6, n).astype(np.float32) * 0.75
+    e2 = rng.choice(x.num_edges, max(n // 4, 1), replace=False)
+    is_ = np.concatenate([r[:, 0], src[e2], r[: n // 5, 0]])
+    id_ = np.concatenate([r[:, 1], x.keys[e2], r[: n // 5, 1]])
+    iw = np.concatenate([rw, np.full(len(e2), 9.0, np.float32), rw[: n // 5]])
+    p, q = rng.permutation(len(ds)), rng.permutation(len(is_))
+    return lvg.HostBatch(ds[p].copy(), dd[p].copy(), dw[p].copy(), is_[q].copy(), id_[q].copy(), iw[q].copy())
+
+
+@pytest.mark.parametrize("kind,size,seed", [("pp", 800, 31), ("rmat", 9, 32), ("pp", 3000, 33)])
+def test_untidy_batch_apply_equals_reference(lvg, orc, ref, kind, size, seed):
+    """tidyBatchUpdateU + applyBatchUpdateOmpU (the reference, in place on its
+    DiGraph) against the oracle's restatement, three batches in a row: the
+    graph after each and the tidied batch, bit for bit."""
+    x = (lvg.planted_partition(size, 32, 8, 0.8, seed) if kind == "pp" else lvg.rmat(size, 8, seed=seed))
+    rg = ref.graph(x)
+    for step in range(3):
+        b = _untidy_batch(lvg, x, max(8, x.num_edges // 40), seed * 10 + step)
+        (yo, yk, yw, yex), t_ref = rg.apply_batch(b)
+        (oo, ok, ow, oex), t_orc = orc.apply_batch(x, b)
+        assert np.array_equal(yo, oo) and np.array_equal(yk, ok), (kind, step)
+        assert np.array_equal(yw, ow) and np.array_equal(yex, oex), (kind, step)
+        assert all(np.array_equal(a, c) for a, c in zip(t_ref, t_orc)), (kind, step)
+        assert len(t_ref[0]) < b.num_deletions and len(t_ref[3]) < b.num_insertions  # tidying removed some
+        x = lvg.HostGraph(oo, ok, ow, oex)
