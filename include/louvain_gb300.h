@@ -22,8 +22,11 @@
  * different host threads; calls on one handle must be serialised by the
  * caller. Every call runs on the handle's own CUDA stream.
  *
- * Errors: every function returns LVG_OK (0) or a negative status; the message
- * of the last failure on the calling thread is lvg_last_error().
+ * Errors: every function that returns int returns LVG_OK (0) or a negative
+ * status; the message of the last failure on the calling thread is
+ * lvg_last_error(). Arguments are checked before any device work; NULL is
+ * refused with LVG_EINVAL, except by the *_destroy functions, which accept it
+ * as free() does.
  */
 #ifndef LOUVAIN_GB300_H
 #define LOUVAIN_GB300_H
@@ -39,7 +42,9 @@ extern "C" {
 #define LVG_EINVAL   (-22)   /* bad argument: id >= span, unsorted DS batch, size mismatch */
 #define LVG_ENOMEM   (-12)   /* device or host allocation failed */
 #define LVG_ETIMEOUT (-62)   /* a bounded device loop hit its cap (hash table overflow guard) */
-#define LVG_ECUDA    (-1000) /* CUDA runtime error (no device, launch failure, ...) */
+#define LVG_ECUDA    (-1000) /* CUDA runtime error (no device, launch failure, ...), or a
+                                 device-side invariant check (a worklist append outside
+                                 its degree bin) */
 
 /* Options. Mirrors LouvainOptions (inc/louvain.hxx:30-63) with the same
  * defaults, including aggregationTolerance = 1.0 (inc/louvain.hxx:60). */
