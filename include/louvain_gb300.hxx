@@ -89,7 +89,10 @@ struct LouvainResult {
 namespace detail {
 
 inline void check(int rc, const char *what) {
-  if (rc != LVG_OK) throw std::runtime_error(std::string(what) + ": " + lvg_last_error());
+  if (rc == LVG_OK) return;
+  // the library's messages may already open with the failing call's name
+  const std::string msg = lvg_last_error(), head = std::string(what) + ":";
+  throw std::runtime_error(msg.compare(0, head.size(), head) == 0 ? msg : std::string(what) + ": " + msg);
 }
 
 inline lvg_options to_c(const LouvainOptions &o) {

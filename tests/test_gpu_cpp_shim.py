@@ -14,6 +14,21 @@ def test_shim_compiles_without_gpu(lvg, tmp_path):
                     os.path.join(ROOT, "tests", "cpp", "shim_test.cpp"), "-o", str(exe)], check=True)
 
 
+def test_shim_errors_throw_without_gpu(lvg, tmp_path):
+    """The header's entry points throw std::runtime_error with the library's
+    message for an input refused before any device work (runs without a GPU)."""
+    import lvg_build
+
+    lvg_build.build_cuda()
+    exe = tmp_path / "shim_error_test"
+    libdir = os.path.join(PKG, "lib")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "shim_error_test.cpp"), "-L", libdir, "-llouvain_gb300",
+                    f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and "errors ok" in r.stdout, r.stdout + r.stderr
+
+
 @pytest.mark.gpu
 def test_shim_program_runs(cuda, tmp_path):
     exe = tmp_path / "shim_test"
