@@ -154,3 +154,26 @@ def test_experiment_driver_end_to_end(cuda, tmp_path):
     q_df = [r["modularity"] for r in rows if r["technique"] == "louvainDynamicFrontierOmp"]
     assert all(abs(a - b) < 0.02 for a, b in zip(q_static, q_df)), (q_static, q_df)
     assert all(r["batch_insertions_fraction"] == 0.01 for r in rows[1:])
+
+
+def test_csr_from_edges_keeps_the_last_weight(lvg):
+    """lvgg_csr_from_edges against a plain model: rows sorted by neighbour,
+    a repeated edge keeps its last weight, vertices 1..rows and every
+    endpoint present; an id above rows is refused."""
+    rng = np.random.default_rng(17)
+    rows, n = 300, 5000
+    src = rng.integers(1, rows + 1, n).astype(np.uint32)
+    dst = rng.integers(1, rows + 1, n).astype(np.uint32)
+    src[:500], dst[:500] = src[500:1000], dst[500:1000]  # repeats, with other weights
+    w = rng.integers(1, 100, n).astype(np.float32)
+    x = lvg.csr_from_edges(rows, src, dst, w)
+    model = [dict() for _ in range(rows + 1)]
+    for u, v, a in zip(src.tolist(), dst.tolist(), w.tolist()):
+        model[u][v] = a  # later entries overwrite earlier ones
+    assert x.span == rows + 1 and x.exists.tolist() == [0] + [1] * rows
+    for u in range(rows + 1):
+        o, e = int(x.offsets[u]), int(x.offsets[u + 1])
+        assert x.keys[o:e].tolist() == sorted(model[u]), u
+        assert x.weights[o:e].tolist() == [model[u][v] for v in sorted(model[u])], u
+    with pytest.raises(lvg.LvgError):
+        lvg.csr_from_edges(rows, np.array([rows + 1], np.uint32), np.array([1], np.uint32))
